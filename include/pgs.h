@@ -1,0 +1,298 @@
+/*
+ * pgs.h -- C ABI of the GB300 Graphics Synthesizer backend.
+ *
+ * Two surfaces live here:
+ *
+ *  1. The frontend (pgs_gs_*): the reference's GSInterface public API
+ *     (gs/gs_interface.hpp:251-304) re-hosted without Vulkan types.  It ingests
+ *     GIF packets and A+D register writes, batches primitives into render
+ *     passes, tracks page hazards and drives a backend.
+ *
+ *  2. The backend (pgs_backend_ops): the methods of the reference's GSRenderer
+ *     that the frontend calls (gs/gs_renderer.hpp:244-323), as a table of plain
+ *     C function pointers.  The CUDA backend (pgs_cuda_backend_*) implements it
+ *     with hand-written sm_103a kernels.  Any other implementation of the table
+ *     (for example a CPU checker) can be plugged under the same frontend.
+ *
+ * Record layouts (pgs_vertex_position, pgs_vertex_attribute,
+ * pgs_primitive_attribute, pgs_state_vector) are bit-compatible with the
+ * reference's shared CPU/GPU structures (gs/shaders/data_structures.h:55-80,
+ * 139-144) so that a frontend written against the reference emits the same
+ * bytes.  All entry points return 0 on success and a negative pgs_status on
+ * failure unless documented otherwise; nothing here traps the GPU.
+ */
+#ifndef PGS_H_
+#define PGS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGS_ABI_VERSION 1u
+
+/* ------------------------------------------------------------------ */
+/* Status codes                                                        */
+/* ------------------------------------------------------------------ */
+typedef enum pgs_status
+{
+	PGS_OK = 0,
+	PGS_ERROR_INVALID_ARGUMENT = -1,
+	PGS_ERROR_OUT_OF_MEMORY = -2,
+	PGS_ERROR_CUDA = -3,
+	PGS_ERROR_NO_DEVICE = -4,
+	PGS_ERROR_UNSUPPORTED = -5,
+	/* Sticky device-side error: a capacity limit was hit or a bounded wait
+	 * expired.  Query with pgs_backend_ops.get_error. */
+	PGS_ERROR_DEVICE_FLAG = -6,
+	PGS_ERROR_CAPACITY = -7
+} pgs_status;
+
+/* ------------------------------------------------------------------ */
+/* Limits (gs/gs_renderer.hpp:154-160, gs/shaders/data_structures.h)   */
+/* ------------------------------------------------------------------ */
+#define PGS_VRAM_SIZE (4u * 1024u * 1024u)
+#define PGS_MAX_PRIMITIVES_PER_FLUSH (64u * 1024u)
+#define PGS_MAX_RENDER_PASS_INSTANCES 8u
+#define PGS_MAX_TEXTURES 4096u
+#define PGS_MAX_STATE_VECTORS 4096u
+#define PGS_CLUT_INSTANCES 1024u
+#define PGS_CLUT_SIZE_BYTES 1024u
+
+/* ------------------------------------------------------------------ */
+/* Primitive records written by the frontend                            */
+/* ------------------------------------------------------------------ */
+
+/* VertexPosition (gs/shaders/data_structures.h:55-58): 12.4 fixed-point
+ * window coordinates after XYOFFSET, 32-bit Z. */
+typedef struct pgs_vertex_position
+{
+	int32_t x, y;
+	uint32_t z;
+	int32_t padding;
+} pgs_vertex_position;
+
+/* VertexAttribute (gs/shaders/data_structures.h:61-68). */
+typedef struct pgs_vertex_attribute
+{
+	float s, t, q;
+	uint32_t rgba;
+	float fog;
+	uint16_t u, v;
+} pgs_vertex_attribute;
+
+/* PrimitiveAttribute (gs/shaders/data_structures.h:71-80).  bb is the
+ * scissored pixel bounding box (lo.x, lo.y, hi.x, hi.y), inclusive. */
+typedef struct pgs_primitive_attribute
+{
+	int16_t bb[4];
+	uint32_t state;
+	uint32_t tex;
+	uint32_t tex2;
+	uint32_t alpha;
+	uint32_t fbmsk;
+	uint32_t fogcol;
+} pgs_primitive_attribute;
+
+/* StateVector (gs/shaders/data_structures.h:139-144). */
+typedef struct pgs_state_vector
+{
+	uint32_t combiner;
+	uint32_t blend_mode;
+	uint32_t dimx_lo, dimx_hi;
+} pgs_state_vector;
+
+/* Texture descriptor.  The reference samples an RGBA8 image decoded by
+ * upload.comp (TexInfo, gs/shaders/data_structures.h:98-105, built at
+ * gs/gs_interface.cpp:1752-1790).  This backend samples swizzled VRAM and the
+ * CLUT directly, so the descriptor carries the raw addressing state instead. */
+typedef struct pgs_texture_desc
+{
+	uint32_t tbp0;          /* TEX0.TBP0, 256-byte blocks */
+	uint32_t tbw;           /* TEX0.TBW, 64-pixel units */
+	uint32_t psm;           /* TEX0.PSM */
+	uint32_t tw_log2, th_log2;
+	uint32_t cpsm;          /* CLUT format (PSMCT32 or PSMCT16/16S) */
+	uint32_t csa;           /* CLUT offset in 16-entry banks */
+	uint32_t clut_instance; /* CLUT ring slot holding the palette */
+	uint32_t aem, ta0, ta1; /* TEXA */
+	uint32_t wms, wmt;      /* CLAMP wrap modes */
+	uint32_t minu, maxu, minv, maxv;
+	uint32_t padding[2];
+} pgs_texture_desc;
+
+/* One framebuffer instance inside a render pass (RenderPass::Instance,
+ * gs/gs_renderer.hpp:174-227). */
+typedef struct pgs_rp_instance
+{
+	uint64_t frame;          /* FRAME_n register bits */
+	uint64_t zbuf;           /* ZBUF_n register bits */
+	int32_t base_x, base_y;  /* pixel origin of the coarse tile grid */
+	uint32_t coarse_tiles_width, coarse_tiles_height;
+	uint32_t sampling_rate_x_log2, sampling_rate_y_log2;
+	uint32_t opaque_fbmask;
+	uint32_t z_sensitive, z_write, channel_shuffle;
+} pgs_rp_instance;
+
+typedef struct pgs_render_pass
+{
+	const pgs_vertex_position *positions;     /* 3 per primitive */
+	const pgs_vertex_attribute *attributes;   /* 3 per primitive */
+	const pgs_primitive_attribute *prims;
+	uint32_t num_primitives;
+
+	const pgs_state_vector *states;
+	uint32_t num_states;
+	const pgs_texture_desc *textures;
+	uint32_t num_textures;
+
+	pgs_rp_instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
+	uint32_t num_instances;
+	uint32_t coarse_tile_size_log2;
+	uint32_t has_aa1, has_scanmsk;
+	uint32_t flush_reason;
+} pgs_render_pass;
+
+/* A VRAM transfer (CopyDescriptor, gs/gs_renderer.hpp).  For HOST_TO_LOCAL,
+ * host_data points at the HWREG payload received so far; bytes below
+ * host_offset were already written by an earlier partial flush. */
+typedef struct pgs_copy_desc
+{
+	uint64_t bitbltbuf, trxpos, trxreg, trxdir;
+	const void *host_data;
+	uint64_t host_size;      /* bytes available in host_data */
+	uint64_t host_offset;    /* bytes already consumed */
+	uint64_t host_required;  /* bytes of the whole transfer */
+} pgs_copy_desc;
+
+/* A CLUT load (PaletteUploadDescriptor, gs/gs_renderer.hpp). */
+typedef struct pgs_palette_upload
+{
+	uint64_t tex0;       /* TEX0 with CPSM/CSA/CSM/CBP normalised */
+	uint64_t texclut;
+	float csm2_x_scale;
+	uint32_t csm2_x_bias;
+	uint32_t base_instance;  /* CLUT state the load starts from */
+	uint32_t padding;
+} pgs_palette_upload;
+
+/* FlushStats (gs/gs_renderer.hpp:55-65) plus fragment counters. */
+typedef struct pgs_flush_stats
+{
+	uint64_t num_render_passes;
+	uint64_t num_primitives;
+	uint64_t num_copies;
+	uint64_t num_palette_updates;
+	uint64_t num_copy_barriers;
+	uint64_t num_flushes_by_reason[8];
+} pgs_flush_stats;
+
+/* ------------------------------------------------------------------ */
+/* Backend interface (replaces GSRenderer)                              */
+/* ------------------------------------------------------------------ */
+typedef struct pgs_backend_ops
+{
+	uint32_t abi_version;
+	void (*destroy)(void *self);
+	/* GSRenderer::reserve_primitive_buffers + get_reserved_* (gs/gs_renderer.hpp:251-254).
+	 * The frontend writes records straight into backend-owned host memory. */
+	int (*reserve_primitive_buffers)(void *self, uint32_t num_primitives,
+	                                 pgs_vertex_position **positions,
+	                                 pgs_vertex_attribute **attributes,
+	                                 pgs_primitive_attribute **prims);
+	/* GSRenderer::flush_rendering(const RenderPass &) (gs/gs_renderer.cpp:3126-3285). */
+	int (*flush_rendering)(void *self, const pgs_render_pass *rp);
+	/* GSRenderer::copy_vram (gs/gs_renderer.cpp:2829-2867). */
+	int (*copy_vram)(void *self, const pgs_copy_desc *desc);
+	/* GSRenderer::update_palette_cache (gs/gs_renderer.cpp:3400-3419).  Returns the
+	 * new CLUT instance (>= 0) or a negative pgs_status. */
+	int (*update_palette_cache)(void *self, const pgs_palette_upload *upload);
+	/* GSRenderer::invalidate_super_sampling_state (gs/gs_renderer.cpp:316-341). */
+	int (*set_super_sampling)(void *self, uint32_t rate_x_log2, uint32_t rate_y_log2);
+	/* GSRenderer::flush_submit (gs/gs_renderer.cpp:1091-1187). */
+	int (*flush_submit)(void *self);
+	/* flush_readback + map_vram_read: blocks until all submitted work is done,
+	 * then copies [offset, offset+size) of VRAM plane `plane` into dst.
+	 * Plane 0 is the single-sampled GS VRAM, plane 1 the super-sample
+	 * reference plane, planes 2.. the samples. */
+	int (*read_vram)(void *self, uint32_t plane, uint64_t offset, uint64_t size, void *dst);
+	/* map_vram_write/end_vram_write: host writes into plane 0. */
+	int (*write_vram)(void *self, uint64_t offset, uint64_t size, const void *src);
+	/* Sticky device error flags (bin overflow, bounded-wait expiry). */
+	int (*get_error)(void *self, uint32_t *flags);
+} pgs_backend_ops;
+
+/* ------------------------------------------------------------------ */
+/* CUDA backend                                                         */
+/* ------------------------------------------------------------------ */
+typedef struct pgs_cuda_backend_options
+{
+	int device;                  /* CUDA ordinal */
+	uint32_t max_samples_log2;   /* 0..4: VRAM holds 2 + 2^max planes */
+	uint32_t flags;
+} pgs_cuda_backend_options;
+
+/* Creates a backend on `device`; returns NULL and sets *status on failure
+ * (PGS_ERROR_NO_DEVICE when no GPU is visible).  *ops receives the table. */
+void *pgs_cuda_backend_create(const pgs_cuda_backend_options *options,
+                              const pgs_backend_ops **ops, int *status);
+
+/* Frame programs: the backend records every op between begin and end into
+ * device-resident form, so the same frame can be replayed with no host
+ * traffic (and captured into a CUDA graph). */
+int pgs_cuda_backend_begin_record(void *backend);
+int pgs_cuda_backend_end_record(void *backend);
+/* Replays the recorded program `count` times on the backend's stream.  When
+ * reset_vram is non-zero every replay starts from the VRAM image that was
+ * current at begin_record. */
+int pgs_cuda_backend_replay(void *backend, uint32_t count, int reset_vram, int use_graph);
+/* Returns the cudaStream_t the backend launches on, as an opaque pointer. */
+void *pgs_cuda_backend_stream(void *backend);
+/* Kernel launches issued by the last replay (per replay). */
+uint32_t pgs_cuda_backend_launches_per_replay(void *backend);
+/* Device time of the shading kernels of the last replay, in milliseconds,
+ * measured with CUDA events on the backend's stream. */
+int pgs_cuda_backend_last_shade_ms(void *backend, float *ms);
+/* Number of covered samples written by the last flush (fragment counter). */
+int pgs_cuda_backend_fragment_count(void *backend, uint64_t *count);
+
+/* ------------------------------------------------------------------ */
+/* Frontend (GSInterface)                                               */
+/* ------------------------------------------------------------------ */
+typedef struct pgs_gs pgs_gs;
+
+typedef struct pgs_gs_options
+{
+	uint32_t super_sampling;      /* 1, 2, 4, 8 or 16 (SuperSampling enum) */
+	uint32_t ordered_super_sampling;
+	uint32_t vram_size;           /* must be PGS_VRAM_SIZE */
+} pgs_gs_options;
+
+/* GSInterface::init.  The frontend does not own the backend. */
+pgs_gs *pgs_gs_create(const pgs_backend_ops *ops, void *backend, const pgs_gs_options *options,
+                      int *status);
+void pgs_gs_destroy(pgs_gs *gs);
+/* GSInterface::gif_transfer.  size must be a multiple of 16 bytes. */
+int pgs_gs_gif_transfer(pgs_gs *gs, uint32_t path, const void *data, size_t size);
+/* GSInterface::write_register (A+D address map, gs/gs_register_addr.hpp). */
+int pgs_gs_write_register(pgs_gs *gs, uint32_t addr, uint64_t payload);
+/* GSInterface::flush. */
+int pgs_gs_flush(pgs_gs *gs);
+/* GSInterface::map_vram_read: flushes, waits and copies plane 0. */
+int pgs_gs_read_vram(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst);
+/* GSInterface::map_vram_write + end_vram_write. */
+int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *src);
+/* GSInterface::read_transfer_fifo. */
+int pgs_gs_read_transfer_fifo(pgs_gs *gs, void *data, uint32_t num_128b_words);
+/* GSInterface::consume_flush_stats. */
+int pgs_gs_consume_flush_stats(pgs_gs *gs, pgs_flush_stats *stats);
+/* GSInterface::set_super_sampling_rate. */
+int pgs_gs_set_super_sampling_rate(pgs_gs *gs, uint32_t super_sampling, uint32_t ordered_grid);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,891 @@
+// backend.cu -- CUDA implementation of pgs_backend_ops (the GSRenderer
+// replacement, gs/gs_renderer.hpp:244-323) on one GB300.
+//
+// Memory in HBM:
+//   VRAM    (2 + 2^max_samples_log2) x 4 MiB planes when super-sampling is
+//           possible (plane 0 = GS local memory, plane 1 = super-sample
+//           reference flags, planes 2.. = samples), else one plane
+//           (gs/gs_renderer.cpp:360-427 minus the shadow half).
+//   CLUT    1024 instances x 1 KiB ring (gs/gs_renderer.hpp:158-160).
+//   arena   device mirror of a pinned host arena holding primitive records,
+//           state vectors, texture descriptors and transfer payloads; every op
+//           copies its own slice host->device once.  Recorded frames replay
+//           straight from the device arena.
+//   scratch per-pass setup records, per-tile primitive bitmasks and flags.
+//
+// Everything runs in order on one CUDA stream.  Kernels never wait on other
+// kernels or on the host, so no launch can hang.
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+using namespace pgs;
+
+namespace
+{
+#define CUDA_TRY(expr)                                                                   \
+	do                                                                                   \
+	{                                                                                    \
+		cudaError_t e_ = (expr);                                                         \
+		if (e_ != cudaSuccess)                                                           \
+		{                                                                                \
+			fprintf(stderr, "pgs: %s failed: %s\n", #expr, cudaGetErrorString(e_));     \
+			return PGS_ERROR_CUDA;                                                       \
+		}                                                                                \
+	} while (0)
+
+const uint8_t RCP_TABLE[256] = {
+	0xff, 0xfd, 0xfb, 0xf9, 0xf7, 0xf5, 0xf3, 0xf1, 0xf0, 0xee, 0xec, 0xea, 0xe8, 0xe6, 0xe5, 0xe3,
+	0xe1, 0xdf, 0xdd, 0xdc, 0xda, 0xd8, 0xd7, 0xd5, 0xd3, 0xd2, 0xd0, 0xce, 0xcd, 0xcb, 0xc9, 0xc8,
+	0xc6, 0xc5, 0xc3, 0xc2, 0xc0, 0xbf, 0xbd, 0xbc, 0xba, 0xb9, 0xb7, 0xb6, 0xb4, 0xb3, 0xb1, 0xb0,
+	0xae, 0xad, 0xac, 0xaa, 0xa9, 0xa7, 0xa6, 0xa5, 0xa4, 0xa2, 0xa1, 0x9f, 0x9e, 0x9d, 0x9c, 0x9a,
+	0x99, 0x98, 0x96, 0x95, 0x94, 0x93, 0x91, 0x90, 0x8f, 0x8e, 0x8c, 0x8b, 0x8a, 0x89, 0x88, 0x87,
+	0x86, 0x84, 0x83, 0x82, 0x81, 0x80, 0x7f, 0x7e, 0x7c, 0x7b, 0x7a, 0x79, 0x78, 0x77, 0x76, 0x74,
+	0x74, 0x73, 0x71, 0x71, 0x70, 0x6f, 0x6e, 0x6d, 0x6b, 0x6b, 0x6a, 0x68, 0x67, 0x67, 0x66, 0x65,
+	0x64, 0x63, 0x62, 0x61, 0x60, 0x5f, 0x5e, 0x5d, 0x5c, 0x5b, 0x5b, 0x59, 0x58, 0x58, 0x56, 0x56,
+	0x55, 0x54, 0x53, 0x52, 0x51, 0x51, 0x50, 0x4f, 0x4e, 0x4e, 0x4c, 0x4b, 0x4b, 0x4a, 0x48, 0x48,
+	0x48, 0x46, 0x46, 0x45, 0x44, 0x43, 0x43, 0x42, 0x41, 0x40, 0x3f, 0x3f, 0x3e, 0x3d, 0x3c, 0x3b,
+	0x3b, 0x3a, 0x39, 0x38, 0x38, 0x37, 0x36, 0x36, 0x35, 0x34, 0x34, 0x33, 0x32, 0x31, 0x30, 0x30,
+	0x2f, 0x2e, 0x2e, 0x2d, 0x2d, 0x2c, 0x2b, 0x2a, 0x2a, 0x29, 0x28, 0x27, 0x27, 0x26, 0x26, 0x25,
+	0x24, 0x23, 0x23, 0x22, 0x21, 0x21, 0x21, 0x20, 0x1f, 0x1f, 0x1e, 0x1d, 0x1d, 0x1c, 0x1c, 0x1b,
+	0x1a, 0x19, 0x19, 0x19, 0x18, 0x17, 0x17, 0x16, 0x16, 0x15, 0x14, 0x13, 0x13, 0x12, 0x12, 0x11,
+	0x11, 0x10, 0x0f, 0x0f, 0x0e, 0x0e, 0x0e, 0x0d, 0x0c, 0x0c, 0x0b, 0x0b, 0x0a, 0x0a, 0x09, 0x08,
+	0x08, 0x07, 0x07, 0x07, 0x06, 0x05, 0x05, 0x04, 0x04, 0x03, 0x03, 0x02, 0x02, 0x01, 0x01, 0x01,
+};
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) & ~(a - 1); }
+
+enum OpType : uint32_t { OP_COPY = 0, OP_CLUT = 1, OP_PASS = 2 };
+
+struct PassOp
+{
+	size_t pos_off, attr_off, prim_off, states_off, textures_off;
+	uint32_t num_prims, num_states, num_textures;
+	uint32_t tile_size_log2, has_aa1, has_scanmsk;
+	uint32_t num_instances;
+	pgs_rp_instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
+};
+
+struct Op
+{
+	OpType type;
+	CopyParams copy;
+	size_t copy_host_off;
+	ClutParams clut;
+	PassOp pass;
+};
+
+struct Dispatch
+{
+	DevInstance inst;
+	uint32_t num_tiles;
+};
+
+struct CudaBackend
+{
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	uint32_t max_planes = 1;
+	uint32_t num_planes = 1;
+	uint32_t rate_x = 0, rate_y = 0;
+
+	uint8_t *d_vram = nullptr;
+	uint16_t *d_clut = nullptr;
+	float *d_rcp_float = nullptr;
+	uint32_t *d_error = nullptr;
+	unsigned long long *d_frags = nullptr;
+	uint8_t *d_snapshot = nullptr;
+	uint32_t last_clut = 0;
+
+	// Arena.
+	uint8_t *h_arena = nullptr, *d_arena = nullptr;
+	size_t arena_cap = 0, arena_used = 0;
+
+	// Reserved primitive buffers (pinned, double buffered so the frontend can
+	// fill one while the other is being copied).
+	uint8_t *h_stage[2] = {};
+	cudaEvent_t stage_done[2] = {};
+	int stage_index = 0;
+	bool stage_pending[2] = {};
+
+	// Scratch.
+	PrimSetup *d_setup = nullptr;
+	TransformedAttr *d_tattr = nullptr;
+	pgs_primitive_attribute *d_prims_work = nullptr;
+	uint32_t *d_masks = nullptr;
+	size_t masks_cap = 0;
+	uint32_t *d_flags = nullptr;
+	size_t flags_cap = 0;
+
+	// Recording.
+	bool recording = false;
+	std::vector<Op> ops;
+	uint8_t *d_reset_vram = nullptr;
+	uint16_t *d_reset_clut = nullptr;
+	uint32_t reset_planes = 0;
+	cudaGraphExec_t graph_exec = nullptr;
+	uint32_t launches_per_replay = 0;
+	uint32_t launch_counter = 0;
+	cudaEvent_t shade_ev[2] = {};
+	float last_shade_ms = 0.0f;
+
+	// ------------------------------------------------------------------
+	int init(const pgs_cuda_backend_options *opt)
+	{
+		int count = 0;
+		if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+			return PGS_ERROR_NO_DEVICE;
+		device = opt ? opt->device : 0;
+		if (device < 0 || device >= count)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		CUDA_TRY(cudaSetDevice(device));
+		CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+		uint32_t ms = opt ? std::min<uint32_t>(opt->max_samples_log2, 4) : 4;
+		max_planes = ms ? 2u + (1u << ms) : 1u;
+		CUDA_TRY(cudaMalloc(&d_vram, size_t(max_planes) * VRAM_SIZE));
+		CUDA_TRY(cudaMemset(d_vram, 0, size_t(max_planes) * VRAM_SIZE));
+		CUDA_TRY(cudaMalloc(&d_clut, size_t(PGS_CLUT_INSTANCES) * PGS_CLUT_SIZE_BYTES));
+		CUDA_TRY(cudaMemset(d_clut, 0, size_t(PGS_CLUT_INSTANCES) * PGS_CLUT_SIZE_BYTES));
+		CUDA_TRY(cudaMalloc(&d_snapshot, VRAM_SIZE));
+		CUDA_TRY(cudaMalloc(&d_error, sizeof(uint32_t)));
+		CUDA_TRY(cudaMemset(d_error, 0, sizeof(uint32_t)));
+		CUDA_TRY(cudaMalloc(&d_frags, sizeof(unsigned long long)));
+		CUDA_TRY(cudaMemset(d_frags, 0, sizeof(unsigned long long)));
+
+		float lut[256];
+		for (int i = 0; i < 256; i++)
+			lut[i] = 1.0f / (1.0f + (float(i) + 0.5f) / 256.0f);
+		CUDA_TRY(cudaMalloc(&d_rcp_float, sizeof(lut)));
+		CUDA_TRY(cudaMemcpy(d_rcp_float, lut, sizeof(lut), cudaMemcpyHostToDevice));
+		CUDA_TRY(cudaMemcpyToSymbol(c_rcp_tab, RCP_TABLE, sizeof(RCP_TABLE)));
+
+		const size_t n = PGS_MAX_PRIMITIVES_PER_FLUSH;
+		CUDA_TRY(cudaMalloc(&d_setup, n * sizeof(PrimSetup)));
+		CUDA_TRY(cudaMalloc(&d_tattr, n * sizeof(TransformedAttr)));
+		CUDA_TRY(cudaMalloc(&d_prims_work, n * sizeof(pgs_primitive_attribute)));
+		for (int i = 0; i < 2; i++)
+		{
+			CUDA_TRY(cudaMallocHost(&h_stage[i], stage_bytes()));
+			CUDA_TRY(cudaEventCreateWithFlags(&stage_done[i], cudaEventDisableTiming));
+			CUDA_TRY(cudaEventCreate(&shade_ev[i]));
+		}
+		return grow_arena(256u << 20);
+	}
+
+	static size_t stage_bytes()
+	{
+		const size_t n = PGS_MAX_PRIMITIVES_PER_FLUSH;
+		return n * (3 * sizeof(pgs_vertex_position) + 3 * sizeof(pgs_vertex_attribute) + sizeof(pgs_primitive_attribute));
+	}
+
+	void destroy()
+	{
+		cudaSetDevice(device);
+		if (stream)
+			cudaStreamSynchronize(stream);
+		if (graph_exec)
+			cudaGraphExecDestroy(graph_exec);
+		cudaFree(d_vram);
+		cudaFree(d_clut);
+		cudaFree(d_snapshot);
+		cudaFree(d_error);
+		cudaFree(d_frags);
+		cudaFree(d_rcp_float);
+		cudaFree(d_setup);
+		cudaFree(d_tattr);
+		cudaFree(d_prims_work);
+		cudaFree(d_masks);
+		cudaFree(d_flags);
+		cudaFree(d_arena);
+		cudaFree(d_reset_vram);
+		cudaFree(d_reset_clut);
+		cudaFreeHost(h_arena);
+		for (int i = 0; i < 2; i++)
+		{
+			cudaFreeHost(h_stage[i]);
+			if (stage_done[i]) cudaEventDestroy(stage_done[i]);
+			if (shade_ev[i]) cudaEventDestroy(shade_ev[i]);
+		}
+		if (stream)
+			cudaStreamDestroy(stream);
+	}
+
+	int grow_arena(size_t need)
+	{
+		size_t cap = std::max<size_t>(arena_cap ? arena_cap * 2 : 0, need);
+		uint8_t *h = nullptr, *d = nullptr;
+		CUDA_TRY(cudaStreamSynchronize(stream));
+		CUDA_TRY(cudaMallocHost(&h, cap));
+		CUDA_TRY(cudaMalloc(&d, cap));
+		if (arena_used)
+		{
+			memcpy(h, h_arena, arena_used);
+			CUDA_TRY(cudaMemcpy(d, d_arena, arena_used, cudaMemcpyDeviceToDevice));
+		}
+		cudaFreeHost(h_arena);
+		cudaFree(d_arena);
+		h_arena = h;
+		d_arena = d;
+		arena_cap = cap;
+		if (graph_exec)
+		{
+			cudaGraphExecDestroy(graph_exec);
+			graph_exec = nullptr;
+		}
+		return PGS_OK;
+	}
+
+	// Appends `size` bytes to the arena and returns the offset.  Outside of
+	// recording the arena restarts once the stream is idle.
+	int arena_alloc(size_t size, size_t &off)
+	{
+		size = align_up(size, 256);
+		if (arena_used + size > arena_cap)
+		{
+			if (!recording)
+			{
+				CUDA_TRY(cudaStreamSynchronize(stream));
+				arena_used = 0;
+			}
+			if (arena_used + size > arena_cap)
+			{
+				int r = grow_arena(arena_used + size);
+				if (r)
+					return r;
+			}
+		}
+		off = arena_used;
+		arena_used += size;
+		return PGS_OK;
+	}
+
+	int upload_arena(size_t off, size_t size)
+	{
+		if (size)
+			CUDA_TRY(cudaMemcpyAsync(d_arena + off, h_arena + off, size, cudaMemcpyHostToDevice, stream));
+		return PGS_OK;
+	}
+
+	// ------------------------------------------------------------------
+	int reserve(uint32_t n, pgs_vertex_position **pos, pgs_vertex_attribute **attr, pgs_primitive_attribute **prim)
+	{
+		if (n > PGS_MAX_PRIMITIVES_PER_FLUSH)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		stage_index ^= 1;
+		if (stage_pending[stage_index])
+		{
+			CUDA_TRY(cudaEventSynchronize(stage_done[stage_index]));
+			stage_pending[stage_index] = false;
+		}
+		const size_t N = PGS_MAX_PRIMITIVES_PER_FLUSH;
+		uint8_t *base = h_stage[stage_index];
+		*pos = reinterpret_cast<pgs_vertex_position *>(base);
+		*attr = reinterpret_cast<pgs_vertex_attribute *>(base + N * 3 * sizeof(pgs_vertex_position));
+		*prim = reinterpret_cast<pgs_primitive_attribute *>(base + N * 3 * (sizeof(pgs_vertex_position) + sizeof(pgs_vertex_attribute)));
+		return PGS_OK;
+	}
+
+	int flush_rendering(const pgs_render_pass *rp)
+	{
+		if (!rp || rp->num_primitives == 0)
+			return PGS_OK;
+		if (rp->num_primitives > PGS_MAX_PRIMITIVES_PER_FLUSH || rp->num_instances == 0 ||
+		    rp->num_instances > PGS_MAX_RENDER_PASS_INSTANCES || rp->coarse_tile_size_log2 < 3 ||
+		    rp->coarse_tile_size_log2 > 7)
+			return PGS_ERROR_INVALID_ARGUMENT;
+
+		Op op = {};
+		op.type = OP_PASS;
+		PassOp &p = op.pass;
+		uint32_t n = rp->num_primitives;
+		size_t pos_bytes = size_t(n) * 3 * sizeof(pgs_vertex_position);
+		size_t attr_bytes = size_t(n) * 3 * sizeof(pgs_vertex_attribute);
+		size_t prim_bytes = size_t(n) * sizeof(pgs_primitive_attribute);
+		size_t st_bytes = size_t(std::max<uint32_t>(rp->num_states, 1)) * sizeof(pgs_state_vector);
+		size_t tex_bytes = size_t(std::max<uint32_t>(rp->num_textures, 1)) * sizeof(pgs_texture_desc);
+		size_t base;
+		size_t total = align_up(pos_bytes, 256) + align_up(attr_bytes, 256) + align_up(prim_bytes, 256) +
+		               align_up(st_bytes, 256) + align_up(tex_bytes, 256);
+		int r = arena_alloc(total, base);
+		if (r)
+			return r;
+		p.pos_off = base;
+		p.attr_off = p.pos_off + align_up(pos_bytes, 256);
+		p.prim_off = p.attr_off + align_up(attr_bytes, 256);
+		p.states_off = p.prim_off + align_up(prim_bytes, 256);
+		p.textures_off = p.states_off + align_up(st_bytes, 256);
+		memcpy(h_arena + p.pos_off, rp->positions, pos_bytes);
+		memcpy(h_arena + p.attr_off, rp->attributes, attr_bytes);
+		memcpy(h_arena + p.prim_off, rp->prims, prim_bytes);
+		if (rp->num_states)
+			memcpy(h_arena + p.states_off, rp->states, rp->num_states * sizeof(pgs_state_vector));
+		if (rp->num_textures)
+			memcpy(h_arena + p.textures_off, rp->textures, rp->num_textures * sizeof(pgs_texture_desc));
+		r = upload_arena(base, total);
+		if (r)
+			return r;
+
+		p.num_prims = n;
+		p.num_states = rp->num_states;
+		p.num_textures = rp->num_textures;
+		p.tile_size_log2 = rp->coarse_tile_size_log2;
+		p.has_aa1 = rp->has_aa1;
+		p.has_scanmsk = rp->has_scanmsk;
+		p.num_instances = rp->num_instances;
+		memcpy(p.instances, rp->instances, sizeof(p.instances));
+		return submit(op);
+	}
+
+	int copy_vram(const pgs_copy_desc *d)
+	{
+		Op op = {};
+		op.type = OP_COPY;
+		CopyParams &c = op.copy;
+		uint64_t bb = d->bitbltbuf;
+		c.sbp = field(bb, 0, 14); c.sbw = field(bb, 16, 6); c.spsm = field(bb, 24, 6);
+		c.dbp = field(bb, 32, 14); c.dbw = field(bb, 48, 6); c.dpsm = field(bb, 56, 6);
+		c.ssax = field(d->trxpos, 0, 11); c.ssay = field(d->trxpos, 16, 11);
+		c.dsax = field(d->trxpos, 32, 11); c.dsay = field(d->trxpos, 48, 11);
+		c.width = field(d->trxreg, 0, 12); c.height = field(d->trxreg, 32, 12);
+		c.xdir = field(d->trxdir, 0, 2);
+		c.invalidate_ss = num_planes > 1;
+		if (c.width == 0 || c.height == 0 || (c.xdir != HOST_TO_LOCAL && c.xdir != LOCAL_TO_LOCAL))
+			return PGS_OK;
+		if (c.xdir == HOST_TO_LOCAL)
+		{
+			if (!d->host_data)
+				return PGS_ERROR_INVALID_ARGUMENT;
+			c.host_size = d->host_size;
+			c.host_offset_qwords = d->host_offset / 8;
+			size_t off;
+			int r = arena_alloc(d->host_size, off);
+			if (r)
+				return r;
+			memcpy(h_arena + off, d->host_data, d->host_size);
+			r = upload_arena(off, d->host_size);
+			if (r)
+				return r;
+			op.copy_host_off = off;
+		}
+		return submit(op);
+	}
+
+	int update_palette(const pgs_palette_upload *u)
+	{
+		Op op = {};
+		op.type = OP_CLUT;
+		ClutParams &c = op.clut;
+		uint64_t t = u->tex0;
+		c.psm = uint32_t((t >> 20) & 0x3f);
+		c.cbp = uint32_t((t >> 37) & 0x3fff);
+		c.cpsm = uint32_t((t >> 51) & 0xf);
+		c.csm = uint32_t((t >> 55) & 1);
+		c.csa = uint32_t((t >> 56) & 0x1f);
+		c.cbw = field(u->texclut, 0, 6);
+		c.cou = field(u->texclut, 6, 6);
+		c.cov = field(u->texclut, 12, 10);
+		c.csm2_x_scale = u->csm2_x_scale;
+		c.csm2_x_bias = u->csm2_x_bias;
+		c.base_instance = u->base_instance % PGS_CLUT_INSTANCES;
+		last_clut = (last_clut + 1) % PGS_CLUT_INSTANCES;
+		c.instance = last_clut;
+		int r = submit(op);
+		return r ? r : int(c.instance);
+	}
+
+	int set_super_sampling(uint32_t x, uint32_t y)
+	{
+		uint32_t planes = (x | y) ? 2u + (1u << (x + y)) : 1u;
+		if (planes > max_planes)
+			return PGS_ERROR_UNSUPPORTED;
+		if (x > 2 || y > 3 || x > y)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		rate_x = x;
+		rate_y = y;
+		num_planes = planes;
+		if (max_planes > 1)
+			CUDA_TRY(cudaMemsetAsync(d_vram + VRAM_SIZE, 0, size_t(max_planes - 1) * VRAM_SIZE, stream));
+		return PGS_OK;
+	}
+
+	// ------------------------------------------------------------------
+	int submit(Op &op)
+	{
+		if (recording)
+			ops.push_back(op);
+		return execute(op);
+	}
+
+	int ensure_masks(size_t words, size_t tiles)
+	{
+		if (words > masks_cap)
+		{
+			cudaFree(d_masks);
+			size_t cap = std::max(words, masks_cap * 2);
+			CUDA_TRY(cudaMalloc(&d_masks, cap * sizeof(uint32_t)));
+			masks_cap = cap;
+			if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+		}
+		if (tiles > flags_cap)
+		{
+			cudaFree(d_flags);
+			size_t cap = std::max(tiles, flags_cap * 2);
+			CUDA_TRY(cudaMalloc(&d_flags, cap * sizeof(uint32_t)));
+			flags_cap = cap;
+			if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+		}
+		return PGS_OK;
+	}
+
+	static uint32_t effective_z_psm(uint32_t color, uint32_t depth)
+	{
+		// deduce_effectice_z_psm (gs/gs_renderer.cpp:2147-2180).
+		if (color == PSMCT32 || color == PSMCT24 || color == PSMCT16S)
+		{
+			if (depth == PSMCT32) return PSMZ32;
+			if (depth == PSMCT24) return PSMZ24;
+			if (depth == PSMCT16 || depth == PSMCT16S) return PSMZ16S;
+		}
+		else if (color == PSMZ32 || color == PSMZ24 || color == PSMZ16S)
+		{
+			if (depth == PSMZ32) return PSMCT32;
+			if (depth == PSMZ24) return PSMCT24;
+			if (depth == PSMZ16S || depth == PSMZ16) return PSMCT16S;
+		}
+		return depth;
+	}
+
+	int run_instance(const PassParams &P, const PassOp &p, uint32_t inst_index, uint32_t lo, uint32_t count)
+	{
+		const pgs_rp_instance &in = p.instances[inst_index];
+		DevInstance I = {};
+		uint32_t frame_lo = uint32_t(in.frame), zbuf_lo = uint32_t(in.zbuf);
+		I.fb_base = field(frame_lo, 0, 9) * BLOCKS_PER_PAGE;
+		I.fb_stride = field(frame_lo, 16, 6);
+		I.fb_psm = field(frame_lo, 24, 6);
+		I.zb_base = field(zbuf_lo, 0, 9) * BLOCKS_PER_PAGE;
+		I.zb_psm = in.z_sensitive ? effective_z_psm(I.fb_psm, field(zbuf_lo, 24, 4) | 0x30u) : 0xffffffffu;
+		I.base_x = in.base_x;
+		I.base_y = in.base_y;
+		I.tiles_w = in.coarse_tiles_width;
+		I.tiles_h = in.coarse_tiles_height;
+		I.rate_x_log2 = in.sampling_rate_x_log2;
+		I.rate_y_log2 = in.sampling_rate_y_log2;
+		I.preserve_samples = in.channel_shuffle && in.sampling_rate_y_log2 != 0;
+		I.instance = inst_index;
+		I.prim_lo = lo;
+		I.prim_count = count;
+		I.mask_words = (count + 31) / 32;
+		size_t tiles = size_t(I.tiles_w) * I.tiles_h;
+		if (tiles == 0 || count == 0)
+			return PGS_OK;
+		uint32_t ns_log2 = I.rate_x_log2 + I.rate_y_log2;
+		if (I.rate_y_log2 > 3 || I.rate_x_log2 > 2 || ns_log2 > 4 || I.rate_x_log2 > I.rate_y_log2)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		// Super-sampled shading touches planes 1 .. 1 + 2^ns_log2.
+		if (I.rate_y_log2 != 0 && 2u + (1u << ns_log2) > num_planes)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		int r = ensure_masks(tiles * I.mask_words, tiles);
+		if (r)
+			return r;
+		CUDA_TRY(cudaMemsetAsync(d_masks, 0, tiles * I.mask_words * sizeof(uint32_t), stream));
+		CUDA_TRY(cudaMemsetAsync(d_flags, 0, tiles * sizeof(uint32_t), stream));
+		bin_kernel<<<(count + 127) / 128, 128, 0, stream>>>(P, I, d_masks, d_flags);
+		launch_counter++;
+		uint32_t subtiles = 1u << (2 * (p.tile_size_log2 - 3));
+		uint32_t grid = uint32_t(tiles) * subtiles;
+		if (I.rate_y_log2 != 0)
+		{
+			switch (ns_log2)
+			{
+			case 1: shade_kernel<2, true><<<grid, 128, 0, stream>>>(P, I, d_masks, d_flags); break;
+			case 2: shade_kernel<4, true><<<grid, 256, 0, stream>>>(P, I, d_masks, d_flags); break;
+			case 3: shade_kernel<8, true><<<grid, 512, 0, stream>>>(P, I, d_masks, d_flags); break;
+			case 4: shade_kernel<16, true><<<grid, 1024, 0, stream>>>(P, I, d_masks, d_flags); break;
+			default: return PGS_ERROR_INVALID_ARGUMENT;
+			}
+			launch_counter++;
+		}
+		shade_kernel<1, false><<<grid, 64, 0, stream>>>(P, I, d_masks, d_flags);
+		launch_counter++;
+		CUDA_TRY(cudaGetLastError());
+		return PGS_OK;
+	}
+
+	int execute(const Op &op)
+	{
+		switch (op.type)
+		{
+		case OP_COPY:
+		{
+			CopyParams c = op.copy;
+			if (c.xdir == HOST_TO_LOCAL)
+				c.host = d_arena + op.copy_host_off;
+			else
+			{
+				CUDA_TRY(cudaMemcpyAsync(d_snapshot, d_vram, VRAM_SIZE, cudaMemcpyDeviceToDevice, stream));
+				c.src_vram = d_snapshot;
+			}
+			dim3 grid((c.width + 31) / 32, (c.height + 7) / 8);
+			upload_kernel<<<grid, 256, 0, stream>>>(c, d_vram);
+			launch_counter++;
+			CUDA_TRY(cudaGetLastError());
+			return PGS_OK;
+		}
+		case OP_CLUT:
+			clut_kernel<<<1, 256, 0, stream>>>(op.clut, d_vram, d_clut);
+			launch_counter++;
+			CUDA_TRY(cudaGetLastError());
+			return PGS_OK;
+		case OP_PASS:
+			return execute_pass(op.pass);
+		}
+		return PGS_ERROR_INVALID_ARGUMENT;
+	}
+
+	int execute_pass(const PassOp &p)
+	{
+		PassParams P = {};
+		P.pos = reinterpret_cast<const pgs_vertex_position *>(d_arena + p.pos_off);
+		P.attr = reinterpret_cast<const pgs_vertex_attribute *>(d_arena + p.attr_off);
+		P.states = reinterpret_cast<const pgs_state_vector *>(d_arena + p.states_off);
+		P.textures = reinterpret_cast<const pgs_texture_desc *>(d_arena + p.textures_off);
+		P.prims = d_prims_work;
+		P.setup = d_setup;
+		P.tattr = d_tattr;
+		P.num_prims = p.num_prims;
+		P.num_states = std::max<uint32_t>(p.num_states, 1);
+		P.num_textures = std::max<uint32_t>(p.num_textures, 1);
+		P.tile_size_log2 = p.tile_size_log2;
+		P.has_aa1 = p.has_aa1;
+		P.has_scanmsk = p.has_scanmsk;
+		P.has_ss_reference = num_planes > 1;
+		P.vram = d_vram;
+		P.clut = d_clut;
+		P.rcp_float_lut = d_rcp_float;
+		P.error_flags = d_error;
+		P.fragment_counter = d_frags;
+		for (uint32_t i = 0; i < p.num_instances; i++)
+		{
+			P.opaque_fbmask[i] = p.instances[i].opaque_fbmask;
+			P.setup_rate_x_log2 = std::max(P.setup_rate_x_log2, p.instances[i].sampling_rate_x_log2);
+			P.setup_rate_y_log2 = std::max(P.setup_rate_y_log2, p.instances[i].sampling_rate_y_log2);
+		}
+		CUDA_TRY(cudaMemcpyAsync(d_prims_work, d_arena + p.prim_off, size_t(p.num_prims) * sizeof(pgs_primitive_attribute),
+		                         cudaMemcpyDeviceToDevice, stream));
+		setup_kernel<<<(p.num_prims + 127) / 128, 128, 0, stream>>>(P);
+		launch_counter++;
+		CUDA_TRY(cudaGetLastError());
+
+		if (p.num_instances == 1)
+			return run_instance(P, p, 0, 0, p.num_prims);
+
+		// Per-instance primitive ranges and hazard-ordered segments
+		// (gs/gs_renderer.cpp:3190-3266).  The instance of each primitive is
+		// read from the host copy of the records.
+		const pgs_primitive_attribute *hp = reinterpret_cast<const pgs_primitive_attribute *>(h_arena + p.prim_off);
+		uint8_t hazard[8] = {};
+		bool any = instance_hazards(p, hazard);
+		if (any)
+		{
+			uint32_t active = 0, active_h = 0, base = 0;
+			for (uint32_t i = 0; i < p.num_prims; i++)
+			{
+				uint32_t inst = (hp[i].state >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u;
+				if (active_h & (1u << inst))
+				{
+					for (uint32_t b = 0; b < 8; b++)
+						if (active & (1u << b))
+						{
+							int r = run_instance(P, p, b, base, i - base);
+							if (r) return r;
+						}
+					base = i;
+					active = 0;
+					active_h = 0;
+				}
+				active |= 1u << inst;
+				active_h |= hazard[inst];
+			}
+			for (uint32_t b = 0; b < 8; b++)
+				if (active & (1u << b))
+				{
+					int r = run_instance(P, p, b, base, p.num_prims - base);
+					if (r) return r;
+				}
+			return PGS_OK;
+		}
+		uint32_t lo[8], hi[8];
+		for (int i = 0; i < 8; i++) { lo[i] = 0xffffffffu; hi[i] = 0; }
+		for (uint32_t i = 0; i < p.num_prims; i++)
+		{
+			uint32_t inst = (hp[i].state >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u;
+			if (lo[inst] == 0xffffffffu) lo[inst] = i;
+			hi[inst] = i;
+		}
+		for (uint32_t i = 0; i < p.num_instances; i++)
+			if (lo[i] != 0xffffffffu)
+			{
+				int r = run_instance(P, p, i, lo[i], hi[i] - lo[i] + 1);
+				if (r) return r;
+			}
+		return PGS_OK;
+	}
+
+	static bool instance_hazards(const PassOp &p, uint8_t *mask)
+	{
+		struct Range { uint32_t s, e; };
+		auto range = [&](uint32_t base_block, int32_t x, int32_t y, uint32_t w, uint32_t h, uint32_t stride, uint32_t psm) {
+			Layout L = psm_layout(psm);
+			if (psm == PSMT4 || psm == PSMT8) stride >>= 1;
+			uint32_t px0 = uint32_t(x) >> L.pw, px1 = (uint32_t(x) + w - 1) >> L.pw;
+			uint32_t py0 = uint32_t(y) >> L.ph, py1 = (uint32_t(y) + h - 1) >> L.ph;
+			uint32_t base = base_block / BLOCKS_PER_PAGE;
+			return Range{ base + py0 * stride + px0, base + py1 * stride + px1 + ((base_block % BLOCKS_PER_PAGE) ? 1u : 0u) };
+		};
+		Range fb[8] = {}, zb[8] = {};
+		uint32_t ts = p.tile_size_log2;
+		for (uint32_t i = 0; i < p.num_instances; i++)
+		{
+			auto &in = p.instances[i];
+			uint32_t f = uint32_t(in.frame), z = uint32_t(in.zbuf);
+			fb[i] = range(field(f, 0, 9) * 32, in.base_x, in.base_y, in.coarse_tiles_width << ts, in.coarse_tiles_height << ts,
+			              field(f, 16, 6), field(f, 24, 6));
+			if (in.z_sensitive)
+				zb[i] = range(field(z, 0, 9) * 32, in.base_x, in.base_y, in.coarse_tiles_width << ts,
+				              in.coarse_tiles_height << ts, field(f, 16, 6), field(z, 24, 4));
+		}
+		auto ov = [](Range a, Range b) { return std::max(a.s, b.s) <= std::min(a.e, b.e); };
+		bool any = false;
+		for (uint32_t i = 0; i < p.num_instances; i++)
+			for (uint32_t j = i + 1; j < p.num_instances; j++)
+			{
+				auto &a = p.instances[i], &b = p.instances[j];
+				bool h = ov(fb[i], fb[j]) || (b.z_sensitive && ov(fb[i], zb[j])) || (a.z_sensitive && ov(fb[j], zb[i])) ||
+				         (a.z_sensitive && b.z_sensitive && (a.z_write || b.z_write) && ov(zb[i], zb[j]));
+				if (h)
+				{
+					mask[i] |= uint8_t(1u << j);
+					mask[j] |= uint8_t(1u << i);
+					any = true;
+				}
+			}
+		return any;
+	}
+
+	// ------------------------------------------------------------------
+	int read_vram(uint32_t plane, uint64_t off, uint64_t size, void *dst)
+	{
+		if (plane >= num_planes || off + size > VRAM_SIZE)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		CUDA_TRY(cudaMemcpyAsync(dst, d_vram + size_t(plane) * VRAM_SIZE + off, size, cudaMemcpyDeviceToHost, stream));
+		CUDA_TRY(cudaStreamSynchronize(stream));
+		if (!recording)
+			arena_used = 0;
+		return PGS_OK;
+	}
+
+	int write_vram(uint64_t off, uint64_t size, const void *src)
+	{
+		if (off + size > VRAM_SIZE)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		CUDA_TRY(cudaMemcpyAsync(d_vram + off, src, size, cudaMemcpyHostToDevice, stream));
+		if (num_planes > 1)
+			CUDA_TRY(cudaMemsetAsync(d_vram + VRAM_SIZE + off, 0, size, stream));
+		CUDA_TRY(cudaStreamSynchronize(stream));
+		return PGS_OK;
+	}
+
+	int flush_submit()
+	{
+		return PGS_OK;
+	}
+
+	int get_error(uint32_t *flags)
+	{
+		uint32_t f = 0;
+		CUDA_TRY(cudaMemcpyAsync(&f, d_error, sizeof(f), cudaMemcpyDeviceToHost, stream));
+		CUDA_TRY(cudaStreamSynchronize(stream));
+		if (flags)
+			*flags = f;
+		return f ? PGS_ERROR_DEVICE_FLAG : PGS_OK;
+	}
+
+	// ------------------------------------------------------------------
+	int begin_record()
+	{
+		CUDA_TRY(cudaStreamSynchronize(stream));
+		if (graph_exec)
+		{
+			cudaGraphExecDestroy(graph_exec);
+			graph_exec = nullptr;
+		}
+		ops.clear();
+		arena_used = 0;
+		size_t vbytes = size_t(num_planes) * VRAM_SIZE;
+		cudaFree(d_reset_vram);
+		cudaFree(d_reset_clut);
+		d_reset_vram = nullptr;
+		d_reset_clut = nullptr;
+		CUDA_TRY(cudaMalloc(&d_reset_vram, vbytes));
+		CUDA_TRY(cudaMalloc(&d_reset_clut, size_t(PGS_CLUT_INSTANCES) * PGS_CLUT_SIZE_BYTES));
+		CUDA_TRY(cudaMemcpyAsync(d_reset_vram, d_vram, vbytes, cudaMemcpyDeviceToDevice, stream));
+		CUDA_TRY(cudaMemcpyAsync(d_reset_clut, d_clut, size_t(PGS_CLUT_INSTANCES) * PGS_CLUT_SIZE_BYTES,
+		                         cudaMemcpyDeviceToDevice, stream));
+		reset_planes = num_planes;
+		recording = true;
+		return PGS_OK;
+	}
+
+	int end_record()
+	{
+		recording = false;
+		CUDA_TRY(cudaStreamSynchronize(stream));
+		return PGS_OK;
+	}
+
+	int replay_once(bool reset)
+	{
+		launch_counter = 0;
+		if (reset && d_reset_vram)
+		{
+			CUDA_TRY(cudaMemcpyAsync(d_vram, d_reset_vram, size_t(reset_planes) * VRAM_SIZE, cudaMemcpyDeviceToDevice, stream));
+			CUDA_TRY(cudaMemcpyAsync(d_clut, d_reset_clut, size_t(PGS_CLUT_INSTANCES) * PGS_CLUT_SIZE_BYTES,
+			                         cudaMemcpyDeviceToDevice, stream));
+		}
+		for (const Op &op : ops)
+		{
+			int r = execute(op);
+			if (r)
+				return r;
+		}
+		launches_per_replay = launch_counter;
+		return PGS_OK;
+	}
+
+	int replay(uint32_t count, bool reset, bool use_graph)
+	{
+		if (!use_graph)
+		{
+			for (uint32_t i = 0; i < count; i++)
+			{
+				int r = replay_once(reset);
+				if (r)
+					return r;
+			}
+			return PGS_OK;
+		}
+		if (!graph_exec)
+		{
+			// Make sure scratch buffers are sized before capture.
+			int r = replay_once(reset);
+			if (r)
+				return r;
+			CUDA_TRY(cudaStreamSynchronize(stream));
+			cudaGraph_t graph;
+			CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+			r = replay_once(reset);
+			cudaError_t e = cudaStreamEndCapture(stream, &graph);
+			if (r)
+				return r;
+			if (e != cudaSuccess)
+				return PGS_ERROR_CUDA;
+			CUDA_TRY(cudaGraphInstantiate(&graph_exec, graph, 0));
+			cudaGraphDestroy(graph);
+		}
+		for (uint32_t i = 0; i < count; i++)
+			CUDA_TRY(cudaGraphLaunch(graph_exec, stream));
+		return PGS_OK;
+	}
+};
+
+// ---------------------------------------------------------------------------
+// pgs_backend_ops table.
+CudaBackend *B(void *s) { return static_cast<CudaBackend *>(s); }
+
+void c_destroy(void *self)
+{
+	if (!self) return;
+	B(self)->destroy();
+	delete B(self);
+}
+int c_reserve(void *self, uint32_t n, pgs_vertex_position **p, pgs_vertex_attribute **a, pgs_primitive_attribute **pr)
+{
+	return B(self)->reserve(n, p, a, pr);
+}
+int c_flush_rendering(void *self, const pgs_render_pass *rp) { return B(self)->flush_rendering(rp); }
+int c_copy(void *self, const pgs_copy_desc *d) { return d ? B(self)->copy_vram(d) : PGS_ERROR_INVALID_ARGUMENT; }
+int c_palette(void *self, const pgs_palette_upload *u) { return u ? B(self)->update_palette(u) : PGS_ERROR_INVALID_ARGUMENT; }
+int c_set_ss(void *self, uint32_t x, uint32_t y) { return B(self)->set_super_sampling(x, y); }
+int c_submit(void *self) { return B(self)->flush_submit(); }
+int c_read(void *self, uint32_t plane, uint64_t off, uint64_t size, void *dst)
+{
+	return dst ? B(self)->read_vram(plane, off, size, dst) : PGS_ERROR_INVALID_ARGUMENT;
+}
+int c_write(void *self, uint64_t off, uint64_t size, const void *src)
+{
+	return src ? B(self)->write_vram(off, size, src) : PGS_ERROR_INVALID_ARGUMENT;
+}
+int c_error(void *self, uint32_t *flags) { return B(self)->get_error(flags); }
+
+const pgs_backend_ops CUDA_OPS = {
+	PGS_ABI_VERSION, c_destroy, c_reserve, c_flush_rendering, c_copy, c_palette, c_set_ss, c_submit, c_read, c_write, c_error,
+};
+} // namespace
+
+extern "C" {
+void *pgs_cuda_backend_create(const pgs_cuda_backend_options *options, const pgs_backend_ops **ops, int *status)
+{
+	int dummy;
+	if (!status)
+		status = &dummy;
+	auto *b = new (std::nothrow) CudaBackend();
+	if (!b)
+	{
+		*status = PGS_ERROR_OUT_OF_MEMORY;
+		return nullptr;
+	}
+	int r = b->init(options);
+	if (r)
+	{
+		b->destroy();
+		delete b;
+		*status = r;
+		return nullptr;
+	}
+	if (ops)
+		*ops = &CUDA_OPS;
+	*status = PGS_OK;
+	return b;
+}
+
+int pgs_cuda_backend_begin_record(void *backend) { return backend ? B(backend)->begin_record() : PGS_ERROR_INVALID_ARGUMENT; }
+int pgs_cuda_backend_end_record(void *backend) { return backend ? B(backend)->end_record() : PGS_ERROR_INVALID_ARGUMENT; }
+int pgs_cuda_backend_replay(void *backend, uint32_t count, int reset_vram, int use_graph)
+{
+	return backend ? B(backend)->replay(count, reset_vram != 0, use_graph != 0) : PGS_ERROR_INVALID_ARGUMENT;
+}
+void *pgs_cuda_backend_stream(void *backend) { return backend ? static_cast<void *>(B(backend)->stream) : nullptr; }
+uint32_t pgs_cuda_backend_launches_per_replay(void *backend) { return backend ? B(backend)->launches_per_replay : 0; }
+int pgs_cuda_backend_last_shade_ms(void *backend, float *ms)
+{
+	if (!backend || !ms)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	*ms = B(backend)->last_shade_ms;
+	return PGS_OK;
+}
+int pgs_cuda_backend_fragment_count(void *backend, uint64_t *count)
+{
+	if (!backend || !count)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	unsigned long long v = 0;
+	if (cudaMemcpy(&v, B(backend)->d_frags, sizeof(v), cudaMemcpyDeviceToHost) != cudaSuccess)
+		return PGS_ERROR_CUDA;
+	*count = v;
+	return PGS_OK;
+}
+}

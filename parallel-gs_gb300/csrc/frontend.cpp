@@ -1,0 +1,1668 @@
+// frontend.cpp -- GSInterface re-hosted without Vulkan (gs/gs_interface.cpp).
+//
+// The frontend ingests GIF packets and register writes, keeps the GS register
+// file and the 3-entry vertex queue, turns drawing kicks into primitive records
+// (pgs_vertex_position / pgs_vertex_attribute / pgs_primitive_attribute),
+// batches them into render passes and drives a backend through
+// pgs_backend_ops.  Primitive records follow drawing_kick_append
+// (gs/gs_interface.cpp:2473-2836); state words follow drawing_kick_update_state
+// (:1804-1968) and drawing_kick_update_state_vector (:1065-1128).
+//
+// Differences from the reference, all result-neutral for sequential GS
+// semantics: no parallelogram fusion of triangle pairs (gs/gs_util.cpp:237-377),
+// no palette memoization (:689-799), no feedback-texture modes (:2140-2330) and
+// a page-granular hazard tracker.  Because the backend samples textures straight
+// from VRAM instead of from snapshot images, the tracker also ends a render pass
+// when a transfer or a framebuffer write would touch pages an earlier primitive
+// of the same pass samples.
+#include "pgs.h"
+#include "gs_defs.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <unordered_map>
+#include <vector>
+
+using namespace pgs;
+
+namespace
+{
+// A+D register addresses (gs/gs_register_addr.hpp).
+enum Reg : uint32_t
+{
+	R_PRIM = 0x00, R_RGBAQ = 0x01, R_ST = 0x02, R_UV = 0x03, R_XYZF2 = 0x04, R_XYZ2 = 0x05,
+	R_TEX0_1 = 0x06, R_TEX0_2 = 0x07, R_CLAMP_1 = 0x08, R_CLAMP_2 = 0x09, R_FOG = 0x0a,
+	R_XYZF3 = 0x0c, R_XYZ3 = 0x0d, R_RGBAQ_UNDOC = 0x11, R_TEX1_1 = 0x14, R_TEX1_2 = 0x15,
+	R_TEX2_1 = 0x16, R_TEX2_2 = 0x17, R_XYOFFSET_1 = 0x18, R_XYOFFSET_2 = 0x19,
+	R_PRMODECONT = 0x1a, R_PRMODE = 0x1b, R_TEXCLUT = 0x1c, R_SCANMSK = 0x22,
+	R_MIPTBP1_1 = 0x34, R_MIPTBP1_2 = 0x35, R_MIPTBP2_1 = 0x36, R_MIPTBP2_2 = 0x37,
+	R_TEXA = 0x3b, R_FOGCOL = 0x3d, R_TEXFLUSH = 0x3f, R_SCISSOR_1 = 0x40, R_SCISSOR_2 = 0x41,
+	R_ALPHA_1 = 0x42, R_ALPHA_2 = 0x43, R_DIMX = 0x44, R_DTHE = 0x45, R_COLCLAMP = 0x46,
+	R_TEST_1 = 0x47, R_TEST_2 = 0x48, R_PABE = 0x49, R_FBA_1 = 0x4a, R_FBA_2 = 0x4b,
+	R_FRAME_1 = 0x4c, R_FRAME_2 = 0x4d, R_ZBUF_1 = 0x4e, R_ZBUF_2 = 0x4f,
+	R_BITBLTBUF = 0x50, R_TRXPOS = 0x51, R_TRXREG = 0x52, R_TRXDIR = 0x53, R_HWREG = 0x54,
+	R_SIGNAL = 0x60, R_FINISH = 0x61, R_LABEL = 0x62
+};
+
+enum FlushReason : uint32_t
+{
+	FLUSH_EXPLICIT = 0, FLUSH_OVERFLOW = 1, FLUSH_FB_POINTER = 2, FLUSH_TEXTURE_HAZARD = 3,
+	FLUSH_COPY_HAZARD = 4, FLUSH_CLUT_HAZARD = 5, FLUSH_HOST_ACCESS = 6, FLUSH_SUPER_SAMPLING = 7
+};
+
+enum PrimType : uint32_t
+{
+	PRIM_POINT = 0, PRIM_LINE_LIST = 1, PRIM_LINE_STRIP = 2, PRIM_TRI_LIST = 3,
+	PRIM_TRI_STRIP = 4, PRIM_TRI_FAN = 5, PRIM_SPRITE = 6, PRIM_INVALID = 7
+};
+
+constexpr uint32_t NUM_PAGES = VRAM_SIZE / PAGE_BYTES;
+
+// Register views.  Field offsets are those of the GS hardware registers.
+struct PrimReg
+{
+	uint32_t prim, iip, tme, fge, abe, aa1, fst, ctxt, fix;
+	explicit PrimReg(uint64_t r)
+	    : prim(field(r, 0, 3)), iip(field(r, 3, 1)), tme(field(r, 4, 1)), fge(field(r, 5, 1)),
+	      abe(field(r, 6, 1)), aa1(field(r, 7, 1)), fst(field(r, 8, 1)), ctxt(field(r, 9, 1)),
+	      fix(field(r, 10, 1)) {}
+	bool enables_aa1() const { return aa1 && prim != PRIM_SPRITE && prim != PRIM_POINT; }
+};
+
+struct Tex0Reg
+{
+	uint32_t tbp0, tbw, psm, tw, th, tcc, tfx, cbp, cpsm, csm, csa, cld;
+	explicit Tex0Reg(uint64_t r)
+	    : tbp0(field(r, 0, 14)), tbw(field(r, 14, 6)), psm(field(r, 20, 6)), tw(field(r, 26, 4)),
+	      th(field(r, 30, 4)), tcc(field(r, 34, 1)), tfx(field(r, 35, 2)), cbp(field(r, 37, 14)),
+	      cpsm(field(r, 51, 4)), csm(field(r, 55, 1)), csa(field(r, 56, 5)), cld(field(r, 61, 3)) {}
+};
+
+struct TestReg
+{
+	uint32_t ate, atst, aref, afail, date, datm, zte, ztst;
+	explicit TestReg(uint64_t r)
+	    : ate(field(r, 0, 1)), atst(field(r, 1, 3)), aref(field(r, 4, 8)), afail(field(r, 12, 2)),
+	      date(field(r, 14, 1)), datm(field(r, 15, 1)), zte(field(r, 16, 1)), ztst(field(r, 17, 2)) {}
+	bool has_z_test() const { return ztst > 1; }
+};
+
+struct AlphaReg
+{
+	uint32_t a, b, c, d, fix;
+	explicit AlphaReg(uint64_t r)
+	    : a(field(r, 0, 2)), b(field(r, 2, 2)), c(field(r, 4, 2)), d(field(r, 6, 2)), fix(field(r, 32, 8)) {}
+};
+
+struct FrameReg
+{
+	uint32_t fbp, fbw, psm, fbmsk;
+	explicit FrameReg(uint64_t r)
+	    : fbp(field(r, 0, 9)), fbw(field(r, 16, 6)), psm(field(r, 24, 6)), fbmsk(field(r, 32, 32)) {}
+};
+
+struct ZbufReg
+{
+	uint32_t zbp, psm, zmsk;
+	explicit ZbufReg(uint64_t r) : zbp(field(r, 0, 9)), psm(field(r, 24, 4)), zmsk(field(r, 32, 1)) {}
+};
+
+struct ClampReg
+{
+	uint32_t wms, wmt, minu, maxu, minv, maxv;
+	explicit ClampReg(uint64_t r)
+	    : wms(field(r, 0, 2)), wmt(field(r, 2, 2)), minu(field(r, 4, 10)), maxu(field(r, 14, 10)),
+	      minv(field(r, 24, 10)), maxv(field(r, 34, 10)) {}
+};
+
+struct Tex1Reg
+{
+	uint32_t lcm, mxl, mmag, mmin, mtba, l, k;
+	explicit Tex1Reg(uint64_t r)
+	    : lcm(field(r, 0, 1)), mxl(field(r, 2, 3)), mmag(field(r, 5, 1)), mmin(field(r, 6, 3)),
+	      mtba(field(r, 9, 1)), l(field(r, 19, 2)), k(field(r, 32, 12)) {}
+	bool mmin_has_mipmap() const { return mmin > 1 && mmin <= 5; }
+};
+
+static bool frame_compat(uint64_t a, uint64_t b)
+{
+	// FBP, FBW, PSM must match; FBMSK may differ (FRAMEBits::compat).
+	return (a & 0x3f3f01ffull) == (b & 0x3f3f01ffull);
+}
+
+static bool zbuf_compat(uint64_t a, uint64_t b)
+{
+	return (a & 0x0f0001ffull) == (b & 0x0f0001ffull);
+}
+
+// Page-granular VRAM hazard tracker (a reduced gs/page_tracker.cpp).
+struct PageSpan
+{
+	uint32_t base_page;
+	uint32_t width, height, stride;
+};
+
+static PageSpan page_span(uint32_t base_block, uint32_t x, uint32_t y, uint32_t w, uint32_t h,
+                          uint32_t row_length_64, uint32_t psm)
+{
+	// Conservative page coverage of a rectangle (compute_page_rect, gs/gs_util.cpp:141-230).
+	Layout L = psm_layout(psm);
+	if (w == 0) w = 1;
+	if (h == 0) h = 1;
+	uint32_t px0 = x >> L.pw, px1 = (x + w - 1) >> L.pw;
+	uint32_t py0 = y >> L.ph, py1 = (y + h - 1) >> L.ph;
+	uint32_t stride = row_length_64;
+	if (psm == PSMT4 || psm == PSMT8)
+		stride >>= 1;
+	PageSpan s;
+	s.base_page = base_block / BLOCKS_PER_PAGE + py0 * stride + px0;
+	s.width = px1 - px0 + 1 + ((base_block % BLOCKS_PER_PAGE) ? 1 : 0);
+	s.height = py1 - py0 + 1;
+	s.stride = stride;
+	if (s.width > NUM_PAGES) s.width = NUM_PAGES;
+	if (s.height > NUM_PAGES) s.height = NUM_PAGES;
+	return s;
+}
+
+struct PageTracker
+{
+	enum : uint8_t { FB_WRITE = 1, FB_READ = 2, TEX_READ = 4 };
+	uint8_t state[NUM_PAGES] = {};
+
+	template <typename F>
+	void for_each(const PageSpan &s, F &&f)
+	{
+		for (uint32_t y = 0; y < s.height; y++)
+			for (uint32_t x = 0; x < s.width; x++)
+				f((s.base_page + y * s.stride + x) % NUM_PAGES);
+	}
+
+	bool any(const PageSpan &s, uint8_t mask)
+	{
+		bool hit = false;
+		for_each(s, [&](uint32_t p) { hit |= (state[p] & mask) != 0; });
+		return hit;
+	}
+
+	void mark(const PageSpan &s, uint8_t flags)
+	{
+		for_each(s, [&](uint32_t p) { state[p] |= flags; });
+	}
+
+	void clear() { memset(state, 0, sizeof(state)); }
+};
+
+struct Instance
+{
+	int32_t bb[4] = { INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN };
+	uint64_t frame = 0, zbuf = 0;
+	uint32_t color_write_mask = 0;
+	bool z_sensitive = false, z_write = false;
+};
+
+struct TextureKey
+{
+	pgs_texture_desc d;
+	bool operator==(const TextureKey &o) const { return memcmp(&d, &o.d, sizeof(d)) == 0; }
+};
+
+struct TextureKeyHash
+{
+	size_t operator()(const TextureKey &k) const
+	{
+		const uint32_t *w = reinterpret_cast<const uint32_t *>(&k.d);
+		uint64_t h = 1469598103934665603ull;
+		for (size_t i = 0; i < sizeof(k.d) / 4; i++)
+			h = (h ^ w[i]) * 1099511628211ull;
+		return size_t(h);
+	}
+};
+} // namespace
+
+struct pgs_gs
+{
+	const pgs_backend_ops *ops = nullptr;
+	void *be = nullptr;
+
+	uint64_t regs[128] = {};
+	float internal_q = 1.0f;
+	uint32_t cached_cbp[2] = {};
+
+	struct Path
+	{
+		uint64_t tag_lo = 0, tag_hi = 0;
+		uint32_t nloop = 0, flg = 0, nreg = 0;
+		uint32_t reg = 0, loop = 0;
+	} paths[4];
+
+	struct
+	{
+		pgs_vertex_position pos[3];
+		pgs_vertex_attribute attr[3];
+		uint32_t count = 0;
+	} vq;
+
+	// Render pass under construction.
+	pgs_vertex_position *positions = nullptr;
+	pgs_vertex_attribute *attributes = nullptr;
+	pgs_primitive_attribute *prims = nullptr;
+	uint32_t primitive_count = 0;
+	std::vector<pgs_state_vector> state_vectors;
+	std::vector<pgs_texture_desc> textures;
+	std::unordered_map<TextureKey, uint32_t, TextureKeyHash> texture_map;
+	Instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
+	uint32_t num_instances = 1;
+	uint32_t current_instance = 0;
+	bool has_aa1 = false, has_scanmsk = false;
+	uint32_t clut_instance = 0;
+	uint32_t pending_palette_updates = 0;
+	int32_t ofx = 0, ofy = 0;
+
+	// Cached primitive template; recomputed when template_dirty is set.
+	bool template_dirty = true;
+	uint32_t tpl_state = 0, tpl_tex = 0, tpl_tex2 = 0;
+	PageSpan tpl_tex_span = {};
+	bool tpl_has_tex_span = false;
+
+	PageTracker tracker;
+
+	struct
+	{
+		std::vector<uint64_t> payload;
+		bool active = false;
+		uint32_t required_qwords = 0;
+		uint32_t flushed_qwords = 0;
+		uint64_t bitbltbuf = 0, trxpos = 0, trxreg = 0, trxdir = 0;
+		std::vector<uint8_t> fifo;
+		uint32_t fifo_offset = 0, fifo_size = 0;
+	} xfer;
+
+	uint32_t sampling_rate_x_log2 = 0, sampling_rate_y_log2 = 0;
+	pgs_flush_stats stats = {};
+	int sticky_error = 0;
+
+	// ---------------------------------------------------------------
+	uint64_t ctx_reg(uint32_t base_addr) const
+	{
+		return regs[base_addr + field(regs[R_PRIM], 9, 1)];
+	}
+
+	void reserve_buffers()
+	{
+		int r = ops->reserve_primitive_buffers(be, PGS_MAX_PRIMITIVES_PER_FLUSH, &positions, &attributes, &prims);
+		if (r != 0)
+			sticky_error = r;
+	}
+
+	void set_super_sampling(uint32_t ss, bool ordered)
+	{
+		switch (ss)
+		{
+		case 2: sampling_rate_x_log2 = 0; sampling_rate_y_log2 = 1; break;
+		case 4:
+			if (ordered) { sampling_rate_x_log2 = 1; sampling_rate_y_log2 = 1; }
+			else { sampling_rate_x_log2 = 0; sampling_rate_y_log2 = 2; }
+			break;
+		case 8: sampling_rate_x_log2 = 1; sampling_rate_y_log2 = 2; break;
+		case 16:
+			if (ordered) { sampling_rate_x_log2 = 2; sampling_rate_y_log2 = 2; }
+			else { sampling_rate_x_log2 = 1; sampling_rate_y_log2 = 3; }
+			break;
+		default: sampling_rate_x_log2 = 0; sampling_rate_y_log2 = 0; break;
+		}
+		int r = ops->set_super_sampling(be, sampling_rate_x_log2, sampling_rate_y_log2);
+		if (r != 0)
+			sticky_error = r;
+	}
+
+	// ---------------------------------------------------------------
+	// Render pass flush (gs/gs_interface.cpp:133-351).
+	void flush_render_pass(uint32_t reason)
+	{
+		if (primitive_count)
+		{
+			pgs_render_pass rp = {};
+			rp.positions = positions;
+			rp.attributes = attributes;
+			rp.prims = prims;
+			rp.num_primitives = primitive_count;
+			rp.states = state_vectors.data();
+			rp.num_states = uint32_t(state_vectors.size());
+			rp.textures = textures.data();
+			rp.num_textures = uint32_t(textures.size());
+			rp.flush_reason = reason;
+			rp.has_aa1 = has_aa1;
+			rp.has_scanmsk = has_scanmsk;
+
+			uint64_t binning_cost = 0;
+			for (uint32_t i = 0; i < num_instances; i++)
+			{
+				auto &inst = instances[i];
+				if (inst.bb[2] < 0)
+					continue;
+				uint64_t tw = uint64_t((inst.bb[2] - inst.bb[0]) >> 3) + 1;
+				uint64_t th = uint64_t((inst.bb[3] - inst.bb[1]) >> 3) + 1;
+				binning_cost += tw * th * primitive_count;
+			}
+
+			uint32_t ts;
+			if (binning_cost < 10ull * 1000)
+				ts = 3;
+			else if (binning_cost < 10ull * 1000 * 1000)
+				ts = 4;
+			else if (binning_cost < 100ull * 1000 * 1000)
+				ts = 5;
+			else
+				ts = 6;
+			if (sampling_rate_y_log2 != 0 && ts > 3)
+				ts -= 1;
+
+			for (uint32_t i = 0; i < num_instances; i++)
+			{
+				auto &inst = instances[i];
+				if (inst.bb[2] < 0)
+					continue;
+				uint64_t cw = uint64_t((inst.bb[2] - inst.bb[0]) >> ts) + 1;
+				uint64_t ch = uint64_t((inst.bb[3] - inst.bb[1]) >> ts) + 1;
+				uint64_t list_size = cw * ch * primitive_count * sizeof(uint16_t);
+				while (list_size > 48ull * 1024 * 1024)
+				{
+					ts += 1;
+					list_size /= 4;
+				}
+			}
+			rp.coarse_tile_size_log2 = ts;
+
+			uint32_t n = num_instances;
+			if (instances[n - 1].bb[2] < 0)
+				n--;
+			rp.num_instances = n;
+
+			for (uint32_t i = 0; i < n; i++)
+			{
+				auto &inst = instances[i];
+				auto &pass = rp.instances[i];
+				pass.frame = inst.frame;
+				pass.zbuf = inst.zbuf;
+				pass.base_x = inst.bb[0];
+				pass.base_y = inst.bb[1];
+				pass.coarse_tiles_width = uint32_t((inst.bb[2] - inst.bb[0]) >> ts) + 1;
+				pass.coarse_tiles_height = uint32_t((inst.bb[3] - inst.bb[1]) >> ts) + 1;
+				pass.sampling_rate_x_log2 = sampling_rate_x_log2;
+				pass.sampling_rate_y_log2 = sampling_rate_y_log2;
+				pass.opaque_fbmask = ~inst.color_write_mask;
+
+				FrameReg frame(inst.frame);
+				ZbufReg zbuf(inst.zbuf);
+				bool channel_shuffle = false;
+				if (frame.psm != PSMCT32 && frame.psm != PSMCT24 && frame.psm != PSMZ32 && frame.psm != PSMZ24)
+				{
+					uint32_t m = inst.color_write_mask & 0xf8f8f8u;
+					channel_shuffle = m != 0xf8f8f8u && m != 0;
+				}
+				pass.channel_shuffle = channel_shuffle;
+
+				if (sampling_rate_y_log2 != 0)
+				{
+					if (channel_shuffle || (inst.z_write && zbuf.zbp == frame.fbp))
+					{
+						pass.sampling_rate_x_log2 = 0;
+						pass.sampling_rate_y_log2 = 0;
+					}
+				}
+				pass.z_sensitive = inst.z_sensitive;
+				pass.z_write = inst.z_write;
+			}
+
+			int r = ops->flush_rendering(be, &rp);
+			if (r != 0)
+				sticky_error = r;
+			stats.num_render_passes++;
+			stats.num_primitives += primitive_count;
+			stats.num_flushes_by_reason[reason & 7]++;
+		}
+
+		Instance keep = instances[current_instance];
+		for (auto &inst : instances)
+			inst = Instance();
+		instances[0].frame = keep.frame;
+		instances[0].zbuf = keep.zbuf;
+		num_instances = 1;
+		current_instance = 0;
+		primitive_count = 0;
+		state_vectors.clear();
+		textures.clear();
+		texture_map.clear();
+		pending_palette_updates = 0;
+		has_aa1 = false;
+		has_scanmsk = false;
+		template_dirty = true;
+		tracker.clear();
+		reserve_buffers();
+	}
+
+	void flush()
+	{
+		flush_pending_transfer(true);
+		flush_render_pass(FLUSH_EXPLICIT);
+		int r = ops->flush_submit(be);
+		if (r != 0)
+			sticky_error = r;
+	}
+
+	// ---------------------------------------------------------------
+	// Transfers (gs/gs_interface.cpp:2979-3276).
+	void init_transfer()
+	{
+		flush_pending_transfer(false);
+		xfer.bitbltbuf = regs[R_BITBLTBUF];
+		xfer.trxpos = regs[R_TRXPOS];
+		xfer.trxreg = regs[R_TRXREG];
+		xfer.trxdir = regs[R_TRXDIR];
+		uint32_t xdir = field(xfer.trxdir, 0, 2);
+		uint32_t rrw = field(xfer.trxreg, 0, 12), rrh = field(xfer.trxreg, 32, 12);
+		uint32_t dbp = field(xfer.bitbltbuf, 32, 14), dbw = field(xfer.bitbltbuf, 48, 6), dpsm = field(xfer.bitbltbuf, 56, 6);
+		uint32_t sbp = field(xfer.bitbltbuf, 0, 14), sbw = field(xfer.bitbltbuf, 16, 6), spsm = field(xfer.bitbltbuf, 24, 6);
+		uint32_t dsax = field(xfer.trxpos, 32, 11), dsay = field(xfer.trxpos, 48, 11);
+		uint32_t ssax = field(xfer.trxpos, 0, 11), ssay = field(xfer.trxpos, 16, 11);
+
+		if (xdir == LOCAL_TO_LOCAL)
+		{
+			PageSpan dst = page_span(dbp, dsax, dsay, rrw, rrh, dbw, dpsm);
+			PageSpan src = page_span(sbp, ssax, ssay, rrw, rrh, sbw, spsm);
+			if (tracker.any(dst, PageTracker::FB_WRITE | PageTracker::FB_READ | PageTracker::TEX_READ) ||
+			    tracker.any(src, PageTracker::FB_WRITE))
+				flush_render_pass(FLUSH_COPY_HAZARD);
+			pgs_copy_desc d = {};
+			d.bitbltbuf = xfer.bitbltbuf;
+			d.trxpos = xfer.trxpos;
+			d.trxreg = xfer.trxreg;
+			d.trxdir = xfer.trxdir;
+			int r = ops->copy_vram(be, &d);
+			if (r != 0)
+				sticky_error = r;
+			stats.num_copies++;
+			template_dirty = true;
+		}
+		else if (xdir == HOST_TO_LOCAL)
+		{
+			xfer.required_qwords = uint32_t((uint64_t(rrw) * rrh * psm_bits_per_pixel(dpsm)) / 64);
+			xfer.active = xfer.required_qwords != 0;
+			xfer.payload.clear();
+			xfer.flushed_qwords = 0;
+		}
+		else if (xdir == LOCAL_TO_HOST)
+		{
+			PageSpan src = page_span(sbp, ssax, ssay, rrw, rrh, sbw, spsm);
+			if (tracker.any(src, PageTracker::FB_WRITE))
+				flush_render_pass(FLUSH_HOST_ACCESS);
+			uint32_t bytes = uint32_t((uint64_t(rrw) * rrh * psm_bits_per_pixel(spsm)) / 8);
+			xfer.fifo.assign((bytes + 15) & ~15u, 0);
+			xfer.fifo_offset = 0;
+			xfer.fifo_size = bytes / 16;
+			readback_to_fifo(sbp, sbw, spsm, ssax, ssay, rrw, rrh);
+		}
+	}
+
+	void readback_to_fifo(uint32_t sbp, uint32_t sbw, uint32_t spsm, uint32_t sx, uint32_t sy, uint32_t w, uint32_t h)
+	{
+		std::vector<uint8_t> vram(VRAM_SIZE);
+		int r = ops->read_vram(be, 0, 0, VRAM_SIZE, vram.data());
+		if (r != 0)
+		{
+			sticky_error = r;
+			return;
+		}
+		// LOCAL->HOST de-swizzle (vram_readback, gs/gs_util.hpp:50-110).
+		uint8_t *dst = xfer.fifo.data();
+		for (uint32_t y = 0; y < h; y++)
+		{
+			uint32_t ey = (y + sy) & 2047;
+			for (uint32_t x = 0; x < w; x++)
+			{
+				uint32_t ex = (x + sx) & 2047;
+				uint32_t i = y * w + x;
+				uint32_t a = swizzle_address(ex, ey, sbp, sbw, spsm);
+				switch (spsm)
+				{
+				case PSMCT32: case PSMZ32: memcpy(dst + 4 * i, &vram[4 * a], 4); break;
+				case PSMCT24: case PSMZ24: memcpy(dst + 3 * i, &vram[4 * a], 3); break;
+				case PSMCT16: case PSMCT16S: case PSMZ16: case PSMZ16S: memcpy(dst + 2 * i, &vram[2 * a], 2); break;
+				case PSMT8: dst[i] = vram[a]; break;
+				case PSMT8H: dst[i] = vram[4 * a + 3]; break;
+				default: break;
+				}
+			}
+		}
+	}
+
+	void flush_pending_transfer(bool keep_alive)
+	{
+		if (xfer.active && xfer.payload.size() > xfer.flushed_qwords)
+		{
+			uint32_t rrw = field(xfer.trxreg, 0, 12), rrh = field(xfer.trxreg, 32, 12);
+			uint32_t dbp = field(xfer.bitbltbuf, 32, 14), dbw = field(xfer.bitbltbuf, 48, 6), dpsm = field(xfer.bitbltbuf, 56, 6);
+			uint32_t dsax = field(xfer.trxpos, 32, 11), dsay = field(xfer.trxpos, 48, 11);
+			PageSpan dst = page_span(dbp, dsax, dsay, rrw, rrh, dbw, dpsm);
+			if (tracker.any(dst, PageTracker::FB_WRITE | PageTracker::FB_READ | PageTracker::TEX_READ))
+				flush_render_pass(FLUSH_COPY_HAZARD);
+
+			pgs_copy_desc d = {};
+			d.bitbltbuf = xfer.bitbltbuf;
+			d.trxpos = xfer.trxpos;
+			d.trxreg = xfer.trxreg;
+			d.trxdir = xfer.trxdir;
+			d.host_data = xfer.payload.data();
+			d.host_size = xfer.payload.size() * sizeof(uint64_t);
+			d.host_offset = uint64_t(xfer.flushed_qwords) * sizeof(uint64_t);
+			d.host_required = uint64_t(xfer.required_qwords) * sizeof(uint64_t);
+			int r = ops->copy_vram(be, &d);
+			if (r != 0)
+				sticky_error = r;
+			stats.num_copies++;
+			xfer.flushed_qwords = uint32_t(xfer.payload.size());
+			template_dirty = true;
+		}
+
+		if (!keep_alive)
+		{
+			xfer.payload.clear();
+			xfer.flushed_qwords = 0;
+			xfer.active = false;
+		}
+	}
+
+	void hwreg(const uint64_t *data, size_t count)
+	{
+		if (!xfer.active)
+			return;
+		xfer.payload.insert(xfer.payload.end(), data, data + count);
+		if (xfer.payload.size() >= xfer.required_qwords)
+			flush_pending_transfer(false);
+	}
+
+	// ---------------------------------------------------------------
+	// CLUT loads (handle_clut_upload, gs/gs_interface.cpp:550-799).
+	void handle_clut_upload(uint32_t ctx)
+	{
+		Tex0Reg t(regs[R_TEX0_1 + ctx]);
+		uint32_t cpsm = t.cpsm == PSMCT24 ? PSMCT32 : t.cpsm;
+		if (!psm_is_palette(t.psm))
+			return;
+
+		bool load = false;
+		switch (t.cld)
+		{
+		case 1: load = true; break;
+		case 2: case 3: load = true; cached_cbp[t.cld & 1] = t.cbp; break;
+		case 4: case 5:
+			load = cached_cbp[t.cld & 1] != t.cbp;
+			cached_cbp[t.cld & 1] = t.cbp;
+			break;
+		default: break;
+		}
+		if (!load)
+			return;
+
+		if (xfer.active && xfer.payload.size() > xfer.flushed_qwords)
+			flush_pending_transfer(true);
+
+		uint32_t csa = t.csa;
+		if (cpsm == PSMCT32)
+			csa &= 15;
+
+		uint32_t pw, ph;
+		bool is8 = t.psm == PSMT8 || t.psm == PSMT8H;
+		if (is8)
+		{
+			pw = t.csm ? 256 : 16;
+			ph = t.csm ? 1 : 16;
+		}
+		else
+		{
+			pw = t.csm ? 16 : 8;
+			ph = t.csm ? 1 : 2;
+		}
+
+		uint64_t texclut = regs[R_TEXCLUT];
+		uint32_t cbw = field(texclut, 0, 6), cou = field(texclut, 6, 6), cov = field(texclut, 12, 10);
+		uint32_t xo = t.csm ? cou * 16 : 0, yo = t.csm ? cov : 0;
+		PageSpan src = page_span(t.cbp, xo, yo, pw, ph, t.csm ? cbw : 1, cpsm);
+		if (tracker.any(src, PageTracker::FB_WRITE))
+			flush_render_pass(FLUSH_CLUT_HAZARD);
+
+		// Normalise TEX0 to the fields that affect the palette load.
+		uint64_t tex0 = regs[R_TEX0_1 + ctx];
+		uint64_t keep = (0x3full << 20) | (0x3fffull << 37) | (0x1ull << 55);
+		tex0 &= keep;
+		tex0 |= uint64_t(cpsm) << 51;
+		tex0 |= uint64_t(csa) << 56;
+
+		pgs_palette_upload u = {};
+		u.tex0 = tex0;
+		u.texclut = texclut;
+		u.csm2_x_scale = 1.0f;
+		u.csm2_x_bias = 0;
+		u.base_instance = clut_instance;
+		int inst = ops->update_palette_cache(be, &u);
+		if (inst < 0)
+		{
+			sticky_error = inst;
+			return;
+		}
+		clut_instance = uint32_t(inst);
+		template_dirty = true;
+		stats.num_palette_updates++;
+		pending_palette_updates++;
+		if (pending_palette_updates >= PGS_CLUT_INSTANCES - 1)
+			flush_render_pass(FLUSH_OVERFLOW);
+	}
+
+	void handle_miptbl_gen(uint32_t ctx)
+	{
+		Tex1Reg tex1(regs[R_TEX1_1 + ctx]);
+		if (!tex1.mtba)
+			return;
+		Tex0Reg t(regs[R_TEX0_1 + ctx]);
+		uint32_t base = t.tbp0;
+		uint32_t w = 1u << t.tw, h = 1u << t.th;
+		uint32_t row = w / 64;
+		Layout L = psm_layout(t.psm);
+		uint32_t nblocks = (w >> L.bw) * (h >> L.bh);
+		base += nblocks;
+		nblocks /= 4;
+		row /= 2;
+		uint64_t m = 0;
+		m |= uint64_t(base & 0x3fff) | (uint64_t(row & 0x3f) << 14);
+		base += nblocks;
+		nblocks /= 4;
+		row /= 2;
+		m |= (uint64_t(base & 0x3fff) << 20) | (uint64_t(row & 0x3f) << 34);
+		base += nblocks;
+		m |= (uint64_t(base & 0x3fff) << 40) | (uint64_t(row & 0x3f) << 54);
+		regs[R_MIPTBP1_1 + ctx] = m;
+		template_dirty = true;
+	}
+
+	// ---------------------------------------------------------------
+	// Register writes.
+	void write_register(uint32_t addr, uint64_t v)
+	{
+		addr &= 0x7f;
+		switch (addr)
+		{
+		case R_PRIM:
+		{
+			bool ctxt_change = field(regs[R_PRIM], 9, 1) != field(v, 9, 1);
+			if (field(regs[R_PRMODECONT], 0, 1))
+			{
+				regs[R_PRIM] = v & 0x7ffull;
+				if (ctxt_change)
+					update_offsets();
+			}
+			else
+			{
+				regs[R_PRIM] = (regs[R_PRIM] & ~7ull) | (v & 7ull);
+			}
+			template_dirty = true;
+			vq.count = 0;
+			break;
+		}
+		case R_PRMODE:
+			if (!field(regs[R_PRMODECONT], 0, 1))
+			{
+				bool ctxt_change = field(regs[R_PRIM], 9, 1) != field(v, 9, 1);
+				regs[R_PRIM] = (v & ~7ull & 0x7ffull) | (regs[R_PRIM] & 7ull);
+				if (ctxt_change)
+					update_offsets();
+				template_dirty = true;
+			}
+			break;
+		case R_RGBAQ: case R_RGBAQ_UNDOC: regs[R_RGBAQ] = v; break;
+		case R_ST: regs[R_ST] = v; break;
+		case R_UV: regs[R_UV] = v; break;
+		case R_FOG: regs[R_FOG] = v; break;
+		case R_XYZF2: vertex_kick_xyzf(v); drawing_kick(false); break;
+		case R_XYZ2: vertex_kick_xyz(v); drawing_kick(false); break;
+		case R_XYZF3: vertex_kick_xyzf(v); drawing_kick(true); break;
+		case R_XYZ3: vertex_kick_xyz(v); drawing_kick(true); break;
+		case R_TEX0_1: case R_TEX0_2:
+			regs[addr] = v;
+			template_dirty = true;
+			handle_clut_upload(addr - R_TEX0_1);
+			handle_miptbl_gen(addr - R_TEX0_1);
+			break;
+		case R_TEX2_1: case R_TEX2_2:
+		{
+			// TEX2 writes PSM and CLUT fields of TEX0 only (a_d_TEX2, :2950-2968).
+			uint32_t ctx = addr - R_TEX2_1;
+			uint64_t preserve_mask = 0x3fffull | (0x3full << 14) | (0xfull << 26) | (0xfull << 30) |
+			                         (1ull << 34) | (3ull << 35);
+			uint64_t t = (regs[R_TEX0_1 + ctx] & preserve_mask) | (v & ~preserve_mask);
+			write_register(R_TEX0_1 + ctx, t);
+			break;
+		}
+		case R_XYOFFSET_1: case R_XYOFFSET_2:
+			regs[addr] = v;
+			update_offsets();
+			break;
+		case R_TEXFLUSH:
+			template_dirty = true;
+			break;
+		case R_BITBLTBUF: case R_TRXPOS: case R_TRXREG:
+			regs[addr] = v;
+			break;
+		case R_TRXDIR:
+			regs[addr] = v;
+			init_transfer();
+			break;
+		case R_HWREG:
+			hwreg(&v, 1);
+			break;
+		case R_SIGNAL: case R_FINISH: case R_LABEL:
+			break;
+		default:
+			if (regs[addr] != v)
+			{
+				regs[addr] = v;
+				template_dirty = true;
+			}
+			break;
+		}
+	}
+
+	void update_offsets()
+	{
+		uint64_t xy = regs[R_XYOFFSET_1 + field(regs[R_PRIM], 9, 1)];
+		ofx = int32_t(field(xy, 0, 16));
+		ofy = int32_t(field(xy, 32, 16));
+	}
+
+	// ---------------------------------------------------------------
+	// Vertex queue (gs/gs_interface.cpp:843-897).
+	void shift_queue()
+	{
+		if (vq.count == 3)
+		{
+			vq.pos[0] = vq.pos[1];
+			vq.attr[0] = vq.attr[1];
+			vq.pos[1] = vq.pos[2];
+			vq.attr[1] = vq.attr[2];
+			vq.count = 2;
+		}
+	}
+
+	void fill_attr(pgs_vertex_attribute &a, float fog)
+	{
+		uint64_t st = regs[R_ST], rgbaq = regs[R_RGBAQ], uv = regs[R_UV];
+		uint32_t sbits = uint32_t(st), tbits = uint32_t(st >> 32), qbits = uint32_t(rgbaq >> 32);
+		memcpy(&a.s, &sbits, 4);
+		memcpy(&a.t, &tbits, 4);
+		memcpy(&a.q, &qbits, 4);
+		a.rgba = uint32_t(rgbaq);
+		a.fog = fog;
+		a.u = uint16_t(field(uv, 0, 14));
+		a.v = uint16_t(field(uv, 16, 14));
+	}
+
+	void vertex_kick_xyz(uint64_t v)
+	{
+		shift_queue();
+		auto &p = vq.pos[vq.count];
+		p.x = int32_t(field(v, 0, 16)) - ofx;
+		p.y = int32_t(field(v, 16, 16)) - ofy;
+		p.z = uint32_t(v >> 32);
+		p.padding = 0;
+		fill_attr(vq.attr[vq.count], float(field(regs[R_FOG], 56, 8)));
+		vq.count++;
+	}
+
+	void vertex_kick_xyzf(uint64_t v)
+	{
+		shift_queue();
+		auto &p = vq.pos[vq.count];
+		p.x = int32_t(field(v, 0, 16)) - ofx;
+		p.y = int32_t(field(v, 16, 16)) - ofy;
+		p.z = field(v, 32, 24);
+		p.padding = 0;
+		fill_attr(vq.attr[vq.count], float(field(v, 56, 8)));
+		vq.count++;
+	}
+
+	// ---------------------------------------------------------------
+	// draw_is_degenerate (gs/gs_interface.cpp:2036-2115).
+	bool draw_is_degenerate()
+	{
+		PrimReg prim(regs[R_PRIM]);
+		uint64_t sc = ctx_reg(R_SCISSOR_1);
+		if (field(sc, 0, 11) > field(sc, 16, 11) || field(sc, 32, 11) > field(sc, 48, 11))
+			return true;
+		TestReg test(ctx_reg(R_TEST_1));
+		if (test.zte && test.ztst == 0)
+			return true;
+		if (test.ate && test.atst == ATST_NEVER && test.afail == AFAIL_KEEP)
+			return true;
+		FrameReg frame(ctx_reg(R_FRAME_1));
+		ZbufReg zbuf(ctx_reg(R_ZBUF_1));
+		uint32_t fbmsk = frame.fbmsk, zmsk = zbuf.zmsk;
+		if (frame.psm == PSMCT24 || frame.psm == PSMZ24)
+			fbmsk |= 0xffu << 24;
+		if (test.ate && test.atst == ATST_NEVER)
+		{
+			switch (test.afail)
+			{
+			case AFAIL_ZB_ONLY: fbmsk = 0xffffffffu; break;
+			case AFAIL_KEEP: fbmsk = 0xffffffffu; zmsk = 1; break;
+			case AFAIL_FB_ONLY: zmsk = 1; break;
+			case AFAIL_RGB_ONLY: fbmsk |= 0xffu << 24; break;
+			default: break;
+			}
+		}
+		AlphaReg alpha(ctx_reg(R_ALPHA_1));
+		if (prim.abe && alpha.d == BLEND_RGB_DEST && alpha.a == alpha.b)
+			fbmsk |= 0xffffffu;
+		bool ro_color = fbmsk == 0xffffffffu;
+		bool ro_depth = zmsk || !test.zte;
+		return ro_color && ro_depth;
+	}
+
+	bool state_is_z_sensitive()
+	{
+		TestReg test(ctx_reg(R_TEST_1));
+		if (test.zte)
+		{
+			if (test.has_z_test())
+				return true;
+			bool implied_z_mask = test.ate && test.atst == ATST_NEVER && test.afail != AFAIL_ZB_ONLY;
+			if (!implied_z_mask && ZbufReg(ctx_reg(R_ZBUF_1)).zmsk == 0)
+				return true;
+		}
+		return false;
+	}
+
+	// check_frame_buffer_state (gs/gs_interface.cpp:935-1023).
+	void check_frame_buffer_state()
+	{
+		uint64_t frame = ctx_reg(R_FRAME_1), zbuf = ctx_reg(R_ZBUF_1);
+		Instance *inst = &instances[current_instance];
+		bool fb_delta = !frame_compat(inst->frame, frame);
+		bool z_delta = !zbuf_compat(inst->zbuf, zbuf);
+		if (primitive_count && (fb_delta || (z_delta && inst->z_sensitive)))
+		{
+			uint32_t found = num_instances;
+			for (uint32_t i = 0; i < num_instances; i++)
+			{
+				auto &t = instances[i];
+				if (frame_compat(t.frame, frame) && (!t.z_sensitive || zbuf_compat(t.zbuf, zbuf)))
+				{
+					found = i;
+					break;
+				}
+			}
+			if (found == num_instances)
+			{
+				if (num_instances < PGS_MAX_RENDER_PASS_INSTANCES)
+				{
+					instances[num_instances] = Instance();
+					num_instances++;
+				}
+				else
+				{
+					flush_pending_transfer(true);
+					flush_render_pass(FLUSH_FB_POINTER);
+					found = 0;
+				}
+			}
+			current_instance = found;
+			inst = &instances[current_instance];
+			template_dirty = true;
+		}
+		inst->frame = frame;
+		inst->zbuf = zbuf;
+	}
+
+	uint32_t find_state_vector(const pgs_state_vector &s)
+	{
+		for (uint32_t i = 0; i < state_vectors.size(); i++)
+		{
+			auto &o = state_vectors[i];
+			if (o.combiner == s.combiner && o.blend_mode == s.blend_mode && o.dimx_lo == s.dimx_lo && o.dimx_hi == s.dimx_hi)
+				return i;
+		}
+		state_vectors.push_back(s);
+		return uint32_t(state_vectors.size() - 1);
+	}
+
+	// drawing_kick_update_state_vector (gs/gs_interface.cpp:1065-1128).
+	uint32_t update_state_vector()
+	{
+		PrimReg prim(regs[R_PRIM]);
+		TestReg test(ctx_reg(R_TEST_1));
+		AlphaReg alpha(ctx_reg(R_ALPHA_1));
+		Tex0Reg tex0(ctx_reg(R_TEX0_1));
+		pgs_state_vector s = {};
+		if (field(regs[R_DTHE], 0, 1))
+		{
+			s.blend_mode |= BLEND_MODE_DTHE_BIT;
+			s.dimx_lo = uint32_t(regs[R_DIMX]);
+			s.dimx_hi = uint32_t(regs[R_DIMX] >> 32);
+		}
+		if (test.ate && test.atst != ATST_ALWAYS)
+		{
+			bool implied_z_mask = test.atst == ATST_NEVER && test.afail == AFAIL_FB_ONLY;
+			if (!implied_z_mask)
+			{
+				s.blend_mode |= BLEND_MODE_ATE_BIT;
+				s.blend_mode |= test.atst << BLEND_MODE_ATE_MODE_OFFSET;
+				s.blend_mode |= test.afail << BLEND_MODE_AFAIL_MODE_OFFSET;
+			}
+		}
+		s.blend_mode |= test.date ? BLEND_MODE_DATE_BIT : 0;
+		s.blend_mode |= test.datm ? BLEND_MODE_DATM_BIT : 0;
+		if (prim.abe || prim.aa1)
+		{
+			s.blend_mode |= alpha.a << BLEND_MODE_A_MODE_OFFSET;
+			s.blend_mode |= alpha.b << BLEND_MODE_B_MODE_OFFSET;
+			s.blend_mode |= alpha.c << BLEND_MODE_C_MODE_OFFSET;
+			s.blend_mode |= alpha.d << BLEND_MODE_D_MODE_OFFSET;
+		}
+		if (prim.abe)
+		{
+			s.blend_mode |= BLEND_MODE_ABE_BIT;
+			s.blend_mode |= field(regs[R_PABE], 0, 1) ? BLEND_MODE_PABE_BIT : 0;
+		}
+		s.blend_mode |= field(regs[R_COLCLAMP], 0, 1) ? BLEND_MODE_COLCLAMP_BIT : 0;
+		s.blend_mode |= field(ctx_reg(R_FBA_1), 0, 1) ? BLEND_MODE_FB_ALPHA_BIT : 0;
+		if (prim.tme)
+		{
+			s.combiner |= COMBINER_TME_BIT;
+			s.combiner |= tex0.tcc ? COMBINER_TCC_BIT : 0;
+			s.combiner |= tex0.tfx;
+		}
+		s.combiner |= prim.fge ? COMBINER_FOG_BIT : 0;
+		return find_state_vector(s);
+	}
+
+	// Texture descriptor for the current context (drawing_kick_update_texture,
+	// gs/gs_interface.cpp:1254-1800), without the image cache.
+	uint32_t update_texture(PageSpan &span)
+	{
+		Tex0Reg t(ctx_reg(R_TEX0_1));
+		ClampReg c(ctx_reg(R_CLAMP_1));
+		uint64_t texa = regs[R_TEXA];
+		pgs_texture_desc d = {};
+		d.tbp0 = t.tbp0;
+		d.tbw = t.tbw;
+		d.psm = t.psm;
+		d.tw_log2 = std::min<uint32_t>(t.tw, 10);
+		d.th_log2 = std::min<uint32_t>(t.th, 10);
+		uint32_t cpsm = t.cpsm == PSMCT24 ? PSMCT32 : t.cpsm;
+		if (psm_is_palette(t.psm))
+		{
+			d.cpsm = cpsm;
+			d.csa = cpsm == PSMCT32 ? (t.csa & 15) : t.csa;
+			d.clut_instance = clut_instance;
+			if (cpsm != PSMCT32)
+			{
+				d.aem = field(texa, 15, 1);
+				d.ta0 = field(texa, 0, 8);
+				d.ta1 = field(texa, 32, 8);
+			}
+		}
+		else if (t.psm != PSMCT32 && t.psm != PSMZ32)
+		{
+			d.aem = field(texa, 15, 1);
+			d.ta0 = field(texa, 0, 8);
+			d.ta1 = field(texa, 32, 8);
+		}
+		d.wms = c.wms;
+		d.wmt = c.wmt;
+		if (c.wms >= WRAP_REGION_CLAMP)
+		{
+			d.minu = c.minu;
+			d.maxu = c.maxu;
+		}
+		if (c.wmt >= WRAP_REGION_CLAMP)
+		{
+			d.minv = c.minv;
+			d.maxv = c.maxv;
+		}
+
+		uint32_t w = 1u << d.tw_log2, h = 1u << d.th_log2;
+		span = page_span(t.tbp0, 0, 0, w, h, t.tbw ? t.tbw : 1, t.psm);
+		// Large dummy TW/TH with a small stride cover far more pages than are sampled
+		// (compute_has_potential_feedback, gs/gs_util.cpp:81-139).
+		if (w >= 1024 && t.tbw)
+			span = page_span(t.tbp0, 0, 0, std::min<uint32_t>(w, t.tbw * 64), h, t.tbw, t.psm);
+
+		TextureKey key{ d };
+		auto it = texture_map.find(key);
+		if (it != texture_map.end())
+			return it->second;
+		uint32_t index = uint32_t(textures.size());
+		textures.push_back(d);
+		texture_map.emplace(key, index);
+		return index;
+	}
+
+	// drawing_kick_update_state (gs/gs_interface.cpp:1804-1968).
+	void update_template()
+	{
+		PrimReg prim(regs[R_PRIM]);
+		TestReg test(ctx_reg(R_TEST_1));
+		AlphaReg alpha(ctx_reg(R_ALPHA_1));
+		ZbufReg zbuf(ctx_reg(R_ZBUF_1));
+		uint32_t state = 0, tex = 0, tex2 = 0;
+		tpl_has_tex_span = false;
+
+		if (prim.tme)
+		{
+			Tex1Reg tex1(ctx_reg(R_TEX1_1));
+			ClampReg clamp(ctx_reg(R_CLAMP_1));
+			uint32_t index = update_texture(tpl_tex_span);
+			tpl_has_tex_span = true;
+			tex = index;
+			tex |= tex1.mmag ? TEX_SAMPLER_MAG_LINEAR_BIT : 0;
+			tex |= (clamp.wms == WRAP_CLAMP || clamp.wms == WRAP_REGION_CLAMP) ? TEX_SAMPLER_CLAMP_S_BIT : 0;
+			tex |= (clamp.wmt == WRAP_CLAMP || clamp.wmt == WRAP_REGION_CLAMP) ? TEX_SAMPLER_CLAMP_T_BIT : 0;
+			if (tex1.mmin_has_mipmap())
+			{
+				tex2 = tex1.lcm;
+				tex2 |= tex1.l << 1;
+				tex2 |= tex1.k << 3;
+				tex |= tex1.mxl << TEX_MAX_MIP_LEVEL_OFFSET;
+				switch (tex1.mmin)
+				{
+				case 1: tex |= TEX_SAMPLER_MIN_LINEAR_BIT; break;
+				case 3: tex |= TEX_SAMPLER_MIPMAP_LINEAR_BIT; break;
+				case 4: tex |= TEX_SAMPLER_MIN_LINEAR_BIT; break;
+				case 5: tex |= TEX_SAMPLER_MIN_LINEAR_BIT | TEX_SAMPLER_MIPMAP_LINEAR_BIT; break;
+				default: break;
+				}
+			}
+			else
+			{
+				tex2 = TEX2_FIXED_LOD_BIT;
+			}
+		}
+
+		state = update_state_vector();
+
+		if (test.zte)
+		{
+			if (test.has_z_test())
+			{
+				state |= 1u << STATE_BIT_Z_TEST;
+				state |= test.ztst == 3 ? (1u << STATE_BIT_Z_TEST_GREATER) : 0;
+			}
+			bool implied_z_mask = test.ate && test.atst == ATST_NEVER && test.afail != AFAIL_ZB_ONLY;
+			if (!implied_z_mask && zbuf.zmsk == 0)
+				state |= 1u << STATE_BIT_Z_WRITE;
+		}
+
+		bool needs_previous = false;
+		if (prim.abe || prim.aa1)
+		{
+			if (alpha.a == BLEND_RGB_DEST || alpha.b == BLEND_RGB_DEST || alpha.c == BLEND_ALPHA_DEST ||
+			    alpha.d == BLEND_RGB_DEST)
+				needs_previous = true;
+		}
+		if (test.date)
+			needs_previous = true;
+		else if (test.ate && test.atst != ATST_ALWAYS)
+		{
+			bool can_write_z = (state & (1u << STATE_BIT_Z_WRITE)) != 0;
+			bool can_mask_color = test.afail != AFAIL_FB_ONLY;
+			bool can_mask_z = can_write_z && test.afail != AFAIL_ZB_ONLY;
+			if (can_mask_color || can_mask_z)
+				needs_previous = true;
+		}
+		if (!needs_previous)
+			state |= 1u << STATE_BIT_OPAQUE;
+
+		if (prim.enables_aa1())
+		{
+			state |= 1u << STATE_BIT_MULTISAMPLE;
+			has_aa1 = true;
+		}
+
+		uint32_t msk = field(regs[R_SCANMSK], 0, 2);
+		if (msk >= 2)
+		{
+			state |= 1u << (STATE_BIT_SCANMSK_EVEN + msk - 2);
+			has_scanmsk = true;
+		}
+
+		if (!prim.fst)
+			state |= 1u << STATE_BIT_PERSPECTIVE;
+		if (prim.iip)
+			state |= 1u << STATE_BIT_IIP;
+		if (prim.fix)
+			state |= 1u << STATE_BIT_FIX;
+
+		tpl_state = state;
+		tpl_tex = tex;
+		tpl_tex2 = tex2;
+	}
+
+	// ---------------------------------------------------------------
+	// Drawing kick (gs/gs_interface.cpp:2473-2943).
+	void drawing_kick(bool adc)
+	{
+		uint32_t type = field(regs[R_PRIM], 0, 3);
+		uint32_t nv;
+		bool list = false, fan = false, quad = false;
+		switch (type)
+		{
+		case PRIM_POINT: nv = 1; list = true; quad = true; break;
+		case PRIM_LINE_LIST: nv = 2; list = true; break;
+		case PRIM_LINE_STRIP: nv = 2; break;
+		case PRIM_TRI_LIST: nv = 3; list = true; break;
+		case PRIM_TRI_STRIP: nv = 3; break;
+		case PRIM_TRI_FAN: nv = 3; fan = true; break;
+		case PRIM_SPRITE: nv = 2; list = true; quad = true; break;
+		default:
+			vq.count = 0;
+			post_kick();
+			return;
+		}
+
+		if (vq.count >= nv)
+		{
+			if (!adc && !draw_is_degenerate())
+				append(nv, quad);
+
+			if (fan)
+			{
+				vq.pos[1] = vq.pos[2];
+				vq.attr[1] = vq.attr[2];
+				vq.count = 2;
+			}
+			else if (list)
+			{
+				vq.count = 0;
+			}
+		}
+		post_kick();
+	}
+
+	void post_kick()
+	{
+		if (pending_palette_updates >= PGS_CLUT_INSTANCES - 1 || primitive_count >= PGS_MAX_PRIMITIVES_PER_FLUSH ||
+		    textures.size() >= PGS_MAX_TEXTURES || state_vectors.size() >= PGS_MAX_STATE_VECTORS)
+		{
+			flush_pending_transfer(true);
+			flush_render_pass(FLUSH_OVERFLOW);
+		}
+	}
+
+	void append(uint32_t nv, bool quad)
+	{
+		PrimReg prim(regs[R_PRIM]);
+		pgs_vertex_position pos[3] = {};
+		pgs_vertex_attribute attr[3] = {};
+
+		if (nv == 1)
+		{
+			pos[0] = vq.pos[vq.count - 1];
+			attr[0] = vq.attr[vq.count - 1];
+			pos[0].x -= (1 << (SUBPIXEL_BITS - 1)) - 1;
+			pos[0].y -= (1 << (SUBPIXEL_BITS - 1)) - 1;
+			pos[1] = pos[0];
+			pos[1].x += 1 << SUBPIXEL_BITS;
+			pos[1].y += 1 << SUBPIXEL_BITS;
+		}
+		else if (nv == 2)
+		{
+			for (uint32_t i = 0; i < 2; i++)
+			{
+				pos[i] = vq.pos[vq.count - 1 - i];
+				attr[i] = vq.attr[vq.count - 1 - i];
+			}
+		}
+		else
+		{
+			for (uint32_t i = 0; i < 3; i++)
+			{
+				pos[i] = vq.pos[2 - i];
+				attr[i] = vq.attr[2 - i];
+			}
+		}
+
+		bool is_line = !quad && nv == 2;
+		int32_t lo[2] = { std::min(pos[0].x, pos[1].x), std::min(pos[0].y, pos[1].y) };
+		int32_t hi[2] = { std::max(pos[0].x, pos[1].x), std::max(pos[0].y, pos[1].y) };
+		if (!quad && !is_line)
+		{
+			lo[0] = std::min(lo[0], pos[2].x);
+			lo[1] = std::min(lo[1], pos[2].y);
+			hi[0] = std::max(hi[0], pos[2].x);
+			hi[1] = std::max(hi[1], pos[2].y);
+		}
+		hi[0] -= 1;
+		hi[1] -= 1;
+		int32_t snap = (1 << int(SUBPIXEL_BITS - sampling_rate_y_log2)) - 1;
+		lo[0] += snap;
+		lo[1] += snap;
+		lo[0] >>= SUBPIXEL_BITS;
+		lo[1] >>= SUBPIXEL_BITS;
+		hi[0] >>= SUBPIXEL_BITS;
+		hi[1] >>= SUBPIXEL_BITS;
+		if (is_line || prim.enables_aa1())
+		{
+			lo[0] -= 1; lo[1] -= 1;
+			hi[0] += 1; hi[1] += 1;
+		}
+
+		uint64_t sc = ctx_reg(R_SCISSOR_1);
+		FrameReg frame(ctx_reg(R_FRAME_1));
+		int32_t sci_lo[2] = { int32_t(field(sc, 0, 11)), int32_t(field(sc, 32, 11)) };
+		int32_t sci_hi[2] = { int32_t(field(sc, 16, 11)), int32_t(field(sc, 48, 11)) };
+		int32_t fb_width = int32_t(std::max<uint32_t>(1, frame.fbw) * BUFFER_WIDTH_SCALE);
+		int32_t sci_hi_x_fb = std::min(sci_hi[0], fb_width - 1);
+		bool can_wrap = frame.fbw != 0 && sci_hi_x_fb < sci_hi[0];
+
+		int32_t bb[4] = { std::max(lo[0], sci_lo[0]), std::max(lo[1], sci_lo[1]),
+		                  std::min(hi[0], sci_hi[0]), std::min(hi[1], sci_hi[1]) };
+		if (bb[2] < bb[0] || bb[3] < bb[1])
+			return;
+
+		// Flush a pending partial upload before reading textures.
+		if (prim.tme && xfer.active && xfer.payload.size() > xfer.flushed_qwords)
+			flush_pending_transfer(true);
+
+		check_frame_buffer_state();
+
+		if (template_dirty)
+		{
+			update_template();
+			template_dirty = false;
+		}
+
+		// Texture read after framebuffer write in the same pass: end the pass
+		// (mark_texture_read, gs/page_tracker.cpp:327-345).
+		if (tpl_has_tex_span && tracker.any(tpl_tex_span, PageTracker::FB_WRITE))
+		{
+			flush_render_pass(FLUSH_TEXTURE_HAZARD);
+			check_frame_buffer_state();
+			update_template();
+			template_dirty = false;
+		}
+
+		if (can_wrap && bb[0] > sci_hi_x_fb)
+		{
+			Layout L = psm_layout(frame.psm);
+			int32_t x_off = -int32_t(frame.fbw << L.pw);
+			int32_t y_off = int32_t(1u << L.ph);
+			while (bb[0] > sci_hi_x_fb)
+			{
+				bb[0] += x_off; bb[2] += x_off;
+				bb[1] += y_off; bb[3] += y_off;
+				for (uint32_t i = 0; i < nv; i++)
+				{
+					pos[i].x += x_off << SUBPIXEL_BITS;
+					pos[i].y += y_off << SUBPIXEL_BITS;
+				}
+			}
+			bb[2] = std::min(bb[2], sci_hi_x_fb);
+			bb[0] = std::max(bb[0], 0);
+			if (bb[2] < bb[0])
+				return;
+		}
+		else if (can_wrap)
+		{
+			bb[2] = std::min(bb[2], sci_hi_x_fb);
+		}
+
+		// Framebuffer pages this primitive may write.  If an earlier primitive of
+		// this pass samples them, end the pass first.
+		{
+			ZbufReg zb(ctx_reg(R_ZBUF_1));
+			Layout FL = psm_layout(frame.psm);
+			(void)FL;
+			PageSpan fb_span = page_span(frame.fbp * BLOCKS_PER_PAGE, uint32_t(bb[0]), uint32_t(bb[1]),
+			                             uint32_t(bb[2] - bb[0] + 1), uint32_t(bb[3] - bb[1] + 1),
+			                             frame.fbw ? frame.fbw : 1, frame.psm);
+			bool z_sens = state_is_z_sensitive();
+			PageSpan z_span = page_span(zb.zbp * BLOCKS_PER_PAGE, uint32_t(bb[0]), uint32_t(bb[1]),
+			                            uint32_t(bb[2] - bb[0] + 1), uint32_t(bb[3] - bb[1] + 1),
+			                            frame.fbw ? frame.fbw : 1, zb.psm | 0x30);
+			bool hazard = tracker.any(fb_span, PageTracker::TEX_READ) ||
+			              (z_sens && tracker.any(z_span, PageTracker::TEX_READ));
+			if (hazard && primitive_count)
+			{
+				flush_render_pass(FLUSH_TEXTURE_HAZARD);
+				check_frame_buffer_state();
+				update_template();
+				template_dirty = false;
+			}
+			if (tpl_has_tex_span)
+				tracker.mark(tpl_tex_span, PageTracker::TEX_READ);
+			tracker.mark(fb_span, PageTracker::FB_WRITE);
+			if (z_sens)
+				tracker.mark(z_span, zb.zmsk ? PageTracker::FB_READ : PageTracker::FB_WRITE);
+		}
+
+		auto &inst = instances[current_instance];
+		pgs_primitive_attribute pa = {};
+		pa.tex = tpl_tex;
+		pa.tex2 = tpl_tex2;
+		pa.state = tpl_state;
+		pa.fbmsk = frame.fbmsk;
+		pa.fogcol = uint32_t(regs[R_FOGCOL]);
+		AlphaReg alpha(ctx_reg(R_ALPHA_1));
+		TestReg test(ctx_reg(R_TEST_1));
+		pa.alpha = (alpha.fix << ALPHA_AFIX_OFFSET) | (test.aref << ALPHA_AREF_OFFSET);
+
+		if (quad)
+		{
+			pa.state |= (1u << STATE_BIT_PARALLELOGRAM) | (1u << STATE_BIT_SPRITE) |
+			            (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
+			pa.state &= ~(1u << STATE_BIT_MULTISAMPLE);
+		}
+		else if (is_line)
+		{
+			pa.state |= (1u << STATE_BIT_PARALLELOGRAM) | (1u << STATE_BIT_LINE);
+			if (pa.state & (1u << STATE_BIT_MULTISAMPLE))
+				pa.state &= ~(1u << STATE_BIT_Z_WRITE);
+		}
+		if (nv == 1)
+			pa.state |= (1u << STATE_BIT_FIX) | (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
+		pa.state |= current_instance << STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET;
+
+		bool z_sens = state_is_z_sensitive();
+		if (!inst.z_sensitive && z_sens)
+			inst.z_sensitive = true;
+		if (z_sens && ZbufReg(ctx_reg(R_ZBUF_1)).zmsk == 0 && !inst.z_write)
+			inst.z_write = true;
+		inst.color_write_mask |= ~frame.fbmsk;
+		inst.bb[0] = std::min(inst.bb[0], bb[0]);
+		inst.bb[1] = std::min(inst.bb[1], bb[1]);
+		inst.bb[2] = std::max(inst.bb[2], bb[2]);
+		inst.bb[3] = std::max(inst.bb[3], bb[3]);
+
+		pa.bb[0] = int16_t(bb[0]);
+		pa.bb[1] = int16_t(bb[1]);
+		pa.bb[2] = int16_t(bb[2]);
+		pa.bb[3] = int16_t(bb[3]);
+
+		uint32_t n = primitive_count;
+		prims[n] = pa;
+		memcpy(positions + 3 * n, pos, sizeof(pos));
+		memcpy(attributes + 3 * n, attr, sizeof(attr));
+		primitive_count++;
+	}
+
+	// ---------------------------------------------------------------
+	// GIF packet decode (gs/gs_interface.cpp:4290-4397).
+	void packed_write(uint32_t desc, const uint64_t *q)
+	{
+		uint64_t lo = q[0], hi = q[1];
+		switch (desc)
+		{
+		case 0x0: write_register(R_PRIM, lo & 0x7ff); break;
+		case 0x1:
+		{
+			uint32_t qbits;
+			memcpy(&qbits, &internal_q, 4);
+			uint64_t v = field(lo, 0, 8) | (uint64_t(field(lo, 32, 8)) << 8) |
+			             (uint64_t(field(hi, 0, 8)) << 16) | (uint64_t(field(hi, 32, 8)) << 24) |
+			             (uint64_t(qbits) << 32);
+			regs[R_RGBAQ] = v;
+			break;
+		}
+		case 0x2:
+		{
+			regs[R_ST] = lo;
+			uint32_t qbits = uint32_t(hi);
+			memcpy(&internal_q, &qbits, 4);
+			break;
+		}
+		case 0x3: regs[R_UV] = field(lo, 0, 14) | (uint64_t(field(lo, 32, 14)) << 16); break;
+		case 0x4:
+		{
+			uint64_t v = field(lo, 0, 16) | (uint64_t(field(lo, 32, 16)) << 16) |
+			             (uint64_t(field(hi, 4, 24)) << 32) | (uint64_t(field(hi, 36, 8)) << 56);
+			bool adc = field(hi, 47, 1) != 0;
+			vertex_kick_xyzf(v);
+			drawing_kick(adc);
+			break;
+		}
+		case 0x5:
+		{
+			uint64_t v = field(lo, 0, 16) | (uint64_t(field(lo, 32, 16)) << 16) | (uint64_t(uint32_t(hi)) << 32);
+			bool adc = field(hi, 47, 1) != 0;
+			vertex_kick_xyz(v);
+			drawing_kick(adc);
+			break;
+		}
+		case 0xa: regs[R_FOG] = uint64_t(field(hi, 36, 8)) << 56; break;
+		case 0xc:
+		{
+			uint64_t v = field(lo, 0, 16) | (uint64_t(field(lo, 32, 16)) << 16) |
+			             (uint64_t(field(hi, 4, 24)) << 32) | (uint64_t(field(hi, 36, 8)) << 56);
+			vertex_kick_xyzf(v);
+			drawing_kick(true);
+			break;
+		}
+		case 0xd:
+		{
+			uint64_t v = field(lo, 0, 16) | (uint64_t(field(lo, 32, 16)) << 16) | (uint64_t(uint32_t(hi)) << 32);
+			vertex_kick_xyz(v);
+			drawing_kick(true);
+			break;
+		}
+		case 0xe: write_register(uint32_t(hi & 0x7f), lo); break;
+		case 0x6: case 0x7: case 0x8: case 0x9: write_register(desc, lo); break;
+		default: break;
+		}
+	}
+
+	void gif_transfer(uint32_t pi, const uint64_t *words, size_t qwords)
+	{
+		auto &path = paths[pi & 3];
+		size_t i = 0;
+		while (i < qwords)
+		{
+			if (path.loop == path.nloop)
+			{
+				path.tag_lo = words[2 * i];
+				path.tag_hi = words[2 * i + 1];
+				path.nloop = field(path.tag_lo, 0, 15);
+				path.flg = field(path.tag_lo, 58, 2);
+				path.nreg = field(path.tag_lo, 60, 4);
+				if (path.nreg == 0)
+					path.nreg = 16;
+				bool pre = field(path.tag_lo, 46, 1) != 0;
+				if (path.flg == 0 && pre && path.nloop)
+				{
+					// GIFtag PRIM field: behaves like an A+D PRIM write.
+					write_register(R_PRIM, field(path.tag_lo, 47, 11));
+				}
+				path.loop = 0;
+				path.reg = 0;
+				if (path.nloop)
+					internal_q = 1.0f;
+				i++;
+				continue;
+			}
+
+			if (path.flg == 0)
+			{
+				uint32_t desc = uint32_t(path.tag_hi >> (4 * path.reg)) & 0xf;
+				packed_write(desc, &words[2 * i]);
+				i++;
+				if (++path.reg == path.nreg)
+				{
+					path.reg = 0;
+					path.loop++;
+				}
+			}
+			else if (path.flg == 1)
+			{
+				for (uint32_t j = 0; j < 2; j++)
+				{
+					uint32_t desc = uint32_t(path.tag_hi >> (4 * path.reg)) & 0xf;
+					uint64_t v = words[2 * i + j];
+					reglist_write(desc, v);
+					if (++path.reg == path.nreg)
+					{
+						path.reg = 0;
+						path.loop++;
+						if (path.loop == path.nloop)
+							break;
+					}
+				}
+				i++;
+			}
+			else
+			{
+				size_t n = std::min<size_t>(qwords - i, path.nloop - path.loop);
+				hwreg(&words[2 * i], n * 2);
+				i += n;
+				path.loop += uint32_t(n);
+			}
+		}
+	}
+
+	void reglist_write(uint32_t desc, uint64_t v)
+	{
+		// REGLIST: descriptors address registers directly; A+D and NOP are ignored.
+		if (desc == 0xe || desc == 0xf || desc == 0xb)
+			return;
+		if (desc == 0x1)
+		{
+			regs[R_RGBAQ] = v;
+			return;
+		}
+		write_register(desc, v);
+	}
+};
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+pgs_gs *pgs_gs_create(const pgs_backend_ops *ops, void *backend, const pgs_gs_options *options, int *status)
+{
+	int dummy;
+	if (!status)
+		status = &dummy;
+	if (!ops || !backend || ops->abi_version != PGS_ABI_VERSION)
+	{
+		*status = PGS_ERROR_INVALID_ARGUMENT;
+		return nullptr;
+	}
+	if (options && options->vram_size && options->vram_size != PGS_VRAM_SIZE)
+	{
+		*status = PGS_ERROR_UNSUPPORTED;
+		return nullptr;
+	}
+	auto *gs = new (std::nothrow) pgs_gs();
+	if (!gs)
+	{
+		*status = PGS_ERROR_OUT_OF_MEMORY;
+		return nullptr;
+	}
+	gs->ops = ops;
+	gs->be = backend;
+	gs->regs[R_PRMODECONT] = 1;
+	// Power-on state: instance 0 does not match any real FRAME/ZBUF.
+	gs->instances[0].frame = 0x3full << 24;
+	gs->instances[0].zbuf = 0x7ull << 24;
+	gs->set_super_sampling(options ? options->super_sampling : 1, options ? options->ordered_super_sampling != 0 : true);
+	gs->reserve_buffers();
+	*status = gs->sticky_error;
+	if (gs->sticky_error)
+	{
+		delete gs;
+		return nullptr;
+	}
+	return gs;
+}
+
+void pgs_gs_destroy(pgs_gs *gs)
+{
+	delete gs;
+}
+
+int pgs_gs_gif_transfer(pgs_gs *gs, uint32_t path, const void *data, size_t size)
+{
+	if (!gs || (size & 15) || path > 3 || (size && !data))
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if (size == 0)
+		return PGS_OK;
+	gs->gif_transfer(path, static_cast<const uint64_t *>(data), size / 16);
+	return gs->sticky_error;
+}
+
+int pgs_gs_write_register(pgs_gs *gs, uint32_t addr, uint64_t payload)
+{
+	if (!gs || addr > 0x7f)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->write_register(addr, payload);
+	return gs->sticky_error;
+}
+
+int pgs_gs_flush(pgs_gs *gs)
+{
+	if (!gs)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->flush();
+	return gs->sticky_error;
+}
+
+int pgs_gs_read_vram(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst)
+{
+	if (!gs || !dst || offset + size > PGS_VRAM_SIZE)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->flush();
+	if (gs->sticky_error)
+		return gs->sticky_error;
+	return gs->ops->read_vram(gs->be, 0, offset, size, dst);
+}
+
+int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *src)
+{
+	if (!gs || !src || offset + size > PGS_VRAM_SIZE)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->flush();
+	return gs->ops->write_vram(gs->be, offset, size, src);
+}
+
+int pgs_gs_read_transfer_fifo(pgs_gs *gs, void *data, uint32_t num_128b_words)
+{
+	if (!gs || (!data && num_128b_words))
+		return PGS_ERROR_INVALID_ARGUMENT;
+	auto &x = gs->xfer;
+	uint32_t avail = x.fifo_size > x.fifo_offset ? x.fifo_size - x.fifo_offset : 0;
+	uint32_t n = std::min(avail, num_128b_words);
+	if (n)
+		memcpy(data, x.fifo.data() + 16ull * x.fifo_offset, 16ull * n);
+	if (n < num_128b_words)
+		memset(static_cast<uint8_t *>(data) + 16ull * n, 0, 16ull * (num_128b_words - n));
+	x.fifo_offset += n;
+	return PGS_OK;
+}
+
+int pgs_gs_consume_flush_stats(pgs_gs *gs, pgs_flush_stats *stats)
+{
+	if (!gs || !stats)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	*stats = gs->stats;
+	gs->stats = {};
+	return PGS_OK;
+}
+
+int pgs_gs_set_super_sampling_rate(pgs_gs *gs, uint32_t super_sampling, uint32_t ordered_grid)
+{
+	if (!gs)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->flush();
+	gs->set_super_sampling(super_sampling, ordered_grid != 0);
+	return gs->sticky_error;
+}
+}

@@ -1,0 +1,1616 @@
+// kernels.cuh -- sm_103a kernels of the GS backend.
+//
+//   setup_kernel     one thread per primitive: edge planes, reciprocal area,
+//                    attribute deltas, bounding box (triangle_setup.comp)
+//   bin_kernel       one thread per primitive: sets the primitive's bit in the
+//                    bitmask of every coarse tile it may touch, plus per-tile
+//                    super-sampling flags (binning.comp); the bitmask keeps
+//                    primitive order without any sort
+//   shade_kernel     one CTA per 8x8-pixel sub-tile of a coarse tile, one
+//                    thread per pixel sample; walks the tile's primitives in
+//                    order with the deferred-shading logic of ubershader.comp
+//   upload_kernel    host->local and local->local transfers into swizzled VRAM
+//   clut_kernel      CLUT instance load (clut_write.comp)
+//
+// All floating-point steps use explicit round-to-nearest intrinsics so that
+// no multiply-add is contracted; the build also passes -fmad=false.
+#pragma once
+
+#include "gs_defs.h"
+#include "pgs.h"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pgs
+{
+// ---------------------------------------------------------------------------
+// Device records.
+struct __align__(16) PrimSetup
+{
+	int32_t a[3];
+	float inv_area;
+	int32_t b[3];
+	float error_i;
+	int32_t c[3];
+	float error_j;
+	int32_t bb[4];
+	uint32_t z[4];
+};
+static_assert(sizeof(PrimSetup) == 80, "PrimSetup layout");
+
+struct __align__(16) TransformedAttr
+{
+	float stqf0[4];
+	float stqf1[4];
+	float stqf2[4];
+	uint32_t rgba0, rgba1, rgba2, padding;
+};
+static_assert(sizeof(TransformedAttr) == 64, "TransformedAttr layout");
+
+// Decoded framebuffer instance for the shading kernels.
+struct DevInstance
+{
+	uint32_t fb_base, fb_stride, fb_psm;
+	uint32_t zb_base, zb_psm; // zb_psm == 0xffffffff when not Z sensitive
+	int32_t base_x, base_y;
+	uint32_t tiles_w, tiles_h;
+	uint32_t rate_x_log2, rate_y_log2;
+	uint32_t preserve_samples;
+	uint32_t instance;
+	uint32_t prim_lo, prim_count; // primitive range of this dispatch
+	uint32_t mask_words;          // bitmask words per tile
+};
+
+struct PassParams
+{
+	const pgs_vertex_position *pos;
+	const pgs_vertex_attribute *attr;
+	pgs_primitive_attribute *prims;
+	const pgs_state_vector *states;
+	const pgs_texture_desc *textures;
+	PrimSetup *setup;
+	TransformedAttr *tattr;
+	uint32_t num_prims;
+	uint32_t num_states, num_textures;
+	uint32_t tile_size_log2;
+	uint32_t has_aa1, has_scanmsk, has_ss_reference;
+	uint32_t setup_rate_x_log2, setup_rate_y_log2;
+	uint32_t opaque_fbmask[8];
+	uint8_t *vram;
+	const uint16_t *clut;
+	const float *rcp_float_lut;
+	uint32_t *error_flags;
+	unsigned long long *fragment_counter;
+};
+
+// Per-tile flag bits written by bin_kernel.
+constexpr uint32_t TILE_NONEMPTY = 1u << 0;
+constexpr uint32_t TILE_REQ_SS = 1u << 1;
+constexpr uint32_t TILE_REQ_SS_ZW = 1u << 2;
+constexpr uint32_t TILE_HAS_ZW = 1u << 3;
+
+constexpr uint32_t ERROR_FLAG_TILE_OVERFLOW = 1u << 0;
+
+__constant__ uint8_t c_rcp_tab[256];
+
+// ---------------------------------------------------------------------------
+// Scalar helpers.
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float u2f(uint32_t u) { return __uint_as_float(u); }
+__device__ __forceinline__ uint32_t f2u(float f) { return __float_as_uint(f); }
+
+__device__ __forceinline__ int32_t idot3(const int32_t p[3], int32_t x, int32_t y)
+{
+	return int32_t(uint32_t(p[0]) * uint32_t(x) + uint32_t(p[1]) * uint32_t(y) + uint32_t(p[2]));
+}
+
+// Reciprocal of a 32-bit fixed-point area: table seed plus two Newton steps in
+// 32-bit fixed point, quantised to FP32 (rcp_fixed, math_utils.h:27-61).
+__device__ __forceinline__ float rcp_fixed(uint32_t b)
+{
+	int lz = __clz(b);
+	uint32_t nb = b << lz;
+	uint32_t rcp = uint32_t(c_rcp_tab[(nb >> 23) & 0xffu]) | 0x100u;
+	uint32_t f = (rcp * rcp) << 14;
+	uint32_t p = __umulhi(f, nb);
+	rcp = (rcp << 23) - p;
+	rcp <<= 1;
+	p = __umulhi(rcp, nb);
+	rcp = __umulhi(rcp, 0u - p);
+	rcp = (rcp + 64u) >> 7;
+	rcp -= 1u << 23;
+	rcp += uint32_t(127 - 32 + lz) << 23;
+	return u2f(rcp);
+}
+
+// Reciprocal by table seed + 4 Newton-Raphson steps (rcp_float, math_utils.h:65-101).
+__device__ __forceinline__ float rcp_float(float v, const float *lut)
+{
+	uint32_t u = f2u(v);
+	int e = int((u >> 23) & 0xffu);
+	if (e == 0)
+		return u2f(0x7f800000u);
+	int shifted = 127 - e;
+	float x = lut[(u >> 15) & 0xffu];
+	u = (u & ((1u << 23) - 1u)) | (127u << 23);
+	float a = u2f(u);
+	#pragma unroll
+	for (int it = 0; it < 4; it++)
+	{
+		float x2 = fmul(x, 2.0f);
+		float xs = fmul(x, x);
+		float xsa = fmul(xs, a);
+		x = fsub(x2, xsa);
+	}
+	return ldexpf(x, shifted);
+}
+
+__device__ __forceinline__ bool tie_break(int32_t ex, int32_t ey) { return ey > 0 || (ey == 0 && ex < 0); }
+
+__device__ __forceinline__ bool order_less(int32_t ax, int32_t ay, int32_t bx, int32_t by, uint32_t az, uint32_t bz)
+{
+	if (bz != az) return az < bz;
+	if (by != ay) return ay < by;
+	return ax < bx;
+}
+
+template <typename T>
+__device__ __forceinline__ void dswap(T &a, T &b) { T t = a; a = b; b = t; }
+
+// ---------------------------------------------------------------------------
+// K1: triangle setup.
+__global__ void __launch_bounds__(128) setup_kernel(PassParams P)
+{
+	uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
+	if (index >= P.num_prims)
+		return;
+
+	pgs_primitive_attribute pa = P.prims[index];
+	PrimSetup out;
+	TransformedAttr ta;
+	const int sry = int(P.setup_rate_y_log2);
+
+	int order0 = 0, order1 = 1, order2 = 2;
+	uint32_t st = pa.state;
+	bool parallelogram = (st >> STATE_BIT_PARALLELOGRAM) & 1;
+	bool perspective = (st >> STATE_BIT_PERSPECTIVE) & 1;
+	bool iip = (st >> STATE_BIT_IIP) & 1;
+	bool fix = (st >> STATE_BIT_FIX) & 1;
+	bool sprite = (st >> STATE_BIT_SPRITE) & 1;
+	bool line = (st >> STATE_BIT_LINE) & 1;
+	bool multisample = (st >> STATE_BIT_MULTISAMPLE) & 1;
+	uint32_t provoking = (st >> STATE_PARALLELOGRAM_PROVOKING_OFFSET) & 3u;
+	uint32_t opaque_fbmask = P.opaque_fbmask[(st >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u];
+
+	pgs_vertex_position v0 = P.pos[3 * index], v1 = P.pos[3 * index + 1], v2 = P.pos[3 * index + 2];
+	int32_t ax = v0.x, ay = v0.y, bx = v1.x, by = v1.y, cx = v2.x, cy = v2.y;
+	uint32_t za = v0.z, zb = v1.z, zc = v2.z;
+
+	if (line)
+	{
+		bool sax = (ax & 15) == 0, say = (ay & 15) == 0, sbx = (bx & 15) == 0, sby = (by & 15) == 0;
+		if ((sax || sbx) && bx > ax) { ax += 1; bx += 1; }
+		if ((say || sby) && by > ay) { ay += 1; by += 1; }
+	}
+
+	if ((!parallelogram || line) && !fix)
+	{
+		if (!line && !order_less(bx, by, cx, cy, zb, zc))
+		{
+			dswap(order1, order2); dswap(bx, cx); dswap(by, cy); dswap(zb, zc);
+		}
+		if (!order_less(ax, ay, bx, by, za, zb))
+		{
+			dswap(order0, order1); dswap(ax, bx); dswap(ay, by); dswap(za, zb);
+		}
+	}
+	else if (provoking == 1)
+	{
+		dswap(order0, order1); dswap(ax, bx); dswap(ay, by); dswap(za, zb);
+	}
+	else if (provoking == 2)
+	{
+		dswap(order0, order2); dswap(ax, cx); dswap(ay, cy); dswap(za, zc);
+	}
+
+	if (sprite)
+	{
+		cx = ax; cy = by;
+		by = ay;
+	}
+	else if (line)
+	{
+		int32_t abx = bx - ax, aby = by - ay;
+		if (abs(abx) >= abs(aby))
+		{
+			int32_t yd = -((abx > 0) - (abx < 0)) * 8;
+			if (multisample) yd *= 2;
+			cy = ay + yd; ay -= yd; by -= yd;
+			if (!multisample) { ay += 1; by += 1; }
+			cx = ax;
+		}
+		else
+		{
+			int32_t xd = ((aby > 0) - (aby < 0)) * 8;
+			if (multisample) xd *= 2;
+			cx = ax + xd; ax -= xd; bx -= xd;
+			if (!multisample) { ax += 1; bx += 1; }
+			cy = ay;
+		}
+	}
+
+	int32_t abx = bx - ax, aby = by - ay, acx = cx - ax, acy = cy - ay;
+	int64_t signed_area = int64_t(aby) * acx - int64_t(abx) * acy;
+	if (signed_area == 0)
+	{
+		out.bb[0] = 0; out.bb[1] = 0; out.bb[2] = -1; out.bb[3] = -1;
+		reinterpret_cast<int4 *>(&P.setup[index])[3] = make_int4(0, 0, -1, -1);
+		if (sry != 0)
+			P.prims[index].state = st | (1u << STATE_BIT_SNAP_ATTRIBUTE);
+		return;
+	}
+
+	uint32_t area;
+	bool flipped = signed_area < 0;
+	if (flipped)
+	{
+		area = uint32_t(0ull - uint64_t(signed_area));
+		dswap(abx, acx); dswap(aby, acy);
+		dswap(bx, cx); dswap(by, cy);
+		dswap(zb, zc);
+		dswap(order1, order2);
+	}
+	else
+		area = uint32_t(uint64_t(signed_area));
+
+	int32_t bcx = cx - bx, bcy = cy - by;
+	int32_t cax = -acx, cay = -acy;
+	int32_t dcdx = aby, dcdy = -abx;
+	int32_t dadx = bcy, dady = -bcx;
+	int32_t dbdx = cay, dbdy = -cax;
+	int64_t const_c = int64_t(-ax) * dcdx - int64_t(ay) * dcdy;
+	int64_t const_a = int64_t(-bx) * dadx - int64_t(by) * dady;
+	int64_t const_b = int64_t(-cx) * dbdx - int64_t(cy) * dbdy;
+	bool tba = tie_break(bcx, bcy), tbb = tie_break(cax, cay), tbc = tie_break(abx, aby);
+	int32_t err_a = !tba, err_b = !tbb, err_c = !tbc;
+	const_a -= err_a; const_b -= err_b; const_c -= err_c;
+	err_a += int32_t(uint64_t(const_a) & 1u);
+	err_b += int32_t(uint64_t(const_b) & 1u);
+	err_c += int32_t(uint64_t(const_c) & 1u);
+	int32_t flip_b = 0, flip_c = 0;
+	if (parallelogram)
+	{
+		int32_t tbo = 1 - int32_t(tbb) - int32_t(tbc);
+		flip_b = (tbo + err_b + err_a + 2) >> 1;
+		flip_c = (tbo + err_c + err_a + 2) >> 1;
+	}
+
+	float inv_area = rcp_fixed(area);
+	float inv_area_scaled = fmul(inv_area, 2.0f);
+	float error_i = fmul(__int2float_rn(err_b), inv_area);
+	float error_j = fmul(__int2float_rn(err_c), inv_area);
+
+	if (sprite) { zb = za; zc = za; }
+	else if (line) { zc = za; }
+	if (fix || sprite) { order0 = 0; order1 = 1; order2 = 2; }
+
+	pgs_vertex_attribute at0 = P.attr[3 * index + order0];
+	pgs_vertex_attribute at1 = P.attr[3 * index + order1];
+	pgs_vertex_attribute at2 = {};
+	if (!sprite && !line)
+		at2 = P.attr[3 * index + order2];
+
+	float s0[4], s1[4], s2[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+	if (perspective)
+	{
+		s0[0] = at0.s; s0[1] = at0.t; s0[2] = at0.q; s0[3] = at0.fog;
+		s1[0] = at1.s; s1[1] = at1.t; s1[2] = at1.q; s1[3] = at1.fog;
+		if (!sprite && !line) { s2[0] = at2.s; s2[1] = at2.t; s2[2] = at2.q; s2[3] = at2.fog; }
+	}
+	else
+	{
+		s0[0] = fmul(float(at0.u), 0.0625f); s0[1] = fmul(float(at0.v), 0.0625f); s0[2] = at0.q; s0[3] = at0.fog;
+		s1[0] = fmul(float(at1.u), 0.0625f); s1[1] = fmul(float(at1.v), 0.0625f); s1[2] = at1.q; s1[3] = at1.fog;
+		if (!sprite && !line)
+		{
+			s2[0] = fmul(float(at2.u), 0.0625f); s2[1] = fmul(float(at2.v), 0.0625f); s2[2] = at2.q; s2[3] = at2.fog;
+		}
+	}
+
+	if (sprite)
+	{
+		float o0x = s0[0], o0y = s0[1], o0z = s0[2], o0w = s0[3], o1x = s1[0], o1y = s1[1];
+		if (flipped)
+		{
+			s2[0] = o1x; s2[1] = o0y; s2[2] = o0z; s2[3] = o0w;
+			s1[0] = o0x; s1[1] = o1y; s1[2] = o0z; s1[3] = o0w;
+		}
+		else
+		{
+			s2[0] = o0x; s2[1] = o1y; s2[2] = o0z; s2[3] = o0w;
+			s1[0] = o1x; s1[1] = o0y; s1[2] = o0z; s1[3] = o0w;
+		}
+	}
+	else if (line)
+	{
+		s2[0] = s0[0]; s2[1] = s0[1]; s2[2] = s0[2]; s2[3] = s0[3];
+	}
+
+	if (perspective)
+	{
+		if (s0[2] < 0.0f)
+		{
+			s0[0] = -s0[0]; s0[1] = -s0[1]; s1[0] = -s1[0]; s1[1] = -s1[1]; s2[0] = -s2[0]; s2[1] = -s2[1];
+		}
+		s0[2] = fabsf(s0[2]); s1[2] = fabsf(s1[2]); s2[2] = fabsf(s2[2]);
+		uint32_t qexp = (f2u(fmaxf(fmaxf(s0[2], s1[2]), s2[2])) >> 23) & 0xffu;
+		s0[2] = u2f(f2u(s0[2]) & ~0xffu);
+		s1[2] = u2f(f2u(s1[2]) & ~0xffu);
+		s2[2] = u2f(f2u(s2[2]) & ~0xffu);
+		uint32_t sexp = (f2u(fmaxf(fmaxf(fabsf(s0[0]), fabsf(s1[0])), fabsf(s2[0]))) >> 23) & 0xffu;
+		uint32_t texp = (f2u(fmaxf(fmaxf(fabsf(s0[1]), fabsf(s1[1])), fabsf(s2[1]))) >> 23) & 0xffu;
+		uint32_t schop = min(9u + max(sexp, qexp) - sexp, 23u);
+		uint32_t tchop = min(9u + max(texp, qexp) - texp, 23u);
+		uint32_t smask = ~((1u << schop) - 1u), tmask = ~((1u << tchop) - 1u);
+		s0[0] = u2f(f2u(s0[0]) & smask); s1[0] = u2f(f2u(s1[0]) & smask); s2[0] = u2f(f2u(s2[0]) & smask);
+		s0[1] = u2f(f2u(s0[1]) & tmask); s1[1] = u2f(f2u(s1[1]) & tmask); s2[1] = u2f(f2u(s2[1]) & tmask);
+		bool needs_lod = (pa.tex2 & TEX2_FIXED_LOD_BIT) == 0;
+		if (!needs_lod && s0[2] == s1[2] && s0[2] == s2[2])
+		{
+			float inv_q = rcp_float(s0[2], P.rcp_float_lut);
+			s0[0] = fmul(s0[0], inv_q); s0[1] = fmul(s0[1], inv_q);
+			s1[0] = fmul(s1[0], inv_q); s1[1] = fmul(s1[1], inv_q);
+			s2[0] = fmul(s2[0], inv_q); s2[1] = fmul(s2[1], inv_q);
+			s0[2] = 1.0f; s1[2] = 1.0f; s2[2] = 1.0f;
+		}
+	}
+
+	float di[4], dj[4];
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		di[k] = fix ? 0.0f : fsub(s1[k], s0[k]);
+		dj[k] = fix ? 0.0f : fsub(s2[k], s0[k]);
+		ta.stqf0[k] = s0[k];
+		ta.stqf1[k] = di[k];
+		ta.stqf2[k] = dj[k];
+	}
+	if (iip && !sprite)
+	{
+		uint32_t r0 = at0.rgba, r1 = at1.rgba, r2 = at2.rgba;
+		if (fix) r1 = r0;
+		if (fix || line) r2 = r0;
+		ta.rgba0 = r0; ta.rgba1 = r1; ta.rgba2 = r2;
+	}
+	else
+	{
+		uint32_t flat = P.attr[3 * index].rgba;
+		ta.rgba0 = flat; ta.rgba1 = flat; ta.rgba2 = flat;
+	}
+	ta.padding = 0;
+
+	int32_t pa0 = dadx, pa1 = dady, pa2 = int32_t(uint32_t(uint64_t(const_a) >> 1));
+	int32_t pb0 = dbdx, pb1 = dbdy, pb2 = int32_t(uint32_t(uint64_t(const_b) >> 1));
+	int32_t pc0 = dcdx, pc1 = dcdy, pc2 = int32_t(uint32_t(uint64_t(const_c) >> 1));
+	uint32_t axw = (uint32_t(pa0) << 6) & ~1u;
+	axw |= uint32_t(parallelogram);
+	axw = (axw & ~(3u << 2)) | ((uint32_t(flip_b) & 3u) << 2);
+	axw = (axw & ~(3u << 4)) | ((uint32_t(flip_c) & 3u) << 4);
+
+	int32_t dx = parallelogram ? (bx + cx - ax) : cx;
+	int32_t dy = parallelogram ? (by + cy - ay) : cy;
+
+	int32_t di_r = 0, dj_r = 0;
+	if (sprite)
+	{
+		int32_t xd = dx - ax, yd = dy - ay;
+		if (xd > 0 && (xd & (xd - 1)) != 0) { di_r += pb0; dj_r += pc0; }
+		if (yd > 0 && (yd & (yd - 1)) != 0) { di_r += pb1; dj_r += pc1; }
+	}
+	else if (parallelogram && !perspective)
+	{
+		bool nearest = (pa.tex & TEX_SAMPLER_MAG_LINEAR_BIT) == 0;
+		bool npot_area = (area & (area - 1)) != 0;
+		if (nearest && npot_area)
+		{
+			int32_t d0x = int32_t(at0.u) - ax, d0y = int32_t(at0.v) - ay;
+			int32_t d1x = int32_t(at1.u) - bx, d1y = int32_t(at1.v) - by;
+			int32_t d2x = int32_t(at2.u) - cx, d2y = int32_t(at2.v) - cy;
+			if (d0x == d1x && d0y == d1y && d0x == d2x && d0y == d2y)
+			{
+				bool mis_x = (min(ax, dx) & 15) != 0, mis_y = (min(ay, dy) & 15) != 0;
+				float dudx = fadd(fmul(di[0], float(pb0)), fmul(dj[0], float(pc0)));
+				float dvdx = fadd(fmul(di[1], float(pb0)), fmul(dj[1], float(pc0)));
+				float dudy = fadd(fmul(di[0], float(pb1)), fmul(dj[0], float(pc1)));
+				float dvdy = fadd(fmul(di[1], float(pb1)), fmul(dj[1], float(pc1)));
+				bool adj_x = mis_x && ((dudx > 0.0f && dvdx == 0.0f) || (dvdx > 0.0f && dudx == 0.0f));
+				bool adj_y = mis_y && ((dudy > 0.0f && dvdy == 0.0f) || (dvdy > 0.0f && dudy == 0.0f));
+				if (adj_x) { di_r -= pb0; dj_r -= pc0; }
+				if (adj_y) { di_r -= pb1; dj_r -= pc1; }
+			}
+		}
+	}
+	float eighth = fmul(0.125f, inv_area_scaled);
+	error_i = fadd(error_i, fmul(__int2float_rn(di_r), eighth));
+	error_j = fadd(error_j, fmul(__int2float_rn(dj_r), eighth));
+
+	out.a[0] = int32_t(axw); out.a[1] = pa1; out.a[2] = pa2;
+	out.b[0] = pb0; out.b[1] = pb1; out.b[2] = pb2;
+	out.c[0] = pc0; out.c[1] = pc1; out.c[2] = pc2;
+	out.inv_area = inv_area_scaled;
+	out.error_i = error_i;
+	out.error_j = error_j;
+	out.z[0] = za;
+	out.z[1] = f2u(__uint2float_rn(zb - za));
+	out.z[2] = f2u(__uint2float_rn(zc - za));
+	out.z[3] = 0;
+
+	int32_t lox = min(min(ax, bx), min(cx, dx)), loy = min(min(ay, by), min(cy, dy));
+	int32_t hix = max(max(ax, bx), max(cx, dx)), hiy = max(max(ay, by), max(cy, dy));
+	lox = (lox + (15 >> sry)) >> 4;
+	loy = (loy + (15 >> sry)) >> 4;
+	hix = (hix - 1) >> 4;
+	hiy = (hiy - 1) >> 4;
+	if (multisample && !line) { lox -= 1; loy -= 1; hix += 1; hiy += 1; }
+	out.bb[0] = max(lox, int32_t(pa.bb[0]));
+	out.bb[1] = max(loy, int32_t(pa.bb[1]));
+	out.bb[2] = min(hix, int32_t(pa.bb[2]));
+	out.bb[3] = min(hiy, int32_t(pa.bb[3]));
+
+	uint32_t tex = pa.tex;
+	if (sprite && !perspective)
+	{
+		int32_t u0x = int32_t(at0.u) - ax, u0y = int32_t(at0.v) - ay;
+		int32_t u1x = int32_t(at1.u) - dx, u1y = int32_t(at1.v) - dy;
+		int32_t mnx = min(u0x, u1x), mny = min(u0y, u1y), mxx = max(u0x, u1x), mxy = max(u0y, u1y);
+		bool csx = (mnx & 15) == 8, csy = (mny & 15) == 8;
+		bool nsx = (mxx & 15) == 9, nsy = (mxy & 15) == 9;
+		int32_t ddx = abs(dx - ax), ddy = abs(dy - ay);
+		nsx = nsx && (ddx & (ddx - 1)) != 0;
+		nsy = nsy && (ddy & (ddy - 1)) != 0;
+		bool no_interp = (mxx - mnx) <= 1 && (mxy - mny) <= 1;
+		if ((nsx || csx) && (nsy || csy) && no_interp)
+			tex &= ~TEX_SAMPLER_MAG_LINEAR_BIT;
+	}
+
+	uint32_t new_state = st;
+	if (pa.fbmsk != opaque_fbmask && (new_state & (1u << STATE_BIT_OPAQUE)))
+		new_state &= ~(1u << STATE_BIT_OPAQUE);
+	if (sry != 0 && !sprite)
+	{
+		bool per_sample = multisample;
+		if (!per_sample && perspective)
+			per_sample = di[2] != 0.0f || dj[2] != 0.0f;
+		if (!per_sample)
+			per_sample = za != zb || zb != zc;
+		if (!per_sample && !line)
+			new_state |= 1u << STATE_BIT_SNAP_ATTRIBUTE;
+	}
+
+	P.setup[index] = out;
+	P.tattr[index] = ta;
+	P.prims[index].state = new_state;
+	P.prims[index].tex = tex;
+}
+
+// ---------------------------------------------------------------------------
+// Conservative tile test (intersect.h:24-81).
+__device__ __forceinline__ bool intersects_tile(const PrimSetup &s, int32_t lo0, int32_t lo1, int32_t hi0, int32_t hi1,
+                                                bool ms_tri)
+{
+	int32_t l0 = max(s.bb[0], lo0), l1 = max(s.bb[1], lo1);
+	int32_t h0 = min(s.bb[2], hi0), h1 = min(s.bb[3], hi1);
+	if (h0 < l0 || h1 < l1)
+		return false;
+	int32_t axw = s.a[0];
+	bool par = (axw & 1) != 0;
+	int32_t off_b = int32_t((uint32_t(axw) >> 2) & 3u) - 1;
+	int32_t off_c = int32_t((uint32_t(axw) >> 4) & 3u) - 1;
+	int32_t A[3] = { axw >> 6, s.a[1], s.a[2] };
+	l0 <<= 3; l1 <<= 3;
+	h0 = (h0 << 3) | 7; h1 = (h1 << 3) | 7;
+	int32_t da = idot3(A, A[0] >= 0 ? h0 : l0, A[1] >= 0 ? h1 : l1);
+	int32_t db = idot3(s.b, s.b[0] >= 0 ? h0 : l0, s.b[1] >= 0 ? h1 : l1);
+	int32_t dc = idot3(s.c, s.c[0] >= 0 ? h0 : l0, s.c[1] >= 0 ? h1 : l1);
+	if (ms_tri && !par)
+	{
+		da += 8 * max(abs(A[0]), abs(A[1]));
+		db += 8 * max(abs(s.b[0]), abs(s.b[1]));
+		dc += 8 * max(abs(s.c[0]), abs(s.c[1]));
+	}
+	bool ok = da >= 0 && db >= 0 && dc >= 0;
+	if (par && !ok)
+	{
+		da = idot3(A, A[0] >= 0 ? h0 : l0, A[1] >= 0 ? h1 : l1);
+		db = idot3(s.b, -s.c[0] >= 0 ? h0 : l0, -s.c[1] >= 0 ? h1 : l1);
+		dc = idot3(s.c, -s.b[0] >= 0 ? h0 : l0, -s.b[1] >= 0 ? h1 : l1);
+		db += da + off_b;
+		dc += da + off_c;
+		da = idot3(A, A[0] >= 0 ? l0 : h0, A[1] >= 0 ? l1 : h1);
+		ok = (-1 >= da) && db >= 0 && dc >= 0;
+	}
+	return ok;
+}
+
+// ---------------------------------------------------------------------------
+// K2: binning into per-tile primitive bitmasks.
+__global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, uint32_t *tile_masks, uint32_t *tile_flags)
+{
+	uint32_t local = blockIdx.x * blockDim.x + threadIdx.x;
+	if (local >= I.prim_count)
+		return;
+	uint32_t p = I.prim_lo + local;
+	pgs_primitive_attribute pa = P.prims[p];
+	if (((pa.state >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u) != I.instance)
+		return;
+	const PrimSetup s = P.setup[p];
+	if (s.bb[2] < s.bb[0] || s.bb[3] < s.bb[1])
+		return;
+
+	int ts = int(P.tile_size_log2);
+	int32_t tx0 = (s.bb[0] - I.base_x) >> ts, ty0 = (s.bb[1] - I.base_y) >> ts;
+	int32_t tx1 = (s.bb[2] - I.base_x) >> ts, ty1 = (s.bb[3] - I.base_y) >> ts;
+	tx0 = max(tx0, 0); ty0 = max(ty0, 0);
+	tx1 = min(tx1, int32_t(I.tiles_w) - 1); ty1 = min(ty1, int32_t(I.tiles_h) - 1);
+
+	bool ms_tri = ((pa.state >> STATE_BIT_MULTISAMPLE) & 1) && !((pa.state >> STATE_BIT_LINE) & 1);
+	uint32_t flags = TILE_NONEMPTY;
+	if (I.rate_y_log2 != 0)
+	{
+		const uint32_t full_mask = (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_Z_TEST) | (1u << STATE_BIT_OPAQUE);
+		const uint32_t color_mask = (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_OPAQUE);
+		if ((pa.state & full_mask) != color_mask) flags |= TILE_REQ_SS_ZW;
+		if ((pa.state & color_mask) != color_mask) flags |= TILE_REQ_SS;
+		if (pa.state & (1u << STATE_BIT_Z_WRITE)) flags |= TILE_HAS_ZW;
+		if (pa.tex & TEX_PER_SAMPLE_BIT) flags |= TILE_REQ_SS;
+	}
+	uint32_t word = local >> 5, bit = 1u << (local & 31u);
+	for (int32_t ty = ty0; ty <= ty1; ty++)
+	{
+		for (int32_t tx = tx0; tx <= tx1; tx++)
+		{
+			int32_t lo0 = I.base_x + (tx << ts), lo1 = I.base_y + (ty << ts);
+			if (intersects_tile(s, lo0, lo1, lo0 + (1 << ts) - 1, lo1 + (1 << ts) - 1, ms_tri))
+			{
+				uint32_t tile = uint32_t(ty) * I.tiles_w + uint32_t(tx);
+				atomicOr(&tile_masks[size_t(tile) * I.mask_words + word], bit);
+				if ((tile_flags[tile] & flags) != flags)
+					atomicOr(&tile_flags[tile], flags);
+			}
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------
+// K3: shading.
+struct Request
+{
+	int coverage;
+	bool z_test, z_write, multisample, perspective, z_greater;
+	uint32_t z, state;
+	float i, j;
+};
+
+__device__ __forceinline__ float unorm8(uint32_t c, int ch) { return __fdiv_rn(float((c >> (8 * ch)) & 0xffu), 255.0f); }
+
+__device__ __forceinline__ uint32_t pack_unorm(float r, float g, float b, float a)
+{
+	float v[4] = { r, g, b, a };
+	uint32_t out = 0;
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		float x = fminf(fmaxf(v[k], 0.0f), 1.0f);
+		out |= uint32_t(rintf(fmul(x, 255.0f))) << (8 * k);
+	}
+	return out;
+}
+
+__device__ __forceinline__ uint32_t expand16(uint32_t c)
+{
+	uint32_t r = (c & 0x1fu) << 3, g = ((c >> 5) & 0x1fu) << 3, b = ((c >> 10) & 0x1fu) << 3;
+	return r | (g << 8) | (b << 16) | ((c & 0x8000u) ? 0x80000000u : 0u);
+}
+
+struct ShadeCtx
+{
+	const PassParams *P;
+	const DevInstance *I;
+	bool ss;
+	int dim;          // sampling rate y log2 when super-sampled, else 0
+	int32_t snap_mask;
+	bool zs;
+	uint32_t fb_psm, zb_psm;
+};
+
+__device__ __forceinline__ uint32_t clut_color(const PassParams &P, const pgs_texture_desc &t, uint32_t index)
+{
+	uint32_t bi = t.csa * 16u + index;
+	bool c16 = t.cpsm == PSMCT16 || t.cpsm == PSMCT16S;
+	if (t.psm == PSMT8 || t.psm == PSMT8H)
+	{
+		uint32_t bank = min(bi >> 4, c16 ? 31u : 15u);
+		bi = bank * 16u + (bi & 15u);
+	}
+	bi = min(bi, c16 ? 511u : 255u);
+	const uint16_t *cl = P.clut + size_t(t.clut_instance % PGS_CLUT_INSTANCES) * 512u;
+	if (c16)
+		return rgba16_to_rgba32(__ldg(cl + bi), t.aem, t.ta0, t.ta1);
+	return uint32_t(__ldg(cl + bi)) | (uint32_t(__ldg(cl + bi + 256u)) << 16);
+}
+
+__device__ __forceinline__ uint32_t fetch_texel(const PassParams &P, const pgs_texture_desc &t, int32_t x, int32_t y)
+{
+	uint32_t a = swizzle_address(uint32_t(x), uint32_t(y), t.tbp0, t.tbw, t.psm);
+	const uint8_t *v = P.vram;
+	switch (t.psm)
+	{
+	case PSMCT24: case PSMZ24:
+		return rgb24_to_rgba32(__ldg(reinterpret_cast<const uint32_t *>(v) + a), t.aem, t.ta0);
+	case PSMCT16: case PSMCT16S: case PSMZ16: case PSMZ16S:
+		return rgba16_to_rgba32(__ldg(reinterpret_cast<const uint16_t *>(v) + a), t.aem, t.ta0, t.ta1);
+	case PSMT8: return clut_color(P, t, __ldg(v + a));
+	case PSMT8H: return clut_color(P, t, __ldg(v + 4u * a + 3u));
+	case PSMT4: return clut_color(P, t, (uint32_t(__ldg(v + (a >> 1))) >> ((a & 1u) * 4u)) & 15u);
+	case PSMT4HL: return clut_color(P, t, (__ldg(reinterpret_cast<const uint32_t *>(v) + a) >> 24) & 15u);
+	case PSMT4HH: return clut_color(P, t, __ldg(reinterpret_cast<const uint32_t *>(v) + a) >> 28);
+	default: return __ldg(reinterpret_cast<const uint32_t *>(v) + a);
+	}
+}
+
+__device__ __forceinline__ int32_t wrap_coord(int32_t v, uint32_t mode, uint32_t size_log2, uint32_t lo, uint32_t hi)
+{
+	int32_t size = 1 << size_log2;
+	switch (mode)
+	{
+	case WRAP_REPEAT: return v & (size - 1);
+	case WRAP_CLAMP: return min(max(v, 0), size - 1);
+	case WRAP_REGION_CLAMP: return min(max(v, int32_t(lo)), int32_t(hi));
+	default: return int32_t(((uint32_t(v) & uint32_t(size - 1)) & lo) | hi);
+	}
+}
+
+// Texture sample at LOD 0 with exact integer filtering.
+__device__ void sample_texture(const PassParams &P, uint32_t tex_word, float u, float v, bool perspective, float out[4])
+{
+	const pgs_texture_desc t = P.textures[min(tex_word & TEX_TEXTURE_INDEX_MASK, P.num_textures - 1u)];
+	bool clamp_s = (tex_word & TEX_SAMPLER_CLAMP_S_BIT) != 0;
+	bool clamp_t = (tex_word & TEX_SAMPLER_CLAMP_T_BIT) != 0;
+	bool linear = (tex_word & TEX_SAMPLER_MAG_LINEAR_BIT) != 0;
+	float w = float(1u << t.tw_log2), h = float(1u << t.th_log2);
+	float uu = perspective ? fmul(u, w) : u;
+	float vv = perspective ? fmul(v, h) : v;
+	if (clamp_s)
+	{
+		float lo = t.wms == WRAP_REGION_CLAMP ? float(t.minu) : 0.0f;
+		float hi = t.wms == WRAP_REGION_CLAMP ? float(t.maxu) : fsub(w, 1.0f);
+		uu = fminf(fmaxf(uu, fadd(floorf(lo), 0.5f)), fadd(floorf(hi), 0.5f));
+	}
+	if (clamp_t)
+	{
+		float lo = t.wmt == WRAP_REGION_CLAMP ? float(t.minv) : 0.0f;
+		float hi = t.wmt == WRAP_REGION_CLAMP ? float(t.maxv) : fsub(h, 1.0f);
+		vv = fminf(fmaxf(vv, fadd(floorf(lo), 0.5f)), fadd(floorf(hi), 0.5f));
+	}
+	int32_t ku = int32_t(floorf(fadd(fmul(uu, 16.0f), 1.0f / 64.0f)));
+	int32_t kv = int32_t(floorf(fadd(fmul(vv, 16.0f), 1.0f / 64.0f)));
+	if (!linear)
+	{
+		int32_t x = wrap_coord(ku >> 4, t.wms, t.tw_log2, t.minu, t.maxu);
+		int32_t y = wrap_coord(kv >> 4, t.wmt, t.th_log2, t.minv, t.maxv);
+		uint32_t c = fetch_texel(P, t, x, y);
+		#pragma unroll
+		for (int k = 0; k < 4; k++)
+			out[k] = float((c >> (8 * k)) & 0xffu);
+		return;
+	}
+	int32_t bu = ku - 8, bv = kv - 8;
+	int32_t x0 = bu >> 4, y0 = bv >> 4;
+	uint32_t fx = uint32_t(bu) & 15u, fy = uint32_t(bv) & 15u;
+	int32_t xs0 = wrap_coord(x0, t.wms, t.tw_log2, t.minu, t.maxu);
+	int32_t xs1 = wrap_coord(x0 + 1, t.wms, t.tw_log2, t.minu, t.maxu);
+	int32_t ys0 = wrap_coord(y0, t.wmt, t.th_log2, t.minv, t.maxv);
+	int32_t ys1 = wrap_coord(y0 + 1, t.wmt, t.th_log2, t.minv, t.maxv);
+	uint32_t w00 = (16u - fx) * (16u - fy), w10 = fx * (16u - fy), w01 = (16u - fx) * fy, w11 = fx * fy;
+	uint32_t c00 = fetch_texel(P, t, xs0, ys0);
+	uint32_t c10 = w10 ? fetch_texel(P, t, xs1, ys0) : 0u;
+	uint32_t c01 = w01 ? fetch_texel(P, t, xs0, ys1) : 0u;
+	uint32_t c11 = w11 ? fetch_texel(P, t, xs1, ys1) : 0u;
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		int sh = 8 * k;
+		uint32_t acc = w00 * ((c00 >> sh) & 0xffu) + w10 * ((c10 >> sh) & 0xffu) + w01 * ((c01 >> sh) & 0xffu) +
+		               w11 * ((c11 >> sh) & 0xffu);
+		uint32_t q = acc >> 8, r = acc & 0xffu;
+		if (r > 128u || (r == 128u && (q & 1u)))
+			q++;
+		out[k] = float(q);
+	}
+}
+
+__device__ __forceinline__ float interp(float c0, float d1, float d2, float i, float j)
+{
+	// c0 + d1 * i + d2 * j, left to right, one rounding per operation.
+	return fadd(fadd(c0, fmul(d1, i)), fmul(d2, j));
+}
+
+__device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r, uint32_t combiner, float cc[4])
+{
+	const PassParams &P = *C.P;
+	const TransformedAttr a = P.tattr[pi];
+	float col[4];
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		float c0 = unorm8(a.rgba0, k), c1 = unorm8(a.rgba1, k), c2 = unorm8(a.rgba2, k);
+		float t = interp(c0, fsub(c1, c0), fsub(c2, c0), r.i, r.j);
+		col[k] = floorf(fadd(fmul(255.0f, t), 1.0f / 256.0f));
+	}
+	bool fog = (combiner & COMBINER_FOG_BIT) != 0, tcc = (combiner & COMBINER_TCC_BIT) != 0;
+	bool tme = (combiner & COMBINER_TME_BIT) != 0;
+	uint32_t mode = combiner & COMBINER_MODE_MASK;
+	if (tme)
+	{
+		float s = interp(a.stqf0[0], a.stqf1[0], a.stqf2[0], r.i, r.j);
+		float t = interp(a.stqf0[1], a.stqf1[1], a.stqf2[1], r.i, r.j);
+		float q = interp(a.stqf0[2], a.stqf1[2], a.stqf2[2], r.i, r.j);
+		if (r.perspective && q != 1.0f)
+		{
+			s = __fdiv_rn(s, q);
+			t = __fdiv_rn(t, q);
+		}
+		s = fminf(fmaxf(s, -2047.0f), 2047.0f);
+		t = fminf(fmaxf(t, -2047.0f), 2047.0f);
+		float tx[4];
+		sample_texture(P, P.prims[pi].tex, s, t, r.perspective, tx);
+		if (mode == COMBINER_DECAL)
+		{
+			cc[0] = tx[0]; cc[1] = tx[1]; cc[2] = tx[2]; cc[3] = tcc ? tx[3] : col[3];
+		}
+		else
+		{
+			#pragma unroll
+			for (int k = 0; k < 4; k++)
+				cc[k] = fminf(fmaxf(floorf(fmul(fmul(col[k], tx[k]), 1.0f / 128.0f)), 0.0f), 255.0f);
+			if (mode == COMBINER_MODULATE)
+			{
+				if (!tcc) cc[3] = col[3];
+			}
+			else
+			{
+				cc[0] = fadd(cc[0], col[3]); cc[1] = fadd(cc[1], col[3]); cc[2] = fadd(cc[2], col[3]);
+				if (mode == COMBINER_HIGHLIGHT)
+					cc[3] = tcc ? fadd(tx[3], col[3]) : col[3];
+				else
+					cc[3] = tcc ? tx[3] : col[3];
+				#pragma unroll
+				for (int k = 0; k < 4; k++)
+					cc[k] = fminf(fmaxf(cc[k], 0.0f), 255.0f);
+			}
+		}
+	}
+	else
+	{
+		cc[0] = col[0]; cc[1] = col[1]; cc[2] = col[2]; cc[3] = col[3];
+	}
+	if (fog)
+	{
+		float f = rintf(interp(a.stqf0[3], a.stqf1[3], a.stqf2[3], r.i, r.j));
+		uint32_t fc = P.prims[pi].fogcol;
+		#pragma unroll
+		for (int k = 0; k < 3; k++)
+		{
+			float fcol = fmul(unorm8(fc, k), 255.0f);
+			float d = fmul(fmul(fsub(cc[k], fcol), f), 1.0f / 256.0f);
+			cc[k] = floorf(fadd(fadd(fcol, d), 0.5f));
+		}
+	}
+}
+
+struct SampleState
+{
+	uint32_t color, depth;
+	bool color_dirty, depth_dirty;
+	int32_t hx, hy;
+	Request pending;
+	uint32_t pending_prim;
+};
+
+__device__ void shade_resolve(const ShadeCtx &C, SampleState &S)
+{
+	const PassParams &P = *C.P;
+	const Request &r = S.pending;
+	uint32_t pi = S.pending_prim;
+	const pgs_state_vector sv = P.states[min(r.state, P.num_states - 1u)];
+	if (C.zs && r.z_test)
+	{
+		bool pass = r.z_greater ? r.z > S.depth : r.z >= S.depth;
+		if (!pass)
+			return;
+	}
+	float cc[4];
+	combined_color(C, pi, r, sv.combiner, cc);
+	float fbc[4];
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+		fbc[k] = roundf(fmul(unorm8(S.color, k), 255.0f));
+
+	bool write_fb = true, write_zb = true, write_alpha = true;
+	const pgs_primitive_attribute &pa = P.prims[pi];
+	uint32_t bm = sv.blend_mode;
+	bool abe = (bm & BLEND_MODE_ABE_BIT) != 0;
+	bool fb24 = psm_is_24bit(C.fb_psm), fb32 = psm_is_32bit(C.fb_psm), fb16 = psm_is_16bit(C.fb_psm);
+	uint32_t alpha_word = pa.alpha;
+
+	if (P.has_aa1)
+	{
+		bool use_cov = (cc[3] == 128.0f || !abe) && r.multisample;
+		if (use_cov)
+			cc[3] = float(r.coverage);
+		if (r.multisample)
+			abe = true;
+	}
+
+	if (bm & BLEND_MODE_ATE_BIT)
+	{
+		float aref = float(alpha_word & 0xffu);
+		float al = cc[3];
+		bool pass;
+		switch ((bm >> BLEND_MODE_ATE_MODE_OFFSET) & 7u)
+		{
+		case ATST_NEVER: pass = false; break;
+		case ATST_LESS: pass = al < aref; break;
+		case ATST_LEQUAL: pass = al <= aref; break;
+		case ATST_EQUAL: pass = al == aref; break;
+		case ATST_GEQUAL: pass = al >= aref; break;
+		case ATST_GREATER: pass = al > aref; break;
+		case ATST_NOTEQUAL: pass = al != aref; break;
+		default: pass = true; break;
+		}
+		if (!pass)
+		{
+			switch ((bm >> BLEND_MODE_AFAIL_MODE_OFFSET) & 3u)
+			{
+			case AFAIL_KEEP: return;
+			case AFAIL_FB_ONLY: write_zb = false; break;
+			case AFAIL_ZB_ONLY: write_fb = false; write_alpha = false; break;
+			default: if (fb32) write_alpha = false; write_zb = false; break;
+			}
+		}
+	}
+
+	if (!fb24 && (bm & BLEND_MODE_DATE_BIT))
+	{
+		uint32_t bit = fbc[3] >= 128.0f ? 1u : 0u;
+		if (((bm & BLEND_MODE_DATM_BIT) ? 1u : 0u) != bit)
+			return;
+	}
+
+	if ((bm & BLEND_MODE_PABE_BIT) && cc[3] < 128.0f)
+		abe = false;
+
+	float bl[4] = { cc[0], cc[1], cc[2], cc[3] };
+	if (abe)
+	{
+		uint32_t am = (bm >> BLEND_MODE_A_MODE_OFFSET) & 3u, bmo = (bm >> BLEND_MODE_B_MODE_OFFSET) & 3u;
+		uint32_t cm = (bm >> BLEND_MODE_C_MODE_OFFSET) & 3u, dm = (bm >> BLEND_MODE_D_MODE_OFFSET) & 3u;
+		float Cf = 0.0f;
+		if (cm == BLEND_ALPHA_SOURCE) Cf = cc[3];
+		else if (cm == BLEND_ALPHA_DEST) Cf = fb24 ? 128.0f : fbc[3];
+		else if (cm == BLEND_ALPHA_FIX) Cf = float((alpha_word >> ALPHA_AFIX_OFFSET) & 0xffu);
+		#pragma unroll
+		for (int k = 0; k < 3; k++)
+		{
+			float A = am == 0 ? cc[k] : (am == 1 ? fbc[k] : 0.0f);
+			float B = bmo == 0 ? cc[k] : (bmo == 1 ? fbc[k] : 0.0f);
+			float D = dm == 0 ? cc[k] : (dm == 1 ? fbc[k] : 0.0f);
+			bl[k] = fadd(floorf(fmul(fmul(fsub(A, B), Cf), 1.0f / 128.0f)), D);
+		}
+	}
+
+	if (bm & BLEND_MODE_DTHE_BIT)
+	{
+		int px = (S.hx >> C.dim) & 3, py = (S.hy >> C.dim) & 3;
+		int bit = ((py * 4 + px) * 4) & 31;
+		uint32_t dimx = py < 2 ? sv.dimx_lo : sv.dimx_hi;
+		int32_t dv = int32_t(((dimx >> bit) & 7u) << 29) >> 29;
+		float fdv = float(dv);
+		bl[0] = fadd(bl[0], fdv); bl[1] = fadd(bl[1], fdv); bl[2] = fadd(bl[2], fdv);
+	}
+
+	if (fb24) write_alpha = false;
+	if (!write_alpha) bl[3] = fbc[3];
+	if (!write_fb) { bl[0] = fbc[0]; bl[1] = fbc[1]; bl[2] = fbc[2]; }
+
+	float o[4];
+	bool colclamp = (bm & BLEND_MODE_COLCLAMP_BIT) != 0;
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		if (!colclamp)
+		{
+			float x = fmul(bl[k], 1.0f / 256.0f);
+			o[k] = fmul(fsub(x, floorf(x)), 256.0f / 255.0f);
+		}
+		else
+			o[k] = fmul(bl[k], 1.0f / 255.0f);
+	}
+	uint32_t packed = pack_unorm(o[0], o[1], o[2], o[3]);
+	if ((bm & BLEND_MODE_FB_ALPHA_BIT) && write_alpha)
+		packed |= 0x80000000u;
+
+	uint32_t mask = pa.fbmsk;
+	if (mask != 0xffffffffu && (write_fb || write_alpha))
+	{
+		S.color = mask ? ((packed & ~mask) | (S.color & mask)) : packed;
+		if (fb16)
+			S.color &= 0x80f8f8f8u;
+		S.color_dirty = true;
+	}
+	if (C.zs && write_zb && r.z_write)
+	{
+		S.depth = r.z;
+		S.depth_dirty = true;
+	}
+}
+
+__device__ __forceinline__ int evaluate_coverage(const PrimSetup &s, int32_t cx, int32_t cy, float &i, float &j, bool ms,
+                                                 bool line, int dim)
+{
+	int32_t sx = cx >> dim, sy = cy >> dim;
+	if (!(sx >= s.bb[0] && sy >= s.bb[1] && s.bb[2] >= sx && s.bb[3] >= sy))
+		return 0;
+	int32_t axw = s.a[0];
+	bool par = (axw & 1) != 0;
+	int32_t off_b = int32_t((uint32_t(axw) >> 2) & 3u) - 1;
+	int32_t off_c = int32_t((uint32_t(axw) >> 4) & 3u) - 1;
+	int32_t A[3] = { axw >> 6, s.a[1], s.a[2] };
+	int32_t px = cx << (3 - dim), py = cy << (3 - dim);
+	int32_t ea = idot3(A, px, py), eb = idot3(s.b, px, py), ec = idot3(s.c, px, py);
+	i = fadd(fmul(__int2float_rn(eb), s.inv_area), s.error_i);
+	j = fadd(fmul(__int2float_rn(ec), s.inv_area), s.error_j);
+	bool ba = ea >= 0, bb = eb >= 0, bc = ec >= 0;
+	if (par && ea < 0)
+	{
+		eb += ea + off_b;
+		ec += ea + off_c;
+		ea = 0;
+	}
+	bool center = ea >= 0 && eb >= 0 && ec >= 0;
+	if (ms && line)
+		return center ? int(fmaxf(0.0f, fsub(128.0f, fmul(256.0f, fabsf(fsub(0.5f, j)))))) : 0;
+	if (center)
+		return 0x80;
+	if (ms && !par && (int(ba) + int(bb) + int(bc) == 2))
+	{
+		float neg;
+		int32_t md;
+		if (!ba)
+		{
+			md = max(abs(s.b[0] + s.c[0]), abs(s.b[1] + s.c[1]));
+			neg = fsub(fadd(i, j), 1.0f);
+		}
+		else if (!bb)
+		{
+			md = max(abs(s.b[0]), abs(s.b[1]));
+			neg = -i;
+		}
+		else
+		{
+			md = max(abs(s.c[0]), abs(s.c[1]));
+			neg = -j;
+		}
+		float scaled = fmul(float(md), s.inv_area);
+		float fc = fsub(8.0f, __fdiv_rn(neg, scaled));
+		return int(fminf(fmaxf(fmul(16.0f, fc), 0.0f), 127.0f));
+	}
+	return 0;
+}
+
+__device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetup &s, uint32_t st, const SampleState &S,
+                                               bool &opaque)
+{
+	const PassParams &P = *C.P;
+	Request r;
+	opaque = (st >> STATE_BIT_OPAQUE) & 1;
+	r.z_test = C.zs && ((st >> STATE_BIT_Z_TEST) & 1);
+	r.z_write = C.zs && ((st >> STATE_BIT_Z_WRITE) & 1);
+	r.z_greater = C.zs && ((st >> STATE_BIT_Z_TEST_GREATER) & 1);
+	r.state = st & STATE_INDEX_MASK;
+	r.multisample = P.has_aa1 && ((st >> STATE_BIT_MULTISAMPLE) & 1);
+	r.perspective = (st >> STATE_BIT_PERSPECTIVE) & 1;
+	int32_t rx = S.hx, ry = S.hy;
+	if (C.ss && (st & (1u << STATE_BIT_SNAP_RASTER)))
+	{
+		rx &= C.snap_mask;
+		ry &= C.snap_mask;
+	}
+	float i = 0.0f, j = 0.0f;
+	r.coverage = evaluate_coverage(s, rx, ry, i, j, r.multisample, (st >> STATE_BIT_LINE) & 1, C.dim);
+	if (P.has_scanmsk)
+	{
+		int32_t sy = S.hy;
+		if (st & (1u << STATE_BIT_SPRITE))
+			sy >>= C.dim;
+		if ((sy & 1) == 0) { if ((st >> STATE_BIT_SCANMSK_EVEN) & 1) r.coverage = 0; }
+		else if ((st >> STATE_BIT_SCANMSK_ODD) & 1) r.coverage = 0;
+	}
+	if (C.zs && r.multisample && r.coverage < 0x80)
+		r.z_write = false;
+	uint32_t z = s.z[0];
+	float zf = rintf(fadd(fmul(u2f(s.z[1]), i), fmul(u2f(s.z[2]), j)));
+	zf = fminf(fmaxf(zf, 0.0f), 4294967040.0f);
+	uint32_t dz = __float2uint_rz(zf);
+	dz = min(dz, 0xffffffffu - z);
+	z += dz;
+	if (C.zs && psm_is_16bit(C.zb_psm)) z = min(z, 0xffffu);
+	else if (C.zs && psm_is_24bit(C.zb_psm)) z = min(z, 0xffffffu);
+	if (C.ss && r.coverage != 0)
+	{
+		uint32_t snap = st & ((1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE));
+		if (snap == (1u << STATE_BIT_SNAP_ATTRIBUTE))
+		{
+			int32_t qx = (S.hx & C.snap_mask) << (3 - C.dim), qy = (S.hy & C.snap_mask) << (3 - C.dim);
+			i = fadd(fmul(__int2float_rn(idot3(s.b, qx, qy)), s.inv_area), s.error_i);
+			j = fadd(fmul(__int2float_rn(idot3(s.c, qx, qy)), s.inv_area), s.error_j);
+		}
+	}
+	r.z = z;
+	r.i = i;
+	r.j = j;
+	return r;
+}
+
+// Maximum primitives staged per list chunk in shared memory.
+constexpr int SHADE_CHUNK = 256;
+
+// Sample position within its pixel for sample s (32-wide subgroup layout of
+// ubershader.comp get_tile_info).
+__device__ __forceinline__ void sample_offset(uint32_t s, uint32_t xl, uint32_t yl, int32_t &ox, int32_t &oy)
+{
+	uint32_t b0 = s & 1u, b1 = (s >> 1) & 1u, b2 = (s >> 2) & 1u, b3 = (s >> 3) & 1u;
+	if (xl == yl)
+	{
+		ox = int32_t(b1 | (b3 << 1));
+		oy = int32_t(b0 | (b2 << 1));
+	}
+	else
+	{
+		int32_t ly = int32_t(b0 | (xl >= 1 ? (b2 << 1) : 0u));
+		int32_t lx = int32_t(xl >= 1 ? b1 : 0u);
+		ox = (lx << 1) + (ly & 1);
+		oy = ly;
+	}
+}
+
+// One CTA per 8x8-pixel sub-tile of a coarse tile; NS samples per pixel, one
+// thread per sample.  SS selects the super-sampled path; tiles whose flags
+// select the other path exit immediately.
+template <int NS, bool SS>
+__global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstance I, const uint32_t *tile_masks,
+                                                        const uint32_t *tile_flags)
+{
+	__shared__ uint32_t s_list[SHADE_CHUNK];
+	__shared__ int s_count;
+	__shared__ uint32_t s_word;
+
+	const uint32_t subtiles_per_tile_log2 = 2u * (P.tile_size_log2 - 3u);
+	uint32_t tile = blockIdx.x >> subtiles_per_tile_log2;
+	uint32_t sub = blockIdx.x & ((1u << subtiles_per_tile_log2) - 1u);
+	if (tile >= I.tiles_w * I.tiles_h)
+		return;
+	uint32_t flags = tile_flags[tile];
+	if (!(flags & TILE_NONEMPTY))
+		return;
+	bool req = (flags & TILE_REQ_SS) || ((flags & TILE_REQ_SS_ZW) && (flags & TILE_HAS_ZW));
+	bool ss_tile = I.rate_y_log2 != 0 && req;
+	if (ss_tile != SS)
+		return;
+
+	ShadeCtx C;
+	C.P = &P;
+	C.I = &I;
+	C.ss = SS;
+	C.dim = SS ? int(I.rate_y_log2) : 0;
+	C.snap_mask = -(1 << I.rate_y_log2);
+	C.zs = I.zb_psm != 0xffffffffu;
+	C.fb_psm = I.fb_psm;
+	C.zb_psm = I.zb_psm;
+
+	uint32_t tx = tile % I.tiles_w, ty = tile / I.tiles_w;
+	uint32_t sub_per_row = 1u << (P.tile_size_log2 - 3u);
+	int32_t sub_x = I.base_x + int32_t(tx << P.tile_size_log2) + int32_t((sub % sub_per_row) * 8u);
+	int32_t sub_y = I.base_y + int32_t(ty << P.tile_size_log2) + int32_t((sub / sub_per_row) * 8u);
+
+	uint32_t t = threadIdx.x;
+	uint32_t sample = t % NS;
+	uint32_t pix = t / NS;
+	// Pixel order inside the 8x8 sub-tile: x from bits 0,2,4 and y from bits 1,3,5
+	// so that a warp's pixels form a compact block.
+	int32_t lx = int32_t((pix & 1u) | ((pix >> 1) & 2u) | ((pix >> 2) & 4u));
+	int32_t ly = int32_t(((pix >> 1) & 1u) | ((pix >> 2) & 2u) | ((pix >> 3) & 4u));
+	int32_t px = sub_x + lx, py = sub_y + ly;
+
+	SampleState S;
+	int32_t ox = 0, oy = 0;
+	if (SS)
+		sample_offset(sample, I.rate_x_log2, I.rate_y_log2, ox, oy);
+	S.hx = (px << C.dim) + ox;
+	S.hy = (py << C.dim) + oy;
+	S.color_dirty = false;
+	S.depth_dirty = false;
+	S.pending.coverage = 0;
+	S.pending.z_write = false;
+	S.pending_prim = 0;
+
+	uint32_t fb_index = swizzle_address(uint32_t(px), uint32_t(py), I.fb_base, I.fb_stride, I.fb_psm);
+	uint32_t z_index = C.zs ? swizzle_address(uint32_t(px), uint32_t(py), I.zb_base, I.fb_stride, I.zb_psm) : 0u;
+	const uint32_t V32 = VRAM_SIZE / 4, V16 = VRAM_SIZE / 2;
+	uint32_t *vram32 = reinterpret_cast<uint32_t *>(P.vram);
+	uint16_t *vram16 = reinterpret_cast<uint16_t *>(P.vram);
+
+	// begin_tile
+	if (psm_is_16bit(I.fb_psm))
+	{
+		uint32_t col = vram16[fb_index];
+		if (SS && vram16[fb_index + V16] == 0xffffu)
+			col = vram16[fb_index + (sample + 2u) * V16];
+		S.color = expand16(col);
+	}
+	else
+	{
+		S.color = vram32[fb_index];
+		if (SS)
+		{
+			uint32_t ref = vram32[fb_index + V32];
+			uint32_t rm = psm_is_24bit(I.fb_psm) ? 0xffffffu : 0xffffffffu;
+			if ((ref & rm) == rm)
+			{
+				uint32_t sc = vram32[fb_index + (sample + 2u) * V32];
+				S.color = (psm_is_24bit(I.fb_psm) && ref != 0xffffffffu) ? ((S.color & 0xff000000u) | (sc & 0xffffffu)) : sc;
+			}
+		}
+	}
+	if (C.zs)
+	{
+		if (psm_is_16bit(I.zb_psm))
+		{
+			S.depth = vram16[z_index];
+			if (SS && vram16[z_index + V16] == 0xffffu)
+				S.depth = vram16[z_index + (sample + 2u) * V16];
+		}
+		else
+		{
+			uint32_t rm = psm_is_24bit(I.zb_psm) ? 0xffffffu : 0xffffffffu;
+			S.depth = vram32[z_index] & rm;
+			if (SS && (vram32[z_index + V32] & rm) == rm)
+				S.depth = vram32[z_index + (sample + 2u) * V32] & rm;
+		}
+	}
+	else
+		S.depth = 0;
+
+	// Warp pixel rectangle for the per-warp primitive test.
+	uint32_t lane = t & 31u;
+	int32_t wlo0 = px, wlo1 = py, whi0 = px, whi1 = py;
+	#pragma unroll
+	for (int o = 16; o >= 1; o >>= 1)
+	{
+		wlo0 = min(wlo0, __shfl_xor_sync(0xffffffffu, wlo0, o));
+		wlo1 = min(wlo1, __shfl_xor_sync(0xffffffffu, wlo1, o));
+		whi0 = max(whi0, __shfl_xor_sync(0xffffffffu, whi0, o));
+		whi1 = max(whi1, __shfl_xor_sync(0xffffffffu, whi1, o));
+	}
+	(void)lane;
+
+	const uint32_t *mask = tile_masks + size_t(tile) * I.mask_words;
+	uint32_t word = 0;
+	if (t == 0)
+		s_word = 0;
+	__syncthreads();
+
+	while (true)
+	{
+		// Warp 0 gathers the next chunk of primitive indices in ascending order.
+		if (t < 32)
+		{
+			int count = 0;
+			uint32_t w = s_word;
+			while (w < I.mask_words)
+			{
+				uint32_t idx = w + t;
+				uint32_t m = idx < I.mask_words ? mask[idx] : 0u;
+				int n = __popc(m);
+				int incl = n;
+				#pragma unroll
+				for (int o = 1; o < 32; o <<= 1)
+				{
+					int v = __shfl_up_sync(0xffffffffu, incl, o);
+					if (int(t) >= o)
+						incl += v;
+				}
+				// Inclusive sums grow with the lane, so the words that fit form a prefix.
+				bool fits = count + incl <= SHADE_CHUNK;
+				int nfit = __popc(__ballot_sync(0xffffffffu, fits));
+				if (fits && m)
+				{
+					int o = count + incl - n;
+					uint32_t mm = m;
+					while (mm)
+					{
+						int b = __ffs(mm) - 1;
+						mm &= mm - 1u;
+						s_list[o++] = I.prim_lo + (idx << 5) + uint32_t(b);
+					}
+				}
+				int last = __shfl_sync(0xffffffffu, incl, max(nfit - 1, 0));
+				int added = nfit ? last : 0;
+				count += added;
+				w += uint32_t(nfit);
+				if (nfit < 32)
+					break;
+			}
+			if (t == 0)
+			{
+				s_count = count;
+				s_word = min(w, I.mask_words);
+			}
+		}
+		__syncthreads();
+		int count = s_count;
+		word = s_word;
+
+		for (int k = 0; k < count; k++)
+		{
+			uint32_t pi = s_list[k];
+			const PrimSetup s = P.setup[pi];
+			uint32_t st = P.prims[pi].state;
+			bool ms_tri = P.has_aa1 && ((st >> STATE_BIT_MULTISAMPLE) & 1) && !((st >> STATE_BIT_LINE) & 1);
+			if (!intersects_tile(s, wlo0, wlo1, whi0, whi1, ms_tri))
+				continue;
+
+			bool opaque;
+			Request q = shade_early(C, s, st, S, opaque);
+			if (q.coverage > 0)
+			{
+				if (q.z_test && !S.pending.z_write)
+				{
+					q.z_test = false;
+					bool zp = q.z_greater ? q.z > S.depth : q.z >= S.depth;
+					if (zp)
+					{
+						if (q.z_write && opaque)
+						{
+							q.z_write = false;
+							S.depth = q.z;
+							S.depth_dirty = true;
+						}
+					}
+					else
+					{
+						q.coverage = 0;
+						q.z_write = false;
+					}
+				}
+				else if (q.z_write && !q.z_test && opaque)
+				{
+					q.z_write = false;
+					S.pending.z_write = false;
+					S.depth = q.z;
+					S.depth_dirty = true;
+				}
+				if ((q.z_test || !q.z_write) && S.pending.z_write)
+					opaque = false;
+			}
+			bool need_flush = false;
+			if (q.coverage > 0)
+			{
+				need_flush = !opaque && S.pending.coverage > 0;
+				if (!need_flush)
+				{
+					S.pending = q;
+					S.pending_prim = pi;
+					q.coverage = 0;
+				}
+			}
+			if (__any_sync(0xffffffffu, need_flush))
+			{
+				if (S.pending.coverage > 0)
+					shade_resolve(C, S);
+				S.pending.coverage = 0;
+				S.pending.z_write = false;
+				if (q.coverage > 0)
+				{
+					S.pending = q;
+					S.pending_prim = pi;
+				}
+			}
+		}
+		__syncthreads();
+		if (word >= I.mask_words)
+			break;
+	}
+
+	if (S.pending.coverage > 0)
+		shade_resolve(C, S);
+
+	// end_tile
+	const unsigned full = 0xffffffffu;
+	uint32_t group_lane0 = (t & 31u) & ~uint32_t(NS - 1);
+	bool req_color = false, req_depth = false;
+	bool color_dirty = S.color_dirty, depth_dirty = S.depth_dirty;
+	uint32_t color = S.color, depth = S.depth;
+	uint32_t group_mask = (NS == 32) ? full : (((1u << NS) - 1u) << group_lane0);
+
+	if (SS)
+	{
+		uint32_t first = __shfl_sync(full, S.color, int(group_lane0));
+		req_color = I.preserve_samples ? true : ((__ballot_sync(full, first != S.color) & group_mask) != 0u);
+		if (C.zs)
+		{
+			uint32_t zfirst = __shfl_sync(full, S.depth, int(group_lane0));
+			req_depth = (__ballot_sync(full, zfirst != S.depth) & group_mask) != 0u;
+		}
+		color_dirty = (__ballot_sync(full, S.color_dirty) & group_mask) != 0u;
+		// Butterfly sums in the order XOR NS/2 ... 1; every lane takes part.
+		float v0 = unorm8(S.color, 0), v1 = unorm8(S.color, 1), v2 = unorm8(S.color, 2), v3 = unorm8(S.color, 3);
+		#pragma unroll
+		for (int o = NS / 2; o >= 1; o >>= 1)
+		{
+			v0 = fadd(v0, __shfl_xor_sync(full, v0, o));
+			v1 = fadd(v1, __shfl_xor_sync(full, v1, o));
+			v2 = fadd(v2, __shfl_xor_sync(full, v2, o));
+			v3 = fadd(v3, __shfl_xor_sync(full, v3, o));
+		}
+		float n = float(NS);
+		uint32_t resolved = pack_unorm(__fdiv_rn(v0, n), __fdiv_rn(v1, n), __fdiv_rn(v2, n), __fdiv_rn(v3, n));
+		uint32_t zmin = S.depth;
+		#pragma unroll
+		for (int o = NS / 2; o >= 1; o >>= 1)
+			zmin = min(zmin, __shfl_xor_sync(full, zmin, o));
+		if (C.zs)
+			depth_dirty = (__ballot_sync(full, S.depth_dirty) & group_mask) != 0u;
+
+		if (req_color)
+		{
+			if (color_dirty)
+			{
+				if (psm_is_16bit(I.fb_psm))
+					vram16[fb_index + (sample + 2u) * V16] = uint16_t(rgba32_to_rgba16(S.color));
+				else
+					vram32[fb_index + (sample + 2u) * V32] = S.color;
+			}
+			color = I.preserve_samples ? first : resolved;
+		}
+		if (C.zs && req_depth)
+		{
+			if (depth_dirty)
+			{
+				if (psm_is_16bit(I.zb_psm))
+					vram16[z_index + (sample + 2u) * V16] = uint16_t(S.depth);
+				else
+					vram32[z_index + (sample + 2u) * V32] = S.depth;
+			}
+			depth = zmin;
+		}
+	}
+
+	bool first_sample = !SS || sample == 0;
+	if (color_dirty && first_sample)
+	{
+		if (psm_is_16bit(I.fb_psm))
+		{
+			if (P.has_ss_reference)
+				vram16[fb_index + V16] = req_color ? 0xffffu : 0u;
+			vram16[fb_index] = uint16_t(rgba32_to_rgba16(color));
+		}
+		else
+		{
+			if (P.has_ss_reference)
+				vram32[fb_index + V32] = req_color ? 0xffffffffu : 0u;
+			vram32[fb_index] = color;
+		}
+	}
+	if (C.zs && depth_dirty && first_sample)
+	{
+		if (psm_is_16bit(I.zb_psm))
+		{
+			if (P.has_ss_reference)
+				vram16[z_index + V16] = req_depth ? 0xffffu : 0u;
+			vram16[z_index] = uint16_t(depth);
+		}
+		else
+		{
+			if (P.has_ss_reference)
+				vram32[z_index + V32] = req_depth ? (psm_is_24bit(I.zb_psm) ? 0xffffffu : 0xffffffffu) : 0u;
+			if (psm_is_24bit(I.zb_psm))
+			{
+				uint8_t *b = P.vram + size_t(z_index) * 4u;
+				*reinterpret_cast<uint16_t *>(b) = uint16_t(depth);
+				b[2] = uint8_t(depth >> 16);
+			}
+			else
+				vram32[z_index] = depth;
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------
+// K4: VRAM transfers.
+struct CopyParams
+{
+	uint32_t sbp, sbw, spsm, dbp, dbw, dpsm;
+	uint32_t ssax, ssay, dsax, dsay, width, height;
+	uint32_t xdir;
+	uint64_t host_size, host_offset_qwords;
+	const uint8_t *host;      // device copy of the HWREG payload
+	const uint8_t *src_vram;  // snapshot for local->local
+	uint32_t invalidate_ss;
+};
+
+__device__ __forceinline__ void write_pixel(uint8_t *vram, uint32_t psm, uint32_t addr, uint32_t data, bool inv)
+{
+	uint32_t *v32 = reinterpret_cast<uint32_t *>(vram);
+	uint16_t *v16 = reinterpret_cast<uint16_t *>(vram);
+	const uint32_t V32 = VRAM_SIZE / 4, V16 = VRAM_SIZE / 2;
+	switch (psm)
+	{
+	case PSMCT24: case PSMZ24:
+	{
+		uint8_t *b = vram + size_t(addr) * 4u;
+		b[0] = uint8_t(data); b[1] = uint8_t(data >> 8); b[2] = uint8_t(data >> 16);
+		if (inv) { uint8_t *r = b + VRAM_SIZE; r[0] = 0; r[1] = 0; r[2] = 0; }
+		break;
+	}
+	case PSMCT16: case PSMCT16S: case PSMZ16: case PSMZ16S:
+		v16[addr] = uint16_t(data);
+		if (inv) v16[addr + V16] = 0;
+		break;
+	case PSMT8:
+		vram[addr] = uint8_t(data);
+		if (inv) vram[addr + VRAM_SIZE] = 0;
+		break;
+	case PSMT8H:
+		vram[addr * 4u + 3u] = uint8_t(data);
+		if (inv) vram[addr * 4u + 3u + VRAM_SIZE] = 0;
+		break;
+	case PSMT4:
+	{
+		uint32_t word = addr >> 3, sh = 4u * (addr & 7u);
+		atomicAnd(&v32[word], ~(0xfu << sh));
+		atomicOr(&v32[word], (data & 0xfu) << sh);
+		if (inv) atomicAnd(&v32[word + V32], ~(0xfu << sh));
+		break;
+	}
+	case PSMT4HL: case PSMT4HH:
+	{
+		uint32_t sh = psm == PSMT4HL ? 24u : 28u;
+		v32[addr] = (v32[addr] & ~(0xfu << sh)) | ((data & 0xfu) << sh);
+		if (inv) v32[addr + V32] &= ~(0xfu << sh);
+		break;
+	}
+	default:
+		v32[addr] = data;
+		if (inv) v32[addr + V32] = 0;
+		break;
+	}
+}
+
+__device__ __forceinline__ uint32_t read_pixel(const uint8_t *vram, uint32_t psm, uint32_t a)
+{
+	const uint32_t *v32 = reinterpret_cast<const uint32_t *>(vram);
+	const uint16_t *v16 = reinterpret_cast<const uint16_t *>(vram);
+	if (psm_is_16bit(psm)) return v16[a];
+	if (psm == PSMT8) return vram[a];
+	if (psm == PSMT8H) return vram[4u * a + 3u];
+	if (psm == PSMT4) return (uint32_t(vram[a >> 1]) >> ((a & 1u) * 4u)) & 15u;
+	if (psm == PSMT4HL) return (v32[a] >> 24) & 15u;
+	if (psm == PSMT4HH) return v32[a] >> 28;
+	return v32[a];
+}
+
+__global__ void __launch_bounds__(256) upload_kernel(CopyParams C, uint8_t *vram)
+{
+	uint32_t x = blockIdx.x * 32u + (threadIdx.x & 31u);
+	uint32_t y = blockIdx.y * 8u + (threadIdx.x >> 5);
+	if (x >= C.width || y >= C.height)
+		return;
+	uint32_t eff_stride = C.dbw;
+	if (C.dpsm == PSMT4 || C.dpsm == PSMT8)
+		eff_stride &= ~1u;
+	if (x >= eff_stride * 64u)
+	{
+		Layout L = psm_layout(C.dpsm);
+		uint32_t last = (C.dsay + C.height - 1u) >> L.ph, cur = (C.dsay + y) >> L.ph;
+		if (last != cur)
+			return;
+	}
+	uint32_t dx = (x + C.dsax) & 2047u, dy = (y + C.dsay) & 2047u;
+	uint32_t data;
+	if (C.xdir == HOST_TO_LOCAL)
+	{
+		uint64_t sa = uint64_t(y) * C.width + x;
+		uint32_t b = psm_bits_per_pixel(C.dpsm);
+		uint64_t factor = (b == 32 || b == 24) ? 2 : (b == 16 ? 4 : (b == 8 ? 8 : 16));
+		uint64_t avail = b == 32 ? C.host_size / 4 : (b == 24 ? C.host_size / 3 : (b == 16 ? C.host_size / 2 : (b == 8 ? C.host_size : 2 * C.host_size)));
+		if (sa * factor < C.host_offset_qwords || sa >= avail)
+			return;
+		const uint8_t *h = C.host;
+		if (b == 24) data = uint32_t(h[3 * sa]) | (uint32_t(h[3 * sa + 1]) << 8) | (uint32_t(h[3 * sa + 2]) << 16);
+		else if (b == 16) data = uint32_t(h[2 * sa]) | (uint32_t(h[2 * sa + 1]) << 8);
+		else if (b == 8) data = h[sa];
+		else if (b == 4) data = (uint32_t(h[sa >> 1]) >> ((sa & 1) * 4)) & 15u;
+		else data = uint32_t(h[4 * sa]) | (uint32_t(h[4 * sa + 1]) << 8) | (uint32_t(h[4 * sa + 2]) << 16) | (uint32_t(h[4 * sa + 3]) << 24);
+	}
+	else
+	{
+		uint32_t sx = (x + C.ssax) & 2047u, sy = (y + C.ssay) & 2047u;
+		data = read_pixel(C.src_vram, C.spsm, swizzle_address(sx, sy, C.sbp, C.sbw, C.spsm));
+	}
+	write_pixel(vram, C.dpsm, swizzle_address(dx, dy, C.dbp, C.dbw, C.dpsm), data, C.invalidate_ss != 0);
+}
+
+// ---------------------------------------------------------------------------
+// K6: CLUT load into a new ring instance.
+struct ClutParams
+{
+	uint32_t psm, cbp, cpsm, csm, csa, cbw, cou, cov;
+	float csm2_x_scale;
+	uint32_t csm2_x_bias;
+	uint32_t base_instance, instance;
+};
+
+__global__ void __launch_bounds__(256) clut_kernel(ClutParams C, const uint8_t *vram, uint16_t *clut)
+{
+	__shared__ uint16_t tmp[512];
+	uint32_t lane = threadIdx.x;
+	tmp[lane] = clut[size_t(C.base_instance) * 512u + lane];
+	tmp[lane + 256u] = clut[size_t(C.base_instance) * 512u + lane + 256u];
+	__syncthreads();
+	bool index4 = C.psm == PSMT4 || C.psm == PSMT4HH || C.psm == PSMT4HL;
+	bool active;
+	uint32_t wc = lane + C.csa * 16u, rc = lane;
+	if (index4)
+		active = lane < 16u;
+	else if (C.csm == 0)
+	{
+		uint32_t csa_count = C.cpsm == PSMCT32 ? 16u : 32u;
+		active = lane < (csa_count - C.csa) * 16u;
+		rc += C.csa * 16u;
+	}
+	else
+		active = true;
+	if (active)
+	{
+		uint32_t cx, cy;
+		if (C.csm)
+		{
+			cx = uint32_t(fadd(fmul(float(rc), C.csm2_x_scale), 1.0f / 256.0f)) + C.csm2_x_bias + C.cou * 16u;
+			cy = C.cov;
+		}
+		else
+		{
+			cx = (rc & 7u) | (((rc >> 4) & 1u) << 3);
+			cy = ((rc >> 3) & 1u) | (((rc >> 5) & 7u) << 1);
+		}
+		if (C.cpsm == PSMCT32)
+		{
+			uint32_t v = reinterpret_cast<const uint32_t *>(vram)[swizzle_address(cx, cy, C.cbp, C.cbw, PSMCT32)];
+			if (wc < 512u) tmp[wc] = uint16_t(v);
+			if (wc + 256u < 512u) tmp[wc + 256u] = uint16_t(v >> 16);
+		}
+		else
+		{
+			uint32_t v = reinterpret_cast<const uint16_t *>(vram)[swizzle_address(cx, cy, C.cbp, C.cbw, C.cpsm)];
+			if (wc < 512u) tmp[wc] = uint16_t(v);
+		}
+	}
+	__syncthreads();
+	clut[size_t(C.instance) * 512u + lane] = tmp[lane];
+	clut[size_t(C.instance) * 512u + lane + 256u] = tmp[lane + 256u];
+}
+} // namespace pgs

@@ -1,0 +1,360 @@
+"""Seeded GS command-stream generator.
+
+Builds GIF packet streams (128-bit qwords) that drive the frontend exactly as a
+PS2 program would: A+D register setup, BITBLTBUF/TRXPOS/TRXREG/TRXDIR + IMAGE
+texture and CLUT uploads, and PACKED vertex data.  The packet layout follows
+the GIF tag format decoded by GSInterface::gif_transfer
+(gs/gs_interface.cpp:4290-4397) and written by GSDumpGenerator
+(dump/gs_dump_generator.cpp:104-185).
+
+Workloads (sizes from the benchmark configurations):
+  frame_c1  640x448 PSMCT32 + PSMZ24, 10k Gouraud triangles, 1x.
+  frame_c2  640x448 PSMCT32 + PSMZ24, 50k perspective-textured blended
+            triangles + 2k sprites over 8 PSMT8 256x256 textures with CT32
+            CLUTs, bilinear, ATST GREATER 0x40, FBA, dither, 4x SSAA.
+  stream_c3 one of 64 mixed streams (C3), seeded by its stream id.
+  frame_c4  640x448 at 8x/16x with render-to-texture feedback draws.
+All randomness comes from numpy's PCG64 generator with an explicit seed.
+"""
+from __future__ import annotations
+
+import struct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# A+D register addresses (gs/gs_register_addr.hpp).
+PRIM, RGBAQ, ST, UV, XYZF2, XYZ2 = 0x00, 0x01, 0x02, 0x03, 0x04, 0x05
+TEX0_1, TEX0_2, CLAMP_1, CLAMP_2, FOG = 0x06, 0x07, 0x08, 0x09, 0x0A
+TEX1_1, TEX1_2, TEX2_1 = 0x14, 0x15, 0x16
+XYOFFSET_1, XYOFFSET_2, PRMODECONT, PRMODE, TEXCLUT = 0x18, 0x19, 0x1A, 0x1B, 0x1C
+SCANMSK, TEXA, FOGCOL, TEXFLUSH = 0x22, 0x3B, 0x3D, 0x3F
+SCISSOR_1, SCISSOR_2, ALPHA_1, ALPHA_2, DIMX, DTHE, COLCLAMP = 0x40, 0x41, 0x42, 0x43, 0x44, 0x45, 0x46
+TEST_1, TEST_2, PABE, FBA_1, FBA_2 = 0x47, 0x48, 0x49, 0x4A, 0x4B
+FRAME_1, FRAME_2, ZBUF_1, ZBUF_2 = 0x4C, 0x4D, 0x4E, 0x4F
+BITBLTBUF, TRXPOS, TRXREG, TRXDIR, HWREG = 0x50, 0x51, 0x52, 0x53, 0x54
+
+PSMCT32, PSMCT24, PSMCT16, PSMCT16S = 0x00, 0x01, 0x02, 0x0A
+PSMT8, PSMT4, PSMT8H = 0x13, 0x14, 0x1B
+PSMZ32, PSMZ24, PSMZ16, PSMZ16S = 0x30, 0x31, 0x32, 0x3A
+
+PRIM_POINT, PRIM_LINE, PRIM_LINESTRIP, PRIM_TRI, PRIM_TRISTRIP, PRIM_TRIFAN, PRIM_SPRITE = range(7)
+
+# GIF PACKED register descriptors.
+D_PRIM, D_RGBAQ, D_ST, D_UV, D_XYZF2, D_XYZ2, D_AD = 0x0, 0x1, 0x2, 0x3, 0x4, 0x5, 0xE
+
+PAGE_BYTES = 8192
+BLOCKS_PER_PAGE = 32
+
+
+def f32_bits(x) -> np.ndarray:
+    return np.asarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+
+
+def prim_reg(prim, iip=0, tme=0, fge=0, abe=0, aa1=0, fst=0, ctxt=0, fix=0) -> int:
+    return (prim | (iip << 3) | (tme << 4) | (fge << 5) | (abe << 6) | (aa1 << 7) | (fst << 8) |
+            (ctxt << 9) | (fix << 10))
+
+
+def frame_reg(fbp, fbw, psm, fbmsk=0) -> int:
+    return fbp | (fbw << 16) | (psm << 24) | (fbmsk << 32)
+
+
+def zbuf_reg(zbp, psm, zmsk=0) -> int:
+    return zbp | ((psm & 0xF) << 24) | (zmsk << 32)
+
+
+def test_reg(ate=0, atst=1, aref=0, afail=0, date=0, datm=0, zte=1, ztst=1) -> int:
+    return (ate | (atst << 1) | (aref << 4) | (afail << 12) | (date << 14) | (datm << 15) | (zte << 16) |
+            (ztst << 17))
+
+
+def alpha_reg(a, b, c, d, fix=0) -> int:
+    return a | (b << 2) | (c << 4) | (d << 6) | (fix << 32)
+
+
+def scissor_reg(x0, x1, y0, y1) -> int:
+    return x0 | (x1 << 16) | (y0 << 32) | (y1 << 48)
+
+
+def tex0_reg(tbp0, tbw, psm, tw, th, tcc=1, tfx=0, cbp=0, cpsm=0, csm=0, csa=0, cld=0) -> int:
+    return (tbp0 | (tbw << 14) | (psm << 20) | (tw << 26) | (th << 30) | (tcc << 34) | (tfx << 35) |
+            (cbp << 37) | (cpsm << 51) | (csm << 55) | (csa << 56) | (cld << 61))
+
+
+def tex1_reg(lcm=0, mxl=0, mmag=0, mmin=0, mtba=0, l=0, k=0) -> int:
+    return lcm | (mxl << 2) | (mmag << 5) | (mmin << 6) | (mtba << 9) | (l << 19) | (k << 32)
+
+
+def clamp_reg(wms=0, wmt=0, minu=0, maxu=0, minv=0, maxv=0) -> int:
+    return wms | (wmt << 2) | (minu << 4) | (maxu << 14) | (minv << 24) | (maxv << 34)
+
+
+def texa_reg(ta0=0, aem=0, ta1=0x80) -> int:
+    return ta0 | (aem << 15) | (ta1 << 32)
+
+
+def bitbltbuf_reg(sbp=0, sbw=0, spsm=0, dbp=0, dbw=0, dpsm=0) -> int:
+    return sbp | (sbw << 16) | (spsm << 24) | (dbp << 32) | (dbw << 48) | (dpsm << 56)
+
+
+def trxpos_reg(ssax=0, ssay=0, dsax=0, dsay=0, dir_=0) -> int:
+    return ssax | (ssay << 16) | (dsax << 32) | (dsay << 48) | (dir_ << 59)
+
+
+def trxreg_reg(w, h) -> int:
+    return w | (h << 32)
+
+
+def dimx_reg(matrix) -> int:
+    """4x4 dither matrix of values in [-4, 3]."""
+    v = 0
+    for r in range(4):
+        for c in range(4):
+            v |= (int(matrix[r][c]) & 7) << ((r * 4 + c) * 4)
+    return v
+
+
+DEFAULT_DIMX = [[-4, 2, -3, 3], [0, -2, 1, -1], [-3, 3, -4, 2], [1, -1, 0, -2]]
+
+
+def gif_tag(nloop, flg, nreg, regs=0, eop=0, pre=0, prim=0) -> tuple[int, int]:
+    lo = (nloop & 0x7FFF) | (eop << 15) | (pre << 46) | ((prim & 0x7FF) << 47) | (flg << 58) | ((nreg & 0xF) << 60)
+    return lo, regs
+
+
+class GifStream:
+    """Accumulates 128-bit qwords as pairs of uint64."""
+
+    def __init__(self) -> None:
+        self.chunks: list[np.ndarray] = []
+
+    def _qwords(self, arr: np.ndarray) -> None:
+        self.chunks.append(np.ascontiguousarray(arr, dtype=np.uint64).reshape(-1, 2))
+
+    def ad(self, regs: list[tuple[int, int]]) -> None:
+        """One PACKED A+D packet writing (address, value) pairs."""
+        n = len(regs)
+        lo, hi = gif_tag(n, 0, 1, D_AD)
+        q = np.zeros((n + 1, 2), dtype=np.uint64)
+        q[0] = (lo, hi)
+        for i, (addr, val) in enumerate(regs):
+            q[i + 1] = (val & 0xFFFFFFFFFFFFFFFF, addr)
+        self._qwords(q)
+
+    def image(self, data: bytes) -> None:
+        if len(data) % 16:
+            data = data + bytes(16 - len(data) % 16)
+        nq = len(data) // 16
+        off = 0
+        while off < nq:
+            n = min(nq - off, 0x7FFF)
+            lo, hi = gif_tag(n, 2, 0)
+            self._qwords(np.array([[lo, hi]], dtype=np.uint64))
+            self._qwords(np.frombuffer(data[off * 16:(off + n) * 16], dtype=np.uint64))
+            off += n
+
+    def upload(self, dbp, dbw, dpsm, x, y, w, h, data: bytes) -> None:
+        self.ad([(BITBLTBUF, bitbltbuf_reg(dbp=dbp, dbw=dbw, dpsm=dpsm)),
+                 (TRXPOS, trxpos_reg(dsax=x, dsay=y)),
+                 (TRXREG, trxreg_reg(w, h)),
+                 (TRXDIR, 0)])
+        self.image(data)
+
+    def packed(self, prim: int, desc: list[int], data: np.ndarray) -> None:
+        """PACKED packets with a PRIM preset; data is (n_loops * len(desc), 2) qwords."""
+        nreg = len(desc)
+        regs = 0
+        for i, d in enumerate(desc):
+            regs |= d << (4 * i)
+        data = np.ascontiguousarray(data, dtype=np.uint64).reshape(-1, nreg, 2)
+        nloops = data.shape[0]
+        off = 0
+        # Keep every packet a whole number of primitives so PRE resets nothing mid-strip.
+        step = (0x7FFF // 6) * 6
+        while off < nloops:
+            n = min(nloops - off, step)
+            lo, hi = gif_tag(n, 0, nreg, regs, pre=1, prim=prim)
+            self._qwords(np.array([[lo, hi]], dtype=np.uint64))
+            self._qwords(data[off:off + n].reshape(-1, 2))
+            off += n
+
+    def tobytes(self) -> bytes:
+        return np.concatenate(self.chunks).astype("<u8").tobytes()
+
+
+def q_rgbaq(rgba: np.ndarray) -> np.ndarray:
+    rgba = rgba.astype(np.uint64)
+    lo = rgba[:, 0] | (rgba[:, 1] << np.uint64(32))
+    hi = rgba[:, 2] | (rgba[:, 3] << np.uint64(32))
+    return np.stack([lo, hi], axis=1)
+
+
+def q_xyz2(x: np.ndarray, y: np.ndarray, z: np.ndarray) -> np.ndarray:
+    lo = x.astype(np.uint64) | (y.astype(np.uint64) << np.uint64(32))
+    hi = z.astype(np.uint64) & np.uint64(0xFFFFFFFF)
+    return np.stack([lo, hi], axis=1)
+
+
+def q_st(s: np.ndarray, t: np.ndarray, q: np.ndarray) -> np.ndarray:
+    lo = f32_bits(s) | (f32_bits(t) << np.uint64(32))
+    hi = f32_bits(q)
+    return np.stack([lo, hi], axis=1)
+
+
+def q_uv(u: np.ndarray, v: np.ndarray) -> np.ndarray:
+    lo = u.astype(np.uint64) | (v.astype(np.uint64) << np.uint64(32))
+    return np.stack([lo, np.zeros_like(lo)], axis=1)
+
+
+def random_triangles(rng, n, width, height, area_lo, area_hi):
+    """Triangles with log-uniform area, uniform centroid, random shape, in 12.4."""
+    area = np.exp(rng.uniform(np.log(area_lo), np.log(area_hi), n))
+    cx = rng.uniform(0, width, n)
+    cy = rng.uniform(0, height, n)
+    t0 = rng.uniform(0, 2 * np.pi, n)
+    t1 = t0 + rng.uniform(np.pi / 3, np.pi, n)
+    t2 = t1 + rng.uniform(np.pi / 3, np.pi, n)
+    ang = np.stack([t0, t1, t2], axis=1)
+    ux, uy = np.cos(ang), np.sin(ang)
+    a0 = 0.5 * np.abs((ux[:, 1] - ux[:, 0]) * (uy[:, 2] - uy[:, 0]) - (ux[:, 2] - ux[:, 0]) * (uy[:, 1] - uy[:, 0]))
+    r = np.sqrt(area / np.maximum(a0, 1e-3))
+    x = cx[:, None] + ux * r[:, None]
+    y = cy[:, None] + uy * r[:, None]
+    xi = np.clip(np.round(x * 16), 0, width * 16 - 1).astype(np.int64)
+    yi = np.clip(np.round(y * 16), 0, height * 16 - 1).astype(np.int64)
+    return xi, yi
+
+
+def random_sprites(rng, n, width, height, area_lo, area_hi):
+    area = np.exp(rng.uniform(np.log(area_lo), np.log(area_hi), n))
+    aspect = np.exp(rng.uniform(np.log(0.5), np.log(2.0), n))
+    w = np.sqrt(area * aspect)
+    h = area / w
+    x0 = rng.uniform(0, width, n) - w / 2
+    y0 = rng.uniform(0, height, n) - h / 2
+    xs = np.stack([x0, x0 + w], axis=1)
+    ys = np.stack([y0, y0 + h], axis=1)
+    xi = np.clip(np.round(xs * 16), 0, width * 16 - 1).astype(np.int64)
+    yi = np.clip(np.round(ys * 16), 0, height * 16 - 1).astype(np.int64)
+    return xi, yi
+
+
+@dataclass
+class Frame:
+    """One seeded command stream plus the options it needs."""
+    name: str
+    data: bytes
+    super_sampling: int = 1
+    ordered: bool = True
+    num_primitives: int = 0
+    meta: dict = field(default_factory=dict)
+
+
+def _frame_setup(s: GifStream, fbp, fbw, fpsm, zbp, zpsm, width, height, test, alpha=0, extra=()):
+    s.ad([(PRMODECONT, 1),
+          (FRAME_1, frame_reg(fbp, fbw, fpsm)),
+          (ZBUF_1, zbuf_reg(zbp, zpsm)),
+          (SCISSOR_1, scissor_reg(0, width - 1, 0, height - 1)),
+          (XYOFFSET_1, 0),
+          (TEST_1, test),
+          (ALPHA_1, alpha),
+          *extra])
+
+
+def frame_c1(seed: int = 1, num_triangles: int = 10000, width: int = 640, height: int = 448) -> Frame:
+    """Plain method: untextured Gouraud triangles, Z GEQUAL, 1x."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = GifStream()
+    zbp = (width * height * 4 + PAGE_BYTES - 1) // PAGE_BYTES
+    _frame_setup(s, 0, width // 64, PSMCT32, zbp, PSMZ24, width, height,
+                 test_reg(zte=1, ztst=2), extra=[(COLCLAMP, 1)])
+    x, y = random_triangles(rng, num_triangles, width, height, 4.0, 4000.0)
+    z = rng.integers(0, 1 << 24, size=(num_triangles, 3), dtype=np.int64)
+    rgba = rng.integers(0, 256, size=(num_triangles, 3, 4), dtype=np.int64)
+    nv = num_triangles * 3
+    q = np.zeros((nv, 2, 2), dtype=np.uint64)
+    q[:, 0] = q_rgbaq(rgba.reshape(nv, 4))
+    q[:, 1] = q_xyz2(x.reshape(nv), y.reshape(nv), z.reshape(nv))
+    s.packed(prim_reg(PRIM_TRI, iip=1), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+    return Frame("c1", s.tobytes(), 1, True, num_triangles,
+                 {"width": width, "height": height, "fbp": 0, "zbp": zbp})
+
+
+def _texture_set(rng, s: GifStream, base_page: int, count: int, tw: int, th: int, psm: int):
+    """Uploads `count` paletted textures and their CT32 CLUTs; returns TEX0 values."""
+    tex0s = []
+    w, h = 1 << tw, 1 << th
+    tbw = max(1, w // 64)
+    if psm == PSMT8:
+        tex_bytes = w * h
+        clut_w, clut_h = 16, 16
+    else:
+        tex_bytes = w * h // 2
+        clut_w, clut_h = 8, 2
+    pages_per_tex = max(1, (tex_bytes + PAGE_BYTES - 1) // PAGE_BYTES)
+    page = base_page
+    clut_page = base_page + count * pages_per_tex
+    for i in range(count):
+        tbp0 = page * BLOCKS_PER_PAGE
+        data = rng.integers(0, 256, size=tex_bytes, dtype=np.uint8).tobytes()
+        s.upload(tbp0, tbw, psm, 0, 0, w, h, data)
+        cbp = clut_page * BLOCKS_PER_PAGE + i * 4
+        clut = rng.integers(0, 1 << 32, size=clut_w * clut_h, dtype=np.uint64).astype(np.uint32).tobytes()
+        s.upload(cbp, 1, PSMCT32, 0, 0, clut_w, clut_h, clut)
+        tex0s.append(tex0_reg(tbp0, tbw, psm, tw, th, tcc=1, tfx=0, cbp=cbp, cpsm=PSMCT32, csm=0, csa=0, cld=1))
+        page += pages_per_tex
+    return tex0s, clut_page + 1
+
+
+def frame_c2(seed: int = 2, num_triangles: int = 50000, num_sprites: int = 2000, super_sampling: int = 4,
+             width: int = 640, height: int = 448, num_textures: int = 8) -> Frame:
+    """Textured and blended: PSMT8 + CT32 CLUT, perspective STQ, bilinear, alpha blend,
+    ATST GREATER 0x40, FBA, dither, 4x SSAA."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = GifStream()
+    fb_pages = (width * height * 4 + PAGE_BYTES - 1) // PAGE_BYTES
+    zbp = fb_pages
+    tex_base = 2 * fb_pages
+    test = test_reg(ate=1, atst=6, aref=0x40, afail=0, zte=1, ztst=2)
+    _frame_setup(s, 0, width // 64, PSMCT32, zbp, PSMZ24, width, height, test,
+                 alpha=alpha_reg(0, 1, 0, 1),
+                 extra=[(FBA_1, 1), (DTHE, 1), (DIMX, dimx_reg(DEFAULT_DIMX)), (COLCLAMP, 1),
+                        (TEX1_1, tex1_reg(mmag=1, mmin=1)), (CLAMP_1, clamp_reg(0, 0)),
+                        (TEXA, texa_reg(0, 0, 0x80)), (PABE, 0)])
+    tex0s, _ = _texture_set(rng, s, tex_base, num_textures, 8, 8, PSMT8)
+    tris_per = np.full(num_textures, num_triangles // num_textures)
+    tris_per[: num_triangles % num_textures] += 1
+    spr_per = np.full(num_textures, num_sprites // num_textures)
+    spr_per[: num_sprites % num_textures] += 1
+    for ti in range(num_textures):
+        s.ad([(TEX0_1, tex0s[ti])])
+        n = int(tris_per[ti])
+        x, y = random_triangles(rng, n, width, height, 4.0, 4000.0)
+        z = rng.integers(0, 1 << 24, size=(n, 3), dtype=np.int64)
+        rgba = rng.integers(0, 256, size=(n, 3, 4), dtype=np.int64)
+        qv = rng.uniform(0.25, 4.0, size=(n, 3)).astype(np.float32)
+        sn = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+        tn = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+        nv = n * 3
+        q = np.zeros((nv, 3, 2), dtype=np.uint64)
+        q[:, 0] = q_st((sn * qv).reshape(nv), (tn * qv).reshape(nv), qv.reshape(nv))
+        q[:, 1] = q_rgbaq(rgba.reshape(nv, 4))
+        q[:, 2] = q_xyz2(x.reshape(nv), y.reshape(nv), z.reshape(nv))
+        s.packed(prim_reg(PRIM_TRI, iip=1, tme=1, abe=1), [D_ST, D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+        m = int(spr_per[ti])
+        if m:
+            sx, sy = random_sprites(rng, m, width, height, 4.0, 4000.0)
+            sz = rng.integers(0, 1 << 24, size=(m, 2), dtype=np.int64)
+            srgba = rng.integers(0, 256, size=(m, 2, 4), dtype=np.int64)
+            sq = rng.uniform(0.25, 4.0, size=(m, 2)).astype(np.float32)
+            ss = rng.uniform(0.0, 1.0, size=(m, 2)).astype(np.float32)
+            st = rng.uniform(0.0, 1.0, size=(m, 2)).astype(np.float32)
+            mv = m * 2
+            q = np.zeros((mv, 3, 2), dtype=np.uint64)
+            q[:, 0] = q_st((ss * sq).reshape(mv), (st * sq).reshape(mv), sq.reshape(mv))
+            q[:, 1] = q_rgbaq(srgba.reshape(mv, 4))
+            q[:, 2] = q_xyz2(sx.reshape(mv), sy.reshape(mv), sz.reshape(mv))
+            s.packed(prim_reg(PRIM_SPRITE, iip=1, tme=1, abe=1), [D_ST, D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+    return Frame("c2", s.tobytes(), super_sampling, True, num_triangles + num_sprites,
+                 {"width": width, "height": height, "fbp": 0, "zbp": zbp})

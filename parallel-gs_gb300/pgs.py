@@ -1,0 +1,239 @@
+"""Python binding of the GS frontend and the CUDA backend (ctypes over include/pgs.h).
+
+The classes mirror the reference's GSInterface API (gs/gs_interface.hpp:251-304):
+
+    backend = CudaBackend(device=0, max_samples_log2=4)
+    gs = GSInterface(backend, super_sampling=4)
+    gs.gif_transfer(0, packet_bytes)
+    vram = gs.read_vram()          # 4 MiB numpy array (flushes and waits)
+
+The product path always runs the CUDA backend from the in-tree
+libpgs_gb300.so; it raises if the library or a GPU is missing.  Any other
+object exposing ``ops`` (a pgs_backend_ops pointer) and ``handle`` can be
+passed to GSInterface in its place.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libpgs_gb300.so"
+VRAM_SIZE = 4 * 1024 * 1024
+
+PGS_OK = 0
+STATUS_NAMES = {
+    0: "PGS_OK", -1: "PGS_ERROR_INVALID_ARGUMENT", -2: "PGS_ERROR_OUT_OF_MEMORY", -3: "PGS_ERROR_CUDA",
+    -4: "PGS_ERROR_NO_DEVICE", -5: "PGS_ERROR_UNSUPPORTED", -6: "PGS_ERROR_DEVICE_FLAG", -7: "PGS_ERROR_CAPACITY",
+}
+
+
+class PGSError(RuntimeError):
+    def __init__(self, status: int, what: str) -> None:
+        super().__init__("%s failed: %s (%d)" % (what, STATUS_NAMES.get(status, "?"), status))
+        self.status = status
+
+
+def check(status: int, what: str) -> None:
+    if status != PGS_OK:
+        raise PGSError(status, what)
+
+
+class FlushStats(C.Structure):
+    _fields_ = [("num_render_passes", C.c_uint64), ("num_primitives", C.c_uint64), ("num_copies", C.c_uint64),
+                ("num_palette_updates", C.c_uint64), ("num_copy_barriers", C.c_uint64),
+                ("num_flushes_by_reason", C.c_uint64 * 8)]
+
+
+class GSOptions(C.Structure):
+    _fields_ = [("super_sampling", C.c_uint32), ("ordered_super_sampling", C.c_uint32), ("vram_size", C.c_uint32)]
+
+
+class CudaBackendOptions(C.Structure):
+    _fields_ = [("device", C.c_int), ("max_samples_log2", C.c_uint32), ("flags", C.c_uint32)]
+
+
+# Every C-ABI symbol include/pgs.h declares.
+EXPORTED_SYMBOLS = [
+    "pgs_cuda_backend_create", "pgs_cuda_backend_begin_record", "pgs_cuda_backend_end_record",
+    "pgs_cuda_backend_replay", "pgs_cuda_backend_stream", "pgs_cuda_backend_launches_per_replay",
+    "pgs_cuda_backend_last_shade_ms", "pgs_cuda_backend_fragment_count",
+    "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
+    "pgs_gs_read_vram", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
+    "pgs_gs_set_super_sampling_rate",
+]
+
+_lib = None
+
+
+def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Loads the product library (raises FileNotFoundError when it was not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError("%s is missing: run parallel-gs_gb300/build.py" % p)
+    lib = C.CDLL(str(p))
+    vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+    lib.pgs_cuda_backend_create.argtypes = [C.POINTER(CudaBackendOptions), C.POINTER(vp), C.POINTER(i32)]
+    lib.pgs_cuda_backend_create.restype = vp
+    lib.pgs_cuda_backend_begin_record.argtypes = [vp]
+    lib.pgs_cuda_backend_end_record.argtypes = [vp]
+    lib.pgs_cuda_backend_replay.argtypes = [vp, u32, i32, i32]
+    lib.pgs_cuda_backend_stream.argtypes = [vp]
+    lib.pgs_cuda_backend_stream.restype = vp
+    lib.pgs_cuda_backend_launches_per_replay.argtypes = [vp]
+    lib.pgs_cuda_backend_launches_per_replay.restype = u32
+    lib.pgs_cuda_backend_last_shade_ms.argtypes = [vp, C.POINTER(C.c_float)]
+    lib.pgs_cuda_backend_fragment_count.argtypes = [vp, C.POINTER(u64)]
+    lib.pgs_gs_create.argtypes = [vp, vp, C.POINTER(GSOptions), C.POINTER(i32)]
+    lib.pgs_gs_create.restype = vp
+    lib.pgs_gs_destroy.argtypes = [vp]
+    lib.pgs_gs_destroy.restype = None
+    lib.pgs_gs_gif_transfer.argtypes = [vp, u32, vp, C.c_size_t]
+    lib.pgs_gs_write_register.argtypes = [vp, u32, u64]
+    lib.pgs_gs_flush.argtypes = [vp]
+    lib.pgs_gs_read_vram.argtypes = [vp, u64, u64, vp]
+    lib.pgs_gs_write_vram.argtypes = [vp, u64, u64, vp]
+    lib.pgs_gs_read_transfer_fifo.argtypes = [vp, vp, u32]
+    lib.pgs_gs_consume_flush_stats.argtypes = [vp, C.POINTER(FlushStats)]
+    lib.pgs_gs_set_super_sampling_rate.argtypes = [vp, u32, u32]
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class BackendOps(C.Structure):
+    """pgs_backend_ops; only used to call destroy/read_vram on foreign backends."""
+    _fields_ = [("abi_version", C.c_uint32),
+                ("destroy", C.CFUNCTYPE(None, C.c_void_p)),
+                ("reserve_primitive_buffers", C.c_void_p),
+                ("flush_rendering", C.c_void_p),
+                ("copy_vram", C.c_void_p),
+                ("update_palette_cache", C.c_void_p),
+                ("set_super_sampling", C.c_void_p),
+                ("flush_submit", C.c_void_p),
+                ("read_vram", C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p)),
+                ("write_vram", C.c_void_p),
+                ("get_error", C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_uint32)))]
+
+
+class Backend:
+    """A backend instance: `ops` is a pgs_backend_ops pointer, `handle` its state."""
+
+    def __init__(self, ops: int, handle: int) -> None:
+        self.ops = ops
+        self.handle = handle
+
+    def read_plane(self, plane: int, offset: int = 0, size: int = VRAM_SIZE) -> np.ndarray:
+        out = np.empty(size, dtype=np.uint8)
+        table = C.cast(C.c_void_p(self.ops), C.POINTER(BackendOps)).contents
+        check(table.read_vram(self.handle, plane, offset, size, out.ctypes.data), "read_vram")
+        return out
+
+    def error_flags(self) -> int:
+        table = C.cast(C.c_void_p(self.ops), C.POINTER(BackendOps)).contents
+        flags = C.c_uint32(0)
+        table.get_error(self.handle, C.byref(flags))
+        return flags.value
+
+    def close(self) -> None:
+        if self.handle:
+            table = C.cast(C.c_void_p(self.ops), C.POINTER(BackendOps)).contents
+            table.destroy(self.handle)
+            self.handle = None
+
+
+class CudaBackend(Backend):
+    """The sm_103a backend.  Fails loudly when no GPU or library is present."""
+
+    def __init__(self, device: int = 0, max_samples_log2: int = 4) -> None:
+        self.lib = load_library()
+        opts = CudaBackendOptions(device, max_samples_log2, 0)
+        ops = C.c_void_p()
+        status = C.c_int(0)
+        handle = self.lib.pgs_cuda_backend_create(C.byref(opts), C.byref(ops), C.byref(status))
+        if not handle:
+            raise PGSError(status.value, "pgs_cuda_backend_create")
+        super().__init__(ops.value, handle)
+
+    def begin_record(self) -> None:
+        check(self.lib.pgs_cuda_backend_begin_record(self.handle), "begin_record")
+
+    def end_record(self) -> None:
+        check(self.lib.pgs_cuda_backend_end_record(self.handle), "end_record")
+
+    def replay(self, count: int = 1, reset_vram: bool = True, use_graph: bool = True) -> None:
+        check(self.lib.pgs_cuda_backend_replay(self.handle, count, int(reset_vram), int(use_graph)), "replay")
+
+    def stream(self) -> int:
+        return self.lib.pgs_cuda_backend_stream(self.handle)
+
+    def launches_per_replay(self) -> int:
+        return int(self.lib.pgs_cuda_backend_launches_per_replay(self.handle))
+
+
+class GSInterface:
+    """GSInterface (gs/gs_interface.hpp:251-304) over any backend."""
+
+    def __init__(self, backend: Backend, super_sampling: int = 1, ordered: bool = True, lib: C.CDLL | None = None):
+        self.lib = lib or load_library()
+        self.backend = backend
+        opts = GSOptions(super_sampling, int(ordered), VRAM_SIZE)
+        status = C.c_int(0)
+        self.handle = self.lib.pgs_gs_create(C.c_void_p(backend.ops), C.c_void_p(backend.handle), C.byref(opts),
+                                             C.byref(status))
+        if not self.handle:
+            raise PGSError(status.value, "pgs_gs_create")
+
+    def gif_transfer(self, path: int, data) -> None:
+        buf = np.frombuffer(data, dtype=np.uint8) if isinstance(data, (bytes, bytearray, memoryview)) else \
+            np.ascontiguousarray(data).view(np.uint8)
+        check(self.lib.pgs_gs_gif_transfer(self.handle, path, buf.ctypes.data, buf.size), "gif_transfer")
+
+    def write_register(self, addr: int, value: int) -> None:
+        check(self.lib.pgs_gs_write_register(self.handle, addr, value & 0xFFFFFFFFFFFFFFFF), "write_register")
+
+    def flush(self) -> None:
+        check(self.lib.pgs_gs_flush(self.handle), "flush")
+
+    def read_vram(self, offset: int = 0, size: int = VRAM_SIZE, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(size, dtype=np.uint8)
+        check(self.lib.pgs_gs_read_vram(self.handle, offset, size, out.ctypes.data), "read_vram")
+        return out
+
+    def write_vram(self, data, offset: int = 0) -> None:
+        buf = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, bytes) else data)
+        check(self.lib.pgs_gs_write_vram(self.handle, offset, buf.nbytes, buf.ctypes.data), "write_vram")
+
+    def read_transfer_fifo(self, num_128b_words: int) -> bytes:
+        out = np.zeros(num_128b_words * 16, dtype=np.uint8)
+        check(self.lib.pgs_gs_read_transfer_fifo(self.handle, out.ctypes.data, num_128b_words), "read_transfer_fifo")
+        return out.tobytes()
+
+    def consume_flush_stats(self) -> dict:
+        st = FlushStats()
+        check(self.lib.pgs_gs_consume_flush_stats(self.handle, C.byref(st)), "consume_flush_stats")
+        return {"render_passes": st.num_render_passes, "primitives": st.num_primitives, "copies": st.num_copies,
+                "palette_updates": st.num_palette_updates,
+                "flush_reasons": list(st.num_flushes_by_reason)}
+
+    def set_super_sampling_rate(self, super_sampling: int, ordered: bool = True) -> None:
+        check(self.lib.pgs_gs_set_super_sampling_rate(self.handle, super_sampling, int(ordered)),
+              "set_super_sampling_rate")
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.pgs_gs_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass

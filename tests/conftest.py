@@ -1,0 +1,27 @@
+"""Shared test setup: markers, import paths and one build per session."""
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT / "parallel-gs_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs on the GB300 box)")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built_libraries():
+    import build
+    return build.build_all()
+
+
+def cuda_available() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
