@@ -252,11 +252,28 @@ int pgs_cuda_backend_replay(void *backend, uint32_t count, int reset_vram, int u
 void *pgs_cuda_backend_stream(void *backend);
 /* Kernel launches issued by the last replay (per replay). */
 uint32_t pgs_cuda_backend_launches_per_replay(void *backend);
-/* Device time of the shading kernels of the last replay, in milliseconds,
- * measured with CUDA events on the backend's stream. */
+/* Device time from the first to the last shading kernel of the last replay,
+ * in milliseconds (CUDA events on the backend's stream). */
 int pgs_cuda_backend_last_shade_ms(void *backend, float *ms);
-/* Number of covered samples written by the last flush (fragment counter). */
+/* Covered pixel samples (primitive x sample pairs that passed the coverage
+ * test) counted by the shading kernels since the backend was created. */
 int pgs_cuda_backend_fragment_count(void *backend, uint64_t *count);
+
+typedef struct pgs_backend_stats
+{
+	uint64_t h2d_bytes;     /* host->device bytes copied since creation */
+	uint64_t d2h_bytes;     /* device->host bytes copied since creation */
+	uint64_t kernel_launches;
+	uint64_t render_passes;
+} pgs_backend_stats;
+
+/* Transfer and launch counters of the backend. */
+int pgs_cuda_backend_get_stats(void *backend, pgs_backend_stats *stats);
+/* When enabled, every replay records CUDA events (also inside the replay's
+ * CUDA graph) around the shading kernels of its render passes; the time
+ * between them is returned by pgs_cuda_backend_last_shade_ms once the replay
+ * has completed. */
+int pgs_cuda_backend_set_shade_timing(void *backend, int enable);
 
 /* ------------------------------------------------------------------ */
 /* Frontend (GSInterface)                                               */

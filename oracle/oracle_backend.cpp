@@ -27,6 +27,7 @@
 #include "pgs.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -241,7 +242,7 @@ struct Backend
 	std::vector<pgs_vertex_position> res_pos;
 	std::vector<pgs_vertex_attribute> res_attr;
 	std::vector<pgs_primitive_attribute> res_prim;
-	uint64_t fragments = 0;
+	std::atomic<uint64_t> fragments{0};
 
 	Backend() : clut(PGS_CLUT_INSTANCES * 512, 0)
 	{
@@ -675,9 +676,9 @@ struct Backend
 	struct PassCtx
 	{
 		const pgs_render_pass *rp;
-		std::vector<pgs_primitive_attribute> prims;
-		std::vector<Setup> setup;
-		std::vector<TAttr> tattr;
+		const pgs_primitive_attribute *prims;
+		const Setup *setup;
+		const TAttr *tattr;
 		uint32_t sr_dim_log2, num_samples, sr_x_log2;
 		bool ss;                 // this work item is super-sampled
 		bool has_ss_reference;   // VRAM holds sample planes
@@ -1323,6 +1324,7 @@ struct Backend
 		uint32_t fb_index = swizzle(uint32_t(px), uint32_t(py), P.fb_base, P.fb_stride, P.fb_psm);
 		uint32_t z_index = P.zb_psm != ~0u ? swizzle(uint32_t(px), uint32_t(py), P.zb_base, P.fb_stride, P.zb_psm) : 0;
 		uint32_t D = P.sr_dim_log2;
+		uint64_t covered = 0;
 
 		for (uint32_t s = 0; s < N; s++)
 		{
@@ -1340,7 +1342,7 @@ struct Backend
 				Request px_req = shade_early(P, pi, S, opaque);
 				if (px_req.coverage > 0)
 				{
-					fragments++;
+					covered++;
 					if (px_req.z_test && !S.pending.z_write)
 					{
 						px_req.z_test = false;
@@ -1391,6 +1393,7 @@ struct Backend
 		}
 
 		end_pixel(P, smp, N, fb_index, z_index);
+		fragments.fetch_add(covered, std::memory_order_relaxed);
 	}
 
 	// end_tile (gs/shaders/ubershader.comp:581-780) for one pixel.
@@ -1552,9 +1555,13 @@ struct Backend
 		P.zb_psm = inst.z_sensitive ? effective_z_psm(fb_psm, zpsm_raw) : ~0u;
 		bool ss_inst = inst.sampling_rate_y_log2 != 0;
 
-		for (uint32_t ty = 0; ty < inst.coarse_tiles_height; ty++)
+		const int32_t ntiles = int32_t(inst.coarse_tiles_width * inst.coarse_tiles_height);
+		const PassCtx shared = P;
+		#pragma omp parallel for schedule(dynamic, 1)
+		for (int32_t tile = 0; tile < ntiles; tile++)
 		{
-			for (uint32_t tx = 0; tx < inst.coarse_tiles_width; tx++)
+			PassCtx P = shared;
+			uint32_t tx = uint32_t(tile) % inst.coarse_tiles_width, ty = uint32_t(tile) / inst.coarse_tiles_width;
 			{
 				int32_t lo0 = inst.base_x + int32_t(tx << ts), lo1 = inst.base_y + int32_t(ty << ts);
 				int32_t hi0 = lo0 + (1 << ts) - 1, hi1 = lo1 + (1 << ts) - 1;
@@ -1601,11 +1608,14 @@ struct Backend
 	{
 		if (!rp || rp->num_primitives == 0)
 			return 0;
-		PassCtx P;
+		std::vector<pgs_primitive_attribute> prims(rp->prims, rp->prims + rp->num_primitives);
+		std::vector<Setup> setup(rp->num_primitives);
+		std::vector<TAttr> tattr(rp->num_primitives);
+		PassCtx P = {};
 		P.rp = rp;
-		P.prims.assign(rp->prims, rp->prims + rp->num_primitives);
-		P.setup.resize(rp->num_primitives);
-		P.tattr.resize(rp->num_primitives);
+		P.prims = prims.data();
+		P.setup = setup.data();
+		P.tattr = tattr.data();
 		P.has_ss_reference = num_planes > 1;
 		P.has_aa1 = rp->has_aa1;
 		P.has_scanmsk = rp->has_scanmsk;
@@ -1618,8 +1628,9 @@ struct Backend
 			srx = std::max<int>(srx, int(rp->instances[i].sampling_rate_x_log2));
 			sry = std::max<int>(sry, int(rp->instances[i].sampling_rate_y_log2));
 		}
+		#pragma omp parallel for schedule(static)
 		for (uint32_t i = 0; i < rp->num_primitives; i++)
-			triangle_setup(i, rp->positions, rp->attributes, P.prims[i], P.setup[i], P.tattr[i], fbmasks, srx, sry);
+			triangle_setup(i, rp->positions, rp->attributes, prims[i], setup[i], tattr[i], fbmasks, srx, sry);
 
 		// Instance ordering (gs/gs_renderer.cpp:3190-3266).
 		if (rp->num_instances == 1)
@@ -1994,7 +2005,7 @@ void *pgs_oracle_backend_create(const pgs_backend_ops **ops)
 
 uint64_t pgs_oracle_fragment_count(void *backend)
 {
-	return static_cast<Backend *>(backend)->fragments;
+	return static_cast<Backend *>(backend)->fragments.load();
 }
 
 // Direct access to the restated swizzle for known-answer tests.

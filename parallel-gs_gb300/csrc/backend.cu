@@ -132,6 +132,9 @@ struct CudaBackend
 	uint32_t launch_counter = 0;
 	cudaEvent_t shade_ev[2] = {};
 	float last_shade_ms = 0.0f;
+	bool shade_timing = false;
+	bool shade_started = false;
+	uint64_t h2d_bytes = 0, d2h_bytes = 0, total_launches = 0, render_passes = 0;
 
 	// ------------------------------------------------------------------
 	int init(const pgs_cuda_backend_options *opt)
@@ -267,6 +270,7 @@ struct CudaBackend
 	{
 		if (size)
 			CUDA_TRY(cudaMemcpyAsync(d_arena + off, h_arena + off, size, cudaMemcpyHostToDevice, stream));
+		h2d_bytes += size;
 		return PGS_OK;
 	}
 
@@ -498,6 +502,11 @@ struct CudaBackend
 		launch_counter++;
 		uint32_t subtiles = 1u << (2 * (p.tile_size_log2 - 3));
 		uint32_t grid = uint32_t(tiles) * subtiles;
+		if (shade_timing && !shade_started)
+		{
+			CUDA_TRY(cudaEventRecordWithFlags(shade_ev[0], stream, cudaEventRecordExternal));
+			shade_started = true;
+		}
 		if (I.rate_y_log2 != 0)
 		{
 			switch (ns_log2)
@@ -513,6 +522,8 @@ struct CudaBackend
 		shade_kernel<1, false><<<grid, 64, 0, stream>>>(P, I, d_masks, d_flags);
 		launch_counter++;
 		CUDA_TRY(cudaGetLastError());
+		if (shade_timing)
+			CUDA_TRY(cudaEventRecordWithFlags(shade_ev[1], stream, cudaEventRecordExternal));
 		return PGS_OK;
 	}
 
@@ -549,6 +560,7 @@ struct CudaBackend
 
 	int execute_pass(const PassOp &p)
 	{
+		render_passes++;
 		PassParams P = {};
 		P.pos = reinterpret_cast<const pgs_vertex_position *>(d_arena + p.pos_off);
 		P.attr = reinterpret_cast<const pgs_vertex_attribute *>(d_arena + p.attr_off);
@@ -684,6 +696,9 @@ struct CudaBackend
 			return PGS_ERROR_INVALID_ARGUMENT;
 		CUDA_TRY(cudaMemcpyAsync(dst, d_vram + size_t(plane) * VRAM_SIZE + off, size, cudaMemcpyDeviceToHost, stream));
 		CUDA_TRY(cudaStreamSynchronize(stream));
+		d2h_bytes += size;
+		total_launches += launch_counter;
+		launch_counter = 0;
 		if (!recording)
 			arena_used = 0;
 		return PGS_OK;
@@ -751,6 +766,7 @@ struct CudaBackend
 	int replay_once(bool reset)
 	{
 		launch_counter = 0;
+		shade_started = false;
 		if (reset && d_reset_vram)
 		{
 			CUDA_TRY(cudaMemcpyAsync(d_vram, d_reset_vram, size_t(reset_planes) * VRAM_SIZE, cudaMemcpyDeviceToDevice, stream));
@@ -799,6 +815,7 @@ struct CudaBackend
 		}
 		for (uint32_t i = 0; i < count; i++)
 			CUDA_TRY(cudaGraphLaunch(graph_exec, stream));
+		total_launches += uint64_t(count) * launches_per_replay;
 		return PGS_OK;
 	}
 };
@@ -875,7 +892,39 @@ int pgs_cuda_backend_last_shade_ms(void *backend, float *ms)
 {
 	if (!backend || !ms)
 		return PGS_ERROR_INVALID_ARGUMENT;
-	*ms = B(backend)->last_shade_ms;
+	CudaBackend *b = B(backend);
+	if (!b->shade_timing)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if (cudaEventSynchronize(b->shade_ev[1]) != cudaSuccess)
+		return PGS_ERROR_CUDA;
+	if (cudaEventElapsedTime(ms, b->shade_ev[0], b->shade_ev[1]) != cudaSuccess)
+		return PGS_ERROR_CUDA;
+	return PGS_OK;
+}
+
+int pgs_cuda_backend_get_stats(void *backend, pgs_backend_stats *stats)
+{
+	if (!backend || !stats)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	CudaBackend *b = B(backend);
+	stats->h2d_bytes = b->h2d_bytes;
+	stats->d2h_bytes = b->d2h_bytes;
+	stats->kernel_launches = b->total_launches + b->launch_counter;
+	stats->render_passes = b->render_passes;
+	return PGS_OK;
+}
+
+int pgs_cuda_backend_set_shade_timing(void *backend, int enable)
+{
+	if (!backend)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	CudaBackend *b = B(backend);
+	b->shade_timing = enable != 0;
+	if (b->graph_exec)
+	{
+		cudaGraphExecDestroy(b->graph_exec);
+		b->graph_exec = nullptr;
+	}
 	return PGS_OK;
 }
 int pgs_cuda_backend_fragment_count(void *backend, uint64_t *count)

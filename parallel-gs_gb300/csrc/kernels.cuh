@@ -1209,6 +1209,7 @@ __global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstanc
 
 	const uint32_t *mask = tile_masks + size_t(tile) * I.mask_words;
 	uint32_t word = 0;
+	uint32_t covered = 0;
 	if (t == 0)
 		s_word = 0;
 	__syncthreads();
@@ -1277,6 +1278,7 @@ __global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstanc
 			Request q = shade_early(C, s, st, S, opaque);
 			if (q.coverage > 0)
 			{
+				covered++;
 				if (q.z_test && !S.pending.z_write)
 				{
 					q.z_test = false;
@@ -1337,6 +1339,16 @@ __global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstanc
 
 	if (S.pending.coverage > 0)
 		shade_resolve(C, S);
+
+	// Covered-sample counter: one atomic per warp.
+	{
+		uint32_t c = covered;
+		#pragma unroll
+		for (int o = 16; o >= 1; o >>= 1)
+			c += __shfl_xor_sync(0xffffffffu, c, o);
+		if ((t & 31u) == 0 && c)
+			atomicAdd(P.fragment_counter, (unsigned long long)c);
+	}
 
 	// end_tile
 	const unsigned full = 0xffffffffu;

@@ -56,11 +56,17 @@ class CudaBackendOptions(C.Structure):
     _fields_ = [("device", C.c_int), ("max_samples_log2", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class BackendStats(C.Structure):
+    _fields_ = [("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("kernel_launches", C.c_uint64),
+                ("render_passes", C.c_uint64)]
+
+
 # Every C-ABI symbol include/pgs.h declares.
 EXPORTED_SYMBOLS = [
     "pgs_cuda_backend_create", "pgs_cuda_backend_begin_record", "pgs_cuda_backend_end_record",
     "pgs_cuda_backend_replay", "pgs_cuda_backend_stream", "pgs_cuda_backend_launches_per_replay",
-    "pgs_cuda_backend_last_shade_ms", "pgs_cuda_backend_fragment_count",
+    "pgs_cuda_backend_last_shade_ms", "pgs_cuda_backend_fragment_count", "pgs_cuda_backend_get_stats",
+    "pgs_cuda_backend_set_shade_timing",
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
     "pgs_gs_read_vram", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
     "pgs_gs_set_super_sampling_rate",
@@ -90,6 +96,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.pgs_cuda_backend_launches_per_replay.restype = u32
     lib.pgs_cuda_backend_last_shade_ms.argtypes = [vp, C.POINTER(C.c_float)]
     lib.pgs_cuda_backend_fragment_count.argtypes = [vp, C.POINTER(u64)]
+    lib.pgs_cuda_backend_get_stats.argtypes = [vp, C.POINTER(BackendStats)]
+    lib.pgs_cuda_backend_set_shade_timing.argtypes = [vp, i32]
     lib.pgs_gs_create.argtypes = [vp, vp, C.POINTER(GSOptions), C.POINTER(i32)]
     lib.pgs_gs_create.restype = vp
     lib.pgs_gs_destroy.argtypes = [vp]
@@ -175,6 +183,25 @@ class CudaBackend(Backend):
 
     def launches_per_replay(self) -> int:
         return int(self.lib.pgs_cuda_backend_launches_per_replay(self.handle))
+
+    def fragments(self) -> int:
+        v = C.c_uint64(0)
+        check(self.lib.pgs_cuda_backend_fragment_count(self.handle, C.byref(v)), "fragment_count")
+        return int(v.value)
+
+    def stats(self) -> dict:
+        st = BackendStats()
+        check(self.lib.pgs_cuda_backend_get_stats(self.handle, C.byref(st)), "get_stats")
+        return {"h2d_bytes": st.h2d_bytes, "d2h_bytes": st.d2h_bytes, "kernel_launches": st.kernel_launches,
+                "render_passes": st.render_passes}
+
+    def set_shade_timing(self, enable: bool) -> None:
+        check(self.lib.pgs_cuda_backend_set_shade_timing(self.handle, int(enable)), "set_shade_timing")
+
+    def last_shade_ms(self) -> float:
+        v = C.c_float(0)
+        check(self.lib.pgs_cuda_backend_last_shade_ms(self.handle, C.byref(v)), "last_shade_ms")
+        return float(v.value)
 
 
 class GSInterface:

@@ -14,11 +14,16 @@ pytestmark = pytest.mark.gpu
 
 
 def run_both(frame):
-    ref = pgs_oracle.render(frame, planes=True)
+    obe = pgs_oracle.OracleBackend()
+    ref = pgs_oracle.render(frame, obe, planes=True)
+    ofrags = obe.fragments()
+    obe.close()
     be = pgs.CudaBackend(0, max_samples_log2=4)
     try:
         out = pgs_oracle.render(frame, be, planes=True)
         assert be.error_flags() == 0
+        # Covered samples counted by the shading kernels equal the oracle's.
+        assert be.fragments() == ofrags
     finally:
         be.close()
     return ref, out
@@ -45,3 +50,38 @@ def test_c2_textured_blended_small(ss):
     f = gsgen.frame_c2(seed=5, num_triangles=400, num_sprites=40, super_sampling=ss, num_textures=2)
     ref, out = run_both(f)
     assert_same(ref, out)
+
+
+def test_c1_full_size():
+    """Plain method at its benchmark size: 10k triangles, 640x448, 1x."""
+    ref, out = run_both(gsgen.frame_c1(seed=1))
+    assert_same(ref, out)
+
+
+def test_c2_full_size():
+    """Textured and blended at its benchmark size: 50k triangles + 2k sprites, 4x SSAA."""
+    ref, out = run_both(gsgen.frame_c2(seed=2))
+    assert_same(ref, out)
+
+
+def test_record_replay_reproduces_frame():
+    """A recorded frame program replayed (plain and as a CUDA graph) from its
+    starting VRAM reproduces the recorded result on every plane."""
+    f = gsgen.frame_c2(seed=9, num_triangles=3000, num_sprites=100, super_sampling=4, num_textures=3)
+    be = pgs.CudaBackend(0, max_samples_log2=4)
+    try:
+        gs = pgs.GSInterface(be, super_sampling=4)
+        be.begin_record()
+        gs.gif_transfer(0, f.data)
+        gs.flush()
+        be.end_record()
+        first = np.stack([be.read_plane(p) for p in range(6)])
+        be.replay(1, reset_vram=True, use_graph=False)
+        again = np.stack([be.read_plane(p) for p in range(6)])
+        be.replay(3, reset_vram=True, use_graph=True)
+        graph = np.stack([be.read_plane(p) for p in range(6)])
+        gs.close()
+    finally:
+        be.close()
+    assert np.array_equal(first, again)
+    assert np.array_equal(first, graph)
