@@ -504,7 +504,9 @@ struct CudaBackend
 		uint32_t grid = uint32_t(tiles) * subtiles;
 		if (shade_timing && !shade_started)
 		{
-			CUDA_TRY(cudaEventRecordWithFlags(shade_ev[0], stream, cudaEventRecordExternal));
+			int r = record_timing_event(shade_ev[0]);
+			if (r)
+				return r;
 			shade_started = true;
 		}
 		if (I.rate_y_log2 != 0)
@@ -523,7 +525,20 @@ struct CudaBackend
 		launch_counter++;
 		CUDA_TRY(cudaGetLastError());
 		if (shade_timing)
-			CUDA_TRY(cudaEventRecordWithFlags(shade_ev[1], stream, cudaEventRecordExternal));
+			return record_timing_event(shade_ev[1]);
+		return PGS_OK;
+	}
+
+	// Inside stream capture the event must be recorded as an external node so
+	// that every graph launch records it; outside capture a plain record.
+	int record_timing_event(cudaEvent_t ev)
+	{
+		cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+		CUDA_TRY(cudaStreamIsCapturing(stream, &cs));
+		if (cs == cudaStreamCaptureStatusActive)
+			CUDA_TRY(cudaEventRecordWithFlags(ev, stream, cudaEventRecordExternal));
+		else
+			CUDA_TRY(cudaEventRecord(ev, stream));
 		return PGS_OK;
 	}
 
