@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--sprites", type=int, default=2000)
     ap.add_argument("--super-sampling", type=int, default=4)
     ap.add_argument("--no-verify", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="skip the CPU baseline and the e2e leg (profiling runs)")
     return ap.parse_args()
 
 
@@ -255,7 +256,7 @@ def main():
     fps = world * args.steps / (total_ms / 1000.0)
 
     # End to end through the public API from host memory.
-    e2e_steps = max(3, min(args.steps, 10))
+    e2e_steps = 0 if args.quick else max(3, min(args.steps, 10))
     vram = np.empty(pgs.VRAM_SIZE, dtype=np.uint8)
     gs2 = pgs.GSInterface(backend, super_sampling=frame.super_sampling)
     gs2.gif_transfer(0, frame.data)
@@ -268,9 +269,9 @@ def main():
         gs2.read_vram(out=vram)
     e2e_dt = time.perf_counter() - t0
     st1 = backend.stats()
-    h2d = (st1["h2d_bytes"] - st0["h2d_bytes"]) // e2e_steps
-    d2h = (st1["d2h_bytes"] - st0["d2h_bytes"]) // e2e_steps
-    e2e_fps = world * e2e_steps / e2e_dt
+    h2d = (st1["h2d_bytes"] - st0["h2d_bytes"]) // max(e2e_steps, 1)
+    d2h = (st1["d2h_bytes"] - st0["d2h_bytes"]) // max(e2e_steps, 1)
+    e2e_fps = world * e2e_steps / e2e_dt if e2e_steps else None
     gs2.close()
 
     if rank != 0:
@@ -288,7 +289,7 @@ def main():
     frags = frags_per_frame
     shade_s = statistics.mean(shade_ms) / 1000.0
     achieved = ab["shade"] / shade_s / 1e9
-    cpu = cpu_baseline_sample(frame)
+    cpu = None if args.quick else cpu_baseline_sample(frame)
     out = {
         "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
