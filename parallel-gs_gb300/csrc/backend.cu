@@ -484,7 +484,11 @@ struct CudaBackend
 		I.prim_lo = lo;
 		I.prim_count = count;
 		I.mask_words = (count + 31) / 32;
+		I.summary_words = (I.mask_words + 31) / 32;
+		I.sub_w = I.tiles_w << (p.tile_size_log2 - 3);
+		I.sub_h = I.tiles_h << (p.tile_size_log2 - 3);
 		size_t tiles = size_t(I.tiles_w) * I.tiles_h;
+		size_t subs = size_t(I.sub_w) * I.sub_h;
 		if (tiles == 0 || count == 0)
 			return PGS_OK;
 		uint32_t ns_log2 = I.rate_x_log2 + I.rate_y_log2;
@@ -493,15 +497,16 @@ struct CudaBackend
 		// Super-sampled shading touches planes 1 .. 1 + 2^ns_log2.
 		if (I.rate_y_log2 != 0 && 2u + (1u << ns_log2) > num_planes)
 			return PGS_ERROR_INVALID_ARGUMENT;
-		int r = ensure_masks(tiles * I.mask_words, tiles);
+		size_t mask_words = subs * I.mask_words, summary_words = subs * I.summary_words;
+		int r = ensure_masks(mask_words + summary_words, tiles);
 		if (r)
 			return r;
-		CUDA_TRY(cudaMemsetAsync(d_masks, 0, tiles * I.mask_words * sizeof(uint32_t), stream));
+		uint32_t *d_sub_masks = d_masks, *d_sub_summary = d_masks + mask_words;
+		CUDA_TRY(cudaMemsetAsync(d_masks, 0, (mask_words + summary_words) * sizeof(uint32_t), stream));
 		CUDA_TRY(cudaMemsetAsync(d_flags, 0, tiles * sizeof(uint32_t), stream));
-		bin_kernel<<<(count + 127) / 128, 128, 0, stream>>>(P, I, d_masks, d_flags);
+		bin_kernel<<<(count + 127) / 128, 128, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags);
 		launch_counter++;
-		uint32_t subtiles = 1u << (2 * (p.tile_size_log2 - 3));
-		uint32_t grid = uint32_t(tiles) * subtiles;
+		uint32_t grid = uint32_t(subs);
 		if (shade_timing && !shade_started)
 		{
 			int r = record_timing_event(shade_ev[0]);
@@ -513,15 +518,15 @@ struct CudaBackend
 		{
 			switch (ns_log2)
 			{
-			case 1: shade_kernel<2, true><<<grid, 128, 0, stream>>>(P, I, d_masks, d_flags); break;
-			case 2: shade_kernel<4, true><<<grid, 256, 0, stream>>>(P, I, d_masks, d_flags); break;
-			case 3: shade_kernel<8, true><<<grid, 512, 0, stream>>>(P, I, d_masks, d_flags); break;
-			case 4: shade_kernel<16, true><<<grid, 1024, 0, stream>>>(P, I, d_masks, d_flags); break;
+			case 1: shade_kernel<2, true><<<grid, 128, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags); break;
+			case 2: shade_kernel<4, true><<<grid, 256, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags); break;
+			case 3: shade_kernel<8, true><<<grid, 512, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags); break;
+			case 4: shade_kernel<16, true><<<grid, 1024, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags); break;
 			default: return PGS_ERROR_INVALID_ARGUMENT;
 			}
 			launch_counter++;
 		}
-		shade_kernel<1, false><<<grid, 64, 0, stream>>>(P, I, d_masks, d_flags);
+		shade_kernel<1, false><<<grid, 64, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags);
 		launch_counter++;
 		CUDA_TRY(cudaGetLastError());
 		if (shade_timing)

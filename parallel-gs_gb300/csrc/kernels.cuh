@@ -59,7 +59,9 @@ struct DevInstance
 	uint32_t preserve_samples;
 	uint32_t instance;
 	uint32_t prim_lo, prim_count; // primitive range of this dispatch
-	uint32_t mask_words;          // bitmask words per tile
+	uint32_t mask_words;          // bitmask words per 8x8 sub-tile (1 bit per primitive)
+	uint32_t summary_words;       // summary words per sub-tile (1 bit per mask word)
+	uint32_t sub_w, sub_h;        // 8x8 sub-tiles per row / column
 };
 
 struct PassParams
@@ -536,8 +538,13 @@ __device__ __forceinline__ bool intersects_tile(const PrimSetup &s, int32_t lo0,
 }
 
 // ---------------------------------------------------------------------------
-// K2: binning into per-tile primitive bitmasks.
-__global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, uint32_t *tile_masks, uint32_t *tile_flags)
+// K2: binning.  Coarse tiles (2^tile_size_log2 pixels) carry the reference's
+// membership test and super-sampling flags (binning.comp:74-125); shading
+// lists are kept per 8x8 sub-tile as bitmasks over the pass's primitive range
+// so that ascending primitive order needs no sort.  A summary bitmask marks
+// non-empty mask words.
+__global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, uint32_t *sub_masks,
+                                                  uint32_t *sub_summary, uint32_t *tile_flags)
 {
 	uint32_t local = blockIdx.x * blockDim.x + threadIdx.x;
 	if (local >= I.prim_count)
@@ -550,11 +557,10 @@ __global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, u
 	if (s.bb[2] < s.bb[0] || s.bb[3] < s.bb[1])
 		return;
 
-	int ts = int(P.tile_size_log2);
-	int32_t tx0 = (s.bb[0] - I.base_x) >> ts, ty0 = (s.bb[1] - I.base_y) >> ts;
-	int32_t tx1 = (s.bb[2] - I.base_x) >> ts, ty1 = (s.bb[3] - I.base_y) >> ts;
-	tx0 = max(tx0, 0); ty0 = max(ty0, 0);
-	tx1 = min(tx1, int32_t(I.tiles_w) - 1); ty1 = min(ty1, int32_t(I.tiles_h) - 1);
+	const int ts = int(P.tile_size_log2);
+	int32_t tx0 = max((s.bb[0] - I.base_x) >> ts, 0), ty0 = max((s.bb[1] - I.base_y) >> ts, 0);
+	int32_t tx1 = min((s.bb[2] - I.base_x) >> ts, int32_t(I.tiles_w) - 1);
+	int32_t ty1 = min((s.bb[3] - I.base_y) >> ts, int32_t(I.tiles_h) - 1);
 
 	bool ms_tri = ((pa.state >> STATE_BIT_MULTISAMPLE) & 1) && !((pa.state >> STATE_BIT_LINE) & 1);
 	uint32_t flags = TILE_NONEMPTY;
@@ -567,18 +573,34 @@ __global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, u
 		if (pa.state & (1u << STATE_BIT_Z_WRITE)) flags |= TILE_HAS_ZW;
 		if (pa.tex & TEX_PER_SAMPLE_BIT) flags |= TILE_REQ_SS;
 	}
-	uint32_t word = local >> 5, bit = 1u << (local & 31u);
+	const uint32_t word = local >> 5, bit = 1u << (local & 31u);
+	const uint32_t sword = word >> 5, sbit = 1u << (word & 31u);
 	for (int32_t ty = ty0; ty <= ty1; ty++)
 	{
 		for (int32_t tx = tx0; tx <= tx1; tx++)
 		{
 			int32_t lo0 = I.base_x + (tx << ts), lo1 = I.base_y + (ty << ts);
-			if (intersects_tile(s, lo0, lo1, lo0 + (1 << ts) - 1, lo1 + (1 << ts) - 1, ms_tri))
+			int32_t hi0 = lo0 + (1 << ts) - 1, hi1 = lo1 + (1 << ts) - 1;
+			if (!intersects_tile(s, lo0, lo1, hi0, hi1, ms_tri))
+				continue;
+			uint32_t tile = uint32_t(ty) * I.tiles_w + uint32_t(tx);
+			if ((tile_flags[tile] & flags) != flags)
+				atomicOr(&tile_flags[tile], flags);
+
+			int32_t gx0 = (max(s.bb[0], lo0) - I.base_x) >> 3, gx1 = (min(s.bb[2], hi0) - I.base_x) >> 3;
+			int32_t gy0 = (max(s.bb[1], lo1) - I.base_y) >> 3, gy1 = (min(s.bb[3], hi1) - I.base_y) >> 3;
+			for (int32_t gy = gy0; gy <= gy1; gy++)
 			{
-				uint32_t tile = uint32_t(ty) * I.tiles_w + uint32_t(tx);
-				atomicOr(&tile_masks[size_t(tile) * I.mask_words + word], bit);
-				if ((tile_flags[tile] & flags) != flags)
-					atomicOr(&tile_flags[tile], flags);
+				for (int32_t gx = gx0; gx <= gx1; gx++)
+				{
+					int32_t sx = I.base_x + (gx << 3), sy = I.base_y + (gy << 3);
+					if (!intersects_tile(s, sx, sy, sx + 7, sy + 7, ms_tri))
+						continue;
+					size_t sub = size_t(gy) * I.sub_w + size_t(gx);
+					uint32_t old = atomicOr(&sub_masks[sub * I.mask_words + word], bit);
+					if (old == 0u)
+						atomicOr(&sub_summary[sub * I.summary_words + sword], sbit);
+				}
 			}
 		}
 	}
@@ -1065,9 +1087,6 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 	return r;
 }
 
-// Maximum primitives staged per list chunk in shared memory.
-constexpr int SHADE_CHUNK = 256;
-
 // Sample position within its pixel for sample s (32-wide subgroup layout of
 // ubershader.comp get_tile_info).
 __device__ __forceinline__ void sample_offset(uint32_t s, uint32_t xl, uint32_t yl, int32_t &ox, int32_t &oy)
@@ -1087,29 +1106,102 @@ __device__ __forceinline__ void sample_offset(uint32_t s, uint32_t xl, uint32_t 
 	}
 }
 
-// One CTA per 8x8-pixel sub-tile of a coarse tile; NS samples per pixel, one
-// thread per sample.  SS selects the super-sampled path; tiles whose flags
-// select the other path exit immediately.
-template <int NS, bool SS>
-__global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstance I, const uint32_t *tile_masks,
-                                                        const uint32_t *tile_flags)
+// Processes one primitive for the calling warp: coverage, early depth,
+// deferred-shading bookkeeping (ubershader.comp:1694-1812).  Warp-uniform.
+template <bool SS>
+__device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi, SampleState &S, uint32_t &covered,
+                                                  int32_t wlo0, int32_t wlo1, int32_t whi0, int32_t whi1)
 {
-	__shared__ uint32_t s_list[SHADE_CHUNK];
-	__shared__ int s_count;
-	__shared__ uint32_t s_word;
-
-	const uint32_t subtiles_per_tile_log2 = 2u * (P.tile_size_log2 - 3u);
-	uint32_t tile = blockIdx.x >> subtiles_per_tile_log2;
-	uint32_t sub = blockIdx.x & ((1u << subtiles_per_tile_log2) - 1u);
-	if (tile >= I.tiles_w * I.tiles_h)
+	const PassParams &P = *C.P;
+	const PrimSetup s = P.setup[pi];
+	if (s.bb[2] < wlo0 || s.bb[0] > whi0 || s.bb[3] < wlo1 || s.bb[1] > whi1)
 		return;
-	uint32_t flags = tile_flags[tile];
+	uint32_t st = P.prims[pi].state;
+	bool opaque;
+	Request q = shade_early(C, s, st, S, opaque);
+	bool any_cov = __any_sync(0xffffffffu, q.coverage > 0);
+	if (!any_cov)
+		return;
+	if (q.coverage > 0)
+	{
+		covered++;
+		if (q.z_test && !S.pending.z_write)
+		{
+			q.z_test = false;
+			bool zp = q.z_greater ? q.z > S.depth : q.z >= S.depth;
+			if (zp)
+			{
+				if (q.z_write && opaque)
+				{
+					q.z_write = false;
+					S.depth = q.z;
+					S.depth_dirty = true;
+				}
+			}
+			else
+			{
+				q.coverage = 0;
+				q.z_write = false;
+			}
+		}
+		else if (q.z_write && !q.z_test && opaque)
+		{
+			q.z_write = false;
+			S.pending.z_write = false;
+			S.depth = q.z;
+			S.depth_dirty = true;
+		}
+		if ((q.z_test || !q.z_write) && S.pending.z_write)
+			opaque = false;
+	}
+	bool need_flush = false;
+	if (q.coverage > 0)
+	{
+		need_flush = !opaque && S.pending.coverage > 0;
+		if (!need_flush)
+		{
+			S.pending = q;
+			S.pending_prim = pi;
+			q.coverage = 0;
+		}
+	}
+	if (__any_sync(0xffffffffu, need_flush))
+	{
+		if (S.pending.coverage > 0)
+			shade_resolve(C, S);
+		S.pending.coverage = 0;
+		S.pending.z_write = false;
+		if (q.coverage > 0)
+		{
+			S.pending = q;
+			S.pending_prim = pi;
+		}
+	}
+}
+
+// One CTA per 8x8-pixel sub-tile, NS samples per pixel, one thread per sample.
+// Each warp walks the sub-tile's primitive bitmask on its own (no shared
+// memory, no barriers).  SS selects the super-sampled path; sub-tiles whose
+// coarse tile selects the other path exit immediately.
+template <int NS, bool SS>
+__global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstance I, const uint32_t *sub_masks,
+                                                        const uint32_t *sub_summary, const uint32_t *tile_flags)
+{
+	const uint32_t sub = blockIdx.x;
+	if (sub >= I.sub_w * I.sub_h)
+		return;
+	const uint32_t gx = sub % I.sub_w, gy = sub / I.sub_w;
+	const uint32_t sh = P.tile_size_log2 - 3u;
+	const uint32_t tile = (gy >> sh) * I.tiles_w + (gx >> sh);
+	const uint32_t flags = tile_flags[tile];
 	if (!(flags & TILE_NONEMPTY))
 		return;
 	bool req = (flags & TILE_REQ_SS) || ((flags & TILE_REQ_SS_ZW) && (flags & TILE_HAS_ZW));
 	bool ss_tile = I.rate_y_log2 != 0 && req;
 	if (ss_tile != SS)
 		return;
+	const uint32_t *summary = sub_summary + size_t(sub) * I.summary_words;
+	const uint32_t *mask = sub_masks + size_t(sub) * I.mask_words;
 
 	ShadeCtx C;
 	C.P = &P;
@@ -1121,19 +1213,16 @@ __global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstanc
 	C.fb_psm = I.fb_psm;
 	C.zb_psm = I.zb_psm;
 
-	uint32_t tx = tile % I.tiles_w, ty = tile / I.tiles_w;
-	uint32_t sub_per_row = 1u << (P.tile_size_log2 - 3u);
-	int32_t sub_x = I.base_x + int32_t(tx << P.tile_size_log2) + int32_t((sub % sub_per_row) * 8u);
-	int32_t sub_y = I.base_y + int32_t(ty << P.tile_size_log2) + int32_t((sub / sub_per_row) * 8u);
-
-	uint32_t t = threadIdx.x;
-	uint32_t sample = t % NS;
-	uint32_t pix = t / NS;
-	// Pixel order inside the 8x8 sub-tile: x from bits 0,2,4 and y from bits 1,3,5
-	// so that a warp's pixels form a compact block.
-	int32_t lx = int32_t((pix & 1u) | ((pix >> 1) & 2u) | ((pix >> 2) & 4u));
-	int32_t ly = int32_t(((pix >> 1) & 1u) | ((pix >> 2) & 2u) | ((pix >> 3) & 4u));
-	int32_t px = sub_x + lx, py = sub_y + ly;
+	const int32_t sub_x = I.base_x + int32_t(gx * 8u), sub_y = I.base_y + int32_t(gy * 8u);
+	const uint32_t t = threadIdx.x;
+	const uint32_t lane = t & 31u;
+	const uint32_t sample = t % NS;
+	const uint32_t pix = t / NS;
+	// Pixel order inside the sub-tile: x from bits 0,2,4 and y from bits 1,3,5,
+	// so that each warp covers a compact block.
+	const int32_t lx = int32_t((pix & 1u) | ((pix >> 1) & 2u) | ((pix >> 2) & 4u));
+	const int32_t ly = int32_t(((pix >> 1) & 1u) | ((pix >> 2) & 2u) | ((pix >> 3) & 4u));
+	const int32_t px = sub_x + lx, py = sub_y + ly;
 
 	SampleState S;
 	int32_t ox = 0, oy = 0;
@@ -1147,8 +1236,8 @@ __global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstanc
 	S.pending.z_write = false;
 	S.pending_prim = 0;
 
-	uint32_t fb_index = swizzle_address(uint32_t(px), uint32_t(py), I.fb_base, I.fb_stride, I.fb_psm);
-	uint32_t z_index = C.zs ? swizzle_address(uint32_t(px), uint32_t(py), I.zb_base, I.fb_stride, I.zb_psm) : 0u;
+	const uint32_t fb_index = swizzle_address(uint32_t(px), uint32_t(py), I.fb_base, I.fb_stride, I.fb_psm);
+	const uint32_t z_index = C.zs ? swizzle_address(uint32_t(px), uint32_t(py), I.zb_base, I.fb_stride, I.zb_psm) : 0u;
 	const uint32_t V32 = VRAM_SIZE / 4, V16 = VRAM_SIZE / 2;
 	uint32_t *vram32 = reinterpret_cast<uint32_t *>(P.vram);
 	uint16_t *vram16 = reinterpret_cast<uint16_t *>(P.vram);
@@ -1194,8 +1283,7 @@ __global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstanc
 	else
 		S.depth = 0;
 
-	// Warp pixel rectangle for the per-warp primitive test.
-	uint32_t lane = t & 31u;
+	// Pixel rectangle of this warp.
 	int32_t wlo0 = px, wlo1 = py, whi0 = px, whi1 = py;
 	#pragma unroll
 	for (int o = 16; o >= 1; o >>= 1)
@@ -1205,136 +1293,34 @@ __global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstanc
 		whi0 = max(whi0, __shfl_xor_sync(0xffffffffu, whi0, o));
 		whi1 = max(whi1, __shfl_xor_sync(0xffffffffu, whi1, o));
 	}
-	(void)lane;
 
-	const uint32_t *mask = tile_masks + size_t(tile) * I.mask_words;
-	uint32_t word = 0;
+	// Walk the primitive list in ascending order: summary word -> mask words -> bits.
 	uint32_t covered = 0;
-	if (t == 0)
-		s_word = 0;
-	__syncthreads();
-
-	while (true)
+	for (uint32_t sbase = 0; sbase < I.summary_words; sbase += 32u)
 	{
-		// Warp 0 gathers the next chunk of primitive indices in ascending order.
-		if (t < 32)
+		uint32_t sv = (sbase + lane < I.summary_words) ? __ldg(summary + sbase + lane) : 0u;
+		uint32_t nz_lanes = __ballot_sync(0xffffffffu, sv != 0u);
+		while (nz_lanes)
 		{
-			int count = 0;
-			uint32_t w = s_word;
-			while (w < I.mask_words)
+			int l = __ffs(nz_lanes) - 1;
+			nz_lanes &= nz_lanes - 1u;
+			uint32_t words = __shfl_sync(0xffffffffu, sv, l);
+			uint32_t word_base = (sbase + uint32_t(l)) * 32u;
+			uint32_t mw = ((words >> lane) & 1u) ? __ldg(mask + word_base + lane) : 0u;
+			while (words)
 			{
-				uint32_t idx = w + t;
-				uint32_t m = idx < I.mask_words ? mask[idx] : 0u;
-				int n = __popc(m);
-				int incl = n;
-				#pragma unroll
-				for (int o = 1; o < 32; o <<= 1)
+				int j = __ffs(words) - 1;
+				words &= words - 1u;
+				uint32_t m = __shfl_sync(0xffffffffu, mw, j);
+				uint32_t prim_base = I.prim_lo + (word_base + uint32_t(j)) * 32u;
+				while (m)
 				{
-					int v = __shfl_up_sync(0xffffffffu, incl, o);
-					if (int(t) >= o)
-						incl += v;
-				}
-				// Inclusive sums grow with the lane, so the words that fit form a prefix.
-				bool fits = count + incl <= SHADE_CHUNK;
-				int nfit = __popc(__ballot_sync(0xffffffffu, fits));
-				if (fits && m)
-				{
-					int o = count + incl - n;
-					uint32_t mm = m;
-					while (mm)
-					{
-						int b = __ffs(mm) - 1;
-						mm &= mm - 1u;
-						s_list[o++] = I.prim_lo + (idx << 5) + uint32_t(b);
-					}
-				}
-				int last = __shfl_sync(0xffffffffu, incl, max(nfit - 1, 0));
-				int added = nfit ? last : 0;
-				count += added;
-				w += uint32_t(nfit);
-				if (nfit < 32)
-					break;
-			}
-			if (t == 0)
-			{
-				s_count = count;
-				s_word = min(w, I.mask_words);
-			}
-		}
-		__syncthreads();
-		int count = s_count;
-		word = s_word;
-
-		for (int k = 0; k < count; k++)
-		{
-			uint32_t pi = s_list[k];
-			const PrimSetup s = P.setup[pi];
-			uint32_t st = P.prims[pi].state;
-			bool ms_tri = P.has_aa1 && ((st >> STATE_BIT_MULTISAMPLE) & 1) && !((st >> STATE_BIT_LINE) & 1);
-			if (!intersects_tile(s, wlo0, wlo1, whi0, whi1, ms_tri))
-				continue;
-
-			bool opaque;
-			Request q = shade_early(C, s, st, S, opaque);
-			if (q.coverage > 0)
-			{
-				covered++;
-				if (q.z_test && !S.pending.z_write)
-				{
-					q.z_test = false;
-					bool zp = q.z_greater ? q.z > S.depth : q.z >= S.depth;
-					if (zp)
-					{
-						if (q.z_write && opaque)
-						{
-							q.z_write = false;
-							S.depth = q.z;
-							S.depth_dirty = true;
-						}
-					}
-					else
-					{
-						q.coverage = 0;
-						q.z_write = false;
-					}
-				}
-				else if (q.z_write && !q.z_test && opaque)
-				{
-					q.z_write = false;
-					S.pending.z_write = false;
-					S.depth = q.z;
-					S.depth_dirty = true;
-				}
-				if ((q.z_test || !q.z_write) && S.pending.z_write)
-					opaque = false;
-			}
-			bool need_flush = false;
-			if (q.coverage > 0)
-			{
-				need_flush = !opaque && S.pending.coverage > 0;
-				if (!need_flush)
-				{
-					S.pending = q;
-					S.pending_prim = pi;
-					q.coverage = 0;
-				}
-			}
-			if (__any_sync(0xffffffffu, need_flush))
-			{
-				if (S.pending.coverage > 0)
-					shade_resolve(C, S);
-				S.pending.coverage = 0;
-				S.pending.z_write = false;
-				if (q.coverage > 0)
-				{
-					S.pending = q;
-					S.pending_prim = pi;
+					int b = __ffs(m) - 1;
+					m &= m - 1u;
+					process_primitive<SS>(C, prim_base + uint32_t(b), S, covered, wlo0, wlo1, whi0, whi1);
 				}
 			}
 		}
-		__syncthreads();
-		if (word >= I.mask_words)
-			break;
 	}
 
 	if (S.pending.coverage > 0)
@@ -1346,7 +1332,7 @@ __global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstanc
 		#pragma unroll
 		for (int o = 16; o >= 1; o >>= 1)
 			c += __shfl_xor_sync(0xffffffffu, c, o);
-		if ((t & 31u) == 0 && c)
+		if (lane == 0 && c)
 			atomicAdd(P.fragment_counter, (unsigned long long)c);
 	}
 
