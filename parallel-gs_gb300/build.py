@@ -61,7 +61,9 @@ def build_product(verbose: bool = False) -> Path:
     cpp = CSRC / "frontend.cpp"
     o_cu = BUILD / "backend.o"
     o_cpp = BUILD / "frontend.o"
-    if _newer(out, headers + [cu, cpp, Path(__file__)]):
+    stamp = BUILD / "defines.txt"
+    defines = os.environ.get("PGS_NVCC_DEFINES", "")
+    if _newer(out, headers + [cu, cpp, Path(__file__)]) and stamp.exists() and stamp.read_text() == defines:
         return out
     common = ["-I", str(INCLUDE), "-I", str(CSRC)]
     jobs = [
@@ -71,9 +73,13 @@ def build_product(verbose: bool = False) -> Path:
     ]
     if verbose:
         jobs[0].insert(1, "-Xptxas=-v")
+    # Extra compiler definitions for tuning sweeps, e.g. PGS_NVCC_DEFINES="PGS_SHADE_OCC=3".
+    for d in os.environ.get("PGS_NVCC_DEFINES", "").split():
+        jobs[0].insert(1, "-D" + d)
     with ThreadPoolExecutor(max_workers=2) as ex:
         list(ex.map(_run, jobs))
     _run([nvcc, "-shared", "-gencode", GENCODE, "-cudart", "static", str(o_cu), str(o_cpp), "-o", str(out)])
+    stamp.write_text(defines)
     return out
 
 

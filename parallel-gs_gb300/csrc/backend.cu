@@ -63,7 +63,8 @@ enum OpType : uint32_t { OP_COPY = 0, OP_CLUT = 1, OP_PASS = 2 };
 
 struct PassOp
 {
-	size_t pos_off, attr_off, prim_off, states_off, textures_off;
+	size_t pos_off, attr_off, prim_off, states_off, textures_off, images_off;
+	uint32_t num_texels, max_texels;
 	uint32_t num_prims, num_states, num_textures;
 	uint32_t tile_size_log2, has_aa1, has_scanmsk;
 	uint32_t num_instances;
@@ -120,6 +121,8 @@ struct CudaBackend
 	size_t masks_cap = 0;
 	uint32_t *d_flags = nullptr;
 	size_t flags_cap = 0;
+	uint32_t *d_texels = nullptr;
+	size_t texels_cap = 0;
 
 	// Recording.
 	bool recording = false;
@@ -203,6 +206,7 @@ struct CudaBackend
 		cudaFree(d_prims_work);
 		cudaFree(d_masks);
 		cudaFree(d_flags);
+		cudaFree(d_texels);
 		cudaFree(d_arena);
 		cudaFree(d_reset_vram);
 		cudaFree(d_reset_clut);
@@ -311,9 +315,10 @@ struct CudaBackend
 		size_t prim_bytes = size_t(n) * sizeof(pgs_primitive_attribute);
 		size_t st_bytes = size_t(std::max<uint32_t>(rp->num_states, 1)) * sizeof(pgs_state_vector);
 		size_t tex_bytes = size_t(std::max<uint32_t>(rp->num_textures, 1)) * sizeof(pgs_texture_desc);
+		size_t img_bytes = size_t(std::max<uint32_t>(rp->num_textures, 1)) * sizeof(TexImage);
 		size_t base;
 		size_t total = align_up(pos_bytes, 256) + align_up(attr_bytes, 256) + align_up(prim_bytes, 256) +
-		               align_up(st_bytes, 256) + align_up(tex_bytes, 256);
+		               align_up(st_bytes, 256) + align_up(tex_bytes, 256) + align_up(img_bytes, 256);
 		int r = arena_alloc(total, base);
 		if (r)
 			return r;
@@ -329,6 +334,36 @@ struct CudaBackend
 			memcpy(h_arena + p.states_off, rp->states, rp->num_states * sizeof(pgs_state_vector));
 		if (rp->num_textures)
 			memcpy(h_arena + p.textures_off, rp->textures, rp->num_textures * sizeof(pgs_texture_desc));
+		p.images_off = p.textures_off + align_up(tex_bytes, 256);
+		{
+			// Decoded extent covers every texel index the wrap modes can produce.
+			TexImage *im = reinterpret_cast<TexImage *>(h_arena + p.images_off);
+			uint64_t texels = 0;
+			uint32_t max_texels = 0;
+			for (uint32_t i = 0; i < rp->num_textures; i++)
+			{
+				const pgs_texture_desc &t = rp->textures[i];
+				auto extent = [](uint32_t size_log2, uint32_t mode, uint32_t lo, uint32_t hi) {
+					uint32_t size = 1u << std::min<uint32_t>(size_log2, 10);
+					if (mode == WRAP_REGION_CLAMP)
+						return std::max(size, std::max(lo, hi) + 1u);
+					if (mode == WRAP_REGION_REPEAT)
+						return std::max(size, (((size - 1u) & lo) | hi) + 1u);
+					return size;
+				};
+				im[i].ext_u = extent(t.tw_log2, t.wms, t.minu, t.maxu);
+				im[i].ext_v = extent(t.th_log2, t.wmt, t.minv, t.maxv);
+				im[i].offset = uint32_t(texels);
+				im[i].padding = 0;
+				uint32_t n = im[i].ext_u * im[i].ext_v;
+				texels += n;
+				max_texels = std::max(max_texels, n);
+			}
+			if (texels > (uint64_t(1) << 31))
+				return PGS_ERROR_CAPACITY;
+			p.num_texels = uint32_t(texels);
+			p.max_texels = max_texels;
+		}
 		r = upload_arena(base, total);
 		if (r)
 			return r;
@@ -586,6 +621,17 @@ struct CudaBackend
 		P.attr = reinterpret_cast<const pgs_vertex_attribute *>(d_arena + p.attr_off);
 		P.states = reinterpret_cast<const pgs_state_vector *>(d_arena + p.states_off);
 		P.textures = reinterpret_cast<const pgs_texture_desc *>(d_arena + p.textures_off);
+		P.tex_images = reinterpret_cast<const TexImage *>(d_arena + p.images_off);
+		if (p.num_texels > texels_cap)
+		{
+			cudaFree(d_texels);
+			d_texels = nullptr;
+			size_t cap = std::max<size_t>(p.num_texels, texels_cap * 2);
+			CUDA_TRY(cudaMalloc(&d_texels, cap * sizeof(uint32_t)));
+			texels_cap = cap;
+			if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+		}
+		P.texels = d_texels;
 		P.prims = d_prims_work;
 		P.setup = d_setup;
 		P.tattr = d_tattr;
@@ -611,6 +657,12 @@ struct CudaBackend
 		                         cudaMemcpyDeviceToDevice, stream));
 		setup_kernel<<<(p.num_prims + 127) / 128, 128, 0, stream>>>(P);
 		launch_counter++;
+		if (p.num_textures && p.num_texels)
+		{
+			dim3 grid((p.max_texels + 255) / 256, p.num_textures);
+			texture_decode_kernel<<<grid, 256, 0, stream>>>(P);
+			launch_counter++;
+		}
 		CUDA_TRY(cudaGetLastError());
 
 		if (p.num_instances == 1)

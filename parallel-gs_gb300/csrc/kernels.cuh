@@ -64,6 +64,15 @@ struct DevInstance
 	uint32_t sub_w, sub_h;        // 8x8 sub-tiles per row / column
 };
 
+// Linear RGBA8 image decoded from swizzled VRAM + CLUT for one texture of a
+// pass (the role of the reference's texture cache, upload.comp:108-229).
+struct TexImage
+{
+	uint32_t offset; // first texel in PassParams::texels
+	uint32_t ext_u, ext_v;
+	uint32_t padding;
+};
+
 struct PassParams
 {
 	const pgs_vertex_position *pos;
@@ -71,6 +80,8 @@ struct PassParams
 	pgs_primitive_attribute *prims;
 	const pgs_state_vector *states;
 	const pgs_texture_desc *textures;
+	const TexImage *tex_images;
+	uint32_t *texels;
 	PrimSetup *setup;
 	TransformedAttr *tattr;
 	uint32_t num_prims;
@@ -95,6 +106,13 @@ constexpr uint32_t TILE_HAS_ZW = 1u << 3;
 constexpr uint32_t ERROR_FLAG_TILE_OVERFLOW = 1u << 0;
 
 __constant__ uint8_t c_rcp_tab[256];
+
+// Occupancy target of the shading kernels in 256-thread units per SM: 4 means
+// at most 64 registers per thread for the 1x..4x variants.
+#ifndef PGS_SHADE_OCC
+#define PGS_SHADE_OCC 4
+#endif
+#define PGS_SHADE_MIN_BLOCKS(NS) ((NS) <= 4 && PGS_SHADE_OCC > 0 ? (PGS_SHADE_OCC * 4 / (NS)) : 1)
 
 // ---------------------------------------------------------------------------
 // Scalar helpers.
@@ -607,6 +625,10 @@ __global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, u
 }
 
 // ---------------------------------------------------------------------------
+// K5: texture decode.  One thread per texel of every texture of the pass.
+__global__ void __launch_bounds__(256) texture_decode_kernel(PassParams P);
+
+// ---------------------------------------------------------------------------
 // K3: shading.
 struct Request
 {
@@ -695,10 +717,24 @@ __device__ __forceinline__ int32_t wrap_coord(int32_t v, uint32_t mode, uint32_t
 	}
 }
 
+__global__ void __launch_bounds__(256) texture_decode_kernel(PassParams P)
+{
+	const uint32_t tex = blockIdx.y;
+	if (tex >= P.num_textures)
+		return;
+	const TexImage im = P.tex_images[tex];
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= im.ext_u * im.ext_v)
+		return;
+	const pgs_texture_desc t = P.textures[tex];
+	P.texels[im.offset + i] = fetch_texel(P, t, int32_t(i % im.ext_u), int32_t(i / im.ext_u));
+}
+
 // Texture sample at LOD 0 with exact integer filtering.
 __device__ void sample_texture(const PassParams &P, uint32_t tex_word, float u, float v, bool perspective, float out[4])
 {
-	const pgs_texture_desc t = P.textures[min(tex_word & TEX_TEXTURE_INDEX_MASK, P.num_textures - 1u)];
+	const uint32_t tex_index = min(tex_word & TEX_TEXTURE_INDEX_MASK, P.num_textures - 1u);
+	const pgs_texture_desc t = P.textures[tex_index];
 	bool clamp_s = (tex_word & TEX_SAMPLER_CLAMP_S_BIT) != 0;
 	bool clamp_t = (tex_word & TEX_SAMPLER_CLAMP_T_BIT) != 0;
 	bool linear = (tex_word & TEX_SAMPLER_MAG_LINEAR_BIT) != 0;
@@ -723,7 +759,8 @@ __device__ void sample_texture(const PassParams &P, uint32_t tex_word, float u, 
 	{
 		int32_t x = wrap_coord(ku >> 4, t.wms, t.tw_log2, t.minu, t.maxu);
 		int32_t y = wrap_coord(kv >> 4, t.wmt, t.th_log2, t.minv, t.maxv);
-		uint32_t c = fetch_texel(P, t, x, y);
+		const TexImage im = P.tex_images[tex_index];
+		uint32_t c = __ldg(P.texels + im.offset + uint32_t(y) * im.ext_u + uint32_t(x));
 		#pragma unroll
 		for (int k = 0; k < 4; k++)
 			out[k] = float((c >> (8 * k)) & 0xffu);
@@ -737,10 +774,13 @@ __device__ void sample_texture(const PassParams &P, uint32_t tex_word, float u, 
 	int32_t ys0 = wrap_coord(y0, t.wmt, t.th_log2, t.minv, t.maxv);
 	int32_t ys1 = wrap_coord(y0 + 1, t.wmt, t.th_log2, t.minv, t.maxv);
 	uint32_t w00 = (16u - fx) * (16u - fy), w10 = fx * (16u - fy), w01 = (16u - fx) * fy, w11 = fx * fy;
-	uint32_t c00 = fetch_texel(P, t, xs0, ys0);
-	uint32_t c10 = w10 ? fetch_texel(P, t, xs1, ys0) : 0u;
-	uint32_t c01 = w01 ? fetch_texel(P, t, xs0, ys1) : 0u;
-	uint32_t c11 = w11 ? fetch_texel(P, t, xs1, ys1) : 0u;
+	const TexImage im = P.tex_images[tex_index];
+	const uint32_t *img = P.texels + im.offset;
+	const uint32_t *row0 = img + uint32_t(ys0) * im.ext_u, *row1 = img + uint32_t(ys1) * im.ext_u;
+	uint32_t c00 = __ldg(row0 + xs0);
+	uint32_t c10 = __ldg(row0 + xs1);
+	uint32_t c01 = __ldg(row1 + xs0);
+	uint32_t c11 = __ldg(row1 + xs1);
 	#pragma unroll
 	for (int k = 0; k < 4; k++)
 	{
@@ -1184,7 +1224,7 @@ __device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi
 // memory, no barriers).  SS selects the super-sampled path; sub-tiles whose
 // coarse tile selects the other path exit immediately.
 template <int NS, bool SS>
-__global__ void __launch_bounds__(64 * NS) shade_kernel(PassParams P, DevInstance I, const uint32_t *sub_masks,
+__global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kernel(PassParams P, DevInstance I, const uint32_t *sub_masks,
                                                         const uint32_t *sub_summary, const uint32_t *tile_flags)
 {
 	const uint32_t sub = blockIdx.x;
