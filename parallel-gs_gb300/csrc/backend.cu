@@ -97,6 +97,7 @@ struct CudaBackend
 	uint8_t *d_vram = nullptr;
 	uint16_t *d_clut = nullptr;
 	float *d_rcp_float = nullptr;
+	float *d_unorm_lut = nullptr;
 	uint32_t *d_error = nullptr;
 	unsigned long long *d_frags = nullptr;
 	uint8_t *d_snapshot = nullptr;
@@ -167,6 +168,12 @@ struct CudaBackend
 			lut[i] = 1.0f / (1.0f + (float(i) + 0.5f) / 256.0f);
 		CUDA_TRY(cudaMalloc(&d_rcp_float, sizeof(lut)));
 		CUDA_TRY(cudaMemcpy(d_rcp_float, lut, sizeof(lut), cudaMemcpyHostToDevice));
+		// unpackUnorm4x8 table: float(c) / 255 with IEEE division on the host.
+		volatile float denom = 255.0f;
+		for (int i = 0; i < 256; i++)
+			lut[i] = float(i) / denom;
+		CUDA_TRY(cudaMalloc(&d_unorm_lut, sizeof(lut)));
+		CUDA_TRY(cudaMemcpy(d_unorm_lut, lut, sizeof(lut), cudaMemcpyHostToDevice));
 		CUDA_TRY(cudaMemcpyToSymbol(c_rcp_tab, RCP_TABLE, sizeof(RCP_TABLE)));
 
 		const size_t n = PGS_MAX_PRIMITIVES_PER_FLUSH;
@@ -201,6 +208,7 @@ struct CudaBackend
 		cudaFree(d_error);
 		cudaFree(d_frags);
 		cudaFree(d_rcp_float);
+		cudaFree(d_unorm_lut);
 		cudaFree(d_setup);
 		cudaFree(d_tattr);
 		cudaFree(d_prims_work);
@@ -645,6 +653,7 @@ struct CudaBackend
 		P.vram = d_vram;
 		P.clut = d_clut;
 		P.rcp_float_lut = d_rcp_float;
+		P.unorm_lut = d_unorm_lut;
 		P.error_flags = d_error;
 		P.fragment_counter = d_frags;
 		for (uint32_t i = 0; i < p.num_instances; i++)

@@ -93,6 +93,7 @@ struct PassParams
 	uint8_t *vram;
 	const uint16_t *clut;
 	const float *rcp_float_lut;
+	const float *unorm_lut;
 	uint32_t *error_flags;
 	unsigned long long *fragment_counter;
 };
@@ -602,8 +603,7 @@ __global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, u
 			if (!intersects_tile(s, lo0, lo1, hi0, hi1, ms_tri))
 				continue;
 			uint32_t tile = uint32_t(ty) * I.tiles_w + uint32_t(tx);
-			if ((tile_flags[tile] & flags) != flags)
-				atomicOr(&tile_flags[tile], flags);
+			atomicOr(&tile_flags[tile], flags);
 
 			int32_t gx0 = (max(s.bb[0], lo0) - I.base_x) >> 3, gx1 = (min(s.bb[2], hi0) - I.base_x) >> 3;
 			int32_t gy0 = (max(s.bb[1], lo1) - I.base_y) >> 3, gy1 = (min(s.bb[3], hi1) - I.base_y) >> 3;
@@ -614,10 +614,10 @@ __global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, u
 					int32_t sx = I.base_x + (gx << 3), sy = I.base_y + (gy << 3);
 					if (!intersects_tile(s, sx, sy, sx + 7, sy + 7, ms_tri))
 						continue;
+					// Results unused: both compile to fire-and-forget reductions.
 					size_t sub = size_t(gy) * I.sub_w + size_t(gx);
-					uint32_t old = atomicOr(&sub_masks[sub * I.mask_words + word], bit);
-					if (old == 0u)
-						atomicOr(&sub_summary[sub * I.summary_words + sword], sbit);
+					atomicOr(&sub_masks[sub * I.mask_words + word], bit);
+					atomicOr(&sub_summary[sub * I.summary_words + sword], sbit);
 				}
 			}
 		}
@@ -638,6 +638,9 @@ struct Request
 	float i, j;
 };
 
+// unpackUnorm4x8 channel: float(c) / 255 correctly rounded.  The 256 values are
+// computed on the host with IEEE division and read from a table.
+__device__ __forceinline__ float unorm8_lut(const float *lut, uint32_t c, int ch) { return __ldg(lut + ((c >> (8 * ch)) & 0xffu)); }
 __device__ __forceinline__ float unorm8(uint32_t c, int ch) { return __fdiv_rn(float((c >> (8 * ch)) & 0xffu), 255.0f); }
 
 __device__ __forceinline__ uint32_t pack_unorm(float r, float g, float b, float a)
@@ -808,7 +811,7 @@ __device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r,
 	#pragma unroll
 	for (int k = 0; k < 4; k++)
 	{
-		float c0 = unorm8(a.rgba0, k), c1 = unorm8(a.rgba1, k), c2 = unorm8(a.rgba2, k);
+		float c0 = unorm8_lut(P.unorm_lut, a.rgba0, k), c1 = unorm8_lut(P.unorm_lut, a.rgba1, k), c2 = unorm8_lut(P.unorm_lut, a.rgba2, k);
 		float t = interp(c0, fsub(c1, c0), fsub(c2, c0), r.i, r.j);
 		col[k] = floorf(fadd(fmul(255.0f, t), 1.0f / 256.0f));
 	}
@@ -866,7 +869,7 @@ __device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r,
 		#pragma unroll
 		for (int k = 0; k < 3; k++)
 		{
-			float fcol = fmul(unorm8(fc, k), 255.0f);
+			float fcol = fmul(unorm8_lut(P.unorm_lut, fc, k), 255.0f);
 			float d = fmul(fmul(fsub(cc[k], fcol), f), 1.0f / 256.0f);
 			cc[k] = floorf(fadd(fadd(fcol, d), 0.5f));
 		}
@@ -899,7 +902,7 @@ __device__ void shade_resolve(const ShadeCtx &C, SampleState &S)
 	float fbc[4];
 	#pragma unroll
 	for (int k = 0; k < 4; k++)
-		fbc[k] = roundf(fmul(unorm8(S.color, k), 255.0f));
+		fbc[k] = float((S.color >> (8 * k)) & 0xffu); // == round(unorm8(c) * 255) for every byte
 
 	bool write_fb = true, write_zb = true, write_alpha = true;
 	const pgs_primitive_attribute &pa = P.prims[pi];
@@ -1073,8 +1076,10 @@ __device__ __forceinline__ int evaluate_coverage(const PrimSetup &s, int32_t cx,
 	return 0;
 }
 
+// Must be called by all lanes of a warp; returns with warp_any == false (and no
+// further work) when no lane of the warp is covered.
 __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetup &s, uint32_t st, const SampleState &S,
-                                               bool &opaque)
+                                               bool &opaque, bool &warp_any)
 {
 	const PassParams &P = *C.P;
 	Request r;
@@ -1101,6 +1106,9 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 		if ((sy & 1) == 0) { if ((st >> STATE_BIT_SCANMSK_EVEN) & 1) r.coverage = 0; }
 		else if ((st >> STATE_BIT_SCANMSK_ODD) & 1) r.coverage = 0;
 	}
+	warp_any = __any_sync(0xffffffffu, r.coverage > 0);
+	if (!warp_any)
+		return r;
 	if (C.zs && r.multisample && r.coverage < 0x80)
 		r.z_write = false;
 	uint32_t z = s.z[0];
@@ -1157,9 +1165,8 @@ __device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi
 	if (s.bb[2] < wlo0 || s.bb[0] > whi0 || s.bb[3] < wlo1 || s.bb[1] > whi1)
 		return;
 	uint32_t st = P.prims[pi].state;
-	bool opaque;
-	Request q = shade_early(C, s, st, S, opaque);
-	bool any_cov = __any_sync(0xffffffffu, q.coverage > 0);
+	bool opaque, any_cov;
+	Request q = shade_early(C, s, st, S, opaque, any_cov);
 	if (!any_cov)
 		return;
 	if (q.coverage > 0)
@@ -1395,7 +1402,8 @@ __global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kerne
 		}
 		color_dirty = (__ballot_sync(full, S.color_dirty) & group_mask) != 0u;
 		// Butterfly sums in the order XOR NS/2 ... 1; every lane takes part.
-		float v0 = unorm8(S.color, 0), v1 = unorm8(S.color, 1), v2 = unorm8(S.color, 2), v3 = unorm8(S.color, 3);
+		const float *lut = P.unorm_lut;
+		float v0 = unorm8_lut(lut, S.color, 0), v1 = unorm8_lut(lut, S.color, 1), v2 = unorm8_lut(lut, S.color, 2), v3 = unorm8_lut(lut, S.color, 3);
 		#pragma unroll
 		for (int o = NS / 2; o >= 1; o >>= 1)
 		{
