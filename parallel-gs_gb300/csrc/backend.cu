@@ -506,6 +506,28 @@ struct CudaBackend
 		return depth;
 	}
 
+	// Shading launches: the super-sampled variant for tiles that need it, then
+	// the single-sampled variant (ubershader.comp dispatched twice,
+	// gs/gs_renderer.cpp:2395-2415).
+	template <bool AA>
+	void launch_shade(const PassParams &P, const DevInstance &I, uint32_t ns_log2, uint32_t grid,
+	                  const uint32_t *masks, const uint32_t *summary)
+	{
+		if (I.rate_y_log2 != 0)
+		{
+			switch (ns_log2)
+			{
+			case 1: shade_kernel<2, true, AA><<<grid, 128, 0, stream>>>(P, I, masks, summary, d_flags); break;
+			case 2: shade_kernel<4, true, AA><<<grid, 256, 0, stream>>>(P, I, masks, summary, d_flags); break;
+			case 3: shade_kernel<8, true, AA><<<grid, 512, 0, stream>>>(P, I, masks, summary, d_flags); break;
+			default: shade_kernel<16, true, AA><<<grid, 1024, 0, stream>>>(P, I, masks, summary, d_flags); break;
+			}
+			launch_counter++;
+		}
+		shade_kernel<1, false, AA><<<grid, 64, 0, stream>>>(P, I, masks, summary, d_flags);
+		launch_counter++;
+	}
+
 	int run_instance(const PassParams &P, const PassOp &p, uint32_t inst_index, uint32_t lo, uint32_t count)
 	{
 		const pgs_rp_instance &in = p.instances[inst_index];
@@ -557,20 +579,10 @@ struct CudaBackend
 				return r;
 			shade_started = true;
 		}
-		if (I.rate_y_log2 != 0)
-		{
-			switch (ns_log2)
-			{
-			case 1: shade_kernel<2, true><<<grid, 128, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags); break;
-			case 2: shade_kernel<4, true><<<grid, 256, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags); break;
-			case 3: shade_kernel<8, true><<<grid, 512, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags); break;
-			case 4: shade_kernel<16, true><<<grid, 1024, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags); break;
-			default: return PGS_ERROR_INVALID_ARGUMENT;
-			}
-			launch_counter++;
-		}
-		shade_kernel<1, false><<<grid, 64, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags);
-		launch_counter++;
+		if (p.has_aa1)
+			launch_shade<true>(P, I, ns_log2, grid, d_sub_masks, d_sub_summary);
+		else
+			launch_shade<false>(P, I, ns_log2, grid, d_sub_masks, d_sub_summary);
 		CUDA_TRY(cudaGetLastError());
 		if (shade_timing)
 			return record_timing_event(shade_ev[1]);

@@ -1023,6 +1023,27 @@ __device__ void shade_resolve(const ShadeCtx &C, SampleState &S)
 	}
 }
 
+// Coverage of one sample for primitives without AA1 (evaluate_coverage with
+// multisample == false): 0x80 when the sample is inside, else 0.  The
+// barycentrics are computed separately, only once some lane is covered.
+__device__ __forceinline__ int coverage_plain(const PrimSetup &s, int32_t cx, int32_t cy, int dim)
+{
+	int32_t sx = cx >> dim, sy = cy >> dim;
+	if (!(sx >= s.bb[0] && sy >= s.bb[1] && s.bb[2] >= sx && s.bb[3] >= sy))
+		return 0;
+	int32_t axw = s.a[0];
+	int32_t A[3] = { axw >> 6, s.a[1], s.a[2] };
+	int32_t px = cx << (3 - dim), py = cy << (3 - dim);
+	int32_t ea = idot3(A, px, py), eb = idot3(s.b, px, py), ec = idot3(s.c, px, py);
+	if ((axw & 1) && ea < 0)
+	{
+		eb += ea + int32_t((uint32_t(axw) >> 2) & 3u) - 1;
+		ec += ea + int32_t((uint32_t(axw) >> 4) & 3u) - 1;
+		ea = 0;
+	}
+	return (ea >= 0 && eb >= 0 && ec >= 0) ? 0x80 : 0;
+}
+
 __device__ __forceinline__ int evaluate_coverage(const PrimSetup &s, int32_t cx, int32_t cy, float &i, float &j, bool ms,
                                                  bool line, int dim)
 {
@@ -1077,7 +1098,9 @@ __device__ __forceinline__ int evaluate_coverage(const PrimSetup &s, int32_t cx,
 }
 
 // Must be called by all lanes of a warp; returns with warp_any == false (and no
-// further work) when no lane of the warp is covered.
+// further work) when no lane of the warp is covered.  AA compiles the AA1
+// coverage path in (ubershader variant VARIANT_FLAG_HAS_AA1_BIT).
+template <bool AA>
 __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetup &s, uint32_t st, const SampleState &S,
                                                bool &opaque, bool &warp_any)
 {
@@ -1088,7 +1111,7 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 	r.z_write = C.zs && ((st >> STATE_BIT_Z_WRITE) & 1);
 	r.z_greater = C.zs && ((st >> STATE_BIT_Z_TEST_GREATER) & 1);
 	r.state = st & STATE_INDEX_MASK;
-	r.multisample = P.has_aa1 && ((st >> STATE_BIT_MULTISAMPLE) & 1);
+	r.multisample = AA && ((st >> STATE_BIT_MULTISAMPLE) & 1);
 	r.perspective = (st >> STATE_BIT_PERSPECTIVE) & 1;
 	int32_t rx = S.hx, ry = S.hy;
 	if (C.ss && (st & (1u << STATE_BIT_SNAP_RASTER)))
@@ -1097,7 +1120,10 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 		ry &= C.snap_mask;
 	}
 	float i = 0.0f, j = 0.0f;
-	r.coverage = evaluate_coverage(s, rx, ry, i, j, r.multisample, (st >> STATE_BIT_LINE) & 1, C.dim);
+	if (AA)
+		r.coverage = evaluate_coverage(s, rx, ry, i, j, r.multisample, (st >> STATE_BIT_LINE) & 1, C.dim);
+	else
+		r.coverage = coverage_plain(s, rx, ry, C.dim);
 	if (P.has_scanmsk)
 	{
 		int32_t sy = S.hy;
@@ -1109,6 +1135,13 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 	warp_any = __any_sync(0xffffffffu, r.coverage > 0);
 	if (!warp_any)
 		return r;
+	if (!AA)
+	{
+		// Barycentrics at the raster coordinate (evaluate_coverage_single).
+		int32_t qx = rx << (3 - C.dim), qy = ry << (3 - C.dim);
+		i = fadd(fmul(__int2float_rn(idot3(s.b, qx, qy)), s.inv_area), s.error_i);
+		j = fadd(fmul(__int2float_rn(idot3(s.c, qx, qy)), s.inv_area), s.error_j);
+	}
 	if (C.zs && r.multisample && r.coverage < 0x80)
 		r.z_write = false;
 	uint32_t z = s.z[0];
@@ -1156,17 +1189,20 @@ __device__ __forceinline__ void sample_offset(uint32_t s, uint32_t xl, uint32_t 
 
 // Processes one primitive for the calling warp: coverage, early depth,
 // deferred-shading bookkeeping (ubershader.comp:1694-1812).  Warp-uniform.
-template <bool SS>
+template <bool SS, bool AA>
 __device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi, SampleState &S, uint32_t &covered,
                                                   int32_t wlo0, int32_t wlo1, int32_t whi0, int32_t whi1)
 {
 	const PassParams &P = *C.P;
 	const PrimSetup s = P.setup[pi];
-	if (s.bb[2] < wlo0 || s.bb[0] > whi0 || s.bb[3] < wlo1 || s.bb[1] > whi1)
-		return;
 	uint32_t st = P.prims[pi].state;
+	// Per-warp conservative test against the warp's pixel rectangle
+	// (primitive_intersects_tile, ubershader.comp:1646-1668).
+	bool ms_tri = AA && ((st >> STATE_BIT_MULTISAMPLE) & 1) && !((st >> STATE_BIT_LINE) & 1);
+	if (!intersects_tile(s, wlo0, wlo1, whi0, whi1, ms_tri))
+		return;
 	bool opaque, any_cov;
-	Request q = shade_early(C, s, st, S, opaque, any_cov);
+	Request q = shade_early<AA>(C, s, st, S, opaque, any_cov);
 	if (!any_cov)
 		return;
 	if (q.coverage > 0)
@@ -1230,7 +1266,7 @@ __device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi
 // Each warp walks the sub-tile's primitive bitmask on its own (no shared
 // memory, no barriers).  SS selects the super-sampled path; sub-tiles whose
 // coarse tile selects the other path exit immediately.
-template <int NS, bool SS>
+template <int NS, bool SS, bool AA>
 __global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kernel(PassParams P, DevInstance I, const uint32_t *sub_masks,
                                                         const uint32_t *sub_summary, const uint32_t *tile_flags)
 {
@@ -1364,7 +1400,7 @@ __global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kerne
 				{
 					int b = __ffs(m) - 1;
 					m &= m - 1u;
-					process_primitive<SS>(C, prim_base + uint32_t(b), S, covered, wlo0, wlo1, whi0, whi1);
+					process_primitive<SS, AA>(C, prim_base + uint32_t(b), S, covered, wlo0, wlo1, whi0, whi1);
 				}
 			}
 		}
