@@ -276,6 +276,31 @@ int pgs_cuda_backend_get_stats(void *backend, pgs_backend_stats *stats);
 int pgs_cuda_backend_set_shade_timing(void *backend, int enable);
 
 /* ------------------------------------------------------------------ */
+/* Allocation-free local->local VRAM copy                               */
+/* ------------------------------------------------------------------ */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory — code running under a memory-capture or pool-restricted allocator,
+ * inside another framework's arena, or with a hard no-cudaMalloc rule on a
+ * latency-critical path — this performs the LOCAL_TO_LOCAL transfer described
+ * by desc (BITBLTBUF/TRXPOS/TRXREG, XDIR = 2) on a caller-owned VRAM image
+ * without allocating anything.  vram points to num_planes consecutive 4 MiB
+ * planes in device memory (plane 1, when present, is the super-sample
+ * reference plane whose written bits are cleared as by copy_vram); stream is
+ * a cudaStream_t or NULL.  Results equal those of copy_vram: every source
+ * pixel is read before any destination pixel is written.
+ *
+ * The source rectangle is staged in a fixed device array of
+ * PGS_NOALLOC_COPY_MAX_PIXELS 32-bit entries (1 MiB) that every GPU loading the
+ * library holds until exit; larger rectangles are rejected with
+ * PGS_ERROR_CAPACITY.  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress) with the device current; make that first call
+ * before any stream capture.  All calls share the array, so calls whose work
+ * overlaps on the GPU race; serialise them on one stream.  Nothing in the array
+ * needs to start at zero: each call overwrites the entries it reads. */
+#define PGS_NOALLOC_COPY_MAX_PIXELS (256u * 1024u)
+int pgs_vram_local_copy_noalloc(void *vram, uint32_t num_planes, const pgs_copy_desc *desc, void *stream);
+
+/* ------------------------------------------------------------------ */
 /* Frontend (GSInterface)                                               */
 /* ------------------------------------------------------------------ */
 typedef struct pgs_gs pgs_gs;

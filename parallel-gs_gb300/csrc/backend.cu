@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -945,6 +946,71 @@ int c_error(void *self, uint32_t *flags) { return B(self)->get_error(flags); }
 const pgs_backend_ops CUDA_OPS = {
 	PGS_ABI_VERSION, c_destroy, c_reserve, c_flush_rendering, c_copy, c_palette, c_set_ss, c_submit, c_read, c_write, c_error,
 };
+
+// ---------------------------------------------------------------------------
+// Allocation-free local->local copy.  The staging area is a file-scope device
+// array; host code only ever uses the address cudaGetSymbolAddress returns.
+static __device__ __align__(256) uint32_t g_noalloc_copy_scratch[PGS_NOALLOC_COPY_MAX_PIXELS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+uint32_t *g_noalloc_scratch_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Pass 1: read every source pixel of the rectangle into the staging array.
+__global__ void __launch_bounds__(256) noalloc_gather_kernel(CopyParams C, const uint8_t *vram, uint32_t *staging)
+{
+	uint32_t x = blockIdx.x * 32u + (threadIdx.x & 31u);
+	uint32_t y = blockIdx.y * 8u + (threadIdx.x >> 5);
+	if (x >= C.width || y >= C.height)
+		return;
+	uint32_t sx = (x + C.ssax) & 2047u, sy = (y + C.ssay) & 2047u;
+	staging[y * C.width + x] = read_pixel(vram, C.spsm, swizzle_address(sx, sy, C.sbp, C.sbw, C.spsm));
+}
+
+// Pass 2: write the destination exactly as upload_kernel does for local copies.
+__global__ void __launch_bounds__(256) noalloc_scatter_kernel(CopyParams C, uint8_t *vram, const uint32_t *staging)
+{
+	uint32_t x = blockIdx.x * 32u + (threadIdx.x & 31u);
+	uint32_t y = blockIdx.y * 8u + (threadIdx.x >> 5);
+	if (x >= C.width || y >= C.height)
+		return;
+	uint32_t eff_stride = C.dbw;
+	if (C.dpsm == PSMT4 || C.dpsm == PSMT8)
+		eff_stride &= ~1u;
+	if (x >= eff_stride * 64u)
+	{
+		Layout L = psm_layout(C.dpsm);
+		uint32_t last = (C.dsay + C.height - 1u) >> L.ph, cur = (C.dsay + y) >> L.ph;
+		if (last != cur)
+			return;
+	}
+	uint32_t dx = (x + C.dsax) & 2047u, dy = (y + C.dsay) & 2047u;
+	write_pixel(vram, C.dpsm, swizzle_address(dx, dy, C.dbp, C.dbw, C.dpsm), staging[y * C.width + x],
+	            C.invalidate_ss != 0);
+}
+
+// Per-device set-up: the device address of the staging array, looked up once
+// with the device current.
+int noalloc_scratch(uint32_t **out)
+{
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+		return PGS_ERROR_NO_DEVICE;
+	std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+	if (!g_noalloc_scratch_ptr[dev])
+	{
+		void *p = nullptr;
+		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_copy_scratch);
+		if (e != cudaSuccess || !p)
+		{
+			fprintf(stderr, "pgs: cudaGetSymbolAddress(g_noalloc_copy_scratch) failed: %s\n", cudaGetErrorString(e));
+			return PGS_ERROR_CUDA;
+		}
+		g_noalloc_scratch_ptr[dev] = static_cast<uint32_t *>(p);
+	}
+	*out = g_noalloc_scratch_ptr[dev];
+	return PGS_OK;
+}
 } // namespace
 
 extern "C" {
@@ -1030,4 +1096,44 @@ int pgs_cuda_backend_fragment_count(void *backend, uint64_t *count)
 	*count = v;
 	return PGS_OK;
 }
+}
+
+extern "C" int pgs_vram_local_copy_noalloc(void *vram, uint32_t num_planes, const pgs_copy_desc *desc, void *stream)
+{
+	if (!vram || !desc || num_planes == 0)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	CopyParams c = {};
+	uint64_t bb = desc->bitbltbuf;
+	c.sbp = field(bb, 0, 14); c.sbw = field(bb, 16, 6); c.spsm = field(bb, 24, 6);
+	c.dbp = field(bb, 32, 14); c.dbw = field(bb, 48, 6); c.dpsm = field(bb, 56, 6);
+	c.ssax = field(desc->trxpos, 0, 11); c.ssay = field(desc->trxpos, 16, 11);
+	c.dsax = field(desc->trxpos, 32, 11); c.dsay = field(desc->trxpos, 48, 11);
+	c.width = field(desc->trxreg, 0, 12); c.height = field(desc->trxreg, 32, 12);
+	c.xdir = field(desc->trxdir, 0, 2);
+	c.invalidate_ss = num_planes > 1;
+	if (c.xdir != LOCAL_TO_LOCAL)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if (c.width == 0 || c.height == 0)
+		return PGS_OK;
+	if (uint64_t(c.width) * c.height > PGS_NOALLOC_COPY_MAX_PIXELS)
+	{
+		fprintf(stderr, "pgs: pgs_vram_local_copy_noalloc: %ux%u pixels exceed the %u-pixel staging array\n",
+		        c.width, c.height, PGS_NOALLOC_COPY_MAX_PIXELS);
+		return PGS_ERROR_CAPACITY;
+	}
+	uint32_t *staging = nullptr;
+	int r = noalloc_scratch(&staging);
+	if (r)
+		return r;
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	dim3 grid((c.width + 31) / 32, (c.height + 7) / 8);
+	noalloc_gather_kernel<<<grid, 256, 0, s>>>(c, static_cast<const uint8_t *>(vram), staging);
+	noalloc_scatter_kernel<<<grid, 256, 0, s>>>(c, static_cast<uint8_t *>(vram), staging);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess)
+	{
+		fprintf(stderr, "pgs: pgs_vram_local_copy_noalloc launch failed: %s\n", cudaGetErrorString(e));
+		return PGS_ERROR_CUDA;
+	}
+	return PGS_OK;
 }

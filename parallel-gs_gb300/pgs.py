@@ -31,6 +31,9 @@ STATUS_NAMES = {
 }
 
 
+STATUS_CODES = {v: k for k, v in STATUS_NAMES.items()}
+
+
 class PGSError(RuntimeError):
     def __init__(self, status: int, what: str) -> None:
         super().__init__("%s failed: %s (%d)" % (what, STATUS_NAMES.get(status, "?"), status))
