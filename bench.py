@@ -104,6 +104,20 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def max_over_ranks(value: float, dist, device: str = "cpu") -> float:
+    """Slowest rank's time: every rank renders its own replica, so the job ends
+    when the last one does."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(steps: int, world: int, max_ms: float) -> float:
+    """Frames/s of the whole job: world replicas x steps frames in the slowest rank's time."""
+    return world * steps / (max_ms / 1000.0)
+
+
 def algorithmic_bytes(frame, ss: int) -> dict:
     """Bytes a frame must move at minimum: prim records in,
     setup records written and read, FB/Z read+write per pixel for plane 0,
@@ -247,13 +261,8 @@ def main():
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
     if pg:
-        t = torch.tensor([total_ms], device="cuda:%d" % local)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
-
-    # Shading kernel time: replay the frame with only timing events around the
-    # whole graph is the step; the shade share comes from the ncu launch list.
-    fps = world * args.steps / (total_ms / 1000.0)
+        total_ms = max_over_ranks(total_ms, pg, "cuda:%d" % local)
+    fps = replica_throughput(args.steps, world, total_ms)
 
     # End to end through the public API from host memory.
     e2e_steps = 0 if args.quick else max(3, min(args.steps, 10))
