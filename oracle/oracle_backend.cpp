@@ -243,6 +243,9 @@ struct Backend
 	std::vector<pgs_vertex_attribute> res_attr;
 	std::vector<pgs_primitive_attribute> res_prim;
 	std::atomic<uint64_t> fragments{0};
+	// Primitive states after setup and the single-sample heuristic, appended
+	// per render pass (for tests of the heuristic's decisions).
+	std::vector<uint32_t> state_log;
 
 	Backend() : clut(PGS_CLUT_INSTANCES * 512, 0)
 	{
@@ -260,9 +263,10 @@ struct Backend
 	// triangle_setup.comp main_inner.
 	void triangle_setup(uint32_t index, const pgs_vertex_position *vp, const pgs_vertex_attribute *va,
 	                    pgs_primitive_attribute &pa, Setup &out, TAttr &ta, const uint32_t *opaque_fbmasks,
-	                    int srx, int sry)
+	                    int srx, int sry, uint32_t packed_z_shift, int32_t &bucket_out)
 	{
 		(void)srx;
+		bucket_out = -1;
 		int order[3] = { 0, 1, 2 };
 		uint32_t st = pa.state;
 		bool parallelogram = bfe(st, 15, 1);
@@ -621,8 +625,15 @@ struct Backend
 				per_sample = di[2] != 0.0f || dj[2] != 0.0f;
 			if (!per_sample)
 				per_sample = za != zb || zb != zc;
-			if (!per_sample && !line)
-				pa.state |= 1u << 26;
+			if (!per_sample)
+			{
+				// triangle_setup.comp:836-871: flat primitive, register the
+				// depth bucket (Z >> z_shift_to_bucket * 8, clamped to 255).
+				if (!line)
+					pa.state |= 1u << 26;
+				uint32_t z_shift = bfe(packed_z_shift, 4 * instance, 4) * 8;
+				bucket_out = int32_t(std::min<uint32_t>(255u, za >> z_shift));
+			}
 		}
 	}
 
@@ -1247,6 +1258,15 @@ struct Backend
 			ox = (lx << 1) + (ly & 1);
 			oy = ly;
 		}
+		else if (yl == xl + 2)
+		{
+			// Lanes: local y = bits 0-2, local x = bits 3-4; x is scaled by 4
+			// and offset per row by bits (2 * (y & 3)) of 0x78 (:266-271, :333-338).
+			int32_t ly = int32_t(s & ((1u << yl) - 1u));
+			int32_t lx = int32_t(s >> yl);
+			ox = (lx << 2) + int32_t((0x78u >> ((ly & 3) * 2)) & 3u);
+			oy = ly;
+		}
 		else
 		{
 			ox = 0;
@@ -1604,6 +1624,171 @@ struct Backend
 		}
 	}
 
+	// Push constants of dispatch_triangle_setup / dispatch_single_sample_heuristic
+	// (gs/gs_renderer.cpp:1914-1934, 1998-2036).
+	struct HeuristicPush { uint32_t z_shift_bucket, z_shift, z_max; bool active; };
+
+	static uint32_t heuristic_pushes(const pgs_render_pass *rp, HeuristicPush *push)
+	{
+		uint32_t packed = 0;
+		HeuristicPush cur = {};
+		for (uint32_t i = 0; i < rp->num_instances; i++)
+		{
+			const pgs_rp_instance &in = rp->instances[i];
+			uint32_t depth_psm = in.z_sensitive ? (bfe(uint32_t(in.zbuf >> 24), 0, 4) | 0x30u) : 0x31u;
+			if (depth_psm == 0x32 || depth_psm == 0x3a)
+				packed |= 1u << (4 * i);
+			else if (depth_psm == 0x31)
+				packed |= 2u << (4 * i);
+			else if (depth_psm == 0x30)
+				packed |= 3u << (4 * i);
+			if (in.sampling_rate_y_log2 == 0)
+				continue;
+			// Push constants persist across instances; an unknown format keeps
+			// the previous values.
+			if (depth_psm == 0x32 || depth_psm == 0x3a)
+				cur = { 8, 0, 0xffffu, true };
+			else if (depth_psm == 0x31)
+				cur = { 16, 0, 0xffffffu, true };
+			else if (depth_psm == 0x30)
+				cur = { 16, 8, 0xffffffffu, true };
+			push[i] = cur;
+			push[i].active = true;
+		}
+		return packed;
+	}
+
+	static uint32_t hash_vertex(const pgs_vertex_position &v)
+	{
+		// single_sample_heuristic.comp:86-94.
+		uint32_t s[3] = { uint32_t(v.x), uint32_t(v.y), v.z };
+		for (int r = 0; r < 3; r++)
+		{
+			uint32_t t[3];
+			for (int k = 0; k < 3; k++)
+				t[k] = ((s[k] >> 8) ^ s[(k + 1) % 3]) * 1103515245u;
+			s[0] = t[0]; s[1] = t[1]; s[2] = t[2];
+		}
+		return s[0] >> 16;
+	}
+
+	// single_sample_heuristic.comp:148-291, one workgroup per active bucket
+	// and super-sampled instance.  All buckets read the states triangle setup
+	// produced and the decisions are applied afterwards.  (The reference lets
+	// workgroups see each other's writes; that only matters for a zero-area
+	// primitive with unequal vertex depths, whose outcome there depends on
+	// workgroup scheduling.)
+	static void single_sample_heuristic(const pgs_render_pass *rp, std::vector<pgs_primitive_attribute> &prims,
+	                                    const std::vector<int32_t> &bucket, const HeuristicPush *push)
+	{
+		const uint32_t n = rp->num_primitives;
+		const pgs_vertex_position *vp = rp->positions;
+		bool active_bucket[256] = {};
+		for (uint32_t i = 0; i < n; i++)
+			if (bucket[i] >= 0)
+				active_bucket[bucket[i]] = true;
+		std::vector<uint8_t> action(n, 0);
+		const uint32_t SA = 1u << 26, SR = 1u << 25, LINE = 1u << 22, SPRITE = 1u << 21;
+		const uint32_t NO_FULL_3D = SPRITE | LINE | SA;
+		std::vector<uint8_t> full3d(65536), cand(65536), shared_v(65536);
+		for (uint32_t inst = 0; inst < rp->num_instances; inst++)
+		{
+			if (!push[inst].active)
+				continue;
+			const HeuristicPush &h = push[inst];
+			auto snap = [&](uint32_t z) { return std::min(h.z_max, z) >> h.z_shift; };
+			for (uint32_t b = 0; b < 256; b++)
+			{
+				if (!active_bucket[b])
+					continue;
+				std::fill(full3d.begin(), full3d.end(), 0);
+				std::fill(cand.begin(), cand.end(), 0);
+				std::fill(shared_v.begin(), shared_v.end(), 0);
+				bool any_full3d = false;
+				uint32_t min_z = ~0u, max_z = 0;
+				uint32_t zlo = b << h.z_shift_bucket, zhi = ((b + 1) << h.z_shift_bucket) - 1;
+				auto in_range = [&](uint32_t s) { return s >= zlo && s <= zhi; };
+
+				for (uint32_t i = 0; i < n; i++)
+				{
+					uint32_t st = prims[i].state;
+					if (bfe(st, 29, 3) != inst)
+						continue;
+					if ((st & NO_FULL_3D) == 0)
+					{
+						for (int k = 0; k < 3; k++)
+						{
+							uint32_t z = vp[3 * i + k].z;
+							min_z = std::min(min_z, z);
+							max_z = std::max(max_z, z);
+							uint32_t s = snap(z);
+							if (in_range(s))
+								full3d[s - zlo] = 1;
+							any_full3d = true;
+						}
+					}
+					else if ((st & (SA | SR)) == SA || (st & LINE))
+					{
+						uint32_t s = snap(vp[3 * i].z);
+						if (in_range(s))
+							cand[s - zlo] = 1;
+					}
+				}
+				for (uint32_t i = 0; i < n; i++)
+				{
+					uint32_t st = prims[i].state;
+					if (bfe(st, 29, 3) != inst || (st & NO_FULL_3D) != 0)
+						continue;
+					for (int k = 0; k < 3; k++)
+					{
+						uint32_t s = snap(vp[3 * i + k].z);
+						if (in_range(s) && cand[s - zlo])
+							shared_v[hash_vertex(vp[3 * i + k])] = 1;
+					}
+				}
+				for (uint32_t i = 0; i < n; i++)
+				{
+					uint32_t st = prims[i].state;
+					if (bfe(st, 29, 3) != inst || (st & (SA | SR)) != SA)
+						continue;
+					uint32_t s = snap(vp[3 * i].z);
+					if (!in_range(s) || !full3d[s - zlo])
+						continue;
+					bool conflict = shared_v[hash_vertex(vp[3 * i])] || shared_v[hash_vertex(vp[3 * i + 1])] ||
+					                shared_v[hash_vertex(vp[3 * i + 2])];
+					if (conflict)
+						cand[s - zlo] = 0;
+				}
+				bool force_single_sample = !any_full3d;
+				for (uint32_t i = 0; i < n; i++)
+				{
+					uint32_t z = vp[3 * i].z;
+					uint32_t s = snap(z);
+					if (!in_range(s))
+						continue;
+					uint32_t st = prims[i].state;
+					if (bfe(st, 29, 3) != inst)
+						continue;
+					bool tri = (st & (SA | SR)) == SA;
+					bool line = force_single_sample && (st & LINE);
+					if (!tri && !line)
+						continue;
+					if (cand[s - zlo])
+						action[i] = 1;
+					else if ((st & ((1u << 12) | (1u << 13))) && z > min_z && z < max_z)
+						action[i] = 2;
+				}
+			}
+		}
+		for (uint32_t i = 0; i < n; i++)
+		{
+			if (action[i] == 1)
+				prims[i].state |= SR;
+			else if (action[i] == 2)
+				prims[i].state &= ~SA;
+		}
+	}
+
 	int flush_rendering(const pgs_render_pass *rp)
 	{
 		if (!rp || rp->num_primitives == 0)
@@ -1628,9 +1813,17 @@ struct Backend
 			srx = std::max<int>(srx, int(rp->instances[i].sampling_rate_x_log2));
 			sry = std::max<int>(sry, int(rp->instances[i].sampling_rate_y_log2));
 		}
+		HeuristicPush push[8] = {};
+		uint32_t packed_z_shift = heuristic_pushes(rp, push);
+		std::vector<int32_t> bucket(rp->num_primitives);
 		#pragma omp parallel for schedule(static)
 		for (uint32_t i = 0; i < rp->num_primitives; i++)
-			triangle_setup(i, rp->positions, rp->attributes, prims[i], setup[i], tattr[i], fbmasks, srx, sry);
+			triangle_setup(i, rp->positions, rp->attributes, prims[i], setup[i], tattr[i], fbmasks, srx, sry,
+			               packed_z_shift, bucket[i]);
+		if (sry != 0)
+			single_sample_heuristic(rp, prims, bucket, push);
+		for (uint32_t i = 0; i < rp->num_primitives; i++)
+			state_log.push_back(prims[i].state);
 
 		// Instance ordering (gs/gs_renderer.cpp:3190-3266).
 		if (rp->num_instances == 1)
@@ -2012,6 +2205,15 @@ uint64_t pgs_oracle_fragment_count(void *backend)
 uint32_t pgs_oracle_swizzle(uint32_t x, uint32_t y, uint32_t base, uint32_t stride, uint32_t psm)
 {
 	return oracle::swizzle(x, y, base, stride, psm);
+}
+
+// Copies up to `max` logged primitive states; returns the number logged.
+uint32_t pgs_oracle_state_log(void *backend, uint32_t *out, uint32_t max)
+{
+	auto &log = static_cast<Backend *>(backend)->state_log;
+	for (uint32_t i = 0; i < max && i < log.size(); i++)
+		out[i] = log[i];
+	return uint32_t(log.size());
 }
 
 float pgs_oracle_rcp_fixed(uint32_t b) { return oracle::rcp_fixed(b); }

@@ -42,6 +42,8 @@ def load_oracle() -> C.CDLL:
         lib.pgs_oracle_fragment_count.restype = C.c_uint64
         lib.pgs_oracle_swizzle.argtypes = [C.c_uint32] * 5
         lib.pgs_oracle_swizzle.restype = C.c_uint32
+        lib.pgs_oracle_state_log.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+        lib.pgs_oracle_state_log.restype = C.c_uint32
         lib.pgs_oracle_rcp_fixed.argtypes = [C.c_uint32]
         lib.pgs_oracle_rcp_fixed.restype = C.c_float
         lib.pgs_oracle_rcp_float.argtypes = [C.c_float]
@@ -76,6 +78,14 @@ class OracleBackend(pgs.Backend):
 
     def fragments(self) -> int:
         return int(self.lib.pgs_oracle_fragment_count(self.handle))
+
+    def state_log(self) -> np.ndarray:
+        """Primitive states after triangle setup and the single-sample heuristic,
+        concatenated over the render passes flushed so far."""
+        n = int(self.lib.pgs_oracle_state_log(self.handle, None, 0))
+        out = np.zeros(n, dtype=np.uint32)
+        self.lib.pgs_oracle_state_log(self.handle, out.ctypes.data, n)
+        return out
 
 
 def render(frame, backend: pgs.Backend | None = None, planes: bool = False):

@@ -119,6 +119,8 @@ struct CudaBackend
 	PrimSetup *d_setup = nullptr;
 	TransformedAttr *d_tattr = nullptr;
 	pgs_primitive_attribute *d_prims_work = nullptr;
+	SsHeuristic *d_heuristic = nullptr;
+	uint8_t *d_heuristic_action = nullptr;
 	uint32_t *d_masks = nullptr;
 	size_t masks_cap = 0;
 	uint32_t *d_flags = nullptr;
@@ -181,6 +183,9 @@ struct CudaBackend
 		CUDA_TRY(cudaMalloc(&d_setup, n * sizeof(PrimSetup)));
 		CUDA_TRY(cudaMalloc(&d_tattr, n * sizeof(TransformedAttr)));
 		CUDA_TRY(cudaMalloc(&d_prims_work, n * sizeof(pgs_primitive_attribute)));
+		CUDA_TRY(cudaMalloc(&d_heuristic, sizeof(SsHeuristic)));
+		CUDA_TRY(cudaMalloc(&d_heuristic_action, n));
+		CUDA_TRY(cudaMemset(d_heuristic_action, 0, n));
 		for (int i = 0; i < 2; i++)
 		{
 			CUDA_TRY(cudaMallocHost(&h_stage[i], stage_bytes()));
@@ -213,6 +218,8 @@ struct CudaBackend
 		cudaFree(d_setup);
 		cudaFree(d_tattr);
 		cudaFree(d_prims_work);
+		cudaFree(d_heuristic);
+		cudaFree(d_heuristic_action);
 		cudaFree(d_masks);
 		cudaFree(d_flags);
 		cudaFree(d_texels);
@@ -669,6 +676,10 @@ struct CudaBackend
 		P.unorm_lut = d_unorm_lut;
 		P.error_flags = d_error;
 		P.fragment_counter = d_frags;
+		P.heuristic = d_heuristic;
+		P.heuristic_action = d_heuristic_action;
+		HeuristicParams H = {};
+		heuristic_params(p, P.packed_z_shift, H);
 		for (uint32_t i = 0; i < p.num_instances; i++)
 		{
 			P.opaque_fbmask[i] = p.instances[i].opaque_fbmask;
@@ -677,8 +688,17 @@ struct CudaBackend
 		}
 		CUDA_TRY(cudaMemcpyAsync(d_prims_work, d_arena + p.prim_off, size_t(p.num_prims) * sizeof(pgs_primitive_attribute),
 		                         cudaMemcpyDeviceToDevice, stream));
+		if (H.instance_mask)
+			CUDA_TRY(cudaMemsetAsync(d_heuristic, 0, sizeof(SsHeuristic), stream));
 		setup_kernel<<<(p.num_prims + 127) / 128, 128, 0, stream>>>(P);
 		launch_counter++;
+		if (H.instance_mask)
+		{
+			// Flush order: setup, heuristic, binning (gs/gs_renderer.cpp:3157-3170).
+			single_sample_heuristic_kernel<<<dim3(256, p.num_instances), 1024, 0, stream>>>(P, H);
+			heuristic_apply_kernel<<<(p.num_prims + 255) / 256, 256, 0, stream>>>(P);
+			launch_counter += 2;
+		}
 		if (p.num_textures && p.num_texels)
 		{
 			dim3 grid((p.max_texels + 255) / 256, p.num_textures);
@@ -740,6 +760,44 @@ struct CudaBackend
 				if (r) return r;
 			}
 		return PGS_OK;
+	}
+
+	// Depth quantisation of the flat-primitive buckets per instance.  Triangle
+	// setup buckets by Z >> (8, 16, 24) for Z16, Z24, Z32 (gs/gs_renderer.cpp:
+	// 1914-1934); the heuristic walks 2^16 (2^8) values per bucket
+	// (:1998-2030).  An instance that does not test Z counts as Z24.  A
+	// format outside the four keeps the previous super-sampled instance's
+	// parameters, as the reference's push constants do.
+	static void heuristic_params(const PassOp &p, uint32_t &packed_z_shift, HeuristicParams &H)
+	{
+		packed_z_shift = 0;
+		H = {};
+		uint32_t zsb = 0, zs = 0, zmax = 0;
+		for (uint32_t i = 0; i < p.num_instances; i++)
+		{
+			const pgs_rp_instance &in = p.instances[i];
+			uint32_t depth_psm = in.z_sensitive ? (field(uint32_t(in.zbuf), 24, 4) | 0x30u) : PSMZ24;
+			switch (depth_psm)
+			{
+			case PSMZ16S: case PSMZ16: packed_z_shift |= 1u << (4 * i); break;
+			case PSMZ24: packed_z_shift |= 2u << (4 * i); break;
+			case PSMZ32: packed_z_shift |= 3u << (4 * i); break;
+			default: break;
+			}
+			if (in.sampling_rate_y_log2 == 0)
+				continue;
+			switch (depth_psm)
+			{
+			case PSMZ16S: case PSMZ16: zsb = 8; zs = 0; zmax = 0xffffu; break;
+			case PSMZ24: zsb = 16; zs = 0; zmax = 0xffffffu; break;
+			case PSMZ32: zsb = 16; zs = 8; zmax = 0xffffffffu; break;
+			default: break;
+			}
+			H.z_shift_bucket[i] = zsb;
+			H.z_shift[i] = zs;
+			H.z_max[i] = zmax;
+			H.instance_mask |= 1u << i;
+		}
 	}
 
 	static bool instance_hazards(const PassOp &p, uint8_t *mask)

@@ -73,6 +73,31 @@ struct TexImage
 	uint32_t padding;
 };
 
+// Flat-primitive depth buckets found by triangle setup in a super-sampled pass
+// (SingleSampleHeuristic, gs/shaders/data_structures.h:190-195).  Each of the
+// 256 buckets covers 2^16 (2^8 for 16-bit Z) depth values.
+struct SsHeuristic
+{
+	uint32_t bucket_count;
+	uint32_t active[8];
+	uint32_t bucket[256];
+};
+
+// Per-instance depth quantisation for the heuristic
+// (dispatch_single_sample_heuristic, gs/gs_renderer.cpp:1979-2039).
+struct HeuristicParams
+{
+	uint32_t z_shift_bucket[8];
+	uint32_t z_shift[8];
+	uint32_t z_max[8];
+	uint32_t instance_mask;
+};
+
+// Decision of the heuristic for one primitive, applied after every bucket has
+// been evaluated against the states triangle setup produced.
+constexpr uint8_t HEURISTIC_SET_SNAP_RASTER = 1;
+constexpr uint8_t HEURISTIC_CLEAR_SNAP_ATTRIBUTE = 2;
+
 struct PassParams
 {
 	const pgs_vertex_position *pos;
@@ -96,6 +121,11 @@ struct PassParams
 	const float *unorm_lut;
 	uint32_t *error_flags;
 	unsigned long long *fragment_counter;
+	// 4 bits per instance: flat-primitive bucket shift / 8 (z_shift_to_bucket,
+	// gs/gs_renderer.cpp:1914-1934).
+	uint32_t packed_z_shift;
+	SsHeuristic *heuristic;
+	uint8_t *heuristic_action;
 };
 
 // Per-tile flag bits written by bin_kernel.
@@ -507,14 +537,221 @@ __global__ void __launch_bounds__(128) setup_kernel(PassParams P)
 			per_sample = di[2] != 0.0f || dj[2] != 0.0f;
 		if (!per_sample)
 			per_sample = za != zb || zb != zc;
-		if (!per_sample && !line)
-			new_state |= 1u << STATE_BIT_SNAP_ATTRIBUTE;
+		if (!per_sample)
+		{
+			// Flat primitive: snap attributes and register its depth bucket
+			// for the single-sample heuristic (triangle_setup.comp:826-871).
+			if (!line)
+				new_state |= 1u << STATE_BIT_SNAP_ATTRIBUTE;
+			uint32_t inst = (st >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u;
+			uint32_t z_shift = ((P.packed_z_shift >> (4 * inst)) & 15u) * 8u;
+			uint32_t bucket = min(255u, z_shift >= 32 ? 0u : za >> z_shift);
+			uint32_t old = atomicOr(&P.heuristic->active[bucket >> 5], 1u << (bucket & 31));
+			if (((old >> (bucket & 31)) & 1u) == 0)
+			{
+				uint32_t slot = atomicAdd(&P.heuristic->bucket_count, 1u);
+				P.heuristic->bucket[slot] = bucket;
+			}
+		}
 	}
 
 	P.setup[index] = out;
 	P.tattr[index] = ta;
 	P.prims[index].state = new_state;
 	P.prims[index].tex = tex;
+}
+
+// ---------------------------------------------------------------------------
+// Single-sample heuristic (single_sample_heuristic.comp:148-291): for every
+// depth bucket that holds a flat primitive, decide which flat primitives are
+// UI elements to rasterise single-sampled (SNAP_RASTER) and which sit inside
+// the 3D depth range and go back to full SSAA (SNAP_ATTRIBUTE cleared).
+// One CTA per (bucket, instance); 3 x 64K-bit masks in shared memory.
+// Decisions go to P.heuristic_action so that every bucket reads the states
+// triangle setup wrote, whatever order the CTAs run in.
+
+__device__ __forceinline__ uint32_t heuristic_hash_vertex(const pgs_vertex_position &v)
+{
+	// Three rounds of ((s >> 8) ^ s.yzx) * 1103515245 (:86-94).
+	uint32_t x = uint32_t(v.x), y = uint32_t(v.y), z = v.z;
+	#pragma unroll
+	for (int r = 0; r < 3; r++)
+	{
+		uint32_t nx = ((x >> 8) ^ y) * 1103515245u;
+		uint32_t ny = ((y >> 8) ^ z) * 1103515245u;
+		uint32_t nz = ((z >> 8) ^ x) * 1103515245u;
+		x = nx; y = ny; z = nz;
+	}
+	return x >> 16;
+}
+
+constexpr uint32_t HEURISTIC_MASK_WORDS = 65536 / 32;
+
+__global__ void __launch_bounds__(1024) single_sample_heuristic_kernel(PassParams P, HeuristicParams H)
+{
+	const uint32_t inst = blockIdx.y;
+	if (((H.instance_mask >> inst) & 1u) == 0)
+		return;
+	if (blockIdx.x >= P.heuristic->bucket_count)
+		return;
+
+	__shared__ uint32_t full3d[HEURISTIC_MASK_WORDS];
+	__shared__ uint32_t candidate[HEURISTIC_MASK_WORDS];
+	__shared__ uint32_t shared_vertex[HEURISTIC_MASK_WORDS];
+	__shared__ uint32_t any_full3d, min_z, max_z;
+
+	const uint32_t tid = threadIdx.x, nthreads = blockDim.x;
+	for (uint32_t i = tid; i < HEURISTIC_MASK_WORDS; i += nthreads)
+	{
+		full3d[i] = 0;
+		candidate[i] = 0;
+		shared_vertex[i] = 0;
+	}
+	if (tid == 0)
+	{
+		any_full3d = 0;
+		min_z = ~0u;
+		max_z = 0;
+	}
+	__syncthreads();
+
+	const uint32_t z_shift = H.z_shift[inst], z_max = H.z_max[inst];
+	uint32_t zlo = P.heuristic->bucket[blockIdx.x];
+	uint32_t zhi = ((zlo + 1) << H.z_shift_bucket[inst]) - 1;
+	zlo <<= H.z_shift_bucket[inst];
+
+	const uint32_t SA = 1u << STATE_BIT_SNAP_ATTRIBUTE, SR = 1u << STATE_BIT_SNAP_RASTER;
+	const uint32_t LINE = 1u << STATE_BIT_LINE;
+	const uint32_t NO_FULL_3D = (1u << STATE_BIT_SPRITE) | LINE | SA;
+	const uint32_t n = P.num_prims;
+	auto inst_of = [](uint32_t st) { return (st >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u; };
+	auto snap = [&](uint32_t z) { return min(z_max, z) >> z_shift; };
+
+	// Pass 1: depth values used by 3D primitives, and flat candidates.
+	uint32_t lmin = ~0u, lmax = 0, lany = 0;
+	for (uint32_t i = tid; i < n; i += nthreads)
+	{
+		uint32_t st = P.prims[i].state;
+		if (inst_of(st) != inst)
+			continue;
+		if ((st & NO_FULL_3D) == 0)
+		{
+			#pragma unroll
+			for (int k = 0; k < 3; k++)
+			{
+				uint32_t z = P.pos[3 * i + k].z;
+				lmin = min(lmin, z);
+				lmax = max(lmax, z);
+				uint32_t s = snap(z);
+				if (s >= zlo && s <= zhi)
+					atomicOr(&full3d[(s - zlo) >> 5], 1u << ((s - zlo) & 31));
+			}
+			lany = 1;
+		}
+		else if ((st & (SA | SR)) == SA || (st & LINE) != 0)
+		{
+			uint32_t s = snap(P.pos[3 * i].z);
+			if (s >= zlo && s <= zhi)
+				atomicOr(&candidate[(s - zlo) >> 5], 1u << ((s - zlo) & 31));
+		}
+	}
+	lmin = __reduce_min_sync(0xffffffffu, lmin);
+	lmax = __reduce_max_sync(0xffffffffu, lmax);
+	lany = __reduce_or_sync(0xffffffffu, lany);
+	if ((tid & 31) == 0)
+	{
+		atomicMin(&min_z, lmin);
+		atomicMax(&max_z, lmax);
+		if (lany)
+			any_full3d = 1;
+	}
+	__syncthreads();
+
+	// Pass 2: hash the vertices of 3D primitives whose depth is a candidate.
+	for (uint32_t i = tid; i < n; i += nthreads)
+	{
+		uint32_t st = P.prims[i].state;
+		if (inst_of(st) != inst || (st & NO_FULL_3D) != 0)
+			continue;
+		#pragma unroll
+		for (int k = 0; k < 3; k++)
+		{
+			pgs_vertex_position v = P.pos[3 * i + k];
+			uint32_t s = snap(v.z);
+			if (s >= zlo && s <= zhi && ((candidate[(s - zlo) >> 5] >> ((s - zlo) & 31)) & 1u))
+			{
+				uint32_t h = heuristic_hash_vertex(v);
+				atomicOr(&shared_vertex[h >> 5], 1u << (h & 31));
+			}
+		}
+	}
+	__syncthreads();
+
+	// Pass 3: a flat candidate that shares a vertex with a 3D primitive at a
+	// depth the 3D geometry uses keeps its depth out of demotion.
+	for (uint32_t i = tid; i < n; i += nthreads)
+	{
+		uint32_t st = P.prims[i].state;
+		if (inst_of(st) != inst || (st & (SA | SR)) != SA)
+			continue;
+		uint32_t s = snap(P.pos[3 * i].z);
+		if (s < zlo || s > zhi)
+			continue;
+		uint32_t o = s - zlo;
+		if (((full3d[o >> 5] >> (o & 31)) & 1u) == 0)
+			continue;
+		bool conflict = false;
+		#pragma unroll
+		for (int k = 0; k < 3; k++)
+		{
+			uint32_t h = heuristic_hash_vertex(P.pos[3 * i + k]);
+			conflict |= ((shared_vertex[h >> 5] >> (h & 31)) & 1u) != 0;
+		}
+		if (conflict)
+			atomicAnd(&candidate[o >> 5], ~(1u << (o & 31)));
+	}
+	__syncthreads();
+
+	// Pass 4: decisions.
+	const bool force_single_sample = any_full3d == 0;
+	const uint32_t zmin3d = min_z, zmax3d = max_z;
+	for (uint32_t i = tid; i < n; i += nthreads)
+	{
+		uint32_t z = P.pos[3 * i].z;
+		uint32_t s = snap(z);
+		if (s < zlo || s > zhi)
+			continue;
+		uint32_t st = P.prims[i].state;
+		if (inst_of(st) != inst)
+			continue;
+		bool tri_candidate = (st & (SA | SR)) == SA;
+		bool line_candidate = force_single_sample && (st & LINE) != 0;
+		if (!tri_candidate && !line_candidate)
+			continue;
+		uint32_t o = s - zlo;
+		if ((candidate[o >> 5] >> (o & 31)) & 1u)
+			P.heuristic_action[i] = HEURISTIC_SET_SNAP_RASTER;
+		else if ((st & ((1u << STATE_BIT_Z_TEST) | (1u << STATE_BIT_Z_WRITE))) != 0 && z > zmin3d && z < zmax3d)
+			P.heuristic_action[i] = HEURISTIC_CLEAR_SNAP_ATTRIBUTE;
+	}
+}
+
+// Applies and clears the heuristic's decisions.
+__global__ void __launch_bounds__(256) heuristic_apply_kernel(PassParams P)
+{
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= P.num_prims)
+		return;
+	uint8_t a = P.heuristic_action[i];
+	if (a == 0)
+		return;
+	uint32_t st = P.prims[i].state;
+	if (a == HEURISTIC_SET_SNAP_RASTER)
+		st |= 1u << STATE_BIT_SNAP_RASTER;
+	else
+		st &= ~(1u << STATE_BIT_SNAP_ATTRIBUTE);
+	P.prims[i].state = st;
+	P.heuristic_action[i] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1169,7 +1406,9 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 }
 
 // Sample position within its pixel for sample s (32-wide subgroup layout of
-// ubershader.comp get_tile_info).
+// ubershader.comp get_tile_info, :253-340).  Ordered grids interleave x/y
+// lane bits; a 2:1 grid is a checkerboard; a 4:1 grid puts one sample per
+// high-res row at x offsets 0, 2, 3, 1 (the 0x78 pattern, :333-338).
 __device__ __forceinline__ void sample_offset(uint32_t s, uint32_t xl, uint32_t yl, int32_t &ox, int32_t &oy)
 {
 	uint32_t b0 = s & 1u, b1 = (s >> 1) & 1u, b2 = (s >> 2) & 1u, b3 = (s >> 3) & 1u;
@@ -1177,6 +1416,11 @@ __device__ __forceinline__ void sample_offset(uint32_t s, uint32_t xl, uint32_t 
 	{
 		ox = int32_t(b1 | (b3 << 1));
 		oy = int32_t(b0 | (b2 << 1));
+	}
+	else if (yl == xl + 2)
+	{
+		oy = int32_t(s & ((1u << yl) - 1u));
+		ox = int32_t(((s >> yl) << 2) + ((0x78u >> ((oy & 3) * 2)) & 3u));
 	}
 	else
 	{

@@ -358,3 +358,166 @@ def frame_c2(seed: int = 2, num_triangles: int = 50000, num_sprites: int = 2000,
             s.packed(prim_reg(PRIM_SPRITE, iip=1, tme=1, abe=1), [D_ST, D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
     return Frame("c2", s.tobytes(), super_sampling, True, num_triangles + num_sprites,
                  {"width": width, "height": height, "fbp": 0, "zbp": zbp})
+
+
+def _mesh(rng, gx, gy, width, height, zlo, zhi):
+    """A jittered grid mesh as a triangle list; returns (x, y, z) of shape (n, 3) in 12.4."""
+    xs = np.linspace(8, width - 8, gx)
+    ys = np.linspace(8, height - 8, gy)
+    px = np.round((xs[None, :] + rng.uniform(-3, 3, (gy, gx))) * 16).astype(np.int64)
+    py = np.round((ys[:, None] + rng.uniform(-3, 3, (gy, gx))) * 16).astype(np.int64)
+    pz = rng.integers(zlo, zhi, size=(gy, gx), dtype=np.int64)
+    tris = []
+    for j in range(gy - 1):
+        for i in range(gx - 1):
+            tris.append(((j, i), (j, i + 1), (j + 1, i)))
+            tris.append(((j, i + 1), (j + 1, i + 1), (j + 1, i)))
+    idx = np.array(tris)
+    return px[idx[..., 0], idx[..., 1]], py[idx[..., 0], idx[..., 1]], pz[idx[..., 0], idx[..., 1]]
+
+
+def frame_flat_ui(seed: int = 5, super_sampling: int = 4, zpsm: int = PSMZ24, width: int = 640,
+                  height: int = 448, grid: int = 24, num_flat: int = 400, num_lines: int = 64) -> Frame:
+    """Super-sampled pass mixing a 3D mesh with flat (constant-Z) triangles and lines.
+
+    Exercises the single-sample heuristic (triangle_setup.comp:826-871 and
+    single_sample_heuristic.comp): flat triangles that share a vertex with the
+    3D mesh at a depth the mesh uses, flat triangles at mesh depths without a
+    shared vertex, flat UI triangles in front of the mesh, flat lines, and a
+    second framebuffer with flat primitives only (every flat line demoted)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = GifStream()
+    zbits = {PSMZ16: 16, PSMZ16S: 16, PSMZ24: 24, PSMZ32: 32}[zpsm]
+    zmax = (1 << zbits) - 1
+    fb_pages = (width * height * 4 + PAGE_BYTES - 1) // PAGE_BYTES
+    zbp = fb_pages
+    fb2 = 2 * fb_pages
+    _frame_setup(s, 0, width // 64, PSMCT32, zbp, zpsm, width, height, test_reg(zte=1, ztst=2),
+                 extra=[(COLCLAMP, 1)])
+
+    def emit(prim, x, y, z):
+        n = x.shape[0]
+        nv = n * x.shape[1]
+        rgba = rng.integers(0, 256, size=(nv, 4), dtype=np.int64)
+        q = np.zeros((nv, 2, 2), dtype=np.uint64)
+        q[:, 0] = q_rgbaq(rgba)
+        q[:, 1] = q_xyz2(x.reshape(nv), y.reshape(nv), z.reshape(nv))
+        s.packed(prim, [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+
+    def flat_tris(n, zvals, lo=2.0, hi=600.0):
+        x, y = random_triangles(rng, n, width, height, lo, hi)
+        return x, y, np.repeat(np.asarray(zvals, dtype=np.int64)[:, None], 3, axis=1)
+
+    # 3D mesh in the middle of the depth range.
+    z3lo, z3hi = zmax // 8, zmax // 2
+    mx, my, mz = _mesh(rng, grid, grid * height // width + 2, width, height, z3lo, z3hi)
+    emit(prim_reg(PRIM_TRI, iip=1), mx, my, mz)
+
+    nq = num_flat // 4
+    # Flat triangles sharing one mesh vertex and its depth.
+    pick = rng.integers(0, mx.shape[0], nq)
+    corner = rng.integers(0, 3, nq)
+    sx, sy, sz = flat_tris(nq, mz[pick, corner])
+    sx[:, 0], sy[:, 0] = mx[pick, corner], my[pick, corner]
+    emit(prim_reg(PRIM_TRI, iip=1), sx, sy, sz)
+    # Flat triangles at mesh depths, no shared vertex.
+    pick = rng.integers(0, mx.shape[0], nq)
+    emit(prim_reg(PRIM_TRI, iip=1), *flat_tris(nq, mz[pick, 0]))
+    # Flat triangles at depths inside the mesh range that the mesh does not use.
+    emit(prim_reg(PRIM_TRI, iip=1), *flat_tris(nq, rng.integers(z3lo, z3hi, nq) | 1))
+    # UI in front of everything, few distinct depths.
+    emit(prim_reg(PRIM_TRI, iip=1), *flat_tris(num_flat - 3 * nq, zmax - rng.integers(0, 4, num_flat - 3 * nq)))
+    # Flat lines, in front and at mesh depths.
+    lx, ly = random_sprites(rng, num_lines, width, height, 16.0, 4000.0)
+    lz = np.where(rng.uniform(size=num_lines) < 0.5, zmax - 1, mz[rng.integers(0, mx.shape[0], num_lines), 0])
+    emit(prim_reg(PRIM_LINE, iip=1), lx, ly, np.repeat(lz[:, None], 2, axis=1))
+
+    # Second framebuffer: flat primitives only.
+    s.ad([(FRAME_1, frame_reg(fb2, width // 64, PSMCT32))])
+    emit(prim_reg(PRIM_TRI, iip=1), *flat_tris(nq, rng.integers(0, zmax, nq)))
+    lx, ly = random_sprites(rng, num_lines, width, height, 16.0, 4000.0)
+    emit(prim_reg(PRIM_LINE, iip=1), lx, ly, np.repeat(rng.integers(0, zmax, num_lines)[:, None], 2, axis=1))
+    nprims = mx.shape[0] + num_flat + num_lines + nq + num_lines
+    return Frame("flat_ui", s.tobytes(), super_sampling, True, nprims,
+                 {"width": width, "height": height, "fbp": 0, "zbp": zbp, "fb2": fb2})
+
+
+def _textured_draw(rng, n, width, height, area_lo_small, area_hi_small, area_lo_big, area_hi_big, big_frac):
+    """n triangles, a `big_frac` share with large areas; returns x, y (n, 3) in 12.4."""
+    big = rng.uniform(size=n) < big_frac
+    nb = int(big.sum())
+    x = np.zeros((n, 3), dtype=np.int64)
+    y = np.zeros((n, 3), dtype=np.int64)
+    if nb:
+        x[big], y[big] = random_triangles(rng, nb, width, height, area_lo_big, area_hi_big)
+    if n - nb:
+        x[~big], y[~big] = random_triangles(rng, n - nb, width, height, area_lo_small, area_hi_small)
+    return x, y
+
+
+def frame_c4(seed: int = 4, super_sampling: int = 8, num_triangles: int = 100000, passes: int = 10,
+             draws_per_pass: int = 50, feedback_frac: float = 0.2, width: int = 640, height: int = 448) -> Frame:
+    """High-rate SSAA with render-to-texture feedback.
+
+    640x448 PSMCT32 + PSMZ24 at 8x (2x4) or 16x (4x4).  `passes` passes, each
+    opened by TEXFLUSH and a FRAME switch between two framebuffers A and B.
+    80% of the triangles have areas log-uniform in [1, 16] px, 20% in
+    [16, 4000].  A `feedback_frac` share of the draws samples the framebuffer the
+    previous pass rendered (TBP0 on pages written earlier in the frame, CT32,
+    bilinear, clamped to its top 512x256 region), so the sampled pages never
+    overlap the framebuffer being drawn; the others are Gouraud or PSMT8
+    textured.  Z GEQUAL throughout; feedback draws blend Cs over Cd by As."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = GifStream()
+    fb_pages = (width * height * 4 + PAGE_BYTES - 1) // PAGE_BYTES
+    fbw = width // 64
+    fb_a, zbp, fb_b = 0, fb_pages, 2 * fb_pages
+    tex_base = 3 * fb_pages
+    _frame_setup(s, fb_a, fbw, PSMCT32, zbp, PSMZ24, width, height, test_reg(zte=1, ztst=2),
+                 alpha=alpha_reg(0, 1, 0, 1),
+                 extra=[(COLCLAMP, 1), (TEX1_1, tex1_reg(mmag=1, mmin=1)), (TEXA, texa_reg(0, 0, 0x80))])
+    tex0s, _ = _texture_set(rng, s, tex_base, 4, 7, 7, PSMT8)
+    per_pass = np.full(passes, num_triangles // passes)
+    per_pass[: num_triangles % passes] += 1
+    for p in range(passes):
+        fb = fb_a if p % 2 == 0 else fb_b
+        other = fb_b if p % 2 == 0 else fb_a
+        s.ad([(TEXFLUSH, 0), (FRAME_1, frame_reg(fb, fbw, PSMCT32))])
+        per_draw = np.full(draws_per_pass, int(per_pass[p]) // draws_per_pass)
+        per_draw[: int(per_pass[p]) % draws_per_pass] += 1
+        for d in range(draws_per_pass):
+            n = int(per_draw[d])
+            if n == 0:
+                continue
+            kind = rng.uniform()
+            x, y = _textured_draw(rng, n, width, height, 1.0, 16.0, 16.0, 4000.0, 0.2)
+            z = rng.integers(0, 1 << 24, size=(n, 3), dtype=np.int64)
+            rgba = rng.integers(0, 256, size=(n, 3, 4), dtype=np.int64)
+            nv = n * 3
+            if p > 0 and kind < feedback_frac:
+                s.ad([(TEX0_1, tex0_reg(other * BLOCKS_PER_PAGE, fbw, PSMCT32, 9, 8, tcc=1, tfx=0)),
+                      (CLAMP_1, clamp_reg(1, 1))])
+                u = rng.integers(0, 512 * 16, size=(n, 3), dtype=np.int64)
+                v = rng.integers(0, 256 * 16, size=(n, 3), dtype=np.int64)
+                q = np.zeros((nv, 3, 2), dtype=np.uint64)
+                q[:, 0] = q_uv(u.reshape(nv), v.reshape(nv))
+                q[:, 1] = q_rgbaq(rgba.reshape(nv, 4))
+                q[:, 2] = q_xyz2(x.reshape(nv), y.reshape(nv), z.reshape(nv))
+                s.packed(prim_reg(PRIM_TRI, iip=1, tme=1, abe=1, fst=1), [D_UV, D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+            elif kind < 0.6:
+                s.ad([(TEX0_1, tex0s[int(rng.integers(0, len(tex0s)))]), (CLAMP_1, clamp_reg(0, 0))])
+                sn = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+                tn = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+                qv = np.ones((n, 3), dtype=np.float32)
+                q = np.zeros((nv, 3, 2), dtype=np.uint64)
+                q[:, 0] = q_st(sn.reshape(nv), tn.reshape(nv), qv.reshape(nv))
+                q[:, 1] = q_rgbaq(rgba.reshape(nv, 4))
+                q[:, 2] = q_xyz2(x.reshape(nv), y.reshape(nv), z.reshape(nv))
+                s.packed(prim_reg(PRIM_TRI, iip=1, tme=1), [D_ST, D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+            else:
+                q = np.zeros((nv, 2, 2), dtype=np.uint64)
+                q[:, 0] = q_rgbaq(rgba.reshape(nv, 4))
+                q[:, 1] = q_xyz2(x.reshape(nv), y.reshape(nv), z.reshape(nv))
+                s.packed(prim_reg(PRIM_TRI, iip=1), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+    return Frame("c4", s.tobytes(), super_sampling, super_sampling != 8, num_triangles,
+                 {"width": width, "height": height, "fbp": fb_a, "fb_b": fb_b, "zbp": zbp})

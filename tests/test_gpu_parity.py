@@ -85,3 +85,40 @@ def test_record_replay_reproduces_frame():
         be.close()
     assert np.array_equal(first, again)
     assert np.array_equal(first, graph)
+
+
+@pytest.mark.parametrize("ss,ordered", [(2, True), (4, False), (8, False), (16, True), (16, False)])
+def test_c2_small_sampling_rates(ss, ordered):
+    """Every sampling grid the frontend offers: 2x, 4x sparse, 8x (2x4), 16x ordered and sparse."""
+    f = gsgen.frame_c2(seed=7, num_triangles=400, num_sprites=40, super_sampling=ss, num_textures=2)
+    f.ordered = ordered
+    ref, out = run_both(f)
+    assert_same(ref, out)
+
+
+@pytest.mark.parametrize("zpsm", [gsgen.PSMZ16, gsgen.PSMZ24, gsgen.PSMZ32])
+def test_flat_ui_single_sample_heuristic(zpsm):
+    """Flat UI triangles and lines next to a 3D mesh at 4x: the single-sample
+    heuristic's demotions must match the oracle's."""
+    ref, out = run_both(gsgen.frame_flat_ui(zpsm=zpsm))
+    assert_same(ref, out)
+
+
+@pytest.mark.parametrize("ss", [8, 16])
+def test_flat_ui_high_rates(ss):
+    ref, out = run_both(gsgen.frame_flat_ui(seed=6, super_sampling=ss))
+    assert_same(ref, out)
+
+
+@pytest.mark.parametrize("ss", [8, 16])
+def test_c4_feedback_small(ss):
+    """Render-to-texture feedback across 10 passes with texture-hazard flushes."""
+    ref, out = run_both(gsgen.frame_c4(seed=12, super_sampling=ss, num_triangles=8000))
+    assert_same(ref, out)
+
+
+@pytest.mark.parametrize("ss", [8, 16])
+def test_c4_full_size(ss):
+    """8x / 16x at its benchmark size: 100k triangles over 10 feedback passes."""
+    ref, out = run_both(gsgen.frame_c4(seed=4, super_sampling=ss))
+    assert_same(ref, out)
