@@ -38,6 +38,20 @@ sys.path.insert(0, str(ROOT / "parallel-gs_gb300"))
 METRIC = "bit-exact GS frames/s + Gfrag/s on 1 GB300; upscaler px/s at PSNR vs 16x SSAA"
 WORKLOAD = "textured+blended 640x448 CT32/Z24, 50k STQ tris + 2k sprites, 8x PSMT8 256^2 + CT32 CLUT, bilinear, ATST>0x40, FBA, dither, 4x SSAA"
 
+# Other workloads for --workload (the default line is c2).  Each entry: a
+# description and the gsgen call that builds the frame.
+WORKLOADS = {
+    "c2": (WORKLOAD, "gsgen.frame_c2(num_triangles={triangles}, num_sprites={sprites}, super_sampling={ss})"),
+    "c1": ("plain 640x448 CT32/Z24, 10k Gouraud tris, Z GEQUAL, 1x", "gsgen.frame_c1()"),
+    "c4x8": ("feedback 640x448 CT32/Z24, 100k tris (80% 1-16 px), 10 passes, 20% draws sample the previous "
+             "pass's framebuffer, 8x SSAA (2x4)", "gsgen.frame_c4(super_sampling=8)"),
+    "c4x16": ("feedback 640x448 CT32/Z24, 100k tris (80% 1-16 px), 10 passes, 20% draws sample the previous "
+              "pass's framebuffer, 16x SSAA (4x4)", "gsgen.frame_c4(super_sampling=16)"),
+}
+# Texture and CLUT bytes uploaded per frame.
+TEXTURE_BYTES = {"c2": 8 * (256 * 256 + 16 * 16 * 4), "c1": 0, "c4x8": 4 * (128 * 128 + 16 * 16 * 4),
+                 "c4x16": 4 * (128 * 128 + 16 * 16 * 4)}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -45,11 +59,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gs_gb300", choices=["gs_gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--triangles", type=int, default=50000)
     ap.add_argument("--sprites", type=int, default=2000)
     ap.add_argument("--super-sampling", type=int, default=4)
     ap.add_argument("--no-verify", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the CPU baseline and the e2e leg (profiling runs)")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the single-thread oracle timing")
     return ap.parse_args()
 
 
@@ -127,7 +143,8 @@ def algorithmic_bytes(frame, ss: int) -> dict:
     px = w * h
     p = frame.num_primitives
     planes = 1 if ss == 1 else 2 + ss
-    fbz = 2 * (4 + 4) * px * (planes - 1 if ss > 1 else 1) + (2 * 8 * px if ss > 1 else 0)
+    passes = frame.meta.get("passes", 1)
+    fbz = passes * (2 * (4 + 4) * px * (planes - 1 if ss > 1 else 1) + (2 * 8 * px if ss > 1 else 0))
     setup_rw = (80 + 64 + 32) * p * 2
     records = 152 * p
     textures = frame.meta.get("texture_bytes", 0)
@@ -159,8 +176,7 @@ def run_reference(args, frame):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+fp32",
         "data": "synthetic (seeded GS command stream)",
-        "config": {"workload": WORKLOAD, "triangles": args.triangles, "sprites": args.sprites,
-                   "super_sampling": args.super_sampling},
+        "config": workload_config(args, frame),
         "gfrag_per_s": frags * fps / 1e9,
         "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
                          "sample": "full frame, %d steps, oracle_backend.cpp with OpenMP over tiles" % args.steps},
@@ -168,16 +184,35 @@ def run_reference(args, frame):
     }
 
 
-def cpu_baseline_sample(frame) -> dict:
+def workload_expr(args) -> str:
+    return WORKLOADS[args.workload][1].format(triangles=args.triangles, sprites=args.sprites,
+                                              ss=args.super_sampling)
+
+
+def make_frame(args):
+    import gsgen  # noqa: F401,E402
+    frame = eval(workload_expr(args), {"gsgen": gsgen})
+    frame.meta["texture_bytes"] = TEXTURE_BYTES[args.workload]
+    return frame
+
+
+def workload_config(args, frame) -> dict:
+    cfg = {"workload": WORKLOADS[args.workload][0], "primitives": frame.num_primitives,
+           "super_sampling": frame.super_sampling}
+    if args.workload == "c2":
+        cfg.update({"triangles": args.triangles, "sprites": args.sprites})
+    return cfg
+
+
+def cpu_baseline_sample(args) -> dict:
     """Oracle on one host thread over one full frame (bounded: ~15-30 s)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     env = dict(os.environ, OMP_NUM_THREADS="1")
     code = ("import sys,time; sys.path.insert(0,%r); sys.path.insert(0,%r);"
             "import gsgen,pgs_oracle;"
-            "f=gsgen.frame_c2(num_triangles=%d,num_sprites=%d,super_sampling=%d);"
+            "f=%s;"
             "t=time.perf_counter(); pgs_oracle.render(f); print(time.perf_counter()-t)") % (
-        str(ROOT / "parallel-gs_gb300"), str(ROOT / "oracle"), frame.meta["triangles"], frame.meta["sprites"],
-        frame.super_sampling)
+        str(ROOT / "parallel-gs_gb300"), str(ROOT / "oracle"), workload_expr(args))
     try:
         out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=240)
         dt = float(out.stdout.strip().splitlines()[-1])
@@ -192,11 +227,7 @@ def main():
     rank, world, local = dist_env()
     import gsgen  # noqa: E402
 
-    frame = gsgen.frame_c2(num_triangles=args.triangles, num_sprites=args.sprites,
-                           super_sampling=args.super_sampling)
-    frame.meta["triangles"] = args.triangles
-    frame.meta["sprites"] = args.sprites
-    frame.meta["texture_bytes"] = 8 * (256 * 256 + 16 * 16 * 4)
+    frame = make_frame(args)
 
     if args.impl == "reference":
         if rank != 0:
@@ -220,7 +251,7 @@ def main():
     stream = torch.cuda.ExternalStream(backend.stream(), device=local)
 
     # Record the frame program.
-    gs = pgs.GSInterface(backend, super_sampling=frame.super_sampling)
+    gs = pgs.GSInterface(backend, super_sampling=frame.super_sampling, ordered=frame.ordered)
     backend.begin_record()
     gs.gif_transfer(0, frame.data)
     gs.flush()
@@ -264,18 +295,27 @@ def main():
         total_ms = max_over_ranks(total_ms, pg, "cuda:%d" % local)
     fps = replica_throughput(args.steps, world, total_ms)
 
-    # End to end through the public API from host memory.
-    e2e_steps = 0 if args.quick else max(3, min(args.steps, 10))
-    vram = np.empty(pgs.VRAM_SIZE, dtype=np.uint8)
-    gs2 = pgs.GSInterface(backend, super_sampling=frame.super_sampling)
+    # End to end through the public API from host memory: every step decodes
+    # the frame's GIF stream on the host, uploads its records and payloads,
+    # renders, and reads the 4 MiB GS VRAM back into pinned host memory.  The
+    # readback of frame k is waited for after frame k+1 has been decoded, so
+    # host decoding overlaps the GPU as in an emulator's frame loop.
+    e2e_steps = 0 if args.quick else max(5, min(args.steps, 20))
+    vram = [torch.empty(pgs.VRAM_SIZE, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(2)]
+    gs2 = pgs.GSInterface(backend, super_sampling=frame.super_sampling, ordered=frame.ordered)
     gs2.gif_transfer(0, frame.data)
-    gs2.read_vram(out=vram)
+    gs2.read_vram(out=vram[0])
     torch.cuda.synchronize()
     st0 = backend.stats()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    tickets = []
+    for k in range(e2e_steps):
         gs2.gif_transfer(0, frame.data)
-        gs2.read_vram(out=vram)
+        tickets.append(gs2.read_vram_async(vram[k % 2]))
+        if k >= 1:
+            gs2.wait(tickets[k - 1])
+    if tickets:
+        gs2.wait(tickets[-1])
     e2e_dt = time.perf_counter() - t0
     st1 = backend.stats()
     h2d = (st1["h2d_bytes"] - st0["h2d_bytes"]) // max(e2e_steps, 1)
@@ -298,14 +338,13 @@ def main():
     frags = frags_per_frame
     shade_s = statistics.mean(shade_ms) / 1000.0
     achieved = ab["shade"] / shade_s / 1e9
-    cpu = None if args.quick else cpu_baseline_sample(frame)
+    cpu = None if (args.quick or args.no_cpu_baseline) else cpu_baseline_sample(args)
     out = {
         "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32+fp32", "data": "synthetic (seeded GS command stream)",
-        "config": {"workload": WORKLOAD, "triangles": args.triangles, "sprites": args.sprites,
-                   "super_sampling": args.super_sampling, "l2": "flushed (256 MiB write) between steps",
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": dict(workload_config(args, frame), l2="flushed (256 MiB write) between steps",
+                       parallelism="replicas" if world > 1 else "single"),
         "gfrag_per_s": frags * fps / 1e9,
         "fragments_per_frame": frags,
         "shade_ms_per_frame": statistics.mean(shade_ms),

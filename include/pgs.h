@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define PGS_ABI_VERSION 1u
+#define PGS_ABI_VERSION 2u
 
 /* ------------------------------------------------------------------ */
 /* Status codes                                                        */
@@ -197,7 +197,9 @@ typedef struct pgs_backend_ops
 	uint32_t abi_version;
 	void (*destroy)(void *self);
 	/* GSRenderer::reserve_primitive_buffers + get_reserved_* (gs/gs_renderer.hpp:251-254).
-	 * The frontend writes records straight into backend-owned host memory. */
+	 * The frontend writes records straight into backend-owned host memory; the
+	 * buffers belong to the backend again from flush_rendering until the next
+	 * reserve_primitive_buffers call. */
 	int (*reserve_primitive_buffers)(void *self, uint32_t num_primitives,
 	                                 pgs_vertex_position **positions,
 	                                 pgs_vertex_attribute **attributes,
@@ -222,6 +224,14 @@ typedef struct pgs_backend_ops
 	int (*write_vram)(void *self, uint64_t offset, uint64_t size, const void *src);
 	/* Sticky device error flags (bin overflow, bounded-wait expiry). */
 	int (*get_error)(void *self, uint32_t *flags);
+	/* abi_version >= 2, optional (NULL: the frontend reads synchronously).
+	 * Queues a copy of [offset, offset+size) of plane 0 into dst behind all
+	 * submitted work and returns a ticket; dst must stay valid and untouched
+	 * until wait_ticket(ticket) returns.  This is the asynchronous side of the
+	 * reference's timeline-semaphore readback (GSRenderer::flush_readback +
+	 * wait_timeline, gs/gs_renderer.cpp:1037). */
+	int (*read_vram_async)(void *self, uint64_t offset, uint64_t size, void *dst, uint64_t *ticket);
+	int (*wait_ticket)(void *self, uint64_t ticket);
 } pgs_backend_ops;
 
 /* ------------------------------------------------------------------ */
@@ -324,6 +334,14 @@ int pgs_gs_write_register(pgs_gs *gs, uint32_t addr, uint64_t payload);
 int pgs_gs_flush(pgs_gs *gs);
 /* GSInterface::map_vram_read: flushes, waits and copies plane 0. */
 int pgs_gs_read_vram(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst);
+/* Flushes like pgs_gs_read_vram but only queues the copy: *ticket names it, and
+ * dst holds the VRAM contents as of this call once pgs_gs_wait(ticket) has
+ * returned.  Lets the caller decode the next frame while this one renders
+ * (the reference's asynchronous timeline, GSInterface + GSRenderer::wait_timeline,
+ * gs/gs_renderer.cpp:1037).  With a backend that has no asynchronous read the
+ * copy is made before returning and the ticket is 0. */
+int pgs_gs_read_vram_async(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst, uint64_t *ticket);
+int pgs_gs_wait(pgs_gs *gs, uint64_t ticket);
 /* GSInterface::map_vram_write + end_vram_write. */
 int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *src);
 /* GSInterface::read_transfer_fifo. */

@@ -2185,6 +2185,7 @@ static int o_error(void *, uint32_t *flags) { if (flags) *flags = 0; return 0; }
 
 static const pgs_backend_ops ORACLE_OPS = {
 	PGS_ABI_VERSION, o_destroy, o_reserve, o_flush_rendering, o_copy, o_palette, o_set_ss, o_submit, o_read, o_write, o_error,
+	nullptr, nullptr,
 };
 
 extern "C" {

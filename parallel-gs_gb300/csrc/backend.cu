@@ -70,6 +70,9 @@ struct PassOp
 	uint32_t tile_size_log2, has_aa1, has_scanmsk;
 	uint32_t num_instances;
 	pgs_rp_instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
+	// Host copy of the primitive records while the pass is submitted
+	// (null for recorded passes, which keep theirs in the host arena).
+	const pgs_primitive_attribute *host_prims;
 };
 
 struct Op
@@ -143,6 +146,19 @@ struct CudaBackend
 	bool shade_started = false;
 	uint64_t h2d_bytes = 0, d2h_bytes = 0, total_launches = 0, render_passes = 0;
 
+	// Asynchronous readbacks in flight.  A destination outside pinned memory
+	// is staged through a pinned slot and copied out by wait_ticket.
+	static constexpr int READBACK_SLOTS = 4;
+	struct Readback
+	{
+		uint64_t ticket = 0;
+		cudaEvent_t done = nullptr;
+		uint8_t *staging = nullptr;
+		void *dst = nullptr;
+		uint64_t size = 0;
+	} readbacks[READBACK_SLOTS];
+	uint64_t next_ticket = 1;
+
 	// ------------------------------------------------------------------
 	int init(const pgs_cuda_backend_options *opt)
 	{
@@ -192,6 +208,8 @@ struct CudaBackend
 			CUDA_TRY(cudaEventCreateWithFlags(&stage_done[i], cudaEventDisableTiming));
 			CUDA_TRY(cudaEventCreate(&shade_ev[i]));
 		}
+		for (auto &rb : readbacks)
+			CUDA_TRY(cudaEventCreateWithFlags(&rb.done, cudaEventDisableTiming));
 		return grow_arena(256u << 20);
 	}
 
@@ -232,6 +250,11 @@ struct CudaBackend
 			cudaFreeHost(h_stage[i]);
 			if (stage_done[i]) cudaEventDestroy(stage_done[i]);
 			if (shade_ev[i]) cudaEventDestroy(shade_ev[i]);
+		}
+		for (auto &rb : readbacks)
+		{
+			if (rb.done) cudaEventDestroy(rb.done);
+			cudaFreeHost(rb.staging);
 		}
 		if (stream)
 			cudaStreamDestroy(stream);
@@ -284,6 +307,22 @@ struct CudaBackend
 		off = arena_used;
 		arena_used += size;
 		return PGS_OK;
+	}
+
+	// Index of the staging buffer holding the render pass's records, or -1.
+	int staging_buffer_of(const pgs_render_pass *rp) const
+	{
+		const size_t N = PGS_MAX_PRIMITIVES_PER_FLUSH;
+		for (int i = 0; i < 2; i++)
+		{
+			const uint8_t *base = h_stage[i];
+			if (reinterpret_cast<const uint8_t *>(rp->positions) == base &&
+			    reinterpret_cast<const uint8_t *>(rp->attributes) == base + N * 3 * sizeof(pgs_vertex_position) &&
+			    reinterpret_cast<const uint8_t *>(rp->prims) ==
+			        base + N * 3 * (sizeof(pgs_vertex_position) + sizeof(pgs_vertex_attribute)))
+				return i;
+		}
+		return -1;
 	}
 
 	int upload_arena(size_t off, size_t size)
@@ -343,9 +382,26 @@ struct CudaBackend
 		p.prim_off = p.attr_off + align_up(attr_bytes, 256);
 		p.states_off = p.prim_off + align_up(prim_bytes, 256);
 		p.textures_off = p.states_off + align_up(st_bytes, 256);
-		memcpy(h_arena + p.pos_off, rp->positions, pos_bytes);
-		memcpy(h_arena + p.attr_off, rp->attributes, attr_bytes);
-		memcpy(h_arena + p.prim_off, rp->prims, prim_bytes);
+		// Records written by the frontend into a staging buffer go to the
+		// device straight from there; a recorded frame keeps a host copy.
+		int stage = recording ? -1 : staging_buffer_of(rp);
+		if (stage >= 0)
+		{
+			CUDA_TRY(cudaMemcpyAsync(d_arena + p.pos_off, rp->positions, pos_bytes, cudaMemcpyHostToDevice, stream));
+			CUDA_TRY(cudaMemcpyAsync(d_arena + p.attr_off, rp->attributes, attr_bytes, cudaMemcpyHostToDevice, stream));
+			CUDA_TRY(cudaMemcpyAsync(d_arena + p.prim_off, rp->prims, prim_bytes, cudaMemcpyHostToDevice, stream));
+			CUDA_TRY(cudaEventRecord(stage_done[stage], stream));
+			stage_pending[stage] = true;
+			h2d_bytes += pos_bytes + attr_bytes + prim_bytes;
+			p.host_prims = rp->prims;
+		}
+		else
+		{
+			memcpy(h_arena + p.pos_off, rp->positions, pos_bytes);
+			memcpy(h_arena + p.attr_off, rp->attributes, attr_bytes);
+			memcpy(h_arena + p.prim_off, rp->prims, prim_bytes);
+			p.host_prims = nullptr;
+		}
 		if (rp->num_states)
 			memcpy(h_arena + p.states_off, rp->states, rp->num_states * sizeof(pgs_state_vector));
 		if (rp->num_textures)
@@ -380,7 +436,7 @@ struct CudaBackend
 			p.num_texels = uint32_t(texels);
 			p.max_texels = max_texels;
 		}
-		r = upload_arena(base, total);
+		r = stage >= 0 ? upload_arena(p.states_off, total - (p.states_off - base)) : upload_arena(base, total);
 		if (r)
 			return r;
 
@@ -713,7 +769,8 @@ struct CudaBackend
 		// Per-instance primitive ranges and hazard-ordered segments
 		// (gs/gs_renderer.cpp:3190-3266).  The instance of each primitive is
 		// read from the host copy of the records.
-		const pgs_primitive_attribute *hp = reinterpret_cast<const pgs_primitive_attribute *>(h_arena + p.prim_off);
+		const pgs_primitive_attribute *hp =
+		    p.host_prims ? p.host_prims : reinterpret_cast<const pgs_primitive_attribute *>(h_arena + p.prim_off);
 		uint8_t hazard[8] = {};
 		bool any = instance_hazards(p, hazard);
 		if (any)
@@ -854,6 +911,62 @@ struct CudaBackend
 		if (!recording)
 			arena_used = 0;
 		return PGS_OK;
+	}
+
+	int read_vram_async(uint64_t off, uint64_t size, void *dst, uint64_t &ticket)
+	{
+		if (off + size > VRAM_SIZE)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		// Oldest slot when all are busy: finish it first.
+		Readback *slot = nullptr;
+		for (auto &rb : readbacks)
+			if (rb.ticket == 0) { slot = &rb; break; }
+		if (!slot)
+		{
+			slot = &readbacks[0];
+			for (auto &rb : readbacks)
+				if (rb.ticket < slot->ticket) slot = &rb;
+			int r = wait_ticket(slot->ticket);
+			if (r)
+				return r;
+		}
+		cudaPointerAttributes attr = {};
+		bool pinned = cudaPointerGetAttributes(&attr, dst) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+		cudaGetLastError();
+		void *target = dst;
+		if (!pinned)
+		{
+			if (!slot->staging)
+				CUDA_TRY(cudaMallocHost(&slot->staging, VRAM_SIZE));
+			target = slot->staging;
+		}
+		CUDA_TRY(cudaMemcpyAsync(target, d_vram + off, size, cudaMemcpyDeviceToHost, stream));
+		CUDA_TRY(cudaEventRecord(slot->done, stream));
+		slot->ticket = next_ticket++;
+		slot->dst = pinned ? nullptr : dst;
+		slot->size = size;
+		d2h_bytes += size;
+		total_launches += launch_counter;
+		launch_counter = 0;
+		ticket = slot->ticket;
+		return PGS_OK;
+	}
+
+	int wait_ticket(uint64_t ticket)
+	{
+		for (auto &rb : readbacks)
+		{
+			if (rb.ticket != ticket)
+				continue;
+			CUDA_TRY(cudaEventSynchronize(rb.done));
+			if (rb.dst)
+				memcpy(rb.dst, rb.staging, rb.size);
+			rb.ticket = 0;
+			rb.dst = nullptr;
+			return PGS_OK;
+		}
+		// Unknown or already waited for.
+		return ticket && ticket < next_ticket ? PGS_OK : PGS_ERROR_INVALID_ARGUMENT;
 	}
 
 	int write_vram(uint64_t off, uint64_t size, const void *src)
@@ -1000,9 +1113,15 @@ int c_write(void *self, uint64_t off, uint64_t size, const void *src)
 	return src ? B(self)->write_vram(off, size, src) : PGS_ERROR_INVALID_ARGUMENT;
 }
 int c_error(void *self, uint32_t *flags) { return B(self)->get_error(flags); }
+int c_read_async(void *self, uint64_t off, uint64_t size, void *dst, uint64_t *ticket)
+{
+	return dst && ticket ? B(self)->read_vram_async(off, size, dst, *ticket) : PGS_ERROR_INVALID_ARGUMENT;
+}
+int c_wait(void *self, uint64_t ticket) { return B(self)->wait_ticket(ticket); }
 
 const pgs_backend_ops CUDA_OPS = {
 	PGS_ABI_VERSION, c_destroy, c_reserve, c_flush_rendering, c_copy, c_palette, c_set_ss, c_submit, c_read, c_write, c_error,
+	c_read_async, c_wait,
 };
 
 // ---------------------------------------------------------------------------

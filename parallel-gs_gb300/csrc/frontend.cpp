@@ -166,32 +166,100 @@ static PageSpan page_span(uint32_t base_block, uint32_t x, uint32_t y, uint32_t 
 	return s;
 }
 
+// One bit per page and access kind.  A span covers, per row, the pages
+// base + y * stride + [0, width) modulo the page count.
 struct PageTracker
 {
 	enum : uint8_t { FB_WRITE = 1, FB_READ = 2, TEX_READ = 4 };
-	uint8_t state[NUM_PAGES] = {};
+	static constexpr uint32_t WORDS = NUM_PAGES / 64;
+	uint64_t bits[3][WORDS] = {};
+	// Bumped when a page gains a kind it did not have / when the tracker is cleared.
+	uint64_t gen[3] = {};
+	uint64_t gen_at_clear[3] = {};
+	uint64_t clears = 0;
 
-	template <typename F>
-	void for_each(const PageSpan &s, F &&f)
+	static bool range_any(const uint64_t *b, uint32_t start, uint32_t len)
 	{
+		while (len)
+		{
+			uint32_t o = start & 63, n = std::min<uint32_t>(len, 64 - o);
+			uint64_t m = (n == 64 ? ~0ull : ((1ull << n) - 1)) << o;
+			if (b[start >> 6] & m)
+				return true;
+			len -= n;
+			start = (start + n) % NUM_PAGES;
+		}
+		return false;
+	}
+
+	static bool range_set(uint64_t *b, uint32_t start, uint32_t len)
+	{
+		bool fresh = false;
+		while (len)
+		{
+			uint32_t o = start & 63, n = std::min<uint32_t>(len, 64 - o);
+			uint64_t m = (n == 64 ? ~0ull : ((1ull << n) - 1)) << o;
+			fresh |= (b[start >> 6] & m) != m;
+			b[start >> 6] |= m;
+			len -= n;
+			start = (start + n) % NUM_PAGES;
+		}
+		return fresh;
+	}
+
+	bool any_kind(const PageSpan &s, uint32_t k) const
+	{
+		if (gen[k] == gen_at_clear[k])
+			return false;
 		for (uint32_t y = 0; y < s.height; y++)
-			for (uint32_t x = 0; x < s.width; x++)
-				f((s.base_page + y * s.stride + x) % NUM_PAGES);
+			if (range_any(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width))
+				return true;
+		return false;
+	}
+
+	void mark_kind(const PageSpan &s, uint32_t k)
+	{
+		bool fresh = false;
+		for (uint32_t y = 0; y < s.height; y++)
+			fresh |= range_set(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width);
+		if (fresh)
+			gen[k]++;
 	}
 
 	bool any(const PageSpan &s, uint8_t mask)
 	{
-		bool hit = false;
-		for_each(s, [&](uint32_t p) { hit |= (state[p] & mask) != 0; });
-		return hit;
+		for (uint32_t k = 0; k < 3; k++)
+		{
+			if (!(mask & (1u << k)))
+				continue;
+			for (uint32_t y = 0; y < s.height; y++)
+				if (range_any(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width))
+					return true;
+		}
+		return false;
 	}
 
 	void mark(const PageSpan &s, uint8_t flags)
 	{
-		for_each(s, [&](uint32_t p) { state[p] |= flags; });
+		for (uint32_t k = 0; k < 3; k++)
+		{
+			if (!(flags & (1u << k)))
+				continue;
+			bool fresh = false;
+			for (uint32_t y = 0; y < s.height; y++)
+				fresh |= range_set(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width);
+			if (fresh)
+				gen[k]++;
+		}
 	}
 
-	void clear() { memset(state, 0, sizeof(state)); }
+	void clear()
+	{
+		memset(bits, 0, sizeof(bits));
+		clears++;
+		for (uint32_t k = 0; k < 3; k++)
+			gen_at_clear[k] = gen[k];
+	}
 };
 
 struct Instance
@@ -266,6 +334,64 @@ struct pgs_gs
 	PageSpan tpl_tex_span = {};
 	bool tpl_has_tex_span = false;
 
+	// Caches of values derived from the register file.  reg_serial changes
+	// whenever a register other than vertex data (RGBAQ, ST, UV, FOG, XYZ*) is
+	// written or the sampling rate changes; fb_epoch whenever the render pass
+	// is flushed.
+	uint64_t reg_serial = 1, fb_epoch = 1, tpl_serial = 1;
+	uint64_t degenerate_serial = 0;
+	bool degenerate_cached = false;
+	uint64_t fb_state_serial = 0, fb_state_epoch = 0;
+	uint64_t tex_check_key[3] = {}, tex_mark_key[2] = {};
+	struct DrawConsts
+	{
+		uint64_t serial = 0;
+		int32_t snap = 0;
+		int32_t sci_lo[2] = {}, sci_hi[2] = {};
+		int32_t sci_hi_x_fb = 0;
+		bool can_wrap = false, line_aa1 = false, tme = false, z_sens = false;
+		FrameReg frame{ 0 };
+		ZbufReg zb{ 0 };
+		uint32_t alpha_word = 0, fogcol = 0;
+		// Page geometry of the colour and depth buffers (page_span).
+		uint32_t fb_pw = 0, fb_ph = 0, fb_stride = 0, z_pw = 0, z_ph = 0, z_stride = 0;
+	} dc;
+
+	const DrawConsts &draw_consts()
+	{
+		if (dc.serial == reg_serial)
+			return dc;
+		PrimReg prim(regs[R_PRIM]);
+		dc.snap = (1 << int(SUBPIXEL_BITS - sampling_rate_y_log2)) - 1;
+		uint64_t sc = ctx_reg(R_SCISSOR_1);
+		dc.frame = FrameReg(ctx_reg(R_FRAME_1));
+		dc.zb = ZbufReg(ctx_reg(R_ZBUF_1));
+		dc.sci_lo[0] = int32_t(field(sc, 0, 11));
+		dc.sci_lo[1] = int32_t(field(sc, 32, 11));
+		dc.sci_hi[0] = int32_t(field(sc, 16, 11));
+		dc.sci_hi[1] = int32_t(field(sc, 48, 11));
+		int32_t fb_width = int32_t(std::max<uint32_t>(1, dc.frame.fbw) * BUFFER_WIDTH_SCALE);
+		dc.sci_hi_x_fb = std::min(dc.sci_hi[0], fb_width - 1);
+		dc.can_wrap = dc.frame.fbw != 0 && dc.sci_hi_x_fb < dc.sci_hi[0];
+		dc.line_aa1 = prim.enables_aa1();
+		dc.tme = prim.tme != 0;
+		dc.z_sens = state_is_z_sensitive();
+		AlphaReg alpha(ctx_reg(R_ALPHA_1));
+		TestReg test(ctx_reg(R_TEST_1));
+		dc.alpha_word = (alpha.fix << ALPHA_AFIX_OFFSET) | (test.aref << ALPHA_AREF_OFFSET);
+		dc.fogcol = uint32_t(regs[R_FOGCOL]);
+		uint32_t row = dc.frame.fbw ? dc.frame.fbw : 1;
+		Layout FL = psm_layout(dc.frame.psm), ZL = psm_layout(dc.zb.psm | 0x30);
+		dc.fb_pw = FL.pw;
+		dc.fb_ph = FL.ph;
+		dc.fb_stride = (dc.frame.psm == PSMT4 || dc.frame.psm == PSMT8) ? row >> 1 : row;
+		dc.z_pw = ZL.pw;
+		dc.z_ph = ZL.ph;
+		dc.z_stride = row;
+		dc.serial = reg_serial;
+		return dc;
+	}
+
 	PageTracker tracker;
 
 	struct
@@ -312,6 +438,7 @@ struct pgs_gs
 			break;
 		default: sampling_rate_x_log2 = 0; sampling_rate_y_log2 = 0; break;
 		}
+		reg_serial++;
 		int r = ops->set_super_sampling(be, sampling_rate_x_log2, sampling_rate_y_log2);
 		if (r != 0)
 			sticky_error = r;
@@ -321,6 +448,7 @@ struct pgs_gs
 	// Render pass flush (gs/gs_interface.cpp:133-351).
 	void flush_render_pass(uint32_t reason)
 	{
+		fb_epoch++;
 		if (primitive_count)
 		{
 			pgs_render_pass rp = {};
@@ -693,6 +821,17 @@ struct pgs_gs
 		addr &= 0x7f;
 		switch (addr)
 		{
+		case R_RGBAQ: case R_RGBAQ_UNDOC: case R_ST: case R_UV: case R_FOG:
+		case R_XYZF2: case R_XYZ2: case R_XYZF3: case R_XYZ3:
+		case R_BITBLTBUF: case R_TRXPOS: case R_TRXREG: case R_TRXDIR: case R_HWREG:
+		case R_SIGNAL: case R_FINISH: case R_LABEL:
+			break;
+		default:
+			reg_serial++;
+			break;
+		}
+		switch (addr)
+		{
 		case R_PRIM:
 		{
 			bool ctxt_change = field(regs[R_PRIM], 9, 1) != field(v, 9, 1);
@@ -835,6 +974,15 @@ struct pgs_gs
 	// draw_is_degenerate (gs/gs_interface.cpp:2036-2115).
 	bool draw_is_degenerate()
 	{
+		if (degenerate_serial == reg_serial)
+			return degenerate_cached;
+		degenerate_serial = reg_serial;
+		degenerate_cached = compute_draw_is_degenerate();
+		return degenerate_cached;
+	}
+
+	bool compute_draw_is_degenerate()
+	{
 		PrimReg prim(regs[R_PRIM]);
 		uint64_t sc = ctx_reg(R_SCISSOR_1);
 		if (field(sc, 0, 11) > field(sc, 16, 11) || field(sc, 32, 11) > field(sc, 48, 11))
@@ -885,6 +1033,10 @@ struct pgs_gs
 	// check_frame_buffer_state (gs/gs_interface.cpp:935-1023).
 	void check_frame_buffer_state()
 	{
+		// With no register written and no flush since the last call the
+		// instance already matches FRAME / ZBUF.
+		if (fb_state_serial == reg_serial && fb_state_epoch == fb_epoch)
+			return;
 		uint64_t frame = ctx_reg(R_FRAME_1), zbuf = ctx_reg(R_ZBUF_1);
 		Instance *inst = &instances[current_instance];
 		bool fb_delta = !frame_compat(inst->frame, frame);
@@ -921,6 +1073,8 @@ struct pgs_gs
 		}
 		inst->frame = frame;
 		inst->zbuf = zbuf;
+		fb_state_serial = reg_serial;
+		fb_state_epoch = fb_epoch;
 	}
 
 	uint32_t find_state_vector(const pgs_state_vector &s)
@@ -1050,6 +1204,7 @@ struct pgs_gs
 	// drawing_kick_update_state (gs/gs_interface.cpp:1804-1968).
 	void update_template()
 	{
+		tpl_serial++;
 		PrimReg prim(regs[R_PRIM]);
 		TestReg test(ctx_reg(R_TEST_1));
 		AlphaReg alpha(ctx_reg(R_ALPHA_1));
@@ -1200,7 +1355,7 @@ struct pgs_gs
 
 	void append(uint32_t nv, bool quad)
 	{
-		PrimReg prim(regs[R_PRIM]);
+		const DrawConsts &D = draw_consts();
 		pgs_vertex_position pos[3] = {};
 		pgs_vertex_attribute attr[3] = {};
 
@@ -1243,34 +1398,28 @@ struct pgs_gs
 		}
 		hi[0] -= 1;
 		hi[1] -= 1;
-		int32_t snap = (1 << int(SUBPIXEL_BITS - sampling_rate_y_log2)) - 1;
-		lo[0] += snap;
-		lo[1] += snap;
+		lo[0] += D.snap;
+		lo[1] += D.snap;
 		lo[0] >>= SUBPIXEL_BITS;
 		lo[1] >>= SUBPIXEL_BITS;
 		hi[0] >>= SUBPIXEL_BITS;
 		hi[1] >>= SUBPIXEL_BITS;
-		if (is_line || prim.enables_aa1())
+		if (is_line || D.line_aa1)
 		{
 			lo[0] -= 1; lo[1] -= 1;
 			hi[0] += 1; hi[1] += 1;
 		}
 
-		uint64_t sc = ctx_reg(R_SCISSOR_1);
-		FrameReg frame(ctx_reg(R_FRAME_1));
-		int32_t sci_lo[2] = { int32_t(field(sc, 0, 11)), int32_t(field(sc, 32, 11)) };
-		int32_t sci_hi[2] = { int32_t(field(sc, 16, 11)), int32_t(field(sc, 48, 11)) };
-		int32_t fb_width = int32_t(std::max<uint32_t>(1, frame.fbw) * BUFFER_WIDTH_SCALE);
-		int32_t sci_hi_x_fb = std::min(sci_hi[0], fb_width - 1);
-		bool can_wrap = frame.fbw != 0 && sci_hi_x_fb < sci_hi[0];
-
-		int32_t bb[4] = { std::max(lo[0], sci_lo[0]), std::max(lo[1], sci_lo[1]),
-		                  std::min(hi[0], sci_hi[0]), std::min(hi[1], sci_hi[1]) };
+		const FrameReg &frame = D.frame;
+		const int32_t sci_hi_x_fb = D.sci_hi_x_fb;
+		const bool can_wrap = D.can_wrap;
+		int32_t bb[4] = { std::max(lo[0], D.sci_lo[0]), std::max(lo[1], D.sci_lo[1]),
+		                  std::min(hi[0], D.sci_hi[0]), std::min(hi[1], D.sci_hi[1]) };
 		if (bb[2] < bb[0] || bb[3] < bb[1])
 			return;
 
 		// Flush a pending partial upload before reading textures.
-		if (prim.tme && xfer.active && xfer.payload.size() > xfer.flushed_qwords)
+		if (D.tme && xfer.active && xfer.payload.size() > xfer.flushed_qwords)
 			flush_pending_transfer(true);
 
 		check_frame_buffer_state();
@@ -1282,13 +1431,24 @@ struct pgs_gs
 		}
 
 		// Texture read after framebuffer write in the same pass: end the pass
-		// (mark_texture_read, gs/page_tracker.cpp:327-345).
-		if (tpl_has_tex_span && tracker.any(tpl_tex_span, PageTracker::FB_WRITE))
+		// (mark_texture_read, gs/page_tracker.cpp:327-345).  The answer only
+		// changes with the texture's pages or new framebuffer-written pages.
+		if (tpl_has_tex_span)
 		{
-			flush_render_pass(FLUSH_TEXTURE_HAZARD);
-			check_frame_buffer_state();
-			update_template();
-			template_dirty = false;
+			uint64_t key[3] = { tpl_serial, tracker.gen[0], tracker.clears };
+			if (memcmp(key, tex_check_key, sizeof(key)) != 0)
+			{
+				if (tracker.any(tpl_tex_span, PageTracker::FB_WRITE))
+				{
+					flush_render_pass(FLUSH_TEXTURE_HAZARD);
+					check_frame_buffer_state();
+					update_template();
+					template_dirty = false;
+				}
+				tex_check_key[0] = tpl_serial;
+				tex_check_key[1] = tracker.gen[0];
+				tex_check_key[2] = tracker.clears;
+			}
 		}
 
 		if (can_wrap && bb[0] > sci_hi_x_fb)
@@ -1319,18 +1479,22 @@ struct pgs_gs
 		// Framebuffer pages this primitive may write.  If an earlier primitive of
 		// this pass samples them, end the pass first.
 		{
-			ZbufReg zb(ctx_reg(R_ZBUF_1));
-			Layout FL = psm_layout(frame.psm);
-			(void)FL;
-			PageSpan fb_span = page_span(frame.fbp * BLOCKS_PER_PAGE, uint32_t(bb[0]), uint32_t(bb[1]),
-			                             uint32_t(bb[2] - bb[0] + 1), uint32_t(bb[3] - bb[1] + 1),
-			                             frame.fbw ? frame.fbw : 1, frame.psm);
-			bool z_sens = state_is_z_sensitive();
-			PageSpan z_span = page_span(zb.zbp * BLOCKS_PER_PAGE, uint32_t(bb[0]), uint32_t(bb[1]),
-			                            uint32_t(bb[2] - bb[0] + 1), uint32_t(bb[3] - bb[1] + 1),
-			                            frame.fbw ? frame.fbw : 1, zb.psm | 0x30);
-			bool hazard = tracker.any(fb_span, PageTracker::TEX_READ) ||
-			              (z_sens && tracker.any(z_span, PageTracker::TEX_READ));
+			const ZbufReg &zb = D.zb;
+			// page_span of the primitive's rectangle; FBP and ZBP are page aligned.
+			auto rect_span = [&](uint32_t base_page, uint32_t pw, uint32_t ph, uint32_t stride) {
+				uint32_t px0 = uint32_t(bb[0]) >> pw, px1 = uint32_t(bb[2]) >> pw;
+				uint32_t py0 = uint32_t(bb[1]) >> ph, py1 = uint32_t(bb[3]) >> ph;
+				PageSpan s;
+				s.base_page = base_page + py0 * stride + px0;
+				s.width = std::min<uint32_t>(px1 - px0 + 1, NUM_PAGES);
+				s.height = std::min<uint32_t>(py1 - py0 + 1, NUM_PAGES);
+				s.stride = stride;
+				return s;
+			};
+			PageSpan fb_span = rect_span(frame.fbp, D.fb_pw, D.fb_ph, D.fb_stride);
+			const bool z_sens = D.z_sens;
+			PageSpan z_span = rect_span(zb.zbp, D.z_pw, D.z_ph, D.z_stride);
+			bool hazard = tracker.any_kind(fb_span, 2) || (z_sens && tracker.any_kind(z_span, 2));
 			if (hazard && primitive_count)
 			{
 				flush_render_pass(FLUSH_TEXTURE_HAZARD);
@@ -1338,11 +1502,15 @@ struct pgs_gs
 				update_template();
 				template_dirty = false;
 			}
-			if (tpl_has_tex_span)
+			if (tpl_has_tex_span && (tex_mark_key[0] != tpl_serial || tex_mark_key[1] != tracker.clears))
+			{
 				tracker.mark(tpl_tex_span, PageTracker::TEX_READ);
-			tracker.mark(fb_span, PageTracker::FB_WRITE);
+				tex_mark_key[0] = tpl_serial;
+				tex_mark_key[1] = tracker.clears;
+			}
+			tracker.mark_kind(fb_span, 0);
 			if (z_sens)
-				tracker.mark(z_span, zb.zmsk ? PageTracker::FB_READ : PageTracker::FB_WRITE);
+				tracker.mark_kind(z_span, zb.zmsk ? 1 : 0);
 		}
 
 		auto &inst = instances[current_instance];
@@ -1351,10 +1519,8 @@ struct pgs_gs
 		pa.tex2 = tpl_tex2;
 		pa.state = tpl_state;
 		pa.fbmsk = frame.fbmsk;
-		pa.fogcol = uint32_t(regs[R_FOGCOL]);
-		AlphaReg alpha(ctx_reg(R_ALPHA_1));
-		TestReg test(ctx_reg(R_TEST_1));
-		pa.alpha = (alpha.fix << ALPHA_AFIX_OFFSET) | (test.aref << ALPHA_AREF_OFFSET);
+		pa.fogcol = D.fogcol;
+		pa.alpha = D.alpha_word;
 
 		if (quad)
 		{
@@ -1372,10 +1538,10 @@ struct pgs_gs
 			pa.state |= (1u << STATE_BIT_FIX) | (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
 		pa.state |= current_instance << STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET;
 
-		bool z_sens = state_is_z_sensitive();
+		const bool z_sens = D.z_sens;
 		if (!inst.z_sensitive && z_sens)
 			inst.z_sensitive = true;
-		if (z_sens && ZbufReg(ctx_reg(R_ZBUF_1)).zmsk == 0 && !inst.z_write)
+		if (z_sens && D.zb.zmsk == 0 && !inst.z_write)
 			inst.z_write = true;
 		inst.color_write_mask |= ~frame.fbmsk;
 		inst.bb[0] = std::min(inst.bb[0], bb[0]);
@@ -1551,7 +1717,7 @@ pgs_gs *pgs_gs_create(const pgs_backend_ops *ops, void *backend, const pgs_gs_op
 	int dummy;
 	if (!status)
 		status = &dummy;
-	if (!ops || !backend || ops->abi_version != PGS_ABI_VERSION)
+	if (!ops || !backend || ops->abi_version < 1 || ops->abi_version > PGS_ABI_VERSION)
 	{
 		*status = PGS_ERROR_INVALID_ARGUMENT;
 		return nullptr;
@@ -1623,6 +1789,30 @@ int pgs_gs_read_vram(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst)
 	if (gs->sticky_error)
 		return gs->sticky_error;
 	return gs->ops->read_vram(gs->be, 0, offset, size, dst);
+}
+
+int pgs_gs_read_vram_async(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst, uint64_t *ticket)
+{
+	if (!gs || !dst || !ticket || offset + size > PGS_VRAM_SIZE)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->flush();
+	if (gs->sticky_error)
+		return gs->sticky_error;
+	if (gs->ops->abi_version >= 2 && gs->ops->read_vram_async && gs->ops->wait_ticket)
+		return gs->ops->read_vram_async(gs->be, offset, size, dst, ticket);
+	*ticket = 0;
+	return gs->ops->read_vram(gs->be, 0, offset, size, dst);
+}
+
+int pgs_gs_wait(pgs_gs *gs, uint64_t ticket)
+{
+	if (!gs)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if (ticket == 0)
+		return PGS_OK;
+	if (gs->ops->abi_version < 2 || !gs->ops->wait_ticket)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	return gs->ops->wait_ticket(gs->be, ticket);
 }
 
 int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *src)

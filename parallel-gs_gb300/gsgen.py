@@ -520,4 +520,4 @@ def frame_c4(seed: int = 4, super_sampling: int = 8, num_triangles: int = 100000
                 q[:, 1] = q_xyz2(x.reshape(nv), y.reshape(nv), z.reshape(nv))
                 s.packed(prim_reg(PRIM_TRI, iip=1), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
     return Frame("c4", s.tobytes(), super_sampling, super_sampling != 8, num_triangles,
-                 {"width": width, "height": height, "fbp": fb_a, "fb_b": fb_b, "zbp": zbp})
+                 {"width": width, "height": height, "fbp": fb_a, "fb_b": fb_b, "zbp": zbp, "passes": passes})

@@ -71,7 +71,7 @@ EXPORTED_SYMBOLS = [
     "pgs_cuda_backend_last_shade_ms", "pgs_cuda_backend_fragment_count", "pgs_cuda_backend_get_stats",
     "pgs_cuda_backend_set_shade_timing",
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
-    "pgs_gs_read_vram", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
+    "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
     "pgs_gs_set_super_sampling_rate",
 ]
 
@@ -109,6 +109,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.pgs_gs_write_register.argtypes = [vp, u32, u64]
     lib.pgs_gs_flush.argtypes = [vp]
     lib.pgs_gs_read_vram.argtypes = [vp, u64, u64, vp]
+    lib.pgs_gs_read_vram_async.argtypes = [vp, u64, u64, vp, C.POINTER(u64)]
+    lib.pgs_gs_wait.argtypes = [vp, u64]
     lib.pgs_gs_write_vram.argtypes = [vp, u64, u64, vp]
     lib.pgs_gs_read_transfer_fifo.argtypes = [vp, vp, u32]
     lib.pgs_gs_consume_flush_stats.argtypes = [vp, C.POINTER(FlushStats)]
@@ -236,6 +238,19 @@ class GSInterface:
             out = np.empty(size, dtype=np.uint8)
         check(self.lib.pgs_gs_read_vram(self.handle, offset, size, out.ctypes.data), "read_vram")
         return out
+
+    def read_vram_async(self, out: np.ndarray, offset: int = 0, size: int | None = None) -> int:
+        """Queues a read of plane 0 into `out` behind everything submitted so far;
+        `out` is valid once wait(ticket) returns.  Pinned `out` is written by DMA
+        directly, other memory through a pinned staging copy."""
+        size = out.nbytes if size is None else size
+        ticket = C.c_uint64()
+        check(self.lib.pgs_gs_read_vram_async(self.handle, offset, size, out.ctypes.data, C.byref(ticket)),
+              "read_vram_async")
+        return int(ticket.value)
+
+    def wait(self, ticket: int) -> None:
+        check(self.lib.pgs_gs_wait(self.handle, ticket), "wait")
 
     def write_vram(self, data, offset: int = 0) -> None:
         buf = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, bytes) else data)

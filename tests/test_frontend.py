@@ -246,3 +246,21 @@ def test_super_sampling_rate_sent_to_backend():
     gs.set_super_sampling_rate(8)
     gs.close()
     assert be.ss == [(1, 1), (2, 2), (1, 2)]
+
+
+def test_read_vram_async_falls_back_to_synchronous_copy():
+    """Backends without an asynchronous read (ABI 1 tables, the oracle) copy
+    before pgs_gs_read_vram_async returns and hand out ticket 0."""
+    import gsgen
+    import pgs_oracle
+    f = gsgen.frame_c1(seed=21, num_triangles=200)
+    for be in (pgs_oracle.OracleBackend(), RecordingBackend()):
+        gs = pgs.GSInterface(be)
+        gs.gif_transfer(0, f.data)
+        out = np.zeros(pgs.VRAM_SIZE, dtype=np.uint8)
+        ticket = gs.read_vram_async(out)
+        assert ticket == 0
+        gs.wait(ticket)
+        assert np.array_equal(out, gs.read_vram())
+        gs.close()
+        be.close()

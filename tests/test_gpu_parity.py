@@ -122,3 +122,36 @@ def test_c4_full_size(ss):
     """8x / 16x at its benchmark size: 100k triangles over 10 feedback passes."""
     ref, out = run_both(gsgen.frame_c4(seed=4, super_sampling=ss))
     assert_same(ref, out)
+
+
+def test_pipelined_async_readback():
+    """Frames decoded back to back with asynchronous readbacks in flight: each
+    ticket's buffer holds the VRAM as of its own frame (pinned and pageable
+    destinations)."""
+    import torch
+    frames = [gsgen.frame_c1(seed=30 + k, num_triangles=1500) for k in range(4)]
+    obe = pgs_oracle.OracleBackend()
+    ogs = pgs.GSInterface(obe)
+    expect = []
+    for f in frames:
+        ogs.gif_transfer(0, f.data)
+        expect.append(ogs.read_vram())
+    ogs.close()
+    obe.close()
+    be = pgs.CudaBackend(0, max_samples_log2=4)
+    try:
+        gs = pgs.GSInterface(be)
+        pinned = [torch.empty(pgs.VRAM_SIZE, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(2)]
+        pageable = [np.empty(pgs.VRAM_SIZE, dtype=np.uint8) for _ in range(2)]
+        outs, tickets = [], []
+        for k, f in enumerate(frames):
+            gs.gif_transfer(0, f.data)
+            buf = pinned[k % 2] if k < 2 else pageable[k % 2]
+            tickets.append(gs.read_vram_async(buf))
+            outs.append(buf)
+        for k in range(len(frames)):
+            gs.wait(tickets[k])
+            assert np.array_equal(outs[k], expect[k]), "frame %d" % k
+        gs.close()
+    finally:
+        be.close()
