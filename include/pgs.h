@@ -242,6 +242,7 @@ typedef struct pgs_cuda_backend_options
 	int device;                  /* CUDA ordinal */
 	uint32_t max_samples_log2;   /* 0..4: VRAM holds 2 + 2^max planes */
 	uint32_t flags;
+	uint32_t arena_mib;          /* initial record arena (MiB); 0 = 256.  It grows on demand. */
 } pgs_cuda_backend_options;
 
 /* Creates a backend on `device`; returns NULL and sets *status on failure
@@ -284,6 +285,46 @@ int pgs_cuda_backend_get_stats(void *backend, pgs_backend_stats *stats);
  * between them is returned by pgs_cuda_backend_last_shade_ms once the replay
  * has completed. */
 int pgs_cuda_backend_set_shade_timing(void *backend, int enable);
+
+/* ------------------------------------------------------------------ */
+/* Batched replay of many command streams                               */
+/* ------------------------------------------------------------------ */
+/* Many independent GS command streams, each recorded into its own CUDA
+ * backend (pgs_cuda_backend_begin_record / end_record), replayed together:
+ * every round takes each stream one render pass further, and one persistent
+ * kernel launch shades the current pass of all streams; the schedule is a
+ * single CUDA graph.  No counterpart in the reference, which renders one
+ * stream per GSInterface. */
+typedef struct pgs_batch pgs_batch;
+
+typedef struct pgs_batch_tuning
+{
+	uint32_t cta_threads;    /* 128, 256 or 512 */
+	uint32_t ctas_per_sm;    /* persistent CTAs per SM (1 .. 1024 / cta_threads) */
+	uint32_t largest_first;  /* order work items by size within a round */
+} pgs_batch_tuning;
+
+pgs_batch *pgs_batch_create(int device, int *status);
+void pgs_batch_destroy(pgs_batch *batch);
+/* Adds a CUDA backend that holds a recorded frame; the backend must outlive
+ * the batch and not be replayed on its own while the batch is in use. */
+int pgs_batch_add(pgs_batch *batch, void *cuda_backend);
+/* Replays every stream `count` times (from its begin_record VRAM when
+ * reset_vram is set), as a CUDA graph when use_graph is set. */
+int pgs_batch_replay(pgs_batch *batch, uint32_t count, int reset_vram, int use_graph);
+int pgs_batch_set_tuning(pgs_batch *batch, const pgs_batch_tuning *tuning);
+int pgs_batch_get_tuning(pgs_batch *batch, pgs_batch_tuning *tuning);
+/* Times `trials` graph replays of each candidate tuning (CTA size x CTAs per
+ * SM x item order) and keeps the fastest; *best receives it, *best_ms its
+ * mean time per replay. */
+int pgs_batch_autotune(pgs_batch *batch, uint32_t trials, int reset_vram, pgs_batch_tuning *best, float *best_ms);
+/* The batch's cudaStream_t (graph launches go there), as an opaque pointer. */
+void *pgs_batch_stream(pgs_batch *batch);
+/* Kernel launches of one batched replay. */
+uint32_t pgs_batch_launches_per_replay(pgs_batch *batch);
+/* Waits for every replay issued so far; afterwards each stream's VRAM can be
+ * read through its backend. */
+int pgs_batch_synchronize(pgs_batch *batch);
 
 /* ------------------------------------------------------------------ */
 /* Allocation-free local->local VRAM copy                               */

@@ -210,7 +210,7 @@ struct CudaBackend
 		}
 		for (auto &rb : readbacks)
 			CUDA_TRY(cudaEventCreateWithFlags(&rb.done, cudaEventDisableTiming));
-		return grow_arena(256u << 20);
+		return grow_arena(size_t(opt && opt->arena_mib ? opt->arena_mib : 256u) << 20);
 	}
 
 	static size_t stage_bytes()
@@ -592,8 +592,13 @@ struct CudaBackend
 		launch_counter++;
 	}
 
-	int run_instance(const PassParams &P, const PassOp &p, uint32_t inst_index, uint32_t lo, uint32_t count)
+	// Bins and shades one instance segment.  With `collect` set, a segment the
+	// batched kernel can shade is only binned and returned as a work item.
+	int run_instance(const PassParams &P, const PassOp &p, uint32_t inst_index, uint32_t lo, uint32_t count,
+	                 ShadeItem *collect = nullptr, bool *collected = nullptr)
 	{
+		if (collected)
+			*collected = false;
 		const pgs_rp_instance &in = p.instances[inst_index];
 		DevInstance I = {};
 		uint32_t frame_lo = uint32_t(in.frame), zbuf_lo = uint32_t(in.zbuf);
@@ -636,6 +641,20 @@ struct CudaBackend
 		bin_kernel<<<(count + 127) / 128, 128, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags);
 		launch_counter++;
 		uint32_t grid = uint32_t(subs);
+		if (collect && ns_log2 <= BATCH_MAX_NS_LOG2 && (I.rate_y_log2 != 0 || ns_log2 == 0))
+		{
+			collect->P = P;
+			collect->I = I;
+			collect->masks = d_sub_masks;
+			collect->summary = d_sub_summary;
+			collect->flags = d_flags;
+			collect->ns_log2 = I.rate_y_log2 != 0 ? ns_log2 : 0u;
+			collect->aa = p.has_aa1;
+			collect->units = uint32_t(subs) * (2u << collect->ns_log2);
+			*collected = true;
+			CUDA_TRY(cudaGetLastError());
+			return PGS_OK;
+		}
 		if (shade_timing && !shade_started)
 		{
 			int r = record_timing_event(shade_ev[0]);
@@ -697,10 +716,34 @@ struct CudaBackend
 		return PGS_ERROR_INVALID_ARGUMENT;
 	}
 
+	struct Segment
+	{
+		uint32_t inst, lo, count;
+	};
+
 	int execute_pass(const PassOp &p)
 	{
+		PassParams P;
+		std::vector<Segment> segs;
+		int r = begin_pass(p, P, segs);
+		if (r)
+			return r;
+		for (const Segment &s : segs)
+		{
+			r = run_instance(P, p, s.inst, s.lo, s.count);
+			if (r)
+				return r;
+		}
+		return PGS_OK;
+	}
+
+	// Setup, single-sample heuristic and texture decode of a pass; `segs`
+	// receives the instance segments to bin and shade in order.
+	int begin_pass(const PassOp &p, PassParams &P, std::vector<Segment> &segs)
+	{
 		render_passes++;
-		PassParams P = {};
+		segs.clear();
+		P = {};
 		P.pos = reinterpret_cast<const pgs_vertex_position *>(d_arena + p.pos_off);
 		P.attr = reinterpret_cast<const pgs_vertex_attribute *>(d_arena + p.attr_off);
 		P.states = reinterpret_cast<const pgs_state_vector *>(d_arena + p.states_off);
@@ -763,8 +806,19 @@ struct CudaBackend
 		}
 		CUDA_TRY(cudaGetLastError());
 
+		pass_segments(p, segs);
+		return PGS_OK;
+	}
+
+	// Instance segments of a pass in execution order.
+	void pass_segments(const PassOp &p, std::vector<Segment> &segs) const
+	{
+		segs.clear();
 		if (p.num_instances == 1)
-			return run_instance(P, p, 0, 0, p.num_prims);
+		{
+			segs.push_back({ 0, 0, p.num_prims });
+			return;
+		}
 
 		// Per-instance primitive ranges and hazard-ordered segments
 		// (gs/gs_renderer.cpp:3190-3266).  The instance of each primitive is
@@ -783,10 +837,7 @@ struct CudaBackend
 				{
 					for (uint32_t b = 0; b < 8; b++)
 						if (active & (1u << b))
-						{
-							int r = run_instance(P, p, b, base, i - base);
-							if (r) return r;
-						}
+							segs.push_back({ b, base, i - base });
 					base = i;
 					active = 0;
 					active_h = 0;
@@ -796,11 +847,8 @@ struct CudaBackend
 			}
 			for (uint32_t b = 0; b < 8; b++)
 				if (active & (1u << b))
-				{
-					int r = run_instance(P, p, b, base, p.num_prims - base);
-					if (r) return r;
-				}
-			return PGS_OK;
+					segs.push_back({ b, base, p.num_prims - base });
+			return;
 		}
 		uint32_t lo[8], hi[8];
 		for (int i = 0; i < 8; i++) { lo[i] = 0xffffffffu; hi[i] = 0; }
@@ -812,11 +860,7 @@ struct CudaBackend
 		}
 		for (uint32_t i = 0; i < p.num_instances; i++)
 			if (lo[i] != 0xffffffffu)
-			{
-				int r = run_instance(P, p, i, lo[i], hi[i] - lo[i] + 1);
-				if (r) return r;
-			}
-		return PGS_OK;
+				segs.push_back({ i, lo[i], hi[i] - lo[i] + 1 });
 	}
 
 	// Depth quantisation of the flat-primitive buckets per instance.  Triangle
@@ -1086,6 +1130,367 @@ struct CudaBackend
 };
 
 // ---------------------------------------------------------------------------
+// Batched replay of many recorded command streams (one CudaBackend each).
+//
+// A round takes every stream one render pass further: the stream's transfers
+// and CLUT loads before that pass, its setup / heuristic / texture decode, and
+// the binning of its next instance segment run as one branch per stream; the
+// branches join and a single persistent launch shades all collected segments.
+// Streams with more instance segments continue in further sub-rounds.  The
+// whole schedule is captured as one CUDA graph.
+struct BatchEngine
+{
+	int device = 0;
+	int sm_count = 0;
+	cudaStream_t master = nullptr;
+	cudaEvent_t fork_ev = nullptr;
+	std::vector<CudaBackend *> streams;
+	std::vector<cudaEvent_t> join_ev;
+
+	// Work items of every sub-round, in schedule order.
+	ShadeItem *h_items = nullptr, *d_items = nullptr;
+	size_t items_cap = 0;
+	uint32_t *d_counters = nullptr;
+	size_t counters_cap = 0;
+	size_t n_items = 0, n_launches = 0;
+
+	// Tuning: persistent CTA size and CTAs per SM.
+	uint32_t block = 256, ctas_per_sm = 4;
+	bool largest_first = true;
+
+	cudaGraphExec_t exec = nullptr;
+	uint32_t launches_per_replay = 0;
+
+	struct Cursor
+	{
+		size_t op = 0;
+		const PassOp *pass = nullptr;
+		PassParams P;
+		std::vector<CudaBackend::Segment> segs;
+		size_t seg = 0;
+	};
+
+	int init(int dev)
+	{
+		device = dev;
+		CUDA_TRY(cudaSetDevice(device));
+		CUDA_TRY(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
+		CUDA_TRY(cudaStreamCreateWithFlags(&master, cudaStreamNonBlocking));
+		CUDA_TRY(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+		return PGS_OK;
+	}
+
+	void destroy()
+	{
+		cudaSetDevice(device);
+		if (master)
+			cudaStreamSynchronize(master);
+		if (exec)
+			cudaGraphExecDestroy(exec);
+		for (cudaEvent_t e : join_ev)
+			cudaEventDestroy(e);
+		if (fork_ev)
+			cudaEventDestroy(fork_ev);
+		cudaFreeHost(h_items);
+		cudaFree(d_items);
+		cudaFree(d_counters);
+		if (master)
+			cudaStreamDestroy(master);
+	}
+
+	int add(CudaBackend *b)
+	{
+		if (b->device != device || b->ops.empty() || !b->d_reset_vram)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		cudaEvent_t e;
+		CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+		streams.push_back(b);
+		join_ev.push_back(e);
+		invalidate();
+		return PGS_OK;
+	}
+
+	void invalidate()
+	{
+		if (exec)
+		{
+			cudaGraphExecDestroy(exec);
+			exec = nullptr;
+		}
+	}
+
+	int fork()
+	{
+		CUDA_TRY(cudaEventRecord(fork_ev, master));
+		for (CudaBackend *b : streams)
+			CUDA_TRY(cudaStreamWaitEvent(b->stream, fork_ev, 0));
+		return PGS_OK;
+	}
+
+	int join()
+	{
+		for (size_t i = 0; i < streams.size(); i++)
+		{
+			CUDA_TRY(cudaEventRecord(join_ev[i], streams[i]->stream));
+			CUDA_TRY(cudaStreamWaitEvent(master, join_ev[i], 0));
+		}
+		return PGS_OK;
+	}
+
+	template <int BLOCK>
+	int launch(size_t first, size_t count, uint32_t units, uint32_t counter)
+	{
+		uint32_t grid = std::max<uint32_t>(1u, std::min<uint32_t>(uint32_t(sm_count) * ctas_per_sm,
+		                                                          (units + BLOCK / 32 - 1) / (BLOCK / 32)));
+		batch_shade_kernel<BLOCK><<<grid, BLOCK, 0, master>>>(d_items + first, uint32_t(count), units,
+		                                                      d_counters + counter);
+		CUDA_TRY(cudaGetLastError());
+		return PGS_OK;
+	}
+
+	// One pass over the schedule, launched (or captured) on the master stream
+	// and the streams' own streams.
+	int run(bool reset)
+	{
+		// An eager run rewrites the pinned item table, which an earlier run's
+		// copies may still read.
+		cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+		CUDA_TRY(cudaStreamIsCapturing(master, &cs));
+		if (cs == cudaStreamCaptureStatusNone)
+			CUDA_TRY(cudaStreamSynchronize(master));
+		std::vector<Cursor> cur(streams.size());
+		std::vector<ShadeItem> round_items;
+		n_items = 0;
+		n_launches = 0;
+		uint32_t kernels = 0;
+		for (CudaBackend *b : streams)
+		{
+			b->launch_counter = 0;
+			b->shade_started = false;
+		}
+		if (counters_cap)
+			CUDA_TRY(cudaMemsetAsync(d_counters, 0, counters_cap * sizeof(uint32_t), master));
+		int r = fork();
+		if (r)
+			return r;
+		if (reset)
+			for (CudaBackend *b : streams)
+			{
+				CUDA_TRY(cudaMemcpyAsync(b->d_vram, b->d_reset_vram, size_t(b->reset_planes) * VRAM_SIZE,
+				                         cudaMemcpyDeviceToDevice, b->stream));
+				CUDA_TRY(cudaMemcpyAsync(b->d_clut, b->d_reset_clut, size_t(PGS_CLUT_INSTANCES) * PGS_CLUT_SIZE_BYTES,
+				                         cudaMemcpyDeviceToDevice, b->stream));
+			}
+		for (;;)
+		{
+			// Round: every stream up to and including the start of its next pass.
+			bool any = false;
+			for (size_t s = 0; s < streams.size(); s++)
+			{
+				CudaBackend *b = streams[s];
+				Cursor &c = cur[s];
+				c.pass = nullptr;
+				c.segs.clear();
+				c.seg = 0;
+				while (c.op < b->ops.size() && b->ops[c.op].type != OP_PASS)
+				{
+					r = b->execute(b->ops[c.op++]);
+					if (r)
+						return r;
+				}
+				if (c.op < b->ops.size())
+				{
+					c.pass = &b->ops[c.op++].pass;
+					r = b->begin_pass(*c.pass, c.P, c.segs);
+					if (r)
+						return r;
+					any = true;
+				}
+			}
+			if (!any)
+				break;
+			// Sub-rounds: one instance segment of every stream that has one.
+			for (;;)
+			{
+				size_t first = n_items;
+				round_items.clear();
+				bool more = false;
+				for (size_t s = 0; s < streams.size(); s++)
+				{
+					Cursor &c = cur[s];
+					if (c.seg >= c.segs.size())
+						continue;
+					more = true;
+					const CudaBackend::Segment &g = c.segs[c.seg++];
+					ShadeItem item;
+					bool collected = false;
+					r = streams[s]->run_instance(c.P, *c.pass, g.inst, g.lo, g.count, &item, &collected);
+					if (r)
+						return r;
+					if (collected && item.units)
+					{
+						if (n_items >= items_cap)
+							return PGS_ERROR_CAPACITY;
+						round_items.push_back(item);
+						n_items++;
+					}
+				}
+				if (!more)
+					break;
+				r = join();
+				if (r)
+					return r;
+				if (n_items > first)
+				{
+					{
+						if (n_launches >= counters_cap)
+							return PGS_ERROR_CAPACITY;
+						size_t count = n_items - first;
+						if (largest_first)
+							std::stable_sort(round_items.begin(), round_items.end(),
+							                 [](const ShadeItem &a, const ShadeItem &b) { return a.units > b.units; });
+						uint32_t units = 0;
+						for (ShadeItem &x : round_items)
+						{
+							x.unit_base = units;
+							units += x.units;
+						}
+						ShadeItem *it = h_items + first;
+						memcpy(it, round_items.data(), count * sizeof(ShadeItem));
+						CUDA_TRY(cudaMemcpyAsync(d_items + first, it, count * sizeof(ShadeItem), cudaMemcpyHostToDevice,
+						                         master));
+						switch (block)
+						{
+						case 128: r = launch<128>(first, count, units, uint32_t(n_launches)); break;
+						case 512: r = launch<512>(first, count, units, uint32_t(n_launches)); break;
+						default: r = launch<256>(first, count, units, uint32_t(n_launches)); break;
+						}
+						if (r)
+							return r;
+						kernels++;
+					}
+					n_launches++;
+				}
+				r = fork();
+				if (r)
+					return r;
+			}
+		}
+		// Operations after the last pass of each stream.
+		for (size_t s = 0; s < streams.size(); s++)
+			while (cur[s].op < streams[s]->ops.size())
+			{
+				r = streams[s]->execute(streams[s]->ops[cur[s].op++]);
+				if (r)
+					return r;
+			}
+		r = join();
+		if (r)
+			return r;
+		uint32_t total = kernels;
+		for (CudaBackend *b : streams)
+			total += b->launch_counter;
+		launches_per_replay = total;
+		return PGS_OK;
+	}
+
+	// Upper bounds of work items (every instance segment) and batched launches
+	// (per round, the most segments any stream's pass has) from the recorded
+	// operations alone, and buffers of that size.
+	int size_buffers()
+	{
+		size_t items = 0, launches = 0;
+		std::vector<std::vector<size_t>> per_stream(streams.size());
+		std::vector<CudaBackend::Segment> segs;
+		size_t rounds = 0;
+		for (size_t s = 0; s < streams.size(); s++)
+		{
+			for (const Op &op : streams[s]->ops)
+				if (op.type == OP_PASS)
+				{
+					streams[s]->pass_segments(op.pass, segs);
+					per_stream[s].push_back(segs.size());
+					items += segs.size();
+				}
+			rounds = std::max(rounds, per_stream[s].size());
+		}
+		for (size_t j = 0; j < rounds; j++)
+		{
+			size_t m = 0;
+			for (auto &v : per_stream)
+				if (j < v.size())
+					m = std::max(m, v[j]);
+			launches += m;
+		}
+		items = std::max<size_t>(items, 1);
+		launches = std::max<size_t>(launches, 1);
+		if (items > items_cap)
+		{
+			cudaFreeHost(h_items);
+			cudaFree(d_items);
+			h_items = nullptr;
+			d_items = nullptr;
+			items_cap = 0;
+			CUDA_TRY(cudaMallocHost(&h_items, items * sizeof(ShadeItem)));
+			CUDA_TRY(cudaMalloc(&d_items, items * sizeof(ShadeItem)));
+			items_cap = items;
+		}
+		if (launches > counters_cap)
+		{
+			cudaFree(d_counters);
+			d_counters = nullptr;
+			counters_cap = 0;
+			CUDA_TRY(cudaMalloc(&d_counters, launches * sizeof(uint32_t)));
+			counters_cap = launches;
+		}
+		return PGS_OK;
+	}
+
+	int replay(uint32_t count, bool reset, bool use_graph)
+	{
+		if (streams.empty())
+			return PGS_ERROR_INVALID_ARGUMENT;
+		CUDA_TRY(cudaSetDevice(device));
+		int r = size_buffers();
+		if (r)
+			return r;
+		if (!use_graph)
+		{
+			for (uint32_t i = 0; r == PGS_OK && i < count; i++)
+				r = run(reset);
+			return r;
+		}
+		if (!exec)
+		{
+			if (count == 0)
+				return PGS_OK;
+			// The first replay runs eagerly: it sizes every stream's scratch
+			// buffers, which must not be allocated during capture.
+			r = run(reset);
+			if (r)
+				return r;
+			count--;
+			for (CudaBackend *b : streams)
+				CUDA_TRY(cudaStreamSynchronize(b->stream));
+			CUDA_TRY(cudaStreamSynchronize(master));
+			cudaGraph_t graph;
+			CUDA_TRY(cudaStreamBeginCapture(master, cudaStreamCaptureModeThreadLocal));
+			r = run(reset);
+			cudaError_t e = cudaStreamEndCapture(master, &graph);
+			if (r)
+				return r;
+			if (e != cudaSuccess)
+				return PGS_ERROR_CUDA;
+			CUDA_TRY(cudaGraphInstantiate(&exec, graph, 0));
+			cudaGraphDestroy(graph);
+		}
+		for (uint32_t i = 0; i < count; i++)
+			CUDA_TRY(cudaGraphLaunch(exec, master));
+		return PGS_OK;
+	}
+};
+
+// ---------------------------------------------------------------------------
 // pgs_backend_ops table.
 CudaBackend *B(void *s) { return static_cast<CudaBackend *>(s); }
 
@@ -1223,6 +1628,151 @@ int pgs_cuda_backend_replay(void *backend, uint32_t count, int reset_vram, int u
 	return backend ? B(backend)->replay(count, reset_vram != 0, use_graph != 0) : PGS_ERROR_INVALID_ARGUMENT;
 }
 void *pgs_cuda_backend_stream(void *backend) { return backend ? static_cast<void *>(B(backend)->stream) : nullptr; }
+
+// ---------------------------------------------------------------------------
+// Batched replay.
+struct pgs_batch
+{
+	BatchEngine e;
+};
+
+pgs_batch *pgs_batch_create(int device, int *status)
+{
+	int dummy;
+	if (!status)
+		status = &dummy;
+	int count = 0;
+	if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+	{
+		*status = PGS_ERROR_NO_DEVICE;
+		return nullptr;
+	}
+	auto *b = new (std::nothrow) pgs_batch();
+	if (!b)
+	{
+		*status = PGS_ERROR_OUT_OF_MEMORY;
+		return nullptr;
+	}
+	int r = b->e.init(device);
+	if (r)
+	{
+		b->e.destroy();
+		delete b;
+		*status = r;
+		return nullptr;
+	}
+	*status = PGS_OK;
+	return b;
+}
+
+void pgs_batch_destroy(pgs_batch *batch)
+{
+	if (!batch)
+		return;
+	batch->e.destroy();
+	delete batch;
+}
+
+int pgs_batch_add(pgs_batch *batch, void *cuda_backend)
+{
+	return batch && cuda_backend ? batch->e.add(B(cuda_backend)) : PGS_ERROR_INVALID_ARGUMENT;
+}
+
+int pgs_batch_replay(pgs_batch *batch, uint32_t count, int reset_vram, int use_graph)
+{
+	return batch ? batch->e.replay(count, reset_vram != 0, use_graph != 0) : PGS_ERROR_INVALID_ARGUMENT;
+}
+
+int pgs_batch_set_tuning(pgs_batch *batch, const pgs_batch_tuning *tuning)
+{
+	if (!batch || !tuning)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	uint32_t block = tuning->cta_threads;
+	if ((block != 128 && block != 256 && block != 512) || tuning->ctas_per_sm == 0 ||
+	    tuning->ctas_per_sm * block > 1024)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	batch->e.block = block;
+	batch->e.ctas_per_sm = tuning->ctas_per_sm;
+	batch->e.largest_first = tuning->largest_first != 0;
+	batch->e.invalidate();
+	return PGS_OK;
+}
+
+int pgs_batch_get_tuning(pgs_batch *batch, pgs_batch_tuning *tuning)
+{
+	if (!batch || !tuning)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	tuning->cta_threads = batch->e.block;
+	tuning->ctas_per_sm = batch->e.ctas_per_sm;
+	tuning->largest_first = batch->e.largest_first;
+	return PGS_OK;
+}
+
+int pgs_batch_autotune(pgs_batch *batch, uint32_t trials, int reset_vram, pgs_batch_tuning *best, float *best_ms)
+{
+	if (!batch || trials == 0)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	BatchEngine &e = batch->e;
+	static const pgs_batch_tuning candidates[] = {
+		{ 128, 8, 1 }, { 128, 4, 1 }, { 256, 4, 1 }, { 256, 2, 1 }, { 512, 2, 1 }, { 512, 1, 1 },
+		{ 256, 4, 0 },
+	};
+	cudaEvent_t ev[2];
+	CUDA_TRY(cudaSetDevice(e.device));
+	CUDA_TRY(cudaEventCreate(&ev[0]));
+	CUDA_TRY(cudaEventCreate(&ev[1]));
+	pgs_batch_tuning chosen = candidates[0];
+	float chosen_ms = 0.0f;
+	int r = PGS_OK;
+	for (const pgs_batch_tuning &c : candidates)
+	{
+		r = pgs_batch_set_tuning(batch, &c);
+		if (!r)
+			r = e.replay(1, reset_vram != 0, true);  // builds the graph
+		if (r)
+			break;
+		cudaEventRecord(ev[0], e.master);
+		r = e.replay(trials, reset_vram != 0, true);
+		cudaEventRecord(ev[1], e.master);
+		if (r)
+			break;
+		float ms = 0.0f;
+		if (cudaEventSynchronize(ev[1]) != cudaSuccess || cudaEventElapsedTime(&ms, ev[0], ev[1]) != cudaSuccess)
+		{
+			r = PGS_ERROR_CUDA;
+			break;
+		}
+		ms /= float(trials);
+		if (chosen_ms == 0.0f || ms < chosen_ms)
+		{
+			chosen = c;
+			chosen_ms = ms;
+		}
+	}
+	cudaEventDestroy(ev[0]);
+	cudaEventDestroy(ev[1]);
+	if (r)
+		return r;
+	r = pgs_batch_set_tuning(batch, &chosen);
+	if (best)
+		*best = chosen;
+	if (best_ms)
+		*best_ms = chosen_ms;
+	return r;
+}
+
+void *pgs_batch_stream(pgs_batch *batch) { return batch ? static_cast<void *>(batch->e.master) : nullptr; }
+uint32_t pgs_batch_launches_per_replay(pgs_batch *batch) { return batch ? batch->e.launches_per_replay : 0; }
+int pgs_batch_synchronize(pgs_batch *batch)
+{
+	if (!batch)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	CUDA_TRY(cudaSetDevice(batch->e.device));
+	CUDA_TRY(cudaStreamSynchronize(batch->e.master));
+	for (CudaBackend *b : batch->e.streams)
+		CUDA_TRY(cudaStreamSynchronize(b->stream));
+	return PGS_OK;
+}
 uint32_t pgs_cuda_backend_launches_per_replay(void *backend) { return backend ? B(backend)->launches_per_replay : 0; }
 int pgs_cuda_backend_last_shade_ms(void *backend, float *ms)
 {

@@ -143,7 +143,7 @@ __constant__ uint8_t c_rcp_tab[256];
 #ifndef PGS_SHADE_OCC
 #define PGS_SHADE_OCC 4
 #endif
-#define PGS_SHADE_MIN_BLOCKS(NS) ((NS) <= 4 && PGS_SHADE_OCC > 0 ? (PGS_SHADE_OCC * 4 / (NS)) : 1)
+#define PGS_SHADE_MIN_BLOCKS(NS) (PGS_SHADE_OCC * 4 / (NS) > 0 ? PGS_SHADE_OCC * 4 / (NS) : 1)
 
 // ---------------------------------------------------------------------------
 // Scalar helpers.
@@ -1510,23 +1510,28 @@ __device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi
 // Each warp walks the sub-tile's primitive bitmask on its own (no shared
 // memory, no barriers).  SS selects the super-sampled path; sub-tiles whose
 // coarse tile selects the other path exit immediately.
-template <int NS, bool SS, bool AA>
-__global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kernel(PassParams P, DevInstance I, const uint32_t *sub_masks,
-                                                        const uint32_t *sub_summary, const uint32_t *tile_flags)
+// Coarse-tile state of sub-tile `sub`: 0 = empty, 1 = single-sampled,
+// 2 = super-sampled (binning.comp:272-311 decision).
+__device__ __forceinline__ uint32_t subtile_mode(const PassParams &P, const DevInstance &I, const uint32_t *tile_flags,
+                                                 uint32_t sub)
 {
-	const uint32_t sub = blockIdx.x;
-	if (sub >= I.sub_w * I.sub_h)
-		return;
 	const uint32_t gx = sub % I.sub_w, gy = sub / I.sub_w;
 	const uint32_t sh = P.tile_size_log2 - 3u;
-	const uint32_t tile = (gy >> sh) * I.tiles_w + (gx >> sh);
-	const uint32_t flags = tile_flags[tile];
+	const uint32_t flags = tile_flags[(gy >> sh) * I.tiles_w + (gx >> sh)];
 	if (!(flags & TILE_NONEMPTY))
-		return;
+		return 0;
 	bool req = (flags & TILE_REQ_SS) || ((flags & TILE_REQ_SS_ZW) && (flags & TILE_HAS_ZW));
-	bool ss_tile = I.rate_y_log2 != 0 && req;
-	if (ss_tile != SS)
-		return;
+	return (I.rate_y_log2 != 0 && req) ? 2u : 1u;
+}
+
+// One sub-tile's pixel samples; `t` is the thread's index among the 64 * NS
+// threads that cover the sub-tile.  Warps are independent: each walks the
+// sub-tile's primitive bitmask on its own and needs no barrier.
+template <int NS, bool SS, bool AA>
+__device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInstance &I, const uint32_t *sub_masks,
+                                              const uint32_t *sub_summary, uint32_t sub, uint32_t t)
+{
+	const uint32_t gx = sub % I.sub_w, gy = sub / I.sub_w;
 	const uint32_t *summary = sub_summary + size_t(sub) * I.summary_words;
 	const uint32_t *mask = sub_masks + size_t(sub) * I.mask_words;
 
@@ -1541,7 +1546,6 @@ __global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kerne
 	C.zb_psm = I.zb_psm;
 
 	const int32_t sub_x = I.base_x + int32_t(gx * 8u), sub_y = I.base_y + int32_t(gy * 8u);
-	const uint32_t t = threadIdx.x;
 	const uint32_t lane = t & 31u;
 	const uint32_t sample = t % NS;
 	const uint32_t pix = t / NS;
@@ -1761,6 +1765,120 @@ __global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kerne
 			}
 			else
 				vram32[z_index] = depth;
+		}
+	}
+}
+
+template <int NS, bool SS, bool AA>
+__global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kernel(PassParams P, DevInstance I, const uint32_t *sub_masks,
+                                                        const uint32_t *sub_summary, const uint32_t *tile_flags)
+{
+	const uint32_t sub = blockIdx.x;
+	if (sub >= I.sub_w * I.sub_h)
+		return;
+	if (subtile_mode(P, I, tile_flags, sub) != (SS ? 2u : 1u))
+		return;
+	shade_subtile<NS, SS, AA>(P, I, sub_masks, sub_summary, sub, threadIdx.x);
+}
+
+// ---------------------------------------------------------------------------
+// Batched shading: one launch shades the current instance segment of many
+// independent command streams.  Each item is one (stream, pass, segment)
+// with its own VRAM, records and bins; its work is cut into warp units
+// (sub-tile, warp) -- 2 * 2^ns_log2 units per sub-tile, of which a
+// single-sampled tile uses the first two -- that persistent warps take from a
+// global counter, so streams of very different sizes share the GPU without
+// a tail per stream.
+struct ShadeItem
+{
+	PassParams P;
+	DevInstance I;
+	const uint32_t *masks, *summary, *flags;
+	uint32_t ns_log2, aa;
+	uint32_t unit_base, units;
+};
+
+// Sample counts the batched kernel shades itself (1x, 2x, 4x instances).
+constexpr uint32_t BATCH_MAX_NS_LOG2 = 2;
+
+// Separate functions per variant keep each variant's register allocation
+// its own inside the batched kernel.
+template <int NS, bool SS, bool AA>
+__device__ __noinline__ void shade_subtile_call(const PassParams &P, const DevInstance &I, const uint32_t *sub_masks,
+                                                const uint32_t *sub_summary, uint32_t sub, uint32_t t)
+{
+	shade_subtile<NS, SS, AA>(P, I, sub_masks, sub_summary, sub, t);
+}
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_shade_kernel(const ShadeItem *items, uint32_t n_items,
+                                                                         uint32_t total_units, uint32_t *counter)
+{
+	constexpr int WARPS = BLOCK / 32;
+	__shared__ PassParams sP[WARPS];
+	__shared__ DevInstance sI[WARPS];
+	const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+	uint32_t loaded = 0xffffffffu;
+	for (;;)
+	{
+		uint32_t unit = 0;
+		if (lane == 0)
+			unit = atomicAdd(counter, 1u);
+		unit = __shfl_sync(0xffffffffu, unit, 0);
+		if (unit >= total_units)
+			break;
+		uint32_t lo = 0, hi = n_items - 1;
+		while (lo < hi)
+		{
+			uint32_t mid = (lo + hi + 1u) >> 1;
+			if (items[mid].unit_base <= unit)
+				lo = mid;
+			else
+				hi = mid - 1u;
+		}
+		const ShadeItem &it = items[lo];
+		if (lo != loaded)
+		{
+			// Item parameters into this warp's shared slot.
+			__syncwarp();
+			const uint32_t *srcP = reinterpret_cast<const uint32_t *>(&it.P);
+			uint32_t *dstP = reinterpret_cast<uint32_t *>(&sP[warp]);
+			for (uint32_t k = lane; k < sizeof(PassParams) / 4; k += 32u)
+				dstP[k] = srcP[k];
+			const uint32_t *srcI = reinterpret_cast<const uint32_t *>(&it.I);
+			uint32_t *dstI = reinterpret_cast<uint32_t *>(&sI[warp]);
+			for (uint32_t k = lane; k < sizeof(DevInstance) / 4; k += 32u)
+				dstI[k] = srcI[k];
+			__syncwarp();
+			loaded = lo;
+		}
+		const PassParams &P = sP[warp];
+		const DevInstance &I = sI[warp];
+		const uint32_t local = unit - it.unit_base;
+		const uint32_t per_sub = 2u << it.ns_log2;
+		const uint32_t sub = local / per_sub, w = local % per_sub;
+		const uint32_t mode = subtile_mode(P, I, it.flags, sub);
+		if (mode == 0)
+			continue;
+		const uint32_t ns_log2 = mode == 2 ? it.ns_log2 : 0u;
+		if (w >= (2u << ns_log2))
+			continue;
+		const uint32_t t = w * 32u + lane;
+		const bool aa = it.aa != 0;
+		switch (ns_log2)
+		{
+		case 0:
+			if (aa) shade_subtile_call<1, false, true>(P, I, it.masks, it.summary, sub, t);
+			else shade_subtile_call<1, false, false>(P, I, it.masks, it.summary, sub, t);
+			break;
+		case 1:
+			if (aa) shade_subtile_call<2, true, true>(P, I, it.masks, it.summary, sub, t);
+			else shade_subtile_call<2, true, false>(P, I, it.masks, it.summary, sub, t);
+			break;
+		default:
+			if (aa) shade_subtile_call<4, true, true>(P, I, it.masks, it.summary, sub, t);
+			else shade_subtile_call<4, true, false>(P, I, it.masks, it.summary, sub, t);
+			break;
 		}
 	}
 }

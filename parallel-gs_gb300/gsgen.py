@@ -521,3 +521,119 @@ def frame_c4(seed: int = 4, super_sampling: int = 8, num_triangles: int = 100000
                 s.packed(prim_reg(PRIM_TRI, iip=1), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
     return Frame("c4", s.tobytes(), super_sampling, super_sampling != 8, num_triangles,
                  {"width": width, "height": height, "fbp": fb_a, "fb_b": fb_b, "zbp": zbp, "passes": passes})
+
+
+def _mixed_textures(rng, s: GifStream, base_page: int, page_budget: int):
+    """1-4 textures of PSMT4 / PSMT8 / PSMCT32, 64x64 to 512x512, with random CT32
+    CLUTs, placed from `base_page` within `page_budget` pages.  Returns TEX0 values."""
+    tex0s = []
+    page = base_page
+    end = base_page + page_budget
+    for _ in range(int(rng.integers(1, 5))):
+        psm = [PSMT4, PSMT8, PSMCT32][int(rng.integers(0, 3))]
+        tw, th = int(rng.integers(6, 10)), int(rng.integers(6, 10))
+        w, h = 1 << tw, 1 << th
+        bpp = {PSMT4: 4, PSMT8: 8, PSMCT32: 32}[psm]
+        # Page geometry (width x height in pixels) per format; TBW in 64-pixel units.
+        pw, ph = {PSMT4: (128, 128), PSMT8: (128, 64), PSMCT32: (64, 32)}[psm]
+        pages = max(1, -(-w // pw)) * max(1, -(-h // ph))
+        clut_pages = 1 if psm != PSMCT32 else 0
+        while page + pages + clut_pages > end and (tw > 6 or th > 6):
+            if tw >= th:
+                tw -= 1
+            else:
+                th -= 1
+            w, h = 1 << tw, 1 << th
+            pages = max(1, -(-w // pw)) * max(1, -(-h // ph))
+        if page + pages + clut_pages > end:
+            break
+        tbw = max(1, w // 64)
+        if psm in (PSMT4, PSMT8):
+            tbw = max(2, tbw + (tbw & 1))
+        tbp0 = page * BLOCKS_PER_PAGE
+        data = rng.integers(0, 256, size=w * h * bpp // 8, dtype=np.uint8).tobytes()
+        s.upload(tbp0, tbw, psm, 0, 0, w, h, data)
+        page += pages
+        cbp = cpsm = 0
+        if psm != PSMCT32:
+            cw, ch = (16, 16) if psm == PSMT8 else (8, 2)
+            cbp = page * BLOCKS_PER_PAGE
+            clut = rng.integers(0, 1 << 32, size=cw * ch, dtype=np.uint64).astype(np.uint32).tobytes()
+            s.upload(cbp, 1, PSMCT32, 0, 0, cw, ch, clut)
+            page += 1
+        tex0s.append(tex0_reg(tbp0, tbw, psm, tw, th, tcc=1, tfx=int(rng.integers(0, 2)), cbp=cbp, cpsm=cpsm,
+                              csm=0, csa=0, cld=1 if psm != PSMCT32 else 0))
+    return tex0s
+
+
+def stream_c3(stream_id: int, num_primitives: int | None = None) -> Frame:
+    """One of the 64 mixed streams of the batched-replay workload.
+
+    Seeded by the stream id: primitive count log-uniform in 1k-200k, a
+    PSMCT16 (+PSMZ16) or PSMCT32 (+PSMZ24) framebuffer from 320x240 to 640x512,
+    1-4 PSMT4/PSMT8/PSMCT32 textures of 64x64 to 512x512 with random CLUTs, and
+    1x/2x/4x SSAA.  Draws mix perspective-textured triangles, Gouraud
+    triangles and sprites with random blend and alpha-test state."""
+    rng = np.random.Generator(np.random.PCG64(1000 + stream_id))
+    n = int(round(np.exp(rng.uniform(np.log(1000), np.log(200000))))) if num_primitives is None else num_primitives
+    fpsm = PSMCT16 if rng.uniform() < 0.5 else PSMCT32
+    zpsm = PSMZ16 if fpsm == PSMCT16 else PSMZ24
+    width = int(rng.integers(5, 11)) * 64
+    height = int(rng.integers(15, 33)) * 16
+    ss = [1, 2, 4][int(rng.integers(0, 3))]
+    bpp = 2 if fpsm == PSMCT16 else 4
+    pw, ph = (64, 64) if fpsm == PSMCT16 else (64, 32)
+    fb_pages = -(-width // pw) * -(-height // ph)
+    zbp = fb_pages
+    tex_base = 2 * fb_pages
+    s = GifStream()
+    _frame_setup(s, 0, width // 64, fpsm, zbp, zpsm, width, height, test_reg(zte=1, ztst=2),
+                 alpha=alpha_reg(0, 1, 0, 1),
+                 extra=[(COLCLAMP, 1), (TEX1_1, tex1_reg(mmag=1, mmin=1)), (TEXA, texa_reg(0, 0, 0x80)),
+                        (DTHE, int(rng.integers(0, 2))), (DIMX, dimx_reg(DEFAULT_DIMX))])
+    tex0s = _mixed_textures(rng, s, tex_base, 512 - tex_base)
+    zmax = (1 << (16 if zpsm == PSMZ16 else 24)) - 1
+    area_hi = 4000.0 * (width * height) / (640 * 448)
+    done = 0
+    while done < n:
+        m = min(n - done, int(rng.integers(50, 2000)))
+        kind = rng.uniform()
+        state = [(TEST_1, test_reg(ate=int(rng.uniform() < 0.3), atst=6, aref=int(rng.integers(0, 128)), afail=0,
+                                   zte=1, ztst=2))]
+        abe = int(rng.uniform() < 0.4)
+        if tex0s and kind < 0.7:
+            state += [(TEX0_1, tex0s[int(rng.integers(0, len(tex0s)))]), (CLAMP_1, clamp_reg(0, 0))]
+        s.ad(state)
+        z = rng.integers(0, zmax + 1, size=(m, 3), dtype=np.int64)
+        rgba = rng.integers(0, 256, size=(m, 3, 4), dtype=np.int64)
+        if kind < 0.6 and tex0s:
+            x, y = random_triangles(rng, m, width, height, 4.0, area_hi)
+            qv = rng.uniform(0.25, 4.0, size=(m, 3)).astype(np.float32)
+            sn = rng.uniform(0.0, 1.0, size=(m, 3)).astype(np.float32)
+            tn = rng.uniform(0.0, 1.0, size=(m, 3)).astype(np.float32)
+            nv = m * 3
+            q = np.zeros((nv, 3, 2), dtype=np.uint64)
+            q[:, 0] = q_st((sn * qv).reshape(nv), (tn * qv).reshape(nv), qv.reshape(nv))
+            q[:, 1] = q_rgbaq(rgba.reshape(nv, 4))
+            q[:, 2] = q_xyz2(x.reshape(nv), y.reshape(nv), z.reshape(nv))
+            s.packed(prim_reg(PRIM_TRI, iip=1, tme=1, abe=abe), [D_ST, D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+        elif kind < 0.7 and tex0s:
+            sx, sy = random_sprites(rng, m, width, height, 4.0, area_hi)
+            u = rng.integers(0, 256 * 16, size=(m, 2), dtype=np.int64)
+            v = rng.integers(0, 256 * 16, size=(m, 2), dtype=np.int64)
+            mv = m * 2
+            q = np.zeros((mv, 3, 2), dtype=np.uint64)
+            q[:, 0] = q_uv(u.reshape(mv), v.reshape(mv))
+            q[:, 1] = q_rgbaq(rgba[:, :2].reshape(mv, 4))
+            q[:, 2] = q_xyz2(sx.reshape(mv), sy.reshape(mv), z[:, :2].reshape(mv))
+            s.packed(prim_reg(PRIM_SPRITE, iip=1, tme=1, abe=abe, fst=1), [D_UV, D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+        else:
+            x, y = random_triangles(rng, m, width, height, 4.0, area_hi)
+            nv = m * 3
+            q = np.zeros((nv, 2, 2), dtype=np.uint64)
+            q[:, 0] = q_rgbaq(rgba.reshape(nv, 4))
+            q[:, 1] = q_xyz2(x.reshape(nv), y.reshape(nv), z.reshape(nv))
+            s.packed(prim_reg(PRIM_TRI, iip=1, abe=abe), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+        done += m
+    return Frame("c3_%02d" % stream_id, s.tobytes(), ss, True, n,
+                 {"width": width, "height": height, "fbp": 0, "zbp": zbp, "fpsm": fpsm, "stream": stream_id})

@@ -56,7 +56,12 @@ class GSOptions(C.Structure):
 
 
 class CudaBackendOptions(C.Structure):
-    _fields_ = [("device", C.c_int), ("max_samples_log2", C.c_uint32), ("flags", C.c_uint32)]
+    _fields_ = [("device", C.c_int), ("max_samples_log2", C.c_uint32), ("flags", C.c_uint32),
+                ("arena_mib", C.c_uint32)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("cta_threads", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("largest_first", C.c_uint32)]
 
 
 class BackendStats(C.Structure):
@@ -70,6 +75,9 @@ EXPORTED_SYMBOLS = [
     "pgs_cuda_backend_replay", "pgs_cuda_backend_stream", "pgs_cuda_backend_launches_per_replay",
     "pgs_cuda_backend_last_shade_ms", "pgs_cuda_backend_fragment_count", "pgs_cuda_backend_get_stats",
     "pgs_cuda_backend_set_shade_timing",
+    "pgs_batch_create", "pgs_batch_destroy", "pgs_batch_add", "pgs_batch_replay", "pgs_batch_set_tuning",
+    "pgs_batch_get_tuning", "pgs_batch_autotune", "pgs_batch_stream", "pgs_batch_launches_per_replay",
+    "pgs_batch_synchronize",
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
     "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
     "pgs_gs_set_super_sampling_rate",
@@ -101,6 +109,20 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.pgs_cuda_backend_fragment_count.argtypes = [vp, C.POINTER(u64)]
     lib.pgs_cuda_backend_get_stats.argtypes = [vp, C.POINTER(BackendStats)]
     lib.pgs_cuda_backend_set_shade_timing.argtypes = [vp, i32]
+    lib.pgs_batch_create.argtypes = [C.c_int, C.POINTER(i32)]
+    lib.pgs_batch_create.restype = vp
+    lib.pgs_batch_destroy.argtypes = [vp]
+    lib.pgs_batch_destroy.restype = None
+    lib.pgs_batch_add.argtypes = [vp, vp]
+    lib.pgs_batch_replay.argtypes = [vp, u32, i32, i32]
+    lib.pgs_batch_set_tuning.argtypes = [vp, C.POINTER(BatchTuning)]
+    lib.pgs_batch_get_tuning.argtypes = [vp, C.POINTER(BatchTuning)]
+    lib.pgs_batch_autotune.argtypes = [vp, u32, i32, C.POINTER(BatchTuning), C.POINTER(C.c_float)]
+    lib.pgs_batch_stream.argtypes = [vp]
+    lib.pgs_batch_stream.restype = vp
+    lib.pgs_batch_launches_per_replay.argtypes = [vp]
+    lib.pgs_batch_launches_per_replay.restype = u32
+    lib.pgs_batch_synchronize.argtypes = [vp]
     lib.pgs_gs_create.argtypes = [vp, vp, C.POINTER(GSOptions), C.POINTER(i32)]
     lib.pgs_gs_create.restype = vp
     lib.pgs_gs_destroy.argtypes = [vp]
@@ -164,9 +186,9 @@ class Backend:
 class CudaBackend(Backend):
     """The sm_103a backend.  Fails loudly when no GPU or library is present."""
 
-    def __init__(self, device: int = 0, max_samples_log2: int = 4) -> None:
+    def __init__(self, device: int = 0, max_samples_log2: int = 4, arena_mib: int = 0) -> None:
         self.lib = load_library()
-        opts = CudaBackendOptions(device, max_samples_log2, 0)
+        opts = CudaBackendOptions(device, max_samples_log2, 0, arena_mib)
         ops = C.c_void_p()
         status = C.c_int(0)
         handle = self.lib.pgs_cuda_backend_create(C.byref(opts), C.byref(ops), C.byref(status))
@@ -282,3 +304,52 @@ class GSInterface:
             self.close()
         except Exception:
             pass
+
+
+class Batch:
+    """Batched replay of several recorded CudaBackends (pgs_batch_*)."""
+
+    def __init__(self, device: int = 0) -> None:
+        self.lib = load_library()
+        status = C.c_int(0)
+        self.handle = self.lib.pgs_batch_create(device, C.byref(status))
+        if not self.handle:
+            raise PGSError(status.value, "pgs_batch_create")
+        self.backends = []
+
+    def add(self, backend: "CudaBackend") -> None:
+        check(self.lib.pgs_batch_add(self.handle, backend.handle), "batch_add")
+        self.backends.append(backend)
+
+    def replay(self, count: int = 1, reset_vram: bool = True, use_graph: bool = True) -> None:
+        check(self.lib.pgs_batch_replay(self.handle, count, int(reset_vram), int(use_graph)), "batch_replay")
+
+    def set_tuning(self, cta_threads: int, ctas_per_sm: int, largest_first: bool = True) -> None:
+        t = BatchTuning(cta_threads, ctas_per_sm, int(largest_first))
+        check(self.lib.pgs_batch_set_tuning(self.handle, C.byref(t)), "batch_set_tuning")
+
+    def tuning(self) -> dict:
+        t = BatchTuning()
+        check(self.lib.pgs_batch_get_tuning(self.handle, C.byref(t)), "batch_get_tuning")
+        return {"cta_threads": t.cta_threads, "ctas_per_sm": t.ctas_per_sm, "largest_first": bool(t.largest_first)}
+
+    def autotune(self, trials: int = 3, reset_vram: bool = True) -> tuple[dict, float]:
+        t = BatchTuning()
+        ms = C.c_float(0.0)
+        check(self.lib.pgs_batch_autotune(self.handle, trials, int(reset_vram), C.byref(t), C.byref(ms)), "autotune")
+        return ({"cta_threads": t.cta_threads, "ctas_per_sm": t.ctas_per_sm, "largest_first": bool(t.largest_first)},
+                float(ms.value))
+
+    def stream(self) -> int:
+        return self.lib.pgs_batch_stream(self.handle)
+
+    def launches_per_replay(self) -> int:
+        return int(self.lib.pgs_batch_launches_per_replay(self.handle))
+
+    def synchronize(self) -> None:
+        check(self.lib.pgs_batch_synchronize(self.handle), "batch_synchronize")
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.pgs_batch_destroy(self.handle)
+            self.handle = None
