@@ -47,10 +47,13 @@ WORKLOADS = {
              "pass's framebuffer, 8x SSAA (2x4)", "gsgen.frame_c4(super_sampling=8)"),
     "c4x16": ("feedback 640x448 CT32/Z24, 100k tris (80% 1-16 px), 10 passes, 20% draws sample the previous "
               "pass's framebuffer, 16x SSAA (4x4)", "gsgen.frame_c4(super_sampling=16)"),
+    "c3": ("batched replay: 64 seeded streams, 1k-200k prims (log-uniform), CT16/CT32 320x240-640x512, "
+           "PSMT4/PSMT8/CT32 textures 64^2-512^2 with CLUTs, 1x/2x/4x SSAA per stream",
+           "[gsgen.stream_c3(i) for i in range(64)]"),
 }
 # Texture and CLUT bytes uploaded per frame.
 TEXTURE_BYTES = {"c2": 8 * (256 * 256 + 16 * 16 * 4), "c1": 0, "c4x8": 4 * (128 * 128 + 16 * 16 * 4),
-                 "c4x16": 4 * (128 * 128 + 16 * 16 * 4)}
+                 "c4x16": 4 * (128 * 128 + 16 * 16 * 4), "c3": 0}
 
 
 def parse():
@@ -158,19 +161,23 @@ def run_reference(args, frame):
     import pgs_oracle  # noqa: E402
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    frames = frame if isinstance(frame, list) else [frame]
     for _ in range(max(0, min(args.warmup, 1))):
-        pgs_oracle.render(frame)
+        for f in frames[:1]:
+            pgs_oracle.render(f)
     times = []
     frags = 0
     for _ in range(args.steps):
-        be = pgs_oracle.OracleBackend()
+        frags = 0
         t = time.perf_counter()
-        pgs_oracle.render(frame, be)
+        for f in frames:
+            be = pgs_oracle.OracleBackend()
+            pgs_oracle.render(f, be)
+            frags += be.fragments()
+            be.close()
         times.append(time.perf_counter() - t)
-        frags = be.fragments()
-        be.close()
     total = sum(times)
-    fps = args.steps / total
+    fps = len(frames) * args.steps / total
     return {
         "metric": METRIC, "value": fps, "unit": "frames/s", "impl": "reference", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
@@ -192,11 +199,17 @@ def workload_expr(args) -> str:
 def make_frame(args):
     import gsgen  # noqa: F401,E402
     frame = eval(workload_expr(args), {"gsgen": gsgen})
+    if isinstance(frame, list):
+        return frame
     frame.meta["texture_bytes"] = TEXTURE_BYTES[args.workload]
     return frame
 
 
 def workload_config(args, frame) -> dict:
+    if isinstance(frame, list):
+        return {"workload": WORKLOADS[args.workload][0], "streams": len(frame),
+                "primitives": sum(f.num_primitives for f in frame),
+                "super_sampling": sorted({f.super_sampling for f in frame})}
     cfg = {"workload": WORKLOADS[args.workload][0], "primitives": frame.num_primitives,
            "super_sampling": frame.super_sampling}
     if args.workload == "c2":
@@ -222,12 +235,194 @@ def cpu_baseline_sample(args) -> dict:
         return {"value": None, "unit": "frames/s", "cores": 1, "kind": "port", "sample": "failed: %s" % e}
 
 
+def run_c3(args, frames, rank, world, local):
+    """64 mixed streams: plain per-frame graphs one after another, the same
+    graphs launched concurrently on their own streams, and the batched replay
+    (one CUDA graph per round schedule, persistent shading launch), the last
+    being `value`."""
+    import numpy as np
+    import torch
+    import pgs
+    from concurrent.futures import ThreadPoolExecutor
+
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+    dev = "cuda:%d" % local
+    ss_log2 = {1: 0, 2: 1, 4: 2, 8: 3, 16: 4}
+    backends, recorded = [], []
+    for f in frames:
+        be = pgs.CudaBackend(local, max_samples_log2=ss_log2[f.super_sampling], arena_mib=16)
+        gs = pgs.GSInterface(be, super_sampling=f.super_sampling, ordered=f.ordered)
+        be.begin_record()
+        gs.gif_transfer(0, f.data)
+        gs.flush()
+        be.end_record()
+        gs.close()
+        recorded.append(be.read_plane(0))
+        backends.append(be)
+    batch = pgs.Batch(local)
+    for be in backends:
+        batch.add(be)
+    tuning, tune_ms = batch.autotune(trials=3)
+    batch.replay(1)
+    batch.synchronize()
+    verified = all(np.array_equal(be.read_plane(0), r) for be, r in zip(backends, recorded))
+
+    # Plain per-frame path: each stream's frame graph, one frame at a time.
+    for be in backends:
+        be.replay(1)
+    torch.cuda.synchronize()
+    plain_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(plain_steps):
+        for be in backends:
+            be.replay(1)
+            torch.cuda.synchronize()
+    plain_fps = len(frames) * plain_steps / (time.perf_counter() - t0)
+    # The same graphs issued back to back on the streams' own CUDA streams.
+    t0 = time.perf_counter()
+    for _ in range(plain_steps):
+        for be in backends:
+            be.replay(1)
+    torch.cuda.synchronize()
+    concurrent_fps = len(frames) * plain_steps / (time.perf_counter() - t0)
+
+    # Batched replay, device-timed on the batch's stream.
+    bstream = torch.cuda.ExternalStream(batch.stream(), device=local)
+    flush_buf = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        batch.replay(1)
+    batch.synchronize()
+    frags0 = sum(be.fragments() for be in backends)
+    clocks = ClockSampler(local)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(bstream):
+        for i in range(args.steps):
+            flush_buf.fill_(i & 0xFF)
+            ev[i][0].record(bstream)
+            batch.replay(1)
+            ev[i][1].record(bstream)
+    batch.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    frags = (sum(be.fragments() for be in backends) - frags0) // args.steps
+    if pg:
+        total_ms = max_over_ranks(total_ms, pg, dev)
+    fps = replica_throughput(args.steps, world, total_ms) * len(frames)
+    t_wall = time.perf_counter()
+    batch.replay(args.steps)
+    batch.synchronize()
+    batched_wall_fps = len(frames) * args.steps / (time.perf_counter() - t_wall)
+
+    launches = batch.launches_per_replay()
+    # End to end: every stream decoded on the host by a pool of threads (the
+    # frontends are independent), uploaded, rendered, and read back.
+    e2e_fps, h2d, d2h = None, 0, 0
+    if not args.quick:
+        batch.close()
+        batch = None
+        outs = [torch.empty(pgs.VRAM_SIZE, dtype=torch.uint8, pin_memory=True).numpy() for _ in frames]
+        ifaces = [pgs.GSInterface(be, super_sampling=f.super_sampling, ordered=f.ordered)
+                  for be, f in zip(backends, frames)]
+        e2e_steps = max(2, min(args.steps, 5))
+
+        def one(i):
+            gs = ifaces[i]
+            gs.gif_transfer(0, frames[i].data)
+            gs.wait(gs.read_vram_async(outs[i]))
+
+        st0 = [be.stats() for be in backends]
+        with ThreadPoolExecutor(max_workers=min(32, os.cpu_count() or 1)) as pool:
+            list(pool.map(one, range(len(frames))))
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                list(pool.map(one, range(len(frames))))
+            e2e_dt = time.perf_counter() - t0
+        st1 = [be.stats() for be in backends]
+        e2e_fps = world * len(frames) * e2e_steps / e2e_dt
+        h2d = sum(b["h2d_bytes"] - a["h2d_bytes"] for a, b in zip(st0, st1)) // (e2e_steps + 1)
+        d2h = sum(b["d2h_bytes"] - a["d2h_bytes"] for a, b in zip(st0, st1)) // (e2e_steps + 1)
+        for gs in ifaces:
+            gs.close()
+    if batch:
+        batch.close()
+    if rank != 0:
+        if pg:
+            pg.barrier()
+        return
+    ab = sum(algorithmic_bytes(f, f.super_sampling)["shade"] for f in frames)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    peak_gbs = peaks.get("hbm_gbs", 6800.0)
+    achieved = ab / (total_ms / args.steps / 1000.0) / 1e9
+    cpu = None
+    if not (args.quick or args.no_cpu_baseline):
+        cpu = cpu_baseline_sample_expr("[gsgen.stream_c3(i) for i in range(4)]", "streams 0-3 of 64, one thread")
+    out = {
+        "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32+fp32", "data": "synthetic (seeded GS command stream)",
+        "config": dict(workload_config(args, frames), l2="flushed (256 MiB write) between steps",
+                       parallelism="replicas" if world > 1 else "single"),
+        "gfrag_per_s": frags * (fps / len(frames)) / 1e9,
+        "fragments_per_step": frags,
+        "plain_per_frame_fps": plain_fps,
+        "concurrent_per_frame_fps": concurrent_fps,
+        "batched_wall_fps": batched_wall_fps,
+        "batched_vs_plain": fps / plain_fps,
+        "autotuned": dict(tuning, ms_per_replay=tune_ms),
+        "replay_verified": verified,
+        "gpu_launches": launches * args.steps,
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                     "frac": achieved / peak_gbs, "traffic": None, "shade_bytes_per_step": ab,
+                     "note": "algorithmic bytes of all streams per replay / batched replay time; "
+                             "peak = measured hbm_gbs (of measured)"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+    }
+    print(json.dumps(out))
+    if pg:
+        pg.barrier()
+
+
+def cpu_baseline_sample_expr(expr: str, sample: str) -> dict:
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    code = ("import sys,time; sys.path.insert(0,%r); sys.path.insert(0,%r);"
+            "import gsgen,pgs_oracle;"
+            "fs=%s;"
+            "t=time.perf_counter(); [pgs_oracle.render(f) for f in fs]; print(len(fs)/(time.perf_counter()-t))") % (
+        str(ROOT / "parallel-gs_gb300"), str(ROOT / "oracle"), expr)
+    try:
+        out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+        return {"value": float(out.stdout.strip().splitlines()[-1]), "unit": "frames/s", "cores": 1, "kind": "port",
+                "sample": sample}
+    except Exception as e:  # noqa: BLE001
+        return {"value": None, "unit": "frames/s", "cores": 1, "kind": "port", "sample": "failed: %s" % e}
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     import gsgen  # noqa: E402
 
     frame = make_frame(args)
+    if isinstance(frame, list) and args.impl != "reference":
+        run_c3(args, frame, rank, world, local)
+        return
 
     if args.impl == "reference":
         if rank != 0:

@@ -1492,7 +1492,14 @@ struct BatchEngine
 
 // ---------------------------------------------------------------------------
 // pgs_backend_ops table.
-CudaBackend *B(void *s) { return static_cast<CudaBackend *>(s); }
+// Every entry point makes the backend's device current for the calling
+// thread: frontends of different streams may run on different host threads.
+CudaBackend *B(void *s)
+{
+	CudaBackend *b = static_cast<CudaBackend *>(s);
+	cudaSetDevice(b->device);
+	return b;
+}
 
 void c_destroy(void *self)
 {
