@@ -192,6 +192,19 @@ typedef struct pgs_flush_stats
 /* ------------------------------------------------------------------ */
 /* Backend interface (replaces GSRenderer)                              */
 /* ------------------------------------------------------------------ */
+/* One CRTC circuit read-out (sample_circuit.frag, gs/shaders/sample_circuit.frag:98-148,
+ * as set up by GSRenderer::sample_crtc_circuit, gs/gs_renderer.cpp:4055-4112).
+ * The output is width x height RGBA8; texels outside valid_width x
+ * valid_height are zero (the render pass clear). */
+typedef struct pgs_circuit_params
+{
+	uint32_t fbp, fbw, psm, dbx, dby;   /* DISPFB fields */
+	uint32_t phase, phase_stride;       /* first line offset and line step */
+	uint32_t super_samples;             /* 1, or 4 / 8 / 16 for a 2x2 high-resolution read-out */
+	uint32_t width, height;             /* output image extent */
+	uint32_t valid_width, valid_height; /* sampled part (scissor) */
+} pgs_circuit_params;
+
 typedef struct pgs_backend_ops
 {
 	uint32_t abi_version;
@@ -232,6 +245,9 @@ typedef struct pgs_backend_ops
 	 * wait_timeline, gs/gs_renderer.cpp:1037). */
 	int (*read_vram_async)(void *self, uint64_t offset, uint64_t size, void *dst, uint64_t *ticket);
 	int (*wait_ticket)(void *self, uint64_t ticket);
+	/* abi_version >= 2, optional: CRTC circuit read-out of the current VRAM into
+	 * host memory dst (params->width * params->height * 4 bytes). */
+	int (*sample_circuit)(void *self, const pgs_circuit_params *params, void *dst);
 } pgs_backend_ops;
 
 /* ------------------------------------------------------------------ */
@@ -383,6 +399,26 @@ int pgs_gs_read_vram(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst);
  * copy is made before returning and the ticket is 0. */
 int pgs_gs_read_vram_async(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst, uint64_t *ticket);
 int pgs_gs_wait(pgs_gs *gs, uint64_t ticket);
+
+/* Privileged registers (GSInterface::get_priv_register_state, gs/gs_interface.hpp:70-108):
+ * index 0 PMODE, 1 SMODE1, 2 SMODE2, 3 SRFSH, 4 SYNCH1, 5 SYNCH2, 6 SYNCV,
+ * 7 DISPFB1, 8 DISPLAY1, 9 DISPFB2, 10 DISPLAY2, 11 EXTBUF, 12 EXTDATA,
+ * 13 EXTWRITE, 14 BGCOLOR. */
+int pgs_gs_write_priv_register(pgs_gs *gs, uint32_t index, uint64_t value);
+int pgs_gs_read_priv_register(pgs_gs *gs, uint32_t index, uint64_t *value);
+
+#define PGS_SCANOUT_FORCE_PROGRESSIVE 1u
+#define PGS_SCANOUT_HIGH_RESOLUTION 2u
+/* CRTC read-out of circuit 0 or 1 (DISPFB1/DISPLAY1 or DISPFB2/DISPLAY2) for
+ * field `phase`, as GSRenderer::vsync samples it (compute_circuit_rect +
+ * sample_crtc_circuit, gs/gs_renderer.cpp:4055-4172, 4547-4560): flushes, then
+ * writes the RGBA8 circuit image into dst (capacity dst_size bytes) and its
+ * extent into *width / *height.  With PGS_SCANOUT_HIGH_RESOLUTION and a
+ * super-sampled frame scanned out progressively, the image is 2x2 larger and
+ * resolves the sample planes.  Circuit merging, PMODE blending and CRTC
+ * timings are not applied. */
+int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_t flags, void *dst, uint64_t dst_size,
+                           uint32_t *width, uint32_t *height);
 /* GSInterface::map_vram_write + end_vram_write. */
 int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *src);
 /* GSInterface::read_transfer_fifo. */

@@ -2183,9 +2183,89 @@ static int o_write(void *self, uint64_t off, uint64_t size, const void *src)
 }
 static int o_error(void *, uint32_t *flags) { if (flags) *flags = 0; return 0; }
 
+// sample_circuit.frag:51-148: one circuit read-out from the current VRAM
+// planes.  16-bit texels expand with alpha 0 / 0xff (rgba16_to_rgba32 with
+// TA0 = 0, TA1 = 0xff); 32-bit formats other than CT32 read alpha as 0x80.
+static uint32_t circuit_payload(const std::vector<uint8_t> &vram, uint32_t psm, uint32_t addr, uint32_t plane)
+{
+	const bool is16 = psm == 0x02 || psm == 0x0a || psm == 0x32 || psm == 0x3a;
+	if (is16)
+	{
+		uint16_t v;
+		memcpy(&v, vram.data() + size_t(plane) * oracle::VRAM + size_t(addr) * 2, 2);
+		uint32_t r = (v & 0x1fu) << 3, g = ((v >> 5) & 0x1fu) << 3, b = ((v >> 10) & 0x1fu) << 3;
+		uint32_t a = (v & 0x8000u) ? 0xffu : 0u;
+		return r | (g << 8) | (b << 16) | (a << 24);
+	}
+	uint32_t v;
+	memcpy(&v, vram.data() + size_t(plane) * oracle::VRAM + size_t(addr) * 4, 4);
+	if (psm != 0x00)
+		v = (v & ~0xff000000u) | 0x80000000u;
+	return v;
+}
+
+static int o_circuit(void *self, const pgs_circuit_params *cp, void *dst)
+{
+	if (!cp || !dst)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	const pgs_circuit_params &C = *cp;
+	auto *b = static_cast<Backend *>(self);
+	if (C.super_samples > 1 && 2u + C.super_samples > b->num_planes)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	const bool is16 = C.psm == 0x02 || C.psm == 0x0a || C.psm == 0x32 || C.psm == 0x3a;
+	uint32_t *out = static_cast<uint32_t *>(dst);
+	for (uint32_t y = 0; y < C.height; y++)
+		for (uint32_t x = 0; x < C.width; x++)
+		{
+			uint32_t o = 0;
+			if (x < C.valid_width && y < C.valid_height)
+			{
+				uint32_t sx = C.super_samples >= 4 ? x >> 1 : x, sy = C.super_samples >= 4 ? y >> 1 : y;
+				uint32_t cx = sx + C.dbx, cy = sy * C.phase_stride + C.dby + C.phase;
+				uint32_t addr = oracle::swizzle(cx, cy, C.fbp * 32, C.fbw, C.psm);
+				bool valid = false;
+				if (C.super_samples >= 4)
+				{
+					if (is16)
+					{
+						uint16_t r;
+						memcpy(&r, b->vram.data() + oracle::VRAM + size_t(addr) * 2, 2);
+						valid = r == 0xffff;
+					}
+					else
+					{
+						uint32_t r;
+						memcpy(&r, b->vram.data() + oracle::VRAM + size_t(addr) * 4, 4);
+						valid = C.psm != 0x00 ? (r & 0xffffffu) == 0xffffffu : r == 0xffffffffu;
+					}
+				}
+				if (!valid)
+					o = circuit_payload(b->vram, C.psm, addr, 0);
+				else
+				{
+					uint32_t n = C.super_samples / 4;
+					uint32_t quad = C.super_samples != 8 ? (y & 1u) + (x & 1u) * 2u : (x & 1u) + (y & 1u) * 2u;
+					uint32_t base = 2 + n * quad;
+					float v[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+					for (uint32_t i = 0; i < n; i++)
+					{
+						uint32_t c = circuit_payload(b->vram, C.psm, addr, base + i);
+						for (int k = 0; k < 4; k++)
+							v[k] = v[k] + oracle::unorm(c, k);
+					}
+					for (int k = 0; k < 4; k++)
+						v[k] = v[k] / float(n);
+					o = oracle::pack_unorm(v);
+				}
+			}
+			out[size_t(y) * C.width + x] = o;
+		}
+	return 0;
+}
+
 static const pgs_backend_ops ORACLE_OPS = {
 	PGS_ABI_VERSION, o_destroy, o_reserve, o_flush_rendering, o_copy, o_palette, o_set_ss, o_submit, o_read, o_write, o_error,
-	nullptr, nullptr,
+	nullptr, nullptr, o_circuit,
 };
 
 extern "C" {

@@ -130,6 +130,8 @@ struct CudaBackend
 	size_t flags_cap = 0;
 	uint32_t *d_texels = nullptr;
 	size_t texels_cap = 0;
+	uint32_t *d_circuit = nullptr;
+	size_t circuit_cap = 0;
 
 	// Recording.
 	bool recording = false;
@@ -241,6 +243,7 @@ struct CudaBackend
 		cudaFree(d_masks);
 		cudaFree(d_flags);
 		cudaFree(d_texels);
+		cudaFree(d_circuit);
 		cudaFree(d_arena);
 		cudaFree(d_reset_vram);
 		cudaFree(d_reset_clut);
@@ -1013,6 +1016,31 @@ struct CudaBackend
 		return ticket && ticket < next_ticket ? PGS_OK : PGS_ERROR_INVALID_ARGUMENT;
 	}
 
+	int sample_circuit(const pgs_circuit_params &c, void *dst)
+	{
+		size_t bytes = size_t(c.width) * c.height * 4u;
+		if (bytes == 0)
+			return PGS_OK;
+		if (c.super_samples > 1 && 2u + c.super_samples > num_planes)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		if (bytes > circuit_cap)
+		{
+			cudaFree(d_circuit);
+			d_circuit = nullptr;
+			circuit_cap = 0;
+			CUDA_TRY(cudaMalloc(&d_circuit, bytes));
+			circuit_cap = bytes;
+		}
+		dim3 grid((c.width + 31) / 32, (c.height + 7) / 8);
+		circuit_kernel<<<grid, 256, 0, stream>>>(c, d_vram, d_unorm_lut, d_circuit);
+		launch_counter++;
+		CUDA_TRY(cudaGetLastError());
+		CUDA_TRY(cudaMemcpyAsync(dst, d_circuit, bytes, cudaMemcpyDeviceToHost, stream));
+		CUDA_TRY(cudaStreamSynchronize(stream));
+		d2h_bytes += bytes;
+		return PGS_OK;
+	}
+
 	int write_vram(uint64_t off, uint64_t size, const void *src)
 	{
 		if (off + size > VRAM_SIZE)
@@ -1530,10 +1558,14 @@ int c_read_async(void *self, uint64_t off, uint64_t size, void *dst, uint64_t *t
 	return dst && ticket ? B(self)->read_vram_async(off, size, dst, *ticket) : PGS_ERROR_INVALID_ARGUMENT;
 }
 int c_wait(void *self, uint64_t ticket) { return B(self)->wait_ticket(ticket); }
+int c_circuit(void *self, const pgs_circuit_params *c, void *dst)
+{
+	return c && dst ? B(self)->sample_circuit(*c, dst) : PGS_ERROR_INVALID_ARGUMENT;
+}
 
 const pgs_backend_ops CUDA_OPS = {
 	PGS_ABI_VERSION, c_destroy, c_reserve, c_flush_rendering, c_copy, c_palette, c_set_ss, c_submit, c_read, c_write, c_error,
-	c_read_async, c_wait,
+	c_read_async, c_wait, c_circuit,
 };
 
 // ---------------------------------------------------------------------------

@@ -295,6 +295,8 @@ struct pgs_gs
 	void *be = nullptr;
 
 	uint64_t regs[128] = {};
+	// Privileged registers PMODE .. BGCOLOR (gs/gs_interface.hpp:70-91).
+	uint64_t priv[15] = {};
 	float internal_q = 1.0f;
 	uint32_t cached_cbp[2] = {};
 
@@ -1813,6 +1815,89 @@ int pgs_gs_wait(pgs_gs *gs, uint64_t ticket)
 	if (gs->ops->abi_version < 2 || !gs->ops->wait_ticket)
 		return PGS_ERROR_INVALID_ARGUMENT;
 	return gs->ops->wait_ticket(gs->be, ticket);
+}
+
+int pgs_gs_write_priv_register(pgs_gs *gs, uint32_t index, uint64_t value)
+{
+	if (!gs || index >= 15)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->priv[index] = value;
+	return PGS_OK;
+}
+
+int pgs_gs_read_priv_register(pgs_gs *gs, uint32_t index, uint64_t *value)
+{
+	if (!gs || !value || index >= 15)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	*value = gs->priv[index];
+	return PGS_OK;
+}
+
+int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_t flags, void *dst, uint64_t dst_size,
+                           uint32_t *width, uint32_t *height)
+{
+	if (!gs || circuit > 1 || !width || !height)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if (gs->ops->abi_version < 2 || !gs->ops->sample_circuit)
+		return PGS_ERROR_UNSUPPORTED;
+	gs->flush();
+	if (gs->sticky_error)
+		return gs->sticky_error;
+	const uint64_t dispfb = gs->priv[7 + 2 * circuit], display = gs->priv[8 + 2 * circuit];
+	const uint64_t smode2 = gs->priv[2], extwrite = gs->priv[13];
+	const bool force_progressive = (flags & PGS_SCANOUT_FORCE_PROGRESSIVE) != 0;
+
+	// compute_circuit_rect (gs/gs_renderer.cpp:4114-4172).
+	bool is_interlaced = field(smode2, 0, 1) != 0;
+	bool alternative_sampling = is_interlaced && !field(smode2, 1, 1);
+	if (alternative_sampling && force_progressive)
+		is_interlaced = false;
+	uint32_t DW = field(display, 32, 12) + 1, DH = field(display, 44, 11) + 1;
+	uint32_t MAGH = field(display, 23, 4) + 1, MAGV = field(display, 27, 2) + 1;
+	uint32_t DY = field(display, 12, 11);
+	uint32_t img_w = DW / MAGH, img_h = DH / MAGV, valid_w = img_w, valid_h;
+	uint32_t phase_offset = 0, phase_stride = 1;
+	// vsync samples the field given by `phase` only for alternating-line
+	// interlace that is not forced progressive (:4468-4478).
+	uint32_t field_phase = (alternative_sampling && !force_progressive) ? (phase & 1u) : 0u;
+	if (is_interlaced)
+	{
+		phase_offset = alternative_sampling ? ((DY ^ field_phase) & 1u) : 0u;
+		phase_stride = alternative_sampling ? 2u : 1u;
+		valid_h = (img_h - phase_offset + 1) >> 1;
+		img_h = (img_h + 1) >> 1;
+	}
+	else
+	{
+		valid_h = img_h;
+		img_h = (img_h + 1) & ~1u;
+	}
+
+	// High-resolution read-out of a super-sampled frame (:4217-4239).
+	bool high_res = (flags & PGS_SCANOUT_HIGH_RESOLUTION) != 0;
+	if (!force_progressive || field(extwrite, 0, 1) || !gs->sampling_rate_x_log2 || !gs->sampling_rate_y_log2)
+		high_res = false;
+	pgs_circuit_params c = {};
+	c.fbp = field(dispfb, 0, 9);
+	c.fbw = field(dispfb, 9, 6);
+	c.psm = field(dispfb, 15, 5);
+	c.dbx = field(dispfb, 32, 11);
+	c.dby = field(dispfb, 43, 11);
+	c.phase = phase_offset;
+	c.phase_stride = phase_stride;
+	c.super_samples = high_res ? (1u << (gs->sampling_rate_x_log2 + gs->sampling_rate_y_log2)) : 1u;
+	uint32_t scale = high_res ? 2u : 1u;
+	c.width = img_w * scale;
+	c.height = img_h * scale;
+	c.valid_width = valid_w * scale;
+	c.valid_height = valid_h * scale;
+	*width = c.width;
+	*height = c.height;
+	if (uint64_t(c.width) * c.height * 4u > dst_size || (!dst && c.width * c.height))
+		return PGS_ERROR_CAPACITY;
+	if (c.width == 0 || c.height == 0)
+		return PGS_OK;
+	return gs->ops->sample_circuit(gs->be, &c, dst);
 }
 
 int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *src)

@@ -1884,6 +1884,68 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_shade_kernel(const 
 }
 
 // ---------------------------------------------------------------------------
+// CRTC circuit read-out (sample_circuit.frag:98-148).  One thread per output
+// texel; a 2x2 high-resolution read-out averages the sample planes of the
+// quad position in float, in plane order, then converts to unorm8.
+__device__ __forceinline__ uint32_t circuit_payload(const uint8_t *vram, uint32_t psm, uint32_t addr, uint32_t plane)
+{
+	if (psm_is_16bit(psm))
+	{
+		uint16_t v = reinterpret_cast<const uint16_t *>(vram)[addr + plane * (VRAM_SIZE / 2)];
+		return rgba16_to_rgba32(v, 0, 0x0, 0xff);
+	}
+	uint32_t v = reinterpret_cast<const uint32_t *>(vram)[addr + plane * (VRAM_SIZE / 4)];
+	if (psm != PSMCT32)
+		v = (v & ~0xff000000u) | 0x80000000u;
+	return v;
+}
+
+__global__ void __launch_bounds__(256) circuit_kernel(pgs_circuit_params C, const uint8_t *vram, const float *unorm_lut,
+                                                      uint32_t *dst)
+{
+	const uint32_t x = blockIdx.x * 32u + (threadIdx.x & 31u), y = blockIdx.y * 8u + (threadIdx.x >> 5);
+	if (x >= C.width || y >= C.height)
+		return;
+	uint32_t out = 0;
+	if (x < C.valid_width && y < C.valid_height)
+	{
+		const uint32_t sx = C.super_samples >= 4 ? x >> 1 : x, sy = C.super_samples >= 4 ? y >> 1 : y;
+		const uint32_t cx = sx + C.dbx, cy = sy * C.phase_stride + C.dby + C.phase;
+		const uint32_t addr = swizzle_address(cx, cy, C.fbp * BLOCKS_PER_PAGE, C.fbw, C.psm);
+		bool resolve = false;
+		if (C.super_samples >= 4)
+		{
+			if (psm_is_16bit(C.psm))
+				resolve = reinterpret_cast<const uint16_t *>(vram)[addr + VRAM_SIZE / 2] == 0xffffu;
+			else
+			{
+				uint32_t ref = reinterpret_cast<const uint32_t *>(vram)[addr + VRAM_SIZE / 4];
+				resolve = C.psm != PSMCT32 ? (ref & 0xffffffu) == 0xffffffu : ref == 0xffffffffu;
+			}
+		}
+		if (!resolve)
+			out = circuit_payload(vram, C.psm, addr, 0);
+		else
+		{
+			const uint32_t n = C.super_samples / 4;
+			const uint32_t quad = C.super_samples != 8 ? (y & 1u) + (x & 1u) * 2u : (x & 1u) + (y & 1u) * 2u;
+			const uint32_t base = 2u + n * quad;
+			float v[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+			for (uint32_t i = 0; i < n; i++)
+			{
+				uint32_t c = circuit_payload(vram, C.psm, addr, base + i);
+				#pragma unroll
+				for (int k = 0; k < 4; k++)
+					v[k] = fadd(v[k], unorm_lut[(c >> (8 * k)) & 0xffu]);
+			}
+			const float fn = float(n);
+			out = pack_unorm(__fdiv_rn(v[0], fn), __fdiv_rn(v[1], fn), __fdiv_rn(v[2], fn), __fdiv_rn(v[3], fn));
+		}
+	}
+	dst[size_t(y) * C.width + x] = out;
+}
+
+// ---------------------------------------------------------------------------
 // K4: VRAM transfers.
 struct CopyParams
 {

@@ -637,3 +637,18 @@ def stream_c3(stream_id: int, num_primitives: int | None = None) -> Frame:
         done += m
     return Frame("c3_%02d" % stream_id, s.tobytes(), ss, True, n,
                  {"width": width, "height": height, "fbp": 0, "zbp": zbp, "fpsm": fpsm, "stream": stream_id})
+
+
+def dispfb_reg(fbp, fbw, psm, dbx=0, dby=0) -> int:
+    """DISPFB1/2 (gs/gs_registers.hpp:612-621)."""
+    return (fbp & 0x1FF) | ((fbw & 0x3F) << 9) | ((psm & 0x1F) << 15) | ((dbx & 0x7FF) << 32) | ((dby & 0x7FF) << 43)
+
+
+def display_reg(dx, dy, magh, magv, dw, dh) -> int:
+    """DISPLAY1/2 (gs/gs_registers.hpp:623-633); dw/dh are the register values (size - 1)."""
+    return ((dx & 0xFFF) | ((dy & 0x7FF) << 12) | ((magh & 0xF) << 23) | ((magv & 3) << 27) |
+            ((dw & 0xFFF) << 32) | ((dh & 0x7FF) << 44))
+
+
+def smode2_reg(interlace=0, ffmd=0) -> int:
+    return (interlace & 1) | ((ffmd & 1) << 1)

@@ -79,7 +79,8 @@ EXPORTED_SYMBOLS = [
     "pgs_batch_get_tuning", "pgs_batch_autotune", "pgs_batch_stream", "pgs_batch_launches_per_replay",
     "pgs_batch_synchronize",
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
-    "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
+    "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait",
+    "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
     "pgs_gs_set_super_sampling_rate",
 ]
 
@@ -133,6 +134,9 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.pgs_gs_read_vram.argtypes = [vp, u64, u64, vp]
     lib.pgs_gs_read_vram_async.argtypes = [vp, u64, u64, vp, C.POINTER(u64)]
     lib.pgs_gs_wait.argtypes = [vp, u64]
+    lib.pgs_gs_write_priv_register.argtypes = [vp, u32, u64]
+    lib.pgs_gs_read_priv_register.argtypes = [vp, u32, C.POINTER(u64)]
+    lib.pgs_gs_scanout_circuit.argtypes = [vp, u32, u32, u32, vp, u64, C.POINTER(u32), C.POINTER(u32)]
     lib.pgs_gs_write_vram.argtypes = [vp, u64, u64, vp]
     lib.pgs_gs_read_transfer_fifo.argtypes = [vp, vp, u32]
     lib.pgs_gs_consume_flush_stats.argtypes = [vp, C.POINTER(FlushStats)]
@@ -273,6 +277,30 @@ class GSInterface:
 
     def wait(self, ticket: int) -> None:
         check(self.lib.pgs_gs_wait(self.handle, ticket), "wait")
+
+    PRIV = {"PMODE": 0, "SMODE1": 1, "SMODE2": 2, "SRFSH": 3, "SYNCH1": 4, "SYNCH2": 5, "SYNCV": 6, "DISPFB1": 7,
+            "DISPLAY1": 8, "DISPFB2": 9, "DISPLAY2": 10, "EXTBUF": 11, "EXTDATA": 12, "EXTWRITE": 13, "BGCOLOR": 14}
+    SCANOUT_FORCE_PROGRESSIVE = 1
+    SCANOUT_HIGH_RESOLUTION = 2
+
+    def write_priv_register(self, reg, value: int) -> None:
+        index = self.PRIV[reg] if isinstance(reg, str) else int(reg)
+        check(self.lib.pgs_gs_write_priv_register(self.handle, index, value), "write_priv_register")
+
+    def read_priv_register(self, reg) -> int:
+        index = self.PRIV[reg] if isinstance(reg, str) else int(reg)
+        v = C.c_uint64()
+        check(self.lib.pgs_gs_read_priv_register(self.handle, index, C.byref(v)), "read_priv_register")
+        return int(v.value)
+
+    def scanout_circuit(self, circuit: int, phase: int = 0, flags: int = 0) -> np.ndarray:
+        """RGBA8 image (height, width, 4) of CRTC circuit 0 or 1."""
+        w, h = C.c_uint32(), C.c_uint32()
+        cap = 4096 * 4096 * 4
+        out = np.zeros(cap, dtype=np.uint8)
+        check(self.lib.pgs_gs_scanout_circuit(self.handle, circuit, phase, flags, out.ctypes.data, cap, C.byref(w),
+                                              C.byref(h)), "scanout_circuit")
+        return out[: w.value * h.value * 4].reshape(h.value, w.value, 4).copy()
 
     def write_vram(self, data, offset: int = 0) -> None:
         buf = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, bytes) else data)
