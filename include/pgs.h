@@ -343,6 +343,35 @@ uint32_t pgs_batch_launches_per_replay(pgs_batch *batch);
 int pgs_batch_synchronize(pgs_batch *batch);
 
 /* ------------------------------------------------------------------ */
+/* Learned anti-aliasing upscaler                                       */
+/* ------------------------------------------------------------------ */
+/* A 6-layer 3x3 convolutional network (32 channels, ReLU, residual over the
+ * input) that maps a 1x RGBA8 render to an estimate of the same scene's 16x
+ * SSAA resolve, with BF16 tensor-core forward and backward kernels (FP32
+ * accumulation) and an Adam step on FP32 master weights.  No counterpart in
+ * the reference.  Images are n x h x w x 4 bytes in device memory.  Parameters
+ * are a flat FP32 vector: per layer the weights [tap][out][in] then the biases;
+ * layer shapes 4->32, 32->32 (x4), 32->4. */
+void *pgs_upscaler_create(int device, int *status);
+void pgs_upscaler_destroy(void *upscaler);
+uint32_t pgs_upscaler_param_count(void *upscaler);
+/* Sets the weights and resets the optimiser state. */
+int pgs_upscaler_set_params(void *upscaler, const float *params, uint32_t count);
+int pgs_upscaler_get_params(void *upscaler, float *params, uint32_t count);
+/* Gradient of the last backward call (same layout as the parameters). */
+int pgs_upscaler_get_gradient(void *upscaler, float *grad, uint32_t count);
+/* Inference; d_out_rgba receives the clamped RGBA8 result. */
+int pgs_upscaler_forward(void *upscaler, const void *d_images, uint32_t n, uint32_t h, uint32_t w, void *d_out_rgba);
+/* Forward + mean-squared-error loss against d_targets + backward; *loss (may
+ * be NULL) receives the loss and waits for it. */
+int pgs_upscaler_backward(void *upscaler, const void *d_images, const void *d_targets, uint32_t n, uint32_t h,
+                          uint32_t w, double *loss);
+int pgs_upscaler_adam_step(void *upscaler, float learning_rate);
+/* The upscaler's cudaStream_t, as an opaque pointer. */
+void *pgs_upscaler_stream(void *upscaler);
+int pgs_upscaler_synchronize(void *upscaler);
+
+/* ------------------------------------------------------------------ */
 /* Allocation-free local->local VRAM copy                               */
 /* ------------------------------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device

@@ -58,27 +58,31 @@ def build_product(verbose: bool = False) -> Path:
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "pgs.h"]
     out = BUILD / LIB_NAME
     cu = CSRC / "backend.cu"
+    cu_up = CSRC / "upscaler.cu"
     cpp = CSRC / "frontend.cpp"
     o_cu = BUILD / "backend.o"
+    o_up = BUILD / "upscaler.o"
     o_cpp = BUILD / "frontend.o"
     stamp = BUILD / "defines.txt"
     defines = os.environ.get("PGS_NVCC_DEFINES", "")
-    if _newer(out, headers + [cu, cpp, Path(__file__)]) and stamp.exists() and stamp.read_text() == defines:
+    if _newer(out, headers + [cu, cu_up, cpp, Path(__file__)]) and stamp.exists() and stamp.read_text() == defines:
         return out
     common = ["-I", str(INCLUDE), "-I", str(CSRC)]
     jobs = [
         [nvcc, "-gencode", GENCODE, "-O3", "-lineinfo", "-fmad=false", "-std=c++17",
          "-Xcompiler", "-fPIC", *common, "-c", str(cu), "-o", str(o_cu)],
         ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", *common, "-c", str(cpp), "-o", str(o_cpp)],
+        [nvcc, "-gencode", GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *common, "-c", str(cu_up),
+         "-o", str(o_up)],
     ]
     if verbose:
         jobs[0].insert(1, "-Xptxas=-v")
     # Extra compiler definitions for tuning sweeps, e.g. PGS_NVCC_DEFINES="PGS_SHADE_OCC=3".
     for d in os.environ.get("PGS_NVCC_DEFINES", "").split():
         jobs[0].insert(1, "-D" + d)
-    with ThreadPoolExecutor(max_workers=2) as ex:
+    with ThreadPoolExecutor(max_workers=3) as ex:
         list(ex.map(_run, jobs))
-    _run([nvcc, "-shared", "-gencode", GENCODE, "-cudart", "static", str(o_cu), str(o_cpp), "-o", str(out)])
+    _run([nvcc, "-shared", "-gencode", GENCODE, "-cudart", "static", str(o_cu), str(o_up), str(o_cpp), "-o", str(out)])
     stamp.write_text(defines)
     return out
 

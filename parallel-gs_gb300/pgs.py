@@ -78,6 +78,9 @@ EXPORTED_SYMBOLS = [
     "pgs_batch_create", "pgs_batch_destroy", "pgs_batch_add", "pgs_batch_replay", "pgs_batch_set_tuning",
     "pgs_batch_get_tuning", "pgs_batch_autotune", "pgs_batch_stream", "pgs_batch_launches_per_replay",
     "pgs_batch_synchronize",
+    "pgs_upscaler_create", "pgs_upscaler_destroy", "pgs_upscaler_param_count", "pgs_upscaler_set_params",
+    "pgs_upscaler_get_params", "pgs_upscaler_get_gradient", "pgs_upscaler_forward", "pgs_upscaler_backward",
+    "pgs_upscaler_adam_step", "pgs_upscaler_stream", "pgs_upscaler_synchronize",
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
     "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait",
     "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
@@ -380,4 +383,88 @@ class Batch:
     def close(self) -> None:
         if self.handle:
             self.lib.pgs_batch_destroy(self.handle)
+            self.handle = None
+
+
+UPSCALER_SHAPES = [(4, 32), (32, 32), (32, 32), (32, 32), (32, 32), (32, 4)]
+
+
+def upscaler_init_params(seed: int = 0) -> np.ndarray:
+    """He-initialised flat parameter vector (per layer: weights [tap][out][in],
+    then biases); the last layer starts small so the network starts near the
+    identity through its residual."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for i, (cin, cout) in enumerate(UPSCALER_SHAPES):
+        std = np.sqrt(2.0 / (9 * cin)) * (0.1 if i == len(UPSCALER_SHAPES) - 1 else 1.0)
+        parts.append(rng.normal(0.0, std, size=9 * cout * cin).astype(np.float32))
+        parts.append(np.zeros(cout, dtype=np.float32))
+    return np.concatenate(parts)
+
+
+class Upscaler:
+    """BF16 tensor-core anti-aliasing network (pgs_upscaler_*).  Images are
+    device tensors of shape (n, h, w, 4), uint8, contiguous (e.g. torch)."""
+
+    def __init__(self, device: int = 0) -> None:
+        self.lib = load_library()
+        lib = self.lib
+        vp, u32 = C.c_void_p, C.c_uint32
+        lib.pgs_upscaler_create.argtypes = [C.c_int, C.POINTER(C.c_int)]
+        lib.pgs_upscaler_create.restype = vp
+        lib.pgs_upscaler_destroy.argtypes = [vp]
+        lib.pgs_upscaler_destroy.restype = None
+        lib.pgs_upscaler_param_count.argtypes = [vp]
+        lib.pgs_upscaler_param_count.restype = u32
+        for name in ("pgs_upscaler_set_params", "pgs_upscaler_get_params", "pgs_upscaler_get_gradient"):
+            getattr(lib, name).argtypes = [vp, vp, u32]
+        lib.pgs_upscaler_forward.argtypes = [vp, vp, u32, u32, u32, vp]
+        lib.pgs_upscaler_backward.argtypes = [vp, vp, vp, u32, u32, u32, C.POINTER(C.c_double)]
+        lib.pgs_upscaler_adam_step.argtypes = [vp, C.c_float]
+        lib.pgs_upscaler_stream.argtypes = [vp]
+        lib.pgs_upscaler_stream.restype = vp
+        lib.pgs_upscaler_synchronize.argtypes = [vp]
+        status = C.c_int(0)
+        self.handle = lib.pgs_upscaler_create(device, C.byref(status))
+        if not self.handle:
+            raise PGSError(status.value, "pgs_upscaler_create")
+        self.count = int(lib.pgs_upscaler_param_count(self.handle))
+
+    def set_params(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        check(self.lib.pgs_upscaler_set_params(self.handle, p.ctypes.data, p.size), "upscaler_set_params")
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.count, dtype=np.float32)
+        check(self.lib.pgs_upscaler_get_params(self.handle, out.ctypes.data, self.count), "upscaler_get_params")
+        return out
+
+    def gradient(self) -> np.ndarray:
+        out = np.empty(self.count, dtype=np.float32)
+        check(self.lib.pgs_upscaler_get_gradient(self.handle, out.ctypes.data, self.count), "upscaler_get_gradient")
+        return out
+
+    def forward(self, images, out) -> None:
+        n, h, w, _ = images.shape
+        check(self.lib.pgs_upscaler_forward(self.handle, images.data_ptr(), n, h, w, out.data_ptr()), "upscaler_forward")
+
+    def backward(self, images, targets, want_loss: bool = True):
+        n, h, w, _ = images.shape
+        loss = C.c_double(0.0)
+        check(self.lib.pgs_upscaler_backward(self.handle, images.data_ptr(), targets.data_ptr(), n, h, w,
+                                             C.byref(loss) if want_loss else None), "upscaler_backward")
+        return float(loss.value) if want_loss else None
+
+    def adam_step(self, lr: float) -> None:
+        check(self.lib.pgs_upscaler_adam_step(self.handle, lr), "upscaler_adam_step")
+
+    def stream(self) -> int:
+        return self.lib.pgs_upscaler_stream(self.handle)
+
+    def synchronize(self) -> None:
+        check(self.lib.pgs_upscaler_synchronize(self.handle), "upscaler_synchronize")
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.pgs_upscaler_destroy(self.handle)
             self.handle = None
