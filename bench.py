@@ -47,13 +47,16 @@ WORKLOADS = {
              "pass's framebuffer, 8x SSAA (2x4)", "gsgen.frame_c4(super_sampling=8)"),
     "c4x16": ("feedback 640x448 CT32/Z24, 100k tris (80% 1-16 px), 10 passes, 20% draws sample the previous "
               "pass's framebuffer, 16x SSAA (4x4)", "gsgen.frame_c4(super_sampling=16)"),
+    "c5": ("learned upscaler: 1x render + 6-layer BF16 conv network vs exact 16x SSAA (4x4), 640x448 scenes in "
+           "the textured+blended style (12.5k tris + 500 sprites), held-out seeds",
+           "gsgen.frame_c2(seed=20000, num_triangles=12500, num_sprites=500, super_sampling=16)"),
     "c3": ("batched replay: 64 seeded streams, 1k-200k prims (log-uniform), CT16/CT32 320x240-640x512, "
            "PSMT4/PSMT8/CT32 textures 64^2-512^2 with CLUTs, 1x/2x/4x SSAA per stream",
            "[gsgen.stream_c3(i) for i in range(64)]"),
 }
 # Texture and CLUT bytes uploaded per frame.
 TEXTURE_BYTES = {"c2": 8 * (256 * 256 + 16 * 16 * 4), "c1": 0, "c4x8": 4 * (128 * 128 + 16 * 16 * 4),
-                 "c4x16": 4 * (128 * 128 + 16 * 16 * 4), "c3": 0}
+                 "c4x16": 4 * (128 * 128 + 16 * 16 * 4), "c3": 0, "c5": 8 * (256 * 256 + 16 * 16 * 4)}
 
 
 def parse():
@@ -399,6 +402,131 @@ def run_c3(args, frames, rank, world, local):
         pg.barrier()
 
 
+def run_c5(args, rank, world, local):
+    """Learned upscaler against exact 16x SSAA: output pixels/s of each path
+    (device time of render + CRTC read-out, plus the network for the learned
+    path) and PSNR / maximum error over RGB on held-out seeds."""
+    import numpy as np
+    import torch
+    import pgs
+    import upscaler_train as T
+
+    torch.cuda.set_device(local)
+    dev = "cuda:%d" % local
+    up = pgs.Upscaler(local)
+    up.set_params(np.load(T.WEIGHTS))
+    # Quality on held-out seeds (bounded sample of the 500).
+    r = T.PairRenderer(local)
+    n_eval = 32 if args.quick else 100
+    ev_in, ev_tgt = T.build_dataset(r, range(T.EVAL_SEED0, T.EVAL_SEED0 + n_eval))
+    quality = T.evaluate(up, ev_in, ev_tgt)
+    r.close()
+    del ev_in, ev_tgt
+
+    # Throughput: one recorded scene replayed as CUDA graphs on each path.
+    frame = T.scene(T.EVAL_SEED0)
+    W, H = T.WIDTH, T.HEIGHT
+    paths = {}
+    for ss in (1, 16):
+        be = pgs.CudaBackend(local, max_samples_log2=0 if ss == 1 else 4, arena_mib=32)
+        gs = pgs.GSInterface(be, super_sampling=ss, ordered=True)
+        gs.write_vram(np.zeros(pgs.VRAM_SIZE, dtype=np.uint8))
+        be.begin_record()
+        gs.gif_transfer(0, frame.data)
+        gs.flush()
+        be.end_record()
+        paths[ss] = (be, gs)
+    img = torch.empty((1, H, W, 4), dtype=torch.uint8, device=dev)
+    out = torch.empty_like(img)
+    b1, b16 = paths[1][0], paths[16][0]
+    s1 = torch.cuda.ExternalStream(b1.stream(), device=local)
+    s16 = torch.cuda.ExternalStream(b16.stream(), device=local)
+    su = torch.cuda.ExternalStream(up.stream(), device=local)
+    flush_buf = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def learned_once():
+        b1.replay(1, reset_vram=True, use_graph=True)
+        b1.sample_circuit(img.data_ptr(), 0, W // 64, 0, W, H)
+        e = torch.cuda.Event()
+        e.record(s1)
+        su.wait_event(e)
+        up.forward(img, out)
+
+    def exact_once():
+        b16.replay(1, reset_vram=True, use_graph=True)
+        b16.sample_circuit(img.data_ptr(), 0, W // 64, 0, W, H)
+
+    def timed(fn, start_stream, end_stream):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        total = 0.0
+        net_ms = 0.0
+        for i in range(args.steps):
+            with torch.cuda.stream(start_stream):
+                flush_buf.fill_(i & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(start_stream)
+            fn()
+            b.record(end_stream)
+            torch.cuda.synchronize()
+            total += a.elapsed_time(b)
+        return total / args.steps
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    learned_ms = timed(learned_once, s1, su)
+    exact_ms = timed(exact_once, s16, s16)
+    # Network alone (the tensor-core part).
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    img_c = img.clone()
+    torch.cuda.synchronize()
+    a.record(su)
+    for _ in range(args.steps):
+        up.forward(img_c, out)
+    b.record(su)
+    torch.cuda.synchronize()
+    net_ms = a.elapsed_time(b) / args.steps
+    clk = clocks.stop()
+    for be, gs in paths.values():
+        gs.close()
+        be.close()
+    up.close()
+    if rank != 0:
+        return
+    px = W * H
+    flops = 2 * 9 * px * (4 * 32 + 4 * 32 * 32 + 32 * 4)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    peak = peaks.get("bf16_tflops", 1900.0)
+    achieved = flops / (net_ms / 1000.0) / 1e12
+    out_json = {
+        "metric": METRIC, "value": px / (learned_ms / 1000.0), "unit": "output px/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": learned_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)",
+        "data": "synthetic (seeded GS command streams)",
+        "config": {"workload": WORKLOADS["c5"][0], "width": W, "height": H, "eval_seeds": n_eval,
+                   "l2": "flushed (256 MiB write) between steps"},
+        "ssaa16_px_per_s": px / (exact_ms / 1000.0),
+        "speedup_vs_ssaa16": exact_ms / learned_ms,
+        "network_ms_per_frame": net_ms,
+        "psnr_db": quality["psnr_net_db"], "psnr_input_db": quality["psnr_input_db"],
+        "max_abs_err": quality["max_abs_err_net"], "max_abs_err_input": quality["max_abs_err_input"],
+        "clocks": clk,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "note": "network forward: 2*9*HW*(4*32 + 4*32*32 + 32*4) flops / its CUDA-event time; "
+                             "peak = measured bf16_tflops (of measured)"},
+        "cpu_baseline": None,
+        "e2e": None,
+    }
+    print(json.dumps(out_json))
+
+
 def cpu_baseline_sample_expr(expr: str, sample: str) -> dict:
     env = dict(os.environ, OMP_NUM_THREADS="1")
     code = ("import sys,time; sys.path.insert(0,%r); sys.path.insert(0,%r);"
@@ -419,6 +547,9 @@ def main():
     rank, world, local = dist_env()
     import gsgen  # noqa: E402
 
+    if args.workload == "c5" and args.impl != "reference":
+        run_c5(args, rank, world, local)
+        return
     frame = make_frame(args)
     if isinstance(frame, list) and args.impl != "reference":
         run_c3(args, frame, rank, world, local)

@@ -294,6 +294,10 @@ typedef struct pgs_backend_stats
 	uint64_t render_passes;
 } pgs_backend_stats;
 
+/* CRTC circuit read-out (pgs_circuit_params) of the backend's VRAM into device
+ * memory d_dst (width * height * 4 bytes), queued on the backend's stream. */
+int pgs_cuda_backend_sample_circuit(void *backend, const pgs_circuit_params *params, void *d_dst);
+
 /* Transfer and launch counters of the backend. */
 int pgs_cuda_backend_get_stats(void *backend, pgs_backend_stats *stats);
 /* When enabled, every replay records CUDA events (also inside the replay's

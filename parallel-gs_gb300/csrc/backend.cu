@@ -1016,6 +1016,19 @@ struct CudaBackend
 		return ticket && ticket < next_ticket ? PGS_OK : PGS_ERROR_INVALID_ARGUMENT;
 	}
 
+	int sample_circuit_device(const pgs_circuit_params &c, uint32_t *d_dst)
+	{
+		if (size_t(c.width) * c.height == 0)
+			return PGS_OK;
+		if (c.super_samples > 1 && 2u + c.super_samples > num_planes)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		dim3 grid((c.width + 31) / 32, (c.height + 7) / 8);
+		circuit_kernel<<<grid, 256, 0, stream>>>(c, d_vram, d_unorm_lut, d_dst);
+		launch_counter++;
+		CUDA_TRY(cudaGetLastError());
+		return PGS_OK;
+	}
+
 	int sample_circuit(const pgs_circuit_params &c, void *dst)
 	{
 		size_t bytes = size_t(c.width) * c.height * 4u;
@@ -1667,6 +1680,12 @@ int pgs_cuda_backend_replay(void *backend, uint32_t count, int reset_vram, int u
 	return backend ? B(backend)->replay(count, reset_vram != 0, use_graph != 0) : PGS_ERROR_INVALID_ARGUMENT;
 }
 void *pgs_cuda_backend_stream(void *backend) { return backend ? static_cast<void *>(B(backend)->stream) : nullptr; }
+int pgs_cuda_backend_sample_circuit(void *backend, const pgs_circuit_params *params, void *d_dst)
+{
+	if (!backend || !params || !d_dst)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	return B(backend)->sample_circuit_device(*params, static_cast<uint32_t *>(d_dst));
+}
 
 // ---------------------------------------------------------------------------
 // Batched replay.

@@ -60,6 +60,11 @@ class CudaBackendOptions(C.Structure):
                 ("arena_mib", C.c_uint32)]
 
 
+class CircuitParams(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("fbp", "fbw", "psm", "dbx", "dby", "phase", "phase_stride", "super_samples",
+                                          "width", "height", "valid_width", "valid_height")]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [("cta_threads", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("largest_first", C.c_uint32)]
 
@@ -74,7 +79,7 @@ EXPORTED_SYMBOLS = [
     "pgs_cuda_backend_create", "pgs_cuda_backend_begin_record", "pgs_cuda_backend_end_record",
     "pgs_cuda_backend_replay", "pgs_cuda_backend_stream", "pgs_cuda_backend_launches_per_replay",
     "pgs_cuda_backend_last_shade_ms", "pgs_cuda_backend_fragment_count", "pgs_cuda_backend_get_stats",
-    "pgs_cuda_backend_set_shade_timing",
+    "pgs_cuda_backend_set_shade_timing", "pgs_cuda_backend_sample_circuit",
     "pgs_batch_create", "pgs_batch_destroy", "pgs_batch_add", "pgs_batch_replay", "pgs_batch_set_tuning",
     "pgs_batch_get_tuning", "pgs_batch_autotune", "pgs_batch_stream", "pgs_batch_launches_per_replay",
     "pgs_batch_synchronize",
@@ -113,6 +118,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.pgs_cuda_backend_fragment_count.argtypes = [vp, C.POINTER(u64)]
     lib.pgs_cuda_backend_get_stats.argtypes = [vp, C.POINTER(BackendStats)]
     lib.pgs_cuda_backend_set_shade_timing.argtypes = [vp, i32]
+    lib.pgs_cuda_backend_sample_circuit.argtypes = [vp, C.POINTER(CircuitParams), vp]
     lib.pgs_batch_create.argtypes = [C.c_int, C.POINTER(i32)]
     lib.pgs_batch_create.restype = vp
     lib.pgs_batch_destroy.argtypes = [vp]
@@ -214,6 +220,12 @@ class CudaBackend(Backend):
 
     def stream(self) -> int:
         return self.lib.pgs_cuda_backend_stream(self.handle)
+
+    def sample_circuit(self, d_dst_ptr: int, fbp: int, fbw: int, psm: int, width: int, height: int) -> None:
+        """Progressive 1x read-out of a framebuffer rectangle at (0, 0) into device
+        memory (RGBA8), queued on the backend's stream."""
+        p = CircuitParams(fbp, fbw, psm, 0, 0, 0, 1, 1, width, height, width, height)
+        check(self.lib.pgs_cuda_backend_sample_circuit(self.handle, C.byref(p), d_dst_ptr), "sample_circuit")
 
     def launches_per_replay(self) -> int:
         return int(self.lib.pgs_cuda_backend_launches_per_replay(self.handle))
