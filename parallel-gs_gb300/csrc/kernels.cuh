@@ -867,11 +867,14 @@ __global__ void __launch_bounds__(256) texture_decode_kernel(PassParams P);
 
 // ---------------------------------------------------------------------------
 // K3: shading.
+// A pending or candidate shade of one sample.  Only what changes per sample
+// is kept; the state index, Z comparison, perspective and AA1 flags are
+// read back from the primitive's state word when needed.
 struct Request
 {
 	int coverage;
-	bool z_test, z_write, multisample, perspective, z_greater;
-	uint32_t z, state;
+	bool z_test, z_write;
+	uint32_t z;
 	float i, j;
 };
 
@@ -1040,7 +1043,8 @@ __device__ __forceinline__ float interp(float c0, float d1, float d2, float i, f
 	return fadd(fadd(c0, fmul(d1, i)), fmul(d2, j));
 }
 
-__device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r, uint32_t combiner, float cc[4])
+__device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r, bool perspective, uint32_t combiner,
+                               float cc[4])
 {
 	const PassParams &P = *C.P;
 	const TransformedAttr a = P.tattr[pi];
@@ -1060,7 +1064,7 @@ __device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r,
 		float s = interp(a.stqf0[0], a.stqf1[0], a.stqf2[0], r.i, r.j);
 		float t = interp(a.stqf0[1], a.stqf1[1], a.stqf2[1], r.i, r.j);
 		float q = interp(a.stqf0[2], a.stqf1[2], a.stqf2[2], r.i, r.j);
-		if (r.perspective && q != 1.0f)
+		if (perspective && q != 1.0f)
 		{
 			s = __fdiv_rn(s, q);
 			t = __fdiv_rn(t, q);
@@ -1068,7 +1072,7 @@ __device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r,
 		s = fminf(fmaxf(s, -2047.0f), 2047.0f);
 		t = fminf(fmaxf(t, -2047.0f), 2047.0f);
 		float tx[4];
-		sample_texture(P, P.prims[pi].tex, s, t, r.perspective, tx);
+		sample_texture(P, P.prims[pi].tex, s, t, perspective, tx);
 		if (mode == COMBINER_DECAL)
 		{
 			cc[0] = tx[0]; cc[1] = tx[1]; cc[2] = tx[2]; cc[3] = tcc ? tx[3] : col[3];
@@ -1127,15 +1131,17 @@ __device__ void shade_resolve(const ShadeCtx &C, SampleState &S)
 	const PassParams &P = *C.P;
 	const Request &r = S.pending;
 	uint32_t pi = S.pending_prim;
-	const pgs_state_vector sv = P.states[min(r.state, P.num_states - 1u)];
+	const uint32_t pst = P.prims[pi].state;
+	const pgs_state_vector sv = P.states[min(pst & STATE_INDEX_MASK, P.num_states - 1u)];
 	if (C.zs && r.z_test)
 	{
-		bool pass = r.z_greater ? r.z > S.depth : r.z >= S.depth;
+		bool pass = ((pst >> STATE_BIT_Z_TEST_GREATER) & 1) ? r.z > S.depth : r.z >= S.depth;
 		if (!pass)
 			return;
 	}
+	const bool multisample = (pst >> STATE_BIT_MULTISAMPLE) & 1;
 	float cc[4];
-	combined_color(C, pi, r, sv.combiner, cc);
+	combined_color(C, pi, r, (pst >> STATE_BIT_PERSPECTIVE) & 1, sv.combiner, cc);
 	float fbc[4];
 	#pragma unroll
 	for (int k = 0; k < 4; k++)
@@ -1150,10 +1156,10 @@ __device__ void shade_resolve(const ShadeCtx &C, SampleState &S)
 
 	if (P.has_aa1)
 	{
-		bool use_cov = (cc[3] == 128.0f || !abe) && r.multisample;
+		bool use_cov = (cc[3] == 128.0f || !abe) && multisample;
 		if (use_cov)
 			cc[3] = float(r.coverage);
-		if (r.multisample)
+		if (multisample)
 			abe = true;
 	}
 
@@ -1346,10 +1352,7 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 	opaque = (st >> STATE_BIT_OPAQUE) & 1;
 	r.z_test = C.zs && ((st >> STATE_BIT_Z_TEST) & 1);
 	r.z_write = C.zs && ((st >> STATE_BIT_Z_WRITE) & 1);
-	r.z_greater = C.zs && ((st >> STATE_BIT_Z_TEST_GREATER) & 1);
-	r.state = st & STATE_INDEX_MASK;
-	r.multisample = AA && ((st >> STATE_BIT_MULTISAMPLE) & 1);
-	r.perspective = (st >> STATE_BIT_PERSPECTIVE) & 1;
+	const bool multisample = AA && ((st >> STATE_BIT_MULTISAMPLE) & 1);
 	int32_t rx = S.hx, ry = S.hy;
 	if (C.ss && (st & (1u << STATE_BIT_SNAP_RASTER)))
 	{
@@ -1358,7 +1361,7 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 	}
 	float i = 0.0f, j = 0.0f;
 	if (AA)
-		r.coverage = evaluate_coverage(s, rx, ry, i, j, r.multisample, (st >> STATE_BIT_LINE) & 1, C.dim);
+		r.coverage = evaluate_coverage(s, rx, ry, i, j, multisample, (st >> STATE_BIT_LINE) & 1, C.dim);
 	else
 		r.coverage = coverage_plain(s, rx, ry, C.dim);
 	if (P.has_scanmsk)
@@ -1379,7 +1382,7 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 		i = fadd(fmul(__int2float_rn(idot3(s.b, qx, qy)), s.inv_area), s.error_i);
 		j = fadd(fmul(__int2float_rn(idot3(s.c, qx, qy)), s.inv_area), s.error_j);
 	}
-	if (C.zs && r.multisample && r.coverage < 0x80)
+	if (C.zs && multisample && r.coverage < 0x80)
 		r.z_write = false;
 	uint32_t z = s.z[0];
 	float zf = rintf(fadd(fmul(u2f(s.z[1]), i), fmul(u2f(s.z[2]), j)));
@@ -1433,18 +1436,16 @@ __device__ __forceinline__ void sample_offset(uint32_t s, uint32_t xl, uint32_t 
 
 // Processes one primitive for the calling warp: coverage, early depth,
 // deferred-shading bookkeeping (ubershader.comp:1694-1812).  Warp-uniform.
+// The 8x8 bins already hold only primitives that intersect the sub-tile
+// (primitive_intersects_tile); a second test against each warp's smaller
+// rectangle costs more than the coverage test it would skip, so coverage
+// alone decides.
 template <bool SS, bool AA>
-__device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi, SampleState &S, uint32_t &covered,
-                                                  int32_t wlo0, int32_t wlo1, int32_t whi0, int32_t whi1)
+__device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi, SampleState &S, uint32_t &covered)
 {
 	const PassParams &P = *C.P;
 	const PrimSetup s = P.setup[pi];
 	uint32_t st = P.prims[pi].state;
-	// Per-warp conservative test against the warp's pixel rectangle
-	// (primitive_intersects_tile, ubershader.comp:1646-1668).
-	bool ms_tri = AA && ((st >> STATE_BIT_MULTISAMPLE) & 1) && !((st >> STATE_BIT_LINE) & 1);
-	if (!intersects_tile(s, wlo0, wlo1, whi0, whi1, ms_tri))
-		return;
 	bool opaque, any_cov;
 	Request q = shade_early<AA>(C, s, st, S, opaque, any_cov);
 	if (!any_cov)
@@ -1455,7 +1456,7 @@ __device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi
 		if (q.z_test && !S.pending.z_write)
 		{
 			q.z_test = false;
-			bool zp = q.z_greater ? q.z > S.depth : q.z >= S.depth;
+			bool zp = ((st >> STATE_BIT_Z_TEST_GREATER) & 1) ? q.z > S.depth : q.z >= S.depth;
 			if (zp)
 			{
 				if (q.z_write && opaque)
@@ -1614,17 +1615,6 @@ __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInst
 	else
 		S.depth = 0;
 
-	// Pixel rectangle of this warp.
-	int32_t wlo0 = px, wlo1 = py, whi0 = px, whi1 = py;
-	#pragma unroll
-	for (int o = 16; o >= 1; o >>= 1)
-	{
-		wlo0 = min(wlo0, __shfl_xor_sync(0xffffffffu, wlo0, o));
-		wlo1 = min(wlo1, __shfl_xor_sync(0xffffffffu, wlo1, o));
-		whi0 = max(whi0, __shfl_xor_sync(0xffffffffu, whi0, o));
-		whi1 = max(whi1, __shfl_xor_sync(0xffffffffu, whi1, o));
-	}
-
 	// Walk the primitive list in ascending order: summary word -> mask words -> bits.
 	uint32_t covered = 0;
 	for (uint32_t sbase = 0; sbase < I.summary_words; sbase += 32u)
@@ -1648,7 +1638,7 @@ __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInst
 				{
 					int b = __ffs(m) - 1;
 					m &= m - 1u;
-					process_primitive<SS, AA>(C, prim_base + uint32_t(b), S, covered, wlo0, wlo1, whi0, whi1);
+					process_primitive<SS, AA>(C, prim_base + uint32_t(b), S, covered);
 				}
 			}
 		}
