@@ -373,6 +373,10 @@ int pgs_upscaler_backward(void *upscaler, const void *d_images, const void *d_ta
 int pgs_upscaler_adam_step(void *upscaler, float learning_rate);
 /* The upscaler's cudaStream_t, as an opaque pointer. */
 void *pgs_upscaler_stream(void *upscaler);
+/* Self-test of the tcgen05 tensor-core path: a 128x32x32 BF16 product from
+ * shared memory (mode 0: no-swizzle operand layout, 1: 64-byte swizzle) read
+ * back from tensor memory into out (128 x 32 floats, row-major). */
+int pgs_umma_selftest(int device, uint32_t mode, float *out);
 int pgs_upscaler_synchronize(void *upscaler);
 
 /* ------------------------------------------------------------------ */

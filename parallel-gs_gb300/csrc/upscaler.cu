@@ -16,6 +16,7 @@
 // the epilogue multiplies by the ReLU mask of the layer below), and a second
 // kernel the weight gradient (K = pixels).
 #include "pgs.h"
+#include "umma.cuh"
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -516,6 +517,91 @@ __global__ void __launch_bounds__(256) gather_grad_kernel(const float *padded_w,
 		grad[c_off.b[layer] + (i - nw)] = padded_b[i - nw];
 }
 
+
+// ---------------------------------------------------------------------------
+// Self-test of the tcgen05 building blocks: one CTA computes a 128x32 FP32
+// tile D = A (128x32 BF16) x B (32x32 BF16)^T with two K=16 MMAs from shared
+// memory in the given operand layout (0: no swizzle, 1: 64-byte swizzle) and
+// writes D from tensor memory.  Inputs are small multiples of 1/8 so every
+// product and sum is exact.
+__device__ __forceinline__ float probe_a(uint32_t r, uint32_t k) { return float(int((r * 7u + k * 3u) % 17u) - 8) / 8.0f; }
+__device__ __forceinline__ float probe_b(uint32_t n, uint32_t k) { return float(int((n * 5u + k * 11u) % 13u) - 6) / 4.0f; }
+
+__global__ void __launch_bounds__(128) umma_probe_kernel(uint32_t mode, float *out, uint32_t *err)
+{
+	using namespace pgs_umma;
+	extern __shared__ __align__(1024) uint8_t smem[];
+	uint8_t *sa = smem;               // 128 rows x 64 B = 8 KiB
+	uint8_t *sb = smem + 8192;        // 32 rows x 64 B = 2 KiB
+	__shared__ uint64_t bar;
+	__shared__ uint32_t tmem_slot;
+	const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+	const uint32_t LBO = 128, SBO = 512;
+	for (uint32_t i = tid; i < 128 * 32; i += 128)
+	{
+		uint32_t r = i / 32, k = i % 32;
+		uint32_t off = mode == 1 ? swz64_offset(r, k) : canon_offset(r, k, LBO, SBO);
+		*reinterpret_cast<__nv_bfloat16 *>(sa + off) = __float2bfloat16_rn(probe_a(r, k));
+	}
+	for (uint32_t i = tid; i < 32 * 32; i += 128)
+	{
+		uint32_t n = i / 32, k = i % 32;
+		uint32_t off = mode == 1 ? swz64_offset(n, k) : canon_offset(n, k, LBO, SBO);
+		*reinterpret_cast<__nv_bfloat16 *>(sb + off) = __float2bfloat16_rn(probe_b(n, k));
+	}
+	if (warp == 0)
+		tmem_alloc(&tmem_slot, 32);
+	if (tid == 0)
+	{
+		mbar_init(&bar, 1);
+		fence_barrier_init();
+	}
+	fence_proxy_async();
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tmem = tmem_slot;
+	if (tid == 0)
+	{
+		const uint32_t idesc = idesc_bf16_f32(128, 32);
+		for (uint32_t ks = 0; ks < 2; ks++)
+		{
+			uint64_t ad, bd;
+			if (mode == 1)
+			{
+				ad = smem_desc(smem_addr(sa) + ks * 32u, 16, SBO, LAYOUT_SWIZZLE_64B);
+				bd = smem_desc(smem_addr(sb) + ks * 32u, 16, SBO, LAYOUT_SWIZZLE_64B);
+			}
+			else
+			{
+				ad = smem_desc(smem_addr(sa) + ks * 2u * LBO, LBO, SBO, LAYOUT_NONE);
+				bd = smem_desc(smem_addr(sb) + ks * 2u * LBO, LBO, SBO, LAYOUT_NONE);
+			}
+			pgs_umma::mma_bf16(tmem, ad, bd, idesc, ks > 0);
+		}
+		mma_commit(&bar);
+	}
+	__syncwarp();
+	bool ok = mbar_wait(&bar, 0);
+	tc_fence_after();
+	if (!ok)
+	{
+		if (lane == 0)
+			atomicOr(err, 1u);
+	}
+	else
+	{
+		uint32_t v[32];
+		tmem_ld32(tmem + ((warp * 32u) << 16), v);
+		for (int c = 0; c < 32; c++)
+			out[(warp * 32 + lane) * 32 + c] = __uint_as_float(v[c]);
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	if (warp == 0)
+		tmem_dealloc(tmem, 32);
+}
 // ---------------------------------------------------------------------------
 struct Upscaler
 {
@@ -885,6 +971,34 @@ int pgs_upscaler_adam_step(void *up, float lr)
 	Upscaler *u = static_cast<Upscaler *>(up);
 	cudaSetDevice(u->device);
 	return u->step(lr);
+}
+
+int pgs_umma_selftest(int device, uint32_t mode, float *out_host)
+{
+	if (!out_host || mode > 1)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	UP_TRY(cudaSetDevice(device));
+	float *d_out = nullptr;
+	uint32_t *d_err = nullptr;
+	UP_TRY(cudaMalloc(&d_out, 128 * 32 * 4));
+	UP_TRY(cudaMalloc(&d_err, 4));
+	UP_TRY(cudaMemset(d_out, 0, 128 * 32 * 4));
+	UP_TRY(cudaMemset(d_err, 0, 4));
+	// Generous allocation: every address the descriptors can form stays inside.
+	const int smem = 96 * 1024;
+	UP_TRY(cudaFuncSetAttribute(pgs_up::umma_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+	pgs_up::umma_probe_kernel<<<1, 128, smem>>>(mode, d_out, d_err);
+	cudaError_t e = cudaDeviceSynchronize();
+	uint32_t err = 0;
+	if (e == cudaSuccess)
+		e = cudaMemcpy(out_host, d_out, 128 * 32 * 4, cudaMemcpyDeviceToHost);
+	if (e == cudaSuccess)
+		e = cudaMemcpy(&err, d_err, 4, cudaMemcpyDeviceToHost);
+	cudaFree(d_out);
+	cudaFree(d_err);
+	if (e != cudaSuccess)
+		return PGS_ERROR_CUDA;
+	return err ? PGS_ERROR_DEVICE_FLAG : PGS_OK;
 }
 
 void *pgs_upscaler_stream(void *up) { return up ? static_cast<void *>(static_cast<Upscaler *>(up)->stream) : nullptr; }

@@ -85,7 +85,7 @@ EXPORTED_SYMBOLS = [
     "pgs_batch_synchronize",
     "pgs_upscaler_create", "pgs_upscaler_destroy", "pgs_upscaler_param_count", "pgs_upscaler_set_params",
     "pgs_upscaler_get_params", "pgs_upscaler_get_gradient", "pgs_upscaler_forward", "pgs_upscaler_backward",
-    "pgs_upscaler_adam_step", "pgs_upscaler_stream", "pgs_upscaler_synchronize",
+    "pgs_upscaler_adam_step", "pgs_upscaler_stream", "pgs_upscaler_synchronize", "pgs_umma_selftest",
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
     "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait",
     "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
@@ -480,3 +480,12 @@ class Upscaler:
         if self.handle:
             self.lib.pgs_upscaler_destroy(self.handle)
             self.handle = None
+
+
+def umma_selftest(mode: int, device: int = 0) -> np.ndarray:
+    """128x32 result of the tcgen05 self-test (pgs_umma_selftest)."""
+    lib = load_library()
+    lib.pgs_umma_selftest.argtypes = [C.c_int, C.c_uint32, C.c_void_p]
+    out = np.zeros((128, 32), dtype=np.float32)
+    check(lib.pgs_umma_selftest(device, mode, out.ctypes.data), "umma_selftest")
+    return out
