@@ -18,6 +18,7 @@
 #include "pgs.h"
 #include "umma.cuh"
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -602,6 +603,204 @@ __global__ void __launch_bounds__(128) umma_probe_kernel(uint32_t mode, float *o
 	if (warp == 0)
 		tmem_dealloc(tmem, 32);
 }
+
+// ---------------------------------------------------------------------------
+// 32 -> 32 convolution on the 5th-generation tensor cores (inference and the
+// forward half of training).  Persistent CTAs (one per SM, 128 threads) own
+// tiles of 8 rows x 16 columns = 128 output pixels; per tile:
+//  - TMA loads three copies of the 10 x 16 x 32 input window, shifted by
+//    dx = 0, 1, 2 columns (zero fill outside the image), 64-byte swizzled, so
+//    that for every tap the 128 A rows are contiguous 64-byte rows;
+//  - one thread issues 9 taps x 2 K-steps of tcgen05.mma (M 128, N 32, K 16)
+//    into a 32-column FP32 accumulator in tensor memory;
+//  - four warps read their 32 accumulator lanes, add the bias, apply ReLU and
+//    store BF16 NHWC rows.
+// Two input stages: the loads of the next tile run under the MMAs and the
+// epilogue of the current one.  The layer's weights sit in shared memory
+// (9 x 32 x 32 BF16, 64-byte swizzled) for the whole launch.
+namespace tc
+{
+constexpr int ROWS = 8, COLS = 16, PIX = ROWS * COLS;
+constexpr int WIN_ROWS = ROWS + 2;
+constexpr uint32_t COPY_BYTES = WIN_ROWS * COLS * 64;      // 10240
+constexpr uint32_t STAGE_BYTES = 3 * COPY_BYTES;            // 30720
+constexpr uint32_t W_BYTES = 9 * 32 * 64;                   // 18432
+constexpr uint32_t SMEM_BYTES = 1024 + 2 * STAGE_BYTES + W_BYTES + 1024;
+}
+
+__global__ void __launch_bounds__(128, 1) conv32_tc_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                            const __nv_bfloat16 *wt, const float *bias,
+                                                            __nv_bfloat16 *out, int n, int h, int w, uint32_t *err)
+{
+	using namespace pgs_umma;
+	extern __shared__ uint8_t smem_dyn[];
+	// 1024-byte aligned base for the swizzled operands.
+	uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
+	uint8_t *stage_ptr[2] = { base, base + tc::STAGE_BYTES };
+	uint8_t *sw = base + 2 * tc::STAGE_BYTES;
+	__shared__ uint64_t full_bar[2], mma_bar;
+	__shared__ uint32_t tmem_slot;
+	__shared__ float s_bias[32];
+	__shared__ uint32_t s_abort;
+
+	const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+	const int tiles_x = (w + tc::COLS - 1) / tc::COLS, tiles_y = (h + tc::ROWS - 1) / tc::ROWS;
+	const int tiles = tiles_x * tiles_y * n;
+
+	for (uint32_t i = tid; i < 9 * 32 * 32; i += 128)
+	{
+		uint32_t tap = i / 1024, co = (i / 32) % 32, ci = i % 32;
+		*reinterpret_cast<__nv_bfloat16 *>(sw + tap * 2048u + swz64_offset(co, ci)) = wt[i];
+	}
+	if (tid < 32)
+		s_bias[tid] = bias[tid];
+	if (warp == 0)
+		tmem_alloc(&tmem_slot, 32);
+	if (tid == 0)
+	{
+		mbar_init(&full_bar[0], 1);
+		mbar_init(&full_bar[1], 1);
+		mbar_init(&mma_bar, 1);
+		fence_barrier_init();
+		s_abort = 0;
+	}
+	fence_proxy_async();
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tmem = tmem_slot;
+
+	auto tile_coords = [&](int tile, int &img, int &x0, int &y0) {
+		img = tile / (tiles_x * tiles_y);
+		int rem = tile % (tiles_x * tiles_y);
+		x0 = (rem % tiles_x) * tc::COLS;
+		y0 = (rem / tiles_x) * tc::ROWS;
+	};
+	auto issue_loads = [&](int tile, int s) {
+		int img, x0, y0;
+		tile_coords(tile, img, x0, y0);
+		mbar_expect_tx(&full_bar[s], tc::STAGE_BYTES);
+		for (int dx = 0; dx < 3; dx++)
+			tma_load_4d(stage_ptr[s] + dx * tc::COPY_BYTES, &tmap, &full_bar[s], 0, x0 - 1 + dx, y0 - 1, img);
+	};
+
+	const int first = blockIdx.x, step = gridDim.x;
+	if (tid == 0)
+	{
+		if (first < tiles)
+			issue_loads(first, 0);
+		if (first + step < tiles)
+			issue_loads(first + step, 1);
+	}
+	const uint32_t idesc = idesc_bf16_f32(128, 32);
+	int it = 0;
+	for (int tile = first; tile < tiles; tile += step, it++)
+	{
+		const int s = it & 1;
+		if (tid == 0)
+		{
+			if (!mbar_wait(&full_bar[s], (it >> 1) & 1))
+			{
+				atomicOr(err, 1u);
+				s_abort = 1;
+			}
+			else
+			{
+				tc_fence_after();
+				const uint32_t a0 = smem_addr(stage_ptr[s]), b0 = smem_addr(sw);
+				bool acc = false;
+				for (int tap = 0; tap < 9; tap++)
+				{
+					const int dy = tap / 3, dx = tap % 3;
+					for (int ks = 0; ks < 2; ks++)
+					{
+						uint64_t ad = smem_desc(a0 + dx * tc::COPY_BYTES + dy * tc::COLS * 64u + ks * 32u, 16, 512,
+						                        LAYOUT_SWIZZLE_64B);
+						uint64_t bd = smem_desc(b0 + tap * 2048u + ks * 32u, 16, 512, LAYOUT_SWIZZLE_64B);
+						pgs_umma::mma_bf16(tmem, ad, bd, idesc, acc);
+						acc = true;
+					}
+				}
+				mma_commit(&mma_bar);
+			}
+		}
+		__syncthreads();
+		if (s_abort)
+			break;
+		if (!mbar_wait(&mma_bar, it & 1))
+		{
+			if (lane == 0)
+				atomicOr(err, 2u);
+			s_abort = 1;
+		}
+		tc_fence_after();
+		__syncthreads();
+		if (s_abort)
+			break;
+		// The stage is free again: start the loads of the tile after next.
+		if (tid == 0 && tile + 2 * step < tiles)
+			issue_loads(tile + 2 * step, s);
+
+		// Epilogue: lane = pixel (warp * 32 + lane) of the tile.
+		uint32_t v[32];
+		tmem_ld32(tmem + ((warp * 32u) << 16), v);
+		int img, x0, y0;
+		tile_coords(tile, img, x0, y0);
+		const int pix = int(warp * 32u + lane);
+		const int gy = y0 + pix / tc::COLS, gx = x0 + pix % tc::COLS;
+		if (gx < w && gy < h)
+		{
+			uint32_t packed[16];
+			#pragma unroll
+			for (int c = 0; c < 16; c++)
+			{
+				float lo = fmaxf(__uint_as_float(v[2 * c]) + s_bias[2 * c], 0.0f);
+				float hi = fmaxf(__uint_as_float(v[2 * c + 1]) + s_bias[2 * c + 1], 0.0f);
+				packed[c] = pack_bf16x2(lo, hi);
+			}
+			uint4 *dst = reinterpret_cast<uint4 *>(out + ((size_t(img) * h + gy) * w + gx) * 32);
+			#pragma unroll
+			for (int q = 0; q < 4; q++)
+				dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+		}
+		// Every lane's accumulator read is complete before the next MMAs.
+		tc_fence_before();
+		__syncthreads();
+		tc_fence_after();
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	if (warp == 0)
+		tmem_dealloc(tmem, 32);
+}
+// Tensor map of an N x H x W x 32 BF16 activation tensor for conv32_tc_kernel:
+// boxes of 32 channels x 16 columns x 10 rows, 64-byte swizzle, zero fill.
+static int make_act_tmap(CUtensorMap *m, const void *ptr, int n, int h, int w)
+{
+	using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+	                            const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+	                            CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+	static Encode encode = nullptr;
+	if (!encode)
+	{
+		void *fn = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+		    q != cudaDriverEntryPointSuccess || !fn)
+			return PGS_ERROR_UNSUPPORTED;
+		encode = reinterpret_cast<Encode>(fn);
+	}
+	cuuint64_t dims[4] = { 32, cuuint64_t(w), cuuint64_t(h), cuuint64_t(n) };
+	cuuint64_t strides[3] = { 64, cuuint64_t(w) * 64, cuuint64_t(h) * w * 64 };
+	cuuint32_t box[4] = { 32, uint32_t(tc::COLS), uint32_t(tc::WIN_ROWS), 1 };
+	cuuint32_t estr[4] = { 1, 1, 1, 1 };
+	CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(ptr), dims, strides, box, estr,
+	                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+	                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	return r == CUDA_SUCCESS ? PGS_OK : PGS_ERROR_INVALID_ARGUMENT;
+}
+
 // ---------------------------------------------------------------------------
 struct Upscaler
 {
@@ -621,7 +820,10 @@ struct Upscaler
 	__nv_bfloat16 *d_gout = nullptr;            // last-layer output gradient, 16 channels
 	float *d_out = nullptr;                     // N x H x W x 4
 	double *d_loss = nullptr;
+	uint32_t *d_err = nullptr;
 	int sm_count = 0;
+	// 32 -> 32 layers on tcgen05 (true) or mma.sync (false).
+	bool use_tc = true;
 
 	int init(int dev)
 	{
@@ -655,6 +857,9 @@ struct Upscaler
 			UP_TRY(cudaMalloc(&bf.dgrad[l], size_t(9) * 32 * 32 * 2));
 		}
 		UP_TRY(cudaMalloc(&d_loss, sizeof(double)));
+		UP_TRY(cudaMalloc(&d_err, sizeof(uint32_t)));
+		UP_TRY(cudaMemset(d_err, 0, sizeof(uint32_t)));
+		UP_TRY(cudaFuncSetAttribute(conv32_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::SMEM_BYTES)));
 		return PGS_OK;
 	}
 
@@ -676,6 +881,7 @@ struct Upscaler
 		}
 		free_acts();
 		cudaFree(d_loss);
+		cudaFree(d_err);
 		if (stream)
 			cudaStreamDestroy(stream);
 	}
@@ -745,6 +951,20 @@ struct Upscaler
 		return PGS_OK;
 	}
 
+	// 32 -> 32 + bias + ReLU on tcgen05 (conv32_tc_kernel).
+	int conv_tc(const ConvArgs &a)
+	{
+		CUtensorMap m;
+		int r = make_act_tmap(&m, a.in, a.n, a.h, a.w);
+		if (r)
+			return r;
+		int tiles = ((a.w + tc::COLS - 1) / tc::COLS) * ((a.h + tc::ROWS - 1) / tc::ROWS) * a.n;
+		int grid = std::min(tiles, sm_count);
+		conv32_tc_kernel<<<grid, 128, tc::SMEM_BYTES, stream>>>(m, a.wt, a.bias, a.out, a.n, a.h, a.w, d_err);
+		UP_TRY(cudaGetLastError());
+		return PGS_OK;
+	}
+
 	template <int CIN, int COUT, int EPI>
 	int conv(const ConvArgs &a)
 	{
@@ -777,7 +997,12 @@ struct Upscaler
 			if (l < LAYERS - 1)
 			{
 				k.out = d_act[l];
-				r = l == 0 ? conv<16, 32, EPI_RELU>(k) : conv<32, 32, EPI_RELU>(k);
+				if (l == 0)
+					r = conv<16, 32, EPI_RELU>(k);
+				else if (use_tc)
+					r = conv_tc(k);
+				else
+					r = conv<32, 32, EPI_RELU>(k);
 			}
 			else
 			{
@@ -999,6 +1224,24 @@ int pgs_umma_selftest(int device, uint32_t mode, float *out_host)
 	if (e != cudaSuccess)
 		return PGS_ERROR_CUDA;
 	return err ? PGS_ERROR_DEVICE_FLAG : PGS_OK;
+}
+
+int pgs_upscaler_set_tensor_path(void *up, int tcgen05)
+{
+	if (!up)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	static_cast<Upscaler *>(up)->use_tc = tcgen05 != 0;
+	return PGS_OK;
+}
+
+int pgs_upscaler_get_error(void *up, uint32_t *flags)
+{
+	if (!up || !flags)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	Upscaler *u = static_cast<Upscaler *>(up);
+	UP_TRY(cudaMemcpyAsync(flags, u->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, u->stream));
+	UP_TRY(cudaStreamSynchronize(u->stream));
+	return *flags ? PGS_ERROR_DEVICE_FLAG : PGS_OK;
 }
 
 void *pgs_upscaler_stream(void *up) { return up ? static_cast<void *>(static_cast<Upscaler *>(up)->stream) : nullptr; }

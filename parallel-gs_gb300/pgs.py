@@ -86,6 +86,7 @@ EXPORTED_SYMBOLS = [
     "pgs_upscaler_create", "pgs_upscaler_destroy", "pgs_upscaler_param_count", "pgs_upscaler_set_params",
     "pgs_upscaler_get_params", "pgs_upscaler_get_gradient", "pgs_upscaler_forward", "pgs_upscaler_backward",
     "pgs_upscaler_adam_step", "pgs_upscaler_stream", "pgs_upscaler_synchronize", "pgs_umma_selftest",
+    "pgs_upscaler_set_tensor_path", "pgs_upscaler_get_error",
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
     "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait",
     "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
@@ -436,6 +437,8 @@ class Upscaler:
         lib.pgs_upscaler_stream.argtypes = [vp]
         lib.pgs_upscaler_stream.restype = vp
         lib.pgs_upscaler_synchronize.argtypes = [vp]
+        lib.pgs_upscaler_set_tensor_path.argtypes = [vp, C.c_int]
+        lib.pgs_upscaler_get_error.argtypes = [vp, C.POINTER(u32)]
         status = C.c_int(0)
         self.handle = lib.pgs_upscaler_create(device, C.byref(status))
         if not self.handle:
@@ -466,6 +469,15 @@ class Upscaler:
         check(self.lib.pgs_upscaler_backward(self.handle, images.data_ptr(), targets.data_ptr(), n, h, w,
                                              C.byref(loss) if want_loss else None), "upscaler_backward")
         return float(loss.value) if want_loss else None
+
+    def set_tensor_path(self, tcgen05: bool) -> None:
+        """32->32 layers on tcgen05 (default) or on the mma.sync path."""
+        check(self.lib.pgs_upscaler_set_tensor_path(self.handle, int(tcgen05)), "upscaler_set_tensor_path")
+
+    def error_flags(self) -> int:
+        v = C.c_uint32(0)
+        self.lib.pgs_upscaler_get_error(self.handle, C.byref(v))
+        return int(v.value)
 
     def adam_step(self, lr: float) -> None:
         check(self.lib.pgs_upscaler_adam_step(self.handle, lr), "upscaler_adam_step")
