@@ -371,8 +371,9 @@ int pgs_upscaler_forward(void *upscaler, const void *d_images, uint32_t n, uint3
 int pgs_upscaler_backward(void *upscaler, const void *d_images, const void *d_targets, uint32_t n, uint32_t h,
                           uint32_t w, double *loss);
 int pgs_upscaler_adam_step(void *upscaler, float learning_rate);
-/* 32->32 layers on tcgen05 with TMA-fed operands and TMEM accumulators
- * (non-zero, the default) or on the mma.sync path (zero). */
+/* 32->32 layers on tcgen05 with TMA-fed operands and TMEM accumulators, with
+ * 1 or 2 persistent CTAs per SM (2 is the default), or on the mma.sync path
+ * (0). */
 int pgs_upscaler_set_tensor_path(void *upscaler, int tcgen05);
 /* Sticky error flags of the tcgen05 kernels (a bounded wait that ran out). */
 int pgs_upscaler_get_error(void *upscaler, uint32_t *flags);

@@ -88,6 +88,30 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 	return false;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Bounded wait that also gives up as soon as *abort is set by another warp.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t *bar, uint32_t parity, volatile uint32_t *abort)
+{
+	const uint32_t a = smem_addr(bar);
+	for (uint32_t i = 0; i < WAIT_LIMIT; i++)
+	{
+		uint32_t done;
+		asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+		             : "=r"(done)
+		             : "r"(a), "r"(parity)
+		             : "memory");
+		if (done)
+			return true;
+		if ((i & 255u) == 255u && *abort)
+			return false;
+	}
+	return false;
+}
+
 // TMEM allocation by one full warp; the base address is written to *slot.
 __device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t cols)
 {

@@ -606,61 +606,73 @@ __global__ void __launch_bounds__(128) umma_probe_kernel(uint32_t mode, float *o
 
 // ---------------------------------------------------------------------------
 // 32 -> 32 convolution on the 5th-generation tensor cores (inference and the
-// forward half of training).  Persistent CTAs (one per SM, 128 threads) own
-// tiles of 8 rows x 16 columns = 128 output pixels; per tile:
-//  - TMA loads three copies of the 10 x 16 x 32 input window, shifted by
-//    dx = 0, 1, 2 columns (zero fill outside the image), 64-byte swizzled, so
-//    that for every tap the 128 A rows are contiguous 64-byte rows;
-//  - one thread issues 9 taps x 2 K-steps of tcgen05.mma (M 128, N 32, K 16)
-//    into a 32-column FP32 accumulator in tensor memory;
-//  - four warps read their 32 accumulator lanes, add the bias, apply ReLU and
-//    store BF16 NHWC rows.
-// Two input stages: the loads of the next tile run under the MMAs and the
-// epilogue of the current one.  The layer's weights sit in shared memory
-// (9 x 32 x 32 BF16, 64-byte swizzled) for the whole launch.
+// forward half of training).  Persistent CTAs (one per SM) own tiles of
+// 8 rows x 16 columns = 128 output pixels.  Warp-specialised pipeline:
+//  - warp 0, one lane: TMA loads of three copies of each tile's 10 x 16 x 32
+//    input window, shifted by dx = 0, 1, 2 columns (zero fill outside the
+//    image, 64-byte swizzle), so that for every tap the 128 A rows are
+//    contiguous; three input stages;
+//  - the same lane issues 9 taps x 2 K-steps of tcgen05.mma (M 128, N 32,
+//    K 16) into one of two 32-column FP32 accumulators in tensor memory and
+//    commits to the stage's "empty" and the accumulator's "full" barriers;
+//  - warps 1-4 (one per TMEM lane quarter) read the accumulator, release it,
+//    add the bias, apply ReLU and store BF16 NHWC rows, overlapping the MMAs
+//    of the next tile.
+// The layer's weights sit in shared memory (9 x 32 x 32 BF16, 64-byte
+// swizzled) for the whole launch.  Every wait is bounded and gives up when
+// another warp has given up.
 namespace tc
 {
 constexpr int ROWS = 8, COLS = 16, PIX = ROWS * COLS;
 constexpr int WIN_ROWS = ROWS + 2;
+constexpr int STAGES = 3, ACCS = 2;
 constexpr uint32_t COPY_BYTES = WIN_ROWS * COLS * 64;      // 10240
 constexpr uint32_t STAGE_BYTES = 3 * COPY_BYTES;            // 30720
 constexpr uint32_t W_BYTES = 9 * 32 * 64;                   // 18432
-constexpr uint32_t SMEM_BYTES = 1024 + 2 * STAGE_BYTES + W_BYTES + 1024;
+constexpr uint32_t SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + W_BYTES + 1024;
+constexpr int THREADS = 160;
 }
 
-__global__ void __launch_bounds__(128, 1) conv32_tc_kernel(const __grid_constant__ CUtensorMap tmap,
-                                                            const __nv_bfloat16 *wt, const float *bias,
-                                                            __nv_bfloat16 *out, int n, int h, int w, uint32_t *err)
+__global__ void __launch_bounds__(tc::THREADS, 2) conv32_tc_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                                    const __nv_bfloat16 *wt, const float *bias,
+                                                                    __nv_bfloat16 *out, int n, int h, int w, uint32_t *err)
 {
 	using namespace pgs_umma;
 	extern __shared__ uint8_t smem_dyn[];
-	// 1024-byte aligned base for the swizzled operands.
 	uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
-	uint8_t *stage_ptr[2] = { base, base + tc::STAGE_BYTES };
-	uint8_t *sw = base + 2 * tc::STAGE_BYTES;
-	__shared__ uint64_t full_bar[2], mma_bar;
+	uint8_t *sw = base + tc::STAGES * tc::STAGE_BYTES;
+	__shared__ uint64_t full_bar[tc::STAGES], empty_bar[tc::STAGES], acc_full[tc::ACCS], acc_empty[tc::ACCS];
 	__shared__ uint32_t tmem_slot;
 	__shared__ float s_bias[32];
-	__shared__ uint32_t s_abort;
+	__shared__ volatile uint32_t s_abort;
 
 	const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
 	const int tiles_x = (w + tc::COLS - 1) / tc::COLS, tiles_y = (h + tc::ROWS - 1) / tc::ROWS;
 	const int tiles = tiles_x * tiles_y * n;
 
-	for (uint32_t i = tid; i < 9 * 32 * 32; i += 128)
+	// Weights: 16-byte chunks of 8 input channels into their swizzled slots.
+	for (uint32_t i = tid; i < 9 * 32 * 4; i += tc::THREADS)
 	{
-		uint32_t tap = i / 1024, co = (i / 32) % 32, ci = i % 32;
-		*reinterpret_cast<__nv_bfloat16 *>(sw + tap * 2048u + swz64_offset(co, ci)) = wt[i];
+		uint32_t tap = i / 128, co = (i / 4) % 32, ci = (i % 4) * 8;
+		*reinterpret_cast<uint4 *>(sw + tap * 2048u + swz64_offset(co, ci)) =
+		    *reinterpret_cast<const uint4 *>(wt + (tap * 32u + co) * 32u + ci);
 	}
 	if (tid < 32)
 		s_bias[tid] = bias[tid];
 	if (warp == 0)
-		tmem_alloc(&tmem_slot, 32);
+		tmem_alloc(&tmem_slot, 64);
 	if (tid == 0)
 	{
-		mbar_init(&full_bar[0], 1);
-		mbar_init(&full_bar[1], 1);
-		mbar_init(&mma_bar, 1);
+		for (int s = 0; s < tc::STAGES; s++)
+		{
+			mbar_init(&full_bar[s], 1);
+			mbar_init(&empty_bar[s], 1);
+		}
+		for (int a = 0; a < tc::ACCS; a++)
+		{
+			mbar_init(&acc_full[a], 1);
+			mbar_init(&acc_empty[a], 4);
+		}
 		fence_barrier_init();
 		s_abort = 0;
 	}
@@ -676,38 +688,47 @@ __global__ void __launch_bounds__(128, 1) conv32_tc_kernel(const __grid_constant
 		x0 = (rem % tiles_x) * tc::COLS;
 		y0 = (rem / tiles_x) * tc::ROWS;
 	};
-	auto issue_loads = [&](int tile, int s) {
-		int img, x0, y0;
-		tile_coords(tile, img, x0, y0);
-		mbar_expect_tx(&full_bar[s], tc::STAGE_BYTES);
-		for (int dx = 0; dx < 3; dx++)
-			tma_load_4d(stage_ptr[s] + dx * tc::COPY_BYTES, &tmap, &full_bar[s], 0, x0 - 1 + dx, y0 - 1, img);
-	};
-
 	const int first = blockIdx.x, step = gridDim.x;
-	if (tid == 0)
+	const int mine = first < tiles ? (tiles - 1 - first) / step + 1 : 0;
+
+	if (warp == 0)
 	{
-		if (first < tiles)
-			issue_loads(first, 0);
-		if (first + step < tiles)
-			issue_loads(first + step, 1);
-	}
-	const uint32_t idesc = idesc_bf16_f32(128, 32);
-	int it = 0;
-	for (int tile = first; tile < tiles; tile += step, it++)
-	{
-		const int s = it & 1;
-		if (tid == 0)
+		if (lane == 0)
 		{
-			if (!mbar_wait(&full_bar[s], (it >> 1) & 1))
+			const uint32_t idesc = idesc_bf16_f32(128, 32);
+			int loaded = 0;
+			for (int i = 0; i < mine && !s_abort; i++)
 			{
-				atomicOr(err, 1u);
-				s_abort = 1;
-			}
-			else
-			{
+				// Keep up to STAGES tiles of input in flight.
+				for (; loaded < mine && loaded < i + tc::STAGES; loaded++)
+				{
+					const int s = loaded % tc::STAGES;
+					if (loaded >= tc::STAGES && !mbar_wait_or_abort(&empty_bar[s], ((loaded / tc::STAGES) - 1) & 1, &s_abort))
+					{
+						atomicOr(err, 1u);
+						s_abort = 1;
+						break;
+					}
+					int img, x0, y0;
+					tile_coords(first + loaded * step, img, x0, y0);
+					uint8_t *dst = base + s * tc::STAGE_BYTES;
+					mbar_expect_tx(&full_bar[s], tc::STAGE_BYTES);
+					for (int dx = 0; dx < 3; dx++)
+						tma_load_4d(dst + dx * tc::COPY_BYTES, &tmap, &full_bar[s], 0, x0 - 1 + dx, y0 - 1, img);
+				}
+				if (s_abort)
+					break;
+				const int s = i % tc::STAGES, a = i % tc::ACCS;
+				if (!mbar_wait_or_abort(&full_bar[s], (i / tc::STAGES) & 1, &s_abort) ||
+				    (i >= tc::ACCS && !mbar_wait_or_abort(&acc_empty[a], ((i / tc::ACCS) - 1) & 1, &s_abort)))
+				{
+					atomicOr(err, 2u);
+					s_abort = 1;
+					break;
+				}
 				tc_fence_after();
-				const uint32_t a0 = smem_addr(stage_ptr[s]), b0 = smem_addr(sw);
+				const uint32_t a0 = smem_addr(base + s * tc::STAGE_BYTES), b0 = smem_addr(sw);
+				const uint32_t d = tmem + uint32_t(a) * 32u;
 				bool acc = false;
 				for (int tap = 0; tap < 9; tap++)
 				{
@@ -717,63 +738,66 @@ __global__ void __launch_bounds__(128, 1) conv32_tc_kernel(const __grid_constant
 						uint64_t ad = smem_desc(a0 + dx * tc::COPY_BYTES + dy * tc::COLS * 64u + ks * 32u, 16, 512,
 						                        LAYOUT_SWIZZLE_64B);
 						uint64_t bd = smem_desc(b0 + tap * 2048u + ks * 32u, 16, 512, LAYOUT_SWIZZLE_64B);
-						pgs_umma::mma_bf16(tmem, ad, bd, idesc, acc);
+						pgs_umma::mma_bf16(d, ad, bd, idesc, acc);
 						acc = true;
 					}
 				}
-				mma_commit(&mma_bar);
+				mma_commit(&empty_bar[s]);
+				mma_commit(&acc_full[a]);
 			}
 		}
-		__syncthreads();
-		if (s_abort)
-			break;
-		if (!mbar_wait(&mma_bar, it & 1))
+		__syncwarp();
+	}
+	else
+	{
+		// Epilogue warps: warp w reads TMEM lanes 32 * (w % 4) .. + 31.
+		const uint32_t quarter = warp & 3u;
+		for (int i = 0; i < mine; i++)
 		{
-			if (lane == 0)
-				atomicOr(err, 2u);
-			s_abort = 1;
-		}
-		tc_fence_after();
-		__syncthreads();
-		if (s_abort)
-			break;
-		// The stage is free again: start the loads of the tile after next.
-		if (tid == 0 && tile + 2 * step < tiles)
-			issue_loads(tile + 2 * step, s);
-
-		// Epilogue: lane = pixel (warp * 32 + lane) of the tile.
-		uint32_t v[32];
-		tmem_ld32(tmem + ((warp * 32u) << 16), v);
-		int img, x0, y0;
-		tile_coords(tile, img, x0, y0);
-		const int pix = int(warp * 32u + lane);
-		const int gy = y0 + pix / tc::COLS, gx = x0 + pix % tc::COLS;
-		if (gx < w && gy < h)
-		{
-			uint32_t packed[16];
-			#pragma unroll
-			for (int c = 0; c < 16; c++)
+			const int a = i % tc::ACCS;
+			bool ok = mbar_wait_or_abort(&acc_full[a], (i / tc::ACCS) & 1, &s_abort);
+			if (!__all_sync(0xffffffffu, ok))
 			{
-				float lo = fmaxf(__uint_as_float(v[2 * c]) + s_bias[2 * c], 0.0f);
-				float hi = fmaxf(__uint_as_float(v[2 * c + 1]) + s_bias[2 * c + 1], 0.0f);
-				packed[c] = pack_bf16x2(lo, hi);
+				if (lane == 0)
+					atomicOr(err, 4u);
+				s_abort = 1;
+				break;
 			}
-			uint4 *dst = reinterpret_cast<uint4 *>(out + ((size_t(img) * h + gy) * w + gx) * 32);
-			#pragma unroll
-			for (int q = 0; q < 4; q++)
-				dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+			tc_fence_after();
+			uint32_t v[32];
+			tmem_ld32(tmem + uint32_t(a) * 32u + ((quarter * 32u) << 16), v);
+			tc_fence_before();
+			__syncwarp();
+			if (lane == 0)
+				mbar_arrive(&acc_empty[a]);
+			int img, x0, y0;
+			tile_coords(first + i * step, img, x0, y0);
+			const int pix = int(quarter * 32u + lane);
+			const int gy = y0 + pix / tc::COLS, gx = x0 + pix % tc::COLS;
+			if (gx < w && gy < h)
+			{
+				uint32_t packed[16];
+				#pragma unroll
+				for (int c = 0; c < 16; c++)
+				{
+					float lo = fmaxf(__uint_as_float(v[2 * c]) + s_bias[2 * c], 0.0f);
+					float hi = fmaxf(__uint_as_float(v[2 * c + 1]) + s_bias[2 * c + 1], 0.0f);
+					packed[c] = pack_bf16x2(lo, hi);
+				}
+				uint4 *dst = reinterpret_cast<uint4 *>(out + ((size_t(img) * h + gy) * w + gx) * 32);
+				#pragma unroll
+				for (int q = 0; q < 4; q++)
+					dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+			}
 		}
-		// Every lane's accumulator read is complete before the next MMAs.
-		tc_fence_before();
-		__syncthreads();
-		tc_fence_after();
 	}
 	tc_fence_before();
 	__syncthreads();
 	tc_fence_after();
 	if (warp == 0)
-		tmem_dealloc(tmem, 32);
+		tmem_dealloc(tmem, 64);
 }
+
 // Tensor map of an N x H x W x 32 BF16 activation tensor for conv32_tc_kernel:
 // boxes of 32 channels x 16 columns x 10 rows, 64-byte swizzle, zero fill.
 static int make_act_tmap(CUtensorMap *m, const void *ptr, int n, int h, int w)
@@ -822,8 +846,38 @@ struct Upscaler
 	double *d_loss = nullptr;
 	uint32_t *d_err = nullptr;
 	int sm_count = 0;
-	// 32 -> 32 layers on tcgen05 (true) or mma.sync (false).
-	bool use_tc = true;
+	// 32 -> 32 layers: 0 = mma.sync, otherwise tcgen05 with this many
+	// persistent CTAs per SM.
+	int use_tc = 2;
+	// Tensor maps of the activation buffers (encoded once per buffer and shape).
+	struct TmapEntry
+	{
+		const void *ptr;
+		int n, h, w;
+		CUtensorMap map;
+	};
+	TmapEntry tmaps[8] = {};
+	int tmap_count = 0;
+
+	int act_tmap(const void *ptr, int n, int h, int w, CUtensorMap *&out)
+	{
+		for (int i = 0; i < tmap_count; i++)
+			if (tmaps[i].ptr == ptr && tmaps[i].n == n && tmaps[i].h == h && tmaps[i].w == w)
+			{
+				out = &tmaps[i].map;
+				return PGS_OK;
+			}
+		TmapEntry &e = tmaps[tmap_count < 8 ? tmap_count++ : 7];
+		int r = make_act_tmap(&e.map, ptr, n, h, w);
+		if (r)
+			return r;
+		e.ptr = ptr;
+		e.n = n;
+		e.h = h;
+		e.w = w;
+		out = &e.map;
+		return PGS_OK;
+	}
 
 	int init(int dev)
 	{
@@ -908,6 +962,7 @@ struct Upscaler
 			return PGS_OK;
 		UP_TRY(cudaStreamSynchronize(stream));
 		free_acts();
+		tmap_count = 0;
 		UP_TRY(cudaMalloc(&d_x0, pixels * 16 * 2));
 		for (auto &a : d_act)
 			UP_TRY(cudaMalloc(&a, pixels * 32 * 2));
@@ -954,13 +1009,13 @@ struct Upscaler
 	// 32 -> 32 + bias + ReLU on tcgen05 (conv32_tc_kernel).
 	int conv_tc(const ConvArgs &a)
 	{
-		CUtensorMap m;
-		int r = make_act_tmap(&m, a.in, a.n, a.h, a.w);
+		CUtensorMap *m = nullptr;
+		int r = act_tmap(a.in, a.n, a.h, a.w, m);
 		if (r)
 			return r;
 		int tiles = ((a.w + tc::COLS - 1) / tc::COLS) * ((a.h + tc::ROWS - 1) / tc::ROWS) * a.n;
-		int grid = std::min(tiles, sm_count);
-		conv32_tc_kernel<<<grid, 128, tc::SMEM_BYTES, stream>>>(m, a.wt, a.bias, a.out, a.n, a.h, a.w, d_err);
+		int grid = std::min(tiles, sm_count * use_tc);
+		conv32_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, stream>>>(*m, a.wt, a.bias, a.out, a.n, a.h, a.w, d_err);
 		UP_TRY(cudaGetLastError());
 		return PGS_OK;
 	}
@@ -1230,7 +1285,9 @@ int pgs_upscaler_set_tensor_path(void *up, int tcgen05)
 {
 	if (!up)
 		return PGS_ERROR_INVALID_ARGUMENT;
-	static_cast<Upscaler *>(up)->use_tc = tcgen05 != 0;
+	if (tcgen05 < 0 || tcgen05 > 2)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	static_cast<Upscaler *>(up)->use_tc = tcgen05;
 	return PGS_OK;
 }
 

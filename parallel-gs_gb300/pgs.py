@@ -470,9 +470,11 @@ class Upscaler:
                                              C.byref(loss) if want_loss else None), "upscaler_backward")
         return float(loss.value) if want_loss else None
 
-    def set_tensor_path(self, tcgen05: bool) -> None:
-        """32->32 layers on tcgen05 (default) or on the mma.sync path."""
-        check(self.lib.pgs_upscaler_set_tensor_path(self.handle, int(tcgen05)), "upscaler_set_tensor_path")
+    def set_tensor_path(self, tcgen05) -> None:
+        """32->32 layers on tcgen05 (True or 2: two persistent CTAs per SM, 1: one)
+        or on the mma.sync path (False / 0)."""
+        mode = 2 if tcgen05 is True else int(tcgen05)
+        check(self.lib.pgs_upscaler_set_tensor_path(self.handle, mode), "upscaler_set_tensor_path")
 
     def error_flags(self) -> int:
         v = C.c_uint32(0)
