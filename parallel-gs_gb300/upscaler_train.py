@@ -153,6 +153,8 @@ def main() -> None:
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default="gpurun_out/upscaler")
+    ap.add_argument("--tensor-path", type=int, default=2,
+                    help="32->32 layers: 0 mma.sync, 1 or 2 tcgen05 with that many persistent CTAs per SM")
     args = ap.parse_args()
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
@@ -172,6 +174,7 @@ def main() -> None:
     t_data = time.perf_counter() - t0
     r.close()
     up = pgs.Upscaler(0)
+    up.set_tensor_path(args.tensor_path)
     up.set_params(pgs.upscaler_init_params(0))
     before = evaluate(up, ev_in[:64], ev_tgt[:64])
     log("before training: %s" % json.dumps(before))
