@@ -140,6 +140,18 @@ def replica_throughput(steps: int, world: int, max_ms: float) -> float:
     return world * steps / (max_ms / 1000.0)
 
 
+def profiled_traffic(summary: str):
+    """DRAM bytes (read + write) per launch of the dominant kernel from the ncu
+    summary committed under profiles/ (its `traffic_bytes_per_launch:` line)."""
+    try:
+        for line in (ROOT / "profiles" / summary).read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":")[1])
+    except Exception:
+        pass
+    return None
+
+
 def algorithmic_bytes(frame, ss: int) -> dict:
     """Bytes a frame must move at minimum: prim records in,
     setup records written and read, FB/Z read+write per pixel for plane 0,
@@ -689,7 +701,8 @@ def main():
         "gpu_launches": launches * args.steps,
         "clocks": clk,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-                     "frac": achieved / peak_gbs, "traffic": None,
+                     "frac": achieved / peak_gbs,
+                     "traffic": profiled_traffic("shade_kernel_c2.md") if args.workload == "c2" else None,
                      "shade_bytes_per_frame": ab["shade"],
                      "note": "algorithmic bytes of the shading kernels per frame / their CUDA-event time "
                              "inside the timed replays; peak = measured hbm_gbs (of measured)"},
