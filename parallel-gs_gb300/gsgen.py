@@ -652,3 +652,119 @@ def display_reg(dx, dy, magh, magv, dw, dh) -> int:
 
 def smode2_reg(interlace=0, ffmd=0) -> int:
     return (interlace & 1) | ((ffmd & 1) << 1)
+
+
+FUZZ_TEXTURE_PSMS = [PSMT8, PSMT4, PSMT8H, 0x24, 0x2C, PSMCT32, PSMCT24, PSMCT16, PSMCT16S]
+
+
+def frame_fuzz(seed: int, draws: int = 40, width: int = 256, height: int = 224) -> Frame:
+    """Random state coverage: every primitive type, AA1, fog, all blend / alpha
+    test / destination alpha / depth test modes, FBMSK, scissor, SCANMSK, XYOFFSET,
+    colour formats CT32/CT24/CT16/CT16S with Z32/Z24/Z16/Z16S, textures in PSMT8 /
+    PSMT4 / PSMT8H / PSMT4HL / PSMT4HH (CT32 or CT16 CLUTs) and CT32 / CT24 / CT16 /
+    CT16S, every wrap mode including region clamp / repeat, TEXA alpha expansion,
+    nearest and bilinear filtering; the sampling rate is random too."""
+    rng = np.random.Generator(np.random.PCG64(50000 + seed))
+    s = GifStream()
+    fpsm = [PSMCT32, PSMCT24, PSMCT16, PSMCT16S][int(rng.integers(0, 4))]
+    zpsm = [PSMZ32, PSMZ24, PSMZ16, PSMZ16S][int(rng.integers(0, 4))]
+    fbw = width // 64
+    zbp = 32
+    ss, ordered = [(1, True), (2, True), (4, True), (4, False), (8, True), (16, True), (16, False)][int(rng.integers(0, 7))]
+    s.ad([(PRMODECONT, 1), (FRAME_1, frame_reg(0, fbw, fpsm)), (ZBUF_1, zbuf_reg(zbp, zpsm)),
+          (SCISSOR_1, scissor_reg(0, width - 1, 0, height - 1)), (XYOFFSET_1, 0), (COLCLAMP, 1),
+          (DIMX, dimx_reg(DEFAULT_DIMX))])
+    # Textures from page 64 on.
+    texs = []
+    page = 64
+    for psm in FUZZ_TEXTURE_PSMS:
+        tw, th = int(rng.integers(4, 8)), int(rng.integers(4, 8))
+        w, h = 1 << tw, 1 << th
+        bpp = {PSMT8: 8, PSMT4: 4, PSMT8H: 32, 0x24: 32, 0x2C: 32, PSMCT32: 32, PSMCT24: 24, PSMCT16: 16,
+               PSMCT16S: 16}[psm]
+        tbw = max(2, w // 64) if psm in (PSMT8, PSMT4) else max(1, w // 64)
+        data = rng.integers(0, 256, size=w * h * bpp // 8, dtype=np.uint8).tobytes()
+        tbp0 = page * BLOCKS_PER_PAGE
+        s.upload(tbp0, tbw, psm, 0, 0, w, h, data)
+        page += 10
+        cpsm = cbp = cld = csa = 0
+        if psm in (PSMT8, PSMT4, PSMT8H, 0x24, 0x2C):
+            cpsm = PSMCT32 if rng.uniform() < 0.5 else PSMCT16
+            n = 256 if psm in (PSMT8, PSMT8H) else 16
+            cw, ch = (16, 16) if n == 256 else (8, 2)
+            cbp = page * BLOCKS_PER_PAGE
+            cbytes = 4 if cpsm == PSMCT32 else 2
+            clut = rng.integers(0, 256, size=cw * ch * cbytes, dtype=np.uint8).tobytes()
+            s.upload(cbp, 1, cpsm, 0, 0, cw, ch, clut)
+            page += 1
+            cld = 1
+            csa = int(rng.integers(0, 16)) if (n == 16 and cpsm == PSMCT16) else 0
+        texs.append((psm, tbp0, tbw, tw, th, cbp, cpsm, csa, cld, w, h))
+    zmax = {PSMZ32: (1 << 32) - 1, PSMZ24: (1 << 24) - 1, PSMZ16: 0xFFFF, PSMZ16S: 0xFFFF}[zpsm]
+    for d in range(draws):
+        prim = int(rng.integers(0, 7))
+        tme = int(rng.uniform() < 0.5)
+        fst = int(tme and rng.uniform() < 0.5)
+        fge = int(rng.uniform() < 0.2)
+        abe = int(rng.uniform() < 0.4)
+        aa1 = int(rng.uniform() < 0.15)
+        iip = int(rng.uniform() < 0.8)
+        regs = [(TEST_1, test_reg(ate=int(rng.uniform() < 0.3), atst=int(rng.integers(0, 8)),
+                                  aref=int(rng.integers(0, 256)), afail=int(rng.integers(0, 4)),
+                                  date=int(rng.uniform() < 0.15), datm=int(rng.integers(0, 2)),
+                                  zte=1, ztst=int(rng.integers(1, 4)))),
+                (ALPHA_1, alpha_reg(int(rng.integers(0, 3)), int(rng.integers(0, 3)), int(rng.integers(0, 3)),
+                                    int(rng.integers(0, 3)), int(rng.integers(0, 256)))),
+                (FBA_1, int(rng.uniform() < 0.2)), (DTHE, int(rng.uniform() < 0.3)),
+                (COLCLAMP, int(rng.uniform() < 0.7)), (PABE, int(rng.uniform() < 0.2)),
+                (FOGCOL, int(rng.integers(0, 1 << 24))),
+                (SCANMSK, [0, 0, 0, 2, 3][int(rng.integers(0, 5))]),
+                (TEXA, texa_reg(int(rng.integers(0, 256)), int(rng.integers(0, 2)), int(rng.integers(0, 256))))]
+        if rng.uniform() < 0.3:
+            x0, y0 = int(rng.integers(0, width // 2)), int(rng.integers(0, height // 2))
+            regs.append((SCISSOR_1, scissor_reg(x0, int(rng.integers(x0, width)), y0, int(rng.integers(y0, height)))))
+        else:
+            regs.append((SCISSOR_1, scissor_reg(0, width - 1, 0, height - 1)))
+        fbmsk = 0 if rng.uniform() < 0.7 else int(rng.integers(0, 1 << 32, dtype=np.uint64))
+        regs.append((FRAME_1, frame_reg(0, fbw, fpsm, fbmsk)))
+        regs.append((ZBUF_1, zbuf_reg(zbp, zpsm, int(rng.uniform() < 0.2))))
+        if tme:
+            psm, tbp0, tbw, tw, th, cbp, cpsm, csa, cld, w, h = texs[int(rng.integers(0, len(texs)))]
+            regs.append((TEX0_1, tex0_reg(tbp0, tbw, psm, tw, th, tcc=int(rng.integers(0, 2)),
+                                          tfx=int(rng.integers(0, 4)), cbp=cbp, cpsm=cpsm, csm=0, csa=csa, cld=cld)))
+            regs.append((TEX1_1, tex1_reg(mmag=int(rng.integers(0, 2)), mmin=int(rng.integers(0, 2)))))
+            wm = [int(rng.integers(0, 4)), int(rng.integers(0, 4))]
+            lo_u, lo_v = int(rng.integers(0, w)), int(rng.integers(0, h))
+            regs.append((CLAMP_1, clamp_reg(wm[0], wm[1], lo_u, int(rng.integers(lo_u, w)) if wm[0] == 2 else
+                                            int(rng.integers(0, w)), lo_v,
+                                            int(rng.integers(lo_v, h)) if wm[1] == 2 else int(rng.integers(0, h)))))
+        s.ad(regs)
+        s.ad([(PRIM, prim_reg(prim, iip=iip, tme=tme, fge=fge, abe=abe, aa1=aa1, fst=fst))])
+        nv = int(rng.integers(3, 48))
+        x = np.round(rng.uniform(-16, width + 16, nv) * 16).astype(np.int64) & 0xFFFF
+        y = np.round(rng.uniform(-16, height + 16, nv) * 16).astype(np.int64) & 0xFFFF
+        z = rng.integers(0, min(zmax, (1 << 32) - 1) + 1, nv, dtype=np.uint64).astype(np.int64)
+        rgba = rng.integers(0, 256, size=(nv, 4), dtype=np.int64)
+        desc = [D_RGBAQ]
+        q = [q_rgbaq(rgba)]
+        if tme and fst:
+            desc.append(D_UV)
+            q.append(q_uv(rng.integers(0, 256 * 16, nv), rng.integers(0, 256 * 16, nv)))
+        elif tme:
+            qq = rng.uniform(0.5, 2.0, nv).astype(np.float32)
+            desc.append(D_ST)
+            q.append(q_st((rng.uniform(-0.25, 1.25, nv) * qq).astype(np.float32),
+                          (rng.uniform(-0.25, 1.25, nv) * qq).astype(np.float32), qq))
+        if fge:
+            desc.append(D_XYZF2)
+            fog = rng.integers(0, 256, nv, dtype=np.uint64)
+            lo = (x.astype(np.uint64) | (y.astype(np.uint64) << np.uint64(32)))
+            hi = ((z.astype(np.uint64) & np.uint64(0xFFFFFF)) << np.uint64(4)) | (fog << np.uint64(36))
+            q.append(np.stack([lo, hi], axis=1))
+        else:
+            desc.append(D_XYZ2)
+            q.append(q_xyz2(x, y, z))
+        data = np.stack(q, axis=1).reshape(-1, 2)
+        s.packed(prim_reg(prim, iip=iip, tme=tme, fge=fge, abe=abe, aa1=aa1, fst=fst), desc, data)
+    return Frame("fuzz_%d" % seed, s.tobytes(), ss, ordered, draws,
+                 {"width": width, "height": height, "fbp": 0, "zbp": zbp})

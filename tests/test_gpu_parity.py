@@ -190,3 +190,13 @@ def test_scanout_circuit_parity(ss, ordered):
     for r, o in zip(ref, out):
         assert r.shape == o.shape
         assert np.array_equal(r, o)
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_feature_fuzz(seed):
+    """Random state coverage (every primitive type, AA1, fog, blend / alpha /
+    depth / destination-alpha modes, masks, scissor, all colour and depth
+    formats, every texture format and wrap mode, random sampling rate)."""
+    f = gsgen.frame_fuzz(seed)
+    ref, out = run_both(f)
+    assert_same(ref, out)
