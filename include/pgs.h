@@ -47,7 +47,9 @@ typedef enum pgs_status
 	/* Sticky device-side error: a capacity limit was hit or a bounded wait
 	 * expired.  Query with pgs_backend_ops.get_error. */
 	PGS_ERROR_DEVICE_FLAG = -6,
-	PGS_ERROR_CAPACITY = -7
+	PGS_ERROR_CAPACITY = -7,
+	/* A file could not be opened, read or written, or is not a GS dump. */
+	PGS_ERROR_IO = -8
 } pgs_status;
 
 /* ------------------------------------------------------------------ */
@@ -442,6 +444,27 @@ int pgs_gs_read_vram(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst);
  * copy is made before returning and the ticket is 0. */
 int pgs_gs_read_vram_async(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst, uint64_t *ticket);
 int pgs_gs_wait(pgs_gs *gs, uint64_t ticket);
+
+/* GS dumps (the PCSX2 / GSdx dump format read by GSDumpParser,
+ * dump/gs_dump_parser.cpp:8-263, and written by GSDumpGenerator,
+ * dump/gs_dump_generator.cpp:104-237): header, register file, 4 MiB VRAM,
+ * GIF path state, internal Q and privileged registers, then packets (0 GIF
+ * transfer, 1 vsync, 2 FIFO read, 3 privileged registers).
+ *
+ * pgs_gs_dump_open restores the dump's start state into gs; each
+ * pgs_gs_dump_next_vsync call then replays packets up to the next vsync that
+ * follows a transfer (*field = its field) and returns 1, or 0 at the end of
+ * the dump. */
+int pgs_gs_dump_open(pgs_gs *gs, const char *path);
+int pgs_gs_dump_next_vsync(pgs_gs *gs, uint32_t *field);
+int pgs_gs_dump_close(pgs_gs *gs);
+/* Recording: writes the header and gs's current state to path; afterwards
+ * every pgs_gs_gif_transfer and pgs_gs_write_register is appended as a
+ * transfer packet until pgs_gs_dump_record_end.  pgs_gs_dump_record_vsync
+ * appends the privileged registers and a vsync packet. */
+int pgs_gs_dump_record_begin(pgs_gs *gs, const char *path);
+int pgs_gs_dump_record_vsync(pgs_gs *gs, uint32_t field);
+int pgs_gs_dump_record_end(pgs_gs *gs);
 
 /* Privileged registers (GSInterface::get_priv_register_state, gs/gs_interface.hpp:70-108):
  * index 0 PMODE, 1 SMODE1, 2 SMODE2, 3 SRFSH, 4 SYNCH1, 5 SYNCH2, 6 SYNCV,

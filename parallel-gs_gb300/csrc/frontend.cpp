@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <unordered_map>
@@ -297,6 +298,9 @@ struct pgs_gs
 	uint64_t regs[128] = {};
 	// Privileged registers PMODE .. BGCOLOR (gs/gs_interface.hpp:70-91).
 	uint64_t priv[15] = {};
+	// GS dump being replayed / recorded.
+	FILE *dump_in = nullptr, *dump_out = nullptr;
+	std::vector<uint64_t> dump_buf;
 	float internal_q = 1.0f;
 	uint32_t cached_cbp[2] = {};
 
@@ -358,6 +362,29 @@ struct pgs_gs
 		// Page geometry of the colour and depth buffers (page_span).
 		uint32_t fb_pw = 0, fb_ph = 0, fb_stride = 0, z_pw = 0, z_ph = 0, z_stride = 0;
 	} dc;
+
+	// Marks every value derived from the register file dirty after the file
+	// was replaced wholesale (clobber_register_state).
+	void clobber_state()
+	{
+		reg_serial++;
+		template_dirty = true;
+		vq.count = 0;
+		update_offsets();
+	}
+
+	void record_transfer(uint32_t path, const void *data, size_t size)
+	{
+		uint8_t type = 0, p = uint8_t(path);
+		uint32_t sz = uint32_t(size);
+		if (fwrite(&type, 1, 1, dump_out) != 1 || fwrite(&p, 1, 1, dump_out) != 1 ||
+		    fwrite(&sz, 4, 1, dump_out) != 1 || fwrite(data, 1, size, dump_out) != size)
+		{
+			fclose(dump_out);
+			dump_out = nullptr;
+			sticky_error = PGS_ERROR_IO;
+		}
+	}
 
 	const DrawConsts &draw_consts()
 	{
@@ -1754,6 +1781,10 @@ pgs_gs *pgs_gs_create(const pgs_backend_ops *ops, void *backend, const pgs_gs_op
 
 void pgs_gs_destroy(pgs_gs *gs)
 {
+	if (!gs)
+		return;
+	pgs_gs_dump_close(gs);
+	pgs_gs_dump_record_end(gs);
 	delete gs;
 }
 
@@ -1763,6 +1794,8 @@ int pgs_gs_gif_transfer(pgs_gs *gs, uint32_t path, const void *data, size_t size
 		return PGS_ERROR_INVALID_ARGUMENT;
 	if (size == 0)
 		return PGS_OK;
+	if (gs->dump_out)
+		gs->record_transfer(path, data, size);
 	gs->gif_transfer(path, static_cast<const uint64_t *>(data), size / 16);
 	return gs->sticky_error;
 }
@@ -1771,6 +1804,13 @@ int pgs_gs_write_register(pgs_gs *gs, uint32_t addr, uint64_t payload)
 {
 	if (!gs || addr > 0x7f)
 		return PGS_ERROR_INVALID_ARGUMENT;
+	if (gs->dump_out)
+	{
+		// One A+D loop (GSDumpGenerator::write_register): GIF tag NLOOP 1,
+		// EOP, PACKED, NREG 1, REGS = A+D; then payload and address.
+		const uint64_t words[4] = { 1ull | (1ull << 15) | (1ull << 60), 0xeull, payload, uint64_t(addr) };
+		gs->record_transfer(1, words, sizeof(words));
+	}
 	gs->write_register(addr, payload);
 	return gs->sticky_error;
 }
@@ -1939,5 +1979,264 @@ int pgs_gs_set_super_sampling_rate(pgs_gs *gs, uint32_t super_sampling, uint32_t
 	gs->flush();
 	gs->set_super_sampling(super_sampling, ordered_grid != 0);
 	return gs->sticky_error;
+}
+}
+
+// ---------------------------------------------------------------------------
+// GS dumps (PCSX2 / GSdx format as read by GSDumpParser, dump/gs_dump_parser.cpp,
+// and written by GSDumpGenerator, dump/gs_dump_generator.cpp).
+namespace
+{
+constexpr uint32_t DUMP_STATE_VERSION = 9, DUMP_STATE_VERSION_MIN = 8;
+constexpr size_t PRIV_STATE_BYTES = 2 * 0x200 * 8;   // PrivRegisterState: two 0x200-qword halves
+enum : uint8_t { DUMP_TRANSFER = 0, DUMP_VSYNC = 1, DUMP_READ_FIFO = 2, DUMP_PRIV = 3 };
+
+// Register file order of the dump's state block (read_register_state).
+constexpr uint32_t DUMP_GLOBAL_REGS[] = { R_PRIM, R_PRMODECONT, R_TEXCLUT, R_SCANMSK, R_TEXA, R_FOGCOL, R_DIMX,
+                                          R_DTHE, R_COLCLAMP, R_PABE, R_BITBLTBUF, R_TRXDIR, R_TRXPOS, R_TRXREG };
+constexpr uint32_t DUMP_CTX_REGS[] = { R_XYOFFSET_1, R_TEX0_1, R_TEX1_1, R_CLAMP_1, R_MIPTBP1_1, R_MIPTBP2_1,
+                                       R_SCISSOR_1, R_ALPHA_1, R_TEST_1, R_FBA_1, R_FRAME_1, R_ZBUF_1 };
+
+bool rd(FILE *f, void *p, size_t n) { return fread(p, 1, n, f) == n; }
+bool wr(FILE *f, const void *p, size_t n) { return fwrite(p, 1, n, f) == n; }
+template <typename T> bool rdv(FILE *f, T &v) { return rd(f, &v, sizeof(v)); }
+template <typename T> bool wrv(FILE *f, const T &v) { return wr(f, &v, sizeof(v)); }
+}
+
+extern "C" {
+int pgs_gs_dump_open(pgs_gs *gs, const char *path)
+{
+	if (!gs || !path)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	pgs_gs_dump_close(gs);
+	FILE *f = fopen(path, "rb");
+	if (!f)
+		return PGS_ERROR_IO;
+	auto fail = [&]() { fclose(f); return PGS_ERROR_IO; };
+	uint32_t crc = 0, header_size = 0, header[9] = {};
+	if (!rdv(f, crc) || crc != 0xffffffffu || !rdv(f, header_size) || header_size < sizeof(header) ||
+	    !rd(f, header, sizeof(header)) || header[0] < DUMP_STATE_VERSION_MIN || header[0] > DUMP_STATE_VERSION)
+		return fail();
+	if (fseek(f, long(header_size - sizeof(header)), SEEK_CUR) != 0)
+		return fail();
+	uint32_t version = 0;
+	uint64_t v64 = 0;
+	uint32_t v32 = 0;
+	if (!rdv(f, version))
+		return fail();
+	uint64_t regs[128];
+	memcpy(regs, gs->regs, sizeof(regs));
+	for (uint32_t r : DUMP_GLOBAL_REGS)
+		if (!rdv(f, regs[r]))
+			return fail();
+	if (!rdv(f, v64))   // dummy
+		return fail();
+	for (uint32_t ctx = 0; ctx < 2; ctx++)
+		for (uint32_t r : DUMP_CTX_REGS)
+			if (!rdv(f, regs[r + ctx]))
+				return fail();
+	if (!rdv(f, regs[R_RGBAQ]) || !rdv(f, regs[R_ST]) || !rdv(f, v32))
+		return fail();
+	regs[R_UV] = v32;
+	if (!rdv(f, v32))
+		return fail();
+	regs[R_FOG] = v32;
+	uint8_t skip[8 + 4 * 4 + 61];
+	if (!rd(f, skip, 8 + 4 * 4) || (version >= 9 && !rd(f, skip, 61)))
+		return fail();
+	std::vector<uint8_t> vram(PGS_VRAM_SIZE);
+	if (!rd(f, vram.data(), vram.size()))
+		return fail();
+	uint64_t tags[4][2];
+	uint32_t path_reg[4];
+	for (int i = 0; i < 4; i++)
+		if (!rd(f, tags[i], 16) || !rdv(f, path_reg[i]))
+			return fail();
+	float q = 1.0f;
+	std::vector<uint64_t> priv(PRIV_STATE_BYTES / 8);
+	if (!rdv(f, q) || !rd(f, priv.data(), PRIV_STATE_BYTES))
+		return fail();
+
+	// Restore: VRAM through the backend, then the register file as-is
+	// (clobber_register_state: no side effects, every derived state dirty).
+	gs->flush();
+	int r = gs->ops->write_vram(gs->be, 0, PGS_VRAM_SIZE, vram.data());
+	if (r)
+	{
+		fclose(f);
+		return r;
+	}
+	memcpy(gs->regs, regs, sizeof(regs));
+	gs->internal_q = q;
+	for (int i = 0; i < 4; i++)
+	{
+		auto &p = gs->paths[i];
+		p.tag_lo = tags[i][0];
+		p.tag_hi = tags[i][1];
+		p.nloop = field(p.tag_lo, 0, 15);
+		p.flg = field(p.tag_lo, 58, 2);
+		p.nreg = field(p.tag_lo, 60, 4);
+		if (p.nreg == 0)
+			p.nreg = 16;
+		p.loop = 0;
+		p.reg = path_reg[i];
+	}
+	for (int i = 0; i < 15; i++)
+		gs->priv[i] = priv[2 * i];
+	gs->clobber_state();
+	gs->write_register(R_TEXFLUSH, 0);
+	gs->dump_in = f;
+	return gs->sticky_error;
+}
+
+int pgs_gs_dump_next_vsync(pgs_gs *gs, uint32_t *field_out)
+{
+	if (!gs || !gs->dump_in)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	FILE *f = gs->dump_in;
+	bool has_transfer = false;
+	for (;;)
+	{
+		uint8_t type;
+		if (!rdv(f, type))
+			return 0;
+		switch (type)
+		{
+		case DUMP_TRANSFER:
+		{
+			uint8_t path;
+			uint32_t size;
+			if (!rdv(f, path) || !rdv(f, size))
+				return 0;
+			gs->dump_buf.resize((size + 15) / 8 + 2);
+			if (!rd(f, gs->dump_buf.data(), size))
+				return 0;
+			if (size >= 16)
+				gs->gif_transfer(path & 3, gs->dump_buf.data(), size / 16);
+			has_transfer = true;
+			break;
+		}
+		case DUMP_VSYNC:
+		{
+			uint8_t fld;
+			if (!rdv(f, fld))
+				return 0;
+			gs->flush();
+			if (has_transfer)
+			{
+				if (field_out)
+					*field_out = fld;
+				return gs->sticky_error ? gs->sticky_error : 1;
+			}
+			break;
+		}
+		case DUMP_PRIV:
+		{
+			std::vector<uint64_t> priv(PRIV_STATE_BYTES / 8);
+			if (!rd(f, priv.data(), PRIV_STATE_BYTES))
+				return 0;
+			for (int i = 0; i < 15; i++)
+				gs->priv[i] = priv[2 * i];
+			break;
+		}
+		case DUMP_READ_FIFO:
+		{
+			// As the reference's parser: the FIFO read is not replayed.
+			uint32_t size;
+			if (!rdv(f, size))
+				return 0;
+			if (field_out)
+				*field_out = 0;
+			return 1;
+		}
+		default:
+			return PGS_ERROR_IO;
+		}
+	}
+}
+
+int pgs_gs_dump_close(pgs_gs *gs)
+{
+	if (!gs)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if (gs->dump_in)
+		fclose(gs->dump_in);
+	gs->dump_in = nullptr;
+	return PGS_OK;
+}
+
+int pgs_gs_dump_record_begin(pgs_gs *gs, const char *path)
+{
+	if (!gs || !path)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	pgs_gs_dump_record_end(gs);
+	gs->flush();
+	std::vector<uint8_t> vram(PGS_VRAM_SIZE);
+	int r = gs->ops->read_vram(gs->be, 0, 0, PGS_VRAM_SIZE, vram.data());
+	if (r)
+		return r;
+	FILE *f = fopen(path, "wb");
+	if (!f)
+		return PGS_ERROR_IO;
+	bool ok = true;
+	uint32_t header[9] = {};
+	header[0] = DUMP_STATE_VERSION;
+	header[1] = uint32_t(PGS_VRAM_SIZE + (18 + 12 * 2) * 8 + 7 * 4 + 4 * 5 * 4 + 4);
+	ok = ok && wrv(f, uint32_t(0xffffffffu)) && wrv(f, uint32_t(sizeof(header))) && wr(f, header, sizeof(header));
+	ok = ok && wrv(f, DUMP_STATE_VERSION_MIN);
+	for (uint32_t reg : DUMP_GLOBAL_REGS)
+		ok = ok && wrv(f, gs->regs[reg]);
+	ok = ok && wrv(f, gs->regs[R_TRXREG]);   // dummy
+	for (uint32_t ctx = 0; ctx < 2; ctx++)
+		for (uint32_t reg : DUMP_CTX_REGS)
+			ok = ok && wrv(f, gs->regs[reg + ctx]);
+	ok = ok && wrv(f, gs->regs[R_RGBAQ]) && wrv(f, gs->regs[R_ST]) && wrv(f, uint32_t(gs->regs[R_UV])) &&
+	     wrv(f, uint32_t(gs->regs[R_FOG])) && wrv(f, uint64_t(0)) && wrv(f, 0xffffffffu) && wrv(f, 0xffffffffu) &&
+	     wrv(f, uint32_t(0)) && wrv(f, uint32_t(0));
+	ok = ok && wr(f, vram.data(), vram.size());
+	for (int i = 0; i < 4; i++)
+	{
+		const auto &p = gs->paths[i];
+		uint64_t lo = p.tag_lo;
+		// NLOOP minus the loops already done (the format has no loop counter).
+		uint32_t remaining = p.nloop >= p.loop ? p.nloop - p.loop : 0;
+		lo = (lo & ~0x7fffull) | (remaining & 0x7fffu);
+		ok = ok && wrv(f, lo) && wrv(f, p.tag_hi) && wrv(f, p.reg);
+	}
+	ok = ok && wrv(f, gs->internal_q);
+	std::vector<uint64_t> priv(PRIV_STATE_BYTES / 8, 0);
+	for (int i = 0; i < 15; i++)
+		priv[2 * i] = gs->priv[i];
+	ok = ok && wr(f, priv.data(), PRIV_STATE_BYTES);
+	if (!ok)
+	{
+		fclose(f);
+		return PGS_ERROR_IO;
+	}
+	gs->dump_out = f;
+	return PGS_OK;
+}
+
+int pgs_gs_dump_record_vsync(pgs_gs *gs, uint32_t fld)
+{
+	if (!gs || !gs->dump_out)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	std::vector<uint64_t> priv(PRIV_STATE_BYTES / 8, 0);
+	for (int i = 0; i < 15; i++)
+		priv[2 * i] = gs->priv[i];
+	bool ok = wrv(gs->dump_out, uint8_t(DUMP_PRIV)) && wr(gs->dump_out, priv.data(), PRIV_STATE_BYTES) &&
+	          wrv(gs->dump_out, uint8_t(DUMP_VSYNC)) && wrv(gs->dump_out, uint8_t(fld));
+	return ok ? PGS_OK : PGS_ERROR_IO;
+}
+
+int pgs_gs_dump_record_end(pgs_gs *gs)
+{
+	if (!gs)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	int r = PGS_OK;
+	if (gs->dump_out && fclose(gs->dump_out) != 0)
+		r = PGS_ERROR_IO;
+	gs->dump_out = nullptr;
+	return r;
 }
 }

@@ -768,3 +768,45 @@ def frame_fuzz(seed: int, draws: int = 40, width: int = 256, height: int = 224) 
         s.packed(prim_reg(prim, iip=iip, tme=tme, fge=fge, abe=abe, aa1=aa1, fst=fst), desc, data)
     return Frame("fuzz_%d" % seed, s.tobytes(), ss, ordered, draws,
                  {"width": width, "height": height, "fbp": 0, "zbp": zbp})
+
+
+def write_dump(path, transfers, vram: bytes | None = None, regs: dict | None = None, version: int = 9,
+               serial: bytes = b"", vsync_fields=(0,)) -> None:
+    """Writes a GS dump in the PCSX2 / GSdx layout (GSDumpGenerator::init,
+    dump/gs_dump_generator.cpp:186-237): fake CRC, header (+ serial bytes), the
+    register block in its fixed order, VRAM, four GIF paths, internal Q and the
+    privileged registers; then one transfer packet per entry of `transfers`
+    ((path, bytes) pairs) followed by a vsync packet per field."""
+    regs = regs or {}
+    vram = vram if vram is not None else bytes(4 * 1024 * 1024)
+    out = bytearray()
+    u32 = lambda v: struct.pack("<I", v & 0xFFFFFFFF)
+    u64 = lambda v: struct.pack("<Q", v & 0xFFFFFFFFFFFFFFFF)
+    out += u32(0xFFFFFFFF)
+    header = [version, len(vram) + (18 + 24) * 8 + 7 * 4 + 80 + 4, 36, len(serial), 0, 0, 0, 0, 0]
+    out += u32(36 + len(serial))
+    out += b"".join(u32(v) for v in header) + serial
+    out += u32(version)
+    for r in (PRIM, PRMODECONT, TEXCLUT, SCANMSK, TEXA, FOGCOL, DIMX, DTHE, COLCLAMP, PABE, BITBLTBUF, TRXDIR,
+              TRXPOS, TRXREG):
+        out += u64(regs.get(r, 0))
+    out += u64(0)
+    for ctx in range(2):
+        for r in (XYOFFSET_1, TEX0_1, TEX1_1, CLAMP_1, 0x34, 0x36, SCISSOR_1, ALPHA_1, TEST_1, FBA_1, FRAME_1,
+                  ZBUF_1):
+            out += u64(regs.get(r + ctx, 0))
+    out += u64(regs.get(RGBAQ, 0)) + u64(regs.get(ST, 0)) + u32(regs.get(UV, 0)) + u32(regs.get(FOG, 0))
+    out += u64(0) + u32(0xFFFFFFFF) + u32(0xFFFFFFFF) + u32(0) + u32(0)
+    if version >= 9:
+        out += bytes(61)
+    out += vram
+    for _ in range(4):
+        out += u64(0) + u64(0) + u32(0)
+    out += struct.pack("<f", 1.0)
+    out += bytes(2 * 0x200 * 8)
+    for p, data in transfers:
+        out += bytes([0, p]) + u32(len(data)) + data
+    for f in vsync_fields:
+        out += bytes([1, f])
+    with open(path, "wb") as fh:
+        fh.write(bytes(out))

@@ -28,6 +28,7 @@ PGS_OK = 0
 STATUS_NAMES = {
     0: "PGS_OK", -1: "PGS_ERROR_INVALID_ARGUMENT", -2: "PGS_ERROR_OUT_OF_MEMORY", -3: "PGS_ERROR_CUDA",
     -4: "PGS_ERROR_NO_DEVICE", -5: "PGS_ERROR_UNSUPPORTED", -6: "PGS_ERROR_DEVICE_FLAG", -7: "PGS_ERROR_CAPACITY",
+    -8: "PGS_ERROR_IO",
 }
 
 
@@ -89,7 +90,9 @@ EXPORTED_SYMBOLS = [
     "pgs_upscaler_set_tensor_path", "pgs_upscaler_get_error",
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
     "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait",
-    "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
+    "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit",
+    "pgs_gs_dump_open", "pgs_gs_dump_next_vsync", "pgs_gs_dump_close", "pgs_gs_dump_record_begin",
+    "pgs_gs_dump_record_vsync", "pgs_gs_dump_record_end", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
     "pgs_gs_set_super_sampling_rate",
 ]
 
@@ -145,6 +148,12 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.pgs_gs_read_vram_async.argtypes = [vp, u64, u64, vp, C.POINTER(u64)]
     lib.pgs_gs_wait.argtypes = [vp, u64]
     lib.pgs_gs_write_priv_register.argtypes = [vp, u32, u64]
+    lib.pgs_gs_dump_open.argtypes = [vp, C.c_char_p]
+    lib.pgs_gs_dump_next_vsync.argtypes = [vp, C.POINTER(u32)]
+    lib.pgs_gs_dump_close.argtypes = [vp]
+    lib.pgs_gs_dump_record_begin.argtypes = [vp, C.c_char_p]
+    lib.pgs_gs_dump_record_vsync.argtypes = [vp, u32]
+    lib.pgs_gs_dump_record_end.argtypes = [vp]
     lib.pgs_gs_read_priv_register.argtypes = [vp, u32, C.POINTER(u64)]
     lib.pgs_gs_scanout_circuit.argtypes = [vp, u32, u32, u32, vp, u64, C.POINTER(u32), C.POINTER(u32)]
     lib.pgs_gs_write_vram.argtypes = [vp, u64, u64, vp]
@@ -293,6 +302,30 @@ class GSInterface:
 
     def wait(self, ticket: int) -> None:
         check(self.lib.pgs_gs_wait(self.handle, ticket), "wait")
+
+    def dump_open(self, path) -> None:
+        """Restores the start state of a GS dump (PCSX2 / GSdx format)."""
+        check(self.lib.pgs_gs_dump_open(self.handle, str(path).encode()), "dump_open")
+
+    def dump_next_vsync(self):
+        """Replays packets up to the next vsync; returns its field, or None at the end."""
+        f = C.c_uint32(0)
+        r = self.lib.pgs_gs_dump_next_vsync(self.handle, C.byref(f))
+        if r < 0:
+            check(r, "dump_next_vsync")
+        return int(f.value) if r == 1 else None
+
+    def dump_close(self) -> None:
+        check(self.lib.pgs_gs_dump_close(self.handle), "dump_close")
+
+    def dump_record_begin(self, path) -> None:
+        check(self.lib.pgs_gs_dump_record_begin(self.handle, str(path).encode()), "dump_record_begin")
+
+    def dump_record_vsync(self, field: int = 0) -> None:
+        check(self.lib.pgs_gs_dump_record_vsync(self.handle, field), "dump_record_vsync")
+
+    def dump_record_end(self) -> None:
+        check(self.lib.pgs_gs_dump_record_end(self.handle), "dump_record_end")
 
     PRIV = {"PMODE": 0, "SMODE1": 1, "SMODE2": 2, "SRFSH": 3, "SYNCH1": 4, "SYNCH2": 5, "SYNCV": 6, "DISPFB1": 7,
             "DISPLAY1": 8, "DISPFB2": 9, "DISPLAY2": 10, "EXTBUF": 11, "EXTDATA": 12, "EXTWRITE": 13, "BGCOLOR": 14}
