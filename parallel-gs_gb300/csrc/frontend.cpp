@@ -208,10 +208,27 @@ struct PageTracker
 		return fresh;
 	}
 
+	static uint64_t low_mask(uint32_t n) { return n >= 64 ? ~0ull : ((1ull << n) - 1); }
+
+	// Spans up to 64 pages wide touch at most two words per row: one 128-bit
+	// mask per row, no data-dependent loop (the common case; primitives are
+	// small).
 	bool any_kind(const PageSpan &s, uint32_t k) const
 	{
 		if (gen[k] == gen_at_clear[k])
 			return false;
+		if (s.width <= 64)
+		{
+			const uint64_t m = low_mask(s.width);
+			uint64_t acc = 0;
+			for (uint32_t y = 0; y < s.height; y++)
+			{
+				uint32_t start = (s.base_page + y * s.stride) % NUM_PAGES, w = start >> 6;
+				unsigned __int128 mm = (unsigned __int128)m << (start & 63);
+				acc |= (bits[k][w] & uint64_t(mm)) | (bits[k][(w + 1) % WORDS] & uint64_t(mm >> 64));
+			}
+			return acc != 0;
+		}
 		for (uint32_t y = 0; y < s.height; y++)
 			if (range_any(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width))
 				return true;
@@ -221,8 +238,25 @@ struct PageTracker
 	void mark_kind(const PageSpan &s, uint32_t k)
 	{
 		bool fresh = false;
-		for (uint32_t y = 0; y < s.height; y++)
-			fresh |= range_set(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width);
+		if (s.width <= 64)
+		{
+			const uint64_t m = low_mask(s.width);
+			uint64_t missing = 0;
+			for (uint32_t y = 0; y < s.height; y++)
+			{
+				uint32_t start = (s.base_page + y * s.stride) % NUM_PAGES, w = start >> 6, w1 = (w + 1) % WORDS;
+				unsigned __int128 mm = (unsigned __int128)m << (start & 63);
+				missing |= (~bits[k][w] & uint64_t(mm)) | (~bits[k][w1] & uint64_t(mm >> 64));
+				bits[k][w] |= uint64_t(mm);
+				bits[k][w1] |= uint64_t(mm >> 64);
+			}
+			fresh = missing != 0;
+		}
+		else
+		{
+			for (uint32_t y = 0; y < s.height; y++)
+				fresh |= range_set(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width);
+		}
 		if (fresh)
 			gen[k]++;
 	}
