@@ -122,7 +122,12 @@ typedef struct pgs_texture_desc
 	uint32_t aem, ta0, ta1; /* TEXA */
 	uint32_t wms, wmt;      /* CLAMP wrap modes */
 	uint32_t minu, maxu, minv, maxv;
-	uint32_t padding[2];
+	/* Mip levels sampled (1..7; 1 unless TEX1.MMIN selects a mipmap mode):
+	 * min(MXL + 1, min(TW, TH) + 1, 7) as compute_effective_texture_rect
+	 * (gs/gs_renderer.cpp:1235-1265).  mip[l - 1] = TBP | TBW << 16 of level l
+	 * from MIPTBP1 / MIPTBP2; zero for levels not sampled. */
+	uint32_t levels;
+	uint32_t mip[6];
 } pgs_texture_desc;
 
 /* One framebuffer instance inside a render pass (RenderPass::Instance,
@@ -155,6 +160,8 @@ typedef struct pgs_render_pass
 	uint32_t coarse_tile_size_log2;
 	uint32_t has_aa1, has_scanmsk;
 	uint32_t flush_reason;
+	/* Some primitive samples mip levels (TEX1.MXL > 0 with a mipmapping MMIN). */
+	uint32_t has_mipmap;
 } pgs_render_pass;
 
 /* A VRAM transfer (CopyDescriptor, gs/gs_renderer.hpp).  For HOST_TO_LOCAL,

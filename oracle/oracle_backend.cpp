@@ -884,9 +884,11 @@ struct Backend
 		return uint32_t(cl[bi]) | (uint32_t(cl[bi + 256]) << 16);
 	}
 
-	uint32_t texel(const pgs_texture_desc &t, int32_t x, int32_t y)
+	uint32_t texel(const pgs_texture_desc &t, uint32_t level, int32_t x, int32_t y)
 	{
-		uint32_t a = swizzle(uint32_t(x), uint32_t(y), t.tbp0, t.tbw, t.psm);
+		uint32_t tbp = level ? (t.mip[level - 1] & 0x3fffu) : t.tbp0;
+		uint32_t tbw = level ? (t.mip[level - 1] >> 16) : t.tbw;
+		uint32_t a = swizzle(uint32_t(x), uint32_t(y), tbp, tbw, t.psm);
 		switch (t.psm)
 		{
 		case CT24: case Z24:
@@ -927,26 +929,38 @@ struct Backend
 		}
 	}
 
-	// sample_texture (gs/shaders/ubershader.comp:1042-1258) for LOD 0.
-	void sample_texture(const PassCtx &P, uint32_t tex_word, float u, float v, bool perspective, float out[4])
+	// One filtered sample of mip level `level`: coordinates as sample_texture
+	// (gs/shaders/ubershader.comp:1133-1151,1214-1227), region bounds and masks
+	// shifted down by the level (texture_clamp :947-953; upload_texture
+	// gs/gs_renderer.cpp:3578-3590), bilinear as exact k/16 weights + roundEven.
+	void sample_level(const pgs_texture_desc &t, uint32_t level, bool clamp_s, bool clamp_t, bool linear, float u,
+	                  float v, bool perspective, uint32_t rgba[4])
 	{
-		const pgs_texture_desc &t = P.rp->textures[tex_word & 0xffffu];
-		bool clamp_s = tex_word & (1u << 19), clamp_t = tex_word & (1u << 20);
-		bool linear = tex_word & (1u << 16);
-		float w = float(1u << t.tw_log2), h = float(1u << t.th_log2);
-		float uu = perspective ? u * w : u;
-		float vv = perspective ? v * h : v;
+		uint32_t twl = t.tw_log2 - level, thl = t.th_log2 - level;
+		float uu, vv;
+		if (perspective)
+		{
+			uu = u * float(1u << twl);
+			vv = v * float(1u << thl);
+		}
+		else
+		{
+			float scale = std::ldexp(1.0f, -int(level));
+			uu = u * scale;
+			vv = v * scale;
+		}
+		uint32_t minu = t.minu >> level, maxu = t.maxu >> level, minv = t.minv >> level, maxv = t.maxv >> level;
 		if (clamp_s)
 		{
-			float lo = (t.wms == 2) ? float(t.minu) : 0.0f;
-			float hi = (t.wms == 2) ? float(t.maxu) : w - 1.0f;
-			uu = std::min(std::max(uu, std::floor(lo) + 0.5f), std::floor(hi) + 0.5f);
+			float lo = (t.wms == 2) ? float(minu) : 0.0f;
+			float hi = (t.wms == 2) ? float(maxu) : float((1u << twl) - 1u);
+			uu = std::min(std::max(uu, lo + 0.5f), hi + 0.5f);
 		}
 		if (clamp_t)
 		{
-			float lo = (t.wmt == 2) ? float(t.minv) : 0.0f;
-			float hi = (t.wmt == 2) ? float(t.maxv) : h - 1.0f;
-			vv = std::min(std::max(vv, std::floor(lo) + 0.5f), std::floor(hi) + 0.5f);
+			float lo = (t.wmt == 2) ? float(minv) : 0.0f;
+			float hi = (t.wmt == 2) ? float(maxv) : float((1u << thl) - 1u);
+			vv = std::min(std::max(vv, lo + 0.5f), hi + 0.5f);
 		}
 		float fu = uu * 16.0f;
 		fu = fu + (1.0f / 64.0f);
@@ -954,22 +968,20 @@ struct Backend
 		fv = fv + (1.0f / 64.0f);
 		int32_t ku = int32_t(std::floor(fu));
 		int32_t kv = int32_t(std::floor(fv));
-		uint32_t wms = t.wms == 1 ? 1u : t.wms, wmt = t.wmt == 1 ? 1u : t.wmt;
-		uint32_t c;
 		if (!linear)
 		{
-			int32_t x = wrap_coord(ku >> 4, wms, t.tw_log2, t.minu, t.maxu);
-			int32_t y = wrap_coord(kv >> 4, wmt, t.th_log2, t.minv, t.maxv);
-			c = texel(t, x, y);
+			int32_t x = wrap_coord(ku >> 4, t.wms, twl, minu, maxu);
+			int32_t y = wrap_coord(kv >> 4, t.wmt, thl, minv, maxv);
+			uint32_t c = texel(t, level, x, y);
 			for (int k = 0; k < 4; k++)
-				out[k] = float((c >> (8 * k)) & 0xff);
+				rgba[k] = (c >> (8 * k)) & 0xffu;
 			return;
 		}
 		int32_t bu = ku - 8, bv = kv - 8;
 		int32_t x0 = bu >> 4, y0 = bv >> 4;
 		uint32_t fx = uint32_t(bu) & 15u, fy = uint32_t(bv) & 15u;
-		int32_t xs[2] = { wrap_coord(x0, wms, t.tw_log2, t.minu, t.maxu), wrap_coord(x0 + 1, wms, t.tw_log2, t.minu, t.maxu) };
-		int32_t ys[2] = { wrap_coord(y0, wmt, t.th_log2, t.minv, t.maxv), wrap_coord(y0 + 1, wmt, t.th_log2, t.minv, t.maxv) };
+		int32_t xs[2] = { wrap_coord(x0, t.wms, twl, minu, maxu), wrap_coord(x0 + 1, t.wms, twl, minu, maxu) };
+		int32_t ys[2] = { wrap_coord(y0, t.wmt, thl, minv, maxv), wrap_coord(y0 + 1, t.wmt, thl, minv, maxv) };
 		uint32_t wx[2] = { 16 - fx, fx }, wy[2] = { 16 - fy, fy };
 		uint32_t acc[4] = { 0, 0, 0, 0 };
 		for (int yy = 0; yy < 2; yy++)
@@ -978,7 +990,7 @@ struct Backend
 				uint32_t wgt = wx[xx] * wy[yy];
 				if (!wgt)
 					continue;
-				uint32_t tc = texel(t, xs[xx], ys[yy]);
+				uint32_t tc = texel(t, level, xs[xx], ys[yy]);
 				for (int k = 0; k < 4; k++)
 					acc[k] += wgt * ((tc >> (8 * k)) & 0xffu);
 			}
@@ -988,8 +1000,110 @@ struct Backend
 			uint32_t q = acc[k] >> 8, r = acc[k] & 0xffu;
 			if (r > 128 || (r == 128 && (q & 1)))
 				q++;
-			out[k] = float(q);
+			rgba[k] = q;
 		}
+	}
+
+	// log2 for the LOD formula: ln m = 2 atanh((m - 1) / (m + 1)) by the series
+	// s + s^3/3 + s^5/5 + s^7/7 + s^9/9 after reducing m to [sqrt(1/2), sqrt(2)];
+	// one rounding per operation (the definition the CUDA sampler shares).
+	static float lod_log2(float x)
+	{
+		uint32_t b;
+		memcpy(&b, &x, 4);
+		int32_t e = int32_t((b >> 23) & 0xffu) - 127;
+		uint32_t mb = (b & 0x7fffffu) | 0x3f800000u;
+		float m;
+		memcpy(&m, &mb, 4);
+		if (m > 1.41421356f)
+		{
+			m = m * 0.5f;
+			e++;
+		}
+		float s = (m - 1.0f) / (m + 1.0f);
+		float s2 = s * s;
+		float poly = s2 * (1.0f / 9.0f);
+		poly = poly + (1.0f / 7.0f);
+		poly = s2 * poly;
+		poly = poly + (1.0f / 5.0f);
+		poly = s2 * poly;
+		poly = poly + (1.0f / 3.0f);
+		poly = s2 * poly;
+		poly = poly + 1.0f;
+		float ln_m = (2.0f * s) * poly;
+		float l2 = ln_m * 1.44269504f;
+		return float(e) + l2;
+	}
+
+	// sample_texture (gs/shaders/ubershader.comp:1042-1258): LOD from Q
+	// (ceil(-log2|Q| * 2^(L+4) + K) / 16) or fixed (K >> 4), clamped to
+	// [0, MXL]; MMIN applies when the LOD is positive; trilinear blends
+	// floor(fract * 16) / 16 of the next level.  Levels past the texture's
+	// chain read its last level.
+	void sample_texture(const PassCtx &P, uint32_t tex_word, uint32_t tex2, float u, float v, float q,
+	                    bool perspective, float out[4])
+	{
+		const pgs_texture_desc &t = P.rp->textures[tex_word & 0xffffu];
+		bool clamp_s = tex_word & (1u << 19), clamp_t = tex_word & (1u << 20);
+		bool mag_linear = tex_word & (1u << 16), min_linear = tex_word & (1u << 17);
+		bool trilinear = tex_word & (1u << 18);
+		uint32_t max_mip = (tex_word >> 21) & 7u;
+		uint32_t rgba[4];
+		if (max_mip == 0)
+		{
+			sample_level(t, 0, clamp_s, clamp_t, mag_linear, u, v, perspective, rgba);
+		}
+		else
+		{
+			int32_t K = int32_t((tex2 >> 3) & 0xfffu);
+			if (K & 0x800)
+				K -= 0x1000;
+			float lod;
+			bool linear;
+			if (!(tex2 & 1u))
+			{
+				uint32_t L = (tex2 >> 1) & 3u;
+				float aq = std::fabs(q), formula = 0.0f;
+				if (std::isnormal(aq))
+				{
+					float scaled = -lod_log2(aq) * float(1u << (L + 4));
+					formula = scaled + float(K);
+				}
+				lod = std::ceil(formula) * 0.0625f;
+				linear = formula > 0.0f ? min_linear : mag_linear;
+			}
+			else
+			{
+				lod = float(K / 16 - ((K % 16) < 0 ? 1 : 0));
+				linear = lod > 0.0f ? min_linear : mag_linear;
+			}
+			lod = std::min(std::max(lod, 0.0f), float(max_mip));
+			float l1 = std::floor(lod), l2 = std::ceil(lod);
+			uint32_t weight = uint32_t((lod - l1) * 16.0f);
+			if (!trilinear)
+			{
+				weight = 0;
+				l1 = float(int32_t(lod + 0.5f));
+			}
+			uint32_t last = std::max<uint32_t>(t.levels, 1) - 1;
+			sample_level(t, std::min<uint32_t>(uint32_t(l1), last), clamp_s, clamp_t, linear, u, v, perspective, rgba);
+			if (weight)
+			{
+				uint32_t c2[4];
+				sample_level(t, std::min<uint32_t>(uint32_t(l2), last), clamp_s, clamp_t, linear, u, v, perspective,
+				             c2);
+				for (int k = 0; k < 4; k++)
+				{
+					uint32_t acc = (16 - weight) * rgba[k] + weight * c2[k];
+					uint32_t r = acc / 16, f = acc % 16;
+					if (f > 8 || (f == 8 && (r & 1)))
+						r++;
+					rgba[k] = r;
+				}
+			}
+		}
+		for (int k = 0; k < 4; k++)
+			out[k] = float(rgba[k]);
 	}
 
 	// compute_combined_color (gs/shaders/ubershader.comp:1260-1339).
@@ -1029,7 +1143,7 @@ struct Backend
 			u = std::fmin(std::fmax(u, -2047.0f), 2047.0f);
 			v = std::fmin(std::fmax(v, -2047.0f), 2047.0f);
 			float tx[4];
-			sample_texture(P, P.prims[pi].tex, u, v, r.perspective, tx);
+			sample_texture(P, P.prims[pi].tex, P.prims[pi].tex2, u, v, stq[2], r.perspective, tx);
 			switch (mode)
 			{
 			case 1:
@@ -1793,6 +1907,12 @@ struct Backend
 	{
 		if (!rp || rp->num_primitives == 0)
 			return 0;
+		for (uint32_t i = 0; i < rp->num_textures; i++)
+		{
+			const pgs_texture_desc &d = rp->textures[i];
+			if (d.levels > 7 || std::min(std::min(d.tw_log2, d.th_log2), 10u) + 1 < d.levels)
+				return PGS_ERROR_INVALID_ARGUMENT;
+		}
 		std::vector<pgs_primitive_attribute> prims(rp->prims, rp->prims + rp->num_primitives);
 		std::vector<Setup> setup(rp->num_primitives);
 		std::vector<TAttr> tattr(rp->num_primitives);

@@ -65,9 +65,9 @@ enum OpType : uint32_t { OP_COPY = 0, OP_CLUT = 1, OP_PASS = 2 };
 struct PassOp
 {
 	size_t pos_off, attr_off, prim_off, states_off, textures_off, images_off;
-	uint32_t num_texels, max_texels;
+	uint32_t num_texels, max_texels, max_levels;
 	uint32_t num_prims, num_states, num_textures;
-	uint32_t tile_size_log2, has_aa1, has_scanmsk;
+	uint32_t tile_size_log2, has_aa1, has_scanmsk, has_mipmap;
 	uint32_t num_instances;
 	pgs_rp_instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
 	// Host copy of the primitive records while the pass is submitted
@@ -373,7 +373,7 @@ struct CudaBackend
 		size_t prim_bytes = size_t(n) * sizeof(pgs_primitive_attribute);
 		size_t st_bytes = size_t(std::max<uint32_t>(rp->num_states, 1)) * sizeof(pgs_state_vector);
 		size_t tex_bytes = size_t(std::max<uint32_t>(rp->num_textures, 1)) * sizeof(pgs_texture_desc);
-		size_t img_bytes = size_t(std::max<uint32_t>(rp->num_textures, 1)) * sizeof(TexImage);
+		size_t img_bytes = size_t(std::max<uint32_t>(rp->num_textures, 1)) * TEX_LEVELS * sizeof(TexImage);
 		size_t base;
 		size_t total = align_up(pos_bytes, 256) + align_up(attr_bytes, 256) + align_up(prim_bytes, 256) +
 		               align_up(st_bytes, 256) + align_up(tex_bytes, 256) + align_up(img_bytes, 256);
@@ -411,33 +411,45 @@ struct CudaBackend
 			memcpy(h_arena + p.textures_off, rp->textures, rp->num_textures * sizeof(pgs_texture_desc));
 		p.images_off = p.textures_off + align_up(tex_bytes, 256);
 		{
-			// Decoded extent covers every texel index the wrap modes can produce.
+			// Decoded extent of each mip level covers every texel index the wrap
+			// modes can produce at that level (region bounds scale with the level).
 			TexImage *im = reinterpret_cast<TexImage *>(h_arena + p.images_off);
+			memset(im, 0, img_bytes);
 			uint64_t texels = 0;
-			uint32_t max_texels = 0;
+			uint32_t max_texels = 0, max_levels = 1;
 			for (uint32_t i = 0; i < rp->num_textures; i++)
 			{
 				const pgs_texture_desc &t = rp->textures[i];
-				auto extent = [](uint32_t size_log2, uint32_t mode, uint32_t lo, uint32_t hi) {
-					uint32_t size = 1u << std::min<uint32_t>(size_log2, 10);
-					if (mode == WRAP_REGION_CLAMP)
-						return std::max(size, std::max(lo, hi) + 1u);
-					if (mode == WRAP_REGION_REPEAT)
-						return std::max(size, (((size - 1u) & lo) | hi) + 1u);
-					return size;
-				};
-				im[i].ext_u = extent(t.tw_log2, t.wms, t.minu, t.maxu);
-				im[i].ext_v = extent(t.th_log2, t.wmt, t.minv, t.maxv);
-				im[i].offset = uint32_t(texels);
-				im[i].padding = 0;
-				uint32_t n = im[i].ext_u * im[i].ext_v;
-				texels += n;
-				max_texels = std::max(max_texels, n);
+				uint32_t levels = std::max<uint32_t>(t.levels, 1);
+				if (levels > TEX_LEVELS || std::min(std::min(t.tw_log2, t.th_log2), 10u) + 1 < levels)
+					return PGS_ERROR_INVALID_ARGUMENT;
+				max_levels = std::max(max_levels, levels);
+				for (uint32_t l = 0; l < levels; l++)
+				{
+					auto extent = [l](uint32_t size_log2, uint32_t mode, uint32_t lo, uint32_t hi) {
+						uint32_t size = 1u << (std::min<uint32_t>(size_log2, 10) - l);
+						lo >>= l;
+						hi >>= l;
+						if (mode == WRAP_REGION_CLAMP)
+							return std::max(size, std::max(lo, hi) + 1u);
+						if (mode == WRAP_REGION_REPEAT)
+							return std::max(size, (((size - 1u) & lo) | hi) + 1u);
+						return size;
+					};
+					TexImage &m = im[i * TEX_LEVELS + l];
+					m.ext_u = extent(t.tw_log2, t.wms, t.minu, t.maxu);
+					m.ext_v = extent(t.th_log2, t.wmt, t.minv, t.maxv);
+					m.offset = uint32_t(texels);
+					uint32_t n = m.ext_u * m.ext_v;
+					texels += n;
+					max_texels = std::max(max_texels, n);
+				}
 			}
 			if (texels > (uint64_t(1) << 31))
 				return PGS_ERROR_CAPACITY;
 			p.num_texels = uint32_t(texels);
 			p.max_texels = max_texels;
+			p.max_levels = max_levels;
 		}
 		r = stage >= 0 ? upload_arena(p.states_off, total - (p.states_off - base)) : upload_arena(base, total);
 		if (r)
@@ -448,6 +460,7 @@ struct CudaBackend
 		p.num_textures = rp->num_textures;
 		p.tile_size_log2 = rp->coarse_tile_size_log2;
 		p.has_aa1 = rp->has_aa1;
+		p.has_mipmap = rp->has_mipmap;
 		p.has_scanmsk = rp->has_scanmsk;
 		p.num_instances = rp->num_instances;
 		memcpy(p.instances, rp->instances, sizeof(p.instances));
@@ -576,7 +589,7 @@ struct CudaBackend
 	// Shading launches: the super-sampled variant for tiles that need it, then
 	// the single-sampled variant (ubershader.comp dispatched twice,
 	// gs/gs_renderer.cpp:2395-2415).
-	template <bool AA>
+	template <bool AA, bool MIP>
 	void launch_shade(const PassParams &P, const DevInstance &I, uint32_t ns_log2, uint32_t grid,
 	                  const uint32_t *masks, const uint32_t *summary)
 	{
@@ -584,14 +597,14 @@ struct CudaBackend
 		{
 			switch (ns_log2)
 			{
-			case 1: shade_kernel<2, true, AA><<<grid, 128, 0, stream>>>(P, I, masks, summary, d_flags); break;
-			case 2: shade_kernel<4, true, AA><<<grid, 256, 0, stream>>>(P, I, masks, summary, d_flags); break;
-			case 3: shade_kernel<8, true, AA><<<grid, 512, 0, stream>>>(P, I, masks, summary, d_flags); break;
-			default: shade_kernel<16, true, AA><<<grid, 1024, 0, stream>>>(P, I, masks, summary, d_flags); break;
+			case 1: shade_kernel<2, true, AA, MIP><<<grid, 128, 0, stream>>>(P, I, masks, summary, d_flags); break;
+			case 2: shade_kernel<4, true, AA, MIP><<<grid, 256, 0, stream>>>(P, I, masks, summary, d_flags); break;
+			case 3: shade_kernel<8, true, AA, MIP><<<grid, 512, 0, stream>>>(P, I, masks, summary, d_flags); break;
+			default: shade_kernel<16, true, AA, MIP><<<grid, 1024, 0, stream>>>(P, I, masks, summary, d_flags); break;
 			}
 			launch_counter++;
 		}
-		shade_kernel<1, false, AA><<<grid, 64, 0, stream>>>(P, I, masks, summary, d_flags);
+		shade_kernel<1, false, AA, MIP><<<grid, 64, 0, stream>>>(P, I, masks, summary, d_flags);
 		launch_counter++;
 	}
 
@@ -644,7 +657,7 @@ struct CudaBackend
 		bin_kernel<<<(count + 127) / 128, 128, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags);
 		launch_counter++;
 		uint32_t grid = uint32_t(subs);
-		if (collect && ns_log2 <= BATCH_MAX_NS_LOG2 && (I.rate_y_log2 != 0 || ns_log2 == 0))
+		if (collect && !p.has_mipmap && ns_log2 <= BATCH_MAX_NS_LOG2 && (I.rate_y_log2 != 0 || ns_log2 == 0))
 		{
 			collect->P = P;
 			collect->I = I;
@@ -665,10 +678,13 @@ struct CudaBackend
 				return r;
 			shade_started = true;
 		}
-		if (p.has_aa1)
-			launch_shade<true>(P, I, ns_log2, grid, d_sub_masks, d_sub_summary);
+		// Mipmapped passes take the AA-capable variant too (three variants per rate).
+		if (p.has_mipmap)
+			launch_shade<true, true>(P, I, ns_log2, grid, d_sub_masks, d_sub_summary);
+		else if (p.has_aa1)
+			launch_shade<true, false>(P, I, ns_log2, grid, d_sub_masks, d_sub_summary);
 		else
-			launch_shade<false>(P, I, ns_log2, grid, d_sub_masks, d_sub_summary);
+			launch_shade<false, false>(P, I, ns_log2, grid, d_sub_masks, d_sub_summary);
 		CUDA_TRY(cudaGetLastError());
 		if (shade_timing)
 			return record_timing_event(shade_ev[1]);
@@ -752,6 +768,7 @@ struct CudaBackend
 		P.states = reinterpret_cast<const pgs_state_vector *>(d_arena + p.states_off);
 		P.textures = reinterpret_cast<const pgs_texture_desc *>(d_arena + p.textures_off);
 		P.tex_images = reinterpret_cast<const TexImage *>(d_arena + p.images_off);
+		P.max_tex_levels = p.max_levels;
 		if (p.num_texels > texels_cap)
 		{
 			cudaFree(d_texels);
@@ -803,7 +820,7 @@ struct CudaBackend
 		}
 		if (p.num_textures && p.num_texels)
 		{
-			dim3 grid((p.max_texels + 255) / 256, p.num_textures);
+			dim3 grid((p.max_texels + 255) / 256, p.num_textures * p.max_levels);
 			texture_decode_kernel<<<grid, 256, 0, stream>>>(P);
 			launch_counter++;
 		}

@@ -363,7 +363,7 @@ struct pgs_gs
 	Instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
 	uint32_t num_instances = 1;
 	uint32_t current_instance = 0;
-	bool has_aa1 = false, has_scanmsk = false;
+	bool has_aa1 = false, has_scanmsk = false, has_mipmap = false;
 	uint32_t clut_instance = 0;
 	uint32_t pending_palette_updates = 0;
 	int32_t ofx = 0, ofy = 0;
@@ -371,7 +371,9 @@ struct pgs_gs
 	// Cached primitive template; recomputed when template_dirty is set.
 	bool template_dirty = true;
 	uint32_t tpl_state = 0, tpl_tex = 0, tpl_tex2 = 0;
-	PageSpan tpl_tex_span = {};
+	// Pages of every sampled mip level of the current template's texture.
+	PageSpan tpl_tex_spans[7] = {};
+	uint32_t tpl_num_tex_spans = 0;
 	bool tpl_has_tex_span = false;
 
 	// Caches of values derived from the register file.  reg_serial changes
@@ -526,6 +528,7 @@ struct pgs_gs
 			rp.flush_reason = reason;
 			rp.has_aa1 = has_aa1;
 			rp.has_scanmsk = has_scanmsk;
+			rp.has_mipmap = has_mipmap;
 
 			uint64_t binning_cost = 0;
 			for (uint32_t i = 0; i < num_instances; i++)
@@ -629,6 +632,7 @@ struct pgs_gs
 		pending_palette_updates = 0;
 		has_aa1 = false;
 		has_scanmsk = false;
+		has_mipmap = false;
 		template_dirty = true;
 		tracker.clear();
 		reserve_buffers();
@@ -1204,10 +1208,11 @@ struct pgs_gs
 
 	// Texture descriptor for the current context (drawing_kick_update_texture,
 	// gs/gs_interface.cpp:1254-1800), without the image cache.
-	uint32_t update_texture(PageSpan &span)
+	uint32_t update_texture(PageSpan *spans, uint32_t &num_spans)
 	{
 		Tex0Reg t(ctx_reg(R_TEX0_1));
 		ClampReg c(ctx_reg(R_CLAMP_1));
+		Tex1Reg tex1(ctx_reg(R_TEX1_1));
 		uint64_t texa = regs[R_TEXA];
 		pgs_texture_desc d = {};
 		d.tbp0 = t.tbp0;
@@ -1248,11 +1253,26 @@ struct pgs_gs
 		}
 
 		uint32_t w = 1u << d.tw_log2, h = 1u << d.th_log2;
-		span = page_span(t.tbp0, 0, 0, w, h, t.tbw ? t.tbw : 1, t.psm);
+		spans[0] = page_span(t.tbp0, 0, 0, w, h, t.tbw ? t.tbw : 1, t.psm);
 		// Large dummy TW/TH with a small stride cover far more pages than are sampled
 		// (compute_has_potential_feedback, gs/gs_util.cpp:81-139).
 		if (w >= 1024 && t.tbw)
-			span = page_span(t.tbp0, 0, 0, std::min<uint32_t>(w, t.tbw * 64), h, t.tbw, t.psm);
+			spans[0] = page_span(t.tbp0, 0, 0, std::min<uint32_t>(w, t.tbw * 64), h, t.tbw, t.psm);
+
+		// Mip chain: MXL only counts with a mipmapping MMIN
+		// (gs/gs_interface.cpp:1538-1582); levels stop at a 1-texel side.
+		d.levels = 1;
+		if (tex1.mmin_has_mipmap())
+			d.levels = std::min<uint32_t>(std::min<uint32_t>(tex1.mxl + 1, std::min(d.tw_log2, d.th_log2) + 1), 7);
+		for (uint32_t l = 1; l < d.levels; l++)
+		{
+			uint64_t m = ctx_reg(l <= 3 ? R_MIPTBP1_1 : R_MIPTBP2_1);
+			uint32_t slot = (l - 1) % 3;
+			uint32_t tbp = field(m, 20 * slot, 14), tbw = field(m, 20 * slot + 14, 6);
+			d.mip[l - 1] = tbp | (tbw << 16);
+			spans[l] = page_span(tbp, 0, 0, w >> l, h >> l, tbw ? tbw : 1, t.psm);
+		}
+		num_spans = d.levels;
 
 		TextureKey key{ d };
 		auto it = texture_map.find(key);
@@ -1279,7 +1299,7 @@ struct pgs_gs
 		{
 			Tex1Reg tex1(ctx_reg(R_TEX1_1));
 			ClampReg clamp(ctx_reg(R_CLAMP_1));
-			uint32_t index = update_texture(tpl_tex_span);
+			uint32_t index = update_texture(tpl_tex_spans, tpl_num_tex_spans);
 			tpl_has_tex_span = true;
 			tex = index;
 			tex |= tex1.mmag ? TEX_SAMPLER_MAG_LINEAR_BIT : 0;
@@ -1291,6 +1311,7 @@ struct pgs_gs
 				tex2 |= tex1.l << 1;
 				tex2 |= tex1.k << 3;
 				tex |= tex1.mxl << TEX_MAX_MIP_LEVEL_OFFSET;
+				has_mipmap = has_mipmap || tex1.mxl != 0;
 				switch (tex1.mmin)
 				{
 				case 1: tex |= TEX_SAMPLER_MIN_LINEAR_BIT; break;
@@ -1501,7 +1522,10 @@ struct pgs_gs
 			uint64_t key[3] = { tpl_serial, tracker.gen[0], tracker.clears };
 			if (memcmp(key, tex_check_key, sizeof(key)) != 0)
 			{
-				if (tracker.any(tpl_tex_span, PageTracker::FB_WRITE))
+				bool hit = false;
+				for (uint32_t l = 0; l < tpl_num_tex_spans; l++)
+					hit = hit || tracker.any(tpl_tex_spans[l], PageTracker::FB_WRITE);
+				if (hit)
 				{
 					flush_render_pass(FLUSH_TEXTURE_HAZARD);
 					check_frame_buffer_state();
@@ -1567,7 +1591,8 @@ struct pgs_gs
 			}
 			if (tpl_has_tex_span && (tex_mark_key[0] != tpl_serial || tex_mark_key[1] != tracker.clears))
 			{
-				tracker.mark(tpl_tex_span, PageTracker::TEX_READ);
+				for (uint32_t l = 0; l < tpl_num_tex_spans; l++)
+					tracker.mark(tpl_tex_spans[l], PageTracker::TEX_READ);
 				tex_mark_key[0] = tpl_serial;
 				tex_mark_key[1] = tracker.clears;
 			}

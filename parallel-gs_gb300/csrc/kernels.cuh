@@ -64,8 +64,11 @@ struct DevInstance
 	uint32_t sub_w, sub_h;        // 8x8 sub-tiles per row / column
 };
 
-// Linear RGBA8 image decoded from swizzled VRAM + CLUT for one texture of a
-// pass (the role of the reference's texture cache, upload.comp:108-229).
+// Linear RGBA8 image decoded from swizzled VRAM + CLUT for one mip level of
+// one texture of a pass (the role of the reference's texture cache,
+// upload.comp:108-229); level l of texture t is entry t * TEX_LEVELS + l.
+constexpr uint32_t TEX_LEVELS = 7;
+
 struct TexImage
 {
 	uint32_t offset; // first texel in PassParams::texels
@@ -111,6 +114,7 @@ struct PassParams
 	TransformedAttr *tattr;
 	uint32_t num_prims;
 	uint32_t num_states, num_textures;
+	uint32_t max_tex_levels;      // largest mip level count of the pass's textures
 	uint32_t tile_size_log2;
 	uint32_t has_aa1, has_scanmsk, has_ss_reference;
 	uint32_t setup_rate_x_log2, setup_rate_y_log2;
@@ -929,9 +933,10 @@ __device__ __forceinline__ uint32_t clut_color(const PassParams &P, const pgs_te
 	return uint32_t(__ldg(cl + bi)) | (uint32_t(__ldg(cl + bi + 256u)) << 16);
 }
 
-__device__ __forceinline__ uint32_t fetch_texel(const PassParams &P, const pgs_texture_desc &t, int32_t x, int32_t y)
+__device__ __forceinline__ uint32_t fetch_texel(const PassParams &P, const pgs_texture_desc &t, uint32_t tbp,
+                                                uint32_t tbw, int32_t x, int32_t y)
 {
-	uint32_t a = swizzle_address(uint32_t(x), uint32_t(y), t.tbp0, t.tbw, t.psm);
+	uint32_t a = swizzle_address(uint32_t(x), uint32_t(y), tbp, tbw, t.psm);
 	const uint8_t *v = P.vram;
 	switch (t.psm)
 	{
@@ -960,65 +965,108 @@ __device__ __forceinline__ int32_t wrap_coord(int32_t v, uint32_t mode, uint32_t
 	}
 }
 
+// One block row per (texture, mip level); level l reads from MIPTBP's base
+// and stride (upload_texture's per-level loop, gs/gs_renderer.cpp:3543-3590).
 __global__ void __launch_bounds__(256) texture_decode_kernel(PassParams P)
 {
-	const uint32_t tex = blockIdx.y;
+	const uint32_t tex = blockIdx.y / P.max_tex_levels, level = blockIdx.y % P.max_tex_levels;
 	if (tex >= P.num_textures)
 		return;
-	const TexImage im = P.tex_images[tex];
+	const pgs_texture_desc t = P.textures[tex];
+	if (level >= max(t.levels, 1u))
+		return;
+	const TexImage im = P.tex_images[tex * TEX_LEVELS + level];
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= im.ext_u * im.ext_v)
 		return;
-	const pgs_texture_desc t = P.textures[tex];
-	P.texels[im.offset + i] = fetch_texel(P, t, int32_t(i % im.ext_u), int32_t(i / im.ext_u));
+	uint32_t tbp = t.tbp0, tbw = t.tbw;
+	if (level)
+	{
+		tbp = t.mip[level - 1] & 0x3fffu;
+		tbw = t.mip[level - 1] >> 16;
+	}
+	P.texels[im.offset + i] = fetch_texel(P, t, tbp, tbw, int32_t(i % im.ext_u), int32_t(i / im.ext_u));
 }
 
-// Texture sample at LOD 0 with exact integer filtering.
-__device__ void sample_texture(const PassParams &P, uint32_t tex_word, float u, float v, bool perspective, float out[4])
+// log2 of a positive normal float: ln m = 2 atanh(s), s = (m - 1) / (m + 1),
+// by the series s + s^3/3 + ... + s^9/9 with m reduced to [sqrt(1/2), sqrt(2)]
+// (|s| <= 0.172, truncation error below 2e-8).  Every operation is rounded on
+// its own, so the CPU restatement computes the same bits.
+__device__ __forceinline__ float lod_log2(float x)
 {
-	const uint32_t tex_index = min(tex_word & TEX_TEXTURE_INDEX_MASK, P.num_textures - 1u);
-	const pgs_texture_desc t = P.textures[tex_index];
-	bool clamp_s = (tex_word & TEX_SAMPLER_CLAMP_S_BIT) != 0;
-	bool clamp_t = (tex_word & TEX_SAMPLER_CLAMP_T_BIT) != 0;
-	bool linear = (tex_word & TEX_SAMPLER_MAG_LINEAR_BIT) != 0;
-	float w = float(1u << t.tw_log2), h = float(1u << t.th_log2);
-	float uu = perspective ? fmul(u, w) : u;
-	float vv = perspective ? fmul(v, h) : v;
+	uint32_t b = f2u(x);
+	int32_t e = int32_t((b >> 23) & 0xffu) - 127;
+	float m = u2f((b & 0x7fffffu) | 0x3f800000u);
+	if (m > 1.41421356f)
+	{
+		m = fmul(m, 0.5f);
+		e++;
+	}
+	float s = __fdiv_rn(fsub(m, 1.0f), fadd(m, 1.0f));
+	float s2 = fmul(s, s);
+	float poly = fadd(fmul(s2, 1.0f / 9.0f), 1.0f / 7.0f);
+	poly = fadd(fmul(s2, poly), 1.0f / 5.0f);
+	poly = fadd(fmul(s2, poly), 1.0f / 3.0f);
+	poly = fadd(fmul(s2, poly), 1.0f);
+	float ln_m = fmul(fmul(2.0f, s), poly);
+	return fadd(__int2float_rn(e), fmul(ln_m, 1.44269504f));
+}
+
+// One filtered sample of mip level `level` (exact integer filtering; the
+// level's coordinates follow sample_texture, ubershader.comp:1133-1151,
+// 1214-1227, with region bounds and masks shifted down by the level as in
+// texture_clamp, :947-953, and upload_texture, gs/gs_renderer.cpp:3578-3590).
+__device__ void sample_level(const PassParams &P, uint32_t tex_index, const pgs_texture_desc &t, uint32_t level,
+                             bool clamp_s, bool clamp_t, bool linear, float u, float v, bool perspective, uint32_t rgba[4])
+{
+	const uint32_t twl = t.tw_log2 - level, thl = t.th_log2 - level;
+	float uu, vv;
+	if (perspective)
+	{
+		uu = fmul(u, float(1u << twl));
+		vv = fmul(v, float(1u << thl));
+	}
+	else
+	{
+		float inv = u2f((127u - level) << 23);
+		uu = fmul(u, inv);
+		vv = fmul(v, inv);
+	}
+	const uint32_t minu = t.minu >> level, maxu = t.maxu >> level, minv = t.minv >> level, maxv = t.maxv >> level;
 	if (clamp_s)
 	{
-		float lo = t.wms == WRAP_REGION_CLAMP ? float(t.minu) : 0.0f;
-		float hi = t.wms == WRAP_REGION_CLAMP ? float(t.maxu) : fsub(w, 1.0f);
-		uu = fminf(fmaxf(uu, fadd(floorf(lo), 0.5f)), fadd(floorf(hi), 0.5f));
+		uint32_t lo = t.wms == WRAP_REGION_CLAMP ? minu : 0u;
+		uint32_t hi = t.wms == WRAP_REGION_CLAMP ? maxu : (1u << twl) - 1u;
+		uu = fminf(fmaxf(uu, fadd(float(lo), 0.5f)), fadd(float(hi), 0.5f));
 	}
 	if (clamp_t)
 	{
-		float lo = t.wmt == WRAP_REGION_CLAMP ? float(t.minv) : 0.0f;
-		float hi = t.wmt == WRAP_REGION_CLAMP ? float(t.maxv) : fsub(h, 1.0f);
-		vv = fminf(fmaxf(vv, fadd(floorf(lo), 0.5f)), fadd(floorf(hi), 0.5f));
+		uint32_t lo = t.wmt == WRAP_REGION_CLAMP ? minv : 0u;
+		uint32_t hi = t.wmt == WRAP_REGION_CLAMP ? maxv : (1u << thl) - 1u;
+		vv = fminf(fmaxf(vv, fadd(float(lo), 0.5f)), fadd(float(hi), 0.5f));
 	}
 	int32_t ku = int32_t(floorf(fadd(fmul(uu, 16.0f), 1.0f / 64.0f)));
 	int32_t kv = int32_t(floorf(fadd(fmul(vv, 16.0f), 1.0f / 64.0f)));
+	const TexImage im = P.tex_images[tex_index * TEX_LEVELS + level];
+	const uint32_t *img = P.texels + im.offset;
 	if (!linear)
 	{
-		int32_t x = wrap_coord(ku >> 4, t.wms, t.tw_log2, t.minu, t.maxu);
-		int32_t y = wrap_coord(kv >> 4, t.wmt, t.th_log2, t.minv, t.maxv);
-		const TexImage im = P.tex_images[tex_index];
-		uint32_t c = __ldg(P.texels + im.offset + uint32_t(y) * im.ext_u + uint32_t(x));
+		int32_t x = wrap_coord(ku >> 4, t.wms, twl, minu, maxu);
+		int32_t y = wrap_coord(kv >> 4, t.wmt, thl, minv, maxv);
+		uint32_t c = __ldg(img + uint32_t(y) * im.ext_u + uint32_t(x));
 		#pragma unroll
 		for (int k = 0; k < 4; k++)
-			out[k] = float((c >> (8 * k)) & 0xffu);
+			rgba[k] = (c >> (8 * k)) & 0xffu;
 		return;
 	}
 	int32_t bu = ku - 8, bv = kv - 8;
 	int32_t x0 = bu >> 4, y0 = bv >> 4;
 	uint32_t fx = uint32_t(bu) & 15u, fy = uint32_t(bv) & 15u;
-	int32_t xs0 = wrap_coord(x0, t.wms, t.tw_log2, t.minu, t.maxu);
-	int32_t xs1 = wrap_coord(x0 + 1, t.wms, t.tw_log2, t.minu, t.maxu);
-	int32_t ys0 = wrap_coord(y0, t.wmt, t.th_log2, t.minv, t.maxv);
-	int32_t ys1 = wrap_coord(y0 + 1, t.wmt, t.th_log2, t.minv, t.maxv);
+	int32_t xs0 = wrap_coord(x0, t.wms, twl, minu, maxu);
+	int32_t xs1 = wrap_coord(x0 + 1, t.wms, twl, minu, maxu);
+	int32_t ys0 = wrap_coord(y0, t.wmt, thl, minv, maxv);
+	int32_t ys1 = wrap_coord(y0 + 1, t.wmt, thl, minv, maxv);
 	uint32_t w00 = (16u - fx) * (16u - fy), w10 = fx * (16u - fy), w01 = (16u - fx) * fy, w11 = fx * fy;
-	const TexImage im = P.tex_images[tex_index];
-	const uint32_t *img = P.texels + im.offset;
 	const uint32_t *row0 = img + uint32_t(ys0) * im.ext_u, *row1 = img + uint32_t(ys1) * im.ext_u;
 	uint32_t c00 = __ldg(row0 + xs0);
 	uint32_t c10 = __ldg(row0 + xs1);
@@ -1033,7 +1081,84 @@ __device__ void sample_texture(const PassParams &P, uint32_t tex_word, float u, 
 		uint32_t q = acc >> 8, r = acc & 0xffu;
 		if (r > 128u || (r == 128u && (q & 1u)))
 			q++;
-		out[k] = float(q);
+		rgba[k] = q;
+	}
+}
+
+// Level of detail and filter choice (sample_texture, ubershader.comp:1064-1131):
+// LOD = ceil(-log2|Q| * 2^(L+4) + K) / 16 or the fixed K >> 4, clamped to
+// [0, MXL]; MMIN applies when the LOD is positive; trilinear blends the next
+// level by floor(fract * 16) / 16.  Levels beyond the texture's chain read its
+// last level.  Returns level | next level << 4 | weight of the next level << 8
+// | linear << 16.
+__device__ __forceinline__ uint32_t select_lod(uint32_t levels, uint32_t tex_word, uint32_t tex2, float q)
+{
+	const bool mag_linear = (tex_word & TEX_SAMPLER_MAG_LINEAR_BIT) != 0;
+	const bool min_linear = (tex_word & TEX_SAMPLER_MIN_LINEAR_BIT) != 0;
+	const uint32_t max_mip = (tex_word >> TEX_MAX_MIP_LEVEL_OFFSET) & 7u;
+	const int32_t K = int32_t(tex2 << 17) >> 20; // signed 12-bit field at bit 3
+	float lod;
+	bool linear;
+	if ((tex2 & TEX2_FIXED_LOD_BIT) == 0)
+	{
+		const uint32_t L = (tex2 >> 1) & 3u;
+		float aq = fabsf(q), formula = 0.0f;
+		if (aq >= 1.17549435e-38f && aq <= 3.40282347e38f)
+			formula = fadd(fmul(-lod_log2(aq), float(1u << (L + 4))), __int2float_rn(K));
+		lod = fmul(ceilf(formula), 0.0625f);
+		linear = formula > 0.0f ? min_linear : mag_linear;
+	}
+	else
+	{
+		lod = __int2float_rn(K >> 4);
+		linear = lod > 0.0f ? min_linear : mag_linear;
+	}
+	lod = fminf(fmaxf(lod, 0.0f), float(max_mip));
+	float l1 = floorf(lod), l2 = ceilf(lod);
+	uint32_t weight = uint32_t(fmul(fsub(lod, l1), 16.0f));
+	if ((tex_word & TEX_SAMPLER_MIPMAP_LINEAR_BIT) == 0)
+	{
+		weight = 0;
+		l1 = float(int32_t(fadd(lod, 0.5f)));
+	}
+	const uint32_t last = max(levels, 1u) - 1u;
+	return min(uint32_t(l1), last) | (min(uint32_t(l2), last) << 4) | (weight << 8) | (uint32_t(linear) << 16);
+}
+
+// MIP: the pass samples mip levels (some primitive has TEX1.MXL > 0 with a
+// mipmapping MMIN); without it every sample reads level 0 through MMAG.
+template <bool MIP>
+__device__ void sample_texture(const PassParams &P, uint32_t tex_word, uint32_t tex2, float u, float v, float q,
+                               bool perspective, float out[4])
+{
+	const uint32_t tex_index = min(tex_word & TEX_TEXTURE_INDEX_MASK, P.num_textures - 1u);
+	const pgs_texture_desc t = P.textures[tex_index];
+	const bool clamp_s = (tex_word & TEX_SAMPLER_CLAMP_S_BIT) != 0;
+	const bool clamp_t = (tex_word & TEX_SAMPLER_CLAMP_T_BIT) != 0;
+	uint32_t sel = (tex_word & TEX_SAMPLER_MAG_LINEAR_BIT) ? (1u << 16) : 0u;
+	if (MIP && ((tex_word >> TEX_MAX_MIP_LEVEL_OFFSET) & 7u))
+		sel = select_lod(t.levels, tex_word, tex2, q);
+	// One pass per sampled level: weight 16 - w on the first, w on the second,
+	// then roundEven(sum / 16) (exact for a single level).
+	const uint32_t weight = (sel >> 8) & 0xffu;
+	uint32_t acc[4] = { 0, 0, 0, 0 };
+	for (uint32_t pass = 0; pass < (weight ? 2u : 1u); pass++)
+	{
+		uint32_t c[4];
+		sample_level(P, tex_index, t, pass ? ((sel >> 4) & 15u) : (sel & 15u), clamp_s, clamp_t, (sel >> 16) != 0,
+		             u, v, perspective, c);
+		const uint32_t w = pass ? weight : 16u - weight;
+		#pragma unroll
+		for (int k = 0; k < 4; k++)
+			acc[k] += w * c[k];
+	}
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		uint32_t r = acc[k] >> 4, f = acc[k] & 15u;
+		if (f > 8u || (f == 8u && (r & 1u)))
+			r++;
+		out[k] = float(r);
 	}
 }
 
@@ -1043,6 +1168,7 @@ __device__ __forceinline__ float interp(float c0, float d1, float d2, float i, f
 	return fadd(fadd(c0, fmul(d1, i)), fmul(d2, j));
 }
 
+template <bool MIP>
 __device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r, bool perspective, uint32_t combiner,
                                float cc[4])
 {
@@ -1072,7 +1198,7 @@ __device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r,
 		s = fminf(fmaxf(s, -2047.0f), 2047.0f);
 		t = fminf(fmaxf(t, -2047.0f), 2047.0f);
 		float tx[4];
-		sample_texture(P, P.prims[pi].tex, s, t, perspective, tx);
+		sample_texture<MIP>(P, P.prims[pi].tex, P.prims[pi].tex2, s, t, q, perspective, tx);
 		if (mode == COMBINER_DECAL)
 		{
 			cc[0] = tx[0]; cc[1] = tx[1]; cc[2] = tx[2]; cc[3] = tcc ? tx[3] : col[3];
@@ -1126,6 +1252,7 @@ struct SampleState
 	uint32_t pending_prim;
 };
 
+template <bool MIP>
 __device__ void shade_resolve(const ShadeCtx &C, SampleState &S)
 {
 	const PassParams &P = *C.P;
@@ -1141,7 +1268,7 @@ __device__ void shade_resolve(const ShadeCtx &C, SampleState &S)
 	}
 	const bool multisample = (pst >> STATE_BIT_MULTISAMPLE) & 1;
 	float cc[4];
-	combined_color(C, pi, r, (pst >> STATE_BIT_PERSPECTIVE) & 1, sv.combiner, cc);
+	combined_color<MIP>(C, pi, r, (pst >> STATE_BIT_PERSPECTIVE) & 1, sv.combiner, cc);
 	float fbc[4];
 	#pragma unroll
 	for (int k = 0; k < 4; k++)
@@ -1440,7 +1567,7 @@ __device__ __forceinline__ void sample_offset(uint32_t s, uint32_t xl, uint32_t 
 // (primitive_intersects_tile); a second test against each warp's smaller
 // rectangle costs more than the coverage test it would skip, so coverage
 // alone decides.
-template <bool SS, bool AA>
+template <bool SS, bool AA, bool MIP>
 __device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi, SampleState &S, uint32_t &covered)
 {
 	const PassParams &P = *C.P;
@@ -1496,7 +1623,7 @@ __device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi
 	if (__any_sync(0xffffffffu, need_flush))
 	{
 		if (S.pending.coverage > 0)
-			shade_resolve(C, S);
+			shade_resolve<MIP>(C, S);
 		S.pending.coverage = 0;
 		S.pending.z_write = false;
 		if (q.coverage > 0)
@@ -1528,7 +1655,7 @@ __device__ __forceinline__ uint32_t subtile_mode(const PassParams &P, const DevI
 // One sub-tile's pixel samples; `t` is the thread's index among the 64 * NS
 // threads that cover the sub-tile.  Warps are independent: each walks the
 // sub-tile's primitive bitmask on its own and needs no barrier.
-template <int NS, bool SS, bool AA>
+template <int NS, bool SS, bool AA, bool MIP = false>
 __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInstance &I, const uint32_t *sub_masks,
                                               const uint32_t *sub_summary, uint32_t sub, uint32_t t)
 {
@@ -1638,14 +1765,14 @@ __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInst
 				{
 					int b = __ffs(m) - 1;
 					m &= m - 1u;
-					process_primitive<SS, AA>(C, prim_base + uint32_t(b), S, covered);
+					process_primitive<SS, AA, MIP>(C, prim_base + uint32_t(b), S, covered);
 				}
 			}
 		}
 	}
 
 	if (S.pending.coverage > 0)
-		shade_resolve(C, S);
+		shade_resolve<MIP>(C, S);
 
 	// Covered-sample counter: one atomic per warp.
 	{
@@ -1759,7 +1886,7 @@ __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInst
 	}
 }
 
-template <int NS, bool SS, bool AA>
+template <int NS, bool SS, bool AA, bool MIP>
 __global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kernel(PassParams P, DevInstance I, const uint32_t *sub_masks,
                                                         const uint32_t *sub_summary, const uint32_t *tile_flags)
 {
@@ -1768,7 +1895,7 @@ __global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kerne
 		return;
 	if (subtile_mode(P, I, tile_flags, sub) != (SS ? 2u : 1u))
 		return;
-	shade_subtile<NS, SS, AA>(P, I, sub_masks, sub_summary, sub, threadIdx.x);
+	shade_subtile<NS, SS, AA, MIP>(P, I, sub_masks, sub_summary, sub, threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------

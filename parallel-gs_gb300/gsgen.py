@@ -770,6 +770,133 @@ def frame_fuzz(seed: int, draws: int = 40, width: int = 256, height: int = 224) 
                  {"width": width, "height": height, "fbp": 0, "zbp": zbp})
 
 
+MIPTBP1_1, MIPTBP2_1 = 0x34, 0x36
+
+
+def miptbp_reg(levels: list[tuple[int, int]]) -> int:
+    """MIPTBP1 / MIPTBP2 payload from up to three (TBP, TBW) pairs."""
+    v = 0
+    for i, (tbp, tbw) in enumerate(levels):
+        v |= (tbp & 0x3FFF) << (20 * i) | (tbw & 0x3F) << (20 * i + 14)
+    return v
+
+
+# Page size in pixels (width, height) per format, for laying out mip levels.
+_PAGE_DIMS = {PSMCT32: (64, 32), PSMCT16: (64, 64), PSMT8: (128, 64), PSMT4: (128, 128)}
+_BLOCK_LOG2 = {PSMCT32: (3, 3), PSMCT16: (4, 3), PSMT8: (4, 4), PSMT4: (5, 4)}
+
+
+def frame_mip(seed: int, draws: int = 30, width: int = 256, height: int = 224) -> Frame:
+    """Mipmapping coverage: mip chains of 2-7 levels in CT32 / CT16 / PSMT8 /
+    PSMT4 (CLUT) with level bases from MIPTBP1 / MIPTBP2 or generated by
+    TEX1.MTBA; draws with every MMIN mode, MMAG, MXL (also past the chain), L,
+    signed K, fixed LOD (LCM), perspective STQ with Q over [1/16, 16] and UV
+    addressing, all wrap modes; random sampling rate."""
+    rng = np.random.Generator(np.random.PCG64(70000 + seed))
+    s = GifStream()
+    fpsm = [PSMCT32, PSMCT16][int(rng.integers(0, 2))]
+    zpsm = PSMZ24
+    fbw = width // 64
+    zbp = 32
+    ss, ordered = [(1, True), (2, True), (4, True), (4, False), (8, True), (16, True)][int(rng.integers(0, 6))]
+    s.ad([(PRMODECONT, 1), (FRAME_1, frame_reg(0, fbw, fpsm)), (ZBUF_1, zbuf_reg(zbp, zpsm)),
+          (SCISSOR_1, scissor_reg(0, width - 1, 0, height - 1)), (XYOFFSET_1, 0), (COLCLAMP, 1)])
+    texs = []
+    page = 64
+    for ti in range(4):
+        psm = [PSMCT32, PSMCT16, PSMT8, PSMT4][ti]
+        auto = ti < 3 and rng.uniform() < 0.5
+        tw = 8 if auto else int(rng.integers(2, 9))
+        th = int(rng.integers(6, 9)) if auto else int(rng.integers(2, 9))
+        bpp = {PSMCT32: 32, PSMCT16: 16, PSMT8: 8, PSMT4: 4}[psm]
+        nlev = min(tw, th) + 1
+        levels = []
+        if auto:
+            # TEX1.MTBA layout (gs/gs_interface.cpp:805-843): levels 1-3 follow
+            # level 0 block by block, the buffer width halving each level.
+            bwl, bhl = _BLOCK_LOG2[psm]
+            base = page * BLOCKS_PER_PAGE
+            row = (1 << tw) // 64
+            blocks = ((1 << tw) >> bwl) * ((1 << th) >> bhl)
+            for lv in range(min(nlev, 4)):
+                levels.append((base, row))
+                base += blocks
+                blocks //= 4
+                row //= 2
+            page = (base + BLOCKS_PER_PAGE - 1) // BLOCKS_PER_PAGE + 1
+            nlev = len(levels)
+        else:
+            pw, ph = _PAGE_DIMS[psm]
+            for lv in range(min(nlev, 7)):
+                wl, hl = (1 << tw) >> lv, (1 << th) >> lv
+                tbw = max(1, wl // 64)
+                if psm in (PSMT8, PSMT4):
+                    tbw = max(2, tbw)
+                levels.append((page * BLOCKS_PER_PAGE, tbw))
+                page += max(1, (tbw * 64 + pw - 1) // pw) * ((hl + ph - 1) // ph)
+        for lv, (tbp, tbw) in enumerate(levels):
+            wl, hl = (1 << tw) >> lv, (1 << th) >> lv
+            data = rng.integers(0, 256, size=max(16, wl * hl * bpp // 8), dtype=np.uint8).tobytes()
+            s.upload(tbp, tbw, psm, 0, 0, wl, hl, data[:max(1, wl * hl * bpp // 8)])
+        cpsm = cbp = cld = 0
+        if psm in (PSMT8, PSMT4):
+            cpsm = PSMCT32 if rng.uniform() < 0.5 else PSMCT16
+            cw, ch = (16, 16) if psm == PSMT8 else (8, 2)
+            cbp = page * BLOCKS_PER_PAGE
+            clut = rng.integers(0, 256, size=cw * ch * (4 if cpsm == PSMCT32 else 2), dtype=np.uint8).tobytes()
+            s.upload(cbp, 1, cpsm, 0, 0, cw, ch, clut)
+            page += 1
+            cld = 1
+        texs.append((psm, tw, th, levels, auto, cbp, cpsm, cld))
+    assert page * PAGE_BYTES <= 4 * 1024 * 1024
+    for d in range(draws):
+        psm, tw, th, levels, auto, cbp, cpsm, cld = texs[int(rng.integers(0, len(texs)))]
+        w, h = 1 << tw, 1 << th
+        lcm = int(rng.uniform() < 0.25)
+        k = int(rng.integers(-32, 113)) if lcm else int(rng.integers(-96, 97))
+        tex1 = tex1_reg(lcm=lcm, mxl=int(rng.integers(0, 8)), mmag=int(rng.integers(0, 2)),
+                        mmin=int(rng.integers(0, 6)), mtba=int(auto), l=int(rng.integers(0, 4)), k=k & 0xFFF)
+        regs = [(TEST_1, test_reg(zte=1, ztst=1)), (ALPHA_1, alpha_reg(0, 1, 0, 1)),
+                (TEX1_1, tex1)]
+        if not auto:
+            regs.append((MIPTBP1_1, miptbp_reg(levels[1:4])))
+            regs.append((MIPTBP2_1, miptbp_reg(levels[4:7])))
+        regs.append((TEX0_1, tex0_reg(levels[0][0], levels[0][1], psm, tw, th, tcc=1, tfx=int(rng.integers(0, 2)),
+                                      cbp=cbp, cpsm=cpsm, cld=cld)))
+        wm = [int(rng.integers(0, 4)), int(rng.integers(0, 4))]
+        lo_u, lo_v = int(rng.integers(0, w)), int(rng.integers(0, h))
+        regs.append((CLAMP_1, clamp_reg(wm[0], wm[1], lo_u, int(rng.integers(lo_u, w)) if wm[0] == 2 else
+                                        int(rng.integers(0, w)), lo_v,
+                                        int(rng.integers(lo_v, h)) if wm[1] == 2 else int(rng.integers(0, h)))))
+        s.ad(regs)
+        prim = [PRIM_TRI, PRIM_TRISTRIP, PRIM_SPRITE][int(rng.integers(0, 3))]
+        fst = int(rng.uniform() < 0.3)
+        nv = int(rng.integers(3, 24)) if prim != PRIM_SPRITE else 2 * int(rng.integers(1, 8))
+        x = np.round(rng.uniform(-16, width + 16, nv) * 16).astype(np.int64) & 0xFFFF
+        y = np.round(rng.uniform(-16, height + 16, nv) * 16).astype(np.int64) & 0xFFFF
+        z = rng.integers(0, 1 << 24, nv, dtype=np.int64)
+        rgba = rng.integers(0, 256, size=(nv, 4), dtype=np.int64)
+        desc = [D_RGBAQ]
+        q = [q_rgbaq(rgba)]
+        if fst:
+            desc.append(D_UV)
+            q.append(q_uv(rng.integers(0, 4 * w * 16, nv) - w * 16 // 2 & 0x3FFF,
+                          rng.integers(0, 4 * h * 16, nv) - h * 16 // 2 & 0x3FFF))
+        else:
+            qq = np.exp2(rng.uniform(-4, 4, nv)).astype(np.float32)
+            if rng.uniform() < 0.3:
+                qq[:] = qq[0]
+            desc.append(D_ST)
+            q.append(q_st((rng.uniform(-0.5, 1.5, nv) * qq).astype(np.float32),
+                          (rng.uniform(-0.5, 1.5, nv) * qq).astype(np.float32), qq))
+        desc.append(D_XYZ2)
+        q.append(q_xyz2(x, y, z))
+        data = np.stack(q, axis=1).reshape(-1, 2)
+        s.packed(prim_reg(prim, iip=1, tme=1, fst=fst, abe=int(rng.uniform() < 0.3)), desc, data)
+    return Frame("mip_%d" % seed, s.tobytes(), ss, ordered, draws,
+                 {"width": width, "height": height, "fbp": 0, "zbp": zbp})
+
+
 def write_dump(path, transfers, vram: bytes | None = None, regs: dict | None = None, version: int = 9,
                serial: bytes = b"", vsync_fields=(0,)) -> None:
     """Writes a GS dump in the PCSX2 / GSdx layout (GSDumpGenerator::init,

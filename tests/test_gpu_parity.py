@@ -200,3 +200,12 @@ def test_feature_fuzz(seed):
     f = gsgen.frame_fuzz(seed)
     ref, out = run_both(f)
     assert_same(ref, out)
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_mipmap_parity(seed):
+    """Mip chains (MIPTBP1/2 and MTBA bases), every MMIN mode, LOD from Q with L
+    and signed K, fixed LOD, trilinear, wrap modes, random sampling rate."""
+    f = gsgen.frame_mip(seed)
+    ref, out = run_both(f)
+    assert_same(ref, out)
