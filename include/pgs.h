@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define PGS_ABI_VERSION 2u
+#define PGS_ABI_VERSION 3u
 
 /* ------------------------------------------------------------------ */
 /* Status codes                                                        */
@@ -214,6 +214,35 @@ typedef struct pgs_circuit_params
 	uint32_t valid_width, valid_height; /* sampled part (scissor) */
 } pgs_circuit_params;
 
+/* Output merge of one vsync (GSRenderer::vsync, gs/gs_renderer.cpp:4189-5055),
+ * computed by the frontend from the privileged registers; a backend samples the
+ * circuits, composes them, performs the EXTWRITE write-back into VRAM and
+ * deinterlaces. */
+typedef struct pgs_merge_params
+{
+	pgs_circuit_params circuit[2]; /* read-out of each circuit; width == 0: not sampled */
+	int32_t rect_x[2], rect_y[2];  /* viewport of each circuit in the merged image */
+	uint32_t rect_w[2], rect_h[2]; /* 0 x 0: circuit not drawn */
+	uint32_t width, height;        /* merged image */
+	uint32_t draw_circuit2;        /* SLBG = 0: circuit 2 is drawn first, unblended */
+	uint32_t draw_circuit1;
+	uint32_t blend;                /* circuit 1 over circuit 2 / background: 0 replace,
+	                                * 1 constant ALP, 2 circuit 1 alpha (PMODE.MMOD) */
+	uint32_t alp;
+	uint32_t bgcolor;              /* background RGB (BGCOLOR); background alpha is 0 */
+	/* EXTWRITE feedback write (extwrite.comp:37-98). */
+	uint32_t ext_write;
+	uint32_t ext_source;           /* 0 merged image, 1 circuit 2, 2 circuit 1 */
+	uint32_t ext_width, ext_height;
+	uint32_t ext_wdx, ext_wdy, ext_exbp, ext_exbw, ext_emoda, ext_emodc;
+	float ext_uv_base[2], ext_uv_scale[2];
+	/* FastMAD deinterlace over the last four merged fields (weave.frag). */
+	uint32_t deinterlace;          /* 0: output the merged image, drop the field history */
+	uint32_t phase;
+	uint32_t raw_circuit;          /* 1 / 2: output that circuit's read-out as it is */
+	uint32_t padding;
+} pgs_merge_params;
+
 typedef struct pgs_backend_ops
 {
 	uint32_t abi_version;
@@ -257,6 +286,10 @@ typedef struct pgs_backend_ops
 	/* abi_version >= 2, optional: CRTC circuit read-out of the current VRAM into
 	 * host memory dst (params->width * params->height * 4 bytes). */
 	int (*sample_circuit)(void *self, const pgs_circuit_params *params, void *dst);
+	/* abi_version >= 3, optional: one vsync's output into host memory dst
+	 * (raw circuit: its read-out; deinterlaced: width x 2 * height; else
+	 * width x height RGBA8). */
+	int (*vsync)(void *self, const pgs_merge_params *params, void *dst);
 } pgs_backend_ops;
 
 /* ------------------------------------------------------------------ */
@@ -492,6 +525,43 @@ int pgs_gs_read_priv_register(pgs_gs *gs, uint32_t index, uint64_t *value);
  * timings are not applied. */
 int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_t flags, void *dst, uint64_t dst_size,
                            uint32_t *width, uint32_t *height);
+
+/* vsync (GSInterface::vsync -> GSRenderer::vsync, gs/gs_renderer.cpp:4189-5055):
+ * the display mode from SMODE1/SMODE2, both circuits per PMODE/DISPFB/DISPLAY,
+ * merged over BGCOLOR with ALP or circuit-1 alpha, the EXTWRITE write-back into
+ * VRAM, and a FastMAD deinterlace of interlaced output.  dst receives
+ * result->width x result->height RGBA8; when dst_size is too small nothing
+ * runs and PGS_ERROR_CAPACITY is returned with *result filled in.  An unknown
+ * video mode returns PGS_OK with a 0 x 0 image. */
+#define PGS_VSYNC_FORCE_PROGRESSIVE 1u
+#define PGS_VSYNC_HIGH_RESOLUTION 2u
+#define PGS_VSYNC_OVERSCAN 4u
+#define PGS_VSYNC_CRTC_OFFSETS 8u
+#define PGS_VSYNC_ANTI_BLUR 16u
+#define PGS_VSYNC_ADAPT_HORIZONTAL 32u
+#define PGS_VSYNC_RAW_CIRCUIT 64u
+#define PGS_VSYNC_SKIP_DEINTERLACE 128u
+/* Largest image pgs_gs_vsync writes (1920 x 1080 doubled by high-resolution
+ * read-out). */
+#define PGS_VSYNC_MAX_BYTES (3840ull * 2160ull * 4ull)
+
+typedef struct pgs_vsync_info
+{
+	uint32_t phase; /* field, 0 or 1 */
+	uint32_t flags; /* PGS_VSYNC_* */
+} pgs_vsync_info;
+
+typedef struct pgs_scanout_result
+{
+	uint32_t width, height; /* image written to dst */
+	uint32_t mode_width, mode_height;
+	uint32_t internal_width, internal_height;
+	uint32_t interlaced, interlace_phase, double_strike, high_resolution_scanout;
+	float sampling_rate_mhz;
+	uint32_t padding;
+} pgs_scanout_result;
+
+int pgs_gs_vsync(pgs_gs *gs, const pgs_vsync_info *info, void *dst, uint64_t dst_size, pgs_scanout_result *result);
 /* GSInterface::map_vram_write + end_vram_write. */
 int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *src);
 /* GSInterface::read_transfer_fifo. */

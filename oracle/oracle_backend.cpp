@@ -237,6 +237,9 @@ struct Backend
 	uint32_t rate_x = 0, rate_y = 0;
 	uint32_t num_planes = 1;
 	std::vector<uint8_t> vram;
+	// Deinterlacer history: the last four merged fields, newest first.
+	std::vector<uint32_t> fields[4];
+	uint32_t field_w = 0, field_h = 0;
 	std::vector<uint16_t> clut;
 	uint32_t last_clut_instance = 0;
 	std::vector<pgs_vertex_position> res_pos;
@@ -2383,9 +2386,238 @@ static int o_circuit(void *self, const pgs_circuit_params *cp, void *dst)
 	return 0;
 }
 
+// ---------------------------------------------------------------------------
+// vsync (GSRenderer::vsync, gs/gs_renderer.cpp:4738-5055; extwrite.comp:37-98;
+// weave.frag): restated with the definitions the CUDA backend uses for what
+// the reference leaves to the rasteriser -- an 8-bit sub-texel bilinear
+// stretch clamped to the edge, integer blends rounded to nearest, float
+// expressions evaluated left to right with one rounding per operation.
+
+static uint32_t stretch_sample(const std::vector<uint32_t> &img, uint32_t iw, uint32_t ih, int32_t dx, int32_t dy,
+                               uint32_t vw, uint32_t vh)
+{
+	int64_t fx = (int64_t(2 * dx + 1) * iw * 256) / (2 * int64_t(vw)) - 128;
+	int64_t fy = (int64_t(2 * dy + 1) * ih * 256) / (2 * int64_t(vh)) - 128;
+	int32_t x0 = int32_t(fx >> 8), y0 = int32_t(fy >> 8);
+	uint32_t wx = uint32_t(fx & 255), wy = uint32_t(fy & 255);
+	auto cl = [](int32_t v, uint32_t n) { return uint32_t(std::min(std::max(v, 0), int32_t(n) - 1)); };
+	uint32_t xs[2] = { cl(x0, iw), cl(x0 + 1, iw) }, ys[2] = { cl(y0, ih), cl(y0 + 1, ih) };
+	uint32_t wxs[2] = { 256 - wx, wx }, wys[2] = { 256 - wy, wy };
+	uint32_t out = 0;
+	for (int k = 0; k < 4; k++)
+	{
+		uint32_t acc = 0;
+		for (int j = 0; j < 2; j++)
+			for (int i = 0; i < 2; i++)
+				acc += wxs[i] * wys[j] * ((img[size_t(ys[j]) * iw + xs[i]] >> (8 * k)) & 255u);
+		out |= ((acc + 32768u) >> 16) << (8 * k);
+	}
+	return out;
+}
+
+static uint32_t blend255(uint32_t s, uint32_t d, uint32_t a)
+{
+	uint32_t v = s * a + d * (255 - a);
+	uint32_t q = v / 255, r = v % 255;
+	return q + (2 * r > 255 ? 1 : 0);
+}
+
+static float luma_diff(uint32_t a, uint32_t b)
+{
+	float dr = oracle::unorm(a, 0) - oracle::unorm(b, 0);
+	float dg = oracle::unorm(a, 1) - oracle::unorm(b, 1);
+	float db = oracle::unorm(a, 2) - oracle::unorm(b, 2);
+	float s = dr * 0.299f;
+	s = s + dg * 0.587f;
+	s = s + db * 0.114f;
+	return std::fabs(s);
+}
+
+static int o_vsync(void *self, const pgs_merge_params *mp, void *dst)
+{
+	if (!mp || !dst)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	const pgs_merge_params &M = *mp;
+	auto *b = static_cast<Backend *>(self);
+	std::vector<uint32_t> circ[2];
+	for (int i = 0; i < 2; i++)
+	{
+		const pgs_circuit_params &c = M.circuit[i];
+		if (size_t(c.width) * c.height == 0)
+			continue;
+		if (c.width > 4096 || c.height > 4096)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		circ[i].resize(size_t(c.width) * c.height);
+		int r = o_circuit(self, &c, circ[i].data());
+		if (r)
+			return r;
+	}
+	uint32_t *out = static_cast<uint32_t *>(dst);
+	if (M.raw_circuit == 1 || M.raw_circuit == 2)
+	{
+		const auto &c = circ[M.raw_circuit - 1];
+		if (!c.empty())
+			memcpy(out, c.data(), c.size() * 4);
+		return 0;
+	}
+	if (M.width == 0 || M.height == 0)
+		return 0;
+	if (M.width > 4096 || M.height > 4096)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if ((M.draw_circuit1 && circ[0].empty()) || (M.draw_circuit2 && circ[1].empty()))
+		return PGS_ERROR_INVALID_ARGUMENT;
+	const uint32_t W = M.width, H = M.height;
+	std::vector<uint32_t> merged(size_t(W) * H);
+	auto inside = [&](int i, int32_t x, int32_t y) {
+		return M.rect_w[i] && M.rect_h[i] && x >= M.rect_x[i] && x < M.rect_x[i] + int32_t(M.rect_w[i]) &&
+		       y >= M.rect_y[i] && y < M.rect_y[i] + int32_t(M.rect_h[i]);
+	};
+	for (uint32_t y = 0; y < H; y++)
+		for (uint32_t x = 0; x < W; x++)
+		{
+			int32_t ix = int32_t(x), iy = int32_t(y);
+			uint32_t color = M.bgcolor & 0xffffffu;
+			if (M.draw_circuit2 && inside(1, ix, iy))
+				color = stretch_sample(circ[1], M.circuit[1].width, M.circuit[1].height, ix - M.rect_x[1],
+				                       iy - M.rect_y[1], M.rect_w[1], M.rect_h[1]);
+			if (M.draw_circuit1 && inside(0, ix, iy))
+			{
+				uint32_t s = stretch_sample(circ[0], M.circuit[0].width, M.circuit[0].height, ix - M.rect_x[0],
+				                            iy - M.rect_y[0], M.rect_w[0], M.rect_h[0]);
+				if (M.blend == 0)
+					color = s;
+				else
+				{
+					uint32_t a = M.blend == 1 ? M.alp : (s >> 24);
+					uint32_t o = s & 0xff000000u;
+					for (int k = 0; k < 3; k++)
+						o |= blend255((s >> (8 * k)) & 255u, (color >> (8 * k)) & 255u, a) << (8 * k);
+					color = o;
+				}
+			}
+			merged[size_t(y) * W + x] = color;
+		}
+
+	if (M.ext_write && M.ext_width && M.ext_height)
+	{
+		const std::vector<uint32_t> *src = &merged;
+		uint32_t sw = W, sh = H;
+		if (M.ext_source == 1 || M.ext_source == 2)
+		{
+			int ci = M.ext_source == 1 ? 1 : 0;
+			if (circ[ci].empty())
+				return PGS_ERROR_INVALID_ARGUMENT;
+			src = &circ[ci];
+			sw = M.circuit[ci].width;
+			sh = M.circuit[ci].height;
+		}
+		if (M.ext_width > 4096 || M.ext_height > 4096)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		for (uint32_t gy = 0; gy < M.ext_height; gy++)
+			for (uint32_t gx = 0; gx < M.ext_width; gx++)
+			{
+				float u = M.ext_uv_base[0] + float(gx) * M.ext_uv_scale[0];
+				float v = M.ext_uv_base[1] + float(gy) * M.ext_uv_scale[1];
+				int32_t tx = std::min(std::max(int32_t(std::floor(u * float(sw))), 0), int32_t(sw) - 1);
+				int32_t ty = std::min(std::max(int32_t(std::floor(v * float(sh))), 0), int32_t(sh) - 1);
+				uint32_t c = (*src)[size_t(ty) * sw + tx];
+				float r = oracle::unorm(c, 0), g = oracle::unorm(c, 1), bb = oracle::unorm(c, 2), a = oracle::unorm(c, 3);
+				float ey = 0.587f * g;
+				ey = ey + 0.114f * bb;
+				ey = ey + 0.299f * r;
+				float ecb = -0.311f * g;
+				ecb = ecb + 0.500f * bb;
+				ecb = ecb - 0.169f * r;
+				float ecr = -0.419f * g;
+				ecr = ecr - 0.081f * bb;
+				ecr = ecr + 0.500f * r;
+				float Y = (219.0f * ey + 16.0f) / 255.0f;
+				float Cb = (224.0f * ecb + 128.0f) / 255.0f;
+				float Cr = (224.0f * ecr + 128.0f) / 255.0f;
+				float o[4];
+				switch (M.ext_emodc)
+				{
+				case 0: o[0] = r; o[1] = g; o[2] = bb; break;
+				case 1: o[0] = Y; o[1] = Y; o[2] = Y; break;
+				case 2: o[0] = Y; o[1] = Cb; o[2] = Cr; break;
+				default: o[0] = a; o[1] = a; o[2] = a; break;
+				}
+				switch (M.ext_emoda)
+				{
+				case 0: o[3] = a; break;
+				case 1: o[3] = Y; break;
+				case 2: o[3] = 0.5f * Y; break;
+				default: o[3] = 0.0f; break;
+				}
+				uint32_t addr = oracle::swizzle(gx + M.ext_wdx, gy + M.ext_wdy, M.ext_exbp, M.ext_exbw, 0x00);
+				uint32_t packed = oracle::pack_unorm(o);
+				memcpy(b->vram.data() + size_t(addr) * 4, &packed, 4);
+				if (b->num_planes > 1)
+					memset(b->vram.data() + oracle::VRAM + size_t(addr) * 4, 0, 4);
+			}
+	}
+
+	if (!M.deinterlace)
+	{
+		for (auto &f : b->fields)
+			f.clear();
+		memcpy(out, merged.data(), merged.size() * 4);
+		return 0;
+	}
+	if (W != b->field_w || H != b->field_h)
+	{
+		for (auto &f : b->fields)
+			f.clear();
+		b->field_w = W;
+		b->field_h = H;
+	}
+	for (int i = 3; i >= 1; i--)
+		b->fields[i] = std::move(b->fields[i - 1]);
+	b->fields[0] = std::move(merged);
+	if (b->fields[1].empty())
+		b->fields[1] = b->fields[0];
+	if (b->fields[2].empty())
+		b->fields[2] = b->fields[0];
+	if (b->fields[3].empty())
+		b->fields[3] = b->fields[1];
+	const auto &f0 = b->fields[0], &f1 = b->fields[1], &f2 = b->fields[2], &f3 = b->fields[3];
+	const uint32_t H2 = 2 * H;
+	for (uint32_t y = 0; y < H2; y++)
+		for (uint32_t x = 0; x < W; x++)
+		{
+			uint32_t o;
+			if ((y & 1) == (M.phase & 1))
+				o = f0[size_t(y >> 1) * W + x];
+			else if (y == 0 || y == H2 - 1)
+				o = f1[size_t(y >> 1) * W + x];
+			else
+			{
+				uint32_t up = (y - 1) >> 1;
+				uint32_t cur0 = f0[size_t(up) * W + x], cur1 = f0[size_t(up + 1) * W + x];
+				uint32_t prev0 = f2[size_t(up) * W + x], prev1 = f2[size_t(up + 1) * W + x];
+				uint32_t fld1 = f1[size_t(y >> 1) * W + x], fld3 = f3[size_t(y >> 1) * W + x];
+				float mh = luma_diff(cur0, prev0), ml = luma_diff(cur1, prev1), mc = luma_diff(fld1, fld3);
+				float diff = std::fmax(std::fmin(mh, ml), mc);
+				float tt = (diff - 0.04f) / (0.06f - 0.04f);
+				tt = std::fmin(std::fmax(tt, 0.0f), 1.0f);
+				float bob = (tt * tt) * (3.0f - 2.0f * tt);
+				float c[4];
+				for (int k = 0; k < 3; k++)
+				{
+					float avg = 0.5f * (oracle::unorm(cur0, k) + oracle::unorm(cur1, k));
+					c[k] = oracle::unorm(fld1, k) * (1.0f - bob) + avg * bob;
+				}
+				c[3] = 1.0f;
+				o = oracle::pack_unorm(c);
+			}
+			out[size_t(y) * W + x] = o;
+		}
+	return 0;
+}
+
 static const pgs_backend_ops ORACLE_OPS = {
 	PGS_ABI_VERSION, o_destroy, o_reserve, o_flush_rendering, o_copy, o_palette, o_set_ss, o_submit, o_read, o_write, o_error,
-	nullptr, nullptr, o_circuit,
+	nullptr, nullptr, o_circuit, o_vsync,
 };
 
 extern "C" {

@@ -131,6 +131,16 @@ struct CudaBackend
 	uint32_t *d_texels = nullptr;
 	size_t texels_cap = 0;
 	uint32_t *d_circuit = nullptr;
+	// vsync: circuit read-outs, merged image, output and the last four
+	// merged fields for the deinterlacer (slot order: newest first).
+	struct DevImage
+	{
+		uint32_t *ptr = nullptr;
+		size_t cap = 0;
+	};
+	DevImage vs_circuit[2], vs_merged, vs_out, vs_fields[4];
+	bool vs_field_valid[4] = {};
+	uint32_t vs_field_w = 0, vs_field_h = 0;
 	size_t circuit_cap = 0;
 
 	// Recording.
@@ -244,6 +254,9 @@ struct CudaBackend
 		cudaFree(d_flags);
 		cudaFree(d_texels);
 		cudaFree(d_circuit);
+		for (DevImage *im : { &vs_circuit[0], &vs_circuit[1], &vs_merged, &vs_out, &vs_fields[0], &vs_fields[1],
+		                      &vs_fields[2], &vs_fields[3] })
+			cudaFree(im->ptr);
 		cudaFree(d_arena);
 		cudaFree(d_reset_vram);
 		cudaFree(d_reset_clut);
@@ -1071,6 +1084,137 @@ struct CudaBackend
 		return PGS_OK;
 	}
 
+	static int ensure_image(DevImage &im, size_t pixels)
+	{
+		if (pixels * 4 <= im.cap)
+			return PGS_OK;
+		cudaFree(im.ptr);
+		im.ptr = nullptr;
+		im.cap = 0;
+		CUDA_TRY(cudaMalloc(&im.ptr, pixels * 4));
+		im.cap = pixels * 4;
+		return PGS_OK;
+	}
+
+	// One vsync (pgs_merge_params): circuits, merge, EXTWRITE, deinterlace.
+	int vsync(const pgs_merge_params &m, void *dst)
+	{
+		if (recording)
+			return PGS_ERROR_UNSUPPORTED;
+		const pgs_circuit_params *cp[2] = { &m.circuit[0], &m.circuit[1] };
+		for (int i = 0; i < 2; i++)
+		{
+			const pgs_circuit_params &c = *cp[i];
+			if (size_t(c.width) * c.height == 0)
+				continue;
+			if (c.width > 4096 || c.height > 4096)
+				return PGS_ERROR_INVALID_ARGUMENT;
+			int r = ensure_image(vs_circuit[i], size_t(c.width) * c.height);
+			if (r)
+				return r;
+			r = sample_circuit_device(c, vs_circuit[i].ptr);
+			if (r)
+				return r;
+		}
+		auto grid_of = [](uint32_t w, uint32_t h) { return dim3((w + 31) / 32, (h + 7) / 8); };
+		if (m.raw_circuit == 1 || m.raw_circuit == 2)
+		{
+			const pgs_circuit_params &c = *cp[m.raw_circuit - 1];
+			size_t bytes = size_t(c.width) * c.height * 4;
+			if (bytes)
+				CUDA_TRY(cudaMemcpyAsync(dst, vs_circuit[m.raw_circuit - 1].ptr, bytes, cudaMemcpyDeviceToHost, stream));
+			CUDA_TRY(cudaStreamSynchronize(stream));
+			d2h_bytes += bytes;
+			return PGS_OK;
+		}
+		if (m.width == 0 || m.height == 0)
+			return PGS_OK;
+		if (m.width > 4096 || m.height > 4096)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		if ((m.draw_circuit1 && size_t(cp[0]->width) * cp[0]->height == 0) ||
+		    (m.draw_circuit2 && size_t(cp[1]->width) * cp[1]->height == 0))
+			return PGS_ERROR_INVALID_ARGUMENT;
+		const size_t pixels = size_t(m.width) * m.height;
+		int r = ensure_image(vs_merged, pixels);
+		if (r)
+			return r;
+		merge_kernel<<<grid_of(m.width, m.height), 256, 0, stream>>>(m, vs_circuit[0].ptr, vs_circuit[1].ptr,
+		                                                            vs_merged.ptr);
+		launch_counter++;
+		CUDA_TRY(cudaGetLastError());
+		if (m.ext_write && m.ext_width && m.ext_height)
+		{
+			const uint32_t *src = vs_merged.ptr;
+			uint32_t sw = m.width, sh = m.height;
+			if (m.ext_source == 1 || m.ext_source == 2)
+			{
+				const int ci = m.ext_source == 1 ? 1 : 0;
+				if (size_t(cp[ci]->width) * cp[ci]->height == 0)
+					return PGS_ERROR_INVALID_ARGUMENT;
+				src = vs_circuit[ci].ptr;
+				sw = cp[ci]->width;
+				sh = cp[ci]->height;
+			}
+			if (m.ext_width > 4096 || m.ext_height > 4096)
+				return PGS_ERROR_INVALID_ARGUMENT;
+			extwrite_kernel<<<grid_of(m.ext_width, m.ext_height), 256, 0, stream>>>(m, src, sw, sh, d_unorm_lut, d_vram,
+			                                                                      num_planes > 1 ? 1u : 0u);
+			launch_counter++;
+			CUDA_TRY(cudaGetLastError());
+		}
+		if (!m.deinterlace)
+		{
+			for (bool &v : vs_field_valid)
+				v = false;
+			CUDA_TRY(cudaMemcpyAsync(dst, vs_merged.ptr, pixels * 4, cudaMemcpyDeviceToHost, stream));
+			CUDA_TRY(cudaStreamSynchronize(stream));
+			d2h_bytes += pixels * 4;
+			return PGS_OK;
+		}
+		// Field history: the new merged image becomes slot 0 and the others
+		// move down; holes of the first frames take the newest fields
+		// (:5015-5030).  A size change starts the history over.
+		if (m.width != vs_field_w || m.height != vs_field_h)
+		{
+			for (bool &v : vs_field_valid)
+				v = false;
+			vs_field_w = m.width;
+			vs_field_h = m.height;
+		}
+		std::swap(vs_fields[3], vs_fields[2]);
+		std::swap(vs_fields[2], vs_fields[1]);
+		std::swap(vs_fields[1], vs_fields[0]);
+		std::swap(vs_fields[0], vs_merged);
+		vs_field_valid[3] = vs_field_valid[2];
+		vs_field_valid[2] = vs_field_valid[1];
+		vs_field_valid[1] = vs_field_valid[0];
+		vs_field_valid[0] = true;
+		const int fill_from[4] = { 0, 0, 0, 1 };
+		for (int i = 1; i < 4; i++)
+		{
+			if (vs_field_valid[i])
+				continue;
+			r = ensure_image(vs_fields[i], pixels);
+			if (r)
+				return r;
+			CUDA_TRY(cudaMemcpyAsync(vs_fields[i].ptr, vs_fields[fill_from[i]].ptr, pixels * 4, cudaMemcpyDeviceToDevice,
+			                         stream));
+			vs_field_valid[i] = true;
+		}
+		r = ensure_image(vs_out, pixels * 2);
+		if (r)
+			return r;
+		weave_kernel<<<grid_of(m.width, 2 * m.height), 256, 0, stream>>>(vs_fields[0].ptr, vs_fields[1].ptr,
+		                                                                  vs_fields[2].ptr, vs_fields[3].ptr, m.width,
+		                                                                  m.height, m.phase & 1u, d_unorm_lut, vs_out.ptr);
+		launch_counter++;
+		CUDA_TRY(cudaGetLastError());
+		CUDA_TRY(cudaMemcpyAsync(dst, vs_out.ptr, pixels * 8, cudaMemcpyDeviceToHost, stream));
+		CUDA_TRY(cudaStreamSynchronize(stream));
+		d2h_bytes += pixels * 8;
+		return PGS_OK;
+	}
+
 	int write_vram(uint64_t off, uint64_t size, const void *src)
 	{
 		if (off + size > VRAM_SIZE)
@@ -1592,10 +1736,14 @@ int c_circuit(void *self, const pgs_circuit_params *c, void *dst)
 {
 	return c && dst ? B(self)->sample_circuit(*c, dst) : PGS_ERROR_INVALID_ARGUMENT;
 }
+static int c_vsync(void *self, const pgs_merge_params *m, void *dst)
+{
+	return m && dst ? B(self)->vsync(*m, dst) : PGS_ERROR_INVALID_ARGUMENT;
+}
 
 const pgs_backend_ops CUDA_OPS = {
 	PGS_ABI_VERSION, c_destroy, c_reserve, c_flush_rendering, c_copy, c_palette, c_set_ss, c_submit, c_read, c_write, c_error,
-	c_read_async, c_wait, c_circuit,
+	c_read_async, c_wait, c_circuit, c_vsync,
 };
 
 // ---------------------------------------------------------------------------

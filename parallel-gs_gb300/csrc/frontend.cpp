@@ -1932,21 +1932,18 @@ int pgs_gs_read_priv_register(pgs_gs *gs, uint32_t index, uint64_t *value)
 	return PGS_OK;
 }
 
-int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_t flags, void *dst, uint64_t dst_size,
-                           uint32_t *width, uint32_t *height)
-{
-	if (!gs || circuit > 1 || !width || !height)
-		return PGS_ERROR_INVALID_ARGUMENT;
-	if (gs->ops->abi_version < 2 || !gs->ops->sample_circuit)
-		return PGS_ERROR_UNSUPPORTED;
-	gs->flush();
-	if (gs->sticky_error)
-		return gs->sticky_error;
-	const uint64_t dispfb = gs->priv[7 + 2 * circuit], display = gs->priv[8 + 2 * circuit];
-	const uint64_t smode2 = gs->priv[2], extwrite = gs->priv[13];
-	const bool force_progressive = (flags & PGS_SCANOUT_FORCE_PROGRESSIVE) != 0;
+} // extern "C"
 
-	// compute_circuit_rect (gs/gs_renderer.cpp:4114-4172).
+namespace
+{
+// compute_circuit_rect (gs/gs_renderer.cpp:4114-4172) and the sampling
+// parameters of sample_crtc_circuit (:4055-4112) for one circuit.  `phase` is
+// the field the read-out starts from (alternating-line interlace only).
+void circuit_setup(const pgs_gs *gs, uint32_t circuit, uint32_t phase, bool force_progressive, bool high_res,
+                   pgs_circuit_params &c, uint32_t &phase_offset)
+{
+	const uint64_t dispfb = gs->priv[7 + 2 * circuit], display = gs->priv[8 + 2 * circuit];
+	const uint64_t smode2 = gs->priv[2];
 	bool is_interlaced = field(smode2, 0, 1) != 0;
 	bool alternative_sampling = is_interlaced && !field(smode2, 1, 1);
 	if (alternative_sampling && force_progressive)
@@ -1955,13 +1952,11 @@ int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_
 	uint32_t MAGH = field(display, 23, 4) + 1, MAGV = field(display, 27, 2) + 1;
 	uint32_t DY = field(display, 12, 11);
 	uint32_t img_w = DW / MAGH, img_h = DH / MAGV, valid_w = img_w, valid_h;
-	uint32_t phase_offset = 0, phase_stride = 1;
-	// vsync samples the field given by `phase` only for alternating-line
-	// interlace that is not forced progressive (:4468-4478).
-	uint32_t field_phase = (alternative_sampling && !force_progressive) ? (phase & 1u) : 0u;
+	uint32_t phase_stride = 1;
+	phase_offset = 0;
 	if (is_interlaced)
 	{
-		phase_offset = alternative_sampling ? ((DY ^ field_phase) & 1u) : 0u;
+		phase_offset = alternative_sampling ? ((DY ^ phase) & 1u) : 0u;
 		phase_stride = alternative_sampling ? 2u : 1u;
 		valid_h = (img_h - phase_offset + 1) >> 1;
 		img_h = (img_h + 1) >> 1;
@@ -1971,12 +1966,7 @@ int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_
 		valid_h = img_h;
 		img_h = (img_h + 1) & ~1u;
 	}
-
-	// High-resolution read-out of a super-sampled frame (:4217-4239).
-	bool high_res = (flags & PGS_SCANOUT_HIGH_RESOLUTION) != 0;
-	if (!force_progressive || field(extwrite, 0, 1) || !gs->sampling_rate_x_log2 || !gs->sampling_rate_y_log2)
-		high_res = false;
-	pgs_circuit_params c = {};
+	c = {};
 	c.fbp = field(dispfb, 0, 9);
 	c.fbw = field(dispfb, 9, 6);
 	c.psm = field(dispfb, 15, 5);
@@ -1990,6 +1980,76 @@ int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_
 	c.height = img_h * scale;
 	c.valid_width = valid_w * scale;
 	c.valid_height = valid_h * scale;
+}
+
+// Display mode of SMODE1 (GSRenderer::vsync, gs/gs_renderer.cpp:4262-4378).
+struct VideoMode
+{
+	uint32_t width, height, clock_divider;
+	int32_t scan_x, scan_y;
+	bool hdtv;
+};
+
+bool video_mode(uint64_t smode1, uint64_t smode2, bool overscan, bool tall, VideoMode &m)
+{
+	enum { CMOD_PROGRESSIVE = 0, CMOD_NTSC = 2, CMOD_PAL = 3 };
+	enum { LC_ANALOG = 32, LC_HDTV = 22, LC_VGA = 15, LC_UNKNOWN_29 = 29 };
+	const uint32_t cmod = field(smode1, 13, 2), lc = field(smode1, 3, 7);
+	const bool interlace = field(smode2, 0, 1) != 0;
+	m = {};
+	if ((cmod == CMOD_NTSC || (cmod == CMOD_PROGRESSIVE && !interlace)) && lc == LC_ANALOG)
+	{
+		m = overscan ? VideoMode{ 712, 240, 0, 123, 17, false } : VideoMode{ 640, 224, 0, 159, 25, false };
+		m.clock_divider = cmod == CMOD_PROGRESSIVE ? 2u : 4u;
+	}
+	else if (cmod == CMOD_PAL && lc == LC_ANALOG)
+	{
+		m = overscan ? VideoMode{ 712, 288, 4, 133, 21, false } : VideoMode{ 640, 256, 4, 169, 36, false };
+	}
+	else if (cmod == CMOD_PROGRESSIVE && lc == LC_HDTV)
+	{
+		m = interlace ? VideoMode{ 1920, 540, 1, 236, 0, true } : VideoMode{ 1280, 720, 1, 300, 0, true };
+	}
+	else if (cmod == CMOD_PROGRESSIVE && lc == LC_VGA)
+		return m = VideoMode{ 640, 480, 2, 138, 34, false }, true;
+	else if (lc == LC_UNKNOWN_29)
+		return m = VideoMode{ 640, 480, 4, 318, 50, false }, true;
+	else
+		return false;
+	if (tall)
+	{
+		m.height *= 2;
+		m.scan_y *= 2;
+	}
+	return true;
+}
+} // namespace
+
+extern "C" {
+
+int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_t flags, void *dst, uint64_t dst_size,
+                           uint32_t *width, uint32_t *height)
+{
+	if (!gs || circuit > 1 || !width || !height)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if (gs->ops->abi_version < 2 || !gs->ops->sample_circuit)
+		return PGS_ERROR_UNSUPPORTED;
+	gs->flush();
+	if (gs->sticky_error)
+		return gs->sticky_error;
+	const uint64_t smode2 = gs->priv[2], extwrite = gs->priv[13];
+	const bool force_progressive = (flags & PGS_SCANOUT_FORCE_PROGRESSIVE) != 0;
+	bool alternative_sampling = field(smode2, 0, 1) && !field(smode2, 1, 1);
+	// vsync samples the field given by `phase` only for alternating-line
+	// interlace that is not forced progressive (:4468-4478).
+	uint32_t field_phase = (alternative_sampling && !force_progressive) ? (phase & 1u) : 0u;
+	// High-resolution read-out of a super-sampled frame (:4217-4239).
+	bool high_res = (flags & PGS_SCANOUT_HIGH_RESOLUTION) != 0;
+	if (!force_progressive || field(extwrite, 0, 1) || !gs->sampling_rate_x_log2 || !gs->sampling_rate_y_log2)
+		high_res = false;
+	pgs_circuit_params c;
+	uint32_t phase_offset;
+	circuit_setup(gs, circuit, field_phase, force_progressive, high_res, c, phase_offset);
 	*width = c.width;
 	*height = c.height;
 	if (uint64_t(c.width) * c.height * 4u > dst_size || (!dst && c.width * c.height))
@@ -1997,6 +2057,281 @@ int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_
 	if (c.width == 0 || c.height == 0)
 		return PGS_OK;
 	return gs->ops->sample_circuit(gs->be, &c, dst);
+}
+
+// GSRenderer::vsync (gs/gs_renderer.cpp:4189-5055): everything that is decided
+// from registers happens here; the backend samples, composes, writes back and
+// deinterlaces (pgs_merge_params).
+int pgs_gs_vsync(pgs_gs *gs, const pgs_vsync_info *info, void *dst, uint64_t dst_size, pgs_scanout_result *res)
+{
+	if (!gs || !info || !res)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if (gs->ops->abi_version < 3 || !gs->ops->vsync)
+		return PGS_ERROR_UNSUPPORTED;
+	gs->flush();
+	if (gs->sticky_error)
+		return gs->sticky_error;
+	*res = {};
+	const uint64_t pmode = gs->priv[0], smode1 = gs->priv[1], smode2 = gs->priv[2];
+	const uint64_t extbuf = gs->priv[11], extdata = gs->priv[12], extwrite = gs->priv[13], bgcolor = gs->priv[14];
+	const uint32_t flags = info->flags;
+	const bool force_progressive = (flags & PGS_VSYNC_FORCE_PROGRESSIVE) != 0;
+	const bool overscan = (flags & PGS_VSYNC_OVERSCAN) != 0;
+	const bool crtc_offsets = (flags & PGS_VSYNC_CRTC_OFFSETS) != 0;
+	const bool anti_blur = (flags & PGS_VSYNC_ANTI_BLUR) != 0;
+	const bool adapt = (flags & PGS_VSYNC_ADAPT_HORIZONTAL) != 0;
+	bool high_res = (flags & PGS_VSYNC_HIGH_RESOLUTION) != 0;
+	const bool INT = field(smode2, 0, 1) != 0, FFMD = field(smode2, 1, 1) != 0;
+	const bool progressive = field(smode1, 13, 2) == 0;
+	const bool ext_on = field(extwrite, 0, 1) != 0;
+	const uint32_t rx = gs->sampling_rate_x_log2, ry = gs->sampling_rate_y_log2;
+
+	const bool alternative_sampling = INT && !FFMD;
+	const bool is_interlaced = INT && !(alternative_sampling && force_progressive);
+	const bool force_deinterlace = !high_res && FFMD && INT && !progressive;
+	const bool double_strike = !INT && !progressive;
+	if (!force_progressive || ext_on || !rx || !ry || force_deinterlace)
+		high_res = false;
+	bool field_aware = high_res && ry && FFMD && INT && !progressive;
+
+	VideoMode mode;
+	if (!video_mode(smode1, smode2, overscan, !is_interlaced && !double_strike && !force_deinterlace, mode))
+		return PGS_OK; // unknown video mode: no image
+	if (mode.hdtv)
+	{
+		high_res = false;
+		field_aware = false;
+	}
+	const uint32_t cd = mode.clock_divider;
+	const uint32_t phase = (alternative_sampling && !force_progressive) ? (info->phase & 1u) : 0u;
+
+	bool EN1 = field(pmode, 0, 1) != 0, EN2 = field(pmode, 1, 1) != 0;
+	uint32_t MMOD = field(pmode, 5, 1), ALP = field(pmode, 8, 8), SLBG = field(pmode, 7, 1);
+	if (EN1 && EN2 && anti_blur)
+	{
+		// Anti-blur: two circuits reading the same buffer one line apart
+		// collapse to one (:4478-4531).
+		const uint64_t fb1 = gs->priv[7], d1 = gs->priv[8], fb2 = gs->priv[9], d2 = gs->priv[10];
+		auto DBY = [](uint64_t fb) { return field(fb, 43, 11); };
+		auto DY = [](uint64_t d) { return field(d, 12, 11); };
+		auto DX = [](uint64_t d) { return field(d, 0, 12); };
+		auto MAGH = [](uint64_t d) { return field(d, 23, 4); };
+		if (field(fb1, 0, 9) == field(fb2, 0, 9) && field(fb1, 15, 5) == field(fb2, 15, 5) &&
+		    field(fb1, 9, 6) == field(fb2, 9, 6) && field(fb1, 32, 11) == field(fb2, 32, 11) && MAGH(d1) == MAGH(d2) &&
+		    field(d1, 27, 2) == field(d2, 27, 2))
+		{
+			if (MMOD == 1 && DY(d1) == DY(d2) && DBY(fb1) == DBY(fb2) && DX(d1) != DX(d2) &&
+			    std::abs(int(DX(d1)) - int(DX(d2))) < int(2 * (MAGH(d1) + 1)))
+			{
+				EN2 = false;
+				ALP = 0xff;
+				MMOD = 1;
+			}
+			else if (alternative_sampling && DY(d1) == DY(d2))
+			{
+				if (DBY(fb1) + 1 == DBY(fb2))
+				{
+					EN2 = false;
+					ALP = 0xff;
+					MMOD = 1;
+				}
+				else if (DBY(fb1) == DBY(fb2) + 1)
+				{
+					EN1 = false;
+					SLBG = 0;
+				}
+			}
+			else if (alternative_sampling && DBY(fb1) == DBY(fb2))
+			{
+				if (DY(d1) + 1 == DY(d2))
+				{
+					EN2 = false;
+					ALP = 0xff;
+					MMOD = 1;
+				}
+				else if (DY(d1) == DY(d2) + 1)
+				{
+					EN1 = false;
+					SLBG = 0;
+				}
+			}
+		}
+	}
+
+	pgs_merge_params m = {};
+	bool has_image[2] = { false, false };
+	int32_t shift_x = INT32_MAX, shift_y = INT32_MAX;
+	bool skip_shift_x = false, skip_shift_y = false;
+	const bool en[2] = { EN1, EN2 };
+	for (uint32_t i = 0; i < 2; i++)
+	{
+		if (!en[i])
+			continue;
+		const uint64_t display = gs->priv[8 + 2 * i];
+		uint32_t phase_offset;
+		circuit_setup(gs, i, phase, force_progressive, high_res, m.circuit[i], phase_offset);
+		has_image[i] = m.circuit[i].width && m.circuit[i].height;
+		if (!has_image[i])
+			m.circuit[i] = {};
+		int32_t off_x = int32_t(field(display, 0, 12) + cd / 2) / int32_t(cd) - mode.scan_x;
+		int32_t off_y = int32_t(field(display, 12, 11) + phase_offset) >> int(is_interlaced);
+		off_y -= mode.scan_y;
+		uint32_t w = (field(display, 32, 12) + 1) / cd;
+		uint32_t h = (field(display, 44, 11) + 1 + uint32_t(is_interlaced)) >> int(is_interlaced);
+		if (!is_interlaced)
+			h = (h + 1) & ~1u;
+		m.rect_x[i] = off_x;
+		m.rect_y[i] = off_y;
+		m.rect_w[i] = w;
+		m.rect_h[i] = h;
+		skip_shift_x = skip_shift_x || w != mode.width;
+		skip_shift_y = skip_shift_y || h != mode.height;
+		shift_x = std::min(shift_x, off_x);
+		shift_y = std::min(shift_y, off_y);
+	}
+	if (!overscan && !crtc_offsets)
+	{
+		for (uint32_t i = 0; i < 2; i++)
+		{
+			if (!en[i])
+				continue;
+			if (!skip_shift_x)
+				m.rect_x[i] -= shift_x;
+			if (!skip_shift_y)
+				m.rect_y[i] -= shift_y;
+		}
+	}
+
+	const uint32_t real_mode_width = mode.width;
+	uint32_t mode_width = mode.width;
+	float sampling_rate_mhz = 54.0f / float(cd);
+	if (cd == 4 && !is_interlaced)
+		sampling_rate_mhz *= 2.0f;
+	if (adapt)
+	{
+		// Express the CRTC rectangles in the circuits' own horizontal resolution
+		// (:4646-4685).
+		const uint32_t hr_scale = high_res ? 1u : 0u;
+		uint32_t h0 = has_image[0] ? (m.circuit[0].width >> hr_scale) : 0u;
+		uint32_t h1 = has_image[1] ? (m.circuit[1].width >> hr_scale) : 0u;
+		uint32_t magh1 = field(gs->priv[8], 23, 4) + 1, magh2 = field(gs->priv[10], 23, 4) + 1;
+		if (h0 == 0)
+		{
+			h0 = h1;
+			magh1 = magh2;
+		}
+		if (h1 == 0)
+			h1 = h0;
+		if (h0 && h0 == h1)
+		{
+			float scaling = float(cd) / float(magh1);
+			sampling_rate_mhz *= scaling;
+			for (uint32_t i = 0; i < 2; i++)
+			{
+				if (!en[i])
+					continue;
+				m.rect_x[i] = int32_t(std::round(float(m.rect_x[i]) * scaling));
+				m.rect_w[i] = uint32_t(std::round(float(m.rect_w[i]) * scaling));
+			}
+			mode_width = uint32_t(std::round(float(mode_width) * scaling));
+		}
+	}
+
+	res->mode_width = mode_width;
+	res->mode_height = mode.height;
+	res->high_resolution_scanout = high_res;
+	res->sampling_rate_mhz = sampling_rate_mhz;
+	res->double_strike = double_strike;
+
+	if ((flags & PGS_VSYNC_RAW_CIRCUIT) && !crtc_offsets && !overscan && adapt && !force_deinterlace &&
+	    !is_interlaced && !ext_on)
+	{
+		// A single unblended circuit that fits the mode goes out as it is (:4695-4735).
+		const uint32_t ew = mode_width << int(high_res), eh = mode.height << int(high_res);
+		bool raw1 = has_image[0] && !has_image[1] && MMOD == 1 && ALP == 0xff && m.circuit[0].width <= ew &&
+		            m.circuit[0].height <= eh;
+		bool raw2 = has_image[1] && !has_image[0] && SLBG == 0 && m.circuit[1].width <= ew &&
+		            m.circuit[1].height <= eh;
+		if (raw1 || raw2)
+		{
+			const pgs_circuit_params &c = m.circuit[raw1 ? 0 : 1];
+			m.raw_circuit = raw1 ? 1u : 2u;
+			res->width = c.width;
+			res->height = c.height;
+			res->internal_width = c.width >> int(high_res);
+			res->internal_height = c.height >> int(high_res);
+			if (uint64_t(c.width) * c.height * 4u > dst_size || !dst)
+				return PGS_ERROR_CAPACITY;
+			return gs->ops->vsync(gs->be, &m, dst);
+		}
+	}
+
+	res->internal_width = mode_width;
+	res->internal_height = mode.height;
+	m.width = mode_width << int(high_res);
+	m.height = mode.height << int(high_res);
+	if (field_aware)
+		m.height--;
+	for (uint32_t i = 0; i < 2; i++)
+	{
+		if (high_res)
+		{
+			m.rect_x[i] *= 2;
+			m.rect_y[i] *= 2;
+			m.rect_w[i] *= 2;
+			m.rect_h[i] *= 2;
+			if (field_aware && !info->phase)
+				m.rect_y[i] -= 1;
+		}
+	}
+	m.draw_circuit2 = SLBG == 0 && has_image[1];
+	m.draw_circuit1 = has_image[0];
+	m.blend = MMOD == 1 ? (ALP != 0xff ? 1u : 0u) : 2u;
+	m.alp = ALP;
+	m.bgcolor = uint32_t(bgcolor & 0xffffffu);
+
+	if (ext_on)
+	{
+		// EXTWRITE feedback (:4900-4990).
+		uint32_t rw = field(extdata, 32, 12) + 1, rh = field(extdata, 44, 11) + 1;
+		if (!field(extbuf, 22, 1))
+			rh *= 2;
+		const uint32_t fbin = field(extbuf, 20, 2);
+		m.ext_source = fbin == 0 ? 0u : (has_image[1] ? 1u : (has_image[0] ? 2u : 3u));
+		if (m.ext_source != 3u)
+		{
+			const uint32_t smph = field(extdata, 23, 4), smpv = field(extdata, 27, 2);
+			const uint32_t scan_w = real_mode_width, scan_h = m.height;
+			rw = std::min<uint32_t>(rw, (scan_w * cd + smph) / (smph + 1));
+			rh = std::min<uint32_t>(rh, (scan_h + smpv) / (smpv + 1));
+			m.ext_write = rw && rh;
+			m.ext_width = rw;
+			m.ext_height = rh;
+			m.ext_wdx = field(extbuf, 32, 11);
+			m.ext_wdy = field(extbuf, 43, 11);
+			m.ext_exbp = field(extbuf, 0, 14);
+			m.ext_exbw = field(extbuf, 14, 6);
+			m.ext_emoda = field(extbuf, 23, 2);
+			m.ext_emodc = field(extbuf, 25, 2);
+			m.ext_uv_base[0] = 0.5f / float(rw);
+			m.ext_uv_base[1] = 0.5f / float(rh);
+			m.ext_uv_scale[0] = float(smph + 1) / float(scan_w * cd);
+			m.ext_uv_scale[1] = float(smpv + 1) / float(scan_h);
+		}
+		else
+			m.ext_source = 0;
+	}
+
+	const bool should_deinterlace = !high_res && (is_interlaced || force_deinterlace);
+	m.deinterlace = should_deinterlace && !(flags & PGS_VSYNC_SKIP_DEINTERLACE);
+	m.phase = info->phase & 1u;
+	res->interlaced = should_deinterlace;
+	res->interlace_phase = info->phase;
+	res->width = m.width;
+	res->height = m.deinterlace ? 2 * m.height : m.height;
+	if (uint64_t(res->width) * res->height * 4u > dst_size || (!dst && res->width * res->height))
+		return PGS_ERROR_CAPACITY;
+	return gs->ops->vsync(gs->be, &m, dst);
 }
 
 int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *src)

@@ -2063,6 +2063,168 @@ __global__ void __launch_bounds__(256) circuit_kernel(pgs_circuit_params C, cons
 }
 
 // ---------------------------------------------------------------------------
+// vsync output merge (GSRenderer::vsync, gs/gs_renderer.cpp:4738-4866): the
+// circuits are stretched into their CRTC viewports over a BGCOLOR clear.
+// The stretch is bilinear with 8-bit sub-texel positions, clamped to the
+// edge: texel coordinate = ((2 d + 1) * src / (2 * dst)) - 1/2 in 1/256 units,
+// exact texels when source and viewport have the same size.  Blends are
+// integer: (c * a + d * (255 - a)) / 255 rounded to nearest, alpha from the
+// source (blend factors SRC/CONSTANT_ALPHA, ONE/ZERO on alpha).
+
+__device__ __forceinline__ uint32_t stretch_sample(const uint32_t *img, uint32_t iw, uint32_t ih, int32_t dx, int32_t dy,
+                                                   uint32_t vw, uint32_t vh)
+{
+	const int64_t fx = (int64_t(2 * dx + 1) * iw * 256) / (2 * int64_t(vw)) - 128;
+	const int64_t fy = (int64_t(2 * dy + 1) * ih * 256) / (2 * int64_t(vh)) - 128;
+	const int32_t x0 = int32_t(fx >> 8), y0 = int32_t(fy >> 8);
+	const uint32_t wx = uint32_t(fx & 255), wy = uint32_t(fy & 255);
+	const int32_t xa = min(max(x0, 0), int32_t(iw) - 1), xb = min(max(x0 + 1, 0), int32_t(iw) - 1);
+	const int32_t ya = min(max(y0, 0), int32_t(ih) - 1), yb = min(max(y0 + 1, 0), int32_t(ih) - 1);
+	const uint32_t c00 = img[size_t(ya) * iw + xa], c10 = img[size_t(ya) * iw + xb];
+	const uint32_t c01 = img[size_t(yb) * iw + xa], c11 = img[size_t(yb) * iw + xb];
+	const uint32_t w00 = (256u - wx) * (256u - wy), w10 = wx * (256u - wy), w01 = (256u - wx) * wy, w11 = wx * wy;
+	uint32_t out = 0;
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		const int sh = 8 * k;
+		uint32_t acc = w00 * ((c00 >> sh) & 255u) + w10 * ((c10 >> sh) & 255u) + w01 * ((c01 >> sh) & 255u) +
+		               w11 * ((c11 >> sh) & 255u);
+		out |= ((acc + 32768u) >> 16) << sh;
+	}
+	return out;
+}
+
+__device__ __forceinline__ uint32_t blend255(uint32_t s, uint32_t d, uint32_t a)
+{
+	const uint32_t v = s * a + d * (255u - a);
+	const uint32_t q = v / 255u, r = v % 255u;
+	return q + (2u * r > 255u ? 1u : 0u);
+}
+
+__global__ void __launch_bounds__(256) merge_kernel(pgs_merge_params M, const uint32_t *c1, const uint32_t *c2, uint32_t *dst)
+{
+	const uint32_t x = blockIdx.x * 32u + (threadIdx.x & 31u), y = blockIdx.y * 8u + (threadIdx.x >> 5);
+	if (x >= M.width || y >= M.height)
+		return;
+	uint32_t color = M.bgcolor & 0xffffffu;
+	const int32_t ix = int32_t(x), iy = int32_t(y);
+	if (M.draw_circuit2 && M.rect_w[1] && M.rect_h[1] && ix >= M.rect_x[1] && ix < M.rect_x[1] + int32_t(M.rect_w[1]) &&
+	    iy >= M.rect_y[1] && iy < M.rect_y[1] + int32_t(M.rect_h[1]))
+		color = stretch_sample(c2, M.circuit[1].width, M.circuit[1].height, ix - M.rect_x[1], iy - M.rect_y[1],
+		                       M.rect_w[1], M.rect_h[1]);
+	if (M.draw_circuit1 && M.rect_w[0] && M.rect_h[0] && ix >= M.rect_x[0] && ix < M.rect_x[0] + int32_t(M.rect_w[0]) &&
+	    iy >= M.rect_y[0] && iy < M.rect_y[0] + int32_t(M.rect_h[0]))
+	{
+		const uint32_t s = stretch_sample(c1, M.circuit[0].width, M.circuit[0].height, ix - M.rect_x[0],
+		                                  iy - M.rect_y[0], M.rect_w[0], M.rect_h[0]);
+		if (M.blend == 0)
+			color = s;
+		else
+		{
+			const uint32_t a = M.blend == 1 ? M.alp : (s >> 24);
+			uint32_t out = s & 0xff000000u;
+			#pragma unroll
+			for (int k = 0; k < 3; k++)
+				out |= blend255((s >> (8 * k)) & 255u, (color >> (8 * k)) & 255u, a) << (8 * k);
+			color = out;
+		}
+	}
+	dst[size_t(y) * M.width + x] = color;
+}
+
+// EXTWRITE (extwrite.comp:37-98): the merged image or a circuit written back
+// into VRAM as CT32 at (WDX, WDY) of EXBP / EXBW, nearest texel at
+// uv = base + id * scale, optionally converted to Y / YCbCr / alpha.  Float
+// expressions are evaluated left to right, one rounding per operation.
+__global__ void __launch_bounds__(256) extwrite_kernel(pgs_merge_params M, const uint32_t *src, uint32_t sw, uint32_t sh,
+                                                       const float *unorm_lut, uint8_t *vram, uint32_t invalidate_ss)
+{
+	const uint32_t gx = blockIdx.x * 32u + (threadIdx.x & 31u), gy = blockIdx.y * 8u + (threadIdx.x >> 5);
+	if (gx >= M.ext_width || gy >= M.ext_height)
+		return;
+	const float u = fadd(M.ext_uv_base[0], fmul(__uint2float_rn(gx), M.ext_uv_scale[0]));
+	const float v = fadd(M.ext_uv_base[1], fmul(__uint2float_rn(gy), M.ext_uv_scale[1]));
+	const int32_t tx = min(max(int32_t(floorf(fmul(u, __uint2float_rn(sw)))), 0), int32_t(sw) - 1);
+	const int32_t ty = min(max(int32_t(floorf(fmul(v, __uint2float_rn(sh)))), 0), int32_t(sh) - 1);
+	const uint32_t c = src[size_t(ty) * sw + tx];
+	const float r = unorm_lut[c & 255u], g = unorm_lut[(c >> 8) & 255u], b = unorm_lut[(c >> 16) & 255u];
+	const float a = unorm_lut[c >> 24];
+	const float ey = fadd(fadd(fmul(0.587f, g), fmul(0.114f, b)), fmul(0.299f, r));
+	const float ecb = fsub(fadd(fmul(-0.311f, g), fmul(0.500f, b)), fmul(0.169f, r));
+	const float ecr = fadd(fsub(fmul(-0.419f, g), fmul(0.081f, b)), fmul(0.500f, r));
+	const float Y = __fdiv_rn(fadd(fmul(219.0f, ey), 16.0f), 255.0f);
+	const float Cb = __fdiv_rn(fadd(fmul(224.0f, ecb), 128.0f), 255.0f);
+	const float Cr = __fdiv_rn(fadd(fmul(224.0f, ecr), 128.0f), 255.0f);
+	float o[4];
+	switch (M.ext_emodc)
+	{
+	case 0: o[0] = r; o[1] = g; o[2] = b; break;
+	case 1: o[0] = Y; o[1] = Y; o[2] = Y; break;
+	case 2: o[0] = Y; o[1] = Cb; o[2] = Cr; break;
+	default: o[0] = a; o[1] = a; o[2] = a; break;
+	}
+	switch (M.ext_emoda)
+	{
+	case 0: o[3] = a; break;
+	case 1: o[3] = Y; break;
+	case 2: o[3] = fmul(0.5f, Y); break;
+	default: o[3] = 0.0f; break;
+	}
+	const uint32_t addr = swizzle_address(gx + M.ext_wdx, gy + M.ext_wdy, M.ext_exbp, M.ext_exbw, PSMCT32);
+	reinterpret_cast<uint32_t *>(vram)[addr] = pack_unorm(o[0], o[1], o[2], o[3]);
+	if (invalidate_ss)
+		reinterpret_cast<uint32_t *>(vram)[addr + VRAM_SIZE / 4] = 0;
+}
+
+// FastMAD deinterlace (weave.frag): lines of the current field pass through;
+// the others pick between the previous field (weave) and the average of the
+// current field's neighbours (bob) by the local luma difference, with
+// smoothstep(0.04, 0.06, diff) and mix() evaluated left to right.
+__device__ __forceinline__ float luma_diff(const float *lut, uint32_t a, uint32_t b)
+{
+	const float dr = fsub(lut[a & 255u], lut[b & 255u]);
+	const float dg = fsub(lut[(a >> 8) & 255u], lut[(b >> 8) & 255u]);
+	const float db = fsub(lut[(a >> 16) & 255u], lut[(b >> 16) & 255u]);
+	return fabsf(fadd(fadd(fmul(dr, 0.299f), fmul(dg, 0.587f)), fmul(db, 0.114f)));
+}
+
+__global__ void __launch_bounds__(256) weave_kernel(const uint32_t *f0, const uint32_t *f1, const uint32_t *f2,
+                                                    const uint32_t *f3, uint32_t width, uint32_t field_height,
+                                                    uint32_t phase, const float *lut, uint32_t *dst)
+{
+	const uint32_t x = blockIdx.x * 32u + (threadIdx.x & 31u), y = blockIdx.y * 8u + (threadIdx.x >> 5);
+	const uint32_t height = 2u * field_height;
+	if (x >= width || y >= height)
+		return;
+	uint32_t out;
+	if ((y & 1u) == phase)
+		out = f0[size_t(y >> 1) * width + x];
+	else if (y == 0 || y == height - 1u)
+		out = f1[size_t(y >> 1) * width + x];
+	else
+	{
+		const uint32_t up = (y - 1u) >> 1;
+		const uint32_t cur0 = f0[size_t(up) * width + x], cur1 = f0[size_t(up + 1u) * width + x];
+		const uint32_t prev0 = f2[size_t(up) * width + x], prev1 = f2[size_t(up + 1u) * width + x];
+		const uint32_t fld1 = f1[size_t(y >> 1) * width + x], fld3 = f3[size_t(y >> 1) * width + x];
+		const float mh = luma_diff(lut, cur0, prev0), ml = luma_diff(lut, cur1, prev1), mc = luma_diff(lut, fld1, fld3);
+		const float diff = fmaxf(fminf(mh, ml), mc);
+		const float tt = fminf(fmaxf(__fdiv_rn(fsub(diff, 0.04f), fsub(0.06f, 0.04f)), 0.0f), 1.0f);
+		const float bob = fmul(fmul(tt, tt), fsub(3.0f, fmul(2.0f, tt)));
+		float o[3];
+		#pragma unroll
+		for (int k = 0; k < 3; k++)
+		{
+			const float avg = fmul(0.5f, fadd(lut[(cur0 >> (8 * k)) & 255u], lut[(cur1 >> (8 * k)) & 255u]));
+			o[k] = fadd(fmul(lut[(fld1 >> (8 * k)) & 255u], fsub(1.0f, bob)), fmul(avg, bob));
+		}
+		out = pack_unorm(o[0], o[1], o[2], 1.0f);
+	}
+	dst[size_t(y) * width + x] = out;
+}
+
+// ---------------------------------------------------------------------------
 // K4: VRAM transfers.
 struct CopyParams
 {

@@ -654,6 +654,57 @@ def smode2_reg(interlace=0, ffmd=0) -> int:
     return (interlace & 1) | ((ffmd & 1) << 1)
 
 
+
+def smode1_reg(cmod=2, lc=32) -> int:
+    """SMODE1 (gs/gs_registers.hpp:705-732): CMOD 0 progressive / 2 NTSC / 3 PAL,
+    LC 32 analog, 22 HDTV, 15 VGA."""
+    return ((lc & 0x7F) << 3) | ((cmod & 3) << 13)
+
+
+def pmode_reg(en1=1, en2=0, mmod=1, amod=0, slbg=0, alp=0xFF) -> int:
+    """PMODE (gs/gs_registers.hpp:562-575)."""
+    return en1 | (en2 << 1) | (mmod << 5) | (amod << 6) | (slbg << 7) | ((alp & 0xFF) << 8)
+
+
+def extbuf_reg(exbp=0, exbw=0, fbin=0, wffmd=0, emoda=0, emodc=0, wdx=0, wdy=0) -> int:
+    return ((exbp & 0x3FFF) | ((exbw & 0x3F) << 14) | ((fbin & 3) << 20) | ((wffmd & 1) << 22) |
+            ((emoda & 3) << 23) | ((emodc & 3) << 25) | ((wdx & 0x7FF) << 32) | ((wdy & 0x7FF) << 43))
+
+
+def extdata_reg(sx=0, sy=0, smph=0, smpv=0, ww=0, wh=0) -> int:
+    return ((sx & 0xFFF) | ((sy & 0x7FF) << 12) | ((smph & 0xF) << 23) | ((smpv & 3) << 27) |
+            ((ww & 0xFFF) << 32) | ((wh & 0x7FF) << 44))
+
+
+def random_crtc(rng) -> dict:
+    """Random privileged-register state for vsync coverage: video mode, both
+    circuits (formats, offsets, magnification), PMODE blend modes, BGCOLOR,
+    EXTWRITE feedback; returns {priv index: value}."""
+    mode = [(2, 32), (3, 32), (0, 32), (0, 15), (0, 22)][int(rng.integers(0, 5))]
+    interlace = int(rng.integers(0, 2)) if mode[0] != 0 or mode[1] == 22 else 0
+    regs = {0: pmode_reg(en1=int(rng.uniform() < 0.8), en2=int(rng.uniform() < 0.5), mmod=int(rng.integers(0, 2)),
+                         slbg=int(rng.integers(0, 2)), alp=int(rng.integers(0, 256)) if rng.uniform() < 0.6 else 0xFF),
+            1: smode1_reg(*mode), 2: smode2_reg(interlace, int(rng.integers(0, 2))),
+            14: int(rng.integers(0, 1 << 24))}
+    for c in range(2):
+        psm = [PSMCT32, PSMCT24, PSMCT16, PSMCT16S][int(rng.integers(0, 4))]
+        magh = [3, 3, 1, 4, 9][int(rng.integers(0, 5))]
+        magv = int(rng.integers(0, 2))
+        w = int(rng.integers(64, 641))
+        h = int(rng.integers(32, 449))
+        regs[7 + 2 * c] = dispfb_reg(int(rng.integers(0, 40)), 10, psm, int(rng.integers(0, 64)), int(rng.integers(0, 64)))
+        regs[8 + 2 * c] = display_reg(int(rng.integers(500, 700)), int(rng.integers(20, 60)), magh, magv,
+                                      w * (magh + 1) - 1, h * (magv + 1) - 1)
+    if rng.uniform() < 0.4:
+        regs[13] = 1
+        regs[11] = extbuf_reg(exbp=int(rng.integers(0, 0x3000)), exbw=int(rng.integers(1, 11)),
+                              fbin=int(rng.integers(0, 2)), wffmd=int(rng.integers(0, 2)),
+                              emoda=int(rng.integers(0, 4)), emodc=int(rng.integers(0, 4)),
+                              wdx=int(rng.integers(0, 64)), wdy=int(rng.integers(0, 64)))
+        regs[12] = extdata_reg(smph=int(rng.integers(0, 4)), smpv=int(rng.integers(0, 2)),
+                               ww=int(rng.integers(16, 320)), wh=int(rng.integers(16, 240)))
+    return regs
+
 FUZZ_TEXTURE_PSMS = [PSMT8, PSMT4, PSMT8H, 0x24, 0x2C, PSMCT32, PSMCT24, PSMCT16, PSMCT16S]
 
 

@@ -90,7 +90,7 @@ EXPORTED_SYMBOLS = [
     "pgs_upscaler_set_tensor_path", "pgs_upscaler_get_error",
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
     "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait",
-    "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit",
+    "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit", "pgs_gs_vsync",
     "pgs_gs_dump_open", "pgs_gs_dump_next_vsync", "pgs_gs_dump_close", "pgs_gs_dump_record_begin",
     "pgs_gs_dump_record_vsync", "pgs_gs_dump_record_end", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
     "pgs_gs_set_super_sampling_rate",
@@ -156,6 +156,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.pgs_gs_dump_record_end.argtypes = [vp]
     lib.pgs_gs_read_priv_register.argtypes = [vp, u32, C.POINTER(u64)]
     lib.pgs_gs_scanout_circuit.argtypes = [vp, u32, u32, u32, vp, u64, C.POINTER(u32), C.POINTER(u32)]
+    lib.pgs_gs_vsync.argtypes = [vp, C.POINTER(VsyncInfo), vp, u64, C.POINTER(ScanoutResult)]
     lib.pgs_gs_write_vram.argtypes = [vp, u64, u64, vp]
     lib.pgs_gs_read_transfer_fifo.argtypes = [vp, vp, u32]
     lib.pgs_gs_consume_flush_stats.argtypes = [vp, C.POINTER(FlushStats)]
@@ -178,6 +179,17 @@ class BackendOps(C.Structure):
                 ("read_vram", C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p)),
                 ("write_vram", C.c_void_p),
                 ("get_error", C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_uint32)))]
+
+
+class VsyncInfo(C.Structure):
+    _fields_ = [("phase", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class ScanoutResult(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("width", "height", "mode_width", "mode_height", "internal_width",
+                                          "internal_height", "interlaced", "interlace_phase", "double_strike",
+                                          "high_resolution_scanout")] + \
+               [("sampling_rate_mhz", C.c_float), ("padding", C.c_uint32)]
 
 
 class Backend:
@@ -350,6 +362,20 @@ class GSInterface:
         check(self.lib.pgs_gs_scanout_circuit(self.handle, circuit, phase, flags, out.ctypes.data, cap, C.byref(w),
                                               C.byref(h)), "scanout_circuit")
         return out[: w.value * h.value * 4].reshape(h.value, w.value, 4).copy()
+
+    VSYNC = {"FORCE_PROGRESSIVE": 1, "HIGH_RESOLUTION": 2, "OVERSCAN": 4, "CRTC_OFFSETS": 8, "ANTI_BLUR": 16,
+             "ADAPT_HORIZONTAL": 32, "RAW_CIRCUIT": 64, "SKIP_DEINTERLACE": 128}
+
+    def vsync(self, phase: int = 0, flags: int = 0):
+        """One vsync: (RGBA8 image (height, width, 4), result dict)."""
+        info = VsyncInfo(phase, flags)
+        res = ScanoutResult()
+        cap = 3840 * 2160 * 4
+        out = np.zeros(cap, dtype=np.uint8)
+        check(self.lib.pgs_gs_vsync(self.handle, C.byref(info), out.ctypes.data, cap, C.byref(res)), "vsync")
+        d = {k: getattr(res, k) for k, _ in ScanoutResult._fields_ if k != "padding"}
+        img = out[: res.width * res.height * 4].reshape(res.height, res.width, 4).copy()
+        return img, d
 
     def write_vram(self, data, offset: int = 0) -> None:
         buf = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, bytes) else data)
