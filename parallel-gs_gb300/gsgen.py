@@ -697,7 +697,8 @@ def random_crtc(rng) -> dict:
                                       w * (magh + 1) - 1, h * (magv + 1) - 1)
     if rng.uniform() < 0.4:
         regs[13] = 1
-        regs[11] = extbuf_reg(exbp=int(rng.integers(0, 0x3000)), exbw=int(rng.integers(1, 11)),
+        # EXBW wide enough that the written rectangle does not alias itself.
+        regs[11] = extbuf_reg(exbp=int(rng.integers(0, 0x3000)), exbw=int(rng.integers(7, 11)),
                               fbin=int(rng.integers(0, 2)), wffmd=int(rng.integers(0, 2)),
                               emoda=int(rng.integers(0, 4)), emodc=int(rng.integers(0, 4)),
                               wdx=int(rng.integers(0, 64)), wdy=int(rng.integers(0, 64)))
