@@ -701,6 +701,7 @@ struct Backend
 		int32_t snap_mask;
 		bool preserve_samples;
 		bool has_aa1, has_scanmsk;
+		const uint8_t *zcache;   // depth read from this VRAM snapshot when set
 	};
 
 	struct Request
@@ -1427,18 +1428,29 @@ struct Backend
 		}
 		if (P.zb_psm != ~0u)
 		{
+			const uint8_t *zsrc = P.zcache ? P.zcache : vram.data();
+			auto z16 = [&](uint32_t plane, uint32_t i) {
+				uint16_t v;
+				memcpy(&v, zsrc + plane * size_t(VRAM) + size_t(i) * 2, 2);
+				return uint32_t(v);
+			};
+			auto z32 = [&](uint32_t plane, uint32_t i) {
+				uint32_t v;
+				memcpy(&v, zsrc + plane * size_t(VRAM) + size_t(i) * 4, 4);
+				return v;
+			};
 			if (is16(P.zb_psm))
 			{
-				smp.depth = w16(0, z_index);
-				if (P.ss && w16(1, z_index) == 0xffff)
-					smp.depth = w16(2 + sample_index, z_index);
+				smp.depth = z16(0, z_index);
+				if (P.ss && z16(1, z_index) == 0xffff)
+					smp.depth = z16(2 + sample_index, z_index);
 			}
 			else
 			{
 				uint32_t rm = is24(P.zb_psm) ? 0xffffffu : ~0u;
-				smp.depth = w32(0, z_index) & rm;
-				if (P.ss && (w32(1, z_index) & rm) == rm)
-					smp.depth = w32(2 + sample_index, z_index) & rm;
+				smp.depth = z32(0, z_index) & rm;
+				if (P.ss && (z32(1, z_index) & rm) == rm)
+					smp.depth = z32(2 + sample_index, z_index) & rm;
 			}
 		}
 		else
@@ -1679,6 +1691,98 @@ struct Backend
 	}
 
 	// flush_rendering(rp, instance, base, count) (gs/gs_renderer.cpp:2919-3001).
+	// Frame and depth buffer at the same base (GSRenderer::dispatch_shading,
+	// gs/gs_renderer.cpp:2534-2650, dispatch_read_aliased_depth_passes
+	// :2418-2487): primitives before the first depth-sensitive one render as
+	// usual; while primitives write depth, one primitive at a time; after the
+	// last depth write, in runs whose depth reads see a snapshot of VRAM taken
+	// at the start of the run, a new run starting at each depth-tested sprite
+	// that overlaps the run's area; with no depth reads left, as usual.
+	void render_segment(PassCtx &P, uint32_t inst, uint32_t lo, uint32_t count)
+	{
+		const pgs_rp_instance &in = P.rp->instances[inst];
+		const pgs_primitive_attribute *hp = P.rp->prims;
+		const uint32_t end = lo + count;
+		const uint32_t ZT = 1u << 12, ZW = 1u << 13, SPRITE = 1u << 21;
+		P.zcache = nullptr;
+		if (!in.z_sensitive || bfe(uint32_t(in.frame), 0, 9) != bfe(uint32_t(in.zbuf), 0, 9))
+		{
+			render_instance(P, inst, lo, count);
+			return;
+		}
+		std::vector<uint32_t> mine;
+		for (uint32_t i = lo; i < end; i++)
+			if (bfe(hp[i].state, 29, 3) == inst)
+				mine.push_back(i);
+		int64_t first_zs = -1, last_zs = -1, last_zw = -1;
+		for (uint32_t i : mine)
+		{
+			if (hp[i].state & ZW)
+				last_zw = i;
+			if (hp[i].state & (ZT | ZW))
+			{
+				if (first_zs < 0)
+					first_zs = i;
+				last_zs = i;
+			}
+		}
+		if (first_zs < 0)
+		{
+			render_instance(P, inst, lo, count);
+			return;
+		}
+		if (uint32_t(first_zs) > lo)
+			render_instance(P, inst, lo, uint32_t(first_zs) - lo);
+		uint32_t next = uint32_t(first_zs);
+		if (last_zw >= 0)
+		{
+			for (uint32_t i : mine)
+				if (int64_t(i) >= first_zs && int64_t(i) <= last_zw)
+					render_instance(P, inst, i, 1);
+			next = uint32_t(last_zw) + 1;
+			if (next >= end)
+				return;
+			if (last_zs <= last_zw)
+			{
+				render_instance(P, inst, next, end - next);
+				return;
+			}
+		}
+		std::vector<uint8_t> snapshot;
+		auto run_cached = [&](uint32_t a, uint32_t n) {
+			snapshot.assign(vram.begin(), vram.end());
+			P.zcache = snapshot.data();
+			render_instance(P, inst, a, n);
+			P.zcache = nullptr;
+		};
+		int32_t bx0 = INT32_MAX, by0 = INT32_MAX, bx1 = INT32_MIN, by1 = INT32_MIN;
+		for (uint32_t i : mine)
+		{
+			if (i < next || !(hp[i].state & SPRITE))
+				continue;
+			const int16_t *pb = hp[i].bb;
+			bool overlap = std::max<int32_t>(bx0, pb[0]) <= std::min<int32_t>(bx1, pb[2]) &&
+			               std::max<int32_t>(by0, pb[1]) <= std::min<int32_t>(by1, pb[3]) &&
+			               (hp[i].state & (ZT | ZW)) != 0;
+			if (overlap)
+			{
+				if (i > next)
+					run_cached(next, i - next);
+				next = i;
+				bx0 = pb[0]; by0 = pb[1]; bx1 = pb[2]; by1 = pb[3];
+			}
+			else
+			{
+				bx0 = std::min<int32_t>(bx0, pb[0]);
+				by0 = std::min<int32_t>(by0, pb[1]);
+				bx1 = std::max<int32_t>(bx1, pb[2]);
+				by1 = std::max<int32_t>(by1, pb[3]);
+			}
+		}
+		if (next < end)
+			run_cached(next, end - next);
+	}
+
 	void render_instance(PassCtx &P, uint32_t inst_index, uint32_t base, uint32_t count)
 	{
 		const pgs_rp_instance &inst = P.rp->instances[inst_index];
@@ -1951,7 +2055,7 @@ struct Backend
 		// Instance ordering (gs/gs_renderer.cpp:3190-3266).
 		if (rp->num_instances == 1)
 		{
-			render_instance(P, 0, 0, rp->num_primitives);
+			render_segment(P, 0, 0, rp->num_primitives);
 			return 0;
 		}
 		uint8_t hazard[8] = {};
@@ -1967,7 +2071,7 @@ struct Backend
 				{
 					for (uint32_t b = 0; b < 8; b++)
 						if (active & (1u << b))
-							render_instance(P, b, base, p - base);
+							render_segment(P, b, base, p - base);
 					base = p;
 					active = 0;
 					active_h = 0;
@@ -1977,7 +2081,7 @@ struct Backend
 			}
 			for (uint32_t b = 0; b < 8; b++)
 				if (active & (1u << b))
-					render_instance(P, b, base, rp->num_primitives - base);
+					render_segment(P, b, base, rp->num_primitives - base);
 		}
 		else
 		{
@@ -1991,7 +2095,7 @@ struct Backend
 			}
 			for (uint32_t i = 0; i < rp->num_instances; i++)
 				if (lo[i] != ~0u)
-					render_instance(P, i, lo[i], hi[i] - lo[i] + 1);
+					render_segment(P, i, lo[i], hi[i] - lo[i] + 1);
 		}
 		return 0;
 	}

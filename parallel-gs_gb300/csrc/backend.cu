@@ -131,6 +131,8 @@ struct CudaBackend
 	uint32_t *d_texels = nullptr;
 	size_t texels_cap = 0;
 	uint32_t *d_circuit = nullptr;
+	uint8_t *d_zcache = nullptr; // depth snapshot for aliased frame / depth buffers
+	size_t zcache_cap = 0;
 	// vsync: circuit read-outs, merged image, output and the last four
 	// merged fields for the deinterlacer (slot order: newest first).
 	struct DevImage
@@ -254,6 +256,7 @@ struct CudaBackend
 		cudaFree(d_flags);
 		cudaFree(d_texels);
 		cudaFree(d_circuit);
+		cudaFree(d_zcache);
 		for (DevImage *im : { &vs_circuit[0], &vs_circuit[1], &vs_merged, &vs_out, &vs_fields[0], &vs_fields[1],
 		                      &vs_fields[2], &vs_fields[3] })
 			cudaFree(im->ptr);
@@ -748,9 +751,13 @@ struct CudaBackend
 		return PGS_ERROR_INVALID_ARGUMENT;
 	}
 
+	// One bin + shade dispatch: primitives [lo, lo + count) of instance `inst`.
+	// `cached_depth`: depth is read from a snapshot of VRAM taken just before
+	// the dispatch (frame and depth buffer share memory; see alias_split).
 	struct Segment
 	{
 		uint32_t inst, lo, count;
+		bool cached_depth = false;
 	};
 
 	int execute_pass(const PassOp &p)
@@ -762,11 +769,123 @@ struct CudaBackend
 			return r;
 		for (const Segment &s : segs)
 		{
-			r = run_instance(P, p, s.inst, s.lo, s.count);
+			r = run_segment(P, p, s);
 			if (r)
 				return r;
 		}
 		return PGS_OK;
+	}
+
+	// A segment with cached depth snapshots all VRAM planes first and is
+	// always shaded directly (never collected for batched shading).
+	int run_segment(const PassParams &P, const PassOp &p, const Segment &s, ShadeItem *collect = nullptr,
+	                bool *collected = nullptr)
+	{
+		if (!s.cached_depth)
+			return run_instance(P, p, s.inst, s.lo, s.count, collect, collected);
+		const size_t bytes = size_t(num_planes) * VRAM_SIZE;
+		if (bytes > zcache_cap)
+		{
+			cudaFree(d_zcache);
+			d_zcache = nullptr;
+			zcache_cap = 0;
+			CUDA_TRY(cudaMalloc(&d_zcache, bytes));
+			zcache_cap = bytes;
+		}
+		CUDA_TRY(cudaMemcpyAsync(d_zcache, d_vram, bytes, cudaMemcpyDeviceToDevice, stream));
+		PassParams Pc = P;
+		Pc.zcache = d_zcache;
+		if (collected)
+			*collected = false;
+		return run_instance(Pc, p, s.inst, s.lo, s.count);
+	}
+
+	// Frame and depth buffer at the same base (GSRenderer::dispatch_shading,
+	// gs/gs_renderer.cpp:2534-2650): colour writes can land in depth read by
+	// other tiles, so the segment is cut up -- primitives before the first
+	// depth-sensitive one as usual; while primitives write depth, one
+	// primitive per dispatch; after the last depth write, depth is read from
+	// a snapshot retaken whenever a depth-tested sprite overlaps the area the
+	// current dispatch already covers (dispatch_read_aliased_depth_passes,
+	// :2418-2487); with no depth reads left, as usual.
+	static void alias_split(const PassOp &p, const pgs_primitive_attribute *hp, const Segment &s,
+	                        std::vector<Segment> &out)
+	{
+		const pgs_rp_instance &in = p.instances[s.inst];
+		const uint32_t zmask = (1u << STATE_BIT_Z_TEST) | (1u << STATE_BIT_Z_WRITE);
+		if (!in.z_sensitive || (uint32_t(in.frame) & 0x1ffu) != (uint32_t(in.zbuf) & 0x1ffu))
+		{
+			out.push_back(s);
+			return;
+		}
+		const uint32_t end = s.lo + s.count;
+		auto inst_of = [&](uint32_t i) { return (hp[i].state >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u; };
+		uint32_t first_zs = end, last_zs = 0, last_zw = 0;
+		bool zwrite = false;
+		for (uint32_t i = s.lo; i < end; i++)
+		{
+			if (inst_of(i) != s.inst)
+				continue;
+			const uint32_t st = hp[i].state;
+			if (st & (1u << STATE_BIT_Z_WRITE))
+			{
+				zwrite = true;
+				last_zw = i;
+			}
+			if (st & zmask)
+			{
+				first_zs = std::min(first_zs, i);
+				last_zs = i;
+			}
+		}
+		if (first_zs == end)
+		{
+			out.push_back(s);
+			return;
+		}
+		if (first_zs > s.lo)
+			out.push_back({ s.inst, s.lo, first_zs - s.lo, false });
+		uint32_t next = first_zs;
+		if (zwrite)
+		{
+			for (uint32_t i = first_zs; i <= last_zw; i++)
+				if (inst_of(i) == s.inst)
+					out.push_back({ s.inst, i, 1, false });
+			next = last_zw + 1;
+			if (next >= end)
+				return;
+			if (last_zs <= last_zw)
+			{
+				out.push_back({ s.inst, next, end - next, false });
+				return;
+			}
+		}
+		int32_t bb[4] = { INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN };
+		for (uint32_t i = next; i < end; i++)
+		{
+			const uint32_t st = hp[i].state;
+			if (inst_of(i) != s.inst || !(st & (1u << STATE_BIT_SPRITE)))
+				continue;
+			const int16_t *pb = hp[i].bb;
+			const bool overlap = std::max<int32_t>(bb[0], pb[0]) <= std::min<int32_t>(bb[2], pb[2]) &&
+			                     std::max<int32_t>(bb[1], pb[1]) <= std::min<int32_t>(bb[3], pb[3]) && (st & zmask);
+			if (overlap)
+			{
+				if (i > next)
+					out.push_back({ s.inst, next, i - next, true });
+				next = i;
+				bb[0] = pb[0]; bb[1] = pb[1]; bb[2] = pb[2]; bb[3] = pb[3];
+			}
+			else
+			{
+				bb[0] = std::min<int32_t>(bb[0], pb[0]);
+				bb[1] = std::min<int32_t>(bb[1], pb[1]);
+				bb[2] = std::max<int32_t>(bb[2], pb[2]);
+				bb[3] = std::max<int32_t>(bb[3], pb[3]);
+			}
+		}
+		if (next < end)
+			out.push_back({ s.inst, next, end - next, true });
 	}
 
 	// Setup, single-sample heuristic and texture decode of a pass; `segs`
@@ -843,8 +962,26 @@ struct CudaBackend
 		return PGS_OK;
 	}
 
-	// Instance segments of a pass in execution order.
+	// Instance segments of a pass in execution order, cut up where the frame
+	// and depth buffers alias.
 	void pass_segments(const PassOp &p, std::vector<Segment> &segs) const
+	{
+		instance_segments(p, segs);
+		const pgs_primitive_attribute *hp =
+		    p.host_prims ? p.host_prims : reinterpret_cast<const pgs_primitive_attribute *>(h_arena + p.prim_off);
+		bool any_alias = false;
+		for (uint32_t i = 0; i < p.num_instances; i++)
+			any_alias = any_alias || (p.instances[i].z_sensitive &&
+			                          (uint32_t(p.instances[i].frame) & 0x1ffu) == (uint32_t(p.instances[i].zbuf) & 0x1ffu));
+		if (!any_alias)
+			return;
+		std::vector<Segment> split;
+		for (const Segment &s : segs)
+			alias_split(p, hp, s, split);
+		segs.swap(split);
+	}
+
+	void instance_segments(const PassOp &p, std::vector<Segment> &segs) const
 	{
 		segs.clear();
 		if (p.num_instances == 1)
@@ -1526,7 +1663,7 @@ struct BatchEngine
 					const CudaBackend::Segment &g = c.segs[c.seg++];
 					ShadeItem item;
 					bool collected = false;
-					r = streams[s]->run_instance(c.P, *c.pass, g.inst, g.lo, g.count, &item, &collected);
+					r = streams[s]->run_segment(c.P, *c.pass, g, &item, &collected);
 					if (r)
 						return r;
 					if (collected && item.units)

@@ -120,6 +120,9 @@ struct PassParams
 	uint32_t setup_rate_x_log2, setup_rate_y_log2;
 	uint32_t opaque_fbmask[8];
 	uint8_t *vram;
+	// Depth reads come from this snapshot of all VRAM planes when set
+	// (frame and depth buffer aliased), else from vram.
+	const uint8_t *zcache;
 	const uint16_t *clut;
 	const float *rcp_float_lut;
 	const float *unorm_lut;
@@ -1725,18 +1728,21 @@ __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInst
 	}
 	if (C.zs)
 	{
+		const uint8_t *zsrc = P.zcache ? P.zcache : P.vram;
+		const uint32_t *z32 = reinterpret_cast<const uint32_t *>(zsrc);
+		const uint16_t *z16 = reinterpret_cast<const uint16_t *>(zsrc);
 		if (psm_is_16bit(I.zb_psm))
 		{
-			S.depth = vram16[z_index];
-			if (SS && vram16[z_index + V16] == 0xffffu)
-				S.depth = vram16[z_index + (sample + 2u) * V16];
+			S.depth = z16[z_index];
+			if (SS && z16[z_index + V16] == 0xffffu)
+				S.depth = z16[z_index + (sample + 2u) * V16];
 		}
 		else
 		{
 			uint32_t rm = psm_is_24bit(I.zb_psm) ? 0xffffffu : 0xffffffffu;
-			S.depth = vram32[z_index] & rm;
-			if (SS && (vram32[z_index + V32] & rm) == rm)
-				S.depth = vram32[z_index + (sample + 2u) * V32] & rm;
+			S.depth = z32[z_index] & rm;
+			if (SS && (z32[z_index + V32] & rm) == rm)
+				S.depth = z32[z_index + (sample + 2u) * V32] & rm;
 		}
 	}
 	else

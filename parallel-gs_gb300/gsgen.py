@@ -949,6 +949,62 @@ def frame_mip(seed: int, draws: int = 30, width: int = 256, height: int = 224) -
                  {"width": width, "height": height, "fbp": 0, "zbp": zbp})
 
 
+
+def frame_alias(seed: int, width: int = 256, height: int = 128) -> Frame:
+    """Frame and depth buffer at the same base page (the Z-swizzle tricks that
+    read colour as depth): draws without depth first, then small depth-writing
+    primitives (each inside one 8x8 block, so no primitive reads depth that it
+    also writes as colour elsewhere), then depth-tested sprites and triangles
+    reading the aliased depth, some overlapping earlier sprites."""
+    rng = np.random.Generator(np.random.PCG64(80000 + seed))
+    s = GifStream()
+    fpsm, zpsm = [(PSMCT32, PSMZ32), (PSMCT32, PSMZ24), (PSMCT24, PSMZ24), (PSMCT16, PSMZ16)][int(rng.integers(0, 4))]
+    ss = [1, 2, 4][int(rng.integers(0, 3))]
+    fbw = width // 64
+    s.ad([(PRMODECONT, 1), (FRAME_1, frame_reg(0, fbw, fpsm)), (ZBUF_1, zbuf_reg(0, zpsm)),
+          (SCISSOR_1, scissor_reg(0, width - 1, 0, height - 1)), (XYOFFSET_1, 0), (COLCLAMP, 1)])
+
+    def sprites(n, lo, hi, z_test, z_write, abe=0):
+        x0 = rng.integers(0, width - 8, n)
+        y0 = rng.integers(0, height - 8, n)
+        w = rng.integers(lo, hi + 1, n)
+        h = rng.integers(lo, hi + 1, n)
+        x = np.stack([x0, np.minimum(x0 + w, width)], 1).reshape(-1) * 16
+        y = np.stack([y0, np.minimum(y0 + h, height)], 1).reshape(-1) * 16
+        z = rng.integers(0, 1 << 24, 2 * n)
+        col = rng.integers(0, 256, (2 * n, 4))
+        s.ad([(TEST_1, test_reg(zte=1, ztst=[1, 2, 3][int(rng.integers(0, 3))] if z_test else 1)),
+              (ZBUF_1, zbuf_reg(0, zpsm, 0 if z_write else 1)), (ALPHA_1, alpha_reg(0, 1, 0, 1))])
+        q = np.zeros((2 * n, 2, 2), dtype=np.uint64)
+        q[:, 0] = q_rgbaq(col)
+        q[:, 1] = q_xyz2(x, y, z)
+        s.packed(prim_reg(PRIM_SPRITE, abe=abe), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+
+    def block_sprites(n):
+        # Depth-writing sprites inside one 8x8 block each.
+        bx = rng.integers(0, width // 8, n) * 8
+        by = rng.integers(0, height // 8, n) * 8
+        ox = rng.integers(0, 4, n)
+        oy = rng.integers(0, 4, n)
+        w = rng.integers(1, 5, n)
+        h = rng.integers(1, 5, n)
+        x = np.stack([bx + ox, bx + ox + w], 1).reshape(-1) * 16
+        y = np.stack([by + oy, by + oy + h], 1).reshape(-1) * 16
+        z = rng.integers(0, 1 << 24, 2 * n)
+        col = rng.integers(0, 256, (2 * n, 4))
+        s.ad([(TEST_1, test_reg(zte=1, ztst=[1, 2][int(rng.integers(0, 2))])), (ZBUF_1, zbuf_reg(0, zpsm, 0))])
+        q = np.zeros((2 * n, 2, 2), dtype=np.uint64)
+        q[:, 0] = q_rgbaq(col)
+        q[:, 1] = q_xyz2(x, y, z)
+        s.packed(prim_reg(PRIM_SPRITE), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+
+    sprites(int(rng.integers(5, 30)), 4, 64, z_test=False, z_write=False)
+    if rng.uniform() < 0.7:
+        block_sprites(int(rng.integers(5, 60)))
+    for _ in range(int(rng.integers(1, 4))):
+        sprites(int(rng.integers(5, 30)), 4, 96, z_test=True, z_write=False, abe=int(rng.integers(0, 2)))
+    return Frame("alias_%d" % seed, s.tobytes(), ss, True, 0, {"width": width, "height": height, "fbp": 0, "zbp": 0})
+
 def write_dump(path, transfers, vram: bytes | None = None, regs: dict | None = None, version: int = 9,
                serial: bytes = b"", vsync_fields=(0,)) -> None:
     """Writes a GS dump in the PCSX2 / GSdx layout (GSDumpGenerator::init,

@@ -209,3 +209,12 @@ def test_mipmap_parity(seed):
     f = gsgen.frame_mip(seed)
     ref, out = run_both(f)
     assert_same(ref, out)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_aliased_frame_depth_parity(seed):
+    """Frame and depth buffer at one base: per-primitive steps while depth is
+    written, snapshot depth for the depth-tested runs after it."""
+    f = gsgen.frame_alias(seed)
+    ref, out = run_both(f)
+    assert_same(ref, out)
