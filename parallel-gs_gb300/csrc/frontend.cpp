@@ -1745,6 +1745,22 @@ struct pgs_gs
 
 			if (path.flg == 0)
 			{
+				if (path.reg == 0 && qwords - i >= path.nreg)
+				{
+					// Whole loops at a time: the descriptors come from the tag once.
+					uint32_t desc[16];
+					for (uint32_t r = 0; r < path.nreg; r++)
+						desc[r] = uint32_t(path.tag_hi >> (4 * r)) & 0xf;
+					const size_t loops = std::min<size_t>((qwords - i) / path.nreg, path.nloop - path.loop);
+					const uint32_t nreg = path.nreg;
+					const uint64_t *q = &words[2 * i];
+					for (size_t l = 0; l < loops; l++, q += 2 * nreg)
+						for (uint32_t r = 0; r < nreg; r++)
+							packed_write(desc[r], q + 2 * r);
+					i += loops * nreg;
+					path.loop += uint32_t(loops);
+					continue;
+				}
 				uint32_t desc = uint32_t(path.tag_hi >> (4 * path.reg)) & 0xf;
 				packed_write(desc, &words[2 * i]);
 				i++;
