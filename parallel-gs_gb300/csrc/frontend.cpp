@@ -261,6 +261,60 @@ struct PageTracker
 			gen[k]++;
 	}
 
+	// Pages [x0, x1] x [y0, y1] of a buffer at page `base` with `stride` pages
+	// per row (the page rectangle of one primitive): marks them with kind
+	// `mk` and returns whether any of them is a texture read.  One pass over
+	// the rows does both; a texture-read bit is never set in a pass where no
+	// texture was read, so the test needs no separate early-out.
+	bool test_mark(uint32_t base, uint32_t stride, uint32_t x0, uint32_t x1, uint32_t y0, uint32_t y1, uint32_t mk)
+	{
+		const uint32_t w = std::min<uint32_t>(x1 - x0 + 1, NUM_PAGES), h = std::min<uint32_t>(y1 - y0 + 1, NUM_PAGES);
+		if (w > 64)
+		{
+			PageSpan s{ base + y0 * stride + x0, w, h, stride };
+			bool hit = any_kind(s, 2);
+			mark_kind(s, mk);
+			return hit;
+		}
+		const uint64_t m = low_mask(w);
+		uint32_t start = base + y0 * stride + x0;
+		if (h <= 2)
+		{
+			// Common case, without a data-dependent loop: up to two rows, each
+			// touching the word holding its first page and the next one.
+			const uint32_t s0 = start % NUM_PAGES, s1 = (start + stride) % NUM_PAGES;
+			const uint64_t r1 = h == 2 ? m : 0;
+			const uint64_t a0 = m << (s0 & 63), b0 = (m >> 1) >> (63 - (s0 & 63));
+			const uint64_t a1 = r1 << (s1 & 63), b1 = (r1 >> 1) >> (63 - (s1 & 63));
+			const uint32_t i0 = s0 >> 6, j0 = (i0 + 1) % WORDS, i1 = s1 >> 6, j1 = (i1 + 1) % WORDS;
+			uint64_t *bm = bits[mk];
+			const uint64_t *bt = bits[2];
+			const uint64_t hit = (bt[i0] & a0) | (bt[j0] & b0) | (bt[i1] & a1) | (bt[j1] & b1);
+			const uint64_t missing = (~bm[i0] & a0) | (~bm[j0] & b0) | (~bm[i1] & a1) | (~bm[j1] & b1);
+			bm[i0] |= a0;
+			bm[j0] |= b0;
+			bm[i1] |= a1;
+			bm[j1] |= b1;
+			if (missing)
+				gen[mk]++;
+			return hit != 0;
+		}
+		uint64_t hit = 0, missing = 0;
+		for (uint32_t y = 0; y < h; y++, start += stride)
+		{
+			const uint32_t st = start % NUM_PAGES, wi = st >> 6, wj = (wi + 1) % WORDS;
+			const unsigned __int128 mm = (unsigned __int128)m << (st & 63);
+			const uint64_t m0 = uint64_t(mm), m1 = uint64_t(mm >> 64);
+			hit |= (bits[2][wi] & m0) | (bits[2][wj] & m1);
+			missing |= (~bits[mk][wi] & m0) | (~bits[mk][wj] & m1);
+			bits[mk][wi] |= m0;
+			bits[mk][wj] |= m1;
+		}
+		if (missing)
+			gen[mk]++;
+		return hit != 0;
+	}
+
 	bool any(const PageSpan &s, uint8_t mask)
 	{
 		for (uint32_t k = 0; k < 3; k++)
@@ -1566,28 +1620,30 @@ struct pgs_gs
 		// Framebuffer pages this primitive may write.  If an earlier primitive of
 		// this pass samples them, end the pass first.
 		{
+			// Page rectangles of the primitive in the frame and depth buffers
+			// (FBP and ZBP are page aligned): test for texture reads and mark
+			// them written (depth: read only under ZMSK) in one pass.  A hit
+			// ends the pass, which clears the marks; they are made again in the
+			// new pass.
 			const ZbufReg &zb = D.zb;
-			// page_span of the primitive's rectangle; FBP and ZBP are page aligned.
-			auto rect_span = [&](uint32_t base_page, uint32_t pw, uint32_t ph, uint32_t stride) {
-				uint32_t px0 = uint32_t(bb[0]) >> pw, px1 = uint32_t(bb[2]) >> pw;
-				uint32_t py0 = uint32_t(bb[1]) >> ph, py1 = uint32_t(bb[3]) >> ph;
-				PageSpan s;
-				s.base_page = base_page + py0 * stride + px0;
-				s.width = std::min<uint32_t>(px1 - px0 + 1, NUM_PAGES);
-				s.height = std::min<uint32_t>(py1 - py0 + 1, NUM_PAGES);
-				s.stride = stride;
-				return s;
-			};
-			PageSpan fb_span = rect_span(frame.fbp, D.fb_pw, D.fb_ph, D.fb_stride);
 			const bool z_sens = D.z_sens;
-			PageSpan z_span = rect_span(zb.zbp, D.z_pw, D.z_ph, D.z_stride);
-			bool hazard = tracker.any_kind(fb_span, 2) || (z_sens && tracker.any_kind(z_span, 2));
+			const uint32_t fx0 = uint32_t(bb[0]) >> D.fb_pw, fx1 = uint32_t(bb[2]) >> D.fb_pw;
+			const uint32_t fy0 = uint32_t(bb[1]) >> D.fb_ph, fy1 = uint32_t(bb[3]) >> D.fb_ph;
+			const uint32_t zx0 = uint32_t(bb[0]) >> D.z_pw, zx1 = uint32_t(bb[2]) >> D.z_pw;
+			const uint32_t zy0 = uint32_t(bb[1]) >> D.z_ph, zy1 = uint32_t(bb[3]) >> D.z_ph;
+			const uint32_t zkind = zb.zmsk ? 1u : 0u;
+			bool hazard = tracker.test_mark(frame.fbp, D.fb_stride, fx0, fx1, fy0, fy1, 0);
+			if (z_sens)
+				hazard = tracker.test_mark(zb.zbp, D.z_stride, zx0, zx1, zy0, zy1, zkind) || hazard;
 			if (hazard && primitive_count)
 			{
 				flush_render_pass(FLUSH_TEXTURE_HAZARD);
 				check_frame_buffer_state();
 				update_template();
 				template_dirty = false;
+				tracker.test_mark(frame.fbp, D.fb_stride, fx0, fx1, fy0, fy1, 0);
+				if (z_sens)
+					tracker.test_mark(zb.zbp, D.z_stride, zx0, zx1, zy0, zy1, zkind);
 			}
 			if (tpl_has_tex_span && (tex_mark_key[0] != tpl_serial || tex_mark_key[1] != tracker.clears))
 			{
@@ -1596,9 +1652,6 @@ struct pgs_gs
 				tex_mark_key[0] = tpl_serial;
 				tex_mark_key[1] = tracker.clears;
 			}
-			tracker.mark_kind(fb_span, 0);
-			if (z_sens)
-				tracker.mark_kind(z_span, zb.zmsk ? 1 : 0);
 		}
 
 		auto &inst = instances[current_instance];
