@@ -264,3 +264,32 @@ def test_read_vram_async_falls_back_to_synchronous_copy():
         assert np.array_equal(out, gs.read_vram())
         gs.close()
         be.close()
+
+
+@pytest.mark.parametrize("tex_page,rect", [
+    (37, (6, 3, 8, 3)),      # one page row
+    (37, (6, 2, 8, 3)),      # two rows
+    (37, (6, 1, 8, 5)),      # five rows (general row loop)
+    (64, (3, 6, 4, 6)),      # pages 63 and 64: the span crosses a 64-page word
+    (63, (0, 6, 3, 7)),      # last page of a word, two rows
+])
+def test_framebuffer_write_over_sampled_page_is_a_hazard(tex_page, rect):
+    """A draw whose page rectangle (x0, y0, x1, y1 in 64x32 CT32 pages, 10
+    pages per row) covers a page sampled earlier in the pass ends the pass
+    before it; the same draw moved off that page does not."""
+    def build(shift):
+        def b(s):
+            setup(s)
+            s.ad([(g.TEX0_1, g.tex0_reg(tex_page * 32, 1, g.PSMCT32, 6, 5))])
+            verts(s, g.prim_reg(g.PRIM_SPRITE, tme=1, fst=1), [(0, 0), (16 * 16, 16 * 16)])
+            x0, y0, x1, y1 = rect
+            if shift:
+                # Move the rectangle so that it misses the sampled page.
+                x0 = x1 = (tex_page % 10 + 5) % 10
+            verts(s, g.prim_reg(g.PRIM_SPRITE), [(x0 * 64 * 16, y0 * 32 * 16), ((x1 + 1) * 64 * 16 - 16, (y1 + 1) * 32 * 16 - 16)])
+        return b
+    be = run(build=build(False))
+    assert [p["num_primitives"] for p in be.passes] == [1, 1]
+    assert be.passes[0]["flush_reason"] == 3
+    be = run(build=build(True))
+    assert [p["num_primitives"] for p in be.passes] == [2]
