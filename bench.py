@@ -152,6 +152,36 @@ def profiled_traffic(summary: str):
     return None
 
 
+def profiled_instructions(summary: str):
+    """Warp instructions per launch of the dominant kernel from the committed ncu
+    summary (its smsp__inst_executed.sum line)."""
+    try:
+        for line in (ROOT / "profiles" / summary).read_text().splitlines():
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == "smsp__inst_executed.sum":
+                return float(parts[1])
+    except Exception:
+        pass
+    return None
+
+
+def issue_roofline(inst_per_frame, shade_s: float, clk: dict):
+    """The shading kernels are bound by instruction issue, not DRAM: warp
+    instructions per second against the issue peak of 4 schedulers x SMs x the
+    SM clock sampled during the run."""
+    if not inst_per_frame or not shade_s:
+        return None
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz") or 2070.0
+    peak = sms * 4 * mhz * 1e6 / 1e12
+    achieved = inst_per_frame / shade_s / 1e12
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Twarp-inst/s", "frac": achieved / peak,
+            "instructions_per_frame": inst_per_frame,
+            "note": "warp instructions per frame from the committed ncu capture of the shading kernel / the "
+                    "live CUDA-event shading time; peak = 4 x %d SMs x %.0f MHz" % (sms, mhz)}
+
+
 def algorithmic_bytes(frame, ss: int) -> dict:
     """Bytes a frame must move at minimum: prim records in,
     setup records written and read, FB/Z read+write per pixel for plane 0,
@@ -706,6 +736,8 @@ def main():
                      "shade_bytes_per_frame": ab["shade"],
                      "note": "algorithmic bytes of the shading kernels per frame / their CUDA-event time "
                              "inside the timed replays; peak = measured hbm_gbs (of measured)"},
+        "issue_roofline": issue_roofline(profiled_instructions("shade_kernel_c2.md") if args.workload == "c2"
+                                         else None, shade_s, clk),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
