@@ -1,5 +1,7 @@
 """Host logic of the frontend (GSInterface re-host), checked against the rules in
 gs/gs_interface.cpp with a backend that only records what it is sent."""
+import struct
+
 import numpy as np
 import pytest
 
@@ -293,3 +295,55 @@ def test_framebuffer_write_over_sampled_page_is_a_hazard(tex_page, rect):
     assert be.passes[0]["flush_reason"] == 3
     be = run(build=build(True))
     assert [p["num_primitives"] for p in be.passes] == [2]
+
+
+@pytest.mark.parametrize("maker", ["c2", "fuzz", "strips"])
+def test_records_do_not_depend_on_transfer_chunking(maker):
+    """Long vertex-only PACKED runs are decoded ahead on a helper thread; sent
+    one qword per call they take the per-qword path.  Both must give the same
+    records, states and passes."""
+    if maker == "c2":
+        data = g.frame_c2(seed=9, num_triangles=6000, num_sprites=300, super_sampling=1, num_textures=2).data
+    elif maker == "fuzz":
+        data = g.frame_fuzz(5).data
+    else:
+        # Strips and fans with XYZ3 (no drawing) and XYZF2 kicks, ST/RGBAQ/UV/FOG lists.
+        rng = np.random.default_rng(2)
+        s = g.GifStream()
+        setup(s)
+        for prim, desc in ((g.PRIM_TRISTRIP, [g.D_RGBAQ, 0xD, g.D_XYZ2]), (g.PRIM_TRIFAN, [g.D_ST, g.D_RGBAQ, g.D_XYZF2]),
+                           (g.PRIM_TRI, [0xA, g.D_UV, g.D_RGBAQ, g.D_XYZ2])):
+            n = 3000
+            q = np.zeros((n, len(desc), 2), dtype=np.uint64)
+            for k, d in enumerate(desc):
+                q[:, k, 0] = rng.integers(0, 1 << 63, n, dtype=np.uint64)
+                q[:, k, 1] = rng.integers(0, 1 << 63, n, dtype=np.uint64)
+                if d in (g.D_XYZ2, 0xD, g.D_XYZF2):
+                    q[:, k, 0] = g.q_xyz2(rng.integers(0, 640 * 16, n), rng.integers(0, 448 * 16, n), np.zeros(n))[:, 0]
+            s.packed(g.prim_reg(prim, iip=1, tme=int(g.D_ST in desc or g.D_UV in desc), fst=int(g.D_UV in desc),
+                                fge=int(0xA in desc or g.D_XYZF2 in desc)), desc, q.reshape(-1, 2))
+        data = s.tobytes()
+    outs = []
+    for chunk in (len(data), 16):
+        be, gs = make()
+        if chunk == len(data):
+            gs.gif_transfer(0, data)
+        else:
+            for off in range(0, len(data), chunk):
+                gs.gif_transfer(0, data[off:off + chunk])
+        gs.flush()
+        gs.close()
+        outs.append(be.passes)
+    assert len(outs[0]) == len(outs[1])
+
+    def bits(v):
+        # Compare floats by their bits (random ST payloads include NaNs).
+        if isinstance(v, float):
+            return struct.unpack("<I", struct.pack("<f", v))[0]
+        if isinstance(v, dict):
+            return {k: bits(x) for k, x in v.items()}
+        if isinstance(v, (list, tuple)):
+            return [bits(x) for x in v]
+        return v
+    for a, b in zip(*outs):
+        assert bits(a) == bits(b)
