@@ -299,9 +299,9 @@ def test_framebuffer_write_over_sampled_page_is_a_hazard(tex_page, rect):
 
 @pytest.mark.parametrize("maker", ["c2", "fuzz", "strips"])
 def test_records_do_not_depend_on_transfer_chunking(maker):
-    """Long vertex-only PACKED runs are decoded ahead on a helper thread; sent
-    one qword per call they take the per-qword path.  Both must give the same
-    records, states and passes."""
+    """Whole PACKED loops are decoded a tag's worth at a time; sent one qword
+    per call they take the per-qword path.  Both must give the same records,
+    states and passes."""
     if maker == "c2":
         data = g.frame_c2(seed=9, num_triangles=6000, num_sprites=300, super_sampling=1, num_textures=2).data
     elif maker == "fuzz":
