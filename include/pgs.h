@@ -364,6 +364,11 @@ typedef struct pgs_batch_tuning
 	uint32_t cta_threads;    /* 128, 256 or 512 */
 	uint32_t ctas_per_sm;    /* persistent CTAs per SM (1 .. 1024 / cta_threads) */
 	uint32_t largest_first;  /* order work items by size within a round */
+	/* Streams with at least this many primitives per frame run as their own
+	 * branch of the replay graph (their passes back to back on their own
+	 * stream, no round barriers); the others share the batched kernel.
+	 * 0: every stream goes through the rounds. */
+	uint32_t solo_min_prims;
 } pgs_batch_tuning;
 
 pgs_batch *pgs_batch_create(int device, int *status);

@@ -1496,6 +1496,8 @@ struct BatchEngine
 	// Tuning: persistent CTA size and CTAs per SM.
 	uint32_t block = 256, ctas_per_sm = 4;
 	bool largest_first = true;
+	uint32_t solo_min_prims = 0;
+	std::vector<bool> solo; // per stream, decided at the start of a run
 
 	cudaGraphExec_t exec = nullptr;
 	uint32_t launches_per_replay = 0;
@@ -1558,22 +1560,36 @@ struct BatchEngine
 		}
 	}
 
-	int fork()
+	// Round barriers involve the batched streams only; `all` includes the
+	// solo streams (start and end of a run).
+	int fork(bool all = false)
 	{
 		CUDA_TRY(cudaEventRecord(fork_ev, master));
-		for (CudaBackend *b : streams)
-			CUDA_TRY(cudaStreamWaitEvent(b->stream, fork_ev, 0));
+		for (size_t i = 0; i < streams.size(); i++)
+			if (all || !solo[i])
+				CUDA_TRY(cudaStreamWaitEvent(streams[i]->stream, fork_ev, 0));
 		return PGS_OK;
 	}
 
-	int join()
+	int join(bool all = false)
 	{
 		for (size_t i = 0; i < streams.size(); i++)
 		{
+			if (!all && solo[i])
+				continue;
 			CUDA_TRY(cudaEventRecord(join_ev[i], streams[i]->stream));
 			CUDA_TRY(cudaStreamWaitEvent(master, join_ev[i], 0));
 		}
 		return PGS_OK;
+	}
+
+	static uint64_t frame_prims(const CudaBackend *b)
+	{
+		uint64_t n = 0;
+		for (const Op &op : b->ops)
+			if (op.type == OP_PASS)
+				n += op.pass.num_prims;
+		return n;
 	}
 
 	template <int BLOCK>
@@ -1609,7 +1625,10 @@ struct BatchEngine
 		}
 		if (counters_cap)
 			CUDA_TRY(cudaMemsetAsync(d_counters, 0, counters_cap * sizeof(uint32_t), master));
-		int r = fork();
+		solo.assign(streams.size(), false);
+		for (size_t s = 0; s < streams.size(); s++)
+			solo[s] = solo_min_prims && frame_prims(streams[s]) >= solo_min_prims;
+		int r = fork(true);
 		if (r)
 			return r;
 		if (reset)
@@ -1620,12 +1639,27 @@ struct BatchEngine
 				CUDA_TRY(cudaMemcpyAsync(b->d_clut, b->d_reset_clut, size_t(PGS_CLUT_INSTANCES) * PGS_CLUT_SIZE_BYTES,
 				                         cudaMemcpyDeviceToDevice, b->stream));
 			}
+		// Solo streams: the whole frame on the stream's own CUDA stream.
+		for (size_t s = 0; s < streams.size(); s++)
+		{
+			if (!solo[s])
+				continue;
+			for (const Op &op : streams[s]->ops)
+			{
+				r = streams[s]->execute(op);
+				if (r)
+					return r;
+			}
+			cur[s].op = streams[s]->ops.size();
+		}
 		for (;;)
 		{
 			// Round: every stream up to and including the start of its next pass.
 			bool any = false;
 			for (size_t s = 0; s < streams.size(); s++)
 			{
+				if (solo[s])
+					continue;
 				CudaBackend *b = streams[s];
 				Cursor &c = cur[s];
 				c.pass = nullptr;
@@ -1723,7 +1757,7 @@ struct BatchEngine
 				if (r)
 					return r;
 			}
-		r = join();
+		r = join(true);
 		if (r)
 			return r;
 		uint32_t total = kernels;
@@ -2054,6 +2088,7 @@ int pgs_batch_set_tuning(pgs_batch *batch, const pgs_batch_tuning *tuning)
 	batch->e.block = block;
 	batch->e.ctas_per_sm = tuning->ctas_per_sm;
 	batch->e.largest_first = tuning->largest_first != 0;
+	batch->e.solo_min_prims = tuning->solo_min_prims;
 	batch->e.invalidate();
 	return PGS_OK;
 }
@@ -2065,6 +2100,7 @@ int pgs_batch_get_tuning(pgs_batch *batch, pgs_batch_tuning *tuning)
 	tuning->cta_threads = batch->e.block;
 	tuning->ctas_per_sm = batch->e.ctas_per_sm;
 	tuning->largest_first = batch->e.largest_first;
+	tuning->solo_min_prims = batch->e.solo_min_prims;
 	return PGS_OK;
 }
 
@@ -2074,8 +2110,9 @@ int pgs_batch_autotune(pgs_batch *batch, uint32_t trials, int reset_vram, pgs_ba
 		return PGS_ERROR_INVALID_ARGUMENT;
 	BatchEngine &e = batch->e;
 	static const pgs_batch_tuning candidates[] = {
-		{ 128, 8, 1 }, { 128, 4, 1 }, { 256, 4, 1 }, { 256, 2, 1 }, { 512, 2, 1 }, { 512, 1, 1 },
-		{ 256, 4, 0 },
+		{ 128, 8, 1, 0 }, { 128, 4, 1, 0 }, { 256, 4, 1, 0 }, { 256, 2, 1, 0 }, { 512, 2, 1, 0 }, { 512, 1, 1, 0 },
+		{ 256, 4, 0, 0 }, { 512, 2, 1, 100000 }, { 512, 2, 1, 50000 }, { 512, 2, 1, 20000 }, { 256, 4, 1, 50000 },
+		{ 256, 4, 1, 20000 },
 	};
 	cudaEvent_t ev[2];
 	CUDA_TRY(cudaSetDevice(e.device));

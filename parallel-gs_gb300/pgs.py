@@ -67,7 +67,8 @@ class CircuitParams(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("cta_threads", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("largest_first", C.c_uint32)]
+    _fields_ = [("cta_threads", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("largest_first", C.c_uint32),
+                ("solo_min_prims", C.c_uint32)]
 
 
 class BackendStats(C.Structure):
@@ -427,21 +428,22 @@ class Batch:
     def replay(self, count: int = 1, reset_vram: bool = True, use_graph: bool = True) -> None:
         check(self.lib.pgs_batch_replay(self.handle, count, int(reset_vram), int(use_graph)), "batch_replay")
 
-    def set_tuning(self, cta_threads: int, ctas_per_sm: int, largest_first: bool = True) -> None:
-        t = BatchTuning(cta_threads, ctas_per_sm, int(largest_first))
+    def set_tuning(self, cta_threads: int, ctas_per_sm: int, largest_first: bool = True, solo_min_prims: int = 0) -> None:
+        t = BatchTuning(cta_threads, ctas_per_sm, int(largest_first), solo_min_prims)
         check(self.lib.pgs_batch_set_tuning(self.handle, C.byref(t)), "batch_set_tuning")
 
     def tuning(self) -> dict:
         t = BatchTuning()
         check(self.lib.pgs_batch_get_tuning(self.handle, C.byref(t)), "batch_get_tuning")
-        return {"cta_threads": t.cta_threads, "ctas_per_sm": t.ctas_per_sm, "largest_first": bool(t.largest_first)}
+        return {"cta_threads": t.cta_threads, "ctas_per_sm": t.ctas_per_sm, "largest_first": bool(t.largest_first),
+                "solo_min_prims": t.solo_min_prims}
 
     def autotune(self, trials: int = 3, reset_vram: bool = True) -> tuple[dict, float]:
         t = BatchTuning()
         ms = C.c_float(0.0)
         check(self.lib.pgs_batch_autotune(self.handle, trials, int(reset_vram), C.byref(t), C.byref(ms)), "autotune")
-        return ({"cta_threads": t.cta_threads, "ctas_per_sm": t.ctas_per_sm, "largest_first": bool(t.largest_first)},
-                float(ms.value))
+        return ({"cta_threads": t.cta_threads, "ctas_per_sm": t.ctas_per_sm, "largest_first": bool(t.largest_first),
+                 "solo_min_prims": t.solo_min_prims}, float(ms.value))
 
     def stream(self) -> int:
         return self.lib.pgs_batch_stream(self.handle)

@@ -118,3 +118,11 @@ def test_autotune_keeps_results():
         batch.close()
         for be in backends:
             be.close()
+
+
+@pytest.mark.parametrize("solo", [1, 2500, 70000])
+def test_batched_replay_solo_streams(solo):
+    """Streams at or above `solo_min_prims` run as their own graph branches, the
+    rest through the batched rounds (all solo, mixed, multi-pass solo)."""
+    frames = [gsgen.stream_c3(i, num_primitives=n) for i, n in ((60, 1200), (61, 3000), (62, 800), (63, 70000))]
+    check_batch(frames, tuning=(512, 2, True, solo))
