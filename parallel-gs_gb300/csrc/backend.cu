@@ -2111,8 +2111,8 @@ int pgs_batch_autotune(pgs_batch *batch, uint32_t trials, int reset_vram, pgs_ba
 	BatchEngine &e = batch->e;
 	static const pgs_batch_tuning candidates[] = {
 		{ 128, 8, 1, 0 }, { 128, 4, 1, 0 }, { 256, 4, 1, 0 }, { 256, 2, 1, 0 }, { 512, 2, 1, 0 }, { 512, 1, 1, 0 },
-		{ 256, 4, 0, 0 }, { 512, 2, 1, 100000 }, { 512, 2, 1, 50000 }, { 512, 2, 1, 20000 }, { 256, 4, 1, 50000 },
-		{ 256, 4, 1, 20000 },
+		{ 256, 4, 0, 0 }, { 512, 2, 1, 100000 }, { 512, 2, 1, 50000 }, { 512, 2, 1, 20000 }, { 512, 2, 1, 10000 },
+		{ 512, 2, 1, 5000 }, { 512, 2, 1, 2000 }, { 256, 4, 1, 20000 }, { 256, 4, 1, 5000 }, { 512, 2, 1, 1 },
 	};
 	cudaEvent_t ev[2];
 	CUDA_TRY(cudaSetDevice(e.device));
