@@ -280,6 +280,54 @@ def cpu_baseline_sample(args) -> dict:
         return {"value": None, "unit": "frames/s", "cores": 1, "kind": "port", "sample": "failed: %s" % e}
 
 
+def tiny_stream_mix(local, n=64, prims=400):
+    """Where the batched rounds pay: many small streams (400 primitives each).
+    Frames/s of the per-frame graphs one after another, of the batched rounds
+    (solo threshold 0) and of one graph with every stream as its own branch."""
+    import torch
+    import gsgen
+    import pgs
+    backends = []
+    for i in range(n):
+        f = gsgen.stream_c3(1000 + i, num_primitives=prims)
+        ss_log2 = {1: 0, 2: 1, 4: 2}[f.super_sampling]
+        be = pgs.CudaBackend(local, max_samples_log2=ss_log2, arena_mib=4)
+        gs = pgs.GSInterface(be, super_sampling=f.super_sampling, ordered=f.ordered)
+        be.begin_record()
+        gs.gif_transfer(0, f.data)
+        gs.flush()
+        be.end_record()
+        gs.close()
+        backends.append(be)
+    out = {"streams": n, "primitives_per_stream": prims}
+    try:
+        for be in backends:
+            be.replay(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            for be in backends:
+                be.replay(1)
+                torch.cuda.synchronize()
+        out["plain_fps"] = 3 * n / (time.perf_counter() - t0)
+        for name, tuning in (("batched_rounds_fps", (256, 4, True, 0)), ("graph_branches_fps", (512, 2, True, 1))):
+            batch = pgs.Batch(local)
+            for be in backends:
+                batch.add(be)
+            batch.set_tuning(*tuning)
+            batch.replay(2)
+            batch.synchronize()
+            t0 = time.perf_counter()
+            batch.replay(10)
+            batch.synchronize()
+            out[name] = 10 * n / (time.perf_counter() - t0)
+            batch.close()
+    finally:
+        for be in backends:
+            be.close()
+    return out
+
+
 def run_c3(args, frames, rank, world, local):
     """64 mixed streams: plain per-frame graphs one after another, the same
     graphs launched concurrently on their own streams, and the batched replay
@@ -416,6 +464,7 @@ def run_c3(args, frames, rank, world, local):
     cpu = None
     if not (args.quick or args.no_cpu_baseline):
         cpu = cpu_baseline_sample_expr("[gsgen.stream_c3(i) for i in range(4)]", "streams 0-3 of 64, one thread")
+    tiny_mix = tiny_stream_mix(local) if rank == 0 and not args.quick else None
     out = {
         "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -428,6 +477,7 @@ def run_c3(args, frames, rank, world, local):
         "concurrent_per_frame_fps": concurrent_fps,
         "batched_wall_fps": batched_wall_fps,
         "batched_vs_plain": fps / plain_fps,
+        "tiny_stream_mix": tiny_mix,
         "autotuned": dict(tuning, ms_per_replay=tune_ms),
         "replay_verified": verified,
         "gpu_launches": launches * args.steps,
