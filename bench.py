@@ -183,7 +183,7 @@ def issue_roofline(inst_per_frame, shade_s: float, clk: dict):
 
 
 def algorithmic_bytes(frame, ss: int) -> dict:
-    """Bytes a frame must move at minimum (see DESIGN.md): prim records in,
+    """Bytes a frame must move at minimum: prim records in,
     setup records written and read, FB/Z read+write per pixel for plane 0,
     the reference plane and every sample, texture and CLUT bytes, and the
     VRAM read-back."""

@@ -10,7 +10,7 @@ project's own kernels (pgs_upscaler_*); evaluation runs the full frames of
 held-out seeds and reports PSNR and maximum absolute error over RGB against
 the exact 16x resolve, next to the same figures for the 1x input.
 
-    python parallel-gs_gb300/upscaler_train.py --out gpurun_out/upscaler
+    python parallel-gs_gb300/upscaler_train.py --out upscaler_out
 
 writes weights.npy (the flat FP32 parameter vector) and metrics.json there.
 """
@@ -152,7 +152,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=8000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--out", default="gpurun_out/upscaler")
+    ap.add_argument("--out", default="upscaler_out")
     ap.add_argument("--tensor-path", type=int, default=2,
                     help="32->32 layers: 0 mma.sync, 1 or 2 tcgen05 with that many persistent CTAs per SM")
     args = ap.parse_args()
