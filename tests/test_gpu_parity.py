@@ -218,3 +218,42 @@ def test_aliased_frame_depth_parity(seed):
     f = gsgen.frame_alias(seed)
     ref, out = run_both(f)
     assert_same(ref, out)
+
+
+def _extremes_frame(kind):
+    """Edge cases: the whole 4 MiB as one 1024x1024 CT32 frame (no depth) with
+    screen-filling and degenerate primitives; a 2048-wide CT16 frame with
+    primitives beyond the 12.4 range edges; an empty draw list."""
+    s = gsgen.GifStream()
+    rng = np.random.default_rng(77)
+    if kind == "full_vram":
+        w, h = 1024, 1024
+        gsgen._frame_setup(s, 0, 16, gsgen.PSMCT32, 0, gsgen.PSMZ24, w, h, gsgen.test_reg(zte=1, ztst=1))
+        s.ad([(gsgen.ZBUF_1, gsgen.zbuf_reg(0, gsgen.PSMZ24, 1))])
+        pts = [(0, 0), (w * 16, 0), (0, h * 16), (w * 16, h * 16), (0, h * 16), (w * 16, 0),
+               (100, 100), (100, 100), (100, 100),            # zero area
+               (0, 0), (w * 16, h * 16 // 2), (w * 16, h * 16 // 2 + 1)]  # sliver
+    elif kind == "wide_ct16":
+        w, h = 2048, 1024
+        gsgen._frame_setup(s, 0, 32, gsgen.PSMCT16, 0, gsgen.PSMZ16, w, h, gsgen.test_reg(zte=1, ztst=1))
+        s.ad([(gsgen.ZBUF_1, gsgen.zbuf_reg(0, gsgen.PSMZ16, 1))])
+        pts = [(0, 0), (0xFFFF, 0), (0, 0xFFFF), (40000, 100), (65535, 65535), (100, 40000)]
+    else:
+        w, h = 64, 64
+        gsgen._frame_setup(s, 0, 1, gsgen.PSMCT32, 10, gsgen.PSMZ24, w, h, gsgen.test_reg(zte=1, ztst=1))
+        return gsgen.Frame("empty", s.tobytes(), 4, True, 0, {"width": w, "height": h, "fbp": 0, "zbp": 10})
+    n = len(pts)
+    q = np.zeros((n, 2, 2), dtype=np.uint64)
+    q[:, 0] = gsgen.q_rgbaq(rng.integers(0, 256, (n, 4)))
+    q[:, 1] = gsgen.q_xyz2(np.array([p[0] for p in pts]), np.array([p[1] for p in pts]), np.zeros(n, dtype=np.int64))
+    s.packed(gsgen.prim_reg(gsgen.PRIM_TRI, iip=1), [gsgen.D_RGBAQ, gsgen.D_XYZ2], q.reshape(-1, 2))
+    return gsgen.Frame(kind, s.tobytes(), 1, True, n // 3, {"width": w, "height": h, "fbp": 0, "zbp": 0})
+
+
+@pytest.mark.parametrize("kind,ss", [("full_vram", 1), ("full_vram", 16), ("wide_ct16", 1), ("wide_ct16", 4),
+                                     ("empty", 4)])
+def test_extreme_sizes(kind, ss):
+    f = _extremes_frame(kind)
+    f = gsgen.Frame(f.name, f.data, ss, True, f.num_primitives, f.meta)
+    ref, out = run_both(f)
+    assert_same(ref, out)
