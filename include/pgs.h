@@ -428,7 +428,10 @@ int pgs_upscaler_get_error(void *upscaler, uint32_t *flags);
 void *pgs_upscaler_stream(void *upscaler);
 /* Self-test of the tcgen05 tensor-core path: a 128x32x32 BF16 product from
  * shared memory (mode 0: no-swizzle operand layout, 1: 64-byte swizzle) read
- * back from tensor memory into out (128 x 32 floats, row-major). */
+ * back from tensor memory into out (128 x 32 floats, row-major).  Mode 2
+ * issues nothing and waits on the completion barrier with a short limit: the
+ * wait runs out, the kernel releases its tensor memory and returns, and the
+ * call reports PGS_ERROR_DEVICE_FLAG (the bounded-wait failure path). */
 int pgs_umma_selftest(int device, uint32_t mode, float *out);
 int pgs_upscaler_synchronize(void *upscaler);
 

@@ -88,6 +88,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 	return false;
 }
 
+// Bounded wait with an explicit poll limit.
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t *bar, uint32_t parity, uint32_t limit)
+{
+	const uint32_t a = smem_addr(bar);
+	for (uint32_t i = 0; i < limit; i++)
+	{
+		uint32_t done;
+		asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+		             : "=r"(done)
+		             : "r"(a), "r"(parity)
+		             : "memory");
+		if (done)
+			return true;
+	}
+	return false;
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 {
 	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_addr(bar)) : "memory");

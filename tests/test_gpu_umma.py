@@ -22,3 +22,13 @@ def expected():
 def test_tcgen05_product(mode):
     out = pgs.umma_selftest(mode)
     assert np.array_equal(out, expected())
+
+
+def test_bounded_wait_expiry_is_reported_and_context_survives():
+    """Mode 2 waits on an mbarrier nothing arrives at: the kernel gives up after
+    its poll limit, frees tensor memory, and the host sees the device flag; the
+    context stays usable for the next tcgen05 product."""
+    with pytest.raises(pgs.PGSError) as e:
+        pgs.umma_selftest(2)
+    assert e.value.status == pgs.STATUS_CODES["PGS_ERROR_DEVICE_FLAG"]
+    assert np.array_equal(pgs.umma_selftest(1), expected())
