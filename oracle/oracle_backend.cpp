@@ -50,7 +50,6 @@ static const uint32_t VRAM = 4u * 1024u * 1024u;
 static bool is16(uint32_t p) { return p == CT16 || p == CT16S || p == Z16 || p == Z16S; }
 static bool is24(uint32_t p) { return p == CT24 || p == Z24; }
 static bool is32(uint32_t p) { return p == CT32 || p == Z32; }
-static bool is_palette(uint32_t p) { return p == T8 || p == T4 || p == T8H || p == T4HL || p == T4HH; }
 
 static uint32_t bpp(uint32_t p)
 {

@@ -2121,7 +2121,7 @@ int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_
 	circuit_setup(gs, circuit, field_phase, force_progressive, high_res, c, phase_offset);
 	*width = c.width;
 	*height = c.height;
-	if (uint64_t(c.width) * c.height * 4u > dst_size || (!dst && c.width * c.height))
+	if (uint64_t(c.width) * c.height * 4u > dst_size || (!dst && c.width && c.height))
 		return PGS_ERROR_CAPACITY;
 	if (c.width == 0 || c.height == 0)
 		return PGS_OK;
@@ -2398,7 +2398,7 @@ int pgs_gs_vsync(pgs_gs *gs, const pgs_vsync_info *info, void *dst, uint64_t dst
 	res->interlace_phase = info->phase;
 	res->width = m.width;
 	res->height = m.deinterlace ? 2 * m.height : m.height;
-	if (uint64_t(res->width) * res->height * 4u > dst_size || (!dst && res->width * res->height))
+	if (uint64_t(res->width) * res->height * 4u > dst_size || (!dst && res->width && res->height))
 		return PGS_ERROR_CAPACITY;
 	return gs->ops->vsync(gs->be, &m, dst);
 }
