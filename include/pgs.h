@@ -128,6 +128,13 @@ typedef struct pgs_texture_desc
 	 * from MIPTBP1 / MIPTBP2; zero for levels not sampled. */
 	uint32_t levels;
 	uint32_t mip[6];
+	/* Super-sampled texture (levels == 1): 1 + the frame's samples per pixel
+	 * layers -- layer 0 the single-sampled image, layer s + 1 sample s read
+	 * through the reference plane (create_cached_texture with desc.samples,
+	 * gs/gs_renderer.cpp:1317-1386; upload.comp SUPER_SAMPLED).  0 or 1: a
+	 * plain texture. */
+	uint32_t samples;
+	uint32_t padding;
 } pgs_texture_desc;
 
 /* One framebuffer instance inside a render pass (RenderPass::Instance,
@@ -162,6 +169,8 @@ typedef struct pgs_render_pass
 	uint32_t flush_reason;
 	/* Some primitive samples mip levels (TEX1.MXL > 0 with a mipmapping MMIN). */
 	uint32_t has_mipmap;
+	/* Some texture of the pass is super-sampled (pgs_texture_desc.samples). */
+	uint32_t has_ss_textures;
 } pgs_render_pass;
 
 /* A VRAM transfer (CopyDescriptor, gs/gs_renderer.hpp).  For HOST_TO_LOCAL,
@@ -578,6 +587,10 @@ int pgs_gs_read_transfer_fifo(pgs_gs *gs, void *data, uint32_t num_128b_words);
 int pgs_gs_consume_flush_stats(pgs_gs *gs, pgs_flush_stats *stats);
 /* GSInterface::set_super_sampling_rate. */
 int pgs_gs_set_super_sampling_rate(pgs_gs *gs, uint32_t super_sampling, uint32_t ordered_grid);
+/* The super_sampled_textures argument of set_super_sampling_rate
+ * (gs/gs_interface.hpp:258): sprites sampling pages a super-sampled pass wrote
+ * read per-sample texture layers.  Ignored at 1x. */
+int pgs_gs_set_super_sampled_textures(pgs_gs *gs, int enable);
 
 #ifdef __cplusplus
 }

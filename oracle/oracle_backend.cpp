@@ -236,6 +236,8 @@ struct Backend
 	uint32_t rate_x = 0, rate_y = 0;
 	uint32_t num_planes = 1;
 	std::vector<uint8_t> vram;
+	// Phase LUT of super-sampled texture filtering for the current rate.
+	uint32_t phase_lut[64 * 64 * 2 + 32 * 32] = {};
 	// Deinterlacer history: the last four merged fields, newest first.
 	std::vector<uint32_t> fields[4];
 	uint32_t field_w = 0, field_h = 0;
@@ -265,9 +267,9 @@ struct Backend
 	// triangle_setup.comp main_inner.
 	void triangle_setup(uint32_t index, const pgs_vertex_position *vp, const pgs_vertex_attribute *va,
 	                    pgs_primitive_attribute &pa, Setup &out, TAttr &ta, const uint32_t *opaque_fbmasks,
-	                    int srx, int sry, uint32_t packed_z_shift, int32_t &bucket_out)
+	                    int srx, int sry, uint32_t packed_z_shift, int32_t &bucket_out,
+	                    const pgs_render_pass *rp = nullptr, uint32_t blur_mask = 0)
 	{
-		(void)srx;
 		bucket_out = -1;
 		int order[3] = { 0, 1, 2 };
 		uint32_t st = pa.state;
@@ -620,6 +622,55 @@ struct Backend
 		if (pa.fbmsk != opaque_fbmask && (s & (1u << 14)) != 0)
 			pa.state = s & ~(1u << 14);
 
+		// Super-sampled textures (triangle_setup.comp:677-825; FORCE_LINEAR_SUPER_SAMPLE
+		// off): per sprite, sample-to-sample mapping for nearest blits and
+		// perspective, the single-sampled layer for nearest downsamples and
+		// blur kernels, the resolved layer for linear upsamples; per-sample
+		// interpolation (no attribute snap, i/j moved to the mean sample
+		// position) for what stays per-sample.
+		const uint32_t PER_SAMPLE = 1u << 24, MAPPING = 1u << 25, RESOLVED = 1u << 26;
+		if (sry != 0 && rp && (pa.tex & (PER_SAMPLE | MAPPING)) == PER_SAMPLE)
+		{
+			uint32_t tex = pa.tex;
+			const int32_t udx = std::abs(int32_t(at1.u) - int32_t(at0.u)), udy = std::abs(int32_t(at1.v) - int32_t(at0.v));
+			const int32_t ddx = std::abs(d[0] - a[0]), ddy = std::abs(d[1] - a[1]);
+			if ((tex & (1u << 16)) == 0)
+			{
+				if (perspective)
+					tex |= MAPPING;
+				else if (udx > ddx + 1 || udy > ddy + 1)
+					tex &= ~PER_SAMPLE;
+				else if (udx >= ddx - 16 || udy >= ddy - 16)
+				{
+					const uint32_t bm = rp->states[std::min<uint32_t>(pa.state & 0xfffu, std::max<uint32_t>(rp->num_states, 1) - 1)].blend_mode;
+					const uint32_t inst = bfe(pa.state, 29, 3);
+					const bool blur = ((blur_mask >> inst) & 1u) && (bm & (1u << 9)) && !(pa.state & (1u << 12)) &&
+					                  bfe(bm, 11, 2) == 0 && bfe(bm, 13, 2) == 2 && bfe(bm, 17, 2) == 1;
+					if (blur)
+						tex &= ~PER_SAMPLE;
+					else
+						tex |= MAPPING;
+				}
+			}
+			else if (!perspective)
+			{
+				if (udx > ddx + 1 && udy > ddy + 1)
+					tex &= ~PER_SAMPLE;
+				else if (ddx >= 2 * udx && ddy >= 2 * udy)
+					tex |= RESOLVED;
+			}
+			pa.tex = tex;
+			if ((tex & (PER_SAMPLE | MAPPING)) == PER_SAMPLE)
+			{
+				pa.state &= ~(1u << 26);
+				const float corner = 8.0f * average_sampling_offset(uint32_t(srx), uint32_t(sry));
+				const float di_dcorner = float(pb_[0] + pb_[1]) * corner;
+				const float dj_dcorner = float(pc_[0] + pc_[1]) * corner;
+				out.error_i = out.error_i - di_dcorner * inv_area_scaled;
+				out.error_j = out.error_j - dj_dcorner * inv_area_scaled;
+			}
+		}
+
 		if (sry != 0 && !sprite)
 		{
 			bool per_sample = multisample;
@@ -718,6 +769,7 @@ struct Backend
 		int32_t hx, hy; // high-resolution coordinate
 		Request pending;
 		uint32_t pending_prim;
+		uint32_t index; // sample index within the pixel
 	};
 
 	// evaluate_coverage (gs/shaders/intersect.h:156-244).
@@ -1043,10 +1095,214 @@ struct Backend
 	// [0, MXL]; MMIN applies when the LOD is positive; trilinear blends
 	// floor(fract * 16) / 16 of the next level.  Levels past the texture's
 	// chain read its last level.
+	// Texel of layer `layer` of a super-sampled texture: layer 0 the
+	// single-sampled texel, layer s + 1 sample s where the reference plane
+	// marks it (upload.comp SUPER_SAMPLED, :131-220).
+	uint32_t texel_layer(const pgs_texture_desc &t, uint32_t layer, int32_t x, int32_t y)
+	{
+		if (layer == 0)
+			return texel(t, 0, x, y);
+		const uint32_t s = layer - 1;
+		const uint32_t a = swizzle(uint32_t(x), uint32_t(y), t.tbp0, t.tbw, t.psm);
+		switch (t.psm)
+		{
+		case CT24: case Z24:
+		{
+			uint32_t col = w32(0, a), ref = w32(1, a);
+			if (ref != 0)
+				col = (w32(2 + s, a) & ref) | (col & ~ref);
+			col &= 0xffffffu;
+			uint32_t al = (t.aem && col == 0) ? 0 : t.ta0;
+			return col | (al << 24);
+		}
+		case CT16: case CT16S: case Z16: case Z16S:
+		{
+			uint32_t c = w16(0, a);
+			if (w16(1, a) == 0xffff)
+				c = w16(2 + s, a);
+			uint32_t r = (c & 0x1f) << 3, g = ((c >> 5) & 0x1f) << 3, b = ((c >> 10) & 0x1f) << 3;
+			uint32_t al = (t.aem && c == 0) ? 0 : ((c & 0x8000) ? t.ta1 : t.ta0);
+			return r | (g << 8) | (b << 16) | (al << 24);
+		}
+		case T8:
+		{
+			uint32_t idx = w8(0, a);
+			if (w8(1, a) == 0xff)
+				idx = w8(2 + s, a);
+			return clut_color(t, idx);
+		}
+		case T8H:
+		{
+			uint32_t idx = w8(0, 4 * a + 3);
+			if (w8(1, 4 * a + 3) == 0xff)
+				idx = w8(2 + s, 4 * a + 3);
+			return clut_color(t, idx);
+		}
+		default:
+		{
+			uint32_t c = w32(0, a);
+			if (w32(1, a) == 0xffffffffu)
+				c = w32(2 + s, a);
+			return c;
+		}
+		}
+	}
+
+	static float average_sampling_offset(uint32_t rx, uint32_t ry)
+	{
+		// get_average_sampling_offset (utils.h:108-126).
+		if (rx == ry)
+		{
+			const int rate = 1 << ry;
+			return 0.5f * (float(rate - 1) / float(rate));
+		}
+		if (rx == 0 && ry == 1) return 0.25f;
+		if (rx == 1 && ry == 2) return (0.125f + 0.625f) * 0.5f;
+		if (rx == 0 && ry == 2) return 6.0f / 16.0f;
+		if (rx == 1 && ry == 3) return (6.0f + 22.0f) / 64.0f;
+		return 0.0f;
+	}
+
+	// Super-sampled texture sample (ubershader.comp:1155-1212): sample
+	// mapping -> the shading sample's layer, resolved -> layer 0, otherwise
+	// the phase LUT's taps around the texel below the sampling position with
+	// unorm8 weights (one tap for nearest filtering or on a clamped region
+	// edge); coordinates snap as for plain textures, taps wrap like them.
+	void sample_layered(const PassCtx &P, const pgs_texture_desc &t, uint32_t tex_word, float u, float v,
+	                    bool perspective, uint32_t sample, uint32_t rx, uint32_t ry, uint32_t rgba[4])
+	{
+		const bool clamp_s = tex_word & (1u << 19), clamp_t = tex_word & (1u << 20);
+		const bool mag_linear = tex_word & (1u << 16);
+		if (tex_word & ((1u << 25) | (1u << 26)))
+		{
+			const uint32_t layer = (tex_word & (1u << 25)) ? std::min(sample + 1, t.samples) : 0u;
+			float w = float(1u << t.tw_log2), h = float(1u << t.th_log2);
+			float uu = perspective ? u * w : u, vv = perspective ? v * h : v;
+			if (clamp_s)
+			{
+				float lo = t.wms == 2 ? float(t.minu) : 0.0f, hi = t.wms == 2 ? float(t.maxu) : w - 1.0f;
+				uu = std::min(std::max(uu, lo + 0.5f), hi + 0.5f);
+			}
+			if (clamp_t)
+			{
+				float lo = t.wmt == 2 ? float(t.minv) : 0.0f, hi = t.wmt == 2 ? float(t.maxv) : h - 1.0f;
+				vv = std::min(std::max(vv, lo + 0.5f), hi + 0.5f);
+			}
+			float fu = uu * 16.0f;
+			fu = fu + (1.0f / 64.0f);
+			float fv = vv * 16.0f;
+			fv = fv + (1.0f / 64.0f);
+			const int32_t ku = int32_t(std::floor(fu)), kv = int32_t(std::floor(fv));
+			if (!mag_linear)
+			{
+				uint32_t c = texel_layer(t, layer, wrap_coord(ku >> 4, t.wms, t.tw_log2, t.minu, t.maxu),
+				                         wrap_coord(kv >> 4, t.wmt, t.th_log2, t.minv, t.maxv));
+				for (int k = 0; k < 4; k++)
+					rgba[k] = (c >> (8 * k)) & 0xffu;
+				return;
+			}
+			const int32_t bu = ku - 8, bv = kv - 8;
+			const int32_t x0 = bu >> 4, y0 = bv >> 4;
+			const uint32_t fx = uint32_t(bu) & 15u, fy = uint32_t(bv) & 15u;
+			const int32_t xs[2] = { wrap_coord(x0, t.wms, t.tw_log2, t.minu, t.maxu), wrap_coord(x0 + 1, t.wms, t.tw_log2, t.minu, t.maxu) };
+			const int32_t ys[2] = { wrap_coord(y0, t.wmt, t.th_log2, t.minv, t.maxv), wrap_coord(y0 + 1, t.wmt, t.th_log2, t.minv, t.maxv) };
+			const uint32_t wx[2] = { 16 - fx, fx }, wy[2] = { 16 - fy, fy };
+			uint32_t acc[4] = { 0, 0, 0, 0 };
+			for (int yy = 0; yy < 2; yy++)
+				for (int xx = 0; xx < 2; xx++)
+				{
+					const uint32_t wgt = wx[xx] * wy[yy];
+					if (!wgt)
+						continue;
+					const uint32_t c = texel_layer(t, layer, xs[xx], ys[yy]);
+					for (int k = 0; k < 4; k++)
+						acc[k] += wgt * ((c >> (8 * k)) & 0xffu);
+				}
+			for (int k = 0; k < 4; k++)
+			{
+				uint32_t q = acc[k] >> 8, r = acc[k] & 0xffu;
+				if (r > 128 || (r == 128 && (q & 1)))
+					q++;
+				rgba[k] = q;
+			}
+			return;
+		}
+		const float w = float(1u << t.tw_log2), h = float(1u << t.th_log2);
+		float uu = perspective ? u * w : u, vv = perspective ? v * h : v;
+		const int32_t rx0 = t.wms == 2 ? int32_t(t.minu) : 0;
+		const int32_t rx1 = t.wms == 2 ? int32_t(t.maxu) : (t.wms == 1 ? int32_t(w) - 1 : 0);
+		const int32_t ry0 = t.wmt == 2 ? int32_t(t.minv) : 0;
+		const int32_t ry1 = t.wmt == 2 ? int32_t(t.maxv) : (t.wmt == 1 ? int32_t(h) - 1 : 0);
+		if (clamp_s)
+			uu = std::min(std::max(uu, float(rx0) + 0.5f), float(rx1) + 0.5f);
+		if (clamp_t)
+			vv = std::min(std::max(vv, float(ry0) + 0.5f), float(ry1) + 0.5f);
+		const float shift = 0.5f - average_sampling_offset(rx, ry);
+		float su = uu + (1.0f / 1024.0f);
+		su = su - shift;
+		float sv = vv + (1.0f / 1024.0f);
+		sv = sv - shift;
+		const float fu = std::floor(su), fv = std::floor(sv);
+		const int32_t ix = int32_t(fu), iy = int32_t(fv);
+		const float pu = su - fu, pv = sv - fv;
+		uint32_t entry, weights = 0;
+		if (mag_linear)
+		{
+			const uint32_t lx = std::min(uint32_t(pu * 64.0f), 63u), ly = std::min(uint32_t(pv * 64.0f), 63u);
+			entry = phase_lut[(ly * 64 + lx) * 2];
+			weights = phase_lut[(ly * 64 + lx) * 2 + 1];
+		}
+		else
+		{
+			const uint32_t lx = std::min(uint32_t(pu * 32.0f), 31u), ly = std::min(uint32_t(pv * 32.0f), 31u);
+			entry = phase_lut[64 * 64 * 2 + ly * 32 + lx];
+		}
+		const bool force_nearest = !mag_linear || ((clamp_s || clamp_t) && (ix == rx0 || iy == ry0 || ix == rx1 || iy == ry1));
+		auto tap = [&](uint32_t layer, int32_t x, int32_t y) {
+			return texel_layer(t, std::min(layer + 1, t.samples), wrap_coord(x, t.wms, t.tw_log2, t.minu, t.maxu),
+			                   wrap_coord(y, t.wmt, t.th_log2, t.minv, t.maxv));
+		};
+		const uint32_t c0 = tap(entry & 15u, ix, iy);
+		if (force_nearest)
+		{
+			for (int k = 0; k < 4; k++)
+				rgba[k] = (c0 >> (8 * k)) & 0xffu;
+			return;
+		}
+		uint32_t acc[4];
+		for (int k = 0; k < 4; k++)
+			acc[k] = (weights & 0xffu) * ((c0 >> (8 * k)) & 0xffu);
+		for (uint32_t i = 1; i < 4; i++)
+		{
+			const uint32_t wi = (weights >> (8 * i)) & 0xffu;
+			if (!wi)
+				continue;
+			int32_t ox = int32_t((entry >> (16 + 4 * i)) & 3u), oy = int32_t((entry >> (18 + 4 * i)) & 3u);
+			if (ox >= 2) ox -= 4;
+			if (oy >= 2) oy -= 4;
+			const uint32_t c = tap((entry >> (4 * i)) & 15u, ix + ox, iy + oy);
+			for (int k = 0; k < 4; k++)
+				acc[k] += wi * ((c >> (8 * k)) & 0xffu);
+		}
+		for (int k = 0; k < 4; k++)
+		{
+			const uint32_t q = acc[k] / 255, r = acc[k] % 255;
+			rgba[k] = q + (2 * r > 255 ? 1u : 0u);
+		}
+	}
+
 	void sample_texture(const PassCtx &P, uint32_t tex_word, uint32_t tex2, float u, float v, float q,
-	                    bool perspective, float out[4])
+	                    bool perspective, uint32_t sample, uint32_t rx, uint32_t ry, float out[4])
 	{
 		const pgs_texture_desc &t = P.rp->textures[tex_word & 0xffffu];
+		if ((tex_word & (1u << 24)) && t.samples > 1)
+		{
+			uint32_t rgba[4];
+			sample_layered(P, t, tex_word, u, v, perspective, sample, rx, ry, rgba);
+			for (int k = 0; k < 4; k++)
+				out[k] = float(rgba[k]);
+			return;
+		}
 		bool clamp_s = tex_word & (1u << 19), clamp_t = tex_word & (1u << 20);
 		bool mag_linear = tex_word & (1u << 16), min_linear = tex_word & (1u << 17);
 		bool trilinear = tex_word & (1u << 18);
@@ -1110,7 +1366,8 @@ struct Backend
 	}
 
 	// compute_combined_color (gs/shaders/ubershader.comp:1260-1339).
-	void combined_color(const PassCtx &P, uint32_t pi, const Request &r, uint32_t combiner, float out[4])
+	void combined_color(const PassCtx &P, uint32_t pi, const Request &r, uint32_t combiner, float out[4],
+	                    uint32_t sample_index)
 	{
 		const TAttr &a = P.tattr[pi];
 		float col[4];
@@ -1146,7 +1403,8 @@ struct Backend
 			u = std::fmin(std::fmax(u, -2047.0f), 2047.0f);
 			v = std::fmin(std::fmax(v, -2047.0f), 2047.0f);
 			float tx[4];
-			sample_texture(P, P.prims[pi].tex, P.prims[pi].tex2, u, v, stq[2], r.perspective, tx);
+			sample_texture(P, P.prims[pi].tex, P.prims[pi].tex2, u, v, stq[2], r.perspective, sample_index,
+			               P.ss ? P.sr_x_log2 : 0u, P.ss ? P.sr_dim_log2 : 0u, tx);
 			switch (mode)
 			{
 			case 1:
@@ -1217,7 +1475,7 @@ struct Backend
 			return;
 
 		float cc[4];
-		combined_color(P, pi, r, sv.combiner, cc);
+		combined_color(P, pi, r, sv.combiner, cc, P.ss ? smp.index : 0u);
 		float fbc[4];
 		for (int k = 0; k < 4; k++)
 			fbc[k] = std::round(unorm(smp.color, k) * 255.0f);
@@ -1481,6 +1739,7 @@ struct Backend
 				sample_offset(s, P.sr_x_log2, D, ox, oy);
 			smp[s].hx = (px << D) + ox;
 			smp[s].hy = (py << D) + oy;
+			smp[s].index = s;
 			begin_sample(P, smp[s], s, fb_index, z_index);
 
 			Sample &S = smp[s];
@@ -2018,6 +2277,9 @@ struct Backend
 			const pgs_texture_desc &d = rp->textures[i];
 			if (d.levels > 7 || std::min(std::min(d.tw_log2, d.th_log2), 10u) + 1 < d.levels)
 				return PGS_ERROR_INVALID_ARGUMENT;
+			if (d.samples > 1 && (std::max<uint32_t>(d.levels, 1) != 1 || (d.samples & (d.samples - 1)) ||
+			                      d.samples > 16 || 2 + d.samples > num_planes))
+				return PGS_ERROR_INVALID_ARGUMENT;
 		}
 		std::vector<pgs_primitive_attribute> prims(rp->prims, rp->prims + rp->num_primitives);
 		std::vector<Setup> setup(rp->num_primitives);
@@ -2039,13 +2301,47 @@ struct Backend
 			srx = std::max<int>(srx, int(rp->instances[i].sampling_rate_x_log2));
 			sry = std::max<int>(sry, int(rp->instances[i].sampling_rate_y_log2));
 		}
+		// render_pass_instance_is_deduced_blur (gs/gs_renderer.cpp:1850-1884):
+		// an instance sampling one per-sample texture at two texel phases.
+		uint32_t blur = 0;
+		if (rp->num_primitives <= 64)
+			for (uint32_t inst = 0; inst < rp->num_instances; inst++)
+			{
+				uint32_t last = ~0u;
+				int32_t ph0 = 0, ph1 = 0;
+				for (uint32_t i = 0; i < rp->num_primitives; i++)
+				{
+					const pgs_primitive_attribute &pa = rp->prims[i];
+					if (bfe(pa.state, 29, 3) != inst || !(pa.tex & (1u << 24)))
+						continue;
+					if (pa.state & (1u << 18))
+						break;
+					const uint32_t ti = pa.tex & 0xffffu;
+					const int32_t a0 = int32_t(rp->attributes[3 * i].u) - rp->positions[3 * i].x;
+					const int32_t a1 = int32_t(rp->attributes[3 * i].v) - rp->positions[3 * i].y;
+					if (last == ti)
+					{
+						if (a0 != ph0 || a1 != ph1)
+						{
+							blur |= 1u << inst;
+							break;
+						}
+					}
+					else
+					{
+						ph0 = a0;
+						ph1 = a1;
+					}
+					last = ti;
+				}
+			}
 		HeuristicPush push[8] = {};
 		uint32_t packed_z_shift = heuristic_pushes(rp, push);
 		std::vector<int32_t> bucket(rp->num_primitives);
 		#pragma omp parallel for schedule(static)
 		for (uint32_t i = 0; i < rp->num_primitives; i++)
 			triangle_setup(i, rp->positions, rp->attributes, prims[i], setup[i], tattr[i], fbmasks, srx, sry,
-			               packed_z_shift, bucket[i]);
+			               packed_z_shift, bucket[i], rp, blur);
 		if (sry != 0)
 			single_sample_heuristic(rp, prims, bucket, push);
 		for (uint32_t i = 0; i < rp->num_primitives; i++)
@@ -2350,8 +2646,126 @@ struct Backend
 		return int(inst);
 	}
 
+	// GSRenderer::init_phase_lut (gs/gs_renderer.cpp:93-315): per 64 x 64
+	// sub-texel phase the four nearest sampling-grid points (sample id, texel
+	// offset in -1..1), the first in the centre texel, with tent weights over
+	// the falloff distance quantised to unorm8 summing to 255; per 32 x 32 phase
+	// the nearest sample.  Equal distances keep generation order.
+	void init_phase_lut(uint32_t rx, uint32_t ry)
+	{
+		std::fill(std::begin(phase_lut), std::end(phase_lut), 0u);
+		if (!rx && !ry)
+			return;
+		const int G = 64, n = 1 << (rx + ry);
+		struct Pt { int x, y; };
+		auto grid = [&](std::vector<Pt> &pts, bool nearest) {
+			pts.resize(n);
+			for (int i = 0; i < n; i++)
+			{
+				Pt q;
+				if (int(ry) - int(rx) == 2)
+				{
+					const int sparse[4] = { 0, 2, 3, 1 };
+					q = { (i / 8) * 4 + sparse[i % 4], i % 8 };
+				}
+				else
+				{
+					q.y = ((i >> 0) & 1) + ((i >> 2) & 1) * 2;
+					q.x = ((i >> 1) & 1) + ((i >> 3) & 1) * 2;
+					if (int(ry) - int(rx) == 1)
+						q.x = q.x * 2 + i % 2;
+				}
+				const int scale = G >> ry;
+				q.x *= scale;
+				q.y *= scale;
+				if (nearest)
+				{
+					q.x += (scale - 1) >> 1;
+					q.y += (scale - 1) >> 1;
+				}
+				pts[i] = q;
+			}
+		};
+		struct R { int sample, tx, ty, dx, dy, m; };
+		auto near = [&](int x, int y, const std::vector<Pt> &pts, int sup, std::vector<R> &res) {
+			res.clear();
+			for (int i = 0; i < n; i++)
+				for (int ty = -sup; ty <= sup; ty++)
+					for (int tx = -sup; tx <= sup; tx++)
+					{
+						int dx = std::abs(pts[i].x + G * tx - x), dy = std::abs(pts[i].y + G * ty - y);
+						res.push_back({ i, tx, ty, dx, dy, std::max(dx, dy) });
+					}
+			std::stable_sort(res.begin(), res.end(),
+			                 [](const R &a, const R &b) { return a.m == b.m ? a.dy < b.dy : a.m < b.m; });
+		};
+		std::vector<Pt> pts, pts_n;
+		grid(pts, false);
+		grid(pts_n, true);
+		std::vector<R> res;
+		int falloff = INT32_MAX;
+		for (int y = 0; y < G; y++)
+			for (int x = 0; x < G; x++)
+			{
+				near(x, y, pts, 1, res);
+				falloff = std::min(falloff, res[4].m);
+			}
+		for (int y = 0; y < G; y++)
+			for (int x = 0; x < G; x++)
+			{
+				near(x, y, pts, 1, res);
+				if (res[0].tx != 0 || res[0].ty != 0)
+					for (size_t i = 1; i < res.size(); i++)
+						if (res[i].tx == 0 && res[i].ty == 0)
+						{
+							if (i < 4)
+								std::swap(res[0], res[i]);
+							else
+							{
+								std::swap(res[3], res[i]);
+								std::swap(res[0], res[3]);
+							}
+							break;
+						}
+				uint32_t ex = 0, ey = 0, total = 0;
+				float wt[4], sum = 0.0f;
+				for (int i = 0; i < 4; i++)
+				{
+					ex |= uint32_t(res[i].sample) << (4 * i);
+					ex |= (uint32_t(res[i].tx) & 3u) << (4 * i + 16);
+					ex |= (uint32_t(res[i].ty) & 3u) << (4 * i + 18);
+					float fx = float(res[i].dx) / float(falloff), fy = float(res[i].dy) / float(falloff);
+					wt[i] = std::max(0.0f, 1.0f - fx) * std::max(0.0f, 1.0f - fy);
+					sum += wt[i];
+				}
+				if (sum < 0.001f)
+				{
+					for (float &v : wt)
+						v = 1.0f;
+					sum = 4.0f;
+				}
+				for (int i = 0; i < 3; i++)
+				{
+					float sc = wt[i] * 255.0f / sum;
+					uint32_t q = std::min<uint32_t>(uint32_t(sc + 0.5f), 255u - total);
+					total += q;
+					ey |= q << (8 * i);
+				}
+				ey |= (255u - total) << 24;
+				phase_lut[(y * G + x) * 2] = ex;
+				phase_lut[(y * G + x) * 2 + 1] = ey;
+			}
+		for (int y = 0; y < G / 2; y++)
+			for (int x = 0; x < G / 2; x++)
+			{
+				near(2 * x, 2 * y, pts_n, 0, res);
+				phase_lut[G * G * 2 + y * (G / 2) + x] = uint32_t(res[0].sample);
+			}
+	}
+
 	int set_ss(uint32_t x, uint32_t y)
 	{
+		init_phase_lut(x, y);
 		rate_x = x;
 		rate_y = y;
 		uint32_t planes = (x | y) ? 2u + (1u << (x + y)) : 1u;
@@ -2741,6 +3155,13 @@ uint64_t pgs_oracle_fragment_count(void *backend)
 uint32_t pgs_oracle_swizzle(uint32_t x, uint32_t y, uint32_t base, uint32_t stride, uint32_t psm)
 {
 	return oracle::swizzle(x, y, base, stride, psm);
+}
+
+// The phase LUT of the backend's current sampling rate (64 * 64 * 2 + 32 * 32 words).
+void pgs_oracle_phase_lut(void *backend, uint32_t *out)
+{
+	const auto *b = static_cast<const oracle::Backend *>(backend);
+	memcpy(out, b->phase_lut, sizeof(b->phase_lut));
 }
 
 // Copies up to `max` logged primitive states; returns the number logged.

@@ -41,6 +41,8 @@ def load_oracle() -> C.CDLL:
         lib.pgs_oracle_fragment_count.argtypes = [C.c_void_p]
         lib.pgs_oracle_fragment_count.restype = C.c_uint64
         lib.pgs_oracle_swizzle.argtypes = [C.c_uint32] * 5
+        lib.pgs_oracle_phase_lut.argtypes = [C.c_void_p, C.c_void_p]
+        lib.pgs_oracle_phase_lut.restype = None
         lib.pgs_oracle_swizzle.restype = C.c_uint32
         lib.pgs_oracle_state_log.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
         lib.pgs_oracle_state_log.restype = C.c_uint32
@@ -94,6 +96,8 @@ def render(frame, backend: pgs.Backend | None = None, planes: bool = False):
     Returns the 4 MiB plane-0 image, or all planes when `planes` is set."""
     be = backend or OracleBackend()
     gs = pgs.GSInterface(be, super_sampling=frame.super_sampling, ordered=frame.ordered)
+    if frame.meta.get("ssaa_textures"):
+        gs.set_super_sampled_textures(True)
     gs.gif_transfer(0, frame.data)
     vram = gs.read_vram()
     out = vram

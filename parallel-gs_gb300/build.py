@@ -69,7 +69,7 @@ def build_product(verbose: bool = False) -> Path:
         return out
     common = ["-I", str(INCLUDE), "-I", str(CSRC)]
     jobs = [
-        [nvcc, "-gencode", GENCODE, "-O3", "-lineinfo", "-fmad=false", "-std=c++17",
+        [nvcc, "-gencode", GENCODE, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-ffp-contract=off",
          "-Xcompiler", "-fPIC", *common, "-c", str(cu), "-o", str(o_cu)],
         ["g++", "-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", *common, "-c", str(cpp), "-o", str(o_cpp)],
         [nvcc, "-gencode", GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *common, "-c", str(cu_up),

@@ -67,7 +67,8 @@ struct PassOp
 	size_t pos_off, attr_off, prim_off, states_off, textures_off, images_off;
 	uint32_t num_texels, max_texels, max_levels;
 	uint32_t num_prims, num_states, num_textures;
-	uint32_t tile_size_log2, has_aa1, has_scanmsk, has_mipmap;
+	uint32_t tile_size_log2, has_aa1, has_scanmsk, has_mipmap, has_ss_textures;
+	uint32_t rp_is_blur_mask;
 	uint32_t num_instances;
 	pgs_rp_instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
 	// Host copy of the primitive records while the pass is submitted
@@ -90,6 +91,132 @@ struct Dispatch
 	uint32_t num_tiles;
 };
 
+// Phase LUT of super-sampled texture filtering (GSRenderer::init_phase_lut,
+// gs/gs_renderer.cpp:93-315): for each of 64 x 64 sub-texel phases, the four
+// nearest (sample, texel offset) points of the sampling grid -- the first one
+// always in the centre texel -- with tent weights over the falloff distance in
+// unorm8 summing to 255; for 32 x 32 phases, the nearest sample (nearest
+// filtering).  Ties in the distance order keep generation order.
+static void build_phase_lut(uint32_t rx, uint32_t ry, uint32_t *lut)
+{
+	std::fill(lut, lut + PHASE_LUT_WORDS, 0u);
+	if (!rx && !ry)
+		return;
+	constexpr int G = 64;
+	const int n = 1 << (rx + ry);
+	struct Pt { int x, y; };
+	auto points = [&](Pt *out, bool nearest) {
+		for (int i = 0; i < n; i++)
+		{
+			int x, y;
+			if (int(ry) - int(rx) == 2)
+			{
+				static const int sparse[4] = { 0, 2, 3, 1 };
+				x = (i / 8) * 4 + sparse[i % 4];
+				y = i % 8;
+			}
+			else
+			{
+				y = (i & 1) + ((i >> 2) & 1) * 2;
+				x = ((i >> 1) & 1) + ((i >> 3) & 1) * 2;
+				if (int(ry) - int(rx) == 1)
+					x = x * 2 + i % 2;
+			}
+			const int scale = G >> ry;
+			x *= scale;
+			y *= scale;
+			if (nearest)
+			{
+				x += (scale - 1) >> 1;
+				y += (scale - 1) >> 1;
+			}
+			out[i] = { x, y };
+		}
+	};
+	struct Cand { int sample, ox, oy, dx, dy, maxd; };
+	auto candidates = [&](int x, int y, const Pt *pts, int support, std::vector<Cand> &out) {
+		out.clear();
+		for (int i = 0; i < n; i++)
+			for (int ty = -support; ty <= support; ty++)
+				for (int tx = -support; tx <= support; tx++)
+				{
+					const int dx = std::abs(pts[i].x + G * tx - x), dy = std::abs(pts[i].y + G * ty - y);
+					out.push_back({ i, tx, ty, dx, dy, std::max(dx, dy) });
+				}
+		std::stable_sort(out.begin(), out.end(), [](const Cand &a, const Cand &b) {
+			return a.maxd == b.maxd ? a.dy < b.dy : a.maxd < b.maxd;
+		});
+	};
+	Pt pts[16], pts_nearest[16];
+	points(pts, false);
+	points(pts_nearest, true);
+	std::vector<Cand> c;
+	int falloff = INT32_MAX;
+	for (int y = 0; y < G; y++)
+		for (int x = 0; x < G; x++)
+		{
+			candidates(x, y, pts, 1, c);
+			falloff = std::min(falloff, c[4].maxd);
+		}
+	for (int y = 0; y < G; y++)
+		for (int x = 0; x < G; x++)
+		{
+			candidates(x, y, pts, 1, c);
+			if (c[0].ox != 0 || c[0].oy != 0)
+			{
+				for (size_t i = 1; i < c.size(); i++)
+				{
+					if (c[i].ox == 0 && c[i].oy == 0)
+					{
+						if (i < 4)
+							std::swap(c[0], c[i]);
+						else
+						{
+							std::swap(c[3], c[i]);
+							std::swap(c[0], c[3]);
+						}
+						break;
+					}
+				}
+			}
+			uint32_t ex = 0, ey = 0;
+			float w[4], sum = 0.0f;
+			for (int i = 0; i < 4; i++)
+			{
+				ex |= uint32_t(c[i].sample) << (4 * i);
+				ex |= (uint32_t(c[i].ox) & 3u) << (4 * i + 16);
+				ex |= (uint32_t(c[i].oy) & 3u) << (4 * i + 18);
+				const float fx = float(c[i].dx) / float(falloff), fy = float(c[i].dy) / float(falloff);
+				w[i] = std::max(0.0f, 1.0f - fx) * std::max(0.0f, 1.0f - fy);
+				sum += w[i];
+			}
+			if (sum < 0.001f)
+			{
+				for (float &v : w)
+					v = 1.0f;
+				sum = 4.0f;
+			}
+			uint32_t total = 0;
+			for (int i = 0; i < 3; i++)
+			{
+				const float scaled = w[i] * 255.0f / sum;
+				uint32_t q = uint32_t(scaled + 0.5f);
+				q = std::min<uint32_t>(q, 255u - total);
+				total += q;
+				ey |= q << (8 * i);
+			}
+			ey |= (255u - total) << 24;
+			lut[(y * G + x) * 2] = ex;
+			lut[(y * G + x) * 2 + 1] = ey;
+		}
+	for (int y = 0; y < G / 2; y++)
+		for (int x = 0; x < G / 2; x++)
+		{
+			candidates(2 * x, 2 * y, pts_nearest, 0, c);
+			lut[G * G * 2 + y * (G / 2) + x] = uint32_t(c[0].sample);
+		}
+}
+
 struct CudaBackend
 {
 	int device = 0;
@@ -102,6 +229,7 @@ struct CudaBackend
 	uint16_t *d_clut = nullptr;
 	float *d_rcp_float = nullptr;
 	float *d_unorm_lut = nullptr;
+	uint32_t *d_phase_lut = nullptr; // PHASE_LUT_WORDS, for the current sampling rate
 	uint32_t *d_error = nullptr;
 	unsigned long long *d_frags = nullptr;
 	uint8_t *d_snapshot = nullptr;
@@ -207,6 +335,8 @@ struct CudaBackend
 			lut[i] = float(i) / denom;
 		CUDA_TRY(cudaMalloc(&d_unorm_lut, sizeof(lut)));
 		CUDA_TRY(cudaMemcpy(d_unorm_lut, lut, sizeof(lut), cudaMemcpyHostToDevice));
+		CUDA_TRY(cudaMalloc(&d_phase_lut, PHASE_LUT_WORDS * sizeof(uint32_t)));
+		CUDA_TRY(cudaMemset(d_phase_lut, 0, PHASE_LUT_WORDS * sizeof(uint32_t)));
 		CUDA_TRY(cudaMemcpyToSymbol(c_rcp_tab, RCP_TABLE, sizeof(RCP_TABLE)));
 
 		const size_t n = PGS_MAX_PRIMITIVES_PER_FLUSH;
@@ -257,6 +387,7 @@ struct CudaBackend
 		cudaFree(d_texels);
 		cudaFree(d_circuit);
 		cudaFree(d_zcache);
+		cudaFree(d_phase_lut);
 		for (DevImage *im : { &vs_circuit[0], &vs_circuit[1], &vs_merged, &vs_out, &vs_fields[0], &vs_fields[1],
 		                      &vs_fields[2], &vs_fields[3] })
 			cudaFree(im->ptr);
@@ -389,7 +520,7 @@ struct CudaBackend
 		size_t prim_bytes = size_t(n) * sizeof(pgs_primitive_attribute);
 		size_t st_bytes = size_t(std::max<uint32_t>(rp->num_states, 1)) * sizeof(pgs_state_vector);
 		size_t tex_bytes = size_t(std::max<uint32_t>(rp->num_textures, 1)) * sizeof(pgs_texture_desc);
-		size_t img_bytes = size_t(std::max<uint32_t>(rp->num_textures, 1)) * TEX_LEVELS * sizeof(TexImage);
+		size_t img_bytes = size_t(std::max<uint32_t>(rp->num_textures, 1)) * TEX_SLOTS * sizeof(TexImage);
 		size_t base;
 		size_t total = align_up(pos_bytes, 256) + align_up(attr_bytes, 256) + align_up(prim_bytes, 256) +
 		               align_up(st_bytes, 256) + align_up(tex_bytes, 256) + align_up(img_bytes, 256);
@@ -439,9 +570,15 @@ struct CudaBackend
 				uint32_t levels = std::max<uint32_t>(t.levels, 1);
 				if (levels > TEX_LEVELS || std::min(std::min(t.tw_log2, t.th_log2), 10u) + 1 < levels)
 					return PGS_ERROR_INVALID_ARGUMENT;
-				max_levels = std::max(max_levels, levels);
-				for (uint32_t l = 0; l < levels; l++)
+				// Super-sampled textures: one level, a layer per sample the VRAM holds.
+				if (t.samples > 1 && (levels != 1 || (t.samples & (t.samples - 1)) || t.samples > 16 ||
+				                      2u + t.samples > num_planes))
+					return PGS_ERROR_INVALID_ARGUMENT;
+				const uint32_t slots = texture_slots(t);
+				max_levels = std::max(max_levels, slots);
+				for (uint32_t s = 0; s < slots; s++)
 				{
+					const uint32_t l = t.samples > 1 ? 0u : s;
 					auto extent = [l](uint32_t size_log2, uint32_t mode, uint32_t lo, uint32_t hi) {
 						uint32_t size = 1u << (std::min<uint32_t>(size_log2, 10) - l);
 						lo >>= l;
@@ -452,7 +589,7 @@ struct CudaBackend
 							return std::max(size, (((size - 1u) & lo) | hi) + 1u);
 						return size;
 					};
-					TexImage &m = im[i * TEX_LEVELS + l];
+					TexImage &m = im[i * TEX_SLOTS + s];
 					m.ext_u = extent(t.tw_log2, t.wms, t.minu, t.maxu);
 					m.ext_v = extent(t.th_log2, t.wmt, t.minv, t.maxv);
 					m.offset = uint32_t(texels);
@@ -477,6 +614,8 @@ struct CudaBackend
 		p.tile_size_log2 = rp->coarse_tile_size_log2;
 		p.has_aa1 = rp->has_aa1;
 		p.has_mipmap = rp->has_mipmap;
+		p.has_ss_textures = rp->has_ss_textures;
+		p.rp_is_blur_mask = blur_mask(rp);
 		p.has_scanmsk = rp->has_scanmsk;
 		p.num_instances = rp->num_instances;
 		memcpy(p.instances, rp->instances, sizeof(p.instances));
@@ -552,7 +691,52 @@ struct CudaBackend
 		num_planes = planes;
 		if (max_planes > 1)
 			CUDA_TRY(cudaMemsetAsync(d_vram + VRAM_SIZE, 0, size_t(max_planes - 1) * VRAM_SIZE, stream));
+		build_phase_lut(x, y, h_phase_lut);
+		CUDA_TRY(cudaMemcpyAsync(d_phase_lut, h_phase_lut, sizeof(h_phase_lut), cudaMemcpyHostToDevice, stream));
+		CUDA_TRY(cudaStreamSynchronize(stream));
 		return PGS_OK;
+	}
+	uint32_t h_phase_lut[PHASE_LUT_WORDS] = {};
+
+	// A render pass instance that samples one per-sample texture at more than
+	// one texel phase is taken for a blur kernel
+	// (render_pass_instance_is_deduced_blur, gs/gs_renderer.cpp:1850-1884).
+	static uint32_t blur_mask(const pgs_render_pass *rp)
+	{
+		if (rp->num_primitives > 64)
+			return 0;
+		uint32_t mask = 0;
+		for (uint32_t inst = 0; inst < rp->num_instances; inst++)
+		{
+			uint32_t last = 0xffffffffu;
+			int32_t phase[2] = { 0, 0 };
+			for (uint32_t i = 0; i < rp->num_primitives; i++)
+			{
+				const pgs_primitive_attribute &pa = rp->prims[i];
+				if (((pa.state >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u) != inst || !(pa.tex & TEX_PER_SAMPLE_BIT))
+					continue;
+				if (pa.state & (1u << STATE_BIT_PERSPECTIVE))
+					break;
+				const uint32_t ti = pa.tex & TEX_TEXTURE_INDEX_MASK;
+				const int32_t ph[2] = { int32_t(rp->attributes[3 * i].u) - rp->positions[3 * i].x,
+				                        int32_t(rp->attributes[3 * i].v) - rp->positions[3 * i].y };
+				if (last == ti)
+				{
+					if (ph[0] != phase[0] || ph[1] != phase[1])
+					{
+						mask |= 1u << inst;
+						break;
+					}
+				}
+				else
+				{
+					phase[0] = ph[0];
+					phase[1] = ph[1];
+				}
+				last = ti;
+			}
+		}
+		return mask;
 	}
 
 	// ------------------------------------------------------------------
@@ -673,7 +857,8 @@ struct CudaBackend
 		bin_kernel<<<(count + 127) / 128, 128, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags);
 		launch_counter++;
 		uint32_t grid = uint32_t(subs);
-		if (collect && !p.has_mipmap && ns_log2 <= BATCH_MAX_NS_LOG2 && (I.rate_y_log2 != 0 || ns_log2 == 0))
+		if (collect && !p.has_mipmap && !p.has_ss_textures && ns_log2 <= BATCH_MAX_NS_LOG2 &&
+		    (I.rate_y_log2 != 0 || ns_log2 == 0))
 		{
 			collect->P = P;
 			collect->I = I;
@@ -694,8 +879,9 @@ struct CudaBackend
 				return r;
 			shade_started = true;
 		}
-		// Mipmapped passes take the AA-capable variant too (three variants per rate).
-		if (p.has_mipmap)
+		// Passes with mip levels or super-sampled textures take the AA-capable
+		// variant too (three variants per rate).
+		if (p.has_mipmap || p.has_ss_textures)
 			launch_shade<true, true>(P, I, ns_log2, grid, d_sub_masks, d_sub_summary);
 		else if (p.has_aa1)
 			launch_shade<true, false>(P, I, ns_log2, grid, d_sub_masks, d_sub_summary);
@@ -901,6 +1087,8 @@ struct CudaBackend
 		P.textures = reinterpret_cast<const pgs_texture_desc *>(d_arena + p.textures_off);
 		P.tex_images = reinterpret_cast<const TexImage *>(d_arena + p.images_off);
 		P.max_tex_levels = p.max_levels;
+		P.rp_is_blur_mask = p.rp_is_blur_mask;
+		P.phase_lut = d_phase_lut;
 		if (p.num_texels > texels_cap)
 		{
 			cudaFree(d_texels);
@@ -952,7 +1140,7 @@ struct CudaBackend
 		}
 		if (p.num_textures && p.num_texels)
 		{
-			dim3 grid((p.max_texels + 255) / 256, p.num_textures * p.max_levels);
+			dim3 grid((p.max_texels + 255) / 256, p.num_textures, p.max_levels);
 			texture_decode_kernel<<<grid, 256, 0, stream>>>(P);
 			launch_counter++;
 		}

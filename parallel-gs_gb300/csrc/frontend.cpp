@@ -174,6 +174,10 @@ struct PageTracker
 	enum : uint8_t { FB_WRITE = 1, FB_READ = 2, TEX_READ = 4 };
 	static constexpr uint32_t WORDS = NUM_PAGES / 64;
 	uint64_t bits[3][WORDS] = {};
+	// Pages a pass wrote as frame or depth buffer since a transfer or host
+	// write last replaced them (PAGE_STATE_MAY_SUPER_SAMPLE_BIT,
+	// gs/page_tracker.cpp:155-190,255-265,650-715); kept across passes.
+	uint64_t may_ss[WORDS] = {};
 	// Bumped when a page gains a kind it did not have / when the tracker is cleared.
 	uint64_t gen[3] = {};
 	uint64_t gen_at_clear[3] = {};
@@ -274,6 +278,9 @@ struct PageTracker
 			PageSpan s{ base + y0 * stride + x0, w, h, stride };
 			bool hit = any_kind(s, 2);
 			mark_kind(s, mk);
+			if (mk == 0)
+				for (uint32_t y = 0; y < s.height; y++)
+					range_set(may_ss, (s.base_page + y * s.stride) % NUM_PAGES, s.width);
 			return hit;
 		}
 		const uint64_t m = low_mask(w);
@@ -295,6 +302,13 @@ struct PageTracker
 			bm[j0] |= b0;
 			bm[i1] |= a1;
 			bm[j1] |= b1;
+			if (mk == 0)
+			{
+				may_ss[i0] |= a0;
+				may_ss[j0] |= b0;
+				may_ss[i1] |= a1;
+				may_ss[j1] |= b1;
+			}
 			if (missing)
 				gen[mk]++;
 			return hit != 0;
@@ -309,6 +323,11 @@ struct PageTracker
 			missing |= (~bits[mk][wi] & m0) | (~bits[mk][wj] & m1);
 			bits[mk][wi] |= m0;
 			bits[mk][wj] |= m1;
+			if (mk == 0)
+			{
+				may_ss[wi] |= m0;
+				may_ss[wj] |= m1;
+			}
 		}
 		if (missing)
 			gen[mk]++;
@@ -341,6 +360,26 @@ struct PageTracker
 				gen[k]++;
 		}
 	}
+
+	// A transfer or host write replaced these pages.
+	void clear_may_super_sample(const PageSpan &s)
+	{
+		for (uint32_t y = 0; y < s.height; y++)
+		{
+			uint32_t start = (s.base_page + y * s.stride) % NUM_PAGES, len = s.width;
+			while (len)
+			{
+				uint32_t o = start & 63, n = std::min<uint32_t>(len, 64 - o);
+				may_ss[start >> 6] &= ~((n == 64 ? ~0ull : ((1ull << n) - 1)) << o);
+				len -= n;
+				start = (start + n) % NUM_PAGES;
+			}
+		}
+	}
+
+	// Only the base page counts: W/H round up to powers of two
+	// (texture_may_super_sample, gs/page_tracker.cpp:147-153).
+	bool may_super_sample(uint32_t page) const { return (may_ss[(page % NUM_PAGES) >> 6] >> (page & 63)) & 1; }
 
 	void clear()
 	{
@@ -417,7 +456,8 @@ struct pgs_gs
 	Instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
 	uint32_t num_instances = 1;
 	uint32_t current_instance = 0;
-	bool has_aa1 = false, has_scanmsk = false, has_mipmap = false;
+	bool has_aa1 = false, has_scanmsk = false, has_mipmap = false, has_ss_textures = false;
+	bool ssaa_textures = false; // super_sampled_textures of set_super_sampling_rate
 	uint32_t clut_instance = 0;
 	uint32_t pending_palette_updates = 0;
 	int32_t ofx = 0, ofy = 0;
@@ -583,6 +623,7 @@ struct pgs_gs
 			rp.has_aa1 = has_aa1;
 			rp.has_scanmsk = has_scanmsk;
 			rp.has_mipmap = has_mipmap;
+			rp.has_ss_textures = has_ss_textures;
 
 			uint64_t binning_cost = 0;
 			for (uint32_t i = 0; i < num_instances; i++)
@@ -652,7 +693,9 @@ struct pgs_gs
 				}
 				pass.channel_shuffle = channel_shuffle;
 
-				if (sampling_rate_y_log2 != 0)
+				// With super-sampled textures in the pass the demotions do not
+				// apply (gs/gs_interface.cpp:225-260).
+				if (sampling_rate_y_log2 != 0 && !(ssaa_textures && has_ss_textures))
 				{
 					if (channel_shuffle || (inst.z_write && zbuf.zbp == frame.fbp))
 					{
@@ -687,6 +730,7 @@ struct pgs_gs
 		has_aa1 = false;
 		has_scanmsk = false;
 		has_mipmap = false;
+		has_ss_textures = false;
 		template_dirty = true;
 		tracker.clear();
 		reserve_buffers();
@@ -724,6 +768,7 @@ struct pgs_gs
 			if (tracker.any(dst, PageTracker::FB_WRITE | PageTracker::FB_READ | PageTracker::TEX_READ) ||
 			    tracker.any(src, PageTracker::FB_WRITE))
 				flush_render_pass(FLUSH_COPY_HAZARD);
+			tracker.clear_may_super_sample(dst);
 			pgs_copy_desc d = {};
 			d.bitbltbuf = xfer.bitbltbuf;
 			d.trxpos = xfer.trxpos;
@@ -797,6 +842,7 @@ struct pgs_gs
 			PageSpan dst = page_span(dbp, dsax, dsay, rrw, rrh, dbw, dpsm);
 			if (tracker.any(dst, PageTracker::FB_WRITE | PageTracker::FB_READ | PageTracker::TEX_READ))
 				flush_render_pass(FLUSH_COPY_HAZARD);
+			tracker.clear_may_super_sample(dst);
 
 			pgs_copy_desc d = {};
 			d.bitbltbuf = xfer.bitbltbuf;
@@ -1328,6 +1374,12 @@ struct pgs_gs
 		}
 		num_spans = d.levels;
 
+		// Super-sampled texture: a sprite reading, at 8+ bits per texel, pages
+		// that a pass wrote (gs/gs_interface.cpp:1593-1601).
+		if (d.levels == 1 && ssaa_textures && sampling_rate_y_log2 != 0 && psm_bits_per_pixel(t.psm) >= 8 &&
+		    PrimReg(regs[R_PRIM]).prim == PRIM_SPRITE && tracker.may_super_sample(spans[0].base_page))
+			d.samples = 1u << (sampling_rate_x_log2 + sampling_rate_y_log2);
+
 		TextureKey key{ d };
 		auto it = texture_map.find(key);
 		if (it != texture_map.end())
@@ -1356,6 +1408,15 @@ struct pgs_gs
 			uint32_t index = update_texture(tpl_tex_spans, tpl_num_tex_spans);
 			tpl_has_tex_span = true;
 			tex = index;
+			if (textures[index].samples > 1)
+			{
+				// Per-sample layers; palette textures under region repeat map
+				// sample to sample (gs/gs_interface.cpp:1786-1791,1822-1831).
+				tex |= TEX_PER_SAMPLE_BIT;
+				if (psm_is_palette(textures[index].psm) && (clamp.wms == WRAP_REGION_REPEAT || clamp.wmt == WRAP_REGION_REPEAT))
+					tex |= TEX_SAMPLE_MAPPING_BIT;
+				has_ss_textures = true;
+			}
 			tex |= tex1.mmag ? TEX_SAMPLER_MAG_LINEAR_BIT : 0;
 			tex |= (clamp.wms == WRAP_CLAMP || clamp.wms == WRAP_REGION_CLAMP) ? TEX_SAMPLER_CLAMP_S_BIT : 0;
 			tex |= (clamp.wmt == WRAP_CLAMP || clamp.wmt == WRAP_REGION_CLAMP) ? TEX_SAMPLER_CLAMP_T_BIT : 0;
@@ -2408,6 +2469,13 @@ int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *sr
 	if (!gs || !src || offset + size > PGS_VRAM_SIZE)
 		return PGS_ERROR_INVALID_ARGUMENT;
 	gs->flush();
+	if (size)
+	{
+		// A host write replaces these pages (commit_host_write, gs/page_tracker.cpp:700-715).
+		uint32_t first = uint32_t(offset / PAGE_BYTES), last = uint32_t((offset + size - 1) / PAGE_BYTES);
+		PageSpan s{ first, last - first + 1, 1, 0 };
+		gs->tracker.clear_may_super_sample(s);
+	}
 	return gs->ops->write_vram(gs->be, offset, size, src);
 }
 
@@ -2441,6 +2509,17 @@ int pgs_gs_set_super_sampling_rate(pgs_gs *gs, uint32_t super_sampling, uint32_t
 		return PGS_ERROR_INVALID_ARGUMENT;
 	gs->flush();
 	gs->set_super_sampling(super_sampling, ordered_grid != 0);
+	return gs->sticky_error;
+}
+
+int pgs_gs_set_super_sampled_textures(pgs_gs *gs, int enable)
+{
+	if (!gs)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->flush();
+	gs->ssaa_textures = enable != 0;
+	gs->reg_serial++;
+	gs->template_dirty = true;
 	return gs->sticky_error;
 }
 }

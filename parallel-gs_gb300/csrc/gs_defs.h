@@ -62,6 +62,7 @@ constexpr uint32_t TEX_SAMPLER_CLAMP_T_BIT = 1u << 20;
 constexpr int TEX_MAX_MIP_LEVEL_OFFSET = 21;
 constexpr uint32_t TEX_PER_SAMPLE_BIT = 1u << 24;
 constexpr uint32_t TEX_SAMPLE_MAPPING_BIT = 1u << 25;
+constexpr uint32_t TEX_SAMPLE_RESOLVED_BIT = 1u << 26;
 
 // PrimitiveAttribute::tex2 bits.
 constexpr uint32_t TEX2_FIXED_LOD_BIT = 1u << 0;

@@ -66,8 +66,36 @@ struct DevInstance
 
 // Linear RGBA8 image decoded from swizzled VRAM + CLUT for one mip level of
 // one texture of a pass (the role of the reference's texture cache,
-// upload.comp:108-229); level l of texture t is entry t * TEX_LEVELS + l.
+// upload.comp:108-229); slot l of texture t is entry t * TEX_SLOTS + l: mip
+// level l, or for a super-sampled texture layer l (0: single-sampled image,
+// s + 1: sample s).
 constexpr uint32_t TEX_LEVELS = 7;
+constexpr uint32_t TEX_SLOTS = 17;
+// Phase LUT of super-sampled texture filtering: 64 x 64 (x, y) pairs for
+// bilinear, then 32 x 32 sample ids for nearest.
+constexpr uint32_t PHASE_LUT_WORDS = 64 * 64 * 2 + 32 * 32;
+
+// Mean position of the samples inside a pixel per sampling grid
+// (get_average_sampling_offset, utils.h:108-126).
+__host__ __device__ inline float average_sampling_offset(uint32_t rx, uint32_t ry)
+{
+	if (rx == ry)
+		return ry == 0 ? 0.0f : (ry == 1 ? 0.25f : (ry == 2 ? 0.375f : 0.4375f));
+	if (rx == 0 && ry == 1)
+		return 0.25f;
+	if (rx == 1 && ry == 2)
+		return 0.375f;
+	if (rx == 0 && ry == 2)
+		return 0.375f;
+	if (rx == 1 && ry == 3)
+		return 0.4375f;
+	return 0.0f;
+}
+
+__host__ __device__ inline uint32_t texture_slots(const pgs_texture_desc &t)
+{
+	return t.samples > 1 ? t.samples + 1 : (t.levels > 1 ? t.levels : 1u);
+}
 
 struct TexImage
 {
@@ -114,7 +142,9 @@ struct PassParams
 	TransformedAttr *tattr;
 	uint32_t num_prims;
 	uint32_t num_states, num_textures;
-	uint32_t max_tex_levels;      // largest mip level count of the pass's textures
+	uint32_t max_tex_levels;      // largest slot count (mip levels or sample layers) of the pass's textures
+	uint32_t rp_is_blur_mask;     // per instance: the pass looks like a blur kernel (render_pass_instance_is_deduced_blur)
+	const uint32_t *phase_lut;    // PHASE_LUT_WORDS words
 	uint32_t tile_size_log2;
 	uint32_t has_aa1, has_scanmsk, has_ss_reference;
 	uint32_t setup_rate_x_log2, setup_rate_y_log2;
@@ -537,6 +567,55 @@ __global__ void __launch_bounds__(128) setup_kernel(PassParams P)
 	uint32_t new_state = st;
 	if (pa.fbmsk != opaque_fbmask && (new_state & (1u << STATE_BIT_OPAQUE)))
 		new_state &= ~(1u << STATE_BIT_OPAQUE);
+
+	// Super-sampled textures (triangle_setup.comp:677-825, with
+	// FORCE_LINEAR_SUPER_SAMPLE off): nearest blits map sample to sample,
+	// nearest downsamples and blur kernels fall back to the single-sampled
+	// layer, linear upsamples read the resolved layer; what stays per-sample
+	// interpolates per sample around the single-sampled mean position.
+	if (sry != 0 && (tex & (TEX_PER_SAMPLE_BIT | TEX_SAMPLE_MAPPING_BIT)) == TEX_PER_SAMPLE_BIT)
+	{
+		const int32_t udx = abs(int32_t(at1.u) - int32_t(at0.u)), udy = abs(int32_t(at1.v) - int32_t(at0.v));
+		const int32_t ddx = abs(dx - ax), ddy = abs(dy - ay);
+		if ((tex & TEX_SAMPLER_MAG_LINEAR_BIT) == 0)
+		{
+			if (perspective)
+				tex |= TEX_SAMPLE_MAPPING_BIT;
+			else if (udx > ddx + 1 || udy > ddy + 1)
+				tex &= ~TEX_PER_SAMPLE_BIT;
+			else if (udx >= ddx - 16 || udy >= ddy - 16)
+			{
+				const uint32_t blend = P.states[min(st & STATE_INDEX_MASK, P.num_states - 1u)].blend_mode;
+				const uint32_t inst = (st >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u;
+				const bool blur = ((P.rp_is_blur_mask >> inst) & 1u) && (blend & BLEND_MODE_ABE_BIT) &&
+				                  !(st & (1u << STATE_BIT_Z_TEST)) &&
+				                  ((blend >> BLEND_MODE_A_MODE_OFFSET) & 3u) == BLEND_RGB_SOURCE &&
+				                  ((blend >> BLEND_MODE_B_MODE_OFFSET) & 3u) == BLEND_RGB_ZERO &&
+				                  ((blend >> BLEND_MODE_D_MODE_OFFSET) & 3u) == BLEND_RGB_DEST;
+				if (blur)
+					tex &= ~TEX_PER_SAMPLE_BIT;
+				else
+					tex |= TEX_SAMPLE_MAPPING_BIT;
+			}
+		}
+		else if (!perspective)
+		{
+			if (udx > ddx + 1 && udy > ddy + 1)
+				tex &= ~TEX_PER_SAMPLE_BIT;
+			else if (ddx >= 2 * udx && ddy >= 2 * udy)
+				tex |= TEX_SAMPLE_RESOLVED_BIT;
+		}
+		if ((tex & (TEX_PER_SAMPLE_BIT | TEX_SAMPLE_MAPPING_BIT)) == TEX_PER_SAMPLE_BIT)
+		{
+			new_state &= ~(1u << STATE_BIT_SNAP_ATTRIBUTE);
+			const float corner = fmul(8.0f, average_sampling_offset(P.setup_rate_x_log2, P.setup_rate_y_log2));
+			const float di_dcorner = fmul(__int2float_rn(pb0 + pb1), corner);
+			const float dj_dcorner = fmul(__int2float_rn(pc0 + pc1), corner);
+			out.error_i = fsub(out.error_i, fmul(di_dcorner, inv_area_scaled));
+			out.error_j = fsub(out.error_j, fmul(dj_dcorner, inv_area_scaled));
+		}
+	}
+
 	if (sry != 0 && !sprite)
 	{
 		bool per_sample = multisample;
@@ -918,6 +997,7 @@ struct ShadeCtx
 	int32_t snap_mask;
 	bool zs;
 	uint32_t fb_psm, zb_psm;
+	uint32_t sample; // sample index of the thread in a super-sampled tile, else 0
 };
 
 __device__ __forceinline__ uint32_t clut_color(const PassParams &P, const pgs_texture_desc &t, uint32_t index)
@@ -956,6 +1036,58 @@ __device__ __forceinline__ uint32_t fetch_texel(const PassParams &P, const pgs_t
 	}
 }
 
+// Texel of sample `s` of a super-sampled texture: the single-sampled texel
+// unless the reference plane marks it super-sampled (upload.comp
+// SUPER_SAMPLED, :131-220; 24-bit formats merge by the reference bits).
+__device__ __forceinline__ uint32_t fetch_texel_sample(const PassParams &P, const pgs_texture_desc &t, int32_t x, int32_t y,
+                                                       uint32_t s)
+{
+	const uint32_t a = swizzle_address(uint32_t(x), uint32_t(y), t.tbp0, t.tbw, t.psm);
+	const uint8_t *v = P.vram;
+	const uint32_t *v32 = reinterpret_cast<const uint32_t *>(v);
+	const uint16_t *v16 = reinterpret_cast<const uint16_t *>(v);
+	const uint32_t V32 = VRAM_SIZE / 4, V16 = VRAM_SIZE / 2, V8 = VRAM_SIZE;
+	switch (t.psm)
+	{
+	case PSMCT24: case PSMZ24:
+	{
+		uint32_t col = __ldg(v32 + a), ref = __ldg(v32 + a + V32);
+		if (ref != 0u)
+			col = (__ldg(v32 + a + (2u + s) * V32) & ref) | (col & ~ref);
+		return rgb24_to_rgba32(col, t.aem, t.ta0);
+	}
+	case PSMCT16: case PSMCT16S: case PSMZ16: case PSMZ16S:
+	{
+		uint32_t col = __ldg(v16 + a);
+		if (__ldg(v16 + a + V16) == 0xffffu)
+			col = __ldg(v16 + a + (2u + s) * V16);
+		return rgba16_to_rgba32(col, t.aem, t.ta0, t.ta1);
+	}
+	case PSMT8:
+	{
+		uint32_t idx = __ldg(v + a);
+		if (__ldg(v + a + V8) == 0xffu)
+			idx = __ldg(v + a + (2u + s) * V8);
+		return clut_color(P, t, idx);
+	}
+	case PSMT8H:
+	{
+		const uint32_t a8 = 4u * a + 3u;
+		uint32_t idx = __ldg(v + a8);
+		if (__ldg(v + a8 + V8) == 0xffu)
+			idx = __ldg(v + a8 + (2u + s) * V8);
+		return clut_color(P, t, idx);
+	}
+	default:
+	{
+		uint32_t col = __ldg(v32 + a);
+		if (__ldg(v32 + a + V32) == 0xffffffffu)
+			col = __ldg(v32 + a + (2u + s) * V32);
+		return col;
+	}
+	}
+}
+
 __device__ __forceinline__ int32_t wrap_coord(int32_t v, uint32_t mode, uint32_t size_log2, uint32_t lo, uint32_t hi)
 {
 	int32_t size = 1 << size_log2;
@@ -968,27 +1100,34 @@ __device__ __forceinline__ int32_t wrap_coord(int32_t v, uint32_t mode, uint32_t
 	}
 }
 
-// One block row per (texture, mip level); level l reads from MIPTBP's base
-// and stride (upload_texture's per-level loop, gs/gs_renderer.cpp:3543-3590).
+// Grid y = texture, z = slot (mip level, or sample layer of a super-sampled
+// texture); level l reads from MIPTBP's base and stride (upload_texture's
+// per-level loop, gs/gs_renderer.cpp:3543-3590).
 __global__ void __launch_bounds__(256) texture_decode_kernel(PassParams P)
 {
-	const uint32_t tex = blockIdx.y / P.max_tex_levels, level = blockIdx.y % P.max_tex_levels;
+	const uint32_t tex = blockIdx.y, level = blockIdx.z;
 	if (tex >= P.num_textures)
 		return;
 	const pgs_texture_desc t = P.textures[tex];
-	if (level >= max(t.levels, 1u))
+	if (level >= texture_slots(t))
 		return;
-	const TexImage im = P.tex_images[tex * TEX_LEVELS + level];
+	const TexImage im = P.tex_images[tex * TEX_SLOTS + level];
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= im.ext_u * im.ext_v)
 		return;
+	const int32_t x = int32_t(i % im.ext_u), y = int32_t(i / im.ext_u);
+	if (t.samples > 1 && level > 0)
+	{
+		P.texels[im.offset + i] = fetch_texel_sample(P, t, x, y, level - 1u);
+		return;
+	}
 	uint32_t tbp = t.tbp0, tbw = t.tbw;
 	if (level)
 	{
 		tbp = t.mip[level - 1] & 0x3fffu;
 		tbw = t.mip[level - 1] >> 16;
 	}
-	P.texels[im.offset + i] = fetch_texel(P, t, tbp, tbw, int32_t(i % im.ext_u), int32_t(i / im.ext_u));
+	P.texels[im.offset + i] = fetch_texel(P, t, tbp, tbw, x, y);
 }
 
 // log2 of a positive normal float: ln m = 2 atanh(s), s = (m - 1) / (m + 1),
@@ -1020,7 +1159,8 @@ __device__ __forceinline__ float lod_log2(float x)
 // 1214-1227, with region bounds and masks shifted down by the level as in
 // texture_clamp, :947-953, and upload_texture, gs/gs_renderer.cpp:3578-3590).
 __device__ void sample_level(const PassParams &P, uint32_t tex_index, const pgs_texture_desc &t, uint32_t level,
-                             bool clamp_s, bool clamp_t, bool linear, float u, float v, bool perspective, uint32_t rgba[4])
+                             uint32_t slot, bool clamp_s, bool clamp_t, bool linear, float u, float v, bool perspective,
+                             uint32_t rgba[4])
 {
 	const uint32_t twl = t.tw_log2 - level, thl = t.th_log2 - level;
 	float uu, vv;
@@ -1050,7 +1190,7 @@ __device__ void sample_level(const PassParams &P, uint32_t tex_index, const pgs_
 	}
 	int32_t ku = int32_t(floorf(fadd(fmul(uu, 16.0f), 1.0f / 64.0f)));
 	int32_t kv = int32_t(floorf(fadd(fmul(vv, 16.0f), 1.0f / 64.0f)));
-	const TexImage im = P.tex_images[tex_index * TEX_LEVELS + level];
+	const TexImage im = P.tex_images[tex_index * TEX_SLOTS + slot];
 	const uint32_t *img = P.texels + im.offset;
 	if (!linear)
 	{
@@ -1129,13 +1269,112 @@ __device__ __forceinline__ uint32_t select_lod(uint32_t levels, uint32_t tex_wor
 }
 
 // MIP: the pass samples mip levels (some primitive has TEX1.MXL > 0 with a
-// mipmapping MMIN); without it every sample reads level 0 through MMAG.
+// mipmapping MMIN) or super-sampled textures; without it every sample reads
+// level 0 of a plain texture through MMAG.
+// Super-sampled texture (ubershader.comp:1155-1212).  Sample mapping reads the
+// layer of the shading sample, the resolved bit layer 0; otherwise the phase
+// LUT picks up to four (layer, texel) taps around the texel below the
+// sampling position, weighted in unorm8 (one tap when filtering is nearest or
+// the texel is on a clamped region edge).  Taps wrap like the texture.
+__device__ void sample_layered(const PassParams &P, uint32_t tex_index, const pgs_texture_desc &t, uint32_t tex_word,
+                               float u, float v, bool perspective, uint32_t sample, uint32_t rx, uint32_t ry,
+                               uint32_t rgba[4])
+{
+	const bool clamp_s = (tex_word & TEX_SAMPLER_CLAMP_S_BIT) != 0;
+	const bool clamp_t = (tex_word & TEX_SAMPLER_CLAMP_T_BIT) != 0;
+	const bool mag_linear = (tex_word & TEX_SAMPLER_MAG_LINEAR_BIT) != 0;
+	if (tex_word & (TEX_SAMPLE_MAPPING_BIT | TEX_SAMPLE_RESOLVED_BIT))
+	{
+		const uint32_t layer = (tex_word & TEX_SAMPLE_MAPPING_BIT) ? min(sample + 1u, t.samples) : 0u;
+		sample_level(P, tex_index, t, 0, layer, clamp_s, clamp_t, mag_linear, u, v, perspective, rgba);
+		return;
+	}
+	const float w = float(1u << t.tw_log2), h = float(1u << t.th_log2);
+	float uu = perspective ? fmul(u, w) : u;
+	float vv = perspective ? fmul(v, h) : v;
+	// Region of the reference's TexInfo (CLAMP: the image, REGION_CLAMP: MIN/MAX, else 0).
+	const int32_t rx0 = t.wms == WRAP_REGION_CLAMP ? int32_t(t.minu) : 0;
+	const int32_t rx1 = t.wms == WRAP_REGION_CLAMP ? int32_t(t.maxu) : (t.wms == WRAP_CLAMP ? int32_t(w) - 1 : 0);
+	const int32_t ry0 = t.wmt == WRAP_REGION_CLAMP ? int32_t(t.minv) : 0;
+	const int32_t ry1 = t.wmt == WRAP_REGION_CLAMP ? int32_t(t.maxv) : (t.wmt == WRAP_CLAMP ? int32_t(h) - 1 : 0);
+	if (clamp_s)
+		uu = fminf(fmaxf(uu, fadd(float(rx0), 0.5f)), fadd(float(rx1), 0.5f));
+	if (clamp_t)
+		vv = fminf(fmaxf(vv, fadd(float(ry0), 0.5f)), fadd(float(ry1), 0.5f));
+	const float shift = fsub(0.5f, average_sampling_offset(rx, ry));
+	const float su = fsub(fadd(uu, 1.0f / 1024.0f), shift), sv = fsub(fadd(vv, 1.0f / 1024.0f), shift);
+	const float fu = floorf(su), fv = floorf(sv);
+	const int32_t ix = int32_t(fu), iy = int32_t(fv);
+	const float pu = fsub(su, fu), pv = fsub(sv, fv);
+	uint32_t entry, weights = 0;
+	if (mag_linear)
+	{
+		const uint32_t lx = min(uint32_t(fmul(pu, 64.0f)), 63u), ly = min(uint32_t(fmul(pv, 64.0f)), 63u);
+		entry = __ldg(P.phase_lut + (ly * 64u + lx) * 2u);
+		weights = __ldg(P.phase_lut + (ly * 64u + lx) * 2u + 1u);
+	}
+	else
+	{
+		const uint32_t lx = min(uint32_t(fmul(pu, 32.0f)), 31u), ly = min(uint32_t(fmul(pv, 32.0f)), 31u);
+		entry = __ldg(P.phase_lut + 64u * 64u * 2u + ly * 32u + lx);
+	}
+	const bool force_nearest =
+	    !mag_linear || ((clamp_s || clamp_t) && (ix == rx0 || iy == ry0 || ix == rx1 || iy == ry1));
+	auto tap = [&](uint32_t layer, int32_t x, int32_t y) {
+		layer = min(layer + 1u, t.samples);
+		const TexImage im = P.tex_images[tex_index * TEX_SLOTS + layer];
+		const int32_t wx = wrap_coord(x, t.wms, t.tw_log2, t.minu, t.maxu);
+		const int32_t wy = wrap_coord(y, t.wmt, t.th_log2, t.minv, t.maxv);
+		return __ldg(P.texels + im.offset + uint32_t(wy) * im.ext_u + uint32_t(wx));
+	};
+	const uint32_t c0 = tap(entry & 15u, ix, iy);
+	if (force_nearest)
+	{
+		#pragma unroll
+		for (int k = 0; k < 4; k++)
+			rgba[k] = (c0 >> (8 * k)) & 0xffu;
+		return;
+	}
+	uint32_t acc[4];
+	const uint32_t w0 = weights & 0xffu;
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+		acc[k] = w0 * ((c0 >> (8 * k)) & 0xffu);
+	for (uint32_t i = 1; i < 4; i++)
+	{
+		const uint32_t wi = (weights >> (8 * i)) & 0xffu;
+		if (!wi)
+			continue;
+		const int32_t ox = int32_t(entry << (14 - 4 * i)) >> 30, oy = int32_t(entry << (12 - 4 * i)) >> 30;
+		const uint32_t c = tap((entry >> (4 * i)) & 15u, ix + ox, iy + oy);
+		#pragma unroll
+		for (int k = 0; k < 4; k++)
+			acc[k] += wi * ((c >> (8 * k)) & 0xffu);
+	}
+	// round(acc / 255); a tie would need acc = 255 (2q + 1) / 2.
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		const uint32_t q = acc[k] / 255u, r = acc[k] % 255u;
+		rgba[k] = q + (2u * r > 255u ? 1u : 0u);
+	}
+}
+
 template <bool MIP>
 __device__ void sample_texture(const PassParams &P, uint32_t tex_word, uint32_t tex2, float u, float v, float q,
-                               bool perspective, float out[4])
+                               bool perspective, uint32_t sample, uint32_t rx, uint32_t ry, float out[4])
 {
 	const uint32_t tex_index = min(tex_word & TEX_TEXTURE_INDEX_MASK, P.num_textures - 1u);
 	const pgs_texture_desc t = P.textures[tex_index];
+	if (MIP && (tex_word & TEX_PER_SAMPLE_BIT) && t.samples > 1)
+	{
+		uint32_t rgba[4];
+		sample_layered(P, tex_index, t, tex_word, u, v, perspective, sample, rx, ry, rgba);
+		#pragma unroll
+		for (int k = 0; k < 4; k++)
+			out[k] = float(rgba[k]);
+		return;
+	}
 	const bool clamp_s = (tex_word & TEX_SAMPLER_CLAMP_S_BIT) != 0;
 	const bool clamp_t = (tex_word & TEX_SAMPLER_CLAMP_T_BIT) != 0;
 	uint32_t sel = (tex_word & TEX_SAMPLER_MAG_LINEAR_BIT) ? (1u << 16) : 0u;
@@ -1148,8 +1387,8 @@ __device__ void sample_texture(const PassParams &P, uint32_t tex_word, uint32_t 
 	for (uint32_t pass = 0; pass < (weight ? 2u : 1u); pass++)
 	{
 		uint32_t c[4];
-		sample_level(P, tex_index, t, pass ? ((sel >> 4) & 15u) : (sel & 15u), clamp_s, clamp_t, (sel >> 16) != 0,
-		             u, v, perspective, c);
+		const uint32_t lv = pass ? ((sel >> 4) & 15u) : (sel & 15u);
+		sample_level(P, tex_index, t, lv, lv, clamp_s, clamp_t, (sel >> 16) != 0, u, v, perspective, c);
 		const uint32_t w = pass ? weight : 16u - weight;
 		#pragma unroll
 		for (int k = 0; k < 4; k++)
@@ -1201,7 +1440,8 @@ __device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r,
 		s = fminf(fmaxf(s, -2047.0f), 2047.0f);
 		t = fminf(fmaxf(t, -2047.0f), 2047.0f);
 		float tx[4];
-		sample_texture<MIP>(P, P.prims[pi].tex, P.prims[pi].tex2, s, t, q, perspective, tx);
+		sample_texture<MIP>(P, P.prims[pi].tex, P.prims[pi].tex2, s, t, q, perspective, C.sample,
+		                    C.ss ? C.I->rate_x_log2 : 0u, C.ss ? C.I->rate_y_log2 : 0u, tx);
 		if (mode == COMBINER_DECAL)
 		{
 			cc[0] = tx[0]; cc[1] = tx[1]; cc[2] = tx[2]; cc[3] = tcc ? tx[3] : col[3];
@@ -1679,6 +1919,7 @@ __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInst
 	const int32_t sub_x = I.base_x + int32_t(gx * 8u), sub_y = I.base_y + int32_t(gy * 8u);
 	const uint32_t lane = t & 31u;
 	const uint32_t sample = t % NS;
+	C.sample = SS ? sample : 0u;
 	const uint32_t pix = t / NS;
 	// Pixel order inside the sub-tile: x from bits 0,2,4 and y from bits 1,3,5,
 	// so that each warp covers a compact block.

@@ -1005,6 +1005,83 @@ def frame_alias(seed: int, width: int = 256, height: int = 128) -> Frame:
         sprites(int(rng.integers(5, 30)), 4, 96, z_test=True, z_write=False, abe=int(rng.integers(0, 2)))
     return Frame("alias_%d" % seed, s.tobytes(), ss, True, 0, {"width": width, "height": height, "fbp": 0, "zbp": 0})
 
+
+def frame_ssaa_textures(seed: int) -> Frame:
+    """Super-sampled textures: a super-sampled 3D pass into an off-screen
+    buffer, then sprites that sample it (its pages were written by a pass):
+    nearest and bilinear, 1:1 blits, downsamples, upsamples and in-between
+    scales, perspective and UV addressing, CT32 / CT16 / PSMT8 views with region
+    clamp and repeat, blur-like groups of a few sprites at different phases
+    (ABE Cs * As + Cd), and enough sprites in some passes that the blur
+    heuristic stays off.  Needs set_super_sampled_textures."""
+    rng = np.random.Generator(np.random.PCG64(90000 + seed))
+    s = GifStream()
+    ss = [2, 4, 8, 16][seed % 4]
+    ordered = bool(rng.uniform() < 0.7)
+    ow, oh = 256, 128                       # off-screen buffer at page 0
+    width, height = 320, 224                # final frame at page 100
+    zbp, fin = 60, 100
+    _frame_setup(s, 0, ow // 64, PSMCT32, zbp, PSMZ24, ow, oh, test_reg(zte=1, ztst=2))
+    n = 300
+    x, y = random_triangles(rng, n, ow, oh, 4.0, 1500.0)
+    z = rng.integers(0, 1 << 24, size=(n, 3))
+    rgba = rng.integers(0, 256, size=(3 * n, 4))
+    q = np.zeros((3 * n, 2, 2), dtype=np.uint64)
+    q[:, 0] = q_rgbaq(rgba)
+    q[:, 1] = q_xyz2(x.reshape(-1), y.reshape(-1), z.reshape(-1))
+    s.packed(prim_reg(PRIM_TRI, iip=1), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+    # Final frame; each group samples the off-screen buffer.
+    s.ad([(FRAME_1, frame_reg(fin, width // 64, PSMCT32)), (SCISSOR_1, scissor_reg(0, width - 1, 0, height - 1)),
+          (TEST_1, test_reg(zte=1, ztst=1)), (ZBUF_1, zbuf_reg(zbp, PSMZ24, 1))])
+    clut_cbp = 200 * BLOCKS_PER_PAGE
+    clut = rng.integers(0, 256, size=16 * 16 * 4, dtype=np.uint8).tobytes()
+    s.upload(clut_cbp, 1, PSMCT32, 0, 0, 16, 16, clut)
+    few = seed % 2 == 0  # at most 64 sprites: the blur heuristic is live
+    for g in range(int(rng.integers(3, 6)) if few else int(rng.integers(6, 12))):
+        view = [PSMCT32, PSMCT32, PSMCT16, PSMT8][int(rng.integers(0, 4))]
+        mmag = int(rng.integers(0, 2))
+        fst = int(rng.uniform() < 0.7)
+        blur = rng.uniform() < (0.6 if few else 0.3)
+        nspr = int(rng.integers(2, 6)) if blur else int(rng.integers(2, 6) if few else rng.integers(3, 40))
+        wm = [int(rng.integers(0, 4)), int(rng.integers(0, 4))]
+        regs = [(TEX0_1, tex0_reg(0, ow // 64, view, 8, 7, tcc=1, tfx=1, cbp=clut_cbp, cpsm=PSMCT32,
+                                  cld=1 if view == PSMT8 else 0)),
+                (TEX1_1, tex1_reg(mmag=mmag, mmin=mmag)),
+                (CLAMP_1, clamp_reg(wm[0], wm[1], int(rng.integers(0, 64)), int(rng.integers(64, 255)),
+                                    int(rng.integers(0, 32)), int(rng.integers(32, 127)))),
+                (ALPHA_1, alpha_reg(0, 2, 0, 1) if blur else alpha_reg(0, 1, 0, 1))]
+        s.ad(regs)
+        scale = [1.0, 1.0, 0.5, 2.0, 0.75, 1.5, 3.0][int(rng.integers(0, 7))]
+        pts, uvs, stq = [], [], []
+        for k in range(nspr):
+            w = int(rng.integers(8, 96))
+            h = int(rng.integers(8, 64))
+            x0 = int(rng.integers(0, width - w))
+            y0 = int(rng.integers(0, height - h))
+            u0 = int(rng.integers(0, ow - 8)) * 16 + (int(rng.integers(0, 16)) if not blur else k * 4)
+            v0 = int(rng.integers(0, oh - 8)) * 16 + (int(rng.integers(0, 16)) if not blur else k * 2)
+            pts += [(x0 * 16, y0 * 16), ((x0 + w) * 16, (y0 + h) * 16)]
+            uvs += [(u0, v0), (u0 + int(w * scale * 16), v0 + int(h * scale * 16))]
+        nv = len(pts)
+        xs = np.array([p_[0] for p_ in pts], dtype=np.int64)
+        ys = np.array([p_[1] for p_ in pts], dtype=np.int64)
+        col = rng.integers(0, 256, size=(nv, 4))
+        col[:, 3] = 0x80
+        q = np.zeros((nv, 3, 2), dtype=np.uint64)
+        q[:, 0] = q_rgbaq(col)
+        if fst:
+            q[:, 1] = q_uv(np.array([u for u, _ in uvs]) & 0x3FFF, np.array([v for _, v in uvs]) & 0x3FFF)
+            desc = [D_RGBAQ, D_UV, D_XYZ2]
+        else:
+            qq = np.full(nv, float(rng.uniform(0.5, 2.0)), dtype=np.float32)
+            q[:, 1] = q_st(np.array([u / 16.0 / ow for u, _ in uvs], dtype=np.float32) * qq,
+                           np.array([v / 16.0 / 128.0 for _, v in uvs], dtype=np.float32) * qq, qq)
+            desc = [D_RGBAQ, D_ST, D_XYZ2]
+        q[:, 2] = q_xyz2(xs, ys, np.zeros(nv, dtype=np.int64))
+        s.packed(prim_reg(PRIM_SPRITE, tme=1, fst=fst, abe=1), desc, q.reshape(-1, 2))
+    return Frame("ssaa_tex_%d" % seed, s.tobytes(), ss, ordered, n,
+                 {"width": width, "height": height, "fbp": fin, "zbp": zbp, "ssaa_textures": True})
+
 def write_dump(path, transfers, vram: bytes | None = None, regs: dict | None = None, version: int = 9,
                serial: bytes = b"", vsync_fields=(0,)) -> None:
     """Writes a GS dump in the PCSX2 / GSdx layout (GSDumpGenerator::init,

@@ -92,6 +92,7 @@ EXPORTED_SYMBOLS = [
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
     "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait",
     "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit", "pgs_gs_vsync",
+    "pgs_gs_set_super_sampled_textures",
     "pgs_gs_dump_open", "pgs_gs_dump_next_vsync", "pgs_gs_dump_close", "pgs_gs_dump_record_begin",
     "pgs_gs_dump_record_vsync", "pgs_gs_dump_record_end", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
     "pgs_gs_set_super_sampling_rate",
@@ -162,6 +163,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.pgs_gs_read_transfer_fifo.argtypes = [vp, vp, u32]
     lib.pgs_gs_consume_flush_stats.argtypes = [vp, C.POINTER(FlushStats)]
     lib.pgs_gs_set_super_sampling_rate.argtypes = [vp, u32, u32]
+    lib.pgs_gs_set_super_sampled_textures.argtypes = [vp, i32]
     if path is None:
         _lib = lib
     return lib
@@ -393,6 +395,9 @@ class GSInterface:
         return {"render_passes": st.num_render_passes, "primitives": st.num_primitives, "copies": st.num_copies,
                 "palette_updates": st.num_palette_updates,
                 "flush_reasons": list(st.num_flushes_by_reason)}
+
+    def set_super_sampled_textures(self, enable: bool) -> None:
+        check(self.lib.pgs_gs_set_super_sampled_textures(self.handle, int(enable)), "set_super_sampled_textures")
 
     def set_super_sampling_rate(self, super_sampling: int, ordered: bool = True) -> None:
         check(self.lib.pgs_gs_set_super_sampling_rate(self.handle, super_sampling, int(ordered)),

@@ -34,7 +34,7 @@ class TextureDesc(C.Structure):
     _fields_ = [(n, C.c_uint32) for n in ("tbp0", "tbw", "psm", "tw_log2", "th_log2", "cpsm", "csa", "clut_instance",
                                           "aem", "ta0", "ta1", "wms", "wmt", "minu", "maxu", "minv", "maxv",
                                           "levels")] + \
-               [("mip", C.c_uint32 * 6)]
+               [("mip", C.c_uint32 * 6), ("samples", C.c_uint32), ("padding", C.c_uint32)]
 
 
 class RPInstance(C.Structure):
@@ -52,7 +52,7 @@ class RenderPass(C.Structure):
                 ("textures", C.POINTER(TextureDesc)), ("num_textures", C.c_uint32),
                 ("instances", RPInstance * 8), ("num_instances", C.c_uint32),
                 ("coarse_tile_size_log2", C.c_uint32), ("has_aa1", C.c_uint32), ("has_scanmsk", C.c_uint32),
-                ("flush_reason", C.c_uint32), ("has_mipmap", C.c_uint32)]
+                ("flush_reason", C.c_uint32), ("has_mipmap", C.c_uint32), ("has_ss_textures", C.c_uint32)]
 
 
 class CopyDesc(C.Structure):
@@ -120,12 +120,12 @@ class RecordingBackend(pgs.Backend):
             "attributes": _struct_array(rp.attributes, 3 * n, ("s", "t", "q", "rgba", "fog", "u", "v")),
             "prims": _struct_array(rp.prims, n, ("bb", "state", "tex", "tex2", "alpha", "fbmsk", "fogcol")),
             "states": _struct_array(rp.states, rp.num_states, ("combiner", "blend_mode", "dimx_lo", "dimx_hi")),
-            "textures": _struct_array(rp.textures, rp.num_textures, [f[0] for f in TextureDesc._fields_]),
+            "textures": _struct_array(rp.textures, rp.num_textures, [f[0] for f in TextureDesc._fields_[:-1]]),
             "instances": [{f[0]: getattr(rp.instances[i], f[0]) for f in RPInstance._fields_}
                           for i in range(rp.num_instances)],
             "coarse_tile_size_log2": rp.coarse_tile_size_log2,
             "has_aa1": rp.has_aa1, "has_scanmsk": rp.has_scanmsk, "flush_reason": rp.flush_reason,
-            "has_mipmap": rp.has_mipmap,
+            "has_mipmap": rp.has_mipmap, "has_ss_textures": rp.has_ss_textures,
         }
         self.passes.append(rec)
         return 0

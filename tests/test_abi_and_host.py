@@ -45,7 +45,7 @@ def test_record_layouts_match_reference_sizes(tmp_path):
     exe = tmp_path / "sizes"
     subprocess.check_call(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)])
     sizes = [int(v) for v in subprocess.check_output([str(exe)]).split()]
-    assert sizes == [16, 24, 32, 16, 96]
+    assert sizes == [16, 24, 32, 16, 104]
 
 
 def test_cuda_backend_fails_loudly_without_gpu():

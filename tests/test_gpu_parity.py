@@ -257,3 +257,13 @@ def test_extreme_sizes(kind, ss):
     f = gsgen.Frame(f.name, f.data, ss, True, f.num_primitives, f.meta)
     ref, out = run_both(f)
     assert_same(ref, out)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_super_sampled_textures_parity(seed):
+    """Sprites sampling pages a super-sampled pass wrote, with super-sampled
+    textures on: sample mapping, resolved and single-sampled layers, phase-LUT
+    filtering, blur detection, at 2x / 4x / 8x / 16x."""
+    f = gsgen.frame_ssaa_textures(seed)
+    ref, out = run_both(f)
+    assert_same(ref, out)
