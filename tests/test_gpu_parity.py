@@ -267,3 +267,15 @@ def test_super_sampled_textures_parity(seed):
     f = gsgen.frame_ssaa_textures(seed)
     ref, out = run_both(f)
     assert_same(ref, out)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_combined_feature_streams(seed):
+    """One stream that runs a mipmapped frame, a super-sampled-texture frame, an
+    aliased frame/depth frame and a feature-fuzz frame back to back at one
+    sampling rate (state, textures and pages carried from one to the next)."""
+    parts = [gsgen.frame_ssaa_textures(seed), gsgen.frame_mip(seed), gsgen.frame_alias(seed), gsgen.frame_fuzz(seed)]
+    f = gsgen.Frame("combined_%d" % seed, b"".join(p.data for p in parts), parts[0].super_sampling, parts[0].ordered,
+                    sum(p.num_primitives for p in parts), dict(parts[0].meta))
+    ref, out = run_both(f)
+    assert_same(ref, out)
