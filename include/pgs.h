@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define PGS_ABI_VERSION 3u
+#define PGS_ABI_VERSION 4u
 
 /* ------------------------------------------------------------------ */
 /* Status codes                                                        */
@@ -171,6 +171,15 @@ typedef struct pgs_render_pass
 	uint32_t has_mipmap;
 	/* Some texture of the pass is super-sampled (pgs_texture_desc.samples). */
 	uint32_t has_ss_textures;
+	/* Field-aware rendering (GSRenderer::set_field_aware_super_sampling,
+	 * gs/gs_renderer.cpp:355-358): instances that end at or above row 256
+	 * shade every covered tile super-sampled with rows snapped at half the
+	 * sample pitch, and blur kernels keep per-sample textures.  ABI >= 4. */
+	uint32_t field_aware;
+	/* Hacks::allow_blend_demote (gs/gs_interface.hpp:231-236): when every
+	 * state blends, coarse tiles with 32 or more primitives and no depth
+	 * write shade single-sampled.  ABI >= 4. */
+	uint32_t blend_demote;
 } pgs_render_pass;
 
 /* A VRAM transfer (CopyDescriptor, gs/gs_renderer.hpp).  For HOST_TO_LOCAL,
@@ -579,6 +588,10 @@ typedef struct pgs_scanout_result
 } pgs_scanout_result;
 
 int pgs_gs_vsync(pgs_gs *gs, const pgs_vsync_info *info, void *dst, uint64_t dst_size, pgs_scanout_result *result);
+/* GSInterface::vsync_can_skip (gs/gs_interface.cpp:4692-4695): 1 when the
+ * read-out is progressive (no field alternation) and no SCANMSK primitive
+ * taller than 400 rows was drawn within the last 4 vsyncs, else 0. */
+int pgs_gs_vsync_can_skip(const pgs_gs *gs, const pgs_vsync_info *info);
 /* GSInterface::map_vram_write + end_vram_write. */
 int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *src);
 /* GSInterface::read_transfer_fifo. */
@@ -591,6 +604,21 @@ int pgs_gs_set_super_sampling_rate(pgs_gs *gs, uint32_t super_sampling, uint32_t
  * (gs/gs_interface.hpp:258): sprites sampling pages a super-sampled pass wrote
  * read per-sample texture layers.  Ignored at 1x. */
 int pgs_gs_set_super_sampled_textures(pgs_gs *gs, int enable);
+
+/* Hacks (gs/gs_interface.hpp:209-237, GSInterface::set_hacks): inaccurate
+ * options, all off by default.  disable_mipmaps samples level 0 only;
+ * allow_blend_demote sets pgs_render_pass.blend_demote; unsynced_readbacks is
+ * accepted and has no effect (FIFO readbacks here always wait for the
+ * rendering they read); backbuffer_promotion is not supported and returns
+ * PGS_ERROR_UNSUPPORTED. */
+typedef struct pgs_hacks
+{
+	uint32_t disable_mipmaps;
+	uint32_t unsynced_readbacks;
+	uint32_t backbuffer_promotion;
+	uint32_t allow_blend_demote;
+} pgs_hacks;
+int pgs_gs_set_hacks(pgs_gs *gs, const pgs_hacks *hacks);
 
 #ifdef __cplusplus
 }

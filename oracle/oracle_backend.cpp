@@ -268,7 +268,7 @@ struct Backend
 	void triangle_setup(uint32_t index, const pgs_vertex_position *vp, const pgs_vertex_attribute *va,
 	                    pgs_primitive_attribute &pa, Setup &out, TAttr &ta, const uint32_t *opaque_fbmasks,
 	                    int srx, int sry, uint32_t packed_z_shift, int32_t &bucket_out,
-	                    const pgs_render_pass *rp = nullptr, uint32_t blur_mask = 0)
+	                    const pgs_render_pass *rp = nullptr, uint32_t blur_mask = 0, bool force_linear = false)
 	{
 		bucket_out = -1;
 		int order[3] = { 0, 1, 2 };
@@ -622,12 +622,14 @@ struct Backend
 		if (pa.fbmsk != opaque_fbmask && (s & (1u << 14)) != 0)
 			pa.state = s & ~(1u << 14);
 
-		// Super-sampled textures (triangle_setup.comp:677-825; FORCE_LINEAR_SUPER_SAMPLE
-		// off): per sprite, sample-to-sample mapping for nearest blits and
-		// perspective, the single-sampled layer for nearest downsamples and
-		// blur kernels, the resolved layer for linear upsamples; per-sample
-		// interpolation (no attribute snap, i/j moved to the mean sample
-		// position) for what stays per-sample.
+		// Super-sampled textures (triangle_setup.comp:677-825): per sprite,
+		// sample-to-sample mapping for nearest blits and perspective, the
+		// single-sampled layer for nearest downsamples and blur kernels, the
+		// resolved layer for linear upsamples (force_linear, for field
+		// rendering: blur kernels read the resolved layer linearly, linear
+		// downsamples and upsamples stay per sample); per-sample interpolation
+		// (no attribute snap, i/j moved to the mean sample position) for what
+		// stays per-sample.
 		const uint32_t PER_SAMPLE = 1u << 24, MAPPING = 1u << 25, RESOLVED = 1u << 26;
 		if (sry != 0 && rp && (pa.tex & (PER_SAMPLE | MAPPING)) == PER_SAMPLE)
 		{
@@ -646,7 +648,21 @@ struct Backend
 					const uint32_t inst = bfe(pa.state, 29, 3);
 					const bool blur = ((blur_mask >> inst) & 1u) && (bm & (1u << 9)) && !(pa.state & (1u << 12)) &&
 					                  bfe(bm, 11, 2) == 0 && bfe(bm, 13, 2) == 2 && bfe(bm, 17, 2) == 1;
-					if (blur)
+					if (blur && force_linear)
+					{
+						// Field rendering keeps blur kernels per sample: the
+						// resolved layer, filtered linearly, with the mean
+						// sample position moved to the texel centre
+						// (triangle_setup.comp:729-746).
+						tex |= RESOLVED | (1u << 16);
+						const int32_t avg_u = (int32_t(at0.u) + int32_t(at1.u)) >> 1;
+						const int32_t avg_v = (int32_t(at0.v) + int32_t(at1.v)) >> 1;
+						const int32_t avg_x = (d[0] + a[0]) >> 1, avg_y = (d[1] + a[1]) >> 1;
+						const int32_t ph_x = (avg_u - avg_x) & 15, ph_y = (avg_v - avg_y) & 15;
+						ta.stqf0[0] = ta.stqf0[0] + (0.5f - float(ph_x) / 16.0f);
+						ta.stqf0[1] = ta.stqf0[1] + (0.5f - float(ph_y) / 16.0f);
+					}
+					else if (blur)
 						tex &= ~PER_SAMPLE;
 					else
 						tex |= MAPPING;
@@ -655,9 +671,15 @@ struct Backend
 			else if (!perspective)
 			{
 				if (udx > ddx + 1 && udy > ddy + 1)
-					tex &= ~PER_SAMPLE;
+				{
+					if (!force_linear)
+						tex &= ~PER_SAMPLE;
+				}
 				else if (ddx >= 2 * udx && ddy >= 2 * udy)
-					tex |= RESOLVED;
+				{
+					if (!force_linear)
+						tex |= RESOLVED;
+				}
 			}
 			pa.tex = tex;
 			if ((tex & (PER_SAMPLE | MAPPING)) == PER_SAMPLE)
@@ -748,9 +770,10 @@ struct Backend
 		bool has_ss_reference;   // VRAM holds sample planes
 		uint32_t fb_psm, zb_psm; // effective formats; zb_psm = ~0u when not Z sensitive
 		uint32_t fb_base, fb_stride, zb_base;
-		int32_t snap_mask;
+		int32_t snap_mask_x, snap_mask_y; // raster snap; y halves when field rendering
 		bool preserve_samples;
 		bool has_aa1, has_scanmsk;
+		bool tex_array;          // some texture of the pass is super-sampled
 		const uint8_t *zcache;   // depth read from this VRAM snapshot when set
 	};
 
@@ -876,8 +899,10 @@ struct Backend
 		int32_t rx = smp.hx, ry = smp.hy;
 		if (P.ss && (st & (1u << 25)))
 		{
-			rx &= P.snap_mask;
-			ry &= P.snap_mask;
+			// Sample-mapped textures keep the full-rate row grid when the
+			// rows are snapped for field rendering (ubershader.comp:816-821).
+			rx &= P.snap_mask_x;
+			ry &= (P.tex_array && (P.prims[pi].tex & (1u << 25))) ? P.snap_mask_x : P.snap_mask_y;
 		}
 		float i = 0, j = 0;
 		r.coverage = evaluate_coverage(s, rx, ry, i, j, r.multisample, bfe(st, 22, 1), dim);
@@ -910,7 +935,11 @@ struct Backend
 		{
 			uint32_t snap = st & ((1u << 25) | (1u << 26));
 			if (snap == (1u << 26))
-				barycentric(s, smp.hx & P.snap_mask, smp.hy & P.snap_mask, dim, i, j);
+				barycentric(s, smp.hx & P.snap_mask_x, smp.hy & P.snap_mask_y, dim, i, j);
+			else if (P.tex_array && snap == (1u << 25))
+				// Per-sample textured sprite: coverage snapped, attributes
+				// interpolated per sample (ubershader.comp:888-895).
+				barycentric(s, smp.hx, smp.hy, dim, i, j);
 		}
 		r.z = z;
 		r.i = i;
@@ -2041,6 +2070,27 @@ struct Backend
 			run_cached(next, end - next);
 	}
 
+	// render_pass_instance_might_field_render (gs/gs_renderer.cpp:1888-1895):
+	// an instance that ends above row 256 may be a field; taller ones are
+	// taken as full frames that are downsampled later.
+	static bool might_field_render(const pgs_render_pass &rp, uint32_t instance)
+	{
+		const pgs_rp_instance &inst = rp.instances[instance];
+		return !(inst.base_y + int32_t(inst.coarse_tiles_height << rp.coarse_tile_size_log2) > 256);
+	}
+
+	// Blend demotion budget (gs/gs_renderer.cpp:2082-2091): 32 primitives
+	// per coarse tile when the hack is on and every state of the pass blends.
+	static uint32_t blend_demote_budget(const pgs_render_pass &rp)
+	{
+		if (!rp.blend_demote)
+			return 0;
+		for (uint32_t i = 0; i < rp.num_states; i++)
+			if ((rp.states[i].blend_mode & (1u << 9)) == 0)
+				return 0;
+		return 32;
+	}
+
 	void render_instance(PassCtx &P, uint32_t inst_index, uint32_t base, uint32_t count)
 	{
 		const pgs_rp_instance &inst = P.rp->instances[inst_index];
@@ -2053,6 +2103,9 @@ struct Backend
 		P.zb_base = bfe(uint32_t(inst.zbuf), 0, 9) * 32;
 		P.zb_psm = inst.z_sensitive ? effective_z_psm(fb_psm, zpsm_raw) : ~0u;
 		bool ss_inst = inst.sampling_rate_y_log2 != 0;
+		const bool field_render = P.rp->field_aware && might_field_render(*P.rp, inst_index);
+		const bool force_ss = field_render;
+		const uint32_t blend_demote = blend_demote_budget(*P.rp);
 
 		const int32_t ntiles = int32_t(inst.coarse_tiles_width * inst.coarse_tiles_height);
 		const PassCtx shared = P;
@@ -2065,7 +2118,9 @@ struct Backend
 				int32_t lo0 = inst.base_x + int32_t(tx << ts), lo1 = inst.base_y + int32_t(ty << ts);
 				int32_t hi0 = lo0 + (1 << ts) - 1, hi1 = lo1 + (1 << ts) - 1;
 				std::vector<uint32_t> list;
-				bool req = false, req_zw = false, has_zw = false;
+				// Field rendering forces every covered tile super-sampled
+				// (binning.comp:195, force_super_sample).
+				bool req = force_ss, req_zw = false, has_zw = false;
 				for (uint32_t p = base; p < base + count; p++)
 				{
 					if (bfe(P.prims[p].state, 29, 3) != inst_index)
@@ -2080,6 +2135,10 @@ struct Backend
 				}
 				if (list.empty())
 					continue;
+				// Blend demotion: a tile crowded with blended primitives and no
+				// depth writes shades single-sampled (binning.comp:277-282).
+				if (blend_demote != 0 && list.size() >= blend_demote && !has_zw)
+					req = false;
 				req = req || (req_zw && has_zw);
 				P.ss = ss_inst && req;
 				if (P.ss)
@@ -2094,7 +2153,8 @@ struct Backend
 					P.sr_x_log2 = 0;
 					P.num_samples = 1;
 				}
-				P.snap_mask = -(1 << inst.sampling_rate_y_log2);
+				P.snap_mask_x = -(1 << inst.sampling_rate_y_log2);
+				P.snap_mask_y = (inst.sampling_rate_y_log2 && field_render) ? (P.snap_mask_x >> 1) : P.snap_mask_x;
 				P.preserve_samples = inst.channel_shuffle && inst.sampling_rate_y_log2 != 0;
 				for (int32_t y = lo1; y <= hi1; y++)
 					for (int32_t x = lo0; x <= hi0; x++)
@@ -2292,6 +2352,7 @@ struct Backend
 		P.has_ss_reference = num_planes > 1;
 		P.has_aa1 = rp->has_aa1;
 		P.has_scanmsk = rp->has_scanmsk;
+		P.tex_array = rp->has_ss_textures != 0;
 
 		uint32_t fbmasks[8] = {};
 		int srx = 0, sry = 0;
@@ -2335,13 +2396,19 @@ struct Backend
 					last = ti;
 				}
 			}
+		// FORCE_LINEAR_SUPER_SAMPLE (gs/gs_renderer.cpp:1953-1969): field
+		// rendering with super-sampled textures bound.
+		bool force_linear = false;
+		if (rp->has_ss_textures && rp->field_aware)
+			for (uint32_t inst = 0; inst < rp->num_instances; inst++)
+				force_linear = force_linear || might_field_render(*rp, inst);
 		HeuristicPush push[8] = {};
 		uint32_t packed_z_shift = heuristic_pushes(rp, push);
 		std::vector<int32_t> bucket(rp->num_primitives);
 		#pragma omp parallel for schedule(static)
 		for (uint32_t i = 0; i < rp->num_primitives; i++)
 			triangle_setup(i, rp->positions, rp->attributes, prims[i], setup[i], tattr[i], fbmasks, srx, sry,
-			               packed_z_shift, bucket[i], rp, blur);
+			               packed_z_shift, bucket[i], rp, blur, force_linear);
 		if (sry != 0)
 			single_sample_heuristic(rp, prims, bucket, push);
 		for (uint32_t i = 0; i < rp->num_primitives; i++)

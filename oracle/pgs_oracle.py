@@ -98,6 +98,14 @@ def render(frame, backend: pgs.Backend | None = None, planes: bool = False):
     gs = pgs.GSInterface(be, super_sampling=frame.super_sampling, ordered=frame.ordered)
     if frame.meta.get("ssaa_textures"):
         gs.set_super_sampled_textures(True)
+    if frame.meta.get("hacks"):
+        gs.set_hacks(**frame.meta["hacks"])
+    if frame.meta.get("field_aware"):
+        # Field-rendered interlaced NTSC (SMODE1 CMOD 2, SMODE2 INT | FFMD) read
+        # out at high resolution: the vsync turns field-aware rendering on.
+        gs.write_priv_register("SMODE1", (32 << 3) | (2 << 13))
+        gs.write_priv_register("SMODE2", 3)
+        gs.vsync(0, gs.VSYNC["FORCE_PROGRESSIVE"] | gs.VSYNC["HIGH_RESOLUTION"])
     gs.gif_transfer(0, frame.data)
     vram = gs.read_vram()
     out = vram

@@ -69,6 +69,8 @@ struct PassOp
 	uint32_t num_prims, num_states, num_textures;
 	uint32_t tile_size_log2, has_aa1, has_scanmsk, has_mipmap, has_ss_textures;
 	uint32_t rp_is_blur_mask;
+	uint32_t field_aware;   // pgs_render_pass.field_aware
+	uint32_t blend_demote;  // primitives per coarse tile that demote a blended tile, 0 = off
 	uint32_t num_instances;
 	pgs_rp_instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
 	// Host copy of the primitive records while the pass is submitted
@@ -616,6 +618,8 @@ struct CudaBackend
 		p.has_mipmap = rp->has_mipmap;
 		p.has_ss_textures = rp->has_ss_textures;
 		p.rp_is_blur_mask = blur_mask(rp);
+		p.field_aware = rp->field_aware;
+		p.blend_demote = blend_demote_budget(rp);
 		p.has_scanmsk = rp->has_scanmsk;
 		p.num_instances = rp->num_instances;
 		memcpy(p.instances, rp->instances, sizeof(p.instances));
@@ -701,6 +705,27 @@ struct CudaBackend
 	// A render pass instance that samples one per-sample texture at more than
 	// one texel phase is taken for a blur kernel
 	// (render_pass_instance_is_deduced_blur, gs/gs_renderer.cpp:1850-1884).
+	// Blend demotion (gs/gs_renderer.cpp:2082-2091): 32 primitives per
+	// coarse tile when the hack is on and every state of the pass blends.
+	static uint32_t blend_demote_budget(const pgs_render_pass *rp)
+	{
+		if (!rp->blend_demote)
+			return 0;
+		for (uint32_t i = 0; i < rp->num_states; i++)
+			if ((rp->states[i].blend_mode & BLEND_MODE_ABE_BIT) == 0)
+				return 0;
+		return 32;
+	}
+
+	// render_pass_instance_might_field_render (gs/gs_renderer.cpp:1888-1895):
+	// an instance that ends above row 256 may be a field; taller ones are
+	// taken as full frames that are downsampled later.
+	static bool might_field_render(const PassOp &p, uint32_t instance)
+	{
+		const pgs_rp_instance &in = p.instances[instance];
+		return !(in.base_y + int32_t(in.coarse_tiles_height << p.tile_size_log2) > 256);
+	}
+
 	static uint32_t blur_mask(const pgs_render_pass *rp)
 	{
 		if (rp->num_primitives > 64)
@@ -830,6 +855,12 @@ struct CudaBackend
 		I.rate_x_log2 = in.sampling_rate_x_log2;
 		I.rate_y_log2 = in.sampling_rate_y_log2;
 		I.preserve_samples = in.channel_shuffle && in.sampling_rate_y_log2 != 0;
+		const bool field_render = p.field_aware && might_field_render(p, inst_index);
+		I.snap_mask_y = -(1 << I.rate_y_log2);
+		if (I.rate_y_log2 && field_render)
+			I.snap_mask_y >>= 1;
+		I.force_ss = field_render;
+		I.blend_demote = p.blend_demote;
 		I.instance = inst_index;
 		I.prim_lo = lo;
 		I.prim_count = count;
@@ -1088,6 +1119,10 @@ struct CudaBackend
 		P.tex_images = reinterpret_cast<const TexImage *>(d_arena + p.images_off);
 		P.max_tex_levels = p.max_levels;
 		P.rp_is_blur_mask = p.rp_is_blur_mask;
+		P.force_linear_ss = 0;
+		if (p.has_ss_textures && p.field_aware)
+			for (uint32_t i = 0; i < p.num_instances; i++)
+				P.force_linear_ss |= might_field_render(p, i) ? 1u : 0u;
 		P.phase_lut = d_phase_lut;
 		if (p.num_texels > texels_cap)
 		{

@@ -458,6 +458,14 @@ struct pgs_gs
 	uint32_t current_instance = 0;
 	bool has_aa1 = false, has_scanmsk = false, has_mipmap = false, has_ss_textures = false;
 	bool ssaa_textures = false; // super_sampled_textures of set_super_sampling_rate
+	// Field-aware rendering, chosen by the last vsync (gs/gs_interface.cpp:4662-4672):
+	// high-resolution read-out of field-rendered interlaced output.
+	bool field_aware = false;
+	// Hacks (gs/gs_interface.hpp:209-237).
+	bool hack_disable_mipmaps = false, hack_unsynced_readbacks = false, hack_blend_demote = false;
+	// Vsyncs left with progressive read-out switched off after a tall
+	// SCANMSK primitive (gs/gs_interface.cpp:1947-1959, 4631-4637).
+	uint32_t complex_scanmsk_timeout = 0;
 	uint32_t clut_instance = 0;
 	uint32_t pending_palette_updates = 0;
 	int32_t ofx = 0, ofy = 0;
@@ -521,7 +529,9 @@ struct pgs_gs
 		if (dc.serial == reg_serial)
 			return dc;
 		PrimReg prim(regs[R_PRIM]);
-		dc.snap = (1 << int(SUBPIXEL_BITS - sampling_rate_y_log2)) - 1;
+		// Field-aware rendering keeps the untightened box
+		// (gs/gs_interface.cpp:2528-2531).
+		dc.snap = field_aware ? 0 : (1 << int(SUBPIXEL_BITS - sampling_rate_y_log2)) - 1;
 		uint64_t sc = ctx_reg(R_SCISSOR_1);
 		dc.frame = FrameReg(ctx_reg(R_FRAME_1));
 		dc.zb = ZbufReg(ctx_reg(R_ZBUF_1));
@@ -624,6 +634,8 @@ struct pgs_gs
 			rp.has_scanmsk = has_scanmsk;
 			rp.has_mipmap = has_mipmap;
 			rp.has_ss_textures = has_ss_textures;
+			rp.field_aware = field_aware;
+			rp.blend_demote = hack_blend_demote;
 
 			uint64_t binning_cost = 0;
 			for (uint32_t i = 0; i < num_instances; i++)
@@ -693,9 +705,9 @@ struct pgs_gs
 				}
 				pass.channel_shuffle = channel_shuffle;
 
-				// With super-sampled textures in the pass the demotions do not
-				// apply (gs/gs_interface.cpp:225-260).
-				if (sampling_rate_y_log2 != 0 && !(ssaa_textures && has_ss_textures))
+				// Field-aware rendering, or super-sampled textures in the
+				// pass, keep the pass super-sampled (gs/gs_interface.cpp:225-260).
+				if (sampling_rate_y_log2 != 0 && !field_aware && !(ssaa_textures && has_ss_textures))
 				{
 					if (channel_shuffle || (inst.z_write && zbuf.zbp == frame.fbp))
 					{
@@ -1362,7 +1374,7 @@ struct pgs_gs
 		// Mip chain: MXL only counts with a mipmapping MMIN
 		// (gs/gs_interface.cpp:1538-1582); levels stop at a 1-texel side.
 		d.levels = 1;
-		if (tex1.mmin_has_mipmap())
+		if (tex1.mmin_has_mipmap() && !hack_disable_mipmaps)
 			d.levels = std::min<uint32_t>(std::min<uint32_t>(tex1.mxl + 1, std::min(d.tw_log2, d.th_log2) + 1), 7);
 		for (uint32_t l = 1; l < d.levels; l++)
 		{
@@ -1391,7 +1403,8 @@ struct pgs_gs
 	}
 
 	// drawing_kick_update_state (gs/gs_interface.cpp:1804-1968).
-	void update_template()
+	// bb: the scissored box of the primitive that made the template stale.
+	void update_template(const int32_t *bb)
 	{
 		tpl_serial++;
 		PrimReg prim(regs[R_PRIM]);
@@ -1420,7 +1433,7 @@ struct pgs_gs
 			tex |= tex1.mmag ? TEX_SAMPLER_MAG_LINEAR_BIT : 0;
 			tex |= (clamp.wms == WRAP_CLAMP || clamp.wms == WRAP_REGION_CLAMP) ? TEX_SAMPLER_CLAMP_S_BIT : 0;
 			tex |= (clamp.wmt == WRAP_CLAMP || clamp.wmt == WRAP_REGION_CLAMP) ? TEX_SAMPLER_CLAMP_T_BIT : 0;
-			if (tex1.mmin_has_mipmap())
+			if (tex1.mmin_has_mipmap() && !hack_disable_mipmaps)
 			{
 				tex2 = tex1.lcm;
 				tex2 |= tex1.l << 1;
@@ -1487,6 +1500,10 @@ struct pgs_gs
 		{
 			state |= 1u << (STATE_BIT_SCANMSK_EVEN + msk - 2);
 			has_scanmsk = true;
+			// A SCANMSK primitive taller than 400 rows interleaves fields
+			// itself: progressive read-out is off for the next 4 vsyncs.
+			if (bb[1] + 400 < bb[3])
+				complex_scanmsk_timeout = 4;
 		}
 
 		if (!prim.fst)
@@ -1625,7 +1642,7 @@ struct pgs_gs
 
 		if (template_dirty)
 		{
-			update_template();
+			update_template(bb);
 			template_dirty = false;
 		}
 
@@ -1644,7 +1661,7 @@ struct pgs_gs
 				{
 					flush_render_pass(FLUSH_TEXTURE_HAZARD);
 					check_frame_buffer_state();
-					update_template();
+					update_template(bb);
 					template_dirty = false;
 				}
 				tex_check_key[0] = tpl_serial;
@@ -1700,7 +1717,7 @@ struct pgs_gs
 			{
 				flush_render_pass(FLUSH_TEXTURE_HAZARD);
 				check_frame_buffer_state();
-				update_template();
+				update_template(bb);
 				template_dirty = false;
 				tracker.test_mark(frame.fbp, D.fb_stride, fx0, fx1, fy0, fy1, 0);
 				if (z_sens)
@@ -2192,19 +2209,12 @@ int pgs_gs_scanout_circuit(pgs_gs *gs, uint32_t circuit, uint32_t phase, uint32_
 // GSRenderer::vsync (gs/gs_renderer.cpp:4189-5055): everything that is decided
 // from registers happens here; the backend samples, composes, writes back and
 // deinterlaces (pgs_merge_params).
-int pgs_gs_vsync(pgs_gs *gs, const pgs_vsync_info *info, void *dst, uint64_t dst_size, pgs_scanout_result *res)
+static int vsync_scanout(pgs_gs *gs, const pgs_vsync_info *info, uint32_t flags, void *dst, uint64_t dst_size,
+                         pgs_scanout_result *res)
 {
-	if (!gs || !info || !res)
-		return PGS_ERROR_INVALID_ARGUMENT;
-	if (gs->ops->abi_version < 3 || !gs->ops->vsync)
-		return PGS_ERROR_UNSUPPORTED;
-	gs->flush();
-	if (gs->sticky_error)
-		return gs->sticky_error;
 	*res = {};
 	const uint64_t pmode = gs->priv[0], smode1 = gs->priv[1], smode2 = gs->priv[2];
 	const uint64_t extbuf = gs->priv[11], extdata = gs->priv[12], extwrite = gs->priv[13], bgcolor = gs->priv[14];
-	const uint32_t flags = info->flags;
 	const bool force_progressive = (flags & PGS_VSYNC_FORCE_PROGRESSIVE) != 0;
 	const bool overscan = (flags & PGS_VSYNC_OVERSCAN) != 0;
 	const bool crtc_offsets = (flags & PGS_VSYNC_CRTC_OFFSETS) != 0;
@@ -2518,6 +2528,66 @@ int pgs_gs_set_super_sampled_textures(pgs_gs *gs, int enable)
 		return PGS_ERROR_INVALID_ARGUMENT;
 	gs->flush();
 	gs->ssaa_textures = enable != 0;
+	gs->reg_serial++;
+	gs->template_dirty = true;
+	return gs->sticky_error;
+}
+
+int pgs_gs_vsync(pgs_gs *gs, const pgs_vsync_info *info, void *dst, uint64_t dst_size, pgs_scanout_result *res)
+{
+	if (!gs || !info || !res)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if (gs->ops->abi_version < 3 || !gs->ops->vsync)
+		return PGS_ERROR_UNSUPPORTED;
+	gs->flush();
+	if (gs->sticky_error)
+		return gs->sticky_error;
+
+	// GSInterface::vsync (gs/gs_interface.cpp:4626-4690): a recent tall
+	// SCANMSK primitive turns progressive read-out off, and field-aware
+	// rendering is chosen for the primitives drawn after this vsync.
+	uint32_t flags = info->flags;
+	if (gs->complex_scanmsk_timeout)
+		flags &= ~PGS_VSYNC_FORCE_PROGRESSIVE;
+	const uint64_t smode1 = gs->priv[1], smode2 = gs->priv[2];
+	const bool field_aware = (info->flags & PGS_VSYNC_HIGH_RESOLUTION) && gs->sampling_rate_y_log2 &&
+	                         field(smode2, 1, 1) && field(smode2, 0, 1) && field(smode1, 13, 2) != 0;
+	if (field_aware != gs->field_aware)
+	{
+		gs->field_aware = field_aware;
+		gs->reg_serial++;
+		gs->template_dirty = true;
+	}
+
+	int r = vsync_scanout(gs, info, flags, dst, dst_size, res);
+	if (r != PGS_ERROR_CAPACITY && gs->complex_scanmsk_timeout)
+		gs->complex_scanmsk_timeout--;
+	return r;
+}
+
+int pgs_gs_vsync_can_skip(const pgs_gs *gs, const pgs_vsync_info *info)
+{
+	if (!gs || !info)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	// GSRenderer::scanout_is_interlaced (gs/gs_renderer.cpp:4174-4187).
+	const uint64_t smode2 = gs->priv[2];
+	const bool INT = field(smode2, 0, 1) != 0, FFMD = field(smode2, 1, 1) != 0;
+	bool interlaced = INT;
+	if (INT && !FFMD && (info->flags & PGS_VSYNC_FORCE_PROGRESSIVE))
+		interlaced = false;
+	return (gs->complex_scanmsk_timeout == 0 && !interlaced) ? 1 : 0;
+}
+
+int pgs_gs_set_hacks(pgs_gs *gs, const pgs_hacks *hacks)
+{
+	if (!gs || !hacks)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	if (hacks->backbuffer_promotion)
+		return PGS_ERROR_UNSUPPORTED;
+	gs->flush();
+	gs->hack_disable_mipmaps = hacks->disable_mipmaps != 0;
+	gs->hack_unsynced_readbacks = hacks->unsynced_readbacks != 0;
+	gs->hack_blend_demote = hacks->allow_blend_demote != 0;
 	gs->reg_serial++;
 	gs->template_dirty = true;
 	return gs->sticky_error;

@@ -62,6 +62,9 @@ struct DevInstance
 	uint32_t mask_words;          // bitmask words per 8x8 sub-tile (1 bit per primitive)
 	uint32_t summary_words;       // summary words per sub-tile (1 bit per mask word)
 	uint32_t sub_w, sub_h;        // 8x8 sub-tiles per row / column
+	int32_t snap_mask_y;          // raster snap of rows: half the sample pitch when field rendering
+	uint32_t force_ss;            // field rendering: every covered tile super-sampled
+	uint32_t blend_demote;        // primitives per coarse tile that demote a blended tile, 0 = off
 };
 
 // Linear RGBA8 image decoded from swizzled VRAM + CLUT for one mip level of
@@ -144,6 +147,7 @@ struct PassParams
 	uint32_t num_states, num_textures;
 	uint32_t max_tex_levels;      // largest slot count (mip levels or sample layers) of the pass's textures
 	uint32_t rp_is_blur_mask;     // per instance: the pass looks like a blur kernel (render_pass_instance_is_deduced_blur)
+	uint32_t force_linear_ss;     // FORCE_LINEAR_SUPER_SAMPLE: field rendering with super-sampled textures
 	const uint32_t *phase_lut;    // PHASE_LUT_WORDS words
 	uint32_t tile_size_log2;
 	uint32_t has_aa1, has_scanmsk, has_ss_reference;
@@ -170,6 +174,8 @@ constexpr uint32_t TILE_NONEMPTY = 1u << 0;
 constexpr uint32_t TILE_REQ_SS = 1u << 1;
 constexpr uint32_t TILE_REQ_SS_ZW = 1u << 2;
 constexpr uint32_t TILE_HAS_ZW = 1u << 3;
+// Primitives binned to the tile, counted from this bit when blend demotion is on.
+constexpr uint32_t TILE_COUNT_SHIFT = 8;
 
 constexpr uint32_t ERROR_FLAG_TILE_OVERFLOW = 1u << 0;
 
@@ -568,11 +574,13 @@ __global__ void __launch_bounds__(128) setup_kernel(PassParams P)
 	if (pa.fbmsk != opaque_fbmask && (new_state & (1u << STATE_BIT_OPAQUE)))
 		new_state &= ~(1u << STATE_BIT_OPAQUE);
 
-	// Super-sampled textures (triangle_setup.comp:677-825, with
-	// FORCE_LINEAR_SUPER_SAMPLE off): nearest blits map sample to sample,
-	// nearest downsamples and blur kernels fall back to the single-sampled
-	// layer, linear upsamples read the resolved layer; what stays per-sample
-	// interpolates per sample around the single-sampled mean position.
+	// Super-sampled textures (triangle_setup.comp:677-825): nearest blits map
+	// sample to sample, nearest downsamples and blur kernels fall back to the
+	// single-sampled layer, linear upsamples read the resolved layer (with
+	// FORCE_LINEAR_SUPER_SAMPLE, for field rendering, blur kernels read the
+	// resolved layer linearly and linear downsamples and upsamples stay per
+	// sample); what stays per-sample interpolates per sample around the
+	// single-sampled mean position.
 	if (sry != 0 && (tex & (TEX_PER_SAMPLE_BIT | TEX_SAMPLE_MAPPING_BIT)) == TEX_PER_SAMPLE_BIT)
 	{
 		const int32_t udx = abs(int32_t(at1.u) - int32_t(at0.u)), udy = abs(int32_t(at1.v) - int32_t(at0.v));
@@ -592,7 +600,20 @@ __global__ void __launch_bounds__(128) setup_kernel(PassParams P)
 				                  ((blend >> BLEND_MODE_A_MODE_OFFSET) & 3u) == BLEND_RGB_SOURCE &&
 				                  ((blend >> BLEND_MODE_B_MODE_OFFSET) & 3u) == BLEND_RGB_ZERO &&
 				                  ((blend >> BLEND_MODE_D_MODE_OFFSET) & 3u) == BLEND_RGB_DEST;
-				if (blur)
+				if (blur && P.force_linear_ss)
+				{
+					// Field rendering keeps blur kernels per sample: the
+					// resolved layer, filtered linearly, with the mean sample
+					// position moved to the texel centre
+					// (triangle_setup.comp:729-746).
+					tex |= TEX_SAMPLE_RESOLVED_BIT | TEX_SAMPLER_MAG_LINEAR_BIT;
+					const int32_t avg_u = (int32_t(at0.u) + int32_t(at1.u)) >> 1;
+					const int32_t avg_v = (int32_t(at0.v) + int32_t(at1.v)) >> 1;
+					const int32_t ph_x = (avg_u - ((dx + ax) >> 1)) & 15, ph_y = (avg_v - ((dy + ay) >> 1)) & 15;
+					ta.stqf0[0] = fadd(ta.stqf0[0], fsub(0.5f, fmul(__int2float_rn(ph_x), 0.0625f)));
+					ta.stqf0[1] = fadd(ta.stqf0[1], fsub(0.5f, fmul(__int2float_rn(ph_y), 0.0625f)));
+				}
+				else if (blur)
 					tex &= ~TEX_PER_SAMPLE_BIT;
 				else
 					tex |= TEX_SAMPLE_MAPPING_BIT;
@@ -601,9 +622,15 @@ __global__ void __launch_bounds__(128) setup_kernel(PassParams P)
 		else if (!perspective)
 		{
 			if (udx > ddx + 1 && udy > ddy + 1)
-				tex &= ~TEX_PER_SAMPLE_BIT;
+			{
+				if (!P.force_linear_ss)
+					tex &= ~TEX_PER_SAMPLE_BIT;
+			}
 			else if (ddx >= 2 * udx && ddy >= 2 * udy)
-				tex |= TEX_SAMPLE_RESOLVED_BIT;
+			{
+				if (!P.force_linear_ss)
+					tex |= TEX_SAMPLE_RESOLVED_BIT;
+			}
 		}
 		if ((tex & (TEX_PER_SAMPLE_BIT | TEX_SAMPLE_MAPPING_BIT)) == TEX_PER_SAMPLE_BIT)
 		{
@@ -927,6 +954,8 @@ __global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, u
 				continue;
 			uint32_t tile = uint32_t(ty) * I.tiles_w + uint32_t(tx);
 			atomicOr(&tile_flags[tile], flags);
+			if (I.blend_demote)
+				atomicAdd(&tile_flags[tile], 1u << TILE_COUNT_SHIFT);
 
 			int32_t gx0 = (max(s.bb[0], lo0) - I.base_x) >> 3, gx1 = (min(s.bb[2], hi0) - I.base_x) >> 3;
 			int32_t gy0 = (max(s.bb[1], lo1) - I.base_y) >> 3, gy1 = (min(s.bb[3], hi1) - I.base_y) >> 3;
@@ -994,7 +1023,7 @@ struct ShadeCtx
 	const DevInstance *I;
 	bool ss;
 	int dim;          // sampling rate y log2 when super-sampled, else 0
-	int32_t snap_mask;
+	int32_t snap_mask_x, snap_mask_y;
 	bool zs;
 	uint32_t fb_psm, zb_psm;
 	uint32_t sample; // sample index of the thread in a super-sampled tile, else 0
@@ -1713,9 +1742,9 @@ __device__ __forceinline__ int evaluate_coverage(const PrimSetup &s, int32_t cx,
 // Must be called by all lanes of a warp; returns with warp_any == false (and no
 // further work) when no lane of the warp is covered.  AA compiles the AA1
 // coverage path in (ubershader variant VARIANT_FLAG_HAS_AA1_BIT).
-template <bool AA>
-__device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetup &s, uint32_t st, const SampleState &S,
-                                               bool &opaque, bool &warp_any)
+template <bool AA, bool TEX_ARRAY>
+__device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetup &s, uint32_t pi, uint32_t st,
+                                               const SampleState &S, bool &opaque, bool &warp_any)
 {
 	const PassParams &P = *C.P;
 	Request r;
@@ -1726,8 +1755,10 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 	int32_t rx = S.hx, ry = S.hy;
 	if (C.ss && (st & (1u << STATE_BIT_SNAP_RASTER)))
 	{
-		rx &= C.snap_mask;
-		ry &= C.snap_mask;
+		// Sample-mapped textures keep the full-rate row grid when rows are
+		// snapped for field rendering (ubershader.comp:816-821).
+		rx &= C.snap_mask_x;
+		ry &= (TEX_ARRAY && (P.prims[pi].tex & TEX_SAMPLE_MAPPING_BIT)) ? C.snap_mask_x : C.snap_mask_y;
 	}
 	float i = 0.0f, j = 0.0f;
 	if (AA)
@@ -1767,7 +1798,15 @@ __device__ __forceinline__ Request shade_early(const ShadeCtx &C, const PrimSetu
 		uint32_t snap = st & ((1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE));
 		if (snap == (1u << STATE_BIT_SNAP_ATTRIBUTE))
 		{
-			int32_t qx = (S.hx & C.snap_mask) << (3 - C.dim), qy = (S.hy & C.snap_mask) << (3 - C.dim);
+			int32_t qx = (S.hx & C.snap_mask_x) << (3 - C.dim), qy = (S.hy & C.snap_mask_y) << (3 - C.dim);
+			i = fadd(fmul(__int2float_rn(idot3(s.b, qx, qy)), s.inv_area), s.error_i);
+			j = fadd(fmul(__int2float_rn(idot3(s.c, qx, qy)), s.inv_area), s.error_j);
+		}
+		else if (TEX_ARRAY && snap == (1u << STATE_BIT_SNAP_RASTER))
+		{
+			// Per-sample textured sprite: coverage snapped, attributes
+			// interpolated per sample (ubershader.comp:888-895).
+			int32_t qx = S.hx << (3 - C.dim), qy = S.hy << (3 - C.dim);
 			i = fadd(fmul(__int2float_rn(idot3(s.b, qx, qy)), s.inv_area), s.error_i);
 			j = fadd(fmul(__int2float_rn(idot3(s.c, qx, qy)), s.inv_area), s.error_j);
 		}
@@ -1817,7 +1856,7 @@ __device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi
 	const PrimSetup s = P.setup[pi];
 	uint32_t st = P.prims[pi].state;
 	bool opaque, any_cov;
-	Request q = shade_early<AA>(C, s, st, S, opaque, any_cov);
+	Request q = shade_early<AA, MIP>(C, s, pi, st, S, opaque, any_cov);
 	if (!any_cov)
 		return;
 	if (q.coverage > 0)
@@ -1891,7 +1930,10 @@ __device__ __forceinline__ uint32_t subtile_mode(const PassParams &P, const DevI
 	const uint32_t flags = tile_flags[(gy >> sh) * I.tiles_w + (gx >> sh)];
 	if (!(flags & TILE_NONEMPTY))
 		return 0;
-	bool req = (flags & TILE_REQ_SS) || ((flags & TILE_REQ_SS_ZW) && (flags & TILE_HAS_ZW));
+	bool req = I.force_ss || (flags & TILE_REQ_SS);
+	if (I.blend_demote && (flags >> TILE_COUNT_SHIFT) >= I.blend_demote && !(flags & TILE_HAS_ZW))
+		req = false;
+	req = req || ((flags & TILE_REQ_SS_ZW) && (flags & TILE_HAS_ZW));
 	return (I.rate_y_log2 != 0 && req) ? 2u : 1u;
 }
 
@@ -1911,7 +1953,8 @@ __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInst
 	C.I = &I;
 	C.ss = SS;
 	C.dim = SS ? int(I.rate_y_log2) : 0;
-	C.snap_mask = -(1 << I.rate_y_log2);
+	C.snap_mask_x = -(1 << I.rate_y_log2);
+	C.snap_mask_y = I.snap_mask_y;
 	C.zs = I.zb_psm != 0xffffffffu;
 	C.fb_psm = I.fb_psm;
 	C.zb_psm = I.zb_psm;

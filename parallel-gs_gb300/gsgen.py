@@ -1082,6 +1082,64 @@ def frame_ssaa_textures(seed: int) -> Frame:
     return Frame("ssaa_tex_%d" % seed, s.tobytes(), ss, ordered, n,
                  {"width": width, "height": height, "fbp": fin, "zbp": zbp, "ssaa_textures": True})
 
+def frame_field_aware(seed: int) -> Frame:
+    """Field-aware rendering: a frame drawn after a high-resolution vsync of
+    field-rendered interlaced output.  Even seeds: the super-sampled texture
+    scene (blur groups take the FORCE_LINEAR_SUPER_SAMPLE path), with or
+    without super-sampled textures; odd seeds: the textured 3D scene at
+    320 x 224 (instances that may be fields) or 640 x 448 (too tall to be)."""
+    if seed % 2 == 0:
+        f = frame_ssaa_textures(seed)
+        f.meta["ssaa_textures"] = seed % 4 == 0
+    else:
+        tall = seed % 4 == 3
+        f = frame_c2(seed=seed, num_triangles=600, num_sprites=60, super_sampling=[2, 4, 8, 16][(seed // 2) % 4],
+                     num_textures=2, width=640 if tall else 320, height=448 if tall else 224)
+    f.meta["field_aware"] = True
+    f.name = "field_aware_%d" % seed
+    return f
+
+
+def frame_blend_demote(seed: int) -> Frame:
+    """Blend demotion hack: many overlapping blended triangles and sprites
+    (well over 32 per coarse tile), super-sampled, depth written only in the
+    left 96 columns so that tiles on the right qualify; odd seeds add one
+    unblended sprite, which turns demotion off for the pass."""
+    rng = np.random.Generator(np.random.PCG64(91000 + seed))
+    s = GifStream()
+    ss = [2, 4, 8, 16][seed % 4]
+    width, height, zbp = 256, 224, 60
+    _frame_setup(s, 0, width // 64, PSMCT32, zbp, PSMZ24, width, height, test_reg(zte=1, ztst=1))
+    for p_ in range(3):
+        zmsk = int(p_ != 1)
+        s.ad([(ZBUF_1, zbuf_reg(zbp, PSMZ24, zmsk)), (TEST_1, test_reg(zte=1, ztst=[1, 2, 1][p_])),
+              (ALPHA_1, alpha_reg(0, 1, 0, 1))])
+        n = int(rng.integers(40, 120))
+        x, y = random_triangles(rng, n, 96 if p_ == 1 else width, height, 200.0, 30000.0)
+        z = rng.integers(0, 1 << 24, size=(n, 3))
+        rgba = rng.integers(0, 256, size=(3 * n, 4))
+        q = np.zeros((3 * n, 2, 2), dtype=np.uint64)
+        q[:, 0] = q_rgbaq(rgba)
+        q[:, 1] = q_xyz2(x.reshape(-1), y.reshape(-1), z.reshape(-1))
+        s.packed(prim_reg(PRIM_TRI, iip=1, abe=1), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+        if p_ == 1:
+            continue
+        m = int(rng.integers(20, 60))
+        xs, ys = random_sprites(rng, m, width, height, 400.0, 20000.0)
+        col = rng.integers(0, 256, size=(2 * m, 4))
+        q = np.zeros((2 * m, 2, 2), dtype=np.uint64)
+        q[:, 0] = q_rgbaq(col)
+        q[:, 1] = q_xyz2(xs.reshape(-1), ys.reshape(-1), rng.integers(0, 1 << 24, size=2 * m))
+        s.packed(prim_reg(PRIM_SPRITE, abe=1), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+    if seed % 2 == 1:
+        q = np.zeros((2, 2, 2), dtype=np.uint64)
+        q[:, 0] = q_rgbaq(np.array([[255, 0, 0, 128]] * 2))
+        q[:, 1] = q_xyz2(np.array([16 * 16, 48 * 16]), np.array([16 * 16, 40 * 16]), np.array([5, 5]))
+        s.packed(prim_reg(PRIM_SPRITE), [D_RGBAQ, D_XYZ2], q.reshape(-1, 2))
+    return Frame("blend_demote_%d" % seed, s.tobytes(), ss, True, 0,
+                 {"width": width, "height": height, "fbp": 0, "zbp": zbp, "hacks": {"allow_blend_demote": True}})
+
+
 def write_dump(path, transfers, vram: bytes | None = None, regs: dict | None = None, version: int = 9,
                serial: bytes = b"", vsync_fields=(0,)) -> None:
     """Writes a GS dump in the PCSX2 / GSdx layout (GSDumpGenerator::init,

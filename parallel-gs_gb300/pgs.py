@@ -92,7 +92,7 @@ EXPORTED_SYMBOLS = [
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
     "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait",
     "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit", "pgs_gs_vsync",
-    "pgs_gs_set_super_sampled_textures",
+    "pgs_gs_set_super_sampled_textures", "pgs_gs_vsync_can_skip", "pgs_gs_set_hacks",
     "pgs_gs_dump_open", "pgs_gs_dump_next_vsync", "pgs_gs_dump_close", "pgs_gs_dump_record_begin",
     "pgs_gs_dump_record_vsync", "pgs_gs_dump_record_end", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
     "pgs_gs_set_super_sampling_rate",
@@ -164,6 +164,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.pgs_gs_consume_flush_stats.argtypes = [vp, C.POINTER(FlushStats)]
     lib.pgs_gs_set_super_sampling_rate.argtypes = [vp, u32, u32]
     lib.pgs_gs_set_super_sampled_textures.argtypes = [vp, i32]
+    lib.pgs_gs_vsync_can_skip.argtypes = [vp, C.POINTER(VsyncInfo)]
+    lib.pgs_gs_set_hacks.argtypes = [vp, C.POINTER(Hacks)]
     if path is None:
         _lib = lib
     return lib
@@ -186,6 +188,12 @@ class BackendOps(C.Structure):
 
 class VsyncInfo(C.Structure):
     _fields_ = [("phase", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class Hacks(C.Structure):
+    """pgs_hacks (Hacks, gs/gs_interface.hpp:209-237)."""
+    _fields_ = [(n, C.c_uint32) for n in ("disable_mipmaps", "unsynced_readbacks", "backbuffer_promotion",
+                                          "allow_blend_demote")]
 
 
 class ScanoutResult(C.Structure):
@@ -379,6 +387,18 @@ class GSInterface:
         d = {k: getattr(res, k) for k, _ in ScanoutResult._fields_ if k != "padding"}
         img = out[: res.width * res.height * 4].reshape(res.height, res.width, 4).copy()
         return img, d
+
+    def vsync_can_skip(self, phase: int = 0, flags: int = 0) -> bool:
+        """GSInterface::vsync_can_skip: progressive read-out with no recent tall SCANMSK primitive."""
+        r = self.lib.pgs_gs_vsync_can_skip(self.handle, C.byref(VsyncInfo(phase, flags)))
+        check(min(r, 0), "vsync_can_skip")
+        return r == 1
+
+    def set_hacks(self, disable_mipmaps: bool = False, unsynced_readbacks: bool = False,
+                  backbuffer_promotion: bool = False, allow_blend_demote: bool = False) -> None:
+        """GSInterface::set_hacks; backbuffer_promotion is not supported (PGSError)."""
+        h = Hacks(int(disable_mipmaps), int(unsynced_readbacks), int(backbuffer_promotion), int(allow_blend_demote))
+        check(self.lib.pgs_gs_set_hacks(self.handle, C.byref(h)), "set_hacks")
 
     def write_vram(self, data, offset: int = 0) -> None:
         buf = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, bytes) else data)

@@ -52,7 +52,8 @@ class RenderPass(C.Structure):
                 ("textures", C.POINTER(TextureDesc)), ("num_textures", C.c_uint32),
                 ("instances", RPInstance * 8), ("num_instances", C.c_uint32),
                 ("coarse_tile_size_log2", C.c_uint32), ("has_aa1", C.c_uint32), ("has_scanmsk", C.c_uint32),
-                ("flush_reason", C.c_uint32), ("has_mipmap", C.c_uint32), ("has_ss_textures", C.c_uint32)]
+                ("flush_reason", C.c_uint32), ("has_mipmap", C.c_uint32), ("has_ss_textures", C.c_uint32),
+                ("field_aware", C.c_uint32), ("blend_demote", C.c_uint32)]
 
 
 class CopyDesc(C.Structure):
@@ -77,12 +78,14 @@ SUBMIT = C.CFUNCTYPE(C.c_int, C.c_void_p)
 READ = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p)
 WRITE = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_uint64, C.c_void_p)
 ERROR = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_uint32))
+VSYNC = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)
 
 
 class Ops(C.Structure):
     _fields_ = [("abi_version", C.c_uint32), ("destroy", DESTROY), ("reserve", RESERVE), ("flush", FLUSH),
                 ("copy", COPY), ("palette", PALETTE), ("set_ss", SETSS), ("submit", SUBMIT), ("read", READ),
-                ("write", WRITE), ("error", ERROR)]
+                ("write", WRITE), ("error", ERROR), ("read_async", C.c_void_p), ("wait_ticket", C.c_void_p),
+                ("sample_circuit", C.c_void_p), ("vsync", VSYNC)]
 
 
 def _struct_array(ptr, n, fields):
@@ -100,9 +103,10 @@ class RecordingBackend(pgs.Backend):
         self._pos = (VertexPosition * (3 * MAXP))()
         self._attr = (VertexAttribute * (3 * MAXP))()
         self._prim = (PrimitiveAttribute * MAXP)()
-        self._cbs = Ops(1, DESTROY(lambda s: None), RESERVE(self._reserve), FLUSH(self._flush), COPY(self._copy),
+        self.vsyncs = 0
+        self._cbs = Ops(3, DESTROY(lambda s: None), RESERVE(self._reserve), FLUSH(self._flush), COPY(self._copy),
                         PALETTE(self._palette), SETSS(self._set_ss), SUBMIT(lambda s: 0), READ(self._read),
-                        WRITE(self._write), ERROR(self._error))
+                        WRITE(self._write), ERROR(self._error), None, None, None, VSYNC(self._vsync))
         super().__init__(C.addressof(self._cbs), 1)
 
     def _reserve(self, s, n, pos, attr, prim):
@@ -126,6 +130,7 @@ class RecordingBackend(pgs.Backend):
             "coarse_tile_size_log2": rp.coarse_tile_size_log2,
             "has_aa1": rp.has_aa1, "has_scanmsk": rp.has_scanmsk, "flush_reason": rp.flush_reason,
             "has_mipmap": rp.has_mipmap, "has_ss_textures": rp.has_ss_textures,
+            "field_aware": rp.field_aware, "blend_demote": rp.blend_demote,
         }
         self.passes.append(rec)
         return 0
@@ -154,6 +159,11 @@ class RecordingBackend(pgs.Backend):
 
     def _write(self, s, off, size, src):
         C.memmove(self.vram.ctypes.data + off, src, size)
+        return 0
+
+    def _vsync(self, s, params, dst):
+        # Merging is not recorded: the image stays as the caller allocated it.
+        self.vsyncs += 1
         return 0
 
     def _error(self, s, flags):

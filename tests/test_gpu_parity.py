@@ -279,3 +279,29 @@ def test_combined_feature_streams(seed):
                     sum(p.num_primitives for p in parts), dict(parts[0].meta))
     ref, out = run_both(f)
     assert_same(ref, out)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_field_aware_rendering_parity(seed):
+    """Frames drawn after a high-resolution vsync of field-rendered output:
+    forced super-sampled tiles, rows snapped at half the sample pitch,
+    FORCE_LINEAR_SUPER_SAMPLE blur kernels, and 448-row frames that stay as
+    they were."""
+    ref, out = run_both(gsgen.frame_field_aware(seed))
+    assert_same(ref, out)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_blend_demote_parity(seed):
+    """allow_blend_demote: crowded blended tiles without depth writes shade
+    single-sampled (per-tile primitive counts from binning)."""
+    ref, out = run_both(gsgen.frame_blend_demote(seed))
+    assert_same(ref, out)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_disable_mipmaps_parity(seed):
+    f = gsgen.frame_mip(seed)
+    f.meta["hacks"] = {"disable_mipmaps": True}
+    ref, out = run_both(f)
+    assert_same(ref, out)
