@@ -308,7 +308,25 @@ typedef struct pgs_backend_ops
 	 * (raw circuit: its read-out; deinterlaced: width x 2 * height; else
 	 * width x height RGBA8). */
 	int (*vsync)(void *self, const pgs_merge_params *params, void *dst);
+	/* abi_version >= 4, optional: GPU time per stage (GSRenderer timestamps,
+	 * gs/gs_renderer.cpp:1205-1233).  enable 1 starts timing the stages, 0
+	 * stops it, -1 leaves it as it is; totals (PGS_TIMESTAMP_COUNT doubles,
+	 * may be NULL) receives the seconds accumulated so far per stage, after
+	 * the timed work has completed. */
+	int (*timestamps)(void *self, int enable, double *totals);
 } pgs_backend_ops;
+
+/* TimestampType (gs/gs_renderer.hpp:67-79). */
+#define PGS_TIMESTAMP_SYNC_HOST_TO_VRAM 0u
+#define PGS_TIMESTAMP_COPY_VRAM 1u
+#define PGS_TIMESTAMP_PALETTE_UPDATE 2u
+#define PGS_TIMESTAMP_TEXTURE_UPLOAD 3u
+#define PGS_TIMESTAMP_TRIANGLE_SETUP 4u
+#define PGS_TIMESTAMP_BINNING 5u
+#define PGS_TIMESTAMP_SHADING 6u
+#define PGS_TIMESTAMP_READBACK 7u
+#define PGS_TIMESTAMP_VSYNC 8u
+#define PGS_TIMESTAMP_COUNT 9u
 
 /* ------------------------------------------------------------------ */
 /* CUDA backend                                                         */
@@ -619,6 +637,65 @@ typedef struct pgs_hacks
 	uint32_t allow_blend_demote;
 } pgs_hacks;
 int pgs_gs_set_hacks(pgs_gs *gs, const pgs_hacks *hacks);
+
+/* GSInterface::reset_context_state (gs/gs_interface.cpp:26-39): flushes, then
+ * returns the register file, the GIF paths and the vertex queue to their
+ * power-on state (PRMODECONT.AC = 1, everything else 0). */
+int pgs_gs_reset_context_state(pgs_gs *gs);
+/* GSInterface::clobber_register_state (gs/gs_interface.cpp:4266-4274): state
+ * derived from registers is rebuilt on the next use, for callers that changed
+ * registers behind the interface (pgs_gs_set_register). */
+int pgs_gs_clobber_register_state(pgs_gs *gs);
+/* get_register_state (gs/gs_interface.hpp:287-288): the register file by A+D
+ * address (0x00-0x7f).  pgs_gs_set_register stores a value without the side
+ * effects of pgs_gs_write_register (no transfer, kick or flush); follow it with
+ * pgs_gs_clobber_register_state. */
+int pgs_gs_read_register(const pgs_gs *gs, uint32_t addr, uint64_t *value);
+int pgs_gs_set_register(pgs_gs *gs, uint32_t addr, uint64_t value);
+
+/* GIFPath (gs/gs_interface.hpp:63-68, get_gif_path :293-294): the current
+ * GIFtag of a path, the register index within a loop and the loops done. */
+typedef struct pgs_gif_path
+{
+	uint64_t tag[2];
+	uint32_t reg;
+	uint32_t loop;
+} pgs_gif_path;
+int pgs_gs_get_gif_path(const pgs_gs *gs, uint32_t path, pgs_gif_path *out);
+int pgs_gs_set_gif_path(pgs_gs *gs, uint32_t path, const pgs_gif_path *in);
+
+/* SignalInterface (gs/gs_interface.hpp:238-248, set_signal_interface): called
+ * for SIGNAL, FINISH and LABEL register writes with the written value; a
+ * non-zero return flushes (rendering is submitted, nothing waits).  A NULL
+ * interface, or a NULL member, ignores the register. */
+typedef int (*pgs_signal_fn)(void *user, uint64_t payload);
+typedef struct pgs_signal_interface
+{
+	pgs_signal_fn on_signal;
+	pgs_signal_fn on_finish;
+	pgs_signal_fn on_label;
+	void *user;
+} pgs_signal_interface;
+int pgs_gs_set_signal_interface(pgs_gs *gs, const pgs_signal_interface *iface);
+
+/* DebugMode (gs/gs_interface.hpp:137-153, set_debug_mode).  timestamps turns
+ * per-stage GPU timing on in a backend that has it (pgs_backend_ops.timestamps);
+ * the other members are debugging aids of the Vulkan renderer (render-target
+ * feedback, deterministic timeline queries, sampler feedback, per-draw
+ * stepping), accepted and without effect here. */
+typedef struct pgs_debug_mode
+{
+	uint32_t feedback_render_target;
+	uint32_t timestamps;
+	uint32_t deterministic_timeline_query;
+	uint32_t disable_sampler_feedback;
+	uint32_t draw_mode; /* 0 none, 1 strided, 2 full */
+} pgs_debug_mode;
+int pgs_gs_set_debug_mode(pgs_gs *gs, const pgs_debug_mode *mode);
+/* GSInterface::get_accumulated_timestamps (gs/gs_interface.cpp:4702-4705):
+ * seconds of GPU time spent in stage `type` (PGS_TIMESTAMP_*) while timing
+ * was on; 0 when the backend does not time stages. */
+int pgs_gs_get_accumulated_timestamps(pgs_gs *gs, uint32_t type, double *seconds);
 
 #ifdef __cplusplus
 }

@@ -288,6 +288,89 @@ struct CudaBackend
 	float last_shade_ms = 0.0f;
 	bool shade_timing = false;
 	bool shade_started = false;
+
+	// Stage timestamps (GSRenderer timestamps, gs/gs_renderer.cpp:1205-1233):
+	// while on, each stage issued outside stream capture is bracketed by an
+	// event pair; the pairs are summed per stage when the totals are read.
+	struct StageSpan
+	{
+		uint32_t type;
+		cudaEvent_t ev[2];
+	};
+	bool stage_timing = false;
+	std::vector<StageSpan> stage_spans;
+	std::vector<cudaEvent_t> stage_events; // free events
+	double stage_total[PGS_TIMESTAMP_COUNT] = {};
+
+	bool stage_begin(uint32_t type, StageSpan &sp)
+	{
+		if (!stage_timing)
+			return false;
+		cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+		if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+			return false;
+		while (stage_events.size() < 2)
+		{
+			cudaEvent_t e = nullptr;
+			if (cudaEventCreate(&e) != cudaSuccess)
+				return false;
+			stage_events.push_back(e);
+		}
+		sp.type = type;
+		sp.ev[0] = stage_events.back();
+		stage_events.pop_back();
+		sp.ev[1] = stage_events.back();
+		stage_events.pop_back();
+		cudaEventRecord(sp.ev[0], stream);
+		return true;
+	}
+
+	void stage_end(const StageSpan &sp)
+	{
+		cudaEventRecord(sp.ev[1], stream);
+		stage_spans.push_back(sp);
+		if (stage_spans.size() >= 4096)
+			stage_collect();
+	}
+
+	int stage_collect()
+	{
+		int r = PGS_OK;
+		for (const auto &sp : stage_spans)
+		{
+			float ms = 0.0f;
+			if (r == PGS_OK && cudaEventSynchronize(sp.ev[1]) == cudaSuccess &&
+			    cudaEventElapsedTime(&ms, sp.ev[0], sp.ev[1]) == cudaSuccess)
+				stage_total[sp.type] += double(ms) * 1e-3;
+			else
+				r = PGS_ERROR_CUDA;
+			stage_events.push_back(sp.ev[0]);
+			stage_events.push_back(sp.ev[1]);
+		}
+		stage_spans.clear();
+		return r;
+	}
+
+	// Brackets the work issued in its scope as one span of `type`.
+	struct StageScope
+	{
+		CudaBackend *b;
+		StageSpan sp;
+		bool on;
+		StageScope(CudaBackend *b_, uint32_t type) : b(b_), on(b_->stage_begin(type, sp)) {}
+		~StageScope() { if (on) b->stage_end(sp); }
+	};
+
+	int timestamps(int enable, double *totals)
+	{
+		if (enable >= 0)
+			stage_timing = enable != 0;
+		if (!totals)
+			return PGS_OK;
+		int r = stage_collect();
+		memcpy(totals, stage_total, sizeof(stage_total));
+		return r;
+	}
 	uint64_t h2d_bytes = 0, d2h_bytes = 0, total_launches = 0, render_passes = 0;
 
 	// Asynchronous readbacks in flight.  A destination outside pinned memory
@@ -408,6 +491,13 @@ struct CudaBackend
 			if (rb.done) cudaEventDestroy(rb.done);
 			cudaFreeHost(rb.staging);
 		}
+		for (const auto &sp : stage_spans)
+		{
+			cudaEventDestroy(sp.ev[0]);
+			cudaEventDestroy(sp.ev[1]);
+		}
+		for (cudaEvent_t e : stage_events)
+			cudaEventDestroy(e);
 		if (stream)
 			cudaStreamDestroy(stream);
 	}
@@ -883,10 +973,13 @@ struct CudaBackend
 		if (r)
 			return r;
 		uint32_t *d_sub_masks = d_masks, *d_sub_summary = d_masks + mask_words;
-		CUDA_TRY(cudaMemsetAsync(d_masks, 0, (mask_words + summary_words) * sizeof(uint32_t), stream));
-		CUDA_TRY(cudaMemsetAsync(d_flags, 0, tiles * sizeof(uint32_t), stream));
-		bin_kernel<<<(count + 127) / 128, 128, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags);
-		launch_counter++;
+		{
+			StageScope ts(this, PGS_TIMESTAMP_BINNING);
+			CUDA_TRY(cudaMemsetAsync(d_masks, 0, (mask_words + summary_words) * sizeof(uint32_t), stream));
+			CUDA_TRY(cudaMemsetAsync(d_flags, 0, tiles * sizeof(uint32_t), stream));
+			bin_kernel<<<(count + 127) / 128, 128, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags);
+			launch_counter++;
+		}
 		uint32_t grid = uint32_t(subs);
 		if (collect && !p.has_mipmap && !p.has_ss_textures && ns_log2 <= BATCH_MAX_NS_LOG2 &&
 		    (I.rate_y_log2 != 0 || ns_log2 == 0))
@@ -912,6 +1005,7 @@ struct CudaBackend
 		}
 		// Passes with mip levels or super-sampled textures take the AA-capable
 		// variant too (three variants per rate).
+		StageScope ts(this, PGS_TIMESTAMP_SHADING);
 		if (p.has_mipmap || p.has_ss_textures)
 			launch_shade<true, true>(P, I, ns_log2, grid, d_sub_masks, d_sub_summary);
 		else if (p.has_aa1)
@@ -952,16 +1046,20 @@ struct CudaBackend
 				c.src_vram = d_snapshot;
 			}
 			dim3 grid((c.width + 31) / 32, (c.height + 7) / 8);
+			StageScope ts(this, PGS_TIMESTAMP_COPY_VRAM);
 			upload_kernel<<<grid, 256, 0, stream>>>(c, d_vram);
 			launch_counter++;
 			CUDA_TRY(cudaGetLastError());
 			return PGS_OK;
 		}
 		case OP_CLUT:
+		{
+			StageScope ts(this, PGS_TIMESTAMP_PALETTE_UPDATE);
 			clut_kernel<<<1, 256, 0, stream>>>(op.clut, d_vram, d_clut);
 			launch_counter++;
 			CUDA_TRY(cudaGetLastError());
 			return PGS_OK;
+		}
 		case OP_PASS:
 			return execute_pass(op.pass);
 		}
@@ -1162,19 +1260,23 @@ struct CudaBackend
 		}
 		CUDA_TRY(cudaMemcpyAsync(d_prims_work, d_arena + p.prim_off, size_t(p.num_prims) * sizeof(pgs_primitive_attribute),
 		                         cudaMemcpyDeviceToDevice, stream));
-		if (H.instance_mask)
-			CUDA_TRY(cudaMemsetAsync(d_heuristic, 0, sizeof(SsHeuristic), stream));
-		setup_kernel<<<(p.num_prims + 127) / 128, 128, 0, stream>>>(P);
-		launch_counter++;
-		if (H.instance_mask)
 		{
-			// Flush order: setup, heuristic, binning (gs/gs_renderer.cpp:3157-3170).
-			single_sample_heuristic_kernel<<<dim3(256, p.num_instances), 1024, 0, stream>>>(P, H);
-			heuristic_apply_kernel<<<(p.num_prims + 255) / 256, 256, 0, stream>>>(P);
-			launch_counter += 2;
+			StageScope ts(this, PGS_TIMESTAMP_TRIANGLE_SETUP);
+			if (H.instance_mask)
+				CUDA_TRY(cudaMemsetAsync(d_heuristic, 0, sizeof(SsHeuristic), stream));
+			setup_kernel<<<(p.num_prims + 127) / 128, 128, 0, stream>>>(P);
+			launch_counter++;
+			if (H.instance_mask)
+			{
+				// Flush order: setup, heuristic, binning (gs/gs_renderer.cpp:3157-3170).
+				single_sample_heuristic_kernel<<<dim3(256, p.num_instances), 1024, 0, stream>>>(P, H);
+				heuristic_apply_kernel<<<(p.num_prims + 255) / 256, 256, 0, stream>>>(P);
+				launch_counter += 2;
+			}
 		}
 		if (p.num_textures && p.num_texels)
 		{
+			StageScope ts(this, PGS_TIMESTAMP_TEXTURE_UPLOAD);
 			dim3 grid((p.max_texels + 255) / 256, p.num_textures, p.max_levels);
 			texture_decode_kernel<<<grid, 256, 0, stream>>>(P);
 			launch_counter++;
@@ -1340,7 +1442,11 @@ struct CudaBackend
 	{
 		if (plane >= num_planes || off + size > VRAM_SIZE)
 			return PGS_ERROR_INVALID_ARGUMENT;
-		CUDA_TRY(cudaMemcpyAsync(dst, d_vram + size_t(plane) * VRAM_SIZE + off, size, cudaMemcpyDeviceToHost, stream));
+		{
+			StageScope ts(this, PGS_TIMESTAMP_READBACK);
+			CUDA_TRY(cudaMemcpyAsync(dst, d_vram + size_t(plane) * VRAM_SIZE + off, size, cudaMemcpyDeviceToHost,
+			                         stream));
+		}
 		CUDA_TRY(cudaStreamSynchronize(stream));
 		d2h_bytes += size;
 		total_launches += launch_counter;
@@ -1377,7 +1483,10 @@ struct CudaBackend
 				CUDA_TRY(cudaMallocHost(&slot->staging, VRAM_SIZE));
 			target = slot->staging;
 		}
-		CUDA_TRY(cudaMemcpyAsync(target, d_vram + off, size, cudaMemcpyDeviceToHost, stream));
+		{
+			StageScope ts(this, PGS_TIMESTAMP_READBACK);
+			CUDA_TRY(cudaMemcpyAsync(target, d_vram + off, size, cudaMemcpyDeviceToHost, stream));
+		}
 		CUDA_TRY(cudaEventRecord(slot->done, stream));
 		slot->ticket = next_ticket++;
 		slot->dst = pinned ? nullptr : dst;
@@ -1461,6 +1570,7 @@ struct CudaBackend
 	{
 		if (recording)
 			return PGS_ERROR_UNSUPPORTED;
+		StageScope ts(this, PGS_TIMESTAMP_VSYNC);
 		const pgs_circuit_params *cp[2] = { &m.circuit[0], &m.circuit[1] };
 		for (int i = 0; i < 2; i++)
 		{
@@ -1579,9 +1689,12 @@ struct CudaBackend
 	{
 		if (off + size > VRAM_SIZE)
 			return PGS_ERROR_INVALID_ARGUMENT;
-		CUDA_TRY(cudaMemcpyAsync(d_vram + off, src, size, cudaMemcpyHostToDevice, stream));
-		if (num_planes > 1)
-			CUDA_TRY(cudaMemsetAsync(d_vram + VRAM_SIZE + off, 0, size, stream));
+		{
+			StageScope ts(this, PGS_TIMESTAMP_SYNC_HOST_TO_VRAM);
+			CUDA_TRY(cudaMemcpyAsync(d_vram + off, src, size, cudaMemcpyHostToDevice, stream));
+			if (num_planes > 1)
+				CUDA_TRY(cudaMemsetAsync(d_vram + VRAM_SIZE + off, 0, size, stream));
+		}
 		CUDA_TRY(cudaStreamSynchronize(stream));
 		return PGS_OK;
 	}
@@ -2134,10 +2247,11 @@ static int c_vsync(void *self, const pgs_merge_params *m, void *dst)
 {
 	return m && dst ? B(self)->vsync(*m, dst) : PGS_ERROR_INVALID_ARGUMENT;
 }
+static int c_timestamps(void *self, int enable, double *totals) { return B(self)->timestamps(enable, totals); }
 
 const pgs_backend_ops CUDA_OPS = {
 	PGS_ABI_VERSION, c_destroy, c_reserve, c_flush_rendering, c_copy, c_palette, c_set_ss, c_submit, c_read, c_write, c_error,
-	c_read_async, c_wait, c_circuit, c_vsync,
+	c_read_async, c_wait, c_circuit, c_vsync, c_timestamps,
 };
 
 // ---------------------------------------------------------------------------

@@ -466,6 +466,14 @@ struct pgs_gs
 	// Vsyncs left with progressive read-out switched off after a tall
 	// SCANMSK primitive (gs/gs_interface.cpp:1947-1959, 4631-4637).
 	uint32_t complex_scanmsk_timeout = 0;
+	pgs_signal_interface signal_iface = {};
+	// Triangle-pair fusion (gs/gs_interface.cpp:2569-2602): the last committed
+	// triangle could be the first half of a rectangle, its vertex order, and
+	// the transfer count when it was drawn.
+	bool last_para_candidate = false;
+	uint32_t last_para_order[3] = { 0, 1, 2 };
+	uint64_t transfer_serial = 0, last_para_transfer = 0;
+	pgs_debug_mode debug_mode = {};
 	uint32_t clut_instance = 0;
 	uint32_t pending_palette_updates = 0;
 	int32_t ofx = 0, ofy = 0;
@@ -618,6 +626,7 @@ struct pgs_gs
 	void flush_render_pass(uint32_t reason)
 	{
 		fb_epoch++;
+		last_para_candidate = false;
 		if (primitive_count)
 		{
 			pgs_render_pass rp = {};
@@ -761,6 +770,7 @@ struct pgs_gs
 	// Transfers (gs/gs_interface.cpp:2979-3276).
 	void init_transfer()
 	{
+		transfer_serial++;
 		flush_pending_transfer(false);
 		xfer.bitbltbuf = regs[R_BITBLTBUF];
 		xfer.trxpos = regs[R_TRXPOS];
@@ -1080,7 +1090,14 @@ struct pgs_gs
 			hwreg(&v, 1);
 			break;
 		case R_SIGNAL: case R_FINISH: case R_LABEL:
+		{
+			// a_d_SIGNAL / FINISH / LABEL (gs/gs_interface.cpp:3970-3988).
+			pgs_signal_fn fn = addr == R_SIGNAL ? signal_iface.on_signal :
+			                   addr == R_FINISH ? signal_iface.on_finish : signal_iface.on_label;
+			if (fn && fn(signal_iface.user, v))
+				flush();
 			break;
+		}
 		default:
 			if (regs[addr] != v)
 			{
@@ -1612,6 +1629,7 @@ struct pgs_gs
 			hi[0] = std::max(hi[0], pos[2].x);
 			hi[1] = std::max(hi[1], pos[2].y);
 		}
+		const int32_t pre_lo[2] = { lo[0], lo[1] }, pre_hi[2] = { hi[0], hi[1] };
 		hi[0] -= 1;
 		hi[1] -= 1;
 		lo[0] += D.snap;
@@ -1633,6 +1651,28 @@ struct pgs_gs
 		                  std::min(hi[0], D.sci_hi[0]), std::min(hi[1], D.sci_hi[1]) };
 		if (bb[2] < bb[0] || bb[3] < bb[1])
 			return;
+
+		// A right triangle that completes the rectangle of the previous one,
+		// with no state change in between, turns that one into a
+		// parallelogram (gs/gs_interface.cpp:2569-2602).
+		bool para_candidate = false;
+		if (nv == 3 && !quad)
+		{
+			PrimReg prim(regs[R_PRIM]);
+			uint32_t order[3];
+			para_candidate = parallelogram_candidate(pos, attr, pre_lo, pre_hi, prim, order);
+			if (para_candidate && last_para_candidate && !template_dirty && primitive_count &&
+			    transfer_serial == last_para_transfer &&
+			    forms_parallelogram(pos, attr, order, positions + 3 * (primitive_count - 1),
+			                        attributes + 3 * (primitive_count - 1), last_para_order, prim))
+			{
+				prims[primitive_count - 1].state |= (1u << STATE_BIT_PARALLELOGRAM) |
+				                                    (last_para_order[0] << STATE_PARALLELOGRAM_PROVOKING_OFFSET);
+				last_para_candidate = false;
+				return;
+			}
+			memcpy(last_para_order, order, sizeof(order));
+		}
 
 		// Flush a pending partial upload before reading textures.
 		if (D.tme && xfer.active && xfer.payload.size() > xfer.flushed_qwords)
@@ -1778,6 +1818,99 @@ struct pgs_gs
 		memcpy(positions + 3 * n, pos, sizeof(pos));
 		memcpy(attributes + 3 * n, attr, sizeof(attr));
 		primitive_count++;
+		// Set after any flush above, which clears it.
+		last_para_candidate = para_candidate;
+		last_para_transfer = transfer_serial;
+	}
+
+	// triangle_is_parallelogram_candidate (gs/gs_util.cpp:237-305): flat
+	// attributes, a right angle at one vertex with axis-aligned legs (the
+	// triangle's area equals its box's).  order: the right-angle vertex, then
+	// the two diagonal ends, the left one first.
+	static bool parallelogram_candidate(const pgs_vertex_position *pos, const pgs_vertex_attribute *attr,
+	                                    const int32_t *lo, const int32_t *hi, const PrimReg &prim, uint32_t *order)
+	{
+		if (prim.enables_aa1())
+			return false;
+		if (!prim.fst && prim.tme && (attr[0].q != attr[1].q || attr[1].q != attr[2].q))
+			return false;
+		if (pos[0].z != pos[1].z || pos[1].z != pos[2].z)
+			return false;
+		if (prim.fge && (attr[0].fog != attr[1].fog || attr[1].fog != attr[2].fog))
+			return false;
+		if (attr[0].rgba != attr[1].rgba || attr[1].rgba != attr[2].rgba)
+			return false;
+		const int64_t abx = pos[1].x - pos[0].x, aby = pos[1].y - pos[0].y;
+		const int64_t acx = pos[2].x - pos[0].x, acy = pos[2].y - pos[0].y;
+		const int64_t bcx = pos[2].x - pos[1].x, bcy = pos[2].y - pos[1].y;
+		const int64_t cross = abx * acy - aby * acx;
+		if ((cross < 0 ? -cross : cross) != int64_t(hi[0] - lo[0]) * int64_t(hi[1] - lo[1]))
+			return false;
+		int64_t dot;
+		if (abx != 0 && aby != 0)
+		{
+			order[0] = 2; order[1] = 1; order[2] = 0;
+			dot = acx * bcx + acy * bcy;
+		}
+		else if (acx != 0 && acy != 0)
+		{
+			order[0] = 1; order[1] = 2; order[2] = 0;
+			dot = acx * abx + acy * aby;
+		}
+		else
+		{
+			order[0] = 0; order[1] = 1; order[2] = 2;
+			dot = acx * abx + acy * aby;
+		}
+		if (dot != 0)
+			return false;
+		if (pos[order[1]].x > pos[order[2]].x)
+			std::swap(order[1], order[2]);
+		return true;
+	}
+
+	// triangles_form_parallelogram (gs/gs_util.cpp:307-377): the fourth
+	// corner is the previous triangle's right-angle vertex, the diagonal is
+	// shared, and the attributes continue the previous triangle's.
+	static bool forms_parallelogram(const pgs_vertex_position *pos, const pgs_vertex_attribute *attr,
+	                                const uint32_t *order, const pgs_vertex_position *last_pos,
+	                                const pgs_vertex_attribute *last_attr, const uint32_t *last_order, const PrimReg &prim)
+	{
+		const pgs_vertex_position &p0 = pos[order[0]], &p1 = pos[order[1]], &p2 = pos[order[2]];
+		const pgs_vertex_position &l0 = last_pos[last_order[0]], &l1 = last_pos[last_order[1]],
+		                          &l2 = last_pos[last_order[2]];
+		if (p1.x + p2.x - p0.x != l0.x || p1.y + p2.y - p0.y != l0.y || p1.x != l1.x || p1.y != l1.y ||
+		    p2.x != l2.x || p2.y != l2.y)
+			return false;
+		if (pos[0].z != last_pos[0].z)
+			return false;
+		if (!prim.fst && prim.tme && attr[0].q != last_attr[0].q)
+			return false;
+		if (prim.fge && attr[0].fog != last_attr[0].fog)
+			return false;
+		if (attr[0].rgba != last_attr[0].rgba)
+			return false;
+		const pgs_vertex_attribute &a0 = attr[order[0]], &a1 = attr[order[1]], &a2 = attr[order[2]];
+		const pgs_vertex_attribute &b0 = last_attr[last_order[0]], &b1 = last_attr[last_order[1]],
+		                           &b2 = last_attr[last_order[2]];
+		if (prim.tme)
+		{
+			if (prim.fst)
+			{
+				const uint16_t u3 = uint16_t(a1.u + a2.u - a0.u), v3 = uint16_t(a1.v + a2.v - a0.v);
+				if (u3 != b0.u || v3 != b0.v || a1.u != b1.u || a1.v != b1.v || a2.u != b2.u || a2.v != b2.v)
+					return false;
+			}
+			else
+			{
+				// Within 1e-4 after the divide by Q: under a sub-texel at 1k x 1k.
+				const float es = std::fabs((((a2.s + a1.s) - a0.s) - b0.s) / a0.q);
+				const float et = std::fabs((((a2.t + a1.t) - a0.t) - b0.t) / a0.q);
+				if (a1.s != b1.s || a1.t != b1.t || a2.s != b2.s || a2.t != b2.t || es > 1e-4f || et > 1e-4f)
+					return false;
+			}
+		}
+		return true;
 	}
 
 	// ---------------------------------------------------------------
@@ -2591,6 +2724,108 @@ int pgs_gs_set_hacks(pgs_gs *gs, const pgs_hacks *hacks)
 	gs->reg_serial++;
 	gs->template_dirty = true;
 	return gs->sticky_error;
+}
+
+int pgs_gs_reset_context_state(pgs_gs *gs)
+{
+	if (!gs)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->flush();
+	memset(gs->regs, 0, sizeof(gs->regs));
+	gs->regs[R_PRMODECONT] = 1;
+	for (auto &p : gs->paths)
+		p = pgs_gs::Path();
+	gs->internal_q = 1.0f;
+	gs->clobber_state();
+	return gs->sticky_error;
+}
+
+int pgs_gs_clobber_register_state(pgs_gs *gs)
+{
+	if (!gs)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->clobber_state();
+	return PGS_OK;
+}
+
+int pgs_gs_read_register(const pgs_gs *gs, uint32_t addr, uint64_t *value)
+{
+	if (!gs || !value || addr >= 128)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	*value = gs->regs[addr];
+	return PGS_OK;
+}
+
+int pgs_gs_set_register(pgs_gs *gs, uint32_t addr, uint64_t value)
+{
+	if (!gs || addr >= 128)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->regs[addr] = value;
+	return PGS_OK;
+}
+
+int pgs_gs_get_gif_path(const pgs_gs *gs, uint32_t path, pgs_gif_path *out)
+{
+	if (!gs || !out || path >= 4)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	const auto &p = gs->paths[path];
+	out->tag[0] = p.tag_lo;
+	out->tag[1] = p.tag_hi;
+	out->reg = p.reg;
+	out->loop = p.loop;
+	return PGS_OK;
+}
+
+int pgs_gs_set_gif_path(pgs_gs *gs, uint32_t path, const pgs_gif_path *in)
+{
+	if (!gs || !in || path >= 4)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	pgs_gs::Path p;
+	p.tag_lo = in->tag[0];
+	p.tag_hi = in->tag[1];
+	p.nloop = field(p.tag_lo, 0, 15);
+	p.flg = field(p.tag_lo, 58, 2);
+	p.nreg = field(p.tag_lo, 60, 4);
+	if (p.nreg == 0)
+		p.nreg = 16;
+	if (in->loop > p.nloop || in->reg >= p.nreg)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	p.reg = in->reg;
+	p.loop = in->loop;
+	gs->paths[path] = p;
+	return PGS_OK;
+}
+
+int pgs_gs_set_signal_interface(pgs_gs *gs, const pgs_signal_interface *iface)
+{
+	if (!gs)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->signal_iface = iface ? *iface : pgs_signal_interface{};
+	return PGS_OK;
+}
+
+int pgs_gs_set_debug_mode(pgs_gs *gs, const pgs_debug_mode *mode)
+{
+	if (!gs || !mode || mode->draw_mode > 2)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	gs->debug_mode = *mode;
+	if (gs->ops->abi_version >= 4 && gs->ops->timestamps)
+		return gs->ops->timestamps(gs->be, mode->timestamps ? 1 : 0, nullptr);
+	return PGS_OK;
+}
+
+int pgs_gs_get_accumulated_timestamps(pgs_gs *gs, uint32_t type, double *seconds)
+{
+	if (!gs || !seconds || type >= PGS_TIMESTAMP_COUNT)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	*seconds = 0.0;
+	if (gs->ops->abi_version < 4 || !gs->ops->timestamps)
+		return PGS_OK;
+	double totals[PGS_TIMESTAMP_COUNT] = {};
+	int r = gs->ops->timestamps(gs->be, -1, totals);
+	if (r == PGS_OK)
+		*seconds = totals[type];
+	return r;
 }
 }
 

@@ -1100,6 +1100,80 @@ def frame_field_aware(seed: int) -> Frame:
     return f
 
 
+def frame_quads(seed: int) -> Frame:
+    """Rectangles drawn as triangle pairs (the frontend fuses them into
+    parallelograms): flat colour, FST UV and perspective STQ textures, both
+    diagonals, every vertex order, triangle lists and strips, super-sampled for
+    odd seeds; some pairs broken by a register change, a Z or colour
+    difference or a non-rectangular second triangle."""
+    rng = np.random.Generator(np.random.PCG64(92000 + seed))
+    s = GifStream()
+    ss = 1 if seed % 2 == 0 else [2, 4, 8, 16][(seed // 2) % 4]
+    width, height, zbp = 320, 224, 60
+    _frame_setup(s, 0, width // 64, PSMCT32, zbp, PSMZ24, width, height, test_reg(zte=1, ztst=1))
+    s.upload(200 * BLOCKS_PER_PAGE, 1, PSMCT32, 0, 0, 64, 64, rng.integers(0, 256, size=64 * 64 * 4,
+                                                                                  dtype=np.uint8).tobytes())
+    s.ad([(TEX0_1, tex0_reg(200 * BLOCKS_PER_PAGE, 1, PSMCT32, 6, 6, tcc=1, tfx=1)),
+          (TEX1_1, tex1_reg(mmag=int(seed % 3 == 0), mmin=int(seed % 3 == 0))), (CLAMP_1, clamp_reg(0, 0))])
+    for k in range(int(rng.integers(60, 140))):
+        w, h = int(rng.integers(1, 80)), int(rng.integers(1, 60))
+        x0, y0 = int(rng.integers(0, width - w)), int(rng.integers(0, height - h))
+        sub = rng.integers(0, 16, size=2) if rng.uniform() < 0.3 else np.zeros(2, dtype=np.int64)
+        X = [x0 * 16 + int(sub[0]), (x0 + w) * 16 + int(sub[0])]
+        Y = [y0 * 16 + int(sub[1]), (y0 + h) * 16 + int(sub[1])]
+        corners = [(X[0], Y[0]), (X[1], Y[0]), (X[1], Y[1]), (X[0], Y[1])]
+        u0, v0 = int(rng.integers(0, 32)) * 16, int(rng.integers(0, 32)) * 16
+        du, dv = int(rng.integers(1, 40)) * 16, int(rng.integers(1, 40)) * 16
+        uvs = [(u0, v0), (u0 + du, v0), (u0 + du, v0 + dv), (u0, v0 + dv)]
+        diag = int(rng.integers(0, 2))
+        tri = [[0, 1, 2], [0, 2, 3]] if diag == 0 else [[0, 1, 3], [1, 2, 3]]
+        tri = [[t[i] for i in rng.permutation(3)] for t in tri]
+        z = int(rng.integers(0, 1 << 24))
+        col = [int(c) for c in rng.integers(0, 256, size=4)]
+        break_kind = int(rng.integers(0, 8))
+        kind = int(rng.integers(0, 3))   # 0 flat, 1 FST UV, 2 STQ
+        strip = break_kind == 7 and kind != 2
+        verts = []
+        for t_i, t in enumerate(tri):
+            for c in t:
+                zz = z + (1 if break_kind == 1 and t_i == 1 else 0)
+                cc = list(col)
+                if break_kind == 2 and t_i == 1:
+                    cc[0] ^= 1
+                x, y = corners[c]
+                if break_kind == 3 and t_i == 1 and c == t[0]:
+                    x += 16
+                verts.append((x, y, zz, cc, uvs[c]))
+        if strip:
+            # Strip order: a, b, c then d completing the rectangle.
+            a, b, c, d = [0, 1, 3, 2] if diag == 0 else [1, 2, 0, 3]
+            verts = [(corners[i][0], corners[i][1], z, col, uvs[i]) for i in (a, b, c, d)]
+        n = len(verts)
+        q = np.zeros((n, 3, 2), dtype=np.uint64)
+        q[:, 0] = q_rgbaq(np.array([v[3] for v in verts]))
+        if kind == 2:
+            qq = np.full(n, float(rng.uniform(0.5, 2.0)), dtype=np.float32)
+            q[:, 1] = q_st(np.array([v[4][0] / 16.0 / 64 for v in verts], dtype=np.float32) * qq,
+                           np.array([v[4][1] / 16.0 / 64 for v in verts], dtype=np.float32) * qq, qq)
+            desc = [D_RGBAQ, D_ST, D_XYZ2]
+        else:
+            q[:, 1] = q_uv(np.array([v[4][0] for v in verts]), np.array([v[4][1] for v in verts]))
+            desc = [D_RGBAQ, D_UV, D_XYZ2]
+        q[:, 2] = q_xyz2(np.array([v[0] for v in verts]), np.array([v[1] for v in verts]),
+                         np.array([v[2] for v in verts]))
+        prim = PRIM_TRISTRIP if strip else PRIM_TRI
+        if break_kind == 4:
+            # A state change between the halves keeps them apart.
+            s.packed(prim_reg(prim, tme=int(kind > 0), fst=int(kind == 1)), desc, q[:3].reshape(-1, 2))
+            s.ad([(FOGCOL, int(rng.integers(0, 1 << 24)))])
+            s.packed(prim_reg(prim, tme=int(kind > 0), fst=int(kind == 1)), desc, q[3:].reshape(-1, 2))
+        else:
+            s.packed(prim_reg(prim, tme=int(kind > 0), fst=int(kind == 1), abe=int(k % 5 == 0)), desc,
+                     q.reshape(-1, 2))
+    return Frame("quads_%d" % seed, s.tobytes(), ss, True, 0,
+                 {"width": width, "height": height, "fbp": 0, "zbp": zbp})
+
+
 def frame_blend_demote(seed: int) -> Frame:
     """Blend demotion hack: many overlapping blended triangles and sprites
     (well over 32 per coarse tile), super-sampled, depth written only in the

@@ -93,6 +93,9 @@ EXPORTED_SYMBOLS = [
     "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait",
     "pgs_gs_write_priv_register", "pgs_gs_read_priv_register", "pgs_gs_scanout_circuit", "pgs_gs_vsync",
     "pgs_gs_set_super_sampled_textures", "pgs_gs_vsync_can_skip", "pgs_gs_set_hacks",
+    "pgs_gs_reset_context_state", "pgs_gs_clobber_register_state", "pgs_gs_read_register", "pgs_gs_set_register",
+    "pgs_gs_get_gif_path", "pgs_gs_set_gif_path", "pgs_gs_set_signal_interface", "pgs_gs_set_debug_mode",
+    "pgs_gs_get_accumulated_timestamps",
     "pgs_gs_dump_open", "pgs_gs_dump_next_vsync", "pgs_gs_dump_close", "pgs_gs_dump_record_begin",
     "pgs_gs_dump_record_vsync", "pgs_gs_dump_record_end", "pgs_gs_write_vram", "pgs_gs_read_transfer_fifo", "pgs_gs_consume_flush_stats",
     "pgs_gs_set_super_sampling_rate",
@@ -166,6 +169,15 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.pgs_gs_set_super_sampled_textures.argtypes = [vp, i32]
     lib.pgs_gs_vsync_can_skip.argtypes = [vp, C.POINTER(VsyncInfo)]
     lib.pgs_gs_set_hacks.argtypes = [vp, C.POINTER(Hacks)]
+    lib.pgs_gs_reset_context_state.argtypes = [vp]
+    lib.pgs_gs_clobber_register_state.argtypes = [vp]
+    lib.pgs_gs_read_register.argtypes = [vp, u32, C.POINTER(u64)]
+    lib.pgs_gs_set_register.argtypes = [vp, u32, u64]
+    lib.pgs_gs_get_gif_path.argtypes = [vp, u32, C.POINTER(GifPath)]
+    lib.pgs_gs_set_gif_path.argtypes = [vp, u32, C.POINTER(GifPath)]
+    lib.pgs_gs_set_signal_interface.argtypes = [vp, C.POINTER(SignalInterface)]
+    lib.pgs_gs_set_debug_mode.argtypes = [vp, C.POINTER(DebugMode)]
+    lib.pgs_gs_get_accumulated_timestamps.argtypes = [vp, u32, C.POINTER(C.c_double)]
     if path is None:
         _lib = lib
     return lib
@@ -188,6 +200,29 @@ class BackendOps(C.Structure):
 
 class VsyncInfo(C.Structure):
     _fields_ = [("phase", C.c_uint32), ("flags", C.c_uint32)]
+
+
+SIGNAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64)
+
+
+class GifPath(C.Structure):
+    """pgs_gif_path (GIFPath, gs/gs_interface.hpp:63-68)."""
+    _fields_ = [("tag", C.c_uint64 * 2), ("reg", C.c_uint32), ("loop", C.c_uint32)]
+
+
+class SignalInterface(C.Structure):
+    """pgs_signal_interface (SignalInterface, gs/gs_interface.hpp:238-248)."""
+    _fields_ = [("on_signal", SIGNAL_FN), ("on_finish", SIGNAL_FN), ("on_label", SIGNAL_FN), ("user", C.c_void_p)]
+
+
+class DebugMode(C.Structure):
+    """pgs_debug_mode (DebugMode, gs/gs_interface.hpp:137-153)."""
+    _fields_ = [(n, C.c_uint32) for n in ("feedback_render_target", "timestamps", "deterministic_timeline_query",
+                                          "disable_sampler_feedback", "draw_mode")]
+
+
+TIMESTAMPS = ["SyncHostToVRAM", "CopyVRAM", "PaletteUpdate", "TextureUpload", "TriangleSetup", "Binning", "Shading",
+              "Readback", "VSync"]
 
 
 class Hacks(C.Structure):
@@ -399,6 +434,50 @@ class GSInterface:
         """GSInterface::set_hacks; backbuffer_promotion is not supported (PGSError)."""
         h = Hacks(int(disable_mipmaps), int(unsynced_readbacks), int(backbuffer_promotion), int(allow_blend_demote))
         check(self.lib.pgs_gs_set_hacks(self.handle, C.byref(h)), "set_hacks")
+
+    def reset_context_state(self) -> None:
+        check(self.lib.pgs_gs_reset_context_state(self.handle), "reset_context_state")
+
+    def clobber_register_state(self) -> None:
+        check(self.lib.pgs_gs_clobber_register_state(self.handle), "clobber_register_state")
+
+    def read_register(self, addr: int) -> int:
+        v = C.c_uint64()
+        check(self.lib.pgs_gs_read_register(self.handle, addr, C.byref(v)), "read_register")
+        return v.value
+
+    def set_register(self, addr: int, value: int) -> None:
+        check(self.lib.pgs_gs_set_register(self.handle, addr, value), "set_register")
+
+    def get_gif_path(self, path: int) -> dict:
+        p = GifPath()
+        check(self.lib.pgs_gs_get_gif_path(self.handle, path, C.byref(p)), "get_gif_path")
+        return {"tag": (p.tag[0], p.tag[1]), "reg": p.reg, "loop": p.loop}
+
+    def set_gif_path(self, path: int, tag, reg: int = 0, loop: int = 0) -> None:
+        p = GifPath((C.c_uint64 * 2)(*tag), reg, loop)
+        check(self.lib.pgs_gs_set_gif_path(self.handle, path, C.byref(p)), "set_gif_path")
+
+    def set_signal_interface(self, on_signal=None, on_finish=None, on_label=None) -> None:
+        """Python callables taking the register value; a true result flushes."""
+        def wrap(fn):
+            return SIGNAL_FN(lambda user, payload: int(bool(fn(payload)))) if fn else SIGNAL_FN()
+        self._signal = SignalInterface(wrap(on_signal), wrap(on_finish), wrap(on_label), None)
+        check(self.lib.pgs_gs_set_signal_interface(self.handle, C.byref(self._signal)), "set_signal_interface")
+
+    def set_debug_mode(self, timestamps: bool = False, feedback_render_target: bool = False,
+                       deterministic_timeline_query: bool = False, disable_sampler_feedback: bool = False,
+                       draw_mode: int = 0) -> None:
+        m = DebugMode(int(feedback_render_target), int(timestamps), int(deterministic_timeline_query),
+                      int(disable_sampler_feedback), draw_mode)
+        check(self.lib.pgs_gs_set_debug_mode(self.handle, C.byref(m)), "set_debug_mode")
+
+    def get_accumulated_timestamps(self, kind) -> float:
+        """Seconds of GPU time in a stage (index or name from TIMESTAMPS)."""
+        t = TIMESTAMPS.index(kind) if isinstance(kind, str) else int(kind)
+        v = C.c_double()
+        check(self.lib.pgs_gs_get_accumulated_timestamps(self.handle, t, C.byref(v)), "get_accumulated_timestamps")
+        return v.value
 
     def write_vram(self, data, offset: int = 0) -> None:
         buf = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, bytes) else data)

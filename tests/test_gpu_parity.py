@@ -305,3 +305,12 @@ def test_disable_mipmaps_parity(seed):
     f.meta["hacks"] = {"disable_mipmaps": True}
     ref, out = run_both(f)
     assert_same(ref, out)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_fused_rectangles_parity(seed):
+    """Triangle pairs fused into parallelograms (provoking vertex 0 and 2),
+    flat, FST and STQ textured, lists and strips, 1x and super-sampled, with
+    pairs the fusion must leave apart."""
+    ref, out = run_both(gsgen.frame_quads(seed))
+    assert_same(ref, out)
