@@ -1197,7 +1197,7 @@ struct Backend
 	// the phase LUT's taps around the texel below the sampling position with
 	// unorm8 weights (one tap for nearest filtering or on a clamped region
 	// edge); coordinates snap as for plain textures, taps wrap like them.
-	void sample_layered(const PassCtx &P, const pgs_texture_desc &t, uint32_t tex_word, float u, float v,
+	void sample_layered(const PassCtx &, const pgs_texture_desc &t, uint32_t tex_word, float u, float v,
 	                    bool perspective, uint32_t sample, uint32_t rx, uint32_t ry, uint32_t rgba[4])
 	{
 		const bool clamp_s = tex_word & (1u << 19), clamp_t = tex_word & (1u << 20);
@@ -3201,7 +3201,7 @@ static int o_vsync(void *self, const pgs_merge_params *mp, void *dst)
 
 static const pgs_backend_ops ORACLE_OPS = {
 	PGS_ABI_VERSION, o_destroy, o_reserve, o_flush_rendering, o_copy, o_palette, o_set_ss, o_submit, o_read, o_write, o_error,
-	nullptr, nullptr, o_circuit, o_vsync,
+	nullptr, nullptr, o_circuit, o_vsync, nullptr,
 };
 
 extern "C" {
