@@ -314,3 +314,19 @@ def test_fused_rectangles_parity(seed):
     pairs the fusion must leave apart."""
     ref, out = run_both(gsgen.frame_quads(seed))
     assert_same(ref, out)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_combined_stream_with_fusion_and_hacks(seed):
+    """Fused rectangles, a mipmapped frame, the super-sampled-texture frame and
+    the blend-demotion frame in one stream at one rate, with blend demotion on
+    and field-aware rendering chosen by a vsync first."""
+    parts = [gsgen.frame_ssaa_textures(seed), gsgen.frame_quads(seed), gsgen.frame_mip(seed),
+             gsgen.frame_blend_demote(seed)]
+    meta = dict(parts[0].meta)
+    meta["field_aware"] = seed % 2 == 0
+    meta["hacks"] = {"allow_blend_demote": True}
+    f = gsgen.Frame("combined2_%d" % seed, b"".join(p.data for p in parts), parts[0].super_sampling,
+                    parts[0].ordered, 0, meta)
+    ref, out = run_both(f)
+    assert_same(ref, out)
