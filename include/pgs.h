@@ -506,6 +506,11 @@ typedef struct pgs_gs_options
 	uint32_t super_sampling;      /* 1, 2, 4, 8 or 16 (SuperSampling enum) */
 	uint32_t ordered_super_sampling;
 	uint32_t vram_size;           /* must be PGS_VRAM_SIZE */
+	/* GSOptions::dynamic_super_sampling: accepted; the rate can always change
+	 * in flight up to the sample planes the backend was created with. */
+	uint32_t dynamic_super_sampling;
+	/* GSOptions::super_sampled_textures (pgs_gs_set_super_sampled_textures). */
+	uint32_t super_sampled_textures;
 } pgs_gs_options;
 
 /* GSInterface::init.  The frontend does not own the backend. */

@@ -2108,6 +2108,7 @@ pgs_gs *pgs_gs_create(const pgs_backend_ops *ops, void *backend, const pgs_gs_op
 	gs->instances[0].frame = 0x3full << 24;
 	gs->instances[0].zbuf = 0x7ull << 24;
 	gs->set_super_sampling(options ? options->super_sampling : 1, options ? options->ordered_super_sampling != 0 : true);
+	gs->ssaa_textures = options && options->super_sampled_textures != 0;
 	gs->reserve_buffers();
 	*status = gs->sticky_error;
 	if (gs->sticky_error)

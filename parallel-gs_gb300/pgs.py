@@ -53,7 +53,8 @@ class FlushStats(C.Structure):
 
 
 class GSOptions(C.Structure):
-    _fields_ = [("super_sampling", C.c_uint32), ("ordered_super_sampling", C.c_uint32), ("vram_size", C.c_uint32)]
+    _fields_ = [("super_sampling", C.c_uint32), ("ordered_super_sampling", C.c_uint32), ("vram_size", C.c_uint32),
+                ("dynamic_super_sampling", C.c_uint32), ("super_sampled_textures", C.c_uint32)]
 
 
 class CudaBackendOptions(C.Structure):
@@ -321,10 +322,12 @@ class CudaBackend(Backend):
 class GSInterface:
     """GSInterface (gs/gs_interface.hpp:251-304) over any backend."""
 
-    def __init__(self, backend: Backend, super_sampling: int = 1, ordered: bool = True, lib: C.CDLL | None = None):
+    def __init__(self, backend: Backend, super_sampling: int = 1, ordered: bool = True, lib: C.CDLL | None = None,
+                 super_sampled_textures: bool = False, dynamic_super_sampling: bool = False):
         self.lib = lib or load_library()
         self.backend = backend
-        opts = GSOptions(super_sampling, int(ordered), VRAM_SIZE)
+        opts = GSOptions(super_sampling, int(ordered), VRAM_SIZE, int(dynamic_super_sampling),
+                         int(super_sampled_textures))
         status = C.c_int(0)
         self.handle = self.lib.pgs_gs_create(C.c_void_p(backend.ops), C.c_void_p(backend.handle), C.byref(opts),
                                              C.byref(status))

@@ -44,6 +44,15 @@ def planes_at(img, fbp, psm=g.PSMCT32, stride=2):
     return np.stack([p.view(np.uint32)[idx] for p in img])
 
 
+def test_create_option_turns_super_sampled_textures_on():
+    be = RecordingBackend()
+    gs = pgs.GSInterface(be, super_sampling=4, super_sampled_textures=True)
+    gs.gif_transfer(0, scene(True).data)
+    gs.flush()
+    assert be.passes[-1]["has_ss_textures"] == 1
+    gs.close()
+
+
 def test_descriptor_and_texture_word():
     be = RecordingBackend()
     gs = pgs.GSInterface(be, super_sampling=4)
