@@ -488,9 +488,11 @@ int pgs_upscaler_synchronize(void *upscaler);
  * The source rectangle is staged in a fixed device array of
  * PGS_NOALLOC_COPY_MAX_PIXELS 32-bit entries (1 MiB) that every GPU loading the
  * library holds until exit; larger rectangles are rejected with
- * PGS_ERROR_CAPACITY.  The first call on a device looks up that array's device
- * address (cudaGetSymbolAddress) with the device current; make that first call
- * before any stream capture.  All calls share the array, so calls whose work
+ * PGS_ERROR_CAPACITY.  The first call in a CUDA context looks up that array's
+ * device address (cudaGetSymbolAddress) with the context current and keeps it
+ * for that context; make that first call before any stream capture.  A context
+ * that is destroyed and created again (cudaDeviceReset) counts as a new one, so
+ * the lookup runs again there.  All calls share the array, so calls whose work
  * overlaps on the GPU race; serialise them on one stream.  Nothing in the array
  * needs to start at zero: each call overwrites the entries it reads. */
 #define PGS_NOALLOC_COPY_MAX_PIXELS (256u * 1024u)
@@ -503,13 +505,22 @@ typedef struct pgs_gs pgs_gs;
 
 typedef struct pgs_gs_options
 {
-	uint32_t super_sampling;      /* 1, 2, 4, 8 or 16 (SuperSampling enum) */
+	/* sizeof(pgs_gs_options) as the caller was built; fields past it read as
+	 * zero, so a caller built against a shorter layout keeps working.  0 means
+	 * the whole current layout. */
+	uint32_t struct_size;
+	/* 1, 2, 4, 8 or 16 (SuperSampling enum).  Lowered to the most the backend
+	 * was created for, as set_super_sampling_rate does with
+	 * get_max_supported_super_sampling (gs/gs_interface.cpp:69-70). */
+	uint32_t super_sampling;
 	uint32_t ordered_super_sampling;
 	uint32_t vram_size;           /* must be PGS_VRAM_SIZE */
-	/* GSOptions::dynamic_super_sampling: accepted; the rate can always change
-	 * in flight up to the sample planes the backend was created with. */
+	/* GSOptions::dynamic_super_sampling: accepted and not needed -- the rate
+	 * can always change in flight, limited to the sample planes the backend
+	 * was created with (pgs_cuda_backend_options.max_samples_log2). */
 	uint32_t dynamic_super_sampling;
-	/* GSOptions::super_sampled_textures (pgs_gs_set_super_sampled_textures). */
+	/* GSOptions::super_sampled_textures (pgs_gs_set_super_sampled_textures);
+	 * off when the resulting rate is 1x. */
 	uint32_t super_sampled_textures;
 } pgs_gs_options;
 

@@ -1,10 +1,7 @@
 """Build the in-tree native libraries.
 
 libpgs_gb300.so   frontend (GSInterface re-host) + CUDA backend, sm_103a only.
-liboracle.so      CPU restatement of the backend, used only by tests and the
-                  CPU baseline.
-libpgsref.so      the reference's own CPU swizzle path compiled from its
-                  sources (only where those sources are present).
+                  The test-only oracle has its own recipe (oracle/build_oracle.py).
 
 Run ``python parallel-gs_gb300/build.py`` or call ``build_all()``.  Objects
 are compiled in parallel; nothing uses cmake.
@@ -23,10 +20,6 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 INCLUDE = ROOT / "include"
-ORACLE = ROOT / "oracle"
-ORACLE_BUILD = ORACLE / "_build"
-REF_BUILD = ORACLE / "_ref"
-REFERENCE_SRC = Path(os.environ.get("PGS_REFERENCE_DIR", "/root/reference"))
 
 GENCODE = "arch=compute_103a,code=sm_103a"
 LIB_NAME = "libpgs_gb300.so"
@@ -87,36 +80,8 @@ def build_product(verbose: bool = False) -> Path:
     return out
 
 
-def build_oracle() -> Path:
-    ORACLE_BUILD.mkdir(parents=True, exist_ok=True)
-    src = ORACLE / "oracle_backend.cpp"
-    out = ORACLE_BUILD / "liboracle.so"
-    if not _newer(out, [src, INCLUDE / "pgs.h", Path(__file__)]):
-        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp",
-              "-I", str(INCLUDE), str(src), "-o", str(out)])
-    return out
-
-
-def build_reference_harness() -> Path | None:
-    """Compile the reference's vram_upload/vram_readback where its sources exist."""
-    gs = REFERENCE_SRC / "gs"
-    if not (gs / "gs_util.hpp").exists():
-        return None
-    REF_BUILD.mkdir(parents=True, exist_ok=True)
-    out = REF_BUILD / "libpgsref.so"
-    src = ORACLE / "ref_harness.cpp"
-    if not _newer(out, [src, Path(__file__)]):
-        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", str(ORACLE / "ref_shim"),
-              "-I", str(gs), "-I", str(gs / "shaders"), str(src), "-o", str(out)])
-    return out
-
-
 def build_all(verbose: bool = False) -> dict:
-    with ThreadPoolExecutor(max_workers=3) as ex:
-        f_prod = ex.submit(build_product, verbose)
-        f_orc = ex.submit(build_oracle)
-        f_ref = ex.submit(build_reference_harness)
-        return {"product": f_prod.result(), "oracle": f_orc.result(), "reference": f_ref.result()}
+    return {"product": build_product(verbose)}
 
 
 if __name__ == "__main__":

@@ -2259,9 +2259,19 @@ const pgs_backend_ops CUDA_OPS = {
 // array; host code only ever uses the address cudaGetSymbolAddress returns.
 static __device__ __align__(256) uint32_t g_noalloc_copy_scratch[PGS_NOALLOC_COPY_MAX_PIXELS];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
+// Set-up cache: the array's device address per CUDA context.  A context that
+// is destroyed and created again (cudaDeviceReset, or a host framework that
+// resets the device) loads the module again and the array can move, so the
+// key is the context's process-unique ID (cuCtxGetId), not the device number.
+constexpr int NOALLOC_MAX_CONTEXTS = 64;
 std::mutex g_noalloc_mutex;
-uint32_t *g_noalloc_scratch_ptr[NOALLOC_MAX_DEVICES] = {};
+struct NoallocSlot
+{
+	unsigned long long ctx_id;
+	uint32_t *ptr;
+};
+NoallocSlot g_noalloc_slots[NOALLOC_MAX_CONTEXTS] = {};
+int g_noalloc_num_slots = 0;
 
 // Pass 1: read every source pixel of the rectangle into the staging array.
 __global__ void __launch_bounds__(256) noalloc_gather_kernel(CopyParams C, const uint8_t *vram, uint32_t *staging)
@@ -2296,26 +2306,62 @@ __global__ void __launch_bounds__(256) noalloc_scatter_kernel(CopyParams C, uint
 	            C.invalidate_ss != 0);
 }
 
-// Per-device set-up: the device address of the staging array, looked up once
-// with the device current.
+// Set-up, once per CUDA context: the device address of the staging array,
+// looked up with that context current.  cuCtxGetCurrent / cuCtxGetId come
+// through the runtime's driver entry points (no link against libcuda).
 int noalloc_scratch(uint32_t **out)
 {
+	using CtxGetCurrent = int (*)(void **);
+	using CtxGetId = int (*)(void *, unsigned long long *);
+	static CtxGetCurrent get_current = nullptr;
+	static CtxGetId get_id = nullptr;
 	int dev = 0;
-	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+	if (cudaGetDevice(&dev) != cudaSuccess)
 		return PGS_ERROR_NO_DEVICE;
 	std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-	if (!g_noalloc_scratch_ptr[dev])
+	if (!get_current || !get_id)
 	{
-		void *p = nullptr;
-		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_copy_scratch);
-		if (e != cudaSuccess || !p)
+		void *f0 = nullptr, *f1 = nullptr;
+		cudaDriverEntryPointQueryResult q0, q1;
+		if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) != cudaSuccess ||
+		    q0 != cudaDriverEntryPointSuccess || !f0 ||
+		    cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+		    q1 != cudaDriverEntryPointSuccess || !f1)
 		{
-			fprintf(stderr, "pgs: cudaGetSymbolAddress(g_noalloc_copy_scratch) failed: %s\n", cudaGetErrorString(e));
+			fprintf(stderr, "pgs: cuCtxGetCurrent / cuCtxGetId entry points unavailable\n");
 			return PGS_ERROR_CUDA;
 		}
-		g_noalloc_scratch_ptr[dev] = static_cast<uint32_t *>(p);
+		get_current = reinterpret_cast<CtxGetCurrent>(f0);
+		get_id = reinterpret_cast<CtxGetId>(f1);
 	}
-	*out = g_noalloc_scratch_ptr[dev];
+	void *ctx = nullptr;
+	unsigned long long id = 0;
+	if (get_current(&ctx) != 0)
+		return PGS_ERROR_NO_DEVICE;
+	// No context current on this thread yet: cudaSetDevice binds (and, from
+	// CUDA 12 on, initialises) the device's primary context.
+	if (!ctx && (cudaSetDevice(dev) != cudaSuccess || get_current(&ctx) != 0))
+		return PGS_ERROR_NO_DEVICE;
+	if (!ctx || get_id(ctx, &id) != 0)
+		return PGS_ERROR_NO_DEVICE;
+	for (int i = 0; i < g_noalloc_num_slots; i++)
+		if (g_noalloc_slots[i].ctx_id == id)
+		{
+			*out = g_noalloc_slots[i].ptr;
+			return PGS_OK;
+		}
+	void *p = nullptr;
+	cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_copy_scratch);
+	if (e != cudaSuccess || !p)
+	{
+		fprintf(stderr, "pgs: cudaGetSymbolAddress(g_noalloc_copy_scratch) failed: %s\n", cudaGetErrorString(e));
+		return PGS_ERROR_CUDA;
+	}
+	// Contexts that no longer exist keep their slots; past the table's size
+	// the oldest slot is reused.
+	int slot = g_noalloc_num_slots < NOALLOC_MAX_CONTEXTS ? g_noalloc_num_slots++ : int(id % NOALLOC_MAX_CONTEXTS);
+	g_noalloc_slots[slot] = { id, static_cast<uint32_t *>(p) };
+	*out = g_noalloc_slots[slot].ptr;
 	return PGS_OK;
 }
 } // namespace

@@ -8,17 +8,19 @@
 // (gs/gs_interface.cpp:2473-2836); state words follow drawing_kick_update_state
 // (:1804-1968) and drawing_kick_update_state_vector (:1065-1128).
 //
-// Differences from the reference, all result-neutral for sequential GS
-// semantics: no parallelogram fusion of triangle pairs (gs/gs_util.cpp:237-377),
-// no palette memoization (:689-799), no feedback-texture modes (:2140-2330) and
-// a page-granular hazard tracker.  Because the backend samples textures straight
-// from VRAM instead of from snapshot images, the tracker also ends a render pass
-// when a transfer or a framebuffer write would touch pages an earlier primitive
-// of the same pass samples.
+// Triangle pairs that tile a rectangle are fused into parallelograms as
+// gs/gs_util.cpp:237-377 decides.  Differences from the reference, all
+// result-neutral for sequential GS semantics: no palette memoization
+// (:689-799), no feedback-texture modes (:2140-2330) and a page-granular hazard
+// tracker.  Because the backend samples textures straight from VRAM instead of
+// from snapshot images, the tracker also ends a render pass when a transfer or
+// a framebuffer write would touch pages an earlier primitive of the same pass
+// samples.
 #include "pgs.h"
 #include "gs_defs.h"
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -599,24 +601,45 @@ struct pgs_gs
 			sticky_error = r;
 	}
 
-	void set_super_sampling(uint32_t ss, bool ordered)
+	static void rates_for(uint32_t ss, bool ordered, uint32_t &x, uint32_t &y)
 	{
 		switch (ss)
 		{
-		case 2: sampling_rate_x_log2 = 0; sampling_rate_y_log2 = 1; break;
+		case 2: x = 0; y = 1; break;
 		case 4:
-			if (ordered) { sampling_rate_x_log2 = 1; sampling_rate_y_log2 = 1; }
-			else { sampling_rate_x_log2 = 0; sampling_rate_y_log2 = 2; }
+			if (ordered) { x = 1; y = 1; }
+			else { x = 0; y = 2; }
 			break;
-		case 8: sampling_rate_x_log2 = 1; sampling_rate_y_log2 = 2; break;
+		case 8: x = 1; y = 2; break;
 		case 16:
-			if (ordered) { sampling_rate_x_log2 = 2; sampling_rate_y_log2 = 2; }
-			else { sampling_rate_x_log2 = 1; sampling_rate_y_log2 = 3; }
+			if (ordered) { x = 2; y = 2; }
+			else { x = 1; y = 3; }
 			break;
-		default: sampling_rate_x_log2 = 0; sampling_rate_y_log2 = 0; break;
+		default: x = 0; y = 0; break;
 		}
+	}
+
+	// GSInterface::set_super_sampling_rate (gs/gs_interface.cpp:64-117): the
+	// rate is lowered to the most the backend supports (the reference takes
+	// min(requested, get_max_supported_super_sampling())); this backend table
+	// has no such query, so the rate steps down by halves until the backend
+	// accepts it.  At 1x super-sampled textures are off.
+	void set_super_sampling(uint32_t ss, bool ordered, bool ss_textures)
+	{
+		if (ss != 2 && ss != 4 && ss != 8 && ss != 16)
+			ss = 1;
+		int r = 0;
+		for (;;)
+		{
+			rates_for(ss, ordered, sampling_rate_x_log2, sampling_rate_y_log2);
+			r = ops->set_super_sampling(be, sampling_rate_x_log2, sampling_rate_y_log2);
+			if (r != PGS_ERROR_UNSUPPORTED || ss == 1)
+				break;
+			ss >>= 1;
+		}
+		ssaa_textures = ss_textures && ss > 1;
 		reg_serial++;
-		int r = ops->set_super_sampling(be, sampling_rate_x_log2, sampling_rate_y_log2);
+		template_dirty = true;
 		if (r != 0)
 			sticky_error = r;
 	}
@@ -2090,6 +2113,11 @@ pgs_gs *pgs_gs_create(const pgs_backend_ops *ops, void *backend, const pgs_gs_op
 		*status = PGS_ERROR_INVALID_ARGUMENT;
 		return nullptr;
 	}
+	if (options && options->struct_size && options->struct_size < offsetof(pgs_gs_options, vram_size) + 4)
+	{
+		*status = PGS_ERROR_INVALID_ARGUMENT;
+		return nullptr;
+	}
 	if (options && options->vram_size && options->vram_size != PGS_VRAM_SIZE)
 	{
 		*status = PGS_ERROR_UNSUPPORTED;
@@ -2103,12 +2131,22 @@ pgs_gs *pgs_gs_create(const pgs_backend_ops *ops, void *backend, const pgs_gs_op
 	}
 	gs->ops = ops;
 	gs->be = backend;
-	gs->regs[R_PRMODECONT] = 1;
+	// Power-on register file is all zero, PRMODECONT.AC included
+	// (reset_context_state_registers, gs/gs_interface.cpp:32-38).
 	// Power-on state: instance 0 does not match any real FRAME/ZBUF.
 	gs->instances[0].frame = 0x3full << 24;
 	gs->instances[0].zbuf = 0x7ull << 24;
-	gs->set_super_sampling(options ? options->super_sampling : 1, options ? options->ordered_super_sampling != 0 : true);
-	gs->ssaa_textures = options && options->super_sampled_textures != 0;
+	// Fields past struct_size read as zero (callers built against a shorter
+	// layout); struct_size 0 means the whole current layout.
+	pgs_gs_options o = {};
+	if (options)
+	{
+		size_t n = options->struct_size ? std::min<size_t>(options->struct_size, sizeof(o)) : sizeof(o);
+		memcpy(&o, options, n);
+	}
+	if (!options)
+		o.super_sampling = 1, o.ordered_super_sampling = 1;
+	gs->set_super_sampling(o.super_sampling, o.ordered_super_sampling != 0, o.super_sampled_textures != 0);
 	gs->reserve_buffers();
 	*status = gs->sticky_error;
 	if (gs->sticky_error)
@@ -2652,7 +2690,7 @@ int pgs_gs_set_super_sampling_rate(pgs_gs *gs, uint32_t super_sampling, uint32_t
 	if (!gs)
 		return PGS_ERROR_INVALID_ARGUMENT;
 	gs->flush();
-	gs->set_super_sampling(super_sampling, ordered_grid != 0);
+	gs->set_super_sampling(super_sampling, ordered_grid != 0, gs->ssaa_textures);
 	return gs->sticky_error;
 }
 
@@ -2661,7 +2699,9 @@ int pgs_gs_set_super_sampled_textures(pgs_gs *gs, int enable)
 	if (!gs)
 		return PGS_ERROR_INVALID_ARGUMENT;
 	gs->flush();
-	gs->ssaa_textures = enable != 0;
+	// Super-sampled textures need a super-sampled frame (set_super_sampling_rate
+	// turns them off at X1, gs/gs_interface.cpp:74-78).
+	gs->ssaa_textures = enable != 0 && (gs->sampling_rate_x_log2 | gs->sampling_rate_y_log2) != 0;
 	gs->reg_serial++;
 	gs->template_dirty = true;
 	return gs->sticky_error;
@@ -2733,7 +2773,6 @@ int pgs_gs_reset_context_state(pgs_gs *gs)
 		return PGS_ERROR_INVALID_ARGUMENT;
 	gs->flush();
 	memset(gs->regs, 0, sizeof(gs->regs));
-	gs->regs[R_PRMODECONT] = 1;
 	for (auto &p : gs->paths)
 		p = pgs_gs::Path();
 	gs->internal_q = 1.0f;

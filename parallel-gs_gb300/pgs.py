@@ -53,7 +53,7 @@ class FlushStats(C.Structure):
 
 
 class GSOptions(C.Structure):
-    _fields_ = [("super_sampling", C.c_uint32), ("ordered_super_sampling", C.c_uint32), ("vram_size", C.c_uint32),
+    _fields_ = [("struct_size", C.c_uint32), ("super_sampling", C.c_uint32), ("ordered_super_sampling", C.c_uint32), ("vram_size", C.c_uint32),
                 ("dynamic_super_sampling", C.c_uint32), ("super_sampled_textures", C.c_uint32)]
 
 
@@ -326,7 +326,7 @@ class GSInterface:
                  super_sampled_textures: bool = False, dynamic_super_sampling: bool = False):
         self.lib = lib or load_library()
         self.backend = backend
-        opts = GSOptions(super_sampling, int(ordered), VRAM_SIZE, int(dynamic_super_sampling),
+        opts = GSOptions(C.sizeof(GSOptions), super_sampling, int(ordered), VRAM_SIZE, int(dynamic_super_sampling),
                          int(super_sampled_textures))
         status = C.c_int(0)
         self.handle = self.lib.pgs_gs_create(C.c_void_p(backend.ops), C.c_void_p(backend.handle), C.byref(opts),

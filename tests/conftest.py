@@ -16,7 +16,10 @@ def pytest_configure(config):
 @pytest.fixture(scope="session", autouse=True)
 def built_libraries():
     import build
-    return build.build_all()
+    import build_oracle
+    res = build.build_all()
+    res.update(build_oracle.build_all())
+    return res
 
 
 def cuda_available() -> bool:

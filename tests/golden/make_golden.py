@@ -25,7 +25,7 @@ ROOT = HERE.parents[1]
 sys.path.insert(0, str(ROOT / "parallel-gs_gb300"))
 sys.path.insert(0, str(ROOT / "oracle"))
 
-import build  # noqa: E402
+import build_oracle  # noqa: E402
 import pgs_oracle  # noqa: E402
 
 VRAM = 4 * 1024 * 1024
@@ -49,7 +49,7 @@ def formula_vram(psm: int) -> np.ndarray:
 
 
 def main():
-    build.build_reference_harness()
+    build_oracle.build_reference_harness()
     ref = pgs_oracle.load_reference()
     if ref is None:
         raise SystemExit("reference harness unavailable: reference sources not present")

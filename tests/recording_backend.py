@@ -96,7 +96,8 @@ def _struct_array(ptr, n, fields):
 class RecordingBackend(pgs.Backend):
     """Backend that records; `passes`, `copies`, `palettes`, `ss` hold what was sent."""
 
-    def __init__(self):
+    def __init__(self, max_samples_log2: int = 4):
+        self.max_samples_log2 = max_samples_log2
         self.passes, self.copies, self.palettes, self.ss = [], [], [], []
         self.vram = np.zeros(pgs.VRAM_SIZE, dtype=np.uint8)
         self.next_clut = 0
@@ -150,6 +151,9 @@ class RecordingBackend(pgs.Backend):
         return self.next_clut
 
     def _set_ss(self, s, x, y):
+        # Like a backend created with max_samples_log2 sample planes.
+        if x + y > self.max_samples_log2:
+            return pgs.STATUS_CODES["PGS_ERROR_UNSUPPORTED"]
         self.ss.append((x, y))
         return 0
 

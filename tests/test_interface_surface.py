@@ -2,6 +2,8 @@
 reset_context_state, clobber_register_state, register file and GIF path
 accessors, the signal interface and debug mode / timestamps, on the recording
 backend and the CPU oracle."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -46,7 +48,8 @@ def test_reset_context_state_returns_registers_and_paths_to_power_on():
     assert gs.get_gif_path(2)["loop"] == 1
     gs.reset_context_state()
     assert gs.read_register(g.FRAME_1) == 0
-    assert gs.read_register(g.PRMODECONT) == 1
+    # The reference's power-on file is all zero, PRMODECONT.AC included.
+    assert gs.read_register(g.PRMODECONT) == 0
     assert gs.get_gif_path(2) == {"tag": (0, 0), "reg": 0, "loop": 0}
     # The triangle drawn before the reset was flushed by it.
     assert sum(len(p["prims"]) for p in be.passes) == 1
@@ -127,3 +130,43 @@ def test_debug_mode_without_backend_timing():
         gs.get_accumulated_timestamps(9)
     gs.close()
     be.close()
+
+
+def test_super_sampling_rate_is_lowered_to_what_the_backend_supports():
+    """set_super_sampling_rate takes min(requested, the backend's maximum)
+    (gs/gs_interface.cpp:69-70) instead of failing; 1x turns super-sampled
+    textures off (:74-78)."""
+    be = RecordingBackend(max_samples_log2=2)
+    gs = pgs.GSInterface(be, super_sampling=16, super_sampled_textures=True)
+    # 16x (2, 2) and 8x (1, 2) are refused by a 4-plane backend; 4x ordered is taken.
+    assert be.ss[-1] == (1, 1)
+    gs.set_super_sampling_rate(8)
+    assert be.ss[-1] == (1, 1)
+    gs.set_super_sampling_rate(2)
+    assert be.ss[-1] == (0, 1)
+    gs.set_super_sampling_rate(16, ordered=False)
+    assert be.ss[-1] == (0, 2)
+    gs.close()
+
+    be = RecordingBackend(max_samples_log2=0)
+    gs = pgs.GSInterface(be, super_sampling=4, super_sampled_textures=True)
+    assert be.ss[-1] == (0, 0)
+    gs.close()
+
+
+def test_options_struct_size_reads_older_layouts():
+    """pgs_gs_options.struct_size: fields past it read as zero, so a caller
+    built against the three-field layout gets no super-sampled textures."""
+    lib = pgs.load_library()
+    be = RecordingBackend()
+    full = pgs.GSOptions(0, 4, 1, pgs.VRAM_SIZE, 0, 1)
+    short = pgs.GSOptions(16, 4, 1, pgs.VRAM_SIZE, 1, 1)
+    status = C.c_int(0)
+    for opts in (full, short):
+        h = lib.pgs_gs_create(C.c_void_p(be.ops), C.c_void_p(be.handle), C.byref(opts), C.byref(status))
+        assert h and status.value == 0
+        lib.pgs_gs_destroy(C.c_void_p(h))
+    assert be.ss[-1] == (1, 1)
+    bad = pgs.GSOptions(4, 4, 1, pgs.VRAM_SIZE, 0, 0)
+    h = lib.pgs_gs_create(C.c_void_p(be.ops), C.c_void_p(be.handle), C.byref(bad), C.byref(status))
+    assert not h and status.value == pgs.STATUS_CODES["PGS_ERROR_INVALID_ARGUMENT"]

@@ -82,6 +82,106 @@ def test_noalloc_copy_matches_copy_vram_on_consecutive_calls():
         backend.close()
 
 
+# Copies into the rendered colour buffer (FBP 0, 640 wide), so that they clear
+# super-sample reference bits a 4x render left there.
+SS_COPIES = [
+    regs(8192, 4, PSMCT32, 0, 10, PSMCT32, 0, 0, 16, 16, 256, 128),
+    regs(9216, 2, PSMCT16, 0, 10, PSMCT16, 4, 4, 300, 40, 96, 64),
+    regs(10240, 4, PSMT8, 0, 10, PSMT8, 0, 3, 64, 200, 128, 32),
+    regs(0, 10, PSMCT32, 0, 10, PSMCT32, 100, 100, 120, 110, 64, 64),
+]
+
+
+def _entry_point():
+    lib = pgs.load_library()
+    fn = lib.pgs_vram_local_copy_noalloc
+    fn.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(CopyDesc), C.c_void_p]
+    fn.restype = C.c_int
+    return fn
+
+
+def test_noalloc_copy_clears_reference_plane_like_copy_vram():
+    """On a 4x super-sampled backend copy_vram also clears the destination's
+    bits in the super-sample reference plane (plane 1).  The entry point does
+    the same when it is given every plane; all six planes must match after each
+    of several copies in a row."""
+    torch = pytest.importorskip("torch")
+    import gsgen
+
+    fn = _entry_point()
+    frame = gsgen.frame_c2(seed=3, num_triangles=300, num_sprites=30, super_sampling=4, num_textures=2)
+    backend = pgs.CudaBackend(0, max_samples_log2=2)
+    gs = pgs.GSInterface(backend, super_sampling=4)
+    num_planes = 2 + 4
+    try:
+        gs.gif_transfer(0, frame.data)
+        gs.flush()
+        planes = np.stack([backend.read_plane(p) for p in range(num_planes)])
+        # The render left reference bits for the copies to clear.
+        assert np.count_nonzero(planes[1]) > 0
+        device_vram = torch.from_numpy(planes.reshape(-1).copy()).cuda()
+        torch.cuda.synchronize()
+        for bitbltbuf, trxpos, trxreg in SS_COPIES:
+            before = device_vram.cpu().numpy().reshape(num_planes, -1)
+            gs.write_register(BITBLTBUF, bitbltbuf)
+            gs.write_register(TRXPOS, trxpos)
+            gs.write_register(TRXREG, trxreg)
+            gs.write_register(TRXDIR, 2)
+            gs.flush()
+            expected = np.stack([backend.read_plane(p) for p in range(num_planes)])
+
+            desc = CopyDesc(bitbltbuf, trxpos, trxreg, 2, None, 0, 0, 0)
+            assert fn(C.c_void_p(device_vram.data_ptr()), num_planes, C.byref(desc), None) == 0
+            torch.cuda.synchronize()
+            got = device_vram.cpu().numpy().reshape(num_planes, -1)
+            for p in range(num_planes):
+                assert np.array_equal(got[p], expected[p]), "plane %d differs" % p
+            assert not np.array_equal(got[0], before[0])
+        # Some reference bits were cleared, so plane 1 was really exercised.
+        assert np.count_nonzero(got[1]) < np.count_nonzero(planes[1])
+    finally:
+        gs.close()
+        backend.close()
+
+
+def test_noalloc_copy_accepts_exactly_the_limit():
+    """A rectangle of exactly PGS_NOALLOC_COPY_MAX_PIXELS (512 x 512) is copied
+    bit-exactly; one more row is refused with PGS_ERROR_CAPACITY and leaves
+    VRAM untouched."""
+    torch = pytest.importorskip("torch")
+    fn = _entry_point()
+    rng = np.random.default_rng(11)
+    init = rng.integers(0, 256, size=pgs.VRAM_SIZE, dtype=np.uint8)
+    backend = pgs.CudaBackend(0, max_samples_log2=0)
+    gs = pgs.GSInterface(backend, super_sampling=1)
+    try:
+        gs.write_vram(init)
+        device_vram = torch.from_numpy(init.copy()).cuda()
+        torch.cuda.synchronize()
+        bitbltbuf, trxpos, trxreg = regs(0, 8, PSMCT32, 8192, 8, PSMCT32, 0, 0, 0, 0, 512, 512)
+        assert 512 * 512 == 256 * 1024
+        gs.write_register(BITBLTBUF, bitbltbuf)
+        gs.write_register(TRXPOS, trxpos)
+        gs.write_register(TRXREG, trxreg)
+        gs.write_register(TRXDIR, 2)
+        expected = gs.read_vram()
+        desc = CopyDesc(bitbltbuf, trxpos, trxreg, 2, None, 0, 0, 0)
+        assert fn(C.c_void_p(device_vram.data_ptr()), 1, C.byref(desc), None) == 0
+        torch.cuda.synchronize()
+        got = device_vram.cpu().numpy()
+        assert np.array_equal(got, expected)
+
+        bitbltbuf, trxpos, trxreg = regs(0, 8, PSMCT32, 0, 8, PSMCT32, 0, 0, 0, 1, 512, 513)
+        desc = CopyDesc(bitbltbuf, trxpos, trxreg, 2, None, 0, 0, 0)
+        assert fn(C.c_void_p(device_vram.data_ptr()), 1, C.byref(desc), None) == \
+            pgs.STATUS_CODES["PGS_ERROR_CAPACITY"]
+        torch.cuda.synchronize()
+        assert np.array_equal(device_vram.cpu().numpy(), expected)
+    finally:
+        gs.close()
+        backend.close()
+
+
 def test_noalloc_copy_rejects_oversized_rectangles():
     torch = pytest.importorskip("torch")
     lib = pgs.load_library()
