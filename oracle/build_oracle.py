@@ -4,11 +4,14 @@ liboracle.so   CPU restatement of the backend (oracle_backend.cpp), used only
                by the tests, the smoke check and the CPU-baseline leg of the
                benchmark.
 libpgsref.so   the reference's own CPU swizzle path (gs/gs_util.hpp:50-205)
-               compiled from the reference's sources by ref_harness.cpp.  The
-               sources are read where the reference is mounted:
-               $PGS_REFERENCE_DIR, else /root/reference.  Where neither holds
-               gs/gs_util.hpp the harness is not built and the tests that use
-               it fall back to the committed golden vectors.
+               compiled from the reference's sources by ref_harness.cpp.
+libpgsref_frontend.so
+               the reference's own CPU frontend (gs/gs_interface.cpp,
+               gs/page_tracker.cpp, gs/gs_util.cpp) compiled unmodified over
+               the recording renderer of ref_frontend/ref_frontend.cpp.
+The reference's sources are read where the reference is mounted:
+$PGS_REFERENCE_DIR, else /root/reference.  Where they are absent these two
+are not built and the tests that need them skip.
 
 Outputs go to oracle/_build and oracle/_ref (both git-ignored).
 """
@@ -69,11 +72,45 @@ def build_reference_harness() -> Path | None:
     return out
 
 
+REF_FRONTEND = ORACLE / "ref_frontend"
+REF_FRONTEND_SOURCES = ("gs_interface.cpp", "page_tracker.cpp", "gs_util.cpp")
+
+
+def build_reference_frontend() -> Path | None:
+    """Compile the reference's CPU frontend (GSInterface, PageTracker, gs_util)
+    from its sources, unmodified, against the stand-in headers under
+    ref_frontend/shim and the recording GSRenderer of ref_frontend.cpp."""
+    gs = reference_dir() / "gs"
+    if not all((gs / f).exists() for f in REF_FRONTEND_SOURCES):
+        print("reference sources not found under %s: libpgsref_frontend.so not built" % reference_dir(),
+              file=sys.stderr)
+        return None
+    REF_BUILD.mkdir(parents=True, exist_ok=True)
+    out = REF_BUILD / "libpgsref_frontend.so"
+    shim = sorted(p for p in (REF_FRONTEND / "shim").rglob("*.hpp"))
+    own = REF_FRONTEND / "ref_frontend.cpp"
+    srcs = [gs / f for f in REF_FRONTEND_SOURCES] + [own]
+    if _newer(out, srcs + shim + [Path(__file__)]):
+        return out
+    inc = ["-I", str(REF_FRONTEND / "shim"), "-I", str(gs), "-I", str(gs / "shaders")]
+    objs = []
+    jobs = []
+    for src in srcs:
+        obj = REF_BUILD / ("frontend_" + src.stem + ".o")
+        objs.append(obj)
+        jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-w", *inc, "-c", str(src), "-o", str(obj)])
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        list(ex.map(_run, jobs))
+    _run(["g++", "-shared", "-Wl,--no-undefined", *map(str, objs), "-o", str(out)])
+    return out
+
+
 def build_all() -> dict:
-    with ThreadPoolExecutor(max_workers=2) as ex:
+    with ThreadPoolExecutor(max_workers=3) as ex:
         f_orc = ex.submit(build_oracle)
         f_ref = ex.submit(build_reference_harness)
-        return {"oracle": f_orc.result(), "reference": f_ref.result()}
+        f_fe = ex.submit(build_reference_frontend)
+        return {"oracle": f_orc.result(), "reference": f_ref.result(), "reference_frontend": f_fe.result()}
 
 
 if __name__ == "__main__":

@@ -1773,19 +1773,9 @@ struct pgs_gs
 			const uint32_t zx0 = uint32_t(bb[0]) >> D.z_pw, zx1 = uint32_t(bb[2]) >> D.z_pw;
 			const uint32_t zy0 = uint32_t(bb[1]) >> D.z_ph, zy1 = uint32_t(bb[3]) >> D.z_ph;
 			const uint32_t zkind = zb.zmsk ? 1u : 0u;
-			bool hazard = tracker.test_mark(frame.fbp, D.fb_stride, fx0, fx1, fy0, fy1, 0);
+			tracker.test_mark(frame.fbp, D.fb_stride, fx0, fx1, fy0, fy1, 0);
 			if (z_sens)
-				hazard = tracker.test_mark(zb.zbp, D.z_stride, zx0, zx1, zy0, zy1, zkind) || hazard;
-			if (hazard && primitive_count)
-			{
-				flush_render_pass(FLUSH_TEXTURE_HAZARD);
-				check_frame_buffer_state();
-				update_template(bb);
-				template_dirty = false;
-				tracker.test_mark(frame.fbp, D.fb_stride, fx0, fx1, fy0, fy1, 0);
-				if (z_sens)
-					tracker.test_mark(zb.zbp, D.z_stride, zx0, zx1, zy0, zy1, zkind);
-			}
+				tracker.test_mark(zb.zbp, D.z_stride, zx0, zx1, zy0, zy1, zkind);
 			if (tpl_has_tex_span && (tex_mark_key[0] != tpl_serial || tex_mark_key[1] != tracker.clears))
 			{
 				for (uint32_t l = 0; l < tpl_num_tex_spans; l++)
