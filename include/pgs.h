@@ -150,6 +150,18 @@ typedef struct pgs_rp_instance
 	uint32_t z_sensitive, z_write, channel_shuffle;
 } pgs_rp_instance;
 
+/* Why a render pass ended (FlushReason, gs/page_tracker.hpp:117-126). */
+typedef enum pgs_flush_reason
+{
+	PGS_FLUSH_FB_POINTER = 0,     /* frame/depth buffer change with no instance left */
+	PGS_FLUSH_OVERFLOW = 1,       /* primitive, state, texture or CLUT table full */
+	PGS_FLUSH_TEXTURE_HAZARD = 2, /* texture or CLUT read of pages the pass wrote */
+	PGS_FLUSH_COPY_HAZARD = 3,    /* transfer touching pages the pass reads or writes */
+	PGS_FLUSH_SUBMISSION = 4,     /* explicit flush, vsync, host access to VRAM */
+	PGS_FLUSH_PRESSURE = 5,       /* pending-work limits reached */
+	PGS_FLUSH_HOST_ACCESS = 6     /* LOCAL->HOST read-back of pages the pass wrote */
+} pgs_flush_reason;
+
 typedef struct pgs_render_pass
 {
 	const pgs_vertex_position *positions;     /* 3 per primitive */
@@ -166,7 +178,7 @@ typedef struct pgs_render_pass
 	uint32_t num_instances;
 	uint32_t coarse_tile_size_log2;
 	uint32_t has_aa1, has_scanmsk;
-	uint32_t flush_reason;
+	uint32_t flush_reason;  /* pgs_flush_reason */
 	/* Some primitive samples mip levels (TEX1.MXL > 0 with a mipmapping MMIN). */
 	uint32_t has_mipmap;
 	/* Some texture of the pass is super-sampled (pgs_texture_desc.samples). */

@@ -259,6 +259,14 @@ struct Backend
 		res_prim.resize(PGS_MAX_PRIMITIVES_PER_FLUSH);
 	}
 
+	// Texels come from this copy of the VRAM planes, taken when a pass with
+	// textures begins: textures are sampled as the pass found them (the
+	// reference samples texture-cache images uploaded before the pass renders),
+	// whatever the pass itself writes.
+	std::vector<uint8_t> tex_vram;
+	uint32_t t32(uint32_t plane, uint32_t i) const { return reinterpret_cast<const uint32_t *>(tex_vram.data() + plane * size_t(VRAM))[i]; }
+	uint16_t t16(uint32_t plane, uint32_t i) const { return reinterpret_cast<const uint16_t *>(tex_vram.data() + plane * size_t(VRAM))[i]; }
+	uint8_t t8(uint32_t plane, uint32_t i) const { return tex_vram[plane * size_t(VRAM) + i]; }
 	uint32_t &w32(uint32_t plane, uint32_t i) { return reinterpret_cast<uint32_t *>(vram.data() + plane * size_t(VRAM))[i]; }
 	uint16_t &w16(uint32_t plane, uint32_t i) { return reinterpret_cast<uint16_t *>(vram.data() + plane * size_t(VRAM))[i]; }
 	uint8_t &w8(uint32_t plane, uint32_t i) { return vram[plane * size_t(VRAM) + i]; }
@@ -977,27 +985,27 @@ struct Backend
 		{
 		case CT24: case Z24:
 		{
-			uint32_t c = w32(0, a) & 0xffffffu;
+			uint32_t c = t32(0, a) & 0xffffffu;
 			uint32_t al = (t.aem && c == 0) ? 0 : t.ta0;
 			return c | (al << 24);
 		}
 		case CT16: case CT16S: case Z16: case Z16S:
 		{
-			uint32_t c = w16(0, a);
+			uint32_t c = t16(0, a);
 			uint32_t r = (c & 0x1f) << 3, g = ((c >> 5) & 0x1f) << 3, b = ((c >> 10) & 0x1f) << 3;
 			uint32_t al = (t.aem && c == 0) ? 0 : ((c & 0x8000) ? t.ta1 : t.ta0);
 			return r | (g << 8) | (b << 16) | (al << 24);
 		}
-		case T8: return clut_color(t, w8(0, a));
-		case T8H: return clut_color(t, w32(0, a) >> 24);
+		case T8: return clut_color(t, t8(0, a));
+		case T8H: return clut_color(t, t32(0, a) >> 24);
 		case T4:
 		{
-			uint32_t byte = w8(0, a >> 1);
+			uint32_t byte = t8(0, a >> 1);
 			return clut_color(t, (byte >> ((a & 1) * 4)) & 15u);
 		}
-		case T4HL: return clut_color(t, (w32(0, a) >> 24) & 15u);
-		case T4HH: return clut_color(t, w32(0, a) >> 28);
-		default: return w32(0, a);
+		case T4HL: return clut_color(t, (t32(0, a) >> 24) & 15u);
+		case T4HH: return clut_color(t, t32(0, a) >> 28);
+		default: return t32(0, a);
 		}
 	}
 
@@ -1137,41 +1145,41 @@ struct Backend
 		{
 		case CT24: case Z24:
 		{
-			uint32_t col = w32(0, a), ref = w32(1, a);
+			uint32_t col = t32(0, a), ref = t32(1, a);
 			if (ref != 0)
-				col = (w32(2 + s, a) & ref) | (col & ~ref);
+				col = (t32(2 + s, a) & ref) | (col & ~ref);
 			col &= 0xffffffu;
 			uint32_t al = (t.aem && col == 0) ? 0 : t.ta0;
 			return col | (al << 24);
 		}
 		case CT16: case CT16S: case Z16: case Z16S:
 		{
-			uint32_t c = w16(0, a);
-			if (w16(1, a) == 0xffff)
-				c = w16(2 + s, a);
+			uint32_t c = t16(0, a);
+			if (t16(1, a) == 0xffff)
+				c = t16(2 + s, a);
 			uint32_t r = (c & 0x1f) << 3, g = ((c >> 5) & 0x1f) << 3, b = ((c >> 10) & 0x1f) << 3;
 			uint32_t al = (t.aem && c == 0) ? 0 : ((c & 0x8000) ? t.ta1 : t.ta0);
 			return r | (g << 8) | (b << 16) | (al << 24);
 		}
 		case T8:
 		{
-			uint32_t idx = w8(0, a);
-			if (w8(1, a) == 0xff)
-				idx = w8(2 + s, a);
+			uint32_t idx = t8(0, a);
+			if (t8(1, a) == 0xff)
+				idx = t8(2 + s, a);
 			return clut_color(t, idx);
 		}
 		case T8H:
 		{
-			uint32_t idx = w8(0, 4 * a + 3);
-			if (w8(1, 4 * a + 3) == 0xff)
-				idx = w8(2 + s, 4 * a + 3);
+			uint32_t idx = t8(0, 4 * a + 3);
+			if (t8(1, 4 * a + 3) == 0xff)
+				idx = t8(2 + s, 4 * a + 3);
 			return clut_color(t, idx);
 		}
 		default:
 		{
-			uint32_t c = w32(0, a);
-			if (w32(1, a) == 0xffffffffu)
-				c = w32(2 + s, a);
+			uint32_t c = t32(0, a);
+			if (t32(1, a) == 0xffffffffu)
+				c = t32(2 + s, a);
 			return c;
 		}
 		}
@@ -1323,7 +1331,14 @@ struct Backend
 	void sample_texture(const PassCtx &P, uint32_t tex_word, uint32_t tex2, float u, float v, float q,
 	                    bool perspective, uint32_t sample, uint32_t rx, uint32_t ry, float out[4])
 	{
-		const pgs_texture_desc &t = P.rp->textures[tex_word & 0xffffu];
+		// Descriptors keep only the region modes; plain REPEAT and CLAMP come
+		// from the primitive's sampler bits (TEX_SAMPLER_CLAMP_S/T,
+		// gs/gs_interface.cpp:1514-1528, 1818-1820).
+		pgs_texture_desc t = P.rp->textures[tex_word & 0xffffu];
+		if (t.wms < 2)
+			t.wms = (tex_word & (1u << 19)) ? 1u : 0u;
+		if (t.wmt < 2)
+			t.wmt = (tex_word & (1u << 20)) ? 1u : 0u;
 		if ((tex_word & (1u << 24)) && t.samples > 1)
 		{
 			uint32_t rgba[4];
@@ -2340,6 +2355,13 @@ struct Backend
 			if (d.samples > 1 && (std::max<uint32_t>(d.levels, 1) != 1 || (d.samples & (d.samples - 1)) ||
 			                      d.samples > 16 || 2 + d.samples > num_planes))
 				return PGS_ERROR_INVALID_ARGUMENT;
+		}
+		if (rp->num_textures)
+		{
+			// Plane 0, and every plane when super-sampled texture layers read
+			// the reference plane and the samples.
+			const size_t planes = rp->has_ss_textures ? num_planes : 1;
+			tex_vram.assign(vram.begin(), vram.begin() + planes * size_t(VRAM));
 		}
 		std::vector<pgs_primitive_attribute> prims(rp->prims, rp->prims + rp->num_primitives);
 		std::vector<Setup> setup(rp->num_primitives);

@@ -18,6 +18,7 @@
 // samples.
 #include "pgs.h"
 #include "gs_defs.h"
+#include "gs_tracker.h"
 
 #include <algorithm>
 #include <cstddef>
@@ -49,10 +50,12 @@ enum Reg : uint32_t
 	R_SIGNAL = 0x60, R_FINISH = 0x61, R_LABEL = 0x62
 };
 
+// FlushReason, numbered as the reference's (gs/page_tracker.hpp:117-126).
 enum FlushReason : uint32_t
 {
-	FLUSH_EXPLICIT = 0, FLUSH_OVERFLOW = 1, FLUSH_FB_POINTER = 2, FLUSH_TEXTURE_HAZARD = 3,
-	FLUSH_COPY_HAZARD = 4, FLUSH_CLUT_HAZARD = 5, FLUSH_HOST_ACCESS = 6, FLUSH_SUPER_SAMPLING = 7
+	FLUSH_FB_POINTER = PGS_FLUSH_FB_POINTER, FLUSH_OVERFLOW = PGS_FLUSH_OVERFLOW,
+	FLUSH_TEXTURE_HAZARD = PGS_FLUSH_TEXTURE_HAZARD, FLUSH_COPY_HAZARD = PGS_FLUSH_COPY_HAZARD,
+	FLUSH_EXPLICIT = PGS_FLUSH_SUBMISSION, FLUSH_PRESSURE = PGS_FLUSH_PRESSURE, FLUSH_HOST_ACCESS = PGS_FLUSH_HOST_ACCESS
 };
 
 enum PrimType : uint32_t
@@ -140,264 +143,37 @@ static bool zbuf_compat(uint64_t a, uint64_t b)
 	return (a & 0x0f0001ffull) == (b & 0x0f0001ffull);
 }
 
-// Page-granular VRAM hazard tracker (a reduced gs/page_tracker.cpp).
-struct PageSpan
-{
-	uint32_t base_page;
-	uint32_t width, height, stride;
-};
-
-static PageSpan page_span(uint32_t base_block, uint32_t x, uint32_t y, uint32_t w, uint32_t h,
-                          uint32_t row_length_64, uint32_t psm)
-{
-	// Conservative page coverage of a rectangle (compute_page_rect, gs/gs_util.cpp:141-230).
-	Layout L = psm_layout(psm);
-	if (w == 0) w = 1;
-	if (h == 0) h = 1;
-	uint32_t px0 = x >> L.pw, px1 = (x + w - 1) >> L.pw;
-	uint32_t py0 = y >> L.ph, py1 = (y + h - 1) >> L.ph;
-	uint32_t stride = row_length_64;
-	if (psm == PSMT4 || psm == PSMT8)
-		stride >>= 1;
-	PageSpan s;
-	s.base_page = base_block / BLOCKS_PER_PAGE + py0 * stride + px0;
-	s.width = px1 - px0 + 1 + ((base_block % BLOCKS_PER_PAGE) ? 1 : 0);
-	s.height = py1 - py0 + 1;
-	s.stride = stride;
-	if (s.width > NUM_PAGES) s.width = NUM_PAGES;
-	if (s.height > NUM_PAGES) s.height = NUM_PAGES;
-	return s;
-}
-
-// One bit per page and access kind.  A span covers, per row, the pages
-// base + y * stride + [0, width) modulo the page count.
-struct PageTracker
-{
-	enum : uint8_t { FB_WRITE = 1, FB_READ = 2, TEX_READ = 4 };
-	static constexpr uint32_t WORDS = NUM_PAGES / 64;
-	uint64_t bits[3][WORDS] = {};
-	// Pages a pass wrote as frame or depth buffer since a transfer or host
-	// write last replaced them (PAGE_STATE_MAY_SUPER_SAMPLE_BIT,
-	// gs/page_tracker.cpp:155-190,255-265,650-715); kept across passes.
-	uint64_t may_ss[WORDS] = {};
-	// Bumped when a page gains a kind it did not have / when the tracker is cleared.
-	uint64_t gen[3] = {};
-	uint64_t gen_at_clear[3] = {};
-	uint64_t clears = 0;
-
-	static bool range_any(const uint64_t *b, uint32_t start, uint32_t len)
-	{
-		while (len)
-		{
-			uint32_t o = start & 63, n = std::min<uint32_t>(len, 64 - o);
-			uint64_t m = (n == 64 ? ~0ull : ((1ull << n) - 1)) << o;
-			if (b[start >> 6] & m)
-				return true;
-			len -= n;
-			start = (start + n) % NUM_PAGES;
-		}
-		return false;
-	}
-
-	static bool range_set(uint64_t *b, uint32_t start, uint32_t len)
-	{
-		bool fresh = false;
-		while (len)
-		{
-			uint32_t o = start & 63, n = std::min<uint32_t>(len, 64 - o);
-			uint64_t m = (n == 64 ? ~0ull : ((1ull << n) - 1)) << o;
-			fresh |= (b[start >> 6] & m) != m;
-			b[start >> 6] |= m;
-			len -= n;
-			start = (start + n) % NUM_PAGES;
-		}
-		return fresh;
-	}
-
-	static uint64_t low_mask(uint32_t n) { return n >= 64 ? ~0ull : ((1ull << n) - 1); }
-
-	// Spans up to 64 pages wide touch at most two words per row: one 128-bit
-	// mask per row, no data-dependent loop (the common case; primitives are
-	// small).
-	bool any_kind(const PageSpan &s, uint32_t k) const
-	{
-		if (gen[k] == gen_at_clear[k])
-			return false;
-		if (s.width <= 64)
-		{
-			const uint64_t m = low_mask(s.width);
-			uint64_t acc = 0;
-			for (uint32_t y = 0; y < s.height; y++)
-			{
-				uint32_t start = (s.base_page + y * s.stride) % NUM_PAGES, w = start >> 6;
-				unsigned __int128 mm = (unsigned __int128)m << (start & 63);
-				acc |= (bits[k][w] & uint64_t(mm)) | (bits[k][(w + 1) % WORDS] & uint64_t(mm >> 64));
-			}
-			return acc != 0;
-		}
-		for (uint32_t y = 0; y < s.height; y++)
-			if (range_any(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width))
-				return true;
-		return false;
-	}
-
-	void mark_kind(const PageSpan &s, uint32_t k)
-	{
-		bool fresh = false;
-		if (s.width <= 64)
-		{
-			const uint64_t m = low_mask(s.width);
-			uint64_t missing = 0;
-			for (uint32_t y = 0; y < s.height; y++)
-			{
-				uint32_t start = (s.base_page + y * s.stride) % NUM_PAGES, w = start >> 6, w1 = (w + 1) % WORDS;
-				unsigned __int128 mm = (unsigned __int128)m << (start & 63);
-				missing |= (~bits[k][w] & uint64_t(mm)) | (~bits[k][w1] & uint64_t(mm >> 64));
-				bits[k][w] |= uint64_t(mm);
-				bits[k][w1] |= uint64_t(mm >> 64);
-			}
-			fresh = missing != 0;
-		}
-		else
-		{
-			for (uint32_t y = 0; y < s.height; y++)
-				fresh |= range_set(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width);
-		}
-		if (fresh)
-			gen[k]++;
-	}
-
-	// Pages [x0, x1] x [y0, y1] of a buffer at page `base` with `stride` pages
-	// per row (the page rectangle of one primitive): marks them with kind
-	// `mk` and returns whether any of them is a texture read.  One pass over
-	// the rows does both; a texture-read bit is never set in a pass where no
-	// texture was read, so the test needs no separate early-out.
-	bool test_mark(uint32_t base, uint32_t stride, uint32_t x0, uint32_t x1, uint32_t y0, uint32_t y1, uint32_t mk)
-	{
-		const uint32_t w = std::min<uint32_t>(x1 - x0 + 1, NUM_PAGES), h = std::min<uint32_t>(y1 - y0 + 1, NUM_PAGES);
-		if (w > 64)
-		{
-			PageSpan s{ base + y0 * stride + x0, w, h, stride };
-			bool hit = any_kind(s, 2);
-			mark_kind(s, mk);
-			if (mk == 0)
-				for (uint32_t y = 0; y < s.height; y++)
-					range_set(may_ss, (s.base_page + y * s.stride) % NUM_PAGES, s.width);
-			return hit;
-		}
-		const uint64_t m = low_mask(w);
-		uint32_t start = base + y0 * stride + x0;
-		if (h <= 2)
-		{
-			// Common case, without a data-dependent loop: up to two rows, each
-			// touching the word holding its first page and the next one.
-			const uint32_t s0 = start % NUM_PAGES, s1 = (start + stride) % NUM_PAGES;
-			const uint64_t r1 = h == 2 ? m : 0;
-			const uint64_t a0 = m << (s0 & 63), b0 = (m >> 1) >> (63 - (s0 & 63));
-			const uint64_t a1 = r1 << (s1 & 63), b1 = (r1 >> 1) >> (63 - (s1 & 63));
-			const uint32_t i0 = s0 >> 6, j0 = (i0 + 1) % WORDS, i1 = s1 >> 6, j1 = (i1 + 1) % WORDS;
-			uint64_t *bm = bits[mk];
-			const uint64_t *bt = bits[2];
-			const uint64_t hit = (bt[i0] & a0) | (bt[j0] & b0) | (bt[i1] & a1) | (bt[j1] & b1);
-			const uint64_t missing = (~bm[i0] & a0) | (~bm[j0] & b0) | (~bm[i1] & a1) | (~bm[j1] & b1);
-			bm[i0] |= a0;
-			bm[j0] |= b0;
-			bm[i1] |= a1;
-			bm[j1] |= b1;
-			if (mk == 0)
-			{
-				may_ss[i0] |= a0;
-				may_ss[j0] |= b0;
-				may_ss[i1] |= a1;
-				may_ss[j1] |= b1;
-			}
-			if (missing)
-				gen[mk]++;
-			return hit != 0;
-		}
-		uint64_t hit = 0, missing = 0;
-		for (uint32_t y = 0; y < h; y++, start += stride)
-		{
-			const uint32_t st = start % NUM_PAGES, wi = st >> 6, wj = (wi + 1) % WORDS;
-			const unsigned __int128 mm = (unsigned __int128)m << (st & 63);
-			const uint64_t m0 = uint64_t(mm), m1 = uint64_t(mm >> 64);
-			hit |= (bits[2][wi] & m0) | (bits[2][wj] & m1);
-			missing |= (~bits[mk][wi] & m0) | (~bits[mk][wj] & m1);
-			bits[mk][wi] |= m0;
-			bits[mk][wj] |= m1;
-			if (mk == 0)
-			{
-				may_ss[wi] |= m0;
-				may_ss[wj] |= m1;
-			}
-		}
-		if (missing)
-			gen[mk]++;
-		return hit != 0;
-	}
-
-	bool any(const PageSpan &s, uint8_t mask)
-	{
-		for (uint32_t k = 0; k < 3; k++)
-		{
-			if (!(mask & (1u << k)))
-				continue;
-			for (uint32_t y = 0; y < s.height; y++)
-				if (range_any(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width))
-					return true;
-		}
-		return false;
-	}
-
-	void mark(const PageSpan &s, uint8_t flags)
-	{
-		for (uint32_t k = 0; k < 3; k++)
-		{
-			if (!(flags & (1u << k)))
-				continue;
-			bool fresh = false;
-			for (uint32_t y = 0; y < s.height; y++)
-				fresh |= range_set(bits[k], (s.base_page + y * s.stride) % NUM_PAGES, s.width);
-			if (fresh)
-				gen[k]++;
-		}
-	}
-
-	// A transfer or host write replaced these pages.
-	void clear_may_super_sample(const PageSpan &s)
-	{
-		for (uint32_t y = 0; y < s.height; y++)
-		{
-			uint32_t start = (s.base_page + y * s.stride) % NUM_PAGES, len = s.width;
-			while (len)
-			{
-				uint32_t o = start & 63, n = std::min<uint32_t>(len, 64 - o);
-				may_ss[start >> 6] &= ~((n == 64 ? ~0ull : ((1ull << n) - 1)) << o);
-				len -= n;
-				start = (start + n) % NUM_PAGES;
-			}
-		}
-	}
-
-	// Only the base page counts: W/H round up to powers of two
-	// (texture_may_super_sample, gs/page_tracker.cpp:147-153).
-	bool may_super_sample(uint32_t page) const { return (may_ss[(page % NUM_PAGES) >> 6] >> (page & 63)) & 1; }
-
-	void clear()
-	{
-		memset(bits, 0, sizeof(bits));
-		clears++;
-		for (uint32_t k = 0; k < 3; k++)
-			gen_at_clear[k] = gen[k];
-	}
-};
-
 struct Instance
 {
 	int32_t bb[4] = { INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN };
 	uint64_t frame = 0, zbuf = 0;
 	uint32_t color_write_mask = 0;
+	uint32_t fb_pw = 0, fb_ph = 0, z_pw = 0, z_ph = 0;
 	bool z_sensitive = false, z_write = false;
+	bool has_channel_shuffle = false, z_feedback = false;
+};
+
+// Dirty state (StateDirtyFlags, gs/gs_interface.hpp:116-129): which derived
+// state a register write may have changed.  Register writes set bits only
+// when the value changes; a committed primitive clears them all.
+enum DirtyBits : uint32_t
+{
+	DIRTY_DEGENERATE = 1u << 0, DIRTY_PRIM_TEMPLATE = 1u << 1, DIRTY_TEX = 1u << 2, DIRTY_FB = 1u << 3,
+	DIRTY_FEEDBACK = 1u << 4, DIRTY_SCISSOR = 1u << 5, DIRTY_STATE = 1u << 6, DIRTY_POTENTIAL_FEEDBACK_REGION = 1u << 7,
+	DIRTY_ALL = 0xffu
+};
+
+// How a textured draw relates to the framebuffer it writes
+// (FBFeedbackMode, gs/gs_interface.hpp).
+enum FeedbackMode : uint32_t
+{
+	FEEDBACK_NONE, FEEDBACK_PIXEL, FEEDBACK_SLICED, FEEDBACK_BYPASS_HAZARDS
+};
+
+// The render pass's texture feedback kind (RenderPass::Feedback).
+enum PassFeedback : uint32_t
+{
+	PASS_FEEDBACK_NONE, PASS_FEEDBACK_COLOR, PASS_FEEDBACK_DEPTH
 };
 
 struct TextureKey
@@ -419,7 +195,7 @@ struct TextureKeyHash
 };
 } // namespace
 
-struct pgs_gs
+struct pgs_gs : TrackerClient
 {
 	const pgs_backend_ops *ops = nullptr;
 	void *be = nullptr;
@@ -454,7 +230,6 @@ struct pgs_gs
 	uint32_t primitive_count = 0;
 	std::vector<pgs_state_vector> state_vectors;
 	std::vector<pgs_texture_desc> textures;
-	std::unordered_map<TextureKey, uint32_t, TextureKeyHash> texture_map;
 	Instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
 	uint32_t num_instances = 1;
 	uint32_t current_instance = 0;
@@ -474,7 +249,6 @@ struct pgs_gs
 	// the transfer count when it was drawn.
 	bool last_para_candidate = false;
 	uint32_t last_para_order[3] = { 0, 1, 2 };
-	uint64_t transfer_serial = 0, last_para_transfer = 0;
 	pgs_debug_mode debug_mode = {};
 	uint32_t clut_instance = 0;
 	uint32_t pending_palette_updates = 0;
@@ -484,9 +258,6 @@ struct pgs_gs
 	bool template_dirty = true;
 	uint32_t tpl_state = 0, tpl_tex = 0, tpl_tex2 = 0;
 	// Pages of every sampled mip level of the current template's texture.
-	PageSpan tpl_tex_spans[7] = {};
-	uint32_t tpl_num_tex_spans = 0;
-	bool tpl_has_tex_span = false;
 
 	// Caches of values derived from the register file.  reg_serial changes
 	// whenever a register other than vertex data (RGBAQ, ST, UV, FOG, XYZ*) is
@@ -496,7 +267,6 @@ struct pgs_gs
 	uint64_t degenerate_serial = 0;
 	bool degenerate_cached = false;
 	uint64_t fb_state_serial = 0, fb_state_epoch = 0;
-	uint64_t tex_check_key[3] = {}, tex_mark_key[2] = {};
 	struct DrawConsts
 	{
 		uint64_t serial = 0;
@@ -517,6 +287,7 @@ struct pgs_gs
 	{
 		reg_serial++;
 		template_dirty = true;
+		dirty = DIRTY_ALL;
 		vq.count = 0;
 		update_offsets();
 	}
@@ -571,7 +342,47 @@ struct pgs_gs
 		return dc;
 	}
 
-	PageTracker tracker;
+	HazardTracker tracker{ *this };
+
+	// Drawing state of the reference's state tracker (gs/gs_interface.hpp:386-430).
+	uint32_t dirty = DIRTY_ALL;
+	uint64_t texflush_counter = 0;
+	bool texflush_pending = false;
+	uint32_t last_texture_index = UINT32_MAX;
+	uint64_t last_texture_valid_at = 0;
+	pgs_texture_desc last_texture_desc = {};
+	// Page rectangles of each level of the current texture state.
+	PageRect tex_rects[7];
+	uint32_t tex_num_rects = 0;
+	// The pass's texture table by descriptor hash (TextureStateToLocalIndex).
+	struct TexEntry
+	{
+		uint32_t index;
+		uint64_t valid_at;
+		bool long_term, valid;
+	};
+	std::unordered_map<uint64_t, TexEntry> tex_entries;
+	// Texture feedback against the current frame / depth buffer
+	// (update_color_feedback_state, gs/gs_interface.cpp:2141-2308).
+	bool is_color_feedback = false, is_depth_feedback = false, is_awkward_color_feedback = false;
+	bool is_potential_feedback = false, is_potential_channel_shuffle = false, current_is_channel_shuffle = false;
+	struct
+	{
+		uint32_t base_page, pw, ph, page_stride, width_bias, max_safe_page;
+	} potential = {};
+	uint32_t pass_feedback = PASS_FEEDBACK_NONE, pass_feedback_psm = 0, pass_feedback_cpsm = 0;
+	bool has_hazardous_short_term = false, has_optimized_short_term = false;
+	// Work submitted since the last submission; its limits end a pass early
+	// (check_flush_stats, gs/gs_renderer.cpp:864-895).
+	struct
+	{
+		uint64_t prims, passes, copies, palettes, copy_threads, scratch;
+	} pending = {};
+	// Blocks of each page that textures of the open pass read.  The backend
+	// decodes those textures as the pass begins, so a transfer into them has
+	// to end the pass first.
+	uint32_t pass_tex_blocks[NUM_PAGES] = {};
+	std::vector<uint16_t> pass_tex_pages;
 
 	struct
 	{
@@ -645,8 +456,94 @@ struct pgs_gs
 	}
 
 	// ---------------------------------------------------------------
+	// Flushes go through the tracker, which clears its per-pass marks and
+	// calls back (PageTracker::flush_render_pass, gs/page_tracker.cpp:497-509).
+	void flush_render_pass(uint32_t reason) { tracker.flush_render_pass(reason); }
+
+	// GSInterface::flush(flags, reason) (gs/gs_interface.cpp:353-420).
+	void tracker_flush(uint32_t flags, uint32_t reason) override
+	{
+		if (flags & TRACKER_FLUSH_FB)
+			do_flush_render_pass(reason);
+		if (reason == FLUSH_PRESSURE)
+		{
+			tracker.mark_submission(FLUSH_EXPLICIT);
+			submit();
+		}
+	}
+
+	void tracker_invalidate_texture(uint64_t hash, bool clut) override
+	{
+		if (!clut)
+		{
+			auto it = tex_entries.find(hash);
+			if (it != tex_entries.end())
+				it->second.valid = false;
+		}
+		mark_texture_state_dirty();
+	}
+
+	void tracker_texture_state_dirty_with_flush() override
+	{
+		mark_texture_state_dirty();
+		texflush_counter++;
+	}
+
+	void tracker_forget_memoization() override
+	{
+		mark_texture_state_dirty();
+	}
+
+	void mark_texture_state_dirty()
+	{
+		last_texture_index = UINT32_MAX;
+		last_texture_valid_at = 0;
+		dirty |= DIRTY_PRIM_TEMPLATE | DIRTY_TEX;
+	}
+
+	void submit()
+	{
+		int r = ops->flush_submit(be);
+		if (r != 0)
+			sticky_error = r;
+		pending = {};
+	}
+
+	// Limits of pending work (gs/gs_renderer.cpp:31-39, 864-895): past any of
+	// them the next draw kick or TEX0 write ends the open pass.
+	void check_pending_work()
+	{
+		if (pending.prims >= 4096 || pending.passes >= 1024 || pending.scratch >= 100ull * 1000 * 1000 ||
+		    pending.copies >= 16 * 1024 || pending.palettes >= 4096)
+			tracker.mark_memory_pressure();
+	}
+
+	void mark_pass_texture(const PageRect &r)
+	{
+		for (uint32_t y = 0; y < r.page_height; y++)
+			for (uint32_t x = 0; x < r.page_width; x++)
+			{
+				uint32_t p = (r.base_page + y * r.page_stride + x) & (NUM_PAGES - 1);
+				if (!pass_tex_blocks[p])
+					pass_tex_pages.push_back(uint16_t(p));
+				pass_tex_blocks[p] |= r.block_mask;
+			}
+	}
+
+	bool pass_texture_hit(const PageRect &r) const
+	{
+		if (pass_tex_pages.empty())
+			return false;
+		for (uint32_t y = 0; y < r.page_height; y++)
+			for (uint32_t x = 0; x < r.page_width; x++)
+				if (pass_tex_blocks[(r.base_page + y * r.page_stride + x) & (NUM_PAGES - 1)] & r.block_mask)
+					return true;
+		return false;
+	}
+
+	// ---------------------------------------------------------------
 	// Render pass flush (gs/gs_interface.cpp:133-351).
-	void flush_render_pass(uint32_t reason)
+	void do_flush_render_pass(uint32_t reason)
 	{
 		fb_epoch++;
 		last_para_candidate = false;
@@ -729,19 +626,21 @@ struct pgs_gs
 
 				FrameReg frame(inst.frame);
 				ZbufReg zbuf(inst.zbuf);
-				bool channel_shuffle = false;
+				bool channel_shuffle = inst.has_channel_shuffle;
 				if (frame.psm != PSMCT32 && frame.psm != PSMCT24 && frame.psm != PSMZ32 && frame.psm != PSMZ24)
 				{
 					uint32_t m = inst.color_write_mask & 0xf8f8f8u;
-					channel_shuffle = m != 0xf8f8f8u && m != 0;
+					channel_shuffle = channel_shuffle || (m != 0xf8f8f8u && m != 0);
 				}
 				pass.channel_shuffle = channel_shuffle;
 
 				// Field-aware rendering, or super-sampled textures in the
-				// pass, keep the pass super-sampled (gs/gs_interface.cpp:225-260).
-				if (sampling_rate_y_log2 != 0 && !field_aware && !(ssaa_textures && has_ss_textures))
+				// pass, keep the pass super-sampled; channel shuffles, depth
+				// feedback and frame/depth aliasing with depth writes do not
+				// (gs/gs_interface.cpp:225-260).
+				if ((sampling_rate_x_log2 | sampling_rate_y_log2) != 0 && !field_aware && !(ssaa_textures && has_ss_textures))
 				{
-					if (channel_shuffle || (inst.z_write && zbuf.zbp == frame.fbp))
+					if (channel_shuffle || inst.z_feedback || (inst.z_write && zbuf.zbp == frame.fbp))
 					{
 						pass.sampling_rate_x_log2 = 0;
 						pass.sampling_rate_y_log2 = 0;
@@ -757,6 +656,9 @@ struct pgs_gs
 			stats.num_render_passes++;
 			stats.num_primitives += primitive_count;
 			stats.num_flushes_by_reason[reason & 7]++;
+			pending.prims += primitive_count;
+			pending.passes += rp.num_instances;
+			check_pending_work();
 		}
 
 		Instance keep = instances[current_instance];
@@ -764,36 +666,45 @@ struct pgs_gs
 			inst = Instance();
 		instances[0].frame = keep.frame;
 		instances[0].zbuf = keep.zbuf;
+		instances[0].fb_pw = keep.fb_pw;
+		instances[0].fb_ph = keep.fb_ph;
+		instances[0].z_pw = keep.z_pw;
+		instances[0].z_ph = keep.z_ph;
 		num_instances = 1;
 		current_instance = 0;
 		primitive_count = 0;
 		state_vectors.clear();
 		textures.clear();
-		texture_map.clear();
+		tex_entries.clear();
 		pending_palette_updates = 0;
 		has_aa1 = false;
 		has_scanmsk = false;
 		has_mipmap = false;
 		has_ss_textures = false;
+		last_para_candidate = false;
+		pass_feedback = PASS_FEEDBACK_NONE;
+		has_hazardous_short_term = false;
+		has_optimized_short_term = false;
 		template_dirty = true;
-		tracker.clear();
+		dirty = DIRTY_ALL;
+		for (uint16_t p : pass_tex_pages)
+			pass_tex_blocks[p] = 0;
+		pass_tex_pages.clear();
 		reserve_buffers();
 	}
 
+	// GSInterface::flush (gs/gs_interface.cpp:4257-4264).
 	void flush()
 	{
 		flush_pending_transfer(true);
-		flush_render_pass(FLUSH_EXPLICIT);
-		int r = ops->flush_submit(be);
-		if (r != 0)
-			sticky_error = r;
+		tracker.mark_submission(FLUSH_EXPLICIT);
+		submit();
 	}
 
 	// ---------------------------------------------------------------
 	// Transfers (gs/gs_interface.cpp:2979-3276).
 	void init_transfer()
 	{
-		transfer_serial++;
 		flush_pending_transfer(false);
 		xfer.bitbltbuf = regs[R_BITBLTBUF];
 		xfer.trxpos = regs[R_TRXPOS];
@@ -808,12 +719,16 @@ struct pgs_gs
 
 		if (xdir == LOCAL_TO_LOCAL)
 		{
-			PageSpan dst = page_span(dbp, dsax, dsay, rrw, rrh, dbw, dpsm);
-			PageSpan src = page_span(sbp, ssax, ssay, rrw, rrh, sbw, spsm);
-			if (tracker.any(dst, PageTracker::FB_WRITE | PageTracker::FB_READ | PageTracker::TEX_READ) ||
-			    tracker.any(src, PageTracker::FB_WRITE))
+			// init_transfer (gs/gs_interface.cpp:3168-3202).
+			const PageRect dst = compute_page_rect(dbp, dsax, dsay, rrw, rrh, dbw, dpsm);
+			const PageRect src = compute_page_rect(sbp, ssax, ssay, rrw, rrh, sbw, spsm);
+			tracker.mark_transfer_copy(dst, src);
+			tracker.invalidate_texture_cache(clut_instance);
+			if (pass_texture_hit(dst))
 				flush_render_pass(FLUSH_COPY_HAZARD);
-			tracker.clear_may_super_sample(dst);
+			pending.copies++;
+			pending.copy_threads += uint64_t(rrw) * rrh;
+			check_pending_work();
 			pgs_copy_desc d = {};
 			d.bitbltbuf = xfer.bitbltbuf;
 			d.trxpos = xfer.trxpos;
@@ -834,9 +749,14 @@ struct pgs_gs
 		}
 		else if (xdir == LOCAL_TO_HOST)
 		{
-			PageSpan src = page_span(sbp, ssax, ssay, rrw, rrh, sbw, spsm);
-			if (tracker.any(src, PageTracker::FB_WRITE))
-				flush_render_pass(FLUSH_HOST_ACCESS);
+			// Unsubmitted writes to the source: submit first (init_transfer,
+			// gs/gs_interface.cpp:3214-3245).
+			const PageRect src = compute_page_rect(sbp, ssax, ssay, rrw, rrh, sbw, spsm);
+			if (tracker.host_read_pending(src))
+			{
+				tracker.mark_submission(FLUSH_HOST_ACCESS);
+				submit();
+			}
 			uint32_t bytes = uint32_t((uint64_t(rrw) * rrh * psm_bits_per_pixel(spsm)) / 8);
 			xfer.fifo.assign((bytes + 15) & ~15u, 0);
 			xfer.fifo_offset = 0;
@@ -884,10 +804,24 @@ struct pgs_gs
 			uint32_t rrw = field(xfer.trxreg, 0, 12), rrh = field(xfer.trxreg, 32, 12);
 			uint32_t dbp = field(xfer.bitbltbuf, 32, 14), dbw = field(xfer.bitbltbuf, 48, 6), dpsm = field(xfer.bitbltbuf, 56, 6);
 			uint32_t dsax = field(xfer.trxpos, 32, 11), dsay = field(xfer.trxpos, 48, 11);
-			PageSpan dst = page_span(dbp, dsax, dsay, rrw, rrh, dbw, dpsm);
-			if (tracker.any(dst, PageTracker::FB_WRITE | PageTracker::FB_READ | PageTracker::TEX_READ))
+			// flush_pending_transfer (gs/gs_interface.cpp:2979-3148): a whole
+			// single-page upload with no unsubmitted GPU work on its page is
+			// written by the host at once, otherwise it is a tracked transfer.
+			const PageRect dst = compute_page_rect(dbp, dsax, dsay, rrw, rrh, dbw, dpsm);
+			const uint64_t have = uint64_t(xfer.payload.size()), from = xfer.flushed_qwords;
+			const bool host_copy = dst.page_width == 1 && dst.page_height == 1 && from == 0 &&
+			                       have == xfer.required_qwords && !tracker.host_write_pending(dst);
+			if (host_copy)
+				tracker.commit_host_write(dst);
+			else
+				tracker.mark_transfer_write(dst);
+			if (pass_texture_hit(dst))
 				flush_render_pass(FLUSH_COPY_HAZARD);
-			tracker.clear_may_super_sample(dst);
+			pending.copies++;
+			pending.copy_threads += uint64_t(rrw) * rrh;
+			if (!host_copy)
+				pending.scratch += have * sizeof(uint64_t);
+			check_pending_work();
 
 			pgs_copy_desc d = {};
 			d.bitbltbuf = xfer.bitbltbuf;
@@ -904,6 +838,7 @@ struct pgs_gs
 			stats.num_copies++;
 			xfer.flushed_qwords = uint32_t(xfer.payload.size());
 			template_dirty = true;
+			tracker.invalidate_texture_cache(clut_instance);
 		}
 
 		if (!keep_alive)
@@ -962,16 +897,24 @@ struct pgs_gs
 		}
 		else
 		{
+			// The reference's page rectangle for a 4-bit CLUT in rectangle
+			// layout is 8 x 4 (gs/gs_interface.cpp:624-635).
 			pw = t.csm ? 16 : 8;
-			ph = t.csm ? 1 : 2;
+			ph = t.csm ? 1 : 4;
 		}
 
 		uint64_t texclut = regs[R_TEXCLUT];
 		uint32_t cbw = field(texclut, 0, 6), cou = field(texclut, 6, 6), cov = field(texclut, 12, 10);
 		uint32_t xo = t.csm ? cou * 16 : 0, yo = t.csm ? cov : 0;
-		PageSpan src = page_span(t.cbp, xo, yo, pw, ph, t.csm ? cbw : 1, cpsm);
-		if (tracker.any(src, PageTracker::FB_WRITE))
-			flush_render_pass(FLUSH_CLUT_HAZARD);
+		// The CLUT source is read like a texture, and its cached copy goes
+		// stale with the CSA banks it fills (handle_clut_upload,
+		// gs/gs_interface.cpp:620-683).
+		const PageRect src = compute_page_rect(t.cbp, xo, yo, pw, ph, cbw, cpsm);
+		uint32_t csa_mask = is8 ? (0xffffu << csa) : (1u << csa);
+		if (cpsm == PSMCT32)
+			csa_mask |= csa_mask << 16;
+		tracker.mark_texture_read(src);
+		tracker.register_clut_read(src, csa_mask);
 
 		// Normalise TEX0 to the fields that affect the palette load.
 		uint64_t tex0 = regs[R_TEX0_1 + ctx];
@@ -1024,10 +967,34 @@ struct pgs_gs
 		m |= (uint64_t(base & 0x3fff) << 40) | (uint64_t(row & 0x3f) << 54);
 		regs[R_MIPTBP1_1 + ctx] = m;
 		template_dirty = true;
+		dirty |= DIRTY_TEX | DIRTY_PRIM_TEMPLATE;
 	}
 
 	// ---------------------------------------------------------------
-	// Register writes.
+	// Register writes (the a_d_* handlers, gs/gs_interface.cpp:3506-3990):
+	// each register marks the derived state it feeds dirty when its value
+	// changes (update_internal_register).
+	void set_state_reg(uint32_t addr, uint64_t v, uint32_t flags)
+	{
+		if (regs[addr] != v)
+		{
+			regs[addr] = v;
+			dirty |= flags;
+		}
+	}
+
+	void set_prim_reg(uint64_t v)
+	{
+		// PRIM with PRMODECONT.AC = 1, or PRMODE's attributes with the current
+		// primitive type (a_d_PRIM / a_d_PRMODE).
+		if (field(regs[R_PRIM], 9, 1) != field(v, 9, 1))
+			dirty |= DIRTY_DEGENERATE | DIRTY_PRIM_TEMPLATE | DIRTY_TEX | DIRTY_FB | DIRTY_FEEDBACK | DIRTY_SCISSOR;
+		set_state_reg(R_PRIM, v, DIRTY_FEEDBACK | DIRTY_PRIM_TEMPLATE | DIRTY_TEX | DIRTY_STATE);
+		if (!field(regs[R_PRIM], 4, 1))
+			dirty &= ~DIRTY_TEX;
+		update_offsets();
+	}
+
 	void write_register(uint32_t addr, uint64_t v)
 	{
 		addr &= 0x7f;
@@ -1046,15 +1013,12 @@ struct pgs_gs
 		{
 		case R_PRIM:
 		{
-			bool ctxt_change = field(regs[R_PRIM], 9, 1) != field(v, 9, 1);
 			if (field(regs[R_PRMODECONT], 0, 1))
-			{
-				regs[R_PRIM] = v & 0x7ffull;
-				if (ctxt_change)
-					update_offsets();
-			}
+				set_prim_reg(v);
 			else
 			{
+				if ((regs[R_PRIM] & 7ull) != (v & 7ull) && field(v, 7, 1))
+					dirty |= DIRTY_PRIM_TEMPLATE;
 				regs[R_PRIM] = (regs[R_PRIM] & ~7ull) | (v & 7ull);
 			}
 			template_dirty = true;
@@ -1064,10 +1028,7 @@ struct pgs_gs
 		case R_PRMODE:
 			if (!field(regs[R_PRMODECONT], 0, 1))
 			{
-				bool ctxt_change = field(regs[R_PRIM], 9, 1) != field(v, 9, 1);
-				regs[R_PRIM] = (v & ~7ull & 0x7ffull) | (regs[R_PRIM] & 7ull);
-				if (ctxt_change)
-					update_offsets();
+				set_prim_reg((v & ~7ull) | (regs[R_PRIM] & 7ull));
 				template_dirty = true;
 			}
 			break;
@@ -1080,9 +1041,11 @@ struct pgs_gs
 		case R_XYZF3: vertex_kick_xyzf(v); drawing_kick(true); break;
 		case R_XYZ3: vertex_kick_xyz(v); drawing_kick(true); break;
 		case R_TEX0_1: case R_TEX0_2:
-			regs[addr] = v;
+			// a_d_TEX0 + handle_tex0_write (gs/gs_interface.cpp:802-805).
+			set_state_reg(addr, v, DIRTY_FEEDBACK | DIRTY_STATE | DIRTY_PRIM_TEMPLATE | DIRTY_TEX);
 			template_dirty = true;
 			handle_clut_upload(addr - R_TEX0_1);
+			tracker.flush_if_memory_pressure();
 			handle_miptbl_gen(addr - R_TEX0_1);
 			break;
 		case R_TEX2_1: case R_TEX2_2:
@@ -1095,12 +1058,51 @@ struct pgs_gs
 			write_register(R_TEX0_1 + ctx, t);
 			break;
 		}
+		case R_CLAMP_1: case R_CLAMP_2: case R_TEX1_1: case R_TEX1_2:
+			set_state_reg(addr, v, DIRTY_FEEDBACK | DIRTY_PRIM_TEMPLATE | DIRTY_TEX);
+			template_dirty = true;
+			break;
+		case R_SCANMSK:
+			set_state_reg(addr, v, DIRTY_PRIM_TEMPLATE);
+			template_dirty = true;
+			break;
+		case R_MIPTBP1_1: case R_MIPTBP1_2: case R_MIPTBP2_1: case R_MIPTBP2_2: case R_TEXA:
+			set_state_reg(addr, v, DIRTY_PRIM_TEMPLATE | DIRTY_TEX);
+			template_dirty = true;
+			break;
+		case R_SCISSOR_1: case R_SCISSOR_2:
+			set_state_reg(addr, v, DIRTY_SCISSOR | DIRTY_DEGENERATE);
+			template_dirty = true;
+			break;
+		case R_ALPHA_1: case R_ALPHA_2:
+			set_state_reg(addr, v, DIRTY_STATE | DIRTY_PRIM_TEMPLATE | DIRTY_DEGENERATE);
+			template_dirty = true;
+			break;
+		case R_DIMX: case R_DTHE: case R_COLCLAMP: case R_PABE: case R_FBA_1: case R_FBA_2:
+			set_state_reg(addr, v, DIRTY_STATE | DIRTY_PRIM_TEMPLATE);
+			template_dirty = true;
+			break;
+		case R_TEST_1: case R_TEST_2:
+			set_state_reg(addr, v, DIRTY_DEGENERATE | DIRTY_STATE | DIRTY_PRIM_TEMPLATE);
+			template_dirty = true;
+			break;
+		case R_FRAME_1: case R_FRAME_2:
+			set_state_reg(addr, v, DIRTY_DEGENERATE | DIRTY_FEEDBACK | DIRTY_TEX | DIRTY_FB | DIRTY_PRIM_TEMPLATE |
+			                           DIRTY_SCISSOR);
+			template_dirty = true;
+			break;
+		case R_ZBUF_1: case R_ZBUF_2:
+			set_state_reg(addr, v, DIRTY_FEEDBACK | DIRTY_DEGENERATE | DIRTY_TEX | DIRTY_FB | DIRTY_PRIM_TEMPLATE);
+			template_dirty = true;
+			break;
 		case R_XYOFFSET_1: case R_XYOFFSET_2:
 			regs[addr] = v;
 			update_offsets();
 			break;
 		case R_TEXFLUSH:
-			template_dirty = true;
+			// Counted only when a held texture is next used (a_d_TEXFLUSH,
+			// gs/gs_interface.cpp:3778-3793).
+			texflush_pending = true;
 			break;
 		case R_BITBLTBUF: case R_TRXPOS: case R_TRXREG:
 			regs[addr] = v;
@@ -1122,11 +1124,8 @@ struct pgs_gs
 			break;
 		}
 		default:
-			if (regs[addr] != v)
-			{
-				regs[addr] = v;
-				template_dirty = true;
-			}
+			// PRMODECONT, TEXCLUT, FOGCOL and the rest: stored, no derived state.
+			regs[addr] = v;
 			break;
 		}
 	}
@@ -1249,51 +1248,73 @@ struct pgs_gs
 		return false;
 	}
 
-	// check_frame_buffer_state (gs/gs_interface.cpp:935-1023).
+	// check_frame_buffer_state (gs/gs_interface.cpp:935-1023).  A FRAME / ZBUF
+	// change with primitives in the pass moves to a matching instance or opens
+	// a new one (the texture cache is checked then), unless short-term cached
+	// textures or a full instance table force a flush.
 	void check_frame_buffer_state()
 	{
-		// With no register written and no flush since the last call the
-		// instance already matches FRAME / ZBUF.
-		if (fb_state_serial == reg_serial && fb_state_epoch == fb_epoch)
+		if (!(dirty & DIRTY_FB))
 			return;
-		uint64_t frame = ctx_reg(R_FRAME_1), zbuf = ctx_reg(R_ZBUF_1);
+		dirty &= ~DIRTY_FB;
+		const uint64_t frame = ctx_reg(R_FRAME_1), zbuf = ctx_reg(R_ZBUF_1);
 		Instance *inst = &instances[current_instance];
 		bool fb_delta = !frame_compat(inst->frame, frame);
 		bool z_delta = !zbuf_compat(inst->zbuf, zbuf);
 		if (primitive_count && (fb_delta || (z_delta && inst->z_sensitive)))
 		{
-			uint32_t found = num_instances;
-			for (uint32_t i = 0; i < num_instances; i++)
-			{
-				auto &t = instances[i];
-				if (frame_compat(t.frame, frame) && (!t.z_sensitive || zbuf_compat(t.zbuf, zbuf)))
+			current_instance = num_instances;
+			const bool can_fuse = !has_hazardous_short_term;
+			if (can_fuse)
+				for (uint32_t i = 0; i < num_instances; i++)
 				{
-					found = i;
-					break;
+					auto &t = instances[i];
+					if (frame_compat(t.frame, frame) && (!t.z_sensitive || zbuf_compat(t.zbuf, zbuf)))
+					{
+						current_instance = i;
+						break;
+					}
 				}
-			}
-			if (found == num_instances)
+			if (current_instance == num_instances)
 			{
-				if (num_instances < PGS_MAX_RENDER_PASS_INSTANCES)
+				if (num_instances < PGS_MAX_RENDER_PASS_INSTANCES && can_fuse)
 				{
-					instances[num_instances] = Instance();
+					instances[current_instance] = Instance();
 					num_instances++;
+					tracker.invalidate_texture_cache(clut_instance);
+					if (has_optimized_short_term)
+						tracker.invalidate_fb_write_short_term_references();
 				}
 				else
 				{
 					flush_pending_transfer(true);
 					flush_render_pass(FLUSH_FB_POINTER);
-					found = 0;
 				}
 			}
-			current_instance = found;
+			fb_delta = true;
+			z_delta = true;
+			last_para_candidate = false;
 			inst = &instances[current_instance];
-			template_dirty = true;
 		}
-		inst->frame = frame;
-		inst->zbuf = zbuf;
-		fb_state_serial = reg_serial;
-		fb_state_epoch = fb_epoch;
+		if (fb_delta)
+		{
+			const Layout L = psm_layout(field(frame, 24, 6));
+			inst->fb_pw = L.pw;
+			inst->fb_ph = L.ph;
+			inst->frame = frame;
+			dirty |= DIRTY_POTENTIAL_FEEDBACK_REGION;
+		}
+		if (z_delta)
+		{
+			const Layout L = psm_layout(field(zbuf, 24, 4) | 0x30u);
+			inst->z_pw = L.pw;
+			inst->z_ph = L.ph;
+			inst->zbuf = zbuf;
+			dirty |= DIRTY_POTENTIAL_FEEDBACK_REGION;
+		}
+		// Changing buffers counts as a TEXFLUSH.
+		if (fb_delta || z_delta)
+			texflush_counter++;
 	}
 
 	uint32_t find_state_vector(const pgs_state_vector &s)
@@ -1358,21 +1379,422 @@ struct pgs_gs
 		return find_state_vector(s);
 	}
 
-	// Texture descriptor for the current context (drawing_kick_update_texture,
-	// gs/gs_interface.cpp:1254-1800), without the image cache.
-	uint32_t update_texture(PageSpan *spans, uint32_t &num_spans)
+	static uint64_t texture_hash(const pgs_texture_desc &d)
 	{
-		Tex0Reg t(ctx_reg(R_TEX0_1));
-		ClampReg c(ctx_reg(R_CLAMP_1));
-		Tex1Reg tex1(ctx_reg(R_TEX1_1));
-		uint64_t texa = regs[R_TEXA];
+		const uint32_t *w = reinterpret_cast<const uint32_t *>(&d);
+		uint64_t h = 1469598103934665603ull;
+		for (size_t i = 0; i < sizeof(d) / 4; i++)
+			h = (h ^ w[i]) * 1099511628211ull;
+		return h;
+	}
+
+	static uint32_t swizzle_compat_key(uint32_t psm)
+	{
+		// Formats sharing a swizzle (swizzle_compat_key, gs/shaders/swizzle_utils.h:304-328).
+		switch (psm)
+		{
+		case PSMZ32: return 2;
+		case PSMCT16: return 3;
+		case PSMZ16: return 4;
+		case PSMCT16S: return 5;
+		case PSMZ16S: return 6;
+		case PSMT8: return 7;
+		case PSMT4: return 8;
+		case PSMZ24: return 9;
+		default: return 1;
+		}
+	}
+
+	// UV bounding box of a primitive in texels (compute_uv_bb,
+	// gs/gs_interface.cpp:2308-2384).  uvs: the vertices' UVs in 1/16 texels.
+	void compute_uv_bb(const pgs_vertex_attribute *attr, bool quad, bool conservative, int32_t uv_bb[4],
+	                   int32_t (*uvs)[2], bool *needs_perspective)
+	{
+		const Tex0Reg t0(ctx_reg(R_TEX0_1));
+		const Tex1Reg t1(ctx_reg(R_TEX1_1));
+		const PrimReg prim(regs[R_PRIM]);
+		const float fw = float((1 << int(t0.tw)) * 16), fh = float((1 << int(t0.th)) * 16);
+		int32_t local[3][2];
+		if (!uvs)
+			uvs = local;
+		if (needs_perspective)
+			*needs_perspective = false;
+		const uint32_t nv = quad ? 2 : 3;
+		if (prim.fst)
+		{
+			for (uint32_t i = 0; i < nv; i++)
+			{
+				uvs[i][0] = attr[i].u;
+				uvs[i][1] = attr[i].v;
+			}
+		}
+		else
+		{
+			if (!quad && needs_perspective && (attr[0].q != attr[1].q || attr[1].q != attr[2].q))
+				*needs_perspective = true;
+			for (uint32_t i = 0; i < nv; i++)
+			{
+				const float inv = 1.0f / attr[i].q;
+				uvs[i][0] = int32_t(fw * (attr[i].s * inv));
+				uvs[i][1] = int32_t(fh * (attr[i].t * inv));
+			}
+		}
+		int32_t lo[2] = { std::min(uvs[0][0], uvs[1][0]), std::min(uvs[0][1], uvs[1][1]) };
+		int32_t hi[2] = { std::max(uvs[0][0], uvs[1][0]), std::max(uvs[0][1], uvs[1][1]) };
+		if (!quad)
+			for (int k = 0; k < 2; k++)
+			{
+				lo[k] = std::min(lo[k], uvs[2][k]);
+				hi[k] = std::max(hi[k], uvs[2][k]);
+			}
+		if (conservative)
+		{
+			if (t1.mmag)
+			{
+				// A linear filter reaches half a texel further.
+				for (int k = 0; k < 2; k++)
+				{
+					lo[k] -= 1 << (SUBPIXEL_BITS - 1);
+					hi[k] += (1 << (SUBPIXEL_BITS - 1)) - 1;
+				}
+			}
+			else if (!prim.fst)
+			{
+				for (int k = 0; k < 2; k++)
+				{
+					lo[k] -= 1;
+					hi[k] += 1;
+				}
+			}
+		}
+		uv_bb[0] = lo[0] >> SUBPIXEL_BITS;
+		uv_bb[1] = lo[1] >> SUBPIXEL_BITS;
+		uv_bb[2] = hi[0] >> SUBPIXEL_BITS;
+		uv_bb[3] = hi[1] >> SUBPIXEL_BITS;
+		if (!conservative)
+		{
+			// The last row and column are rarely drawn (raster rules).
+			uv_bb[2] = std::max(uv_bb[2] - 1, 0);
+			uv_bb[3] = std::max(uv_bb[3] - 1, 0);
+		}
+	}
+
+	// compute_has_potential_feedback (gs/gs_util.cpp:81-139): can the
+	// texture's page range reach the frame or depth buffer's base page.
+	void has_potential_feedback(bool &color, bool &depth) const
+	{
+		const Tex0Reg t0(ctx_reg(R_TEX0_1));
+		const ClampReg cl(ctx_reg(R_CLAMP_1));
+		const FrameReg fr(ctx_reg(R_FRAME_1));
+		const ZbufReg zb(ctx_reg(R_ZBUF_1));
+		const Layout L = psm_layout(t0.psm);
+		const uint32_t stride = (t0.psm == PSMT4 || t0.psm == PSMT8) ? (t0.tbw >> 1) : t0.tbw;
+		uint32_t w = 1u << t0.tw, h = 1u << t0.th;
+		const Extent ue = effective_extent(w, cl.wms, cl.minu, cl.maxu, 1);
+		const Extent ve = effective_extent(h, cl.wmt, cl.minv, cl.maxv, 1);
+		w = ue.base + ue.extent;
+		h = ve.base + ve.extent;
+		if (w >= 1024 && t0.tbw)
+			w = std::min<uint32_t>(w, t0.tbw * BUFFER_WIDTH_SCALE);
+		const uint32_t base_block = t0.tbp0, base_page = base_block / BLOCKS_PER_PAGE;
+		uint32_t fb_page = fr.fbp, z_page = zb.zbp;
+		if (fb_page * BLOCKS_PER_PAGE < base_block)
+			fb_page += NUM_PAGES;
+		if (z_page * BLOCKS_PER_PAGE < base_block)
+			z_page += NUM_PAGES;
+		uint32_t last = base_page + ((w - 1) >> L.pw) + ((h - 1) >> L.ph) * stride;
+		if (base_block % BLOCKS_PER_PAGE)
+			last++;
+		last -= base_page;
+		fb_page -= base_page;
+		z_page -= base_page;
+		color = last >= fb_page;
+		depth = last >= z_page;
+	}
+
+	struct Extent
+	{
+		uint32_t base, extent;
+	};
+
+	// compute_effective_texture_extent (gs/gs_util.cpp:31-79).
+	static Extent effective_extent(uint32_t extent, uint32_t wrap, uint32_t lo, uint32_t hi, uint32_t levels)
+	{
+		uint32_t base = 0;
+		if (wrap == WRAP_REGION_CLAMP)
+		{
+			lo = std::min(lo, hi);
+			extent = std::max(hi, lo) - lo + 1;
+			if (levels > 1)
+			{
+				const uint32_t mask = (1u << (levels - 1)) - 1u;
+				extent += lo & mask;
+				lo &= ~mask;
+				extent = (extent + mask) & ~mask;
+			}
+			base = lo;
+		}
+		else if (wrap == WRAP_REGION_REPEAT)
+		{
+			const uint32_t msk = lo, fix = hi;
+			if (msk == 0)
+			{
+				extent = 1;
+				base = fix;
+			}
+			else
+			{
+				const uint32_t msb = 31u - uint32_t(__builtin_clz(msk));
+				const uint32_t lsb = fix ? uint32_t(__builtin_ctz(fix)) : 32u;
+				if (lsb > msb)
+				{
+					extent = std::min(1u << (msb + 1), extent);
+					base = fix;
+				}
+			}
+		}
+		return { base, extent };
+	}
+
+	// update_color_feedback_state (gs/gs_interface.cpp:2141-2306).
+	void update_color_feedback_state()
+	{
+		if (!(dirty & DIRTY_FEEDBACK))
+		{
+			// In feedback every draw re-evaluates its texture state.
+			if (is_color_feedback || is_depth_feedback)
+				dirty |= DIRTY_PRIM_TEMPLATE | DIRTY_TEX;
+			return;
+		}
+		dirty &= ~DIRTY_FEEDBACK;
+		is_color_feedback = is_depth_feedback = is_awkward_color_feedback = false;
+		is_potential_feedback = is_potential_channel_shuffle = false;
+		const PrimReg prim(regs[R_PRIM]);
+		if (!prim.tme)
+			return;
+		const Tex0Reg t0(ctx_reg(R_TEX0_1));
+		const Tex1Reg t1(ctx_reg(R_TEX1_1));
+		const ClampReg cl(ctx_reg(R_CLAMP_1));
+		const FrameReg fr(ctx_reg(R_FRAME_1));
+		const ZbufReg zb(ctx_reg(R_ZBUF_1));
+		const Instance &inst = instances[current_instance];
+		// Mipmapping is left alone.
+		if (t1.mmin_has_mipmap() && t1.mxl != 0 && !hack_disable_mipmaps)
+			return;
+		uint32_t tbp0 = t0.tbp0;
+		const uint32_t tex_psm = t0.psm;
+		if (fr.psm == tex_psm && (tex_psm == PSMCT16 || tex_psm == PSMCT16S || tex_psm == PSMZ16 || tex_psm == PSMZ16S))
+			is_potential_channel_shuffle = true;
+		// A region clamp can move the effective base onto the framebuffer.
+		if (!psm_is_palette(tex_psm))
+		{
+			const Layout L = psm_layout(tex_psm);
+			if (cl.wms == WRAP_REGION_CLAMP && cl.minu != 0)
+				tbp0 += BLOCKS_PER_PAGE * (cl.minu >> L.pw);
+			if (cl.wmt == WRAP_REGION_CLAMP && cl.minv != 0)
+				tbp0 += BLOCKS_PER_PAGE * t0.tbw * (cl.minv >> L.ph);
+		}
+		const bool eq_color = tbp0 == fr.fbp * BLOCKS_PER_PAGE;
+		const bool eq_depth = tbp0 == zb.zbp * BLOCKS_PER_PAGE && (inst.z_sensitive || state_is_z_sensitive());
+		if (eq_color && (swizzle_compat_key(tex_psm) != swizzle_compat_key(fr.psm) || t0.tbw != fr.fbw))
+		{
+			// Same address, different swizzle: no caching makes sense.
+			is_color_feedback = true;
+			is_awkward_color_feedback = true;
+			return;
+		}
+		if (eq_depth && (swizzle_compat_key(tex_psm) != swizzle_compat_key(zb.psm | 0x30u) || t0.tbw != fr.fbw))
+			return;
+		if (cl.wms == WRAP_REGION_REPEAT || cl.wmt == WRAP_REGION_REPEAT)
+			return;
+		if (!eq_color && !eq_depth)
+		{
+			bool pc = false, pd = false;
+			has_potential_feedback(pc, pd);
+			bool existing_z_write = inst.z_write && frame_compat(inst.frame, ctx_reg(R_FRAME_1)) &&
+			                        zbuf_compat(inst.zbuf, ctx_reg(R_ZBUF_1));
+			const bool has_z_write = existing_z_write || (state_is_z_sensitive() && zb.zmsk == 0);
+			const uint32_t tex_wm = psm_word_write_mask(tex_psm);
+			const uint32_t fb_wm = psm_word_write_mask(FrameReg(inst.frame).psm);
+			const uint32_t z_wm = psm_word_write_mask(ZbufReg(inst.zbuf).psm);
+			if ((tex_wm & fb_wm) == 0)
+				pc = false;
+			if ((tex_wm & z_wm) == 0 || !has_z_write)
+				pd = false;
+			is_potential_feedback = pc || pd;
+			if (is_potential_feedback)
+			{
+				const Layout L = psm_layout(t0.psm);
+				potential.base_page = t0.tbp0 / BLOCKS_PER_PAGE;
+				potential.pw = L.pw;
+				potential.ph = L.ph;
+				potential.page_stride = (t0.psm == PSMT4 || t0.psm == PSMT8) ? (t0.tbw >> 1) : t0.tbw;
+				potential.width_bias = (t0.tbp0 & (BLOCKS_PER_PAGE - 1)) ? 1 : 0;
+				uint32_t safe = UINT32_MAX;
+				if (pc)
+					safe = std::min<uint32_t>(safe, (fr.fbp - potential.base_page) & (NUM_PAGES - 1));
+				if (pd)
+					safe = std::min<uint32_t>(safe, (zb.zbp - potential.base_page) & (NUM_PAGES - 1));
+				if (potential.width_bias >= safe)
+					is_potential_feedback = false;
+				else
+					potential.max_safe_page = safe - 1 - potential.width_bias;
+			}
+		}
+		else
+		{
+			is_color_feedback = eq_color && (psm_word_write_mask(tex_psm) & psm_word_write_mask(fr.psm)) != 0;
+			is_depth_feedback = eq_depth && (psm_word_write_mask(tex_psm) & psm_word_write_mask(zb.psm)) != 0;
+			dirty |= DIRTY_PRIM_TEMPLATE | DIRTY_TEX;
+		}
+	}
+
+	// deduce_color_feedback_mode (gs/gs_interface.cpp:2388-2471).
+	uint32_t deduce_feedback_mode(const pgs_vertex_position *pos, const pgs_vertex_attribute *attr, uint32_t nv,
+	                              bool quad, int32_t uv_bb[4], const int32_t *bb)
+	{
+		if (!(nv == 3 || (quad && nv == 2)))
+			return FEEDBACK_NONE;
+		if (is_awkward_color_feedback)
+			return FEEDBACK_BYPASS_HAZARDS;
+		const Tex0Reg t0(ctx_reg(R_TEX0_1));
+		const Tex1Reg t1(ctx_reg(R_TEX1_1));
+		const ClampReg cl(ctx_reg(R_CLAMP_1));
+		const int width = 1 << int(t0.tw), height = 1 << int(t0.th);
+		bool needs_perspective = false;
+		int32_t uvs[3][2] = {};
+		compute_uv_bb(attr, quad, true, uv_bb, uvs, &needs_perspective);
+		if (needs_perspective)
+			return FEEDBACK_SLICED;
+		if (cl.wms == WRAP_REGION_CLAMP)
+		{
+			if (bb[0] < int(cl.minu) || bb[2] > int(cl.maxu))
+				return FEEDBACK_SLICED;
+		}
+		else if (bb[2] >= width)
+			return FEEDBACK_SLICED;
+		if (cl.wmt == WRAP_REGION_CLAMP)
+		{
+			if (bb[1] < int(cl.minv) || bb[3] > int(cl.maxv))
+				return FEEDBACK_SLICED;
+		}
+		else if (bb[3] >= height)
+			return FEEDBACK_SLICED;
+		int32_t dmin[2], dmax[2];
+		for (int k = 0; k < 2; k++)
+		{
+			const int32_t p0 = k ? pos[0].y : pos[0].x, p1 = k ? pos[1].y : pos[1].x;
+			dmin[k] = std::min(uvs[0][k] - p0, uvs[1][k] - p1);
+			dmax[k] = std::max(uvs[0][k] - p0, uvs[1][k] - p1);
+			if (!quad)
+			{
+				const int32_t p2 = k ? pos[2].y : pos[2].x;
+				dmin[k] = std::min(dmin[k], uvs[2][k] - p2);
+				dmax[k] = std::max(dmax[k], uvs[2][k] - p2);
+			}
+		}
+		const int32_t min2 = std::min(dmin[0], dmin[1]), max2 = std::max(dmax[0], dmax[1]);
+		if (t1.mmag)
+		{
+			if (min2 != (1 << (SUBPIXEL_BITS - 1)) || max2 != (1 << (SUBPIXEL_BITS - 1)))
+				return FEEDBACK_SLICED;
+		}
+		else if (min2 < 0 || max2 >= (1 << SUBPIXEL_BITS))
+			return FEEDBACK_SLICED;
+		return FEEDBACK_PIXEL;
+	}
+
+	// Texture page reads (texture_page_rects_read_full / _region /
+	// _safe_region, gs/gs_interface.cpp:1151-1206).
+	void texture_read_full()
+	{
+		for (uint32_t l = 0; l < tex_num_rects; l++)
+			tracker.mark_texture_read(tex_rects[l]);
+	}
+
+	void texture_read_safe_region()
+	{
+		PageRect r;
+		r.base_page = potential.base_page;
+		r.page_width = potential.max_safe_page + 1;
+		r.page_height = 1;
+		r.page_stride = 0;
+		r.block_mask = 0xffffffffu;
+		r.write_mask = 0xffffffffu;
+		tracker.mark_texture_read(r);
+	}
+
+	void texture_read_region(const int32_t *uv_bb)
+	{
+		const Tex0Reg t0(ctx_reg(R_TEX0_1));
+		const uint32_t max_px = uint32_t(uv_bb[2]) >> potential.pw, max_py = uint32_t(uv_bb[3]) >> potential.ph;
+		if (!(dirty & DIRTY_POTENTIAL_FEEDBACK_REGION))
+		{
+			// Known to stay below the framebuffer pages.
+			if (max_px + max_py * potential.page_stride <= potential.max_safe_page)
+				return;
+		}
+		dirty &= ~DIRTY_POTENTIAL_FEEDBACK_REGION;
+		PageRect r;
+		r.base_page = t0.tbp0 / BLOCKS_PER_PAGE;
+		r.page_width = max_px + 1 + potential.width_bias;
+		r.page_height = max_py + 1;
+		r.page_stride = potential.page_stride;
+		r.block_mask = 0xffffffffu;
+		r.write_mask = 0xffffffffu;
+		tracker.mark_texture_read(r);
+	}
+
+	// mark_render_pass_has_texture_feedback (gs/gs_interface.cpp:909-933).
+	void mark_pass_texture_feedback(const Tex0Reg &t0, uint32_t mode)
+	{
+		if (pass_feedback != PASS_FEEDBACK_NONE && mode != pass_feedback)
+			flush_render_pass(FLUSH_TEXTURE_HAZARD);
+		if (pass_feedback != PASS_FEEDBACK_NONE &&
+		    (t0.psm != pass_feedback_psm || (psm_is_palette(pass_feedback_psm) && pass_feedback_cpsm != t0.cpsm)))
+			flush_render_pass(FLUSH_TEXTURE_HAZARD);
+		if (pass_feedback == PASS_FEEDBACK_NONE)
+		{
+			pass_feedback = mode;
+			pass_feedback_psm = t0.psm;
+			pass_feedback_cpsm = psm_is_palette(t0.psm) ? t0.cpsm : 0;
+		}
+		if (pass_feedback == PASS_FEEDBACK_DEPTH)
+			instances[current_instance].z_feedback = true;
+	}
+
+	// Texture of the current context (drawing_kick_update_texture,
+	// gs/gs_interface.cpp:1254-1800).  The descriptor keeps what the decode
+	// depends on; hazard reads follow the reference's caching of the texture
+	// (long-term, short-term for feedback and very large images).  A draw the
+	// reference would sample from the framebuffer tile itself (pixel
+	// feedback) is drawn here as an ordinary texture read, checked like one.
+	uint32_t update_texture(uint32_t feedback_mode, const int32_t *uv_bb, const int32_t *bb)
+	{
+		if (!(dirty & DIRTY_TEX) && last_texture_index != UINT32_MAX)
+			return last_texture_index;
+		dirty &= ~DIRTY_TEX;
+		const PrimReg prim(regs[R_PRIM]);
+		const Tex0Reg t(ctx_reg(R_TEX0_1));
+		const ClampReg c(ctx_reg(R_CLAMP_1));
+		const Tex1Reg tex1(ctx_reg(R_TEX1_1));
+		const FrameReg fr(ctx_reg(R_FRAME_1));
+		const uint64_t texa = regs[R_TEXA];
+		const bool pixel_feedback = feedback_mode == FEEDBACK_PIXEL;
+		if (pixel_feedback)
+		{
+			mark_pass_texture_feedback(t, is_color_feedback ? PASS_FEEDBACK_COLOR : PASS_FEEDBACK_DEPTH);
+			feedback_mode = FEEDBACK_BYPASS_HAZARDS;
+		}
+
 		pgs_texture_desc d = {};
 		d.tbp0 = t.tbp0;
 		d.tbw = t.tbw;
 		d.psm = t.psm;
 		d.tw_log2 = std::min<uint32_t>(t.tw, 10);
 		d.th_log2 = std::min<uint32_t>(t.th, 10);
-		uint32_t cpsm = t.cpsm == PSMCT24 ? PSMCT32 : t.cpsm;
+		const uint32_t cpsm = t.cpsm == PSMCT24 ? PSMCT32 : t.cpsm;
+		uint32_t csa_mask = 0;
 		if (psm_is_palette(t.psm))
 		{
 			d.cpsm = cpsm;
@@ -1384,6 +1806,13 @@ struct pgs_gs
 				d.ta0 = field(texa, 0, 8);
 				d.ta1 = field(texa, 32, 8);
 			}
+			csa_mask = (t.psm == PSMT8 || t.psm == PSMT8H) ? 0xffffu : 1u;
+			csa_mask <<= d.csa;
+			if (cpsm == PSMCT32)
+			{
+				csa_mask &= 0xffffu;
+				csa_mask |= csa_mask << 16;
+			}
 		}
 		else if (t.psm != PSMCT32 && t.psm != PSMZ32)
 		{
@@ -1391,75 +1820,246 @@ struct pgs_gs
 			d.ta0 = field(texa, 0, 8);
 			d.ta1 = field(texa, 32, 8);
 		}
-		d.wms = c.wms;
-		d.wmt = c.wmt;
-		if (c.wms >= WRAP_REGION_CLAMP)
-		{
-			d.minu = c.minu;
-			d.maxu = c.maxu;
-		}
-		if (c.wmt >= WRAP_REGION_CLAMP)
-		{
-			d.minv = c.minv;
-			d.maxv = c.maxv;
-		}
 
-		uint32_t w = 1u << d.tw_log2, h = 1u << d.th_log2;
-		spans[0] = page_span(t.tbp0, 0, 0, w, h, t.tbw ? t.tbw : 1, t.psm);
-		// Large dummy TW/TH with a small stride cover far more pages than are sampled
-		// (compute_has_potential_feedback, gs/gs_util.cpp:81-139).
-		if (w >= 1024 && t.tbw)
-			spans[0] = page_span(t.tbp0, 0, 0, std::min<uint32_t>(w, t.tbw * 64), h, t.tbw, t.psm);
+		uint32_t wms = c.wms, wmt = c.wmt, minu = c.minu, maxu = c.maxu, minv = c.minv, maxv = c.maxv;
+		bool long_term = true;
+		if (feedback_mode == FEEDBACK_SLICED)
+		{
+			auto overlap_empty = [](int32_t x0, int32_t y0, int32_t x1, int32_t y1) { return x0 > x1 || y0 > y1; };
+			if (prim.prim == PRIM_SPRITE)
+			{
+				long_term = !current_is_channel_shuffle;
+				if (long_term && fr.fbw >= 4 && uv_bb[2] - uv_bb[0] < 16 && uv_bb[3] - uv_bb[1] < 16 &&
+				    bb[2] - bb[0] < 16 && bb[3] - bb[1] < 16)
+				{
+					const int32_t hx0 = std::max(uv_bb[0], bb[0]), hy0 = std::max(uv_bb[1], bb[1]);
+					const int32_t hx1 = std::min(uv_bb[2], bb[2]), hy1 = std::min(uv_bb[3], bb[3]);
+					long_term = (hx1 + 64 < hx0) || (hy1 + 64 < hy0);
+				}
+				if (long_term && tex1.mmag)
+				{
+					// In-place blur at a tiny bias.
+					const int u_off = std::abs(uv_bb[0] - bb[0]), v_off = std::abs(uv_bb[1] - bb[1]);
+					const int u_size = uv_bb[2] - uv_bb[0] - 2, v_size = uv_bb[3] - uv_bb[1] - 2;
+					if (u_off <= 1 && v_off <= 1 && u_size == bb[2] - bb[0] && v_size == bb[3] - bb[1])
+						long_term = false;
+				}
+			}
+			else if (wms == WRAP_REGION_CLAMP && wmt == WRAP_REGION_CLAMP)
+			{
+				long_term = overlap_empty(std::max(int32_t(minu), bb[0]), std::max(int32_t(minv), bb[1]),
+				                          std::min(int32_t(maxu), bb[2]), std::min(int32_t(maxv), bb[3]));
+			}
+			else if (last_para_candidate)
+			{
+				long_term = overlap_empty(std::max(uv_bb[0], bb[0]), std::max(uv_bb[1], bb[1]),
+				                          std::min(uv_bb[2], bb[2]), std::min(uv_bb[3], bb[3]));
+			}
+			else
+				long_term = false;
+		}
+		else if (feedback_mode == FEEDBACK_BYPASS_HAZARDS)
+			long_term = false;
 
-		// Mip chain: MXL only counts with a mipmapping MMIN
-		// (gs/gs_interface.cpp:1538-1582); levels stop at a 1-texel side.
-		d.levels = 1;
-		if (tex1.mmin_has_mipmap() && !hack_disable_mipmaps)
-			d.levels = std::min<uint32_t>(std::min<uint32_t>(tex1.mxl + 1, std::min(d.tw_log2, d.th_log2) + 1), 7);
+		const uint32_t width = 1u << t.tw, height = 1u << t.th;
+		if (is_potential_feedback && width > t.tbw * BUFFER_WIDTH_SCALE && t.tbw != 0 && height > (1u << psm_layout(t.psm).ph))
+		{
+			// A texture wider than its stride: clamp to the stride.
+			if (wms == WRAP_CLAMP || wms == WRAP_REPEAT)
+			{
+				wms = WRAP_REGION_CLAMP;
+				minu = 0;
+				maxu = t.tbw * BUFFER_WIDTH_SCALE - 1;
+			}
+			else if (wms == WRAP_REGION_CLAMP)
+			{
+				minu = std::min<uint32_t>(minu, t.tbw * BUFFER_WIDTH_SCALE - 1);
+				maxu = std::min<uint32_t>(maxu, t.tbw * BUFFER_WIDTH_SCALE - 1);
+			}
+		}
+		if (feedback_mode == FEEDBACK_SLICED && long_term && wms != WRAP_REGION_REPEAT && wmt != WRAP_REGION_REPEAT)
+		{
+			// Narrow to the sampled box.
+			if (wms == WRAP_REGION_CLAMP)
+			{
+				minu = uint32_t(std::max<int>(int(minu), std::min<int>(uv_bb[0], int(maxu))));
+				maxu = uint32_t(std::min<int>(int(maxu), std::max<int>(uv_bb[2], int(minu))));
+			}
+			else if (wms == WRAP_CLAMP || (uv_bb[2] < int(width) && uv_bb[0] >= 0))
+			{
+				wms = WRAP_REGION_CLAMP;
+				minu = uint32_t(std::max<int>(0, uv_bb[0]));
+				maxu = uint32_t(std::min<int>(int(width) - 1, uv_bb[2]));
+			}
+			if (wmt == WRAP_REGION_CLAMP)
+			{
+				minv = uint32_t(std::max<int>(int(minv), std::min<int>(uv_bb[1], int(maxv))));
+				maxv = uint32_t(std::min<int>(int(maxv), std::max<int>(uv_bb[3], int(minv))));
+			}
+			else if (wmt == WRAP_CLAMP || (uv_bb[3] < int(height) && uv_bb[1] >= 0))
+			{
+				wmt = WRAP_REGION_CLAMP;
+				minv = uint32_t(std::max<int>(0, uv_bb[1]));
+				maxv = uint32_t(std::min<int>(int(height) - 1, uv_bb[3]));
+			}
+		}
+		// Only the region modes stay in the descriptor; plain REPEAT and CLAMP
+		// read as CLAMP with zero bounds and the primitive's sampler bits pick
+		// between them (gs/gs_interface.cpp:1514-1528), so both share a decode.
+		if (wms < WRAP_REGION_CLAMP)
+		{
+			wms = WRAP_CLAMP;
+			minu = maxu = 0;
+		}
+		if (wmt < WRAP_REGION_CLAMP)
+		{
+			wmt = WRAP_CLAMP;
+			minv = maxv = 0;
+		}
+		d.wms = wms;
+		d.wmt = wmt;
+		d.minu = minu & 0x3ff;
+		d.maxu = maxu & 0x3ff;
+		d.minv = minv & 0x3ff;
+		d.maxv = maxv & 0x3ff;
+
+		// Mip levels sampled (compute_effective_texture_rect,
+		// gs/gs_renderer.cpp:1235-1265); MXL only counts with a mipmapping MMIN.
+		const uint32_t mxl = (tex1.mmin_has_mipmap() && !hack_disable_mipmaps) ? tex1.mxl : 0;
+		const uint32_t max_levels = std::min<uint32_t>(7, std::min(d.tw_log2, d.th_log2) + 1);
+		d.levels = std::min<uint32_t>(mxl + 1, max_levels);
+		const Extent ue = effective_extent(1u << d.tw_log2, d.wms, d.minu, d.maxu, d.levels);
+		const Extent ve = effective_extent(1u << d.th_log2, d.wmt, d.minv, d.maxv, d.levels);
+		uint32_t level_base[7] = { t.tbp0 }, level_stride[7] = { t.tbw };
 		for (uint32_t l = 1; l < d.levels; l++)
 		{
 			uint64_t m = ctx_reg(l <= 3 ? R_MIPTBP1_1 : R_MIPTBP2_1);
 			uint32_t slot = (l - 1) % 3;
-			uint32_t tbp = field(m, 20 * slot, 14), tbw = field(m, 20 * slot + 14, 6);
-			d.mip[l - 1] = tbp | (tbw << 16);
-			spans[l] = page_span(tbp, 0, 0, w >> l, h >> l, tbw ? tbw : 1, t.psm);
+			level_base[l] = field(m, 20 * slot, 14);
+			level_stride[l] = field(m, 20 * slot + 14, 6);
+			d.mip[l - 1] = level_base[l] | (level_stride[l] << 16);
 		}
-		num_spans = d.levels;
+		tex_num_rects = d.levels;
+		for (uint32_t l = 0; l < d.levels; l++)
+			tex_rects[l] = compute_page_rect(level_base[l], ue.base >> l, ve.base >> l, ue.extent >> l, ve.extent >> l,
+			                                 level_stride[l], t.psm);
+
+		// The reference reads a pixel-feedback texel from the tile it shades;
+		// read through a texture, it must not miss framebuffer writes of the
+		// pass.
+		if (pixel_feedback)
+			texture_read_full();
 
 		// Super-sampled texture: a sprite reading, at 8+ bits per texel, pages
 		// that a pass wrote (gs/gs_interface.cpp:1593-1601).
-		if (d.levels == 1 && ssaa_textures && sampling_rate_y_log2 != 0 && psm_bits_per_pixel(t.psm) >= 8 &&
-		    PrimReg(regs[R_PRIM]).prim == PRIM_SPRITE && tracker.may_super_sample(spans[0].base_page))
+		if (d.levels == 1 && ssaa_textures && psm_bits_per_pixel(t.psm) >= 8 && prim.prim == PRIM_SPRITE &&
+		    tracker.texture_may_super_sample(tex_rects[0]))
 			d.samples = 1u << (sampling_rate_x_log2 + sampling_rate_y_log2);
 
-		TextureKey key{ d };
-		auto it = texture_map.find(key);
-		if (it != texture_map.end())
-			return it->second;
-		uint32_t index = uint32_t(textures.size());
-		textures.push_back(d);
-		texture_map.emplace(key, index);
+		const uint64_t hash = texture_hash(d);
+		auto find = [&]() -> TexEntry * {
+			auto it = tex_entries.find(hash);
+			return it == tex_entries.end() ? nullptr : &it->second;
+		};
+		TexEntry *cached = find();
+		const bool skip_hazards = cached && cached->valid && cached->valid_at == texflush_counter &&
+		                          feedback_mode == FEEDBACK_NONE;
+		if (!skip_hazards)
+		{
+			if (is_potential_feedback)
+			{
+				long_term = false;
+				texture_read_region(uv_bb);
+			}
+			else if (long_term)
+				texture_read_full();
+			// The pass may have ended: look again.
+			cached = find();
+			if (cached && cached->valid && cached->long_term && !long_term)
+			{
+				texture_read_full();
+				cached = find();
+			}
+		}
+		if (!long_term)
+			has_hazardous_short_term = true;
+
+		if (last_texture_index != UINT32_MAX && !textures.empty() &&
+		    memcmp(&last_texture_desc, &d, sizeof(d)) == 0)
+		{
+			last_texture_valid_at = texflush_counter;
+			if (cached && cached->valid)
+				cached->valid_at = texflush_counter;
+			return last_texture_index;
+		}
+
+		uint32_t index;
+		if (cached && cached->valid)
+			index = cached->index;
+		else
+		{
+			if (is_potential_feedback)
+				texture_read_safe_region();
+			else if (!long_term || skip_hazards)
+				texture_read_full();
+			if (long_term)
+			{
+				// Very large images are held for this pass only.
+				const uint32_t pixels = ue.extent * ve.extent;
+				const uint32_t threshold = tracker.texture_may_super_sample(tex_rects[0]) ? 128 * 128 : 512 * 512;
+				if (d.levels == 1 && (pixels > threshold || ue.extent >= 1024 || ve.extent >= 1024))
+				{
+					long_term = false;
+					has_optimized_short_term = true;
+				}
+			}
+			if (!tracker.find_texture(hash))
+			{
+				if (long_term)
+					tracker.register_texture(tex_rects, d.levels, csa_mask, clut_instance, hash);
+				else
+					tracker.register_short_term_texture(tex_rects, d.levels, hash);
+			}
+			index = uint32_t(textures.size());
+			if (cached)
+			{
+				cached->valid_at = texflush_counter;
+				cached->index = index;
+				cached->valid = true;
+			}
+			else
+				tex_entries[hash] = { index, texflush_counter, long_term, true };
+			textures.push_back(d);
+			for (uint32_t l = 0; l < d.levels; l++)
+				mark_pass_texture(tex_rects[l]);
+		}
+		last_texture_desc = d;
+		last_texture_index = index;
+		last_texture_valid_at = texflush_counter;
+		texflush_pending = false;
 		return index;
 	}
 
-	// drawing_kick_update_state (gs/gs_interface.cpp:1804-1968).
-	// bb: the scissored box of the primitive that made the template stale.
-	void update_template(const int32_t *bb)
+	// drawing_kick_update_state (gs/gs_interface.cpp:1804-1968): the
+	// primitive template, rebuilt when state it depends on changed.
+	// bb: the scissored box of the primitive being drawn.
+	void update_state(uint32_t feedback_mode, const int32_t *uv_bb, const int32_t *bb)
 	{
+		if (!(dirty & DIRTY_PRIM_TEMPLATE))
+			return;
+		dirty &= ~DIRTY_PRIM_TEMPLATE;
 		tpl_serial++;
 		PrimReg prim(regs[R_PRIM]);
 		TestReg test(ctx_reg(R_TEST_1));
 		AlphaReg alpha(ctx_reg(R_ALPHA_1));
 		ZbufReg zbuf(ctx_reg(R_ZBUF_1));
 		uint32_t state = 0, tex = 0, tex2 = 0;
-		tpl_has_tex_span = false;
 
 		if (prim.tme)
 		{
 			Tex1Reg tex1(ctx_reg(R_TEX1_1));
 			ClampReg clamp(ctx_reg(R_CLAMP_1));
-			uint32_t index = update_texture(tpl_tex_spans, tpl_num_tex_spans);
-			tpl_has_tex_span = true;
+			uint32_t index = update_texture(feedback_mode, uv_bb, bb);
 			tex = index;
 			if (textures[index].samples > 1)
 			{
@@ -1599,6 +2199,7 @@ struct pgs_gs
 		post_kick();
 	}
 
+	// post_draw_kick_handler (gs/gs_interface.cpp:2930-2943).
 	void post_kick()
 	{
 		if (pending_palette_updates >= PGS_CLUT_INSTANCES - 1 || primitive_count >= PGS_MAX_PRIMITIVES_PER_FLUSH ||
@@ -1607,6 +2208,33 @@ struct pgs_gs
 			flush_pending_transfer(true);
 			flush_render_pass(FLUSH_OVERFLOW);
 		}
+		tracker.flush_if_memory_pressure();
+	}
+
+	// Pages of the instance's box in its frame or depth buffer (compute_fb_rect /
+	// compute_z_rect, gs/gs_interface.cpp:1970-2034): block-exact inside one
+	// page, whole pages otherwise.
+	PageRect instance_rect(const Instance &inst, bool depth) const
+	{
+		const FrameReg fr(inst.frame);
+		const ZbufReg zb(inst.zbuf);
+		const uint32_t pw = depth ? inst.z_pw : inst.fb_pw, ph = depth ? inst.z_ph : inst.fb_ph;
+		const uint32_t base = depth ? zb.zbp : fr.fbp;
+		const uint32_t psm = depth ? (zb.psm | 0x30u) : fr.psm;
+		const int32_t px0 = inst.bb[0] >> pw, py0 = inst.bb[1] >> ph, px1 = inst.bb[2] >> pw, py1 = inst.bb[3] >> ph;
+		PageRect r;
+		r.base_page = base;
+		r.page_width = uint32_t(px1 - px0 + 1);
+		r.page_height = uint32_t(py1 - py0 + 1);
+		if (r.page_width == 1 && r.page_height == 1)
+			return compute_page_rect(base * BLOCKS_PER_PAGE, uint32_t(inst.bb[0]), uint32_t(inst.bb[1]),
+			                         uint32_t(inst.bb[2] - inst.bb[0] + 1), uint32_t(inst.bb[3] - inst.bb[1] + 1),
+			                         fr.fbw, psm);
+		r.page_stride = fr.fbw;
+		r.base_page += uint32_t(px0) + uint32_t(py0) * r.page_stride;
+		r.block_mask = 0xffffffffu;
+		r.write_mask = psm_word_write_mask(depth ? zb.psm : fr.psm);
+		return r;
 	}
 
 	void append(uint32_t nv, bool quad)
@@ -1675,6 +2303,9 @@ struct pgs_gs
 		if (bb[2] < bb[0] || bb[3] < bb[1])
 			return;
 
+		// The scissor and degenerate state have been consumed.
+		dirty &= ~(DIRTY_SCISSOR | DIRTY_DEGENERATE);
+
 		// A right triangle that completes the rectangle of the previous one,
 		// with no state change in between, turns that one into a
 		// parallelogram (gs/gs_interface.cpp:2569-2602).
@@ -1684,8 +2315,7 @@ struct pgs_gs
 			PrimReg prim(regs[R_PRIM]);
 			uint32_t order[3];
 			para_candidate = parallelogram_candidate(pos, attr, pre_lo, pre_hi, prim, order);
-			if (para_candidate && last_para_candidate && !template_dirty && primitive_count &&
-			    transfer_serial == last_para_transfer &&
+			if (dirty == 0 && para_candidate && last_para_candidate && primitive_count &&
 			    forms_parallelogram(pos, attr, order, positions + 3 * (primitive_count - 1),
 			                        attributes + 3 * (primitive_count - 1), last_para_order, prim))
 			{
@@ -1697,40 +2327,101 @@ struct pgs_gs
 			memcpy(last_para_order, order, sizeof(order));
 		}
 
+		// Texture feedback against the frame / depth buffer
+		// (drawing_kick_append, gs/gs_interface.cpp:2604-2630).
+		update_color_feedback_state();
+		uint32_t feedback_mode = FEEDBACK_NONE;
+		int32_t uv_bb[4] = {};
+		if (is_color_feedback || is_depth_feedback)
+		{
+			last_para_candidate = para_candidate;
+			feedback_mode = deduce_feedback_mode(pos, attr, nv, quad, uv_bb, bb);
+		}
+		else if (is_potential_feedback || (is_potential_channel_shuffle && quad))
+			compute_uv_bb(attr, quad, false, uv_bb, nullptr, nullptr);
+		current_is_channel_shuffle = false;
+		if (quad && is_potential_channel_shuffle)
+		{
+			// A channel shuffle copies within one 8-pixel column at an X offset of 8.
+			if ((bb[0] & ~7) == (bb[2] & ~7) && (uv_bb[0] ^ 8) == bb[0] && uv_bb[1] == bb[1])
+				current_is_channel_shuffle = true;
+		}
+
 		// Flush a pending partial upload before reading textures.
 		if (D.tme && xfer.active && xfer.payload.size() > xfer.flushed_qwords)
 			flush_pending_transfer(true);
 
 		check_frame_buffer_state();
 
-		if (template_dirty)
+		// A held texture is checked again after a TEXFLUSH or in feedback
+		// (gs/gs_interface.cpp:2646-2670).
+		if (D.tme && !(dirty & DIRTY_TEX))
 		{
-			update_template(bb);
-			template_dirty = false;
+			if (texflush_pending)
+			{
+				texflush_counter++;
+				texflush_pending = false;
+			}
+			if (texflush_counter != last_texture_valid_at || feedback_mode != FEEDBACK_NONE)
+			{
+				if (is_potential_feedback)
+					texture_read_region(uv_bb);
+				else
+					texture_read_full();
+				if (!(dirty & DIRTY_TEX))
+					last_texture_valid_at = texflush_counter;
+			}
 		}
 
-		// Texture read after framebuffer write in the same pass: end the pass
-		// (mark_texture_read, gs/page_tracker.cpp:327-345).  The answer only
-		// changes with the texture's pages or new framebuffer-written pages.
-		if (tpl_has_tex_span)
+		update_state(feedback_mode, uv_bb, bb);
+
+		auto &inst = instances[current_instance];
+		pgs_primitive_attribute pa = {};
+		pa.tex = tpl_tex;
+		pa.tex2 = tpl_tex2;
+		pa.state = tpl_state;
+		pa.fbmsk = frame.fbmsk;
+		pa.fogcol = D.fogcol;
+		pa.alpha = D.alpha_word;
+
+		if (quad)
 		{
-			uint64_t key[3] = { tpl_serial, tracker.gen[0], tracker.clears };
-			if (memcmp(key, tex_check_key, sizeof(key)) != 0)
-			{
-				bool hit = false;
-				for (uint32_t l = 0; l < tpl_num_tex_spans; l++)
-					hit = hit || tracker.any(tpl_tex_spans[l], PageTracker::FB_WRITE);
-				if (hit)
-				{
-					flush_render_pass(FLUSH_TEXTURE_HAZARD);
-					check_frame_buffer_state();
-					update_template(bb);
-					template_dirty = false;
-				}
-				tex_check_key[0] = tpl_serial;
-				tex_check_key[1] = tracker.gen[0];
-				tex_check_key[2] = tracker.clears;
-			}
+			pa.state |= (1u << STATE_BIT_PARALLELOGRAM) | (1u << STATE_BIT_SPRITE) |
+			            (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
+			pa.state &= ~(1u << STATE_BIT_MULTISAMPLE);
+		}
+		else if (is_line)
+		{
+			pa.state |= (1u << STATE_BIT_PARALLELOGRAM) | (1u << STATE_BIT_LINE);
+			if (pa.state & (1u << STATE_BIT_MULTISAMPLE))
+				pa.state &= ~(1u << STATE_BIT_Z_WRITE);
+		}
+		if (nv == 1)
+			pa.state |= (1u << STATE_BIT_FIX) | (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
+		pa.state |= current_instance << STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET;
+
+		// The pages the instance writes are marked when its damage grows
+		// (gs/gs_interface.cpp:2712-2816): from no depth to read-only depth, to
+		// depth writes, to more colour bits written, or a larger box.
+		bool expands = false;
+		const bool z_sens = state_is_z_sensitive();
+		if (!inst.z_sensitive && z_sens)
+		{
+			inst.z_sensitive = true;
+			expands = true;
+		}
+		if (z_sens && ZbufReg(ctx_reg(R_ZBUF_1)).zmsk == 0 && !inst.z_write)
+		{
+			inst.z_write = true;
+			// Depth writes may create a feedback that was not there.
+			dirty |= DIRTY_FEEDBACK;
+			expands = true;
+		}
+		const uint32_t write_mask = ~frame.fbmsk;
+		if ((write_mask & inst.color_write_mask) != write_mask)
+		{
+			inst.color_write_mask |= write_mask;
+			expands = true;
 		}
 
 		if (can_wrap && bb[0] > sci_hi_x_fb)
@@ -1758,68 +2449,24 @@ struct pgs_gs
 			bb[2] = std::min(bb[2], sci_hi_x_fb);
 		}
 
-		// Framebuffer pages this primitive may write.  If an earlier primitive of
-		// this pass samples them, end the pass first.
+		if (bb[0] < inst.bb[0]) { expands = true; inst.bb[0] = bb[0]; }
+		if (bb[1] < inst.bb[1]) { expands = true; inst.bb[1] = bb[1]; }
+		if (bb[2] > inst.bb[2]) { expands = true; inst.bb[2] = bb[2]; }
+		if (bb[3] > inst.bb[3]) { expands = true; inst.bb[3] = bb[3]; }
+		if (expands)
 		{
-			// Page rectangles of the primitive in the frame and depth buffers
-			// (FBP and ZBP are page aligned): test for texture reads and mark
-			// them written (depth: read only under ZMSK) in one pass.  A hit
-			// ends the pass, which clears the marks; they are made again in the
-			// new pass.
-			const ZbufReg &zb = D.zb;
-			const bool z_sens = D.z_sens;
-			const uint32_t fx0 = uint32_t(bb[0]) >> D.fb_pw, fx1 = uint32_t(bb[2]) >> D.fb_pw;
-			const uint32_t fy0 = uint32_t(bb[1]) >> D.fb_ph, fy1 = uint32_t(bb[3]) >> D.fb_ph;
-			const uint32_t zx0 = uint32_t(bb[0]) >> D.z_pw, zx1 = uint32_t(bb[2]) >> D.z_pw;
-			const uint32_t zy0 = uint32_t(bb[1]) >> D.z_ph, zy1 = uint32_t(bb[3]) >> D.z_ph;
-			const uint32_t zkind = zb.zmsk ? 1u : 0u;
-			tracker.test_mark(frame.fbp, D.fb_stride, fx0, fx1, fy0, fy1, 0);
-			if (z_sens)
-				tracker.test_mark(zb.zbp, D.z_stride, zx0, zx1, zy0, zy1, zkind);
-			if (tpl_has_tex_span && (tex_mark_key[0] != tpl_serial || tex_mark_key[1] != tracker.clears))
+			PageRect fb = instance_rect(inst, false);
+			fb.write_mask &= inst.color_write_mask;
+			tracker.mark_fb_write(fb);
+			if (inst.z_sensitive)
 			{
-				for (uint32_t l = 0; l < tpl_num_tex_spans; l++)
-					tracker.mark(tpl_tex_spans[l], PageTracker::TEX_READ);
-				tex_mark_key[0] = tpl_serial;
-				tex_mark_key[1] = tracker.clears;
+				const PageRect z = instance_rect(inst, true);
+				if (inst.z_write)
+					tracker.mark_fb_write(z);
+				else
+					tracker.mark_fb_read(z);
 			}
 		}
-
-		auto &inst = instances[current_instance];
-		pgs_primitive_attribute pa = {};
-		pa.tex = tpl_tex;
-		pa.tex2 = tpl_tex2;
-		pa.state = tpl_state;
-		pa.fbmsk = frame.fbmsk;
-		pa.fogcol = D.fogcol;
-		pa.alpha = D.alpha_word;
-
-		if (quad)
-		{
-			pa.state |= (1u << STATE_BIT_PARALLELOGRAM) | (1u << STATE_BIT_SPRITE) |
-			            (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
-			pa.state &= ~(1u << STATE_BIT_MULTISAMPLE);
-		}
-		else if (is_line)
-		{
-			pa.state |= (1u << STATE_BIT_PARALLELOGRAM) | (1u << STATE_BIT_LINE);
-			if (pa.state & (1u << STATE_BIT_MULTISAMPLE))
-				pa.state &= ~(1u << STATE_BIT_Z_WRITE);
-		}
-		if (nv == 1)
-			pa.state |= (1u << STATE_BIT_FIX) | (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
-		pa.state |= current_instance << STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET;
-
-		const bool z_sens = D.z_sens;
-		if (!inst.z_sensitive && z_sens)
-			inst.z_sensitive = true;
-		if (z_sens && D.zb.zmsk == 0 && !inst.z_write)
-			inst.z_write = true;
-		inst.color_write_mask |= ~frame.fbmsk;
-		inst.bb[0] = std::min(inst.bb[0], bb[0]);
-		inst.bb[1] = std::min(inst.bb[1], bb[1]);
-		inst.bb[2] = std::max(inst.bb[2], bb[2]);
-		inst.bb[3] = std::max(inst.bb[3], bb[3]);
 
 		pa.bb[0] = int16_t(bb[0]);
 		pa.bb[1] = int16_t(bb[1]);
@@ -1833,7 +2480,10 @@ struct pgs_gs
 		primitive_count++;
 		// Set after any flush above, which clears it.
 		last_para_candidate = para_candidate;
-		last_para_transfer = transfer_serial;
+		if (current_is_channel_shuffle)
+			instances[current_instance].has_channel_shuffle = true;
+		// Everything the primitive depends on is up to date now.
+		dirty = 0;
 	}
 
 	// triangle_is_parallelogram_candidate (gs/gs_util.cpp:237-305): flat
@@ -2191,11 +2841,35 @@ int pgs_gs_flush(pgs_gs *gs)
 	return gs->sticky_error;
 }
 
+// Whole pages of a host access (map_vram_read / map_vram_write,
+// gs/gs_interface.cpp:4184-4255).
+static PageRect host_rect(uint64_t offset, uint64_t size)
+{
+	PageRect r;
+	const uint32_t first = uint32_t(offset / PAGE_BYTES), last = uint32_t((offset + size - 1) / PAGE_BYTES);
+	r.base_page = first;
+	r.page_width = last - first + 1;
+	r.page_height = 1;
+	r.block_mask = 0xffffffffu;
+	r.write_mask = 0xffffffffu;
+	return r;
+}
+
+// Host reads wait for the work that writes the pages they read.
+static void host_read_sync(pgs_gs *gs, uint64_t offset, uint64_t size)
+{
+	if (size && gs->tracker.host_read_pending(host_rect(offset, size)))
+	{
+		gs->tracker.mark_submission(PGS_FLUSH_HOST_ACCESS);
+		gs->submit();
+	}
+}
+
 int pgs_gs_read_vram(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst)
 {
 	if (!gs || !dst || offset + size > PGS_VRAM_SIZE)
 		return PGS_ERROR_INVALID_ARGUMENT;
-	gs->flush();
+	host_read_sync(gs, offset, size);
 	if (gs->sticky_error)
 		return gs->sticky_error;
 	return gs->ops->read_vram(gs->be, 0, offset, size, dst);
@@ -2205,7 +2879,7 @@ int pgs_gs_read_vram_async(pgs_gs *gs, uint64_t offset, uint64_t size, void *dst
 {
 	if (!gs || !dst || !ticket || offset + size > PGS_VRAM_SIZE)
 		return PGS_ERROR_INVALID_ARGUMENT;
-	gs->flush();
+	host_read_sync(gs, offset, size);
 	if (gs->sticky_error)
 		return gs->sticky_error;
 	if (gs->ops->abi_version >= 2 && gs->ops->read_vram_async && gs->ops->wait_ticket)
@@ -2640,15 +3314,23 @@ int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *sr
 {
 	if (!gs || !src || offset + size > PGS_VRAM_SIZE)
 		return PGS_ERROR_INVALID_ARGUMENT;
-	gs->flush();
-	if (size)
+	if (!size)
+		return PGS_OK;
+	const PageRect r = host_rect(offset, size);
+	// Work that still reads or writes these pages goes first.
+	if (gs->tracker.host_write_pending(r))
 	{
-		// A host write replaces these pages (commit_host_write, gs/page_tracker.cpp:700-715).
-		uint32_t first = uint32_t(offset / PAGE_BYTES), last = uint32_t((offset + size - 1) / PAGE_BYTES);
-		PageSpan s{ first, last - first + 1, 1, 0 };
-		gs->tracker.clear_may_super_sample(s);
+		gs->tracker.mark_submission(PGS_FLUSH_HOST_ACCESS);
+		gs->submit();
 	}
-	return gs->ops->write_vram(gs->be, offset, size, src);
+	// Textures of the open pass are decoded when it begins.
+	if (gs->pass_texture_hit(r))
+		gs->flush_render_pass(PGS_FLUSH_HOST_ACCESS);
+	int st = gs->ops->write_vram(gs->be, offset, size, src);
+	// The host write replaces these pages (commit_host_write,
+	// gs/page_tracker.cpp:700-715).
+	gs->tracker.commit_host_write(r);
+	return st;
 }
 
 int pgs_gs_read_transfer_fifo(pgs_gs *gs, void *data, uint32_t num_128b_words)

@@ -1117,6 +1117,14 @@ __device__ __forceinline__ uint32_t fetch_texel_sample(const PassParams &P, cons
 	}
 }
 
+__device__ __forceinline__ void effective_wrap(pgs_texture_desc &t, uint32_t tex_word)
+{
+	if (t.wms < WRAP_REGION_CLAMP)
+		t.wms = (tex_word & TEX_SAMPLER_CLAMP_S_BIT) ? WRAP_CLAMP : WRAP_REPEAT;
+	if (t.wmt < WRAP_REGION_CLAMP)
+		t.wmt = (tex_word & TEX_SAMPLER_CLAMP_T_BIT) ? WRAP_CLAMP : WRAP_REPEAT;
+}
+
 __device__ __forceinline__ int32_t wrap_coord(int32_t v, uint32_t mode, uint32_t size_log2, uint32_t lo, uint32_t hi)
 {
 	int32_t size = 1 << size_log2;
@@ -1394,7 +1402,11 @@ __device__ void sample_texture(const PassParams &P, uint32_t tex_word, uint32_t 
                                bool perspective, uint32_t sample, uint32_t rx, uint32_t ry, float out[4])
 {
 	const uint32_t tex_index = min(tex_word & TEX_TEXTURE_INDEX_MASK, P.num_textures - 1u);
-	const pgs_texture_desc t = P.textures[tex_index];
+	pgs_texture_desc t = P.textures[tex_index];
+	// Descriptors keep only the region modes; plain REPEAT and CLAMP come from
+	// the primitive's sampler bits, as the reference's shader takes them
+	// (drawing_kick_update_texture, gs/gs_interface.cpp:1514-1528).
+	effective_wrap(t, tex_word);
 	if (MIP && (tex_word & TEX_PER_SAMPLE_BIT) && t.samples > 1)
 	{
 		uint32_t rgba[4];

@@ -12,6 +12,9 @@ from recording_backend import RecordingBackend
 Z_TEST, Z_WRITE, OPAQUE, PARALLELOGRAM, MULTISAMPLE = 12, 13, 14, 15, 16
 Z_GREATER, PERSPECTIVE, IIP, FIX, SPRITE, LINE = 17, 18, 19, 20, 21, 22
 SNAP_RASTER, SNAP_ATTRIBUTE = 25, 26
+# pgs_flush_reason (the reference's FlushReason numbering).
+FLUSH_FB_POINTER, FLUSH_OVERFLOW, FLUSH_TEXTURE_HAZARD, FLUSH_COPY_HAZARD, FLUSH_SUBMISSION = 0, 1, 2, 3, 4
+FLUSH_PRESSURE, FLUSH_HOST_ACCESS = 5, 6
 
 
 def bit(v, b):
@@ -216,17 +219,47 @@ def test_partial_image_transfer_and_texture_read_flush():
     assert len(be.copies) == 2 and be.copies[1]["offset"] == 4096 and len(be.copies[1]["data"]) == len(data)
 
 
-def test_texture_read_after_framebuffer_write_starts_new_pass():
+def _uv_sprite(s, prim, xy0, xy1, uv0, uv1):
+    """A sprite with explicit UVs (FST = 1), in 1/16 pixel / texel units."""
+    q = np.zeros((2, 3, 2), dtype=np.uint64)
+    q[:, 0] = g.q_rgbaq(np.array([[10, 20, 30, 40]] * 2))
+    for i, (xy, uv) in enumerate(((xy0, uv0), (xy1, uv1))):
+        q[i, 1, 0] = uv[0] | (uv[1] << 16)
+        q[i, 1, 1] = g.D_UV
+        q[i, 2] = g.q_xyz2(np.array([xy[0]]), np.array([xy[1]]), np.array([1000]))[0]
+    lo, hi = g.gif_tag(2, 0, 3, g.D_RGBAQ | (0xE << 4) | (g.D_XYZ2 << 8), pre=1, prim=prim)
+    s._qwords(np.array([[lo, hi]], dtype=np.uint64))
+    s._qwords(q.reshape(-1, 2))
+
+
+@pytest.mark.parametrize("uv_origin,counts", [(10, [1, 1]), (40, [2])])
+def test_texture_read_after_framebuffer_write(uv_origin, counts):
+    """A sprite sampling its own framebuffer (TBP0 = FBP * 32) in sliced
+    feedback: the reference narrows the texture to the sprite's UV box
+    (drawing_kick_update_texture, gs/gs_interface.cpp:1478-1509), so the pass
+    ends only when that box covers blocks an earlier primitive wrote
+    (mark_texture_read, gs/page_tracker.cpp:327-345).  The triangle covers
+    pixels 10..29; UVs from texel 10 overlap it, from texel 40 they do not."""
     def build(s):
         setup(s)
         verts(s, g.prim_reg(g.PRIM_TRI), [(160, 160), (480, 160), (320, 480)])
-        # Sample the framebuffer page just written (TBP0 = FBP * 32).
         s.ad([(g.TEX0_1, g.tex0_reg(0, 10, g.PSMCT32, 6, 6))])
-        verts(s, g.prim_reg(g.PRIM_SPRITE, tme=1, fst=1), [(6400, 6400), (8000, 7000)])
+        u = uv_origin * 16
+        _uv_sprite(s, g.prim_reg(g.PRIM_SPRITE, tme=1, fst=1), (6400, 6400), (8000, 7000), (u, u), (u + 160, u + 160))
     be = run(build=build)
-    assert [p["num_primitives"] for p in be.passes] == [1, 1]
-    assert be.passes[1]["flush_reason"] in (0,)
-    assert be.passes[0]["flush_reason"] == 3  # texture hazard
+    assert [p["num_primitives"] for p in be.passes] == counts
+    assert be.passes[-1]["flush_reason"] == FLUSH_SUBMISSION
+    if len(counts) > 1:
+        assert be.passes[0]["flush_reason"] == FLUSH_TEXTURE_HAZARD
+    import pgs_ref_frontend
+    if pgs_ref_frontend.available():
+        s = g.GifStream()
+        build(s)
+        ref = pgs_ref_frontend.RefFrontend()
+        ref.gif_transfer(0, s.tobytes())
+        ref.flush()
+        assert [e["num_primitives"] for e in ref.events() if e["type"] == "pass"] == counts
+        ref.close()
 
 
 def test_coarse_tile_size_heuristic():
@@ -275,26 +308,42 @@ def test_read_vram_async_falls_back_to_synchronous_copy():
     (64, (3, 6, 4, 6)),      # pages 63 and 64: the span crosses a 64-page word
     (63, (0, 6, 3, 7)),      # last page of a word, two rows
 ])
-def test_framebuffer_write_over_sampled_page_is_a_hazard(tex_page, rect):
+def test_framebuffer_write_over_sampled_page_keeps_the_pass(tex_page, rect):
     """A draw whose page rectangle (x0, y0, x1, y1 in 64x32 CT32 pages, 10
-    pages per row) covers a page sampled earlier in the pass ends the pass
-    before it; the same draw moved off that page does not."""
-    def build(shift):
+    pages per row) covers a page sampled earlier in the pass does not end the
+    pass: the reference samples a texture-cache image taken before the pass
+    renders (gs/page_tracker.cpp:155-190 marks the write without a flush), and
+    this backend decodes every texture of a pass before it shades any primitive
+    of it.  A new texture over those pages after the write does end the pass
+    (mark_texture_read, gs/page_tracker.cpp:327-345); the texture the pass
+    already holds would not be checked again until the next TEXFLUSH that
+    counts.  The reference frontend gives the same passes where it is built."""
+    def build(again):
         def b(s):
             setup(s)
             s.ad([(g.TEX0_1, g.tex0_reg(tex_page * 32, 1, g.PSMCT32, 6, 5))])
             verts(s, g.prim_reg(g.PRIM_SPRITE, tme=1, fst=1), [(0, 0), (16 * 16, 16 * 16)])
             x0, y0, x1, y1 = rect
-            if shift:
-                # Move the rectangle so that it misses the sampled page.
-                x0 = x1 = (tex_page % 10 + 5) % 10
             verts(s, g.prim_reg(g.PRIM_SPRITE), [(x0 * 64 * 16, y0 * 32 * 16), ((x1 + 1) * 64 * 16 - 16, (y1 + 1) * 32 * 16 - 16)])
+            if again:
+                s.ad([(g.TEX0_1, g.tex0_reg(tex_page * 32, 1, g.PSMCT32, 6, 4))])
+                verts(s, g.prim_reg(g.PRIM_SPRITE, tme=1, fst=1), [(0, 0), (16 * 16, 16 * 16)])
         return b
     be = run(build=build(False))
-    assert [p["num_primitives"] for p in be.passes] == [1, 1]
-    assert be.passes[0]["flush_reason"] == 3
-    be = run(build=build(True))
     assert [p["num_primitives"] for p in be.passes] == [2]
+    be = run(build=build(True))
+    assert [p["num_primitives"] for p in be.passes] == [2, 1]
+    assert be.passes[0]["flush_reason"] == FLUSH_TEXTURE_HAZARD
+    import pgs_ref_frontend
+    if pgs_ref_frontend.available():
+        for again, counts in ((False, [2]), (True, [2, 1])):
+            s = g.GifStream()
+            build(again)(s)
+            ref = pgs_ref_frontend.RefFrontend()
+            ref.gif_transfer(0, s.tobytes())
+            ref.flush()
+            assert [e["num_primitives"] for e in ref.events() if e["type"] == "pass"] == counts
+            ref.close()
 
 
 @pytest.mark.parametrize("maker", ["c2", "fuzz", "strips"])

@@ -151,7 +151,10 @@ def test_descriptor_levels_and_bases():
 
 def test_write_to_mip_level_pages_ends_the_pass():
     """A framebuffer write to pages of level 2 followed by a draw sampling the
-    chain must split the pass (hazards cover every level's pages)."""
+    chain splits the pass before that draw: texture hazards cover every
+    level's pages (texture_page_rects_read_full, gs/gs_interface.cpp:1201-1206).
+    The write itself does not end the pass (the chain was read before it).
+    The reference frontend gives the same passes where it is built."""
     be = RecordingBackend()
     gs = pgs.GSInterface(be)
     data = chain_stream(tex1=g.tex1_reg(lcm=1, mxl=3, mmin=2, k=32))
@@ -168,9 +171,9 @@ def test_write_to_mip_level_pages_ends_the_pass():
     first = len(be.passes)
     gs.gif_transfer(0, again + s.tobytes() + again)
     gs.flush()
-    # Writing a sampled level's pages ends the pass, and sampling them after the
-    # write ends the next one.
-    assert len(be.passes) - first == 3
+    # Sampling the chain after the write to its level-2 pages ends the pass.
+    assert [p["num_primitives"] for p in be.passes[first:]] == [2, 1]
+    assert be.passes[first]["flush_reason"] == 2
     # Without a mip chain the same write does not touch the sampled pages.
     be2 = RecordingBackend()
     gs2 = pgs.GSInterface(be2)
@@ -183,3 +186,14 @@ def test_write_to_mip_level_pages_ends_the_pass():
     assert len(be2.passes) - first == 1
     gs.close()
     gs2.close()
+    import pgs_ref_frontend
+    if pgs_ref_frontend.available():
+        for stream, counts in ((again, [2, 1]), (flat, [3])):
+            ref = pgs_ref_frontend.RefFrontend()
+            ref.gif_transfer(0, data)
+            ref.flush()
+            ref.clear()
+            ref.gif_transfer(0, stream + s.tobytes() + stream)
+            ref.flush()
+            assert [e["num_primitives"] for e in ref.events() if e["type"] == "pass"] == counts
+            ref.close()

@@ -14,8 +14,9 @@ PARALLELOGRAM = 1 << 15
 
 
 def rect_stream(split, textured, ss, n=60, seed=7):
-    """n rectangles as triangle pairs in one PACKED list each (split: a FOGCOL
-    write between the halves, which keeps them apart)."""
+    """n rectangles as triangle pairs in one PACKED list each (split: a DIMX
+    write between the halves, state the template depends on, which keeps them
+    apart; a register that feeds no derived state, such as FOGCOL, would not)."""
     rng = np.random.default_rng(seed)
     s = g.GifStream()
     g._frame_setup(s, 0, 5, g.PSMCT32, 60, g.PSMZ24, 320, 224, g.test_reg(zte=1, ztst=1))
@@ -45,7 +46,7 @@ def rect_stream(split, textured, ss, n=60, seed=7):
         desc = [g.D_RGBAQ, g.D_UV, g.D_XYZ2]
         if split:
             s.packed(p, desc, q[:3].reshape(-1, 2))
-            s.ad([(g.FOGCOL, k + 1)])
+            s.ad([(g.DIMX, k + 1)])
             s.packed(p, desc, q[3:].reshape(-1, 2))
         else:
             s.packed(p, desc, q.reshape(-1, 2))
