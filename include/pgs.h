@@ -31,7 +31,9 @@
 extern "C" {
 #endif
 
-#define PGS_ABI_VERSION 4u
+#define PGS_ABI_VERSION 5u
+/* VRAM snapshots a render pass can hold (pgs_render_pass.snapshot_textures). */
+#define PGS_MAX_VRAM_SNAPSHOTS 4u
 
 /* ------------------------------------------------------------------ */
 /* Status codes                                                        */
@@ -134,7 +136,10 @@ typedef struct pgs_texture_desc
 	 * gs/gs_renderer.cpp:1317-1386; upload.comp SUPER_SAMPLED).  0 or 1: a
 	 * plain texture. */
 	uint32_t samples;
-	uint32_t padding;
+	/* TEX1.MXL as written (0 without a mipmapping MMIN).  Backends ignore it;
+	 * it keeps textures that differ only in it apart, as the reference's
+	 * texture key does (gs/gs_interface.cpp:1605-1619). */
+	uint32_t mxl;
 } pgs_texture_desc;
 
 /* One framebuffer instance inside a render pass (RenderPass::Instance,
@@ -192,6 +197,17 @@ typedef struct pgs_render_pass
 	 * state blends, coarse tiles with 32 or more primitives and no depth
 	 * write shade single-sampled.  ABI >= 4. */
 	uint32_t blend_demote;
+	/* ABI >= 5.  VRAM snapshots the frontend took during the pass
+	 * (pgs_backend_ops.snapshot_vram): textures [snapshot_textures[k - 1],
+	 * snapshot_textures[k]) decode from snapshot k (the first from 0), the
+	 * rest from VRAM as the pass begins.  The reference samples textures from
+	 * cache images uploaded before a transfer can overwrite their source
+	 * (flush_cache_upload via PageTracker::flush_cached,
+	 * gs/page_tracker.cpp:585-594); this backend decodes a pass's textures
+	 * when the pass begins, so a transfer into a texture the open pass holds
+	 * is preceded by a snapshot instead. */
+	uint32_t num_snapshots;
+	uint32_t snapshot_textures[PGS_MAX_VRAM_SNAPSHOTS];
 } pgs_render_pass;
 
 /* A VRAM transfer (CopyDescriptor, gs/gs_renderer.hpp).  For HOST_TO_LOCAL,
@@ -214,7 +230,13 @@ typedef struct pgs_palette_upload
 	float csm2_x_scale;
 	uint32_t csm2_x_bias;
 	uint32_t base_instance;  /* CLUT state the load starts from */
-	uint32_t padding;
+	/* ABI >= 5: 1 + the CLUT ring slot the load writes.  The frontend numbers
+	 * the ring as the reference's renderer does (update_palette_cache,
+	 * rewind_clut_instance, gs/gs_renderer.cpp:3384-3419): a load that nothing
+	 * has read yet is rewritten in place by a load replacing it, and a pass
+	 * that ends on an older memoised palette rewinds the ring to it.  0: the
+	 * backend takes the slot after the last one it wrote. */
+	uint32_t target;
 } pgs_palette_upload;
 
 /* FlushStats (gs/gs_renderer.hpp:55-65) plus fragment counters. */
@@ -326,6 +348,13 @@ typedef struct pgs_backend_ops
 	 * may be NULL) receives the seconds accumulated so far per stage, after
 	 * the timed work has completed. */
 	int (*timestamps)(void *self, int enable, double *totals);
+	/* abi_version >= 5, optional (NULL: the frontend ends the pass instead).
+	 * Copies every VRAM plane, behind all submitted work, into the next of
+	 * the PGS_MAX_VRAM_SNAPSHOTS snapshot slots of the open render pass and
+	 * returns the slot (>= 0) or a negative pgs_status.  flush_rendering
+	 * decodes the pass's textures from the snapshots pgs_render_pass names and
+	 * releases the slots. */
+	int (*snapshot_vram)(void *self);
 } pgs_backend_ops;
 
 /* TimestampType (gs/gs_renderer.hpp:67-79). */

@@ -264,9 +264,13 @@ struct Backend
 	// reference samples texture-cache images uploaded before the pass renders),
 	// whatever the pass itself writes.
 	std::vector<uint8_t> tex_vram;
-	uint32_t t32(uint32_t plane, uint32_t i) const { return reinterpret_cast<const uint32_t *>(tex_vram.data() + plane * size_t(VRAM))[i]; }
-	uint16_t t16(uint32_t plane, uint32_t i) const { return reinterpret_cast<const uint16_t *>(tex_vram.data() + plane * size_t(VRAM))[i]; }
-	uint8_t t8(uint32_t plane, uint32_t i) const { return tex_vram[plane * size_t(VRAM) + i]; }
+	// Snapshots of every VRAM plane taken during the open pass
+	// (snapshot_vram); textures the pass names decode from them instead.
+	std::vector<uint8_t> snaps[PGS_MAX_VRAM_SNAPSHOTS];
+	uint32_t snaps_taken = 0;
+	static uint32_t t32(const uint8_t *src, uint32_t plane, uint32_t i) { return reinterpret_cast<const uint32_t *>(src + plane * size_t(VRAM))[i]; }
+	static uint16_t t16(const uint8_t *src, uint32_t plane, uint32_t i) { return reinterpret_cast<const uint16_t *>(src + plane * size_t(VRAM))[i]; }
+	static uint8_t t8(const uint8_t *src, uint32_t plane, uint32_t i) { return src[plane * size_t(VRAM) + i]; }
 	uint32_t &w32(uint32_t plane, uint32_t i) { return reinterpret_cast<uint32_t *>(vram.data() + plane * size_t(VRAM))[i]; }
 	uint16_t &w16(uint32_t plane, uint32_t i) { return reinterpret_cast<uint16_t *>(vram.data() + plane * size_t(VRAM))[i]; }
 	uint8_t &w8(uint32_t plane, uint32_t i) { return vram[plane * size_t(VRAM) + i]; }
@@ -770,6 +774,7 @@ struct Backend
 	struct PassCtx
 	{
 		const pgs_render_pass *rp;
+		const uint8_t *const *tex_src; // VRAM each texture decodes from
 		const pgs_primitive_attribute *prims;
 		const Setup *setup;
 		const TAttr *tattr;
@@ -976,7 +981,7 @@ struct Backend
 		return uint32_t(cl[bi]) | (uint32_t(cl[bi + 256]) << 16);
 	}
 
-	uint32_t texel(const pgs_texture_desc &t, uint32_t level, int32_t x, int32_t y)
+	uint32_t texel(const uint8_t *src, const pgs_texture_desc &t, uint32_t level, int32_t x, int32_t y)
 	{
 		uint32_t tbp = level ? (t.mip[level - 1] & 0x3fffu) : t.tbp0;
 		uint32_t tbw = level ? (t.mip[level - 1] >> 16) : t.tbw;
@@ -985,27 +990,27 @@ struct Backend
 		{
 		case CT24: case Z24:
 		{
-			uint32_t c = t32(0, a) & 0xffffffu;
+			uint32_t c = t32(src, 0, a) & 0xffffffu;
 			uint32_t al = (t.aem && c == 0) ? 0 : t.ta0;
 			return c | (al << 24);
 		}
 		case CT16: case CT16S: case Z16: case Z16S:
 		{
-			uint32_t c = t16(0, a);
+			uint32_t c = t16(src, 0, a);
 			uint32_t r = (c & 0x1f) << 3, g = ((c >> 5) & 0x1f) << 3, b = ((c >> 10) & 0x1f) << 3;
 			uint32_t al = (t.aem && c == 0) ? 0 : ((c & 0x8000) ? t.ta1 : t.ta0);
 			return r | (g << 8) | (b << 16) | (al << 24);
 		}
-		case T8: return clut_color(t, t8(0, a));
-		case T8H: return clut_color(t, t32(0, a) >> 24);
+		case T8: return clut_color(t, t8(src, 0, a));
+		case T8H: return clut_color(t, t32(src, 0, a) >> 24);
 		case T4:
 		{
-			uint32_t byte = t8(0, a >> 1);
+			uint32_t byte = t8(src, 0, a >> 1);
 			return clut_color(t, (byte >> ((a & 1) * 4)) & 15u);
 		}
-		case T4HL: return clut_color(t, (t32(0, a) >> 24) & 15u);
-		case T4HH: return clut_color(t, t32(0, a) >> 28);
-		default: return t32(0, a);
+		case T4HL: return clut_color(t, (t32(src, 0, a) >> 24) & 15u);
+		case T4HH: return clut_color(t, t32(src, 0, a) >> 28);
+		default: return t32(src, 0, a);
 		}
 	}
 
@@ -1025,7 +1030,7 @@ struct Backend
 	// (gs/shaders/ubershader.comp:1133-1151,1214-1227), region bounds and masks
 	// shifted down by the level (texture_clamp :947-953; upload_texture
 	// gs/gs_renderer.cpp:3578-3590), bilinear as exact k/16 weights + roundEven.
-	void sample_level(const pgs_texture_desc &t, uint32_t level, bool clamp_s, bool clamp_t, bool linear, float u,
+	void sample_level(const uint8_t *src, const pgs_texture_desc &t, uint32_t level, bool clamp_s, bool clamp_t, bool linear, float u,
 	                  float v, bool perspective, uint32_t rgba[4])
 	{
 		uint32_t twl = t.tw_log2 - level, thl = t.th_log2 - level;
@@ -1064,7 +1069,7 @@ struct Backend
 		{
 			int32_t x = wrap_coord(ku >> 4, t.wms, twl, minu, maxu);
 			int32_t y = wrap_coord(kv >> 4, t.wmt, thl, minv, maxv);
-			uint32_t c = texel(t, level, x, y);
+			uint32_t c = texel(src, t, level, x, y);
 			for (int k = 0; k < 4; k++)
 				rgba[k] = (c >> (8 * k)) & 0xffu;
 			return;
@@ -1082,7 +1087,7 @@ struct Backend
 				uint32_t wgt = wx[xx] * wy[yy];
 				if (!wgt)
 					continue;
-				uint32_t tc = texel(t, level, xs[xx], ys[yy]);
+				uint32_t tc = texel(src, t, level, xs[xx], ys[yy]);
 				for (int k = 0; k < 4; k++)
 					acc[k] += wgt * ((tc >> (8 * k)) & 0xffu);
 			}
@@ -1135,51 +1140,51 @@ struct Backend
 	// Texel of layer `layer` of a super-sampled texture: layer 0 the
 	// single-sampled texel, layer s + 1 sample s where the reference plane
 	// marks it (upload.comp SUPER_SAMPLED, :131-220).
-	uint32_t texel_layer(const pgs_texture_desc &t, uint32_t layer, int32_t x, int32_t y)
+	uint32_t texel_layer(const uint8_t *src, const pgs_texture_desc &t, uint32_t layer, int32_t x, int32_t y)
 	{
 		if (layer == 0)
-			return texel(t, 0, x, y);
+			return texel(src, t, 0, x, y);
 		const uint32_t s = layer - 1;
 		const uint32_t a = swizzle(uint32_t(x), uint32_t(y), t.tbp0, t.tbw, t.psm);
 		switch (t.psm)
 		{
 		case CT24: case Z24:
 		{
-			uint32_t col = t32(0, a), ref = t32(1, a);
+			uint32_t col = t32(src, 0, a), ref = t32(src, 1, a);
 			if (ref != 0)
-				col = (t32(2 + s, a) & ref) | (col & ~ref);
+				col = (t32(src, 2 + s, a) & ref) | (col & ~ref);
 			col &= 0xffffffu;
 			uint32_t al = (t.aem && col == 0) ? 0 : t.ta0;
 			return col | (al << 24);
 		}
 		case CT16: case CT16S: case Z16: case Z16S:
 		{
-			uint32_t c = t16(0, a);
-			if (t16(1, a) == 0xffff)
-				c = t16(2 + s, a);
+			uint32_t c = t16(src, 0, a);
+			if (t16(src, 1, a) == 0xffff)
+				c = t16(src, 2 + s, a);
 			uint32_t r = (c & 0x1f) << 3, g = ((c >> 5) & 0x1f) << 3, b = ((c >> 10) & 0x1f) << 3;
 			uint32_t al = (t.aem && c == 0) ? 0 : ((c & 0x8000) ? t.ta1 : t.ta0);
 			return r | (g << 8) | (b << 16) | (al << 24);
 		}
 		case T8:
 		{
-			uint32_t idx = t8(0, a);
-			if (t8(1, a) == 0xff)
-				idx = t8(2 + s, a);
+			uint32_t idx = t8(src, 0, a);
+			if (t8(src, 1, a) == 0xff)
+				idx = t8(src, 2 + s, a);
 			return clut_color(t, idx);
 		}
 		case T8H:
 		{
-			uint32_t idx = t8(0, 4 * a + 3);
-			if (t8(1, 4 * a + 3) == 0xff)
-				idx = t8(2 + s, 4 * a + 3);
+			uint32_t idx = t8(src, 0, 4 * a + 3);
+			if (t8(src, 1, 4 * a + 3) == 0xff)
+				idx = t8(src, 2 + s, 4 * a + 3);
 			return clut_color(t, idx);
 		}
 		default:
 		{
-			uint32_t c = t32(0, a);
-			if (t32(1, a) == 0xffffffffu)
-				c = t32(2 + s, a);
+			uint32_t c = t32(src, 0, a);
+			if (t32(src, 1, a) == 0xffffffffu)
+				c = t32(src, 2 + s, a);
 			return c;
 		}
 		}
@@ -1205,7 +1210,7 @@ struct Backend
 	// the phase LUT's taps around the texel below the sampling position with
 	// unorm8 weights (one tap for nearest filtering or on a clamped region
 	// edge); coordinates snap as for plain textures, taps wrap like them.
-	void sample_layered(const PassCtx &, const pgs_texture_desc &t, uint32_t tex_word, float u, float v,
+	void sample_layered(const PassCtx &, const uint8_t *src, const pgs_texture_desc &t, uint32_t tex_word, float u, float v,
 	                    bool perspective, uint32_t sample, uint32_t rx, uint32_t ry, uint32_t rgba[4])
 	{
 		const bool clamp_s = tex_word & (1u << 19), clamp_t = tex_word & (1u << 20);
@@ -1232,7 +1237,7 @@ struct Backend
 			const int32_t ku = int32_t(std::floor(fu)), kv = int32_t(std::floor(fv));
 			if (!mag_linear)
 			{
-				uint32_t c = texel_layer(t, layer, wrap_coord(ku >> 4, t.wms, t.tw_log2, t.minu, t.maxu),
+				uint32_t c = texel_layer(src, t, layer, wrap_coord(ku >> 4, t.wms, t.tw_log2, t.minu, t.maxu),
 				                         wrap_coord(kv >> 4, t.wmt, t.th_log2, t.minv, t.maxv));
 				for (int k = 0; k < 4; k++)
 					rgba[k] = (c >> (8 * k)) & 0xffu;
@@ -1251,7 +1256,7 @@ struct Backend
 					const uint32_t wgt = wx[xx] * wy[yy];
 					if (!wgt)
 						continue;
-					const uint32_t c = texel_layer(t, layer, xs[xx], ys[yy]);
+					const uint32_t c = texel_layer(src, t, layer, xs[xx], ys[yy]);
 					for (int k = 0; k < 4; k++)
 						acc[k] += wgt * ((c >> (8 * k)) & 0xffu);
 				}
@@ -1296,7 +1301,7 @@ struct Backend
 		}
 		const bool force_nearest = !mag_linear || ((clamp_s || clamp_t) && (ix == rx0 || iy == ry0 || ix == rx1 || iy == ry1));
 		auto tap = [&](uint32_t layer, int32_t x, int32_t y) {
-			return texel_layer(t, std::min(layer + 1, t.samples), wrap_coord(x, t.wms, t.tw_log2, t.minu, t.maxu),
+			return texel_layer(src, t, std::min(layer + 1, t.samples), wrap_coord(x, t.wms, t.tw_log2, t.minu, t.maxu),
 			                   wrap_coord(y, t.wmt, t.th_log2, t.minv, t.maxv));
 		};
 		const uint32_t c0 = tap(entry & 15u, ix, iy);
@@ -1335,6 +1340,7 @@ struct Backend
 		// from the primitive's sampler bits (TEX_SAMPLER_CLAMP_S/T,
 		// gs/gs_interface.cpp:1514-1528, 1818-1820).
 		pgs_texture_desc t = P.rp->textures[tex_word & 0xffffu];
+		const uint8_t *src = P.tex_src[std::min<uint32_t>(tex_word & 0xffffu, P.rp->num_textures - 1)];
 		if (t.wms < 2)
 			t.wms = (tex_word & (1u << 19)) ? 1u : 0u;
 		if (t.wmt < 2)
@@ -1342,7 +1348,7 @@ struct Backend
 		if ((tex_word & (1u << 24)) && t.samples > 1)
 		{
 			uint32_t rgba[4];
-			sample_layered(P, t, tex_word, u, v, perspective, sample, rx, ry, rgba);
+			sample_layered(P, src, t, tex_word, u, v, perspective, sample, rx, ry, rgba);
 			for (int k = 0; k < 4; k++)
 				out[k] = float(rgba[k]);
 			return;
@@ -1354,7 +1360,7 @@ struct Backend
 		uint32_t rgba[4];
 		if (max_mip == 0)
 		{
-			sample_level(t, 0, clamp_s, clamp_t, mag_linear, u, v, perspective, rgba);
+			sample_level(src, t, 0, clamp_s, clamp_t, mag_linear, u, v, perspective, rgba);
 		}
 		else
 		{
@@ -1389,11 +1395,11 @@ struct Backend
 				l1 = float(int32_t(lod + 0.5f));
 			}
 			uint32_t last = std::max<uint32_t>(t.levels, 1) - 1;
-			sample_level(t, std::min<uint32_t>(uint32_t(l1), last), clamp_s, clamp_t, linear, u, v, perspective, rgba);
+			sample_level(src, t, std::min<uint32_t>(uint32_t(l1), last), clamp_s, clamp_t, linear, u, v, perspective, rgba);
 			if (weight)
 			{
 				uint32_t c2[4];
-				sample_level(t, std::min<uint32_t>(uint32_t(l2), last), clamp_s, clamp_t, linear, u, v, perspective,
+				sample_level(src, t, std::min<uint32_t>(uint32_t(l2), last), clamp_s, clamp_t, linear, u, v, perspective,
 				             c2);
 				for (int k = 0; k < 4; k++)
 				{
@@ -2345,8 +2351,13 @@ struct Backend
 
 	int flush_rendering(const pgs_render_pass *rp)
 	{
-		if (!rp || rp->num_primitives == 0)
+		if (!rp)
 			return 0;
+		if (rp->num_primitives == 0)
+		{
+			snaps_taken = 0;
+			return 0;
+		}
 		for (uint32_t i = 0; i < rp->num_textures; i++)
 		{
 			const pgs_texture_desc &d = rp->textures[i];
@@ -2356,18 +2367,32 @@ struct Backend
 			                      d.samples > 16 || 2 + d.samples > num_planes))
 				return PGS_ERROR_INVALID_ARGUMENT;
 		}
+		std::vector<const uint8_t *> tex_src(std::max<uint32_t>(rp->num_textures, 1), nullptr);
 		if (rp->num_textures)
 		{
 			// Plane 0, and every plane when super-sampled texture layers read
 			// the reference plane and the samples.
 			const size_t planes = rp->has_ss_textures ? num_planes : 1;
 			tex_vram.assign(vram.begin(), vram.begin() + planes * size_t(VRAM));
+			const uint32_t nsnap = std::min<uint32_t>(rp->num_snapshots, snaps_taken);
+			for (uint32_t i = 0; i < rp->num_textures; i++)
+			{
+				tex_src[i] = tex_vram.data();
+				for (uint32_t k = 0; k < nsnap; k++)
+					if (i < rp->snapshot_textures[k])
+					{
+						tex_src[i] = snaps[k].data();
+						break;
+					}
+			}
 		}
+		snaps_taken = 0;
 		std::vector<pgs_primitive_attribute> prims(rp->prims, rp->prims + rp->num_primitives);
 		std::vector<Setup> setup(rp->num_primitives);
 		std::vector<TAttr> tattr(rp->num_primitives);
 		PassCtx P = {};
 		P.rp = rp;
+		P.tex_src = tex_src.data();
 		P.prims = prims.data();
 		P.setup = setup.data();
 		P.tattr = tattr.data();
@@ -2679,7 +2704,7 @@ struct Backend
 	// clut_write.comp.
 	int update_palette(const pgs_palette_upload *u)
 	{
-		uint32_t inst = (last_clut_instance + 1) % PGS_CLUT_INSTANCES;
+		uint32_t inst = u->target ? (u->target - 1u) % PGS_CLUT_INSTANCES : (last_clut_instance + 1) % PGS_CLUT_INSTANCES;
 		last_clut_instance = inst;
 		uint16_t tmp[512];
 		memcpy(tmp, &clut[size_t(u->base_instance) * 512], sizeof(tmp));
@@ -2891,6 +2916,14 @@ static int o_flush_rendering(void *self, const pgs_render_pass *rp) { return sta
 static int o_copy(void *self, const pgs_copy_desc *d) { return static_cast<Backend *>(self)->copy_vram(d); }
 static int o_palette(void *self, const pgs_palette_upload *u) { return static_cast<Backend *>(self)->update_palette(u); }
 static int o_set_ss(void *self, uint32_t x, uint32_t y) { return static_cast<Backend *>(self)->set_ss(x, y); }
+static int o_snapshot(void *self)
+{
+	auto *b = static_cast<Backend *>(self);
+	if (b->snaps_taken >= PGS_MAX_VRAM_SNAPSHOTS)
+		return PGS_ERROR_CAPACITY;
+	b->snaps[b->snaps_taken].assign(b->vram.begin(), b->vram.end());
+	return int(b->snaps_taken++);
+}
 static int o_submit(void *) { return 0; }
 static int o_read(void *self, uint32_t plane, uint64_t off, uint64_t size, void *dst)
 {
@@ -3223,7 +3256,7 @@ static int o_vsync(void *self, const pgs_merge_params *mp, void *dst)
 
 static const pgs_backend_ops ORACLE_OPS = {
 	PGS_ABI_VERSION, o_destroy, o_reserve, o_flush_rendering, o_copy, o_palette, o_set_ss, o_submit, o_read, o_write, o_error,
-	nullptr, nullptr, o_circuit, o_vsync, nullptr,
+	nullptr, nullptr, o_circuit, o_vsync, nullptr, o_snapshot,
 };
 
 extern "C" {

@@ -60,7 +60,7 @@ const uint8_t RCP_TABLE[256] = {
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) & ~(a - 1); }
 
-enum OpType : uint32_t { OP_COPY = 0, OP_CLUT = 1, OP_PASS = 2 };
+enum OpType : uint32_t { OP_COPY = 0, OP_CLUT = 1, OP_PASS = 2, OP_SNAPSHOT = 3 };
 
 struct PassOp
 {
@@ -73,6 +73,9 @@ struct PassOp
 	uint32_t blend_demote;  // primitives per coarse tile that demote a blended tile, 0 = off
 	uint32_t num_instances;
 	pgs_rp_instance instances[PGS_MAX_RENDER_PASS_INSTANCES];
+	// Textures [snap_limit[k - 1], snap_limit[k]) decode from snapshot slot k.
+	uint32_t num_snaps;
+	uint32_t snap_limit[PGS_MAX_VRAM_SNAPSHOTS];
 	// Host copy of the primitive records while the pass is submitted
 	// (null for recorded passes, which keep theirs in the host arena).
 	const pgs_primitive_attribute *host_prims;
@@ -85,6 +88,7 @@ struct Op
 	size_t copy_host_off;
 	ClutParams clut;
 	PassOp pass;
+	uint32_t snap_slot;
 };
 
 struct Dispatch
@@ -235,6 +239,10 @@ struct CudaBackend
 	uint32_t *d_error = nullptr;
 	unsigned long long *d_frags = nullptr;
 	uint8_t *d_snapshot = nullptr;
+	// VRAM snapshots of the open render pass (snapshot_vram): every plane,
+	// allocated on first use; snapshots_taken counts the pass's slots in use.
+	uint8_t *d_tex_snap[PGS_MAX_VRAM_SNAPSHOTS] = {};
+	uint32_t snapshots_taken = 0;
 	uint32_t last_clut = 0;
 
 	// Arena.
@@ -458,6 +466,11 @@ struct CudaBackend
 		cudaFree(d_vram);
 		cudaFree(d_clut);
 		cudaFree(d_snapshot);
+		for (auto &p : d_tex_snap)
+		{
+			cudaFree(p);
+			p = nullptr;
+		}
 		cudaFree(d_error);
 		cudaFree(d_frags);
 		cudaFree(d_rcp_float);
@@ -596,8 +609,14 @@ struct CudaBackend
 
 	int flush_rendering(const pgs_render_pass *rp)
 	{
-		if (!rp || rp->num_primitives == 0)
+		if (!rp)
 			return PGS_OK;
+		if (rp->num_primitives == 0)
+		{
+			// An empty pass only releases its snapshot slots.
+			snapshots_taken = 0;
+			return PGS_OK;
+		}
 		if (rp->num_primitives > PGS_MAX_PRIMITIVES_PER_FLUSH || rp->num_instances == 0 ||
 		    rp->num_instances > PGS_MAX_RENDER_PASS_INSTANCES || rp->coarse_tile_size_log2 < 3 ||
 		    rp->coarse_tile_size_log2 > 7)
@@ -713,7 +732,32 @@ struct CudaBackend
 		p.has_scanmsk = rp->has_scanmsk;
 		p.num_instances = rp->num_instances;
 		memcpy(p.instances, rp->instances, sizeof(p.instances));
+		p.num_snaps = std::min<uint32_t>(rp->num_snapshots, snapshots_taken);
+		for (uint32_t k = 0; k < p.num_snaps; k++)
+			p.snap_limit[k] = std::min(rp->snapshot_textures[k], rp->num_textures);
+		snapshots_taken = 0;
 		return submit(op);
+	}
+
+	// snapshot_vram: all planes into the pass's next slot, in stream order.
+	int snapshot_vram()
+	{
+		if (snapshots_taken >= PGS_MAX_VRAM_SNAPSHOTS)
+			return PGS_ERROR_CAPACITY;
+		const uint32_t slot = snapshots_taken;
+		if (!d_tex_snap[slot])
+		{
+			CUDA_TRY(cudaMalloc(&d_tex_snap[slot], size_t(max_planes) * VRAM_SIZE));
+			if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+		}
+		Op op = {};
+		op.type = OP_SNAPSHOT;
+		op.snap_slot = slot;
+		int r = submit(op);
+		if (r)
+			return r;
+		snapshots_taken++;
+		return int(slot);
 	}
 
 	int copy_vram(const pgs_copy_desc *d)
@@ -767,7 +811,7 @@ struct CudaBackend
 		c.csm2_x_scale = u->csm2_x_scale;
 		c.csm2_x_bias = u->csm2_x_bias;
 		c.base_instance = u->base_instance % PGS_CLUT_INSTANCES;
-		last_clut = (last_clut + 1) % PGS_CLUT_INSTANCES;
+		last_clut = u->target ? (u->target - 1u) % PGS_CLUT_INSTANCES : (last_clut + 1) % PGS_CLUT_INSTANCES;
 		c.instance = last_clut;
 		int r = submit(op);
 		return r ? r : int(c.instance);
@@ -1062,6 +1106,10 @@ struct CudaBackend
 		}
 		case OP_PASS:
 			return execute_pass(op.pass);
+		case OP_SNAPSHOT:
+			CUDA_TRY(cudaMemcpyAsync(d_tex_snap[op.snap_slot], d_vram, size_t(max_planes) * VRAM_SIZE,
+			                         cudaMemcpyDeviceToDevice, stream));
+			return PGS_OK;
 		}
 		return PGS_ERROR_INVALID_ARGUMENT;
 	}
@@ -1243,6 +1291,12 @@ struct CudaBackend
 		P.has_scanmsk = p.has_scanmsk;
 		P.has_ss_reference = num_planes > 1;
 		P.vram = d_vram;
+		P.num_snaps = p.num_snaps;
+		for (uint32_t k = 0; k < p.num_snaps; k++)
+		{
+			P.snap_vram[k] = d_tex_snap[k];
+			P.snap_limit[k] = p.snap_limit[k];
+		}
 		P.clut = d_clut;
 		P.rcp_float_lut = d_rcp_float;
 		P.unorm_lut = d_unorm_lut;
@@ -2248,10 +2302,11 @@ static int c_vsync(void *self, const pgs_merge_params *m, void *dst)
 	return m && dst ? B(self)->vsync(*m, dst) : PGS_ERROR_INVALID_ARGUMENT;
 }
 static int c_timestamps(void *self, int enable, double *totals) { return B(self)->timestamps(enable, totals); }
+static int c_snapshot(void *self) { return B(self)->snapshot_vram(); }
 
 const pgs_backend_ops CUDA_OPS = {
 	PGS_ABI_VERSION, c_destroy, c_reserve, c_flush_rendering, c_copy, c_palette, c_set_ss, c_submit, c_read, c_write, c_error,
-	c_read_async, c_wait, c_circuit, c_vsync, c_timestamps,
+	c_read_async, c_wait, c_circuit, c_vsync, c_timestamps, c_snapshot,
 };
 
 // ---------------------------------------------------------------------------

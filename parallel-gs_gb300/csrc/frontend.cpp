@@ -252,6 +252,29 @@ struct pgs_gs : TrackerClient
 	pgs_debug_mode debug_mode = {};
 	uint32_t clut_instance = 0;
 	uint32_t pending_palette_updates = 0;
+	// CLUT ring numbering of the reference's renderer (update_palette_cache,
+	// rewind_clut_instance, gs/gs_renderer.cpp:3364-3419): the newest slot,
+	// whether a texture read it since it was written, and the loads not yet
+	// flushed to the cache (format bits and the slot each started from).
+	uint32_t ring_next = 0, latest_clut_instance = 0;
+	bool ring_last_read = false;
+	struct RingLoad
+	{
+		uint32_t cpsm, csa;
+		bool is8;
+		uint32_t incoming;
+	};
+	std::vector<RingLoad> ring_pending;
+	// Palette loads of the pass that can be reused by an identical load
+	// (memoized_palettes, gs/gs_interface.cpp:685-799): a sliding window.
+	struct MemoizedPalette
+	{
+		uint32_t instance, csa_mask;
+		uint64_t tex0, texclut;
+		uint32_t incoming;
+	};
+	MemoizedPalette memo[16];
+	uint32_t num_memo = 0;
 	int32_t ofx = 0, ofy = 0;
 
 	// Cached primitive template; recomputed when template_dirty is set.
@@ -383,6 +406,9 @@ struct pgs_gs : TrackerClient
 	// to end the pass first.
 	uint32_t pass_tex_blocks[NUM_PAGES] = {};
 	std::vector<uint16_t> pass_tex_pages;
+	// VRAM snapshots of the open pass and the texture count at each.
+	uint32_t num_snapshots = 0;
+	uint32_t snapshot_textures[PGS_MAX_VRAM_SNAPSHOTS] = {};
 
 	struct
 	{
@@ -463,6 +489,14 @@ struct pgs_gs : TrackerClient
 	// GSInterface::flush(flags, reason) (gs/gs_interface.cpp:353-420).
 	void tracker_flush(uint32_t flags, uint32_t reason) override
 	{
+		if (flags & TRACKER_FLUSH_CACHE)
+		{
+			// flush_cache_upload: pending CLUT loads reach the ring, and
+			// memoised palettes are forgotten (gs/gs_interface.cpp:386-393).
+			tracker.clear_cache_pages();
+			ring_pending.clear();
+			num_memo = 0;
+		}
 		if (flags & TRACKER_FLUSH_FB)
 			do_flush_render_pass(reason);
 		if (reason == FLUSH_PRESSURE)
@@ -491,6 +525,7 @@ struct pgs_gs : TrackerClient
 
 	void tracker_forget_memoization() override
 	{
+		num_memo = 0;
 		mark_texture_state_dirty();
 	}
 
@@ -530,6 +565,35 @@ struct pgs_gs : TrackerClient
 			}
 	}
 
+	// A transfer or host write is about to replace blocks that textures of
+	// the open pass read.  The reference samples those textures from cache
+	// images taken before (flush_cached); here the textures held so far decode
+	// from a VRAM snapshot taken now, or the pass ends where the backend keeps
+	// no snapshots.
+	void protect_pass_textures(const PageRect &r, uint32_t reason)
+	{
+		if (!pass_texture_hit(r))
+			return;
+		if (ops->abi_version >= 5 && ops->snapshot_vram && num_snapshots < PGS_MAX_VRAM_SNAPSHOTS)
+		{
+			int slot = ops->snapshot_vram(be);
+			if (slot >= 0)
+			{
+				snapshot_textures[num_snapshots++] = uint32_t(textures.size());
+				for (uint16_t p : pass_tex_pages)
+					pass_tex_blocks[p] = 0;
+				pass_tex_pages.clear();
+				return;
+			}
+			if (slot != PGS_ERROR_CAPACITY)
+			{
+				sticky_error = slot;
+				return;
+			}
+		}
+		flush_render_pass(reason);
+	}
+
 	bool pass_texture_hit(const PageRect &r) const
 	{
 		if (pass_tex_pages.empty())
@@ -565,6 +629,8 @@ struct pgs_gs : TrackerClient
 			rp.has_ss_textures = has_ss_textures;
 			rp.field_aware = field_aware;
 			rp.blend_demote = hack_blend_demote;
+			rp.num_snapshots = num_snapshots;
+			memcpy(rp.snapshot_textures, snapshot_textures, sizeof(snapshot_textures));
 
 			uint64_t binning_cost = 0;
 			for (uint32_t i = 0; i < num_instances; i++)
@@ -660,6 +726,15 @@ struct pgs_gs : TrackerClient
 			pending.passes += rp.num_instances;
 			check_pending_work();
 		}
+		else if (num_snapshots)
+		{
+			// Release the snapshot slots of a pass that drew nothing.
+			pgs_render_pass empty = {};
+			int r = ops->flush_rendering(be, &empty);
+			if (r != 0)
+				sticky_error = r;
+		}
+		num_snapshots = 0;
 
 		Instance keep = instances[current_instance];
 		for (auto &inst : instances)
@@ -690,6 +765,15 @@ struct pgs_gs : TrackerClient
 		for (uint16_t p : pass_tex_pages)
 			pass_tex_blocks[p] = 0;
 		pass_tex_pages.clear();
+		// A pass that ended on an older memoised palette rewinds the ring
+		// (rewind_clut_instance, gs/gs_renderer.cpp:3384-3398).
+		if (clut_instance != ring_next)
+		{
+			tracker.register_clut_read(PageRect(), 0xffffffffu);
+			tracker.invalidate_texture_cache(clut_instance);
+		}
+		ring_next = clut_instance;
+		latest_clut_instance = clut_instance;
 		reserve_buffers();
 	}
 
@@ -724,8 +808,7 @@ struct pgs_gs : TrackerClient
 			const PageRect src = compute_page_rect(sbp, ssax, ssay, rrw, rrh, sbw, spsm);
 			tracker.mark_transfer_copy(dst, src);
 			tracker.invalidate_texture_cache(clut_instance);
-			if (pass_texture_hit(dst))
-				flush_render_pass(FLUSH_COPY_HAZARD);
+			protect_pass_textures(dst, FLUSH_COPY_HAZARD);
 			pending.copies++;
 			pending.copy_threads += uint64_t(rrw) * rrh;
 			check_pending_work();
@@ -815,8 +898,7 @@ struct pgs_gs : TrackerClient
 				tracker.commit_host_write(dst);
 			else
 				tracker.mark_transfer_write(dst);
-			if (pass_texture_hit(dst))
-				flush_render_pass(FLUSH_COPY_HAZARD);
+			protect_pass_textures(dst, FLUSH_COPY_HAZARD);
 			pending.copies++;
 			pending.copy_threads += uint64_t(rrw) * rrh;
 			if (!host_copy)
@@ -929,18 +1011,99 @@ struct pgs_gs : TrackerClient
 		u.csm2_x_scale = 1.0f;
 		u.csm2_x_bias = 0;
 		u.base_instance = clut_instance;
+
+		// An identical load earlier in the pass is reused, unless a later
+		// partial load changed banks it did not write (gs/gs_interface.cpp:685-729).
+		uint32_t punchthrough = UINT32_MAX;
+		for (uint32_t i = num_memo; i; i--)
+		{
+			const MemoizedPalette &m = memo[i - 1];
+			if (m.csa_mask & ~csa_mask)
+			{
+				if (punchthrough != UINT32_MAX || m.csa_mask != UINT32_MAX)
+					break;
+				punchthrough = m.instance;
+				continue;
+			}
+			if (m.csa_mask == csa_mask && m.tex0 == u.tex0 && m.texclut == u.texclut)
+			{
+				if (punchthrough != UINT32_MAX && punchthrough != m.incoming)
+					break;
+				if (m.instance != clut_instance)
+					mark_texture_state_dirty();
+				clut_instance = m.instance;
+				if (i < num_memo)
+				{
+					MemoizedPalette moved = m;
+					memmove(memo + i - 1, memo + i, (num_memo - i) * sizeof(memo[0]));
+					moved.csa_mask = csa_mask;
+					moved.tex0 = u.tex0;
+					moved.texclut = u.texclut;
+					moved.incoming = u.base_instance;
+					memo[num_memo - 1] = moved;
+				}
+				return;
+			}
+		}
+
+		// A load nothing has read yet is rewritten in place by one that
+		// replaces it (same CPSM, CSA and index width), starting from the
+		// same palette (update_palette_cache, gs/gs_renderer.cpp:3400-3419).
+		const bool numbered = ops->abi_version >= 5;
+		const bool replace = numbered && !ring_last_read && !ring_pending.empty() &&
+		                     ring_pending.back().cpsm == cpsm && ring_pending.back().csa == csa &&
+		                     ring_pending.back().is8 == is8;
+		uint32_t incoming = clut_instance;
+		if (replace)
+			u.base_instance = ring_pending.back().incoming;
+		else
+		{
+			ring_next = (ring_next + 1) % PGS_CLUT_INSTANCES;
+			ring_pending.push_back({ cpsm, csa, is8, clut_instance });
+			pending.palettes++;
+		}
+		ring_last_read = false;
+		if (numbered)
+			u.target = ring_next + 1;
 		int inst = ops->update_palette_cache(be, &u);
 		if (inst < 0)
 		{
 			sticky_error = inst;
 			return;
 		}
+		if (!numbered)
+			ring_next = uint32_t(inst);
 		clut_instance = uint32_t(inst);
 		template_dirty = true;
 		stats.num_palette_updates++;
-		pending_palette_updates++;
-		if (pending_palette_updates >= PGS_CLUT_INSTANCES - 1)
-			flush_render_pass(FLUSH_OVERFLOW);
+		check_pending_work();
+		const bool replacing = latest_clut_instance == clut_instance;
+		latest_clut_instance = clut_instance;
+		mark_texture_state_dirty();
+		if (replacing)
+		{
+			// The replaced load's memo entry goes; the new one keeps its start.
+			for (uint32_t i = 0; i < num_memo; i++)
+				if (memo[i].instance == clut_instance)
+				{
+					incoming = memo[i].incoming;
+					num_memo--;
+					memmove(memo + i, memo + i + 1, (num_memo - i) * sizeof(memo[0]));
+					break;
+				}
+		}
+		if (num_memo == 16)
+		{
+			memmove(memo, memo + 1, 15 * sizeof(memo[0]));
+			num_memo--;
+		}
+		memo[num_memo++] = { clut_instance, csa_mask, u.tex0, u.texclut, incoming };
+		if (!replacing)
+		{
+			pending_palette_updates++;
+			if (pending_palette_updates >= PGS_CLUT_INSTANCES)
+				flush_render_pass(FLUSH_OVERFLOW);
+		}
 	}
 
 	void handle_miptbl_gen(uint32_t ctx)
@@ -1806,6 +1969,9 @@ struct pgs_gs : TrackerClient
 				d.ta0 = field(texa, 0, 8);
 				d.ta1 = field(texa, 32, 8);
 			}
+			// The newest CLUT load is now in use (mark_clut_read).
+			if (clut_instance == ring_next)
+				ring_last_read = true;
 			csa_mask = (t.psm == PSMT8 || t.psm == PSMT8H) ? 0xffffu : 1u;
 			csa_mask <<= d.csa;
 			if (cpsm == PSMCT32)
@@ -1926,6 +2092,7 @@ struct pgs_gs : TrackerClient
 		// Mip levels sampled (compute_effective_texture_rect,
 		// gs/gs_renderer.cpp:1235-1265); MXL only counts with a mipmapping MMIN.
 		const uint32_t mxl = (tex1.mmin_has_mipmap() && !hack_disable_mipmaps) ? tex1.mxl : 0;
+		d.mxl = mxl;
 		const uint32_t max_levels = std::min<uint32_t>(7, std::min(d.tw_log2, d.th_log2) + 1);
 		d.levels = std::min<uint32_t>(mxl + 1, max_levels);
 		const Extent ue = effective_extent(1u << d.tw_log2, d.wms, d.minu, d.maxu, d.levels);
@@ -3324,8 +3491,7 @@ int pgs_gs_write_vram(pgs_gs *gs, uint64_t offset, uint64_t size, const void *sr
 		gs->submit();
 	}
 	// Textures of the open pass are decoded when it begins.
-	if (gs->pass_texture_hit(r))
-		gs->flush_render_pass(PGS_FLUSH_HOST_ACCESS);
+	gs->protect_pass_textures(r, PGS_FLUSH_HOST_ACCESS);
 	int st = gs->ops->write_vram(gs->be, offset, size, src);
 	// The host write replaces these pages (commit_host_write,
 	// gs/page_tracker.cpp:700-715).

@@ -134,6 +134,11 @@ constexpr uint8_t HEURISTIC_CLEAR_SNAP_ATTRIBUTE = 2;
 
 struct PassParams
 {
+	// Textures [snap_limit[k - 1], snap_limit[k]) are decoded from
+	// snap_vram[k], the rest from vram.
+	const uint8_t *snap_vram[PGS_MAX_VRAM_SNAPSHOTS];
+	uint32_t snap_limit[PGS_MAX_VRAM_SNAPSHOTS];
+	uint32_t num_snaps;
 	const pgs_vertex_position *pos;
 	const pgs_vertex_attribute *attr;
 	pgs_primitive_attribute *prims;
@@ -1045,11 +1050,20 @@ __device__ __forceinline__ uint32_t clut_color(const PassParams &P, const pgs_te
 	return uint32_t(__ldg(cl + bi)) | (uint32_t(__ldg(cl + bi + 256u)) << 16);
 }
 
-__device__ __forceinline__ uint32_t fetch_texel(const PassParams &P, const pgs_texture_desc &t, uint32_t tbp,
-                                                uint32_t tbw, int32_t x, int32_t y)
+// The VRAM a texture of the pass decodes from: a snapshot taken before a
+// transfer overwrote its source, or VRAM as the pass begins.
+__device__ __forceinline__ const uint8_t *texture_source(const PassParams &P, uint32_t tex)
+{
+	for (uint32_t k = 0; k < P.num_snaps; k++)
+		if (tex < P.snap_limit[k])
+			return P.snap_vram[k];
+	return P.vram;
+}
+
+__device__ __forceinline__ uint32_t fetch_texel(const PassParams &P, const uint8_t *v, const pgs_texture_desc &t,
+                                                uint32_t tbp, uint32_t tbw, int32_t x, int32_t y)
 {
 	uint32_t a = swizzle_address(uint32_t(x), uint32_t(y), tbp, tbw, t.psm);
-	const uint8_t *v = P.vram;
 	switch (t.psm)
 	{
 	case PSMCT24: case PSMZ24:
@@ -1068,11 +1082,10 @@ __device__ __forceinline__ uint32_t fetch_texel(const PassParams &P, const pgs_t
 // Texel of sample `s` of a super-sampled texture: the single-sampled texel
 // unless the reference plane marks it super-sampled (upload.comp
 // SUPER_SAMPLED, :131-220; 24-bit formats merge by the reference bits).
-__device__ __forceinline__ uint32_t fetch_texel_sample(const PassParams &P, const pgs_texture_desc &t, int32_t x, int32_t y,
-                                                       uint32_t s)
+__device__ __forceinline__ uint32_t fetch_texel_sample(const PassParams &P, const uint8_t *v, const pgs_texture_desc &t,
+                                                       int32_t x, int32_t y, uint32_t s)
 {
 	const uint32_t a = swizzle_address(uint32_t(x), uint32_t(y), t.tbp0, t.tbw, t.psm);
-	const uint8_t *v = P.vram;
 	const uint32_t *v32 = reinterpret_cast<const uint32_t *>(v);
 	const uint16_t *v16 = reinterpret_cast<const uint16_t *>(v);
 	const uint32_t V32 = VRAM_SIZE / 4, V16 = VRAM_SIZE / 2, V8 = VRAM_SIZE;
@@ -1153,9 +1166,10 @@ __global__ void __launch_bounds__(256) texture_decode_kernel(PassParams P)
 	if (i >= im.ext_u * im.ext_v)
 		return;
 	const int32_t x = int32_t(i % im.ext_u), y = int32_t(i / im.ext_u);
+	const uint8_t *src = texture_source(P, tex);
 	if (t.samples > 1 && level > 0)
 	{
-		P.texels[im.offset + i] = fetch_texel_sample(P, t, x, y, level - 1u);
+		P.texels[im.offset + i] = fetch_texel_sample(P, src, t, x, y, level - 1u);
 		return;
 	}
 	uint32_t tbp = t.tbp0, tbw = t.tbw;
@@ -1164,7 +1178,7 @@ __global__ void __launch_bounds__(256) texture_decode_kernel(PassParams P)
 		tbp = t.mip[level - 1] & 0x3fffu;
 		tbw = t.mip[level - 1] >> 16;
 	}
-	P.texels[im.offset + i] = fetch_texel(P, t, tbp, tbw, x, y);
+	P.texels[im.offset + i] = fetch_texel(P, src, t, tbp, tbw, x, y);
 }
 
 // log2 of a positive normal float: ln m = 2 atanh(s), s = (m - 1) / (m + 1),

@@ -1254,3 +1254,138 @@ def write_dump(path, transfers, vram: bytes | None = None, regs: dict | None = N
         out += bytes([1, f])
     with open(path, "wb") as fh:
         fh.write(bytes(out))
+
+
+def frame_hazards(seed: int, ops: int = 60, width: int = 256, height: int = 128) -> Frame:
+    """A stream made to hit the hazard rules: two CT32 framebuffers A (page 0)
+    and B (page 64) with one depth buffer, textures placed on framebuffer pages
+    (render to texture), on top of the framebuffer being drawn (feedback) and
+    on free pages, uploads into textures the open pass already samples (some
+    split around a draw, so part of the image arrives later), LOCAL->LOCAL
+    copies out of the framebuffers, CLUT reloads (repeated loads for palette
+    memoisation, CLD compare modes, palettes on written pages), TEXFLUSH, FRAME
+    switches and region clamps.  1x or 4x super-sampling."""
+    rng = np.random.Generator(np.random.PCG64(90000 + seed))
+    s = GifStream()
+    ss = [1, 4][int(rng.integers(0, 2))]
+    fbw = width // 64
+    fb_pages = [0, 64]
+    zbp = 160
+    s.ad([(PRMODECONT, 1), (FRAME_1, frame_reg(fb_pages[0], fbw, PSMCT32)), (ZBUF_1, zbuf_reg(zbp, PSMZ24)),
+          (SCISSOR_1, scissor_reg(0, width - 1, 0, height - 1)), (XYOFFSET_1, 0),
+          (TEST_1, test_reg(zte=1, ztst=2)), (ALPHA_1, alpha_reg(0, 1, 0, 1))])
+    # Free texture pages from 200 on: CT32 textures and PSMT8 ones with CLUTs.
+    free = []
+    page = 200
+    for _ in range(4):
+        tw, th = int(rng.integers(4, 7)), int(rng.integers(4, 7))
+        w, h = 1 << tw, 1 << th
+        s.upload(page * BLOCKS_PER_PAGE, max(1, w // 64), PSMCT32, 0, 0, w, h,
+                 rng.integers(0, 256, size=w * h * 4, dtype=np.uint8).tobytes())
+        free.append((page * BLOCKS_PER_PAGE, max(1, w // 64), PSMCT32, tw, th))
+        page += 4
+    clut_pages = [page, page + 1]
+    for cp in clut_pages:
+        s.upload(cp * BLOCKS_PER_PAGE, 1, PSMCT32, 0, 0, 16, 16, rng.integers(0, 256, size=16 * 16 * 4, dtype=np.uint8).tobytes())
+    t8 = (page + 2) * BLOCKS_PER_PAGE
+    s.upload(t8, 2, PSMT8, 0, 0, 64, 64, rng.integers(0, 256, size=64 * 64, dtype=np.uint8).tobytes())
+    current_fb = 0
+    count = 0
+    for _ in range(ops):
+        op = rng.uniform()
+        if op < 0.45:
+            # Draw a few primitives into the current framebuffer.
+            n = int(rng.integers(1, 12))
+            textured = rng.uniform() < 0.7
+            regs = []
+            if rng.uniform() < 0.25:
+                current_fb ^= 1
+                regs.append((FRAME_1, frame_reg(fb_pages[current_fb], fbw, PSMCT32)))
+            if textured:
+                kind = rng.uniform()
+                if kind < 0.3:
+                    # Render to texture: sample the other framebuffer.
+                    tbp = fb_pages[current_fb ^ 1] * BLOCKS_PER_PAGE
+                    tex0 = tex0_reg(tbp, fbw, PSMCT32, 8, 7)
+                elif kind < 0.45:
+                    # Sample the framebuffer being drawn.
+                    tbp = fb_pages[current_fb] * BLOCKS_PER_PAGE
+                    tex0 = tex0_reg(tbp, fbw, PSMCT32, 8, 7)
+                elif kind < 0.75:
+                    tbp, tbw, psm, tw, th = free[int(rng.integers(0, len(free)))]
+                    tex0 = tex0_reg(tbp, tbw, psm, tw, th)
+                else:
+                    cld = [1, 1, 2, 4][int(rng.integers(0, 4))]
+                    cbp = clut_pages[int(rng.integers(0, 2))] * BLOCKS_PER_PAGE
+                    tex0 = tex0_reg(t8, 2, PSMT8, 6, 6, cbp=cbp, cpsm=PSMCT32, cld=cld)
+                regs.append((TEX0_1, tex0))
+                wms, wmt = int(rng.integers(0, 3)), int(rng.integers(0, 3))
+                regs.append((CLAMP_1, clamp_reg(wms, wmt, int(rng.integers(0, 32)), int(rng.integers(32, 128)),
+                                                int(rng.integers(0, 32)), int(rng.integers(32, 128)))))
+                regs.append((TEX1_1, tex1_reg(mmag=int(rng.integers(0, 2)), mmin=int(rng.integers(0, 2)))))
+            s.ad(regs)
+            sprite = rng.uniform() < 0.5
+            if sprite:
+                xs, ys = random_sprites(rng, n, width, height, 4, 2000)
+                nv = 2
+            else:
+                xs, ys = random_triangles(rng, n, width, height, 4, 2000)
+                nv = 3
+            q = np.zeros((n * nv, 3, 2), dtype=np.uint64)
+            q[:, 0] = q_rgbaq(rng.integers(0, 256, size=(n * nv, 4)))
+            q[:, 1] = q_uv(rng.integers(0, width * 16, n * nv), rng.integers(0, height * 16, n * nv))
+            q[:, 2] = q_xyz2(xs.reshape(-1), ys.reshape(-1), rng.integers(0, 1 << 24, n * nv))
+            prim = prim_reg(PRIM_SPRITE if sprite else PRIM_TRI, iip=1, tme=int(textured), fst=1,
+                            abe=int(rng.uniform() < 0.3))
+            s.packed(prim, [D_RGBAQ, D_UV, D_XYZ2], q.reshape(-1, 2))
+            count += n
+        elif op < 0.6:
+            # Upload into a texture that may be in use; sometimes split around a draw.
+            tbp, tbw, psm, tw, th = free[int(rng.integers(0, len(free)))]
+            w, h = 1 << tw, 1 << th
+            x, y = int(rng.integers(0, w // 2)), int(rng.integers(0, h // 2))
+            uw, uh = int(rng.integers(1, w - x + 1)), int(rng.integers(2, h - y + 1)) & ~1
+            uh = max(uh, 2)
+            data = rng.integers(0, 256, size=uw * uh * 4, dtype=np.uint8).tobytes()
+            if rng.uniform() < 0.3 and len(data) >= 64:
+                half = (len(data) // 2) & ~15
+                s.ad([(BITBLTBUF, bitbltbuf_reg(dbp=tbp, dbw=tbw, dpsm=psm)), (TRXPOS, trxpos_reg(dsax=x, dsay=y)),
+                      (TRXREG, trxreg_reg(uw, uh)), (TRXDIR, 0)])
+                s.image(data[:half])
+                # A draw sampling the texture before the rest of the image.
+                s.ad([(TEX0_1, tex0_reg(tbp, tbw, psm, tw, th))])
+                xs, ys = random_sprites(rng, 1, width, height, 16, 400)
+                qq = np.zeros((2, 3, 2), dtype=np.uint64)
+                qq[:, 0] = q_rgbaq(rng.integers(0, 256, size=(2, 4)))
+                qq[:, 1] = q_uv(rng.integers(0, w * 16, 2), rng.integers(0, h * 16, 2))
+                qq[:, 2] = q_xyz2(xs.reshape(-1), ys.reshape(-1), np.array([1, 1]))
+                s.packed(prim_reg(PRIM_SPRITE, tme=1, fst=1), [D_RGBAQ, D_UV, D_XYZ2], qq.reshape(-1, 2))
+                s.image(data[half:])
+                count += 1
+            else:
+                s.upload(tbp, tbw, psm, x, y, uw, uh, data)
+        elif op < 0.72:
+            # Copy a framebuffer rectangle into a free texture or the other framebuffer.
+            src = fb_pages[int(rng.integers(0, 2))] * BLOCKS_PER_PAGE
+            if rng.uniform() < 0.5:
+                dst, dbw = free[int(rng.integers(0, len(free)))][:2]
+            else:
+                dst, dbw = fb_pages[int(rng.integers(0, 2))] * BLOCKS_PER_PAGE, fbw
+            cw, ch = int(rng.integers(8, 64)), int(rng.integers(8, 64))
+            s.ad([(BITBLTBUF, bitbltbuf_reg(sbp=src, sbw=fbw, spsm=PSMCT32, dbp=dst, dbw=dbw, dpsm=PSMCT32)),
+                  (TRXPOS, trxpos_reg(ssax=int(rng.integers(0, width - cw)), ssay=int(rng.integers(0, height - ch)),
+                                      dsax=int(rng.integers(0, 32)), dsay=int(rng.integers(0, 32)))),
+                  (TRXREG, trxreg_reg(cw, ch)), (TRXDIR, 2)])
+        elif op < 0.85:
+            # CLUT reload, often identical to an earlier one.
+            cbp = clut_pages[int(rng.integers(0, 2))] * BLOCKS_PER_PAGE
+            cld = [1, 1, 1, 2, 3, 4, 5][int(rng.integers(0, 7))]
+            s.ad([(TEX0_1, tex0_reg(t8, 2, PSMT8, 6, 6, cbp=cbp, cpsm=PSMCT32, cld=cld))])
+        elif op < 0.93:
+            s.ad([(TEXFLUSH, 0)])
+        else:
+            # A palette page rewritten by the host.
+            cp = clut_pages[int(rng.integers(0, 2))]
+            s.upload(cp * BLOCKS_PER_PAGE, 1, PSMCT32, 0, 0, 16, 16,
+                     rng.integers(0, 256, size=16 * 16 * 4, dtype=np.uint8).tobytes())
+    return Frame("hazards_%d" % seed, s.tobytes(), ss, True, count, {})

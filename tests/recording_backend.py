@@ -34,7 +34,7 @@ class TextureDesc(C.Structure):
     _fields_ = [(n, C.c_uint32) for n in ("tbp0", "tbw", "psm", "tw_log2", "th_log2", "cpsm", "csa", "clut_instance",
                                           "aem", "ta0", "ta1", "wms", "wmt", "minu", "maxu", "minv", "maxv",
                                           "levels")] + \
-               [("mip", C.c_uint32 * 6), ("samples", C.c_uint32), ("padding", C.c_uint32)]
+               [("mip", C.c_uint32 * 6), ("samples", C.c_uint32), ("mxl", C.c_uint32)]
 
 
 class RPInstance(C.Structure):
@@ -53,7 +53,8 @@ class RenderPass(C.Structure):
                 ("instances", RPInstance * 8), ("num_instances", C.c_uint32),
                 ("coarse_tile_size_log2", C.c_uint32), ("has_aa1", C.c_uint32), ("has_scanmsk", C.c_uint32),
                 ("flush_reason", C.c_uint32), ("has_mipmap", C.c_uint32), ("has_ss_textures", C.c_uint32),
-                ("field_aware", C.c_uint32), ("blend_demote", C.c_uint32)]
+                ("field_aware", C.c_uint32), ("blend_demote", C.c_uint32), ("num_snapshots", C.c_uint32),
+                ("snapshot_textures", C.c_uint32 * 4)]
 
 
 class CopyDesc(C.Structure):
@@ -64,7 +65,7 @@ class CopyDesc(C.Structure):
 
 class PaletteUpload(C.Structure):
     _fields_ = [("tex0", C.c_uint64), ("texclut", C.c_uint64), ("csm2_x_scale", C.c_float),
-                ("csm2_x_bias", C.c_uint32), ("base_instance", C.c_uint32), ("padding", C.c_uint32)]
+                ("csm2_x_bias", C.c_uint32), ("base_instance", C.c_uint32), ("target", C.c_uint32)]
 
 
 DESTROY = C.CFUNCTYPE(None, C.c_void_p)
@@ -85,7 +86,8 @@ class Ops(C.Structure):
     _fields_ = [("abi_version", C.c_uint32), ("destroy", DESTROY), ("reserve", RESERVE), ("flush", FLUSH),
                 ("copy", COPY), ("palette", PALETTE), ("set_ss", SETSS), ("submit", SUBMIT), ("read", READ),
                 ("write", WRITE), ("error", ERROR), ("read_async", C.c_void_p), ("wait_ticket", C.c_void_p),
-                ("sample_circuit", C.c_void_p), ("vsync", VSYNC)]
+                ("sample_circuit", C.c_void_p), ("vsync", VSYNC), ("timestamps", C.c_void_p),
+                ("snapshot_vram", SUBMIT)]
 
 
 def _struct_array(ptr, n, fields):
@@ -99,15 +101,18 @@ class RecordingBackend(pgs.Backend):
     def __init__(self, max_samples_log2: int = 4):
         self.max_samples_log2 = max_samples_log2
         self.passes, self.copies, self.palettes, self.ss = [], [], [], []
+        # Every call in order: ("pass", i), ("copy", i), ("palette", i).
+        self.events = []
         self.vram = np.zeros(pgs.VRAM_SIZE, dtype=np.uint8)
         self.next_clut = 0
         self._pos = (VertexPosition * (3 * MAXP))()
         self._attr = (VertexAttribute * (3 * MAXP))()
         self._prim = (PrimitiveAttribute * MAXP)()
         self.vsyncs = 0
-        self._cbs = Ops(3, DESTROY(lambda s: None), RESERVE(self._reserve), FLUSH(self._flush), COPY(self._copy),
+        self._cbs = Ops(5, DESTROY(lambda s: None), RESERVE(self._reserve), FLUSH(self._flush), COPY(self._copy),
                         PALETTE(self._palette), SETSS(self._set_ss), SUBMIT(lambda s: 0), READ(self._read),
-                        WRITE(self._write), ERROR(self._error), None, None, None, VSYNC(self._vsync))
+                        WRITE(self._write), ERROR(self._error), None, None, None, VSYNC(self._vsync), None,
+                        SUBMIT(self._snapshot))
         super().__init__(C.addressof(self._cbs), 1)
 
     def _reserve(self, s, n, pos, attr, prim):
@@ -132,8 +137,13 @@ class RecordingBackend(pgs.Backend):
             "has_aa1": rp.has_aa1, "has_scanmsk": rp.has_scanmsk, "flush_reason": rp.flush_reason,
             "has_mipmap": rp.has_mipmap, "has_ss_textures": rp.has_ss_textures,
             "field_aware": rp.field_aware, "blend_demote": rp.blend_demote,
+            "snapshot_textures": list(rp.snapshot_textures)[:rp.num_snapshots],
         }
+        self.snapshots_taken = 0
+        if n == 0:
+            return 0
         self.passes.append(rec)
+        self.events.append(("pass", len(self.passes) - 1))
         return 0
 
     def _copy(self, s, dp):
@@ -141,14 +151,21 @@ class RecordingBackend(pgs.Backend):
         data = C.string_at(d.host_data, d.host_size) if d.host_data else b""
         self.copies.append({"bitbltbuf": d.bitbltbuf, "trxpos": d.trxpos, "trxreg": d.trxreg, "trxdir": d.trxdir,
                             "data": data, "offset": d.host_offset, "required": d.host_required})
+        self.events.append(("copy", len(self.copies) - 1))
         return 0
 
     def _palette(self, s, up):
         u = up.contents
-        self.next_clut = (self.next_clut + 1) % 1024
+        self.next_clut = (u.target - 1) % 1024 if u.target else (self.next_clut + 1) % 1024
         self.palettes.append({"tex0": u.tex0, "texclut": u.texclut, "base_instance": u.base_instance,
                               "instance": self.next_clut})
+        self.events.append(("palette", len(self.palettes) - 1))
         return self.next_clut
+
+    def _snapshot(self, s):
+        self.events.append(("snapshot", len(self.passes)))
+        self.snapshots_taken = getattr(self, "snapshots_taken", 0) + 1
+        return self.snapshots_taken - 1
 
     def _set_ss(self, s, x, y):
         # Like a backend created with max_samples_log2 sample planes.

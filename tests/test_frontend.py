@@ -181,18 +181,38 @@ def test_state_vector_dedup_and_blend_bits():
 
 
 def test_clut_load_modes():
+    """CLD decides which TEX0 writes load the CLUT (handle_clut_upload,
+    gs/gs_interface.cpp:563-589).  Loads from distinct sources all reach the
+    backend; none is read by a draw in between, so each replaces the last in
+    its ring slot, starting from the same palette (update_palette_cache,
+    gs/gs_renderer.cpp:3400-3419).  An identical load is reused instead
+    (palette memoisation).  The reference frontend makes the same loads."""
     def build(s):
         setup(s)
-        base = g.tex0_reg(0x2000, 4, g.PSMT8, 8, 8, cbp=0x3000, cpsm=g.PSMCT32)
-        s.ad([(g.TEX0_1, base | (1 << 61))])            # CLD=1: load
-        s.ad([(g.TEX0_1, base)])                        # CLD=0: no load
-        s.ad([(g.TEX0_1, base | (2 << 61))])            # CLD=2: load, CBP0 := CBP
-        s.ad([(g.TEX0_1, base | (4 << 61))])            # CLD=4: compare CBP0, equal -> no load
-        other = g.tex0_reg(0x2000, 4, g.PSMT8, 8, 8, cbp=0x3010, cpsm=g.PSMCT32)
-        s.ad([(g.TEX0_1, other | (4 << 61))])           # CBP differs -> load
+        def tex0(cbp, cld):
+            return g.tex0_reg(0x2000, 4, g.PSMT8, 8, 8, cbp=cbp, cpsm=g.PSMCT32) | (cld << 61)
+        s.ad([(g.TEX0_1, tex0(0x3000, 1))])   # CLD=1: load
+        s.ad([(g.TEX0_1, tex0(0x3000, 0))])   # CLD=0: no load
+        s.ad([(g.TEX0_1, tex0(0x3020, 2))])   # CLD=2: load, CBP0 := CBP
+        s.ad([(g.TEX0_1, tex0(0x3020, 4))])   # CLD=4: CBP0 equal -> no load
+        s.ad([(g.TEX0_1, tex0(0x3010, 4))])   # CBP differs -> load
+        s.ad([(g.TEX0_1, tex0(0x3010, 1))])   # identical to the last load -> reused
     be = run(build=build)
-    assert len(be.palettes) == 3
-    assert [p["base_instance"] for p in be.palettes] == [0, 1, 2]
+    cbps = [(p["tex0"] >> 37) & 0x3fff for p in be.palettes]
+    assert cbps == [0x3000, 0x3020, 0x3010]
+    assert [p["instance"] for p in be.palettes] == [1, 1, 1]
+    assert [p["base_instance"] for p in be.palettes] == [0, 0, 0]
+    import pgs_ref_frontend
+    if pgs_ref_frontend.available():
+        s = g.GifStream()
+        build(s)
+        ref = pgs_ref_frontend.RefFrontend()
+        ref.gif_transfer(0, s.tobytes())
+        ref.flush()
+        loads = [e for e in ref.events() if e["type"] == "palette"]
+        assert [(e["tex0"] >> 37) & 0x3fff for e in loads] == cbps
+        assert [e["instance"] for e in loads] == [1, 1, 1]
+        ref.close()
 
 
 def test_partial_image_transfer_and_texture_read_flush():

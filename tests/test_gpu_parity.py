@@ -330,3 +330,23 @@ def test_combined_stream_with_fusion_and_hacks(seed):
                     parts[0].ordered, 0, meta)
     ref, out = run_both(f)
     assert_same(ref, out)
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_hazard_stream_parity(seed):
+    """Hazard-heavy streams: uploads into textures the open pass samples (VRAM
+    snapshots the textures decode from), copies out of framebuffers, CLUT
+    reloads and memoised palettes, TEXFLUSH, render to texture and feedback,
+    at 1x and 4x.  The same streams match the reference frontend record for
+    record (test_frontend_reference.py)."""
+    ref, out = run_both(gsgen.frame_hazards(seed))
+    assert_same(ref, out)
+
+
+def test_snapshot_textures_read_the_data_before_the_upload():
+    """A texture sampled before an upload overwrites it, in the same pass,
+    reads the old texels from a VRAM snapshot; CUDA and the oracle agree
+    (test_snapshot.py checks the oracle against an explicit flush)."""
+    import snapshot_streams
+    ref, out = run_both(snapshot_streams.sample_then_upload())
+    assert_same(ref, out)
