@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--no-verify", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the CPU baseline and the e2e leg (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the single-thread oracle timing")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the bounded C1 / C4 / C3 / C5 sub-records of the default line")
     return ap.parse_args()
 
 
@@ -645,6 +647,347 @@ def cpu_baseline_sample_expr(expr: str, sample: str) -> dict:
         return {"value": None, "unit": "frames/s", "cores": 1, "kind": "port", "sample": "failed: %s" % e}
 
 
+def measure_frame(frame, local, steps, warmup, e2e_steps, verify=True, pg=None) -> dict:
+    """One frame recorded through the public API and replayed as a CUDA graph:
+    device-timed frames/s with L2 flushed between steps, the shading kernels'
+    CUDA-event time, covered samples, and the end-to-end frames/s through the
+    API from host buffers (GIF decode on the host, H2D of records and
+    payloads, render, D2H of the 4 MiB GS VRAM into pinned memory, readback of
+    frame k waited after frame k+1 is decoded)."""
+    import numpy as np
+    import torch
+    import pgs
+
+    backend = pgs.CudaBackend(device=local, max_samples_log2=4)
+    try:
+        backend.set_shade_timing(True)
+        stream = torch.cuda.ExternalStream(backend.stream(), device=local)
+        gs = pgs.GSInterface(backend, super_sampling=frame.super_sampling, ordered=frame.ordered)
+        backend.begin_record()
+        gs.gif_transfer(0, frame.data)
+        gs.flush()
+        backend.end_record()
+        verified = None
+        if verify:
+            # One replay from the recorded start state must reproduce the recorded frame.
+            first = backend.read_plane(0)
+            backend.replay(1, reset_vram=True, use_graph=False)
+            verified = bool(np.array_equal(first, backend.read_plane(0)))
+        flush_buf = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda:%d" % local)
+        for _ in range(warmup):
+            backend.replay(1, reset_vram=True, use_graph=True)
+        torch.cuda.synchronize()
+        launches = backend.launches_per_replay()
+        clocks = ClockSampler(local)
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+        clocks.start()
+        time.sleep(0.3)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        shade_ms = []
+        frags0 = backend.fragments()
+        with torch.cuda.stream(stream):
+            for i in range(steps):
+                flush_buf.fill_(i & 0xFF)
+                ev[i][0].record(stream)
+                backend.replay(1, reset_vram=True, use_graph=True)
+                ev[i][1].record(stream)
+                shade_ms.append(backend.last_shade_ms())
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        frags_per_frame = (backend.fragments() - frags0) // steps
+        total_ms = sum(a.elapsed_time(b) for a, b in ev)
+        if pg:
+            total_ms = max_over_ranks(total_ms, pg, "cuda:%d" % local)
+        del flush_buf
+
+        vram = [torch.empty(pgs.VRAM_SIZE, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(2)]
+        gs2 = pgs.GSInterface(backend, super_sampling=frame.super_sampling, ordered=frame.ordered)
+        gs2.gif_transfer(0, frame.data)
+        gs2.read_vram(out=vram[0])
+        torch.cuda.synchronize()
+        st0 = backend.stats()
+        t0 = time.perf_counter()
+        tickets = []
+        for k in range(e2e_steps):
+            gs2.gif_transfer(0, frame.data)
+            tickets.append(gs2.read_vram_async(vram[k % 2]))
+            if k >= 1:
+                gs2.wait(tickets[k - 1])
+        if tickets:
+            gs2.wait(tickets[-1])
+        e2e_dt = time.perf_counter() - t0
+        st1 = backend.stats()
+        gs2.close()
+        gs.close()
+    finally:
+        backend.close()
+    return {"total_ms": total_ms, "steps": steps, "fps_per_rank": steps / (total_ms / 1000.0),
+            "shade_ms": statistics.mean(shade_ms), "frags_per_frame": frags_per_frame, "launches": launches,
+            "verified": verified, "clocks": clk,
+            "e2e_fps_per_rank": e2e_steps / e2e_dt if e2e_steps else None,
+            "h2d": (st1["h2d_bytes"] - st0["h2d_bytes"]) // max(e2e_steps, 1),
+            "d2h": (st1["d2h_bytes"] - st0["d2h_bytes"]) // max(e2e_steps, 1)}
+
+
+def extra_workloads(local) -> dict:
+    """The other configurations at bounded step counts, for the default line:
+    C1 and C4 (8x, 16x) device and end-to-end frames/s, C3 batched against
+    plain per-frame replay, C5 quality and speed."""
+    import gsgen
+    out = {}
+    for name, expr, steps in (("c1", "gsgen.frame_c1()", 10),
+                              ("c4x8", "gsgen.frame_c4(super_sampling=8)", 5),
+                              ("c4x16", "gsgen.frame_c4(super_sampling=16)", 5)):
+        try:
+            frame = eval(expr, {"gsgen": gsgen})
+            m = measure_frame(frame, local, steps=steps, warmup=3, e2e_steps=steps)
+            out[name] = {"workload": WORKLOADS[name][0], "value": m["fps_per_rank"], "unit": "frames/s",
+                         "steps": steps, "gfrag_per_s": m["frags_per_frame"] * m["fps_per_rank"] / 1e9,
+                         "shade_ms_per_frame": m["shade_ms"], "replay_verified": m["verified"],
+                         "gpu_launches_per_frame": m["launches"], "clocks": m["clocks"],
+                         "e2e": {"value": m["e2e_fps_per_rank"], "unit": "frames/s",
+                                 "h2d_bytes_per_step": m["h2d"], "d2h_bytes_per_step": m["d2h"]}}
+        except Exception as e:  # noqa: BLE001
+            out[name] = {"error": repr(e)}
+    try:
+        out["c3"] = run_c3_bounded(local)
+    except Exception as e:  # noqa: BLE001
+        out["c3"] = {"error": repr(e)}
+    try:
+        out["c5"] = run_c5_bounded(local)
+    except Exception as e:  # noqa: BLE001
+        out["c5"] = {"error": repr(e)}
+    return out
+
+
+def run_c3_bounded(local, steps=3) -> dict:
+    """64 C3 streams: plain per-frame graphs one after another against one
+    batched replay (the tuning the autotuner picks on this mix: every stream
+    its own graph branch), device-timed, L2 flushed between steps."""
+    import numpy as np
+    import torch
+    import gsgen
+    import pgs
+    ss_log2 = {1: 0, 2: 1, 4: 2}
+    frames = [gsgen.stream_c3(i) for i in range(64)]
+    backends, recorded = [], []
+    try:
+        for f in frames:
+            be = pgs.CudaBackend(local, max_samples_log2=ss_log2[f.super_sampling], arena_mib=16)
+            gs = pgs.GSInterface(be, super_sampling=f.super_sampling, ordered=f.ordered)
+            be.begin_record()
+            gs.gif_transfer(0, f.data)
+            gs.flush()
+            be.end_record()
+            gs.close()
+            recorded.append(be.read_plane(0))
+            backends.append(be)
+        for be in backends:
+            be.replay(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            for be in backends:
+                be.replay(1)
+                torch.cuda.synchronize()
+        plain_fps = len(frames) * steps / (time.perf_counter() - t0)
+        batch = pgs.Batch(local)
+        for be in backends:
+            batch.add(be)
+        batch.set_tuning(512, 2, True, 1)
+        batch.replay(1)
+        batch.synchronize()
+        verified = all(np.array_equal(be.read_plane(0), r) for be, r in zip(backends, recorded))
+        bstream = torch.cuda.ExternalStream(batch.stream(), device=local)
+        flush_buf = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda:%d" % local)
+        for _ in range(2):
+            batch.replay(1)
+        batch.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(bstream):
+            for i in range(steps):
+                flush_buf.fill_(i & 0xFF)
+                ev[i][0].record(bstream)
+                batch.replay(1)
+                ev[i][1].record(bstream)
+        batch.synchronize()
+        torch.cuda.synchronize()
+        total_ms = sum(a.elapsed_time(b) for a, b in ev)
+        launches = batch.launches_per_replay()
+        batch.close()
+    finally:
+        for be in backends:
+            be.close()
+    fps = len(frames) * steps / (total_ms / 1000.0)
+    return {"workload": WORKLOADS["c3"][0], "value": fps, "unit": "frames/s", "steps": steps,
+            "plain_per_frame_fps": plain_fps, "batched_vs_plain": fps / plain_fps,
+            "replay_verified": verified, "gpu_launches_per_replay": launches,
+            "tuning": "graph branch per stream (512 threads x 2 CTAs/SM)"}
+
+
+def run_c5_bounded(local, n_eval=24, steps=10) -> dict:
+    """The learned upscaler on held-out seeds: PSNR against 16x SSAA, output
+    px/s of 1x render + read-out + network against exact 16x SSAA (device
+    time), the network's TFLOP/s, end to end through the API from host
+    buffers (GIF decode, render, read-out, network, D2H of the output image),
+    and the CPU restatement of the network on one core."""
+    import numpy as np
+    import torch
+    import pgs
+    import upscaler_train as T
+    dev = "cuda:%d" % local
+    up = pgs.Upscaler(local)
+    params = np.load(T.WEIGHTS)
+    up.set_params(params)
+    r = T.PairRenderer(local)
+    ev_in, ev_tgt = T.build_dataset(r, range(T.EVAL_SEED0, T.EVAL_SEED0 + n_eval))
+    quality = T.evaluate(up, ev_in, ev_tgt)
+    r.close()
+    del ev_in, ev_tgt
+    frame = T.scene(T.EVAL_SEED0)
+    W, H = T.WIDTH, T.HEIGHT
+    paths = {}
+    for ss in (1, 16):
+        be = pgs.CudaBackend(local, max_samples_log2=0 if ss == 1 else 4, arena_mib=32)
+        gs = pgs.GSInterface(be, super_sampling=ss, ordered=True)
+        gs.write_vram(np.zeros(pgs.VRAM_SIZE, dtype=np.uint8))
+        be.begin_record()
+        gs.gif_transfer(0, frame.data)
+        gs.flush()
+        be.end_record()
+        paths[ss] = (be, gs)
+    img = torch.empty((1, H, W, 4), dtype=torch.uint8, device=dev)
+    out = torch.empty_like(img)
+    b1, b16 = paths[1][0], paths[16][0]
+    s1 = torch.cuda.ExternalStream(b1.stream(), device=local)
+    s16 = torch.cuda.ExternalStream(b16.stream(), device=local)
+    su = torch.cuda.ExternalStream(up.stream(), device=local)
+    flush_buf = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def learned_once():
+        b1.replay(1, reset_vram=True, use_graph=True)
+        b1.sample_circuit(img.data_ptr(), 0, W // 64, 0, W, H)
+        e = torch.cuda.Event()
+        e.record(s1)
+        su.wait_event(e)
+        up.forward(img, out)
+
+    def exact_once():
+        b16.replay(1, reset_vram=True, use_graph=True)
+        b16.sample_circuit(img.data_ptr(), 0, W // 64, 0, W, H)
+
+    def timed(fn, start_stream, end_stream):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        total = 0.0
+        for i in range(steps):
+            with torch.cuda.stream(start_stream):
+                flush_buf.fill_(i & 0xFF)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(start_stream)
+            fn()
+            b.record(end_stream)
+            torch.cuda.synchronize()
+            total += a.elapsed_time(b)
+        return total / steps
+
+    learned_ms = timed(learned_once, s1, su)
+    exact_ms = timed(exact_once, s16, s16)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    img_c = img.clone()
+    for _ in range(3):
+        up.forward(img_c, out)
+    torch.cuda.synchronize()
+    a.record(su)
+    for _ in range(steps):
+        up.forward(img_c, out)
+    b.record(su)
+    torch.cuda.synchronize()
+    net_ms = a.elapsed_time(b) / steps
+    for be, gs in paths.values():
+        gs.close()
+        be.close()
+    # End to end from host buffers.
+    be = pgs.CudaBackend(local, max_samples_log2=0, arena_mib=32)
+    gs = pgs.GSInterface(be, super_sampling=1)
+    host = torch.empty((1, H, W, 4), dtype=torch.uint8, pin_memory=True)
+    zeros = np.zeros(pgs.VRAM_SIZE, dtype=np.uint8)
+    st0 = be.stats()
+    e2e_steps = steps
+    t0 = time.perf_counter()
+    for k in range(e2e_steps + 1):
+        if k == 1:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st0 = be.stats()
+        gs.write_vram(zeros)
+        gs.gif_transfer(0, frame.data)
+        gs.flush()
+        be.sample_circuit(img.data_ptr(), frame.meta["fbp"], W // 64, 0, W, H)
+        e = torch.cuda.Event()
+        e.record(torch.cuda.ExternalStream(be.stream(), device=local))
+        su.wait_event(e)
+        up.forward(img, out)
+        # The read-out runs on torch's own stream (after the network): the
+        # pinned buffer's use is then recorded on a stream that outlives it.
+        e = torch.cuda.Event()
+        e.record(su)
+        torch.cuda.current_stream().wait_event(e)
+        host.copy_(out, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_dt = time.perf_counter() - t0
+    st1 = be.stats()
+    del host, img, out, img_c, flush_buf
+    gs.close()
+    be.close()
+    up.close()
+    px = W * H
+    flops = 2 * 9 * px * (4 * 32 + 4 * 32 * 32 + 32 * 4)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    peak = peaks.get("bf16_tflops", 1900.0)
+    return {"workload": WORKLOADS["c5"][0], "value": px / (learned_ms / 1000.0), "unit": "output px/s",
+            "steps": steps, "eval_seeds": n_eval,
+            "psnr_db": quality["psnr_net_db"], "psnr_input_db": quality["psnr_input_db"],
+            "max_abs_err": quality["max_abs_err_net"],
+            "ssaa16_px_per_s": px / (exact_ms / 1000.0), "speedup_vs_ssaa16": exact_ms / learned_ms,
+            "network_ms_per_frame": net_ms, "network_tflops": flops / (net_ms / 1000.0) / 1e12,
+            "network_frac_of_bf16_peak": flops / (net_ms / 1000.0) / 1e12 / peak,
+            "e2e": {"value": px * e2e_steps / e2e_dt, "unit": "output px/s",
+                    "h2d_bytes_per_step": (st1["h2d_bytes"] - st0["h2d_bytes"]) // e2e_steps,
+                    "d2h_bytes_per_step": px * 4},
+            "cpu_baseline": upscaler_cpu_baseline(params)}
+
+
+def upscaler_cpu_baseline(params) -> dict:
+    """The network's CPU restatement (oracle/upscaler_ref.py, numpy, one
+    thread) on a 160x112 crop of a frame, as output px/s."""
+    env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    with tempfile.NamedTemporaryFile(suffix=".npy", delete=False) as f:
+        np_path = f.name
+    import numpy as np
+    np.save(np_path, params)
+    code = ("import sys,time; sys.path.insert(0,%r); import numpy as np, upscaler_ref as R;"
+            "p=np.load(%r); x=np.random.default_rng(0).integers(0,256,(1,112,160,4),dtype=np.uint8);"
+            "t=time.perf_counter(); R.forward(x,p); print(160*112/(time.perf_counter()-t))") % (str(ROOT / "oracle"),
+                                                                                              np_path)
+    try:
+        res = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+        val = float(res.stdout.strip().splitlines()[-1])
+        return {"value": val, "unit": "output px/s", "cores": 1, "kind": "port",
+                "sample": "one 160x112 crop through the 6-layer network (numpy restatement)"}
+    except Exception as e:  # noqa: BLE001
+        return {"value": None, "unit": "output px/s", "cores": 1, "kind": "port", "sample": "failed: %s" % e}
+    finally:
+        os.unlink(np_path)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -675,82 +1018,19 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         pg = dist
 
-    backend = pgs.CudaBackend(device=local, max_samples_log2=4)
-    backend.set_shade_timing(True)
-    stream = torch.cuda.ExternalStream(backend.stream(), device=local)
-
-    # Record the frame program.
-    gs = pgs.GSInterface(backend, super_sampling=frame.super_sampling, ordered=frame.ordered)
-    backend.begin_record()
-    gs.gif_transfer(0, frame.data)
-    gs.flush()
-    backend.end_record()
-    verified = None
-    if not args.no_verify and rank == 0:
-        # One replay from the recorded start state must reproduce the recorded frame.
-        first = backend.read_plane(0)
-        backend.replay(1, reset_vram=True, use_graph=False)
-        verified = bool(np.array_equal(first, backend.read_plane(0)))
-
-    flush_buf = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda:%d" % local)
-    # Warm-up (also instantiates the CUDA graph).
-    for _ in range(args.warmup):
-        backend.replay(1, reset_vram=True, use_graph=True)
-    torch.cuda.synchronize()
-    launches = backend.launches_per_replay()
-
-    clocks = ClockSampler(local)
-    if pg:
-        pg.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    time.sleep(0.3)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    shade_ms = []
-    frags0 = backend.fragments()
-    with torch.cuda.stream(stream):
-        for i in range(args.steps):
-            flush_buf.fill_(i & 0xFF)
-            ev[i][0].record(stream)
-            backend.replay(1, reset_vram=True, use_graph=True)
-            ev[i][1].record(stream)
-            shade_ms.append(backend.last_shade_ms())
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    frags_per_frame = (backend.fragments() - frags0) // args.steps
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
-    if pg:
-        total_ms = max_over_ranks(total_ms, pg, "cuda:%d" % local)
-    fps = replica_throughput(args.steps, world, total_ms)
-
-    # End to end through the public API from host memory: every step decodes
-    # the frame's GIF stream on the host, uploads its records and payloads,
-    # renders, and reads the 4 MiB GS VRAM back into pinned host memory.  The
-    # readback of frame k is waited for after frame k+1 has been decoded, so
-    # host decoding overlaps the GPU as in an emulator's frame loop.
     e2e_steps = 0 if args.quick else max(5, min(args.steps, 20))
-    vram = [torch.empty(pgs.VRAM_SIZE, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(2)]
-    gs2 = pgs.GSInterface(backend, super_sampling=frame.super_sampling, ordered=frame.ordered)
-    gs2.gif_transfer(0, frame.data)
-    gs2.read_vram(out=vram[0])
-    torch.cuda.synchronize()
-    st0 = backend.stats()
-    t0 = time.perf_counter()
-    tickets = []
-    for k in range(e2e_steps):
-        gs2.gif_transfer(0, frame.data)
-        tickets.append(gs2.read_vram_async(vram[k % 2]))
-        if k >= 1:
-            gs2.wait(tickets[k - 1])
-    if tickets:
-        gs2.wait(tickets[-1])
-    e2e_dt = time.perf_counter() - t0
-    st1 = backend.stats()
-    h2d = (st1["h2d_bytes"] - st0["h2d_bytes"]) // max(e2e_steps, 1)
-    d2h = (st1["d2h_bytes"] - st0["d2h_bytes"]) // max(e2e_steps, 1)
-    e2e_fps = world * e2e_steps / e2e_dt if e2e_steps else None
-    gs2.close()
+    m = measure_frame(frame, local, args.steps, args.warmup, e2e_steps, verify=not args.no_verify and rank == 0,
+                      pg=pg)
+    total_ms = m["total_ms"]
+    fps = replica_throughput(args.steps, world, total_ms)
+    e2e_fps = world * m["e2e_fps_per_rank"] if m["e2e_fps_per_rank"] else None
+    h2d, d2h = m["h2d"], m["d2h"]
+    frags_per_frame = m["frags_per_frame"]
+    shade_ms = [m["shade_ms"]]
+    verified = m["verified"]
+    launches = m["launches"]
+    clk = m["clocks"]
+    extras = None if (args.quick or args.no_extra or rank != 0) else extra_workloads(local)
 
     if rank != 0:
         if pg:
@@ -791,6 +1071,7 @@ def main():
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
+        "workloads": extras,
     }
     print(json.dumps(out))
     if pg:
