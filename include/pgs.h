@@ -563,7 +563,20 @@ typedef struct pgs_gs_options
 	/* GSOptions::super_sampled_textures (pgs_gs_set_super_sampled_textures);
 	 * off when the resulting rate is 1x. */
 	uint32_t super_sampled_textures;
+	/* PGS_THREADED_DECODE_*: whether a GIF transfer is decoded on a worker
+	 * thread of the interface while the calling thread runs the state side
+	 * (hazard tracking, render passes, backend calls and host callbacks stay
+	 * on the calling thread, in stream order).  The results are the same
+	 * either way.  Not part of the reference's GSOptions. */
+	uint32_t threaded_decode;
 } pgs_gs_options;
+
+/* Transfers of 256 KiB and more are decoded on the worker thread. */
+#define PGS_THREADED_DECODE_AUTO 0u
+/* Every transfer is decoded on the calling thread. */
+#define PGS_THREADED_DECODE_OFF 1u
+/* Every transfer is decoded on the worker thread. */
+#define PGS_THREADED_DECODE_ALWAYS 2u
 
 /* GSInterface::init.  The frontend does not own the backend. */
 pgs_gs *pgs_gs_create(const pgs_backend_ops *ops, void *backend, const pgs_gs_options *options,

@@ -64,7 +64,8 @@ def build_product(verbose: bool = False) -> Path:
     jobs = [
         [nvcc, "-gencode", GENCODE, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-ffp-contract=off",
          "-Xcompiler", "-fPIC", *common, "-c", str(cu), "-o", str(o_cu)],
-        ["g++", "-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", *common, "-c", str(cpp), "-o", str(o_cpp)],
+        ["g++", "-std=c++17", "-O3", "-fPIC", "-pthread", "-ffp-contract=off", *common, "-c", str(cpp), "-o",
+         str(o_cpp)],
         [nvcc, "-gencode", GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *common, "-c", str(cu_up),
          "-o", str(o_up)],
     ]
@@ -75,7 +76,8 @@ def build_product(verbose: bool = False) -> Path:
         jobs[0].insert(1, "-D" + d)
     with ThreadPoolExecutor(max_workers=3) as ex:
         list(ex.map(_run, jobs))
-    _run([nvcc, "-shared", "-gencode", GENCODE, "-cudart", "static", str(o_cu), str(o_up), str(o_cpp), "-o", str(out)])
+    _run([nvcc, "-shared", "-gencode", GENCODE, "-cudart", "static", str(o_cu), str(o_up), str(o_cpp), "-lpthread",
+          "-o", str(out)])
     stamp.write_text(defines)
     return out
 

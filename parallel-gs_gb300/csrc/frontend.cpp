@@ -21,11 +21,17 @@
 #include "gs_tracker.h"
 
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <new>
+#include <thread>
+#include <unistd.h>
 #include <unordered_map>
 #include <vector>
 
@@ -132,6 +138,26 @@ struct Tex1Reg
 	bool mmin_has_mipmap() const { return mmin > 1 && mmin <= 5; }
 };
 
+// Two 64-bit lanes (GCC/Clang vector extension, lowered to SSE on x86-64 and
+// NEON on AArch64).
+typedef uint64_t Word2 __attribute__((vector_size(16), aligned(4), may_alias));
+
+// Vertex copy in the widths the vertex queue writes: the 16-byte position,
+// then the attributes as 16 + 8 bytes.
+static inline void copy_vertex(pgs_vertex_position &dp, pgs_vertex_attribute &da, const pgs_vertex_position &sp,
+                               const pgs_vertex_attribute &sa)
+{
+	static_assert(sizeof(pgs_vertex_position) == 16 && sizeof(pgs_vertex_attribute) == 24, "vertex layout");
+	Word2 p, lo;
+	uint64_t hi;
+	memcpy(&p, &sp, 16);
+	memcpy(&lo, &sa, 16);
+	memcpy(&hi, reinterpret_cast<const char *>(&sa) + 16, 8);
+	memcpy(&dp, &p, 16);
+	memcpy(&da, &lo, 16);
+	memcpy(reinterpret_cast<char *>(&da) + 16, &hi, 8);
+}
+
 static bool frame_compat(uint64_t a, uint64_t b)
 {
 	// FBP, FBW, PSM must match; FBMSK may differ (FRAMEBits::compat).
@@ -206,7 +232,6 @@ struct pgs_gs : TrackerClient
 	// GS dump being replayed / recorded.
 	FILE *dump_in = nullptr, *dump_out = nullptr;
 	std::vector<uint64_t> dump_buf;
-	float internal_q = 1.0f;
 	uint32_t cached_cbp[2] = {};
 
 	struct Path
@@ -214,14 +239,32 @@ struct pgs_gs : TrackerClient
 		uint64_t tag_lo = 0, tag_hi = 0;
 		uint32_t nloop = 0, flg = 0, nreg = 0;
 		uint32_t reg = 0, loop = 0;
-	} paths[4];
+	};
 
-	struct
+	// Vertex assembly state: GIF paths, the vertex registers (RGBAQ, ST, UV,
+	// FOG, the internal Q), the vertex queue and its own copies of the
+	// registers vertex assembly reads (PRIM as drawn, PRMODECONT, XYOFFSET).
+	// Only the decoder touches it while a transfer runs, so the decoder can
+	// run on a thread of its own ahead of the register-file state; regs[]
+	// gets the vertex registers back when the transfer ends.  On a cache line
+	// of its own: the state thread never shares one with it.
+	struct alignas(64) Decoder
 	{
-		pgs_vertex_position pos[3];
-		pgs_vertex_attribute attr[3];
-		uint32_t count = 0;
-	} vq;
+		Path paths[4];
+		uint64_t rgbaq = 0, st = 0, uv = 0, fog = 0;
+		float internal_q = 1.0f;
+		uint64_t prim = 0, prmodecont = 0, xyoffset[2] = {};
+		int32_t ofx = 0, ofy = 0;
+		// Vertex queue.  A vertex is written as one 16-byte position word and
+		// a 16 + 8 byte attribute pair and read back with the same widths, so
+		// the reads forward from the stores still in flight.
+		struct
+		{
+			pgs_vertex_position pos[3];
+			pgs_vertex_attribute attr[3];
+			uint32_t count = 0;
+		} vq;
+	} dec;
 
 	// Render pass under construction.
 	pgs_vertex_position *positions = nullptr;
@@ -275,7 +318,6 @@ struct pgs_gs : TrackerClient
 	};
 	MemoizedPalette memo[16];
 	uint32_t num_memo = 0;
-	int32_t ofx = 0, ofy = 0;
 
 	// Cached primitive template; recomputed when template_dirty is set.
 	bool template_dirty = true;
@@ -311,8 +353,63 @@ struct pgs_gs : TrackerClient
 		reg_serial++;
 		template_dirty = true;
 		dirty = DIRTY_ALL;
-		vq.count = 0;
+		decoder_load();
+	}
+
+	// The decoder's copies from the register file, after the file was set
+	// from outside a transfer (reset, dump restore, clobber).
+	void decoder_load()
+	{
+		dec.rgbaq = regs[R_RGBAQ];
+		dec.st = regs[R_ST];
+		dec.uv = regs[R_UV];
+		dec.fog = regs[R_FOG];
+		dec.prim = regs[R_PRIM];
+		dec.prmodecont = regs[R_PRMODECONT];
+		dec.xyoffset[0] = regs[R_XYOFFSET_1];
+		dec.xyoffset[1] = regs[R_XYOFFSET_2];
+		dec.vq.count = 0;
 		update_offsets();
+	}
+
+	// Register file reads and side-effect free writes from the host: the
+	// vertex registers live in the decoder while a transfer runs (a host
+	// callback may ask), and the decoder's copies follow direct writes.
+	uint64_t read_reg(uint32_t addr) const
+	{
+		switch (addr)
+		{
+		case R_RGBAQ: return dec.rgbaq;
+		case R_ST: return dec.st;
+		case R_UV: return dec.uv;
+		case R_FOG: return dec.fog;
+		default: return regs[addr];
+		}
+	}
+
+	void set_reg(uint32_t addr, uint64_t v)
+	{
+		regs[addr] = v;
+		switch (addr)
+		{
+		case R_RGBAQ: dec.rgbaq = v; break;
+		case R_ST: dec.st = v; break;
+		case R_UV: dec.uv = v; break;
+		case R_FOG: dec.fog = v; break;
+		case R_PRIM: dec.prim = v; break;
+		case R_PRMODECONT: dec.prmodecont = v; break;
+		case R_XYOFFSET_1: case R_XYOFFSET_2: dec.xyoffset[addr - R_XYOFFSET_1] = v; break;
+		default: break;
+		}
+	}
+
+	// The vertex registers back into the register file (read_register, dumps).
+	void decoder_store()
+	{
+		regs[R_RGBAQ] = dec.rgbaq;
+		regs[R_ST] = dec.st;
+		regs[R_UV] = dec.uv;
+		regs[R_FOG] = dec.fog;
 	}
 
 	void record_transfer(uint32_t path, const void *data, size_t size)
@@ -1155,10 +1252,12 @@ struct pgs_gs : TrackerClient
 		set_state_reg(R_PRIM, v, DIRTY_FEEDBACK | DIRTY_PRIM_TEMPLATE | DIRTY_TEX | DIRTY_STATE);
 		if (!field(regs[R_PRIM], 4, 1))
 			dirty &= ~DIRTY_TEX;
-		update_offsets();
 	}
 
-	void write_register(uint32_t addr, uint64_t v)
+	// A register write on the register-file side: every register except the
+	// vertex registers and vertex kicks, which vertex assembly handles
+	// (assemble_register) before passing the rest on in stream order.
+	void write_state_register(uint32_t addr, uint64_t v)
 	{
 		addr &= 0x7f;
 		switch (addr)
@@ -1185,7 +1284,6 @@ struct pgs_gs : TrackerClient
 				regs[R_PRIM] = (regs[R_PRIM] & ~7ull) | (v & 7ull);
 			}
 			template_dirty = true;
-			vq.count = 0;
 			break;
 		}
 		case R_PRMODE:
@@ -1195,14 +1293,6 @@ struct pgs_gs : TrackerClient
 				template_dirty = true;
 			}
 			break;
-		case R_RGBAQ: case R_RGBAQ_UNDOC: regs[R_RGBAQ] = v; break;
-		case R_ST: regs[R_ST] = v; break;
-		case R_UV: regs[R_UV] = v; break;
-		case R_FOG: regs[R_FOG] = v; break;
-		case R_XYZF2: vertex_kick_xyzf(v); drawing_kick(false); break;
-		case R_XYZ2: vertex_kick_xyz(v); drawing_kick(false); break;
-		case R_XYZF3: vertex_kick_xyzf(v); drawing_kick(true); break;
-		case R_XYZ3: vertex_kick_xyz(v); drawing_kick(true); break;
 		case R_TEX0_1: case R_TEX0_2:
 			// a_d_TEX0 + handle_tex0_write (gs/gs_interface.cpp:802-805).
 			set_state_reg(addr, v, DIRTY_FEEDBACK | DIRTY_STATE | DIRTY_PRIM_TEMPLATE | DIRTY_TEX);
@@ -1218,7 +1308,7 @@ struct pgs_gs : TrackerClient
 			uint64_t preserve_mask = 0x3fffull | (0x3full << 14) | (0xfull << 26) | (0xfull << 30) |
 			                         (1ull << 34) | (3ull << 35);
 			uint64_t t = (regs[R_TEX0_1 + ctx] & preserve_mask) | (v & ~preserve_mask);
-			write_register(R_TEX0_1 + ctx, t);
+			write_state_register(R_TEX0_1 + ctx, t);
 			break;
 		}
 		case R_CLAMP_1: case R_CLAMP_2: case R_TEX1_1: case R_TEX1_2:
@@ -1260,7 +1350,6 @@ struct pgs_gs : TrackerClient
 			break;
 		case R_XYOFFSET_1: case R_XYOFFSET_2:
 			regs[addr] = v;
-			update_offsets();
 			break;
 		case R_TEXFLUSH:
 			// Counted only when a held texture is next used (a_d_TEXFLUSH,
@@ -1295,61 +1384,46 @@ struct pgs_gs : TrackerClient
 
 	void update_offsets()
 	{
-		uint64_t xy = regs[R_XYOFFSET_1 + field(regs[R_PRIM], 9, 1)];
-		ofx = int32_t(field(xy, 0, 16));
-		ofy = int32_t(field(xy, 32, 16));
+		uint64_t xy = dec.xyoffset[field(dec.prim, 9, 1)];
+		dec.ofx = int32_t(field(xy, 0, 16));
+		dec.ofy = int32_t(field(xy, 32, 16));
 	}
 
 	// ---------------------------------------------------------------
 	// Vertex queue (gs/gs_interface.cpp:843-897).
 	void shift_queue()
 	{
+		auto &vq = dec.vq;
 		if (vq.count == 3)
 		{
-			vq.pos[0] = vq.pos[1];
-			vq.attr[0] = vq.attr[1];
-			vq.pos[1] = vq.pos[2];
-			vq.attr[1] = vq.attr[2];
+			copy_vertex(vq.pos[0], vq.attr[0], vq.pos[1], vq.attr[1]);
+			copy_vertex(vq.pos[1], vq.attr[1], vq.pos[2], vq.attr[2]);
 			vq.count = 2;
 		}
 	}
 
-	void fill_attr(pgs_vertex_attribute &a, float fog)
-	{
-		uint64_t st = regs[R_ST], rgbaq = regs[R_RGBAQ], uv = regs[R_UV];
-		uint32_t sbits = uint32_t(st), tbits = uint32_t(st >> 32), qbits = uint32_t(rgbaq >> 32);
-		memcpy(&a.s, &sbits, 4);
-		memcpy(&a.t, &tbits, 4);
-		memcpy(&a.q, &qbits, 4);
-		a.rgba = uint32_t(rgbaq);
-		a.fog = fog;
-		a.u = uint16_t(field(uv, 0, 14));
-		a.v = uint16_t(field(uv, 16, 14));
-	}
-
-	void vertex_kick_xyz(uint64_t v)
+	// The queue entry: position (x, y, z, 0) and attributes (s, t, q, rgba |
+	// fog, u, v) packed into words in registers and stored whole.
+	void push_vertex(uint64_t v, uint32_t z, float fog)
 	{
 		shift_queue();
-		auto &p = vq.pos[vq.count];
-		p.x = int32_t(field(v, 0, 16)) - ofx;
-		p.y = int32_t(field(v, 16, 16)) - ofy;
-		p.z = uint32_t(v >> 32);
-		p.padding = 0;
-		fill_attr(vq.attr[vq.count], float(field(regs[R_FOG], 56, 8)));
+		auto &vq = dec.vq;
+		const uint64_t st = dec.st, rgbaq = dec.rgbaq, uv = dec.uv;
+		const uint32_t x = uint32_t(int32_t(field(v, 0, 16)) - dec.ofx);
+		const uint32_t y = uint32_t(int32_t(field(v, 16, 16)) - dec.ofy);
+		uint32_t fog_bits;
+		memcpy(&fog_bits, &fog, 4);
+		const Word2 pos = { uint64_t(x) | (uint64_t(y) << 32), uint64_t(z) };
+		const Word2 lo = { st, (rgbaq >> 32) | (rgbaq << 32) };
+		const uint64_t hi = uint64_t(fog_bits) | (uint64_t(field(uv, 0, 14)) << 32) | (uint64_t(field(uv, 16, 14)) << 48);
+		memcpy(&vq.pos[vq.count], &pos, 16);
+		memcpy(&vq.attr[vq.count], &lo, 16);
+		memcpy(reinterpret_cast<char *>(&vq.attr[vq.count]) + 16, &hi, 8);
 		vq.count++;
 	}
 
-	void vertex_kick_xyzf(uint64_t v)
-	{
-		shift_queue();
-		auto &p = vq.pos[vq.count];
-		p.x = int32_t(field(v, 0, 16)) - ofx;
-		p.y = int32_t(field(v, 16, 16)) - ofy;
-		p.z = field(v, 32, 24);
-		p.padding = 0;
-		fill_attr(vq.attr[vq.count], float(field(v, 56, 8)));
-		vq.count++;
-	}
+	void vertex_kick_xyz(uint64_t v) { push_vertex(v, uint32_t(v >> 32), float(field(dec.fog, 56, 8))); }
+	void vertex_kick_xyzf(uint64_t v) { push_vertex(v, field(v, 32, 24), float(field(v, 56, 8))); }
 
 	// ---------------------------------------------------------------
 	// draw_is_degenerate (gs/gs_interface.cpp:2036-2115).
@@ -2327,9 +2401,15 @@ struct pgs_gs : TrackerClient
 
 	// ---------------------------------------------------------------
 	// Drawing kick (gs/gs_interface.cpp:2473-2943).
-	void drawing_kick(bool adc)
+	// Vertex side of the drawing kick: a kick that completes a primitive
+	// hands its vertices, newest first, to the state side (draw), which
+	// checks for degenerate state and appends; every kick ends in post_kick
+	// on the state side.
+	template <class Sink>
+	void drawing_kick(Sink &s, bool adc)
 	{
-		uint32_t type = field(regs[R_PRIM], 0, 3);
+		auto &vq = dec.vq;
+		uint32_t type = field(dec.prim, 0, 3);
 		uint32_t nv;
 		bool list = false, fan = false, quad = false;
 		switch (type)
@@ -2343,26 +2423,38 @@ struct pgs_gs : TrackerClient
 		case PRIM_SPRITE: nv = 2; list = true; quad = true; break;
 		default:
 			vq.count = 0;
-			post_kick();
+			s.kick();
 			return;
 		}
 
-		if (vq.count >= nv)
+		if (vq.count < nv)
 		{
-			if (!adc && !draw_is_degenerate())
-				append(nv, quad);
-
-			if (fan)
-			{
-				vq.pos[1] = vq.pos[2];
-				vq.attr[1] = vq.attr[2];
-				vq.count = 2;
-			}
-			else if (list)
-			{
-				vq.count = 0;
-			}
+			s.kick();
+			return;
 		}
+		if (!adc)
+		{
+			const DrawSlot d = s.begin_draw(nv, quad);
+			for (uint32_t i = 0; i < nv && i < 3; i++)
+				copy_vertex(d.pos[i], d.attr[i], vq.pos[vq.count - 1 - i], vq.attr[vq.count - 1 - i]);
+			s.end_draw();
+		}
+		else
+			s.kick();
+		if (fan)
+		{
+			copy_vertex(vq.pos[1], vq.attr[1], vq.pos[2], vq.attr[2]);
+			vq.count = 2;
+		}
+		else if (list)
+			vq.count = 0;
+	}
+
+	// State side of a drawing kick that completes a primitive.
+	void draw(uint32_t nv, bool quad, const pgs_vertex_position *vp, const pgs_vertex_attribute *va)
+	{
+		if (!draw_is_degenerate())
+			append(nv, quad, vp, va);
 		post_kick();
 	}
 
@@ -2404,7 +2496,8 @@ struct pgs_gs : TrackerClient
 		return r;
 	}
 
-	void append(uint32_t nv, bool quad)
+	// vp / va: the primitive's vertices, newest first.
+	void append(uint32_t nv, bool quad, const pgs_vertex_position *vp, const pgs_vertex_attribute *va)
 	{
 		const DrawConsts &D = draw_consts();
 		pgs_vertex_position pos[3] = {};
@@ -2412,8 +2505,7 @@ struct pgs_gs : TrackerClient
 
 		if (nv == 1)
 		{
-			pos[0] = vq.pos[vq.count - 1];
-			attr[0] = vq.attr[vq.count - 1];
+			copy_vertex(pos[0], attr[0], vp[0], va[0]);
 			pos[0].x -= (1 << (SUBPIXEL_BITS - 1)) - 1;
 			pos[0].y -= (1 << (SUBPIXEL_BITS - 1)) - 1;
 			pos[1] = pos[0];
@@ -2423,18 +2515,12 @@ struct pgs_gs : TrackerClient
 		else if (nv == 2)
 		{
 			for (uint32_t i = 0; i < 2; i++)
-			{
-				pos[i] = vq.pos[vq.count - 1 - i];
-				attr[i] = vq.attr[vq.count - 1 - i];
-			}
+				copy_vertex(pos[i], attr[i], vp[i], va[i]);
 		}
 		else
 		{
 			for (uint32_t i = 0; i < 3; i++)
-			{
-				pos[i] = vq.pos[2 - i];
-				attr[i] = vq.attr[2 - i];
-			}
+				copy_vertex(pos[i], attr[i], vp[i], va[i]);
 		}
 
 		bool is_line = !quad && nv == 2;
@@ -2642,8 +2728,8 @@ struct pgs_gs : TrackerClient
 
 		uint32_t n = primitive_count;
 		prims[n] = pa;
-		memcpy(positions + 3 * n, pos, sizeof(pos));
-		memcpy(attributes + 3 * n, attr, sizeof(attr));
+		for (uint32_t i = 0; i < 3; i++)
+			copy_vertex(positions[3 * n + i], attributes[3 * n + i], pos[i], attr[i]);
 		primitive_count++;
 		// Set after any flush above, which clears it.
 		last_para_candidate = para_candidate;
@@ -2745,37 +2831,38 @@ struct pgs_gs : TrackerClient
 
 	// ---------------------------------------------------------------
 	// GIF packet decode (gs/gs_interface.cpp:4290-4397).
-	void packed_write(uint32_t desc, const uint64_t *q)
+	template <class Sink>
+	void packed_write(Sink &s, uint32_t desc, const uint64_t *q)
 	{
 		uint64_t lo = q[0], hi = q[1];
 		switch (desc)
 		{
-		case 0x0: write_register(R_PRIM, lo & 0x7ff); break;
+		case 0x0: assemble_register(s, R_PRIM, lo & 0x7ff); break;
 		case 0x1:
 		{
 			uint32_t qbits;
-			memcpy(&qbits, &internal_q, 4);
+			memcpy(&qbits, &dec.internal_q, 4);
 			uint64_t v = field(lo, 0, 8) | (uint64_t(field(lo, 32, 8)) << 8) |
 			             (uint64_t(field(hi, 0, 8)) << 16) | (uint64_t(field(hi, 32, 8)) << 24) |
 			             (uint64_t(qbits) << 32);
-			regs[R_RGBAQ] = v;
+			dec.rgbaq = v;
 			break;
 		}
 		case 0x2:
 		{
-			regs[R_ST] = lo;
+			dec.st = lo;
 			uint32_t qbits = uint32_t(hi);
-			memcpy(&internal_q, &qbits, 4);
+			memcpy(&dec.internal_q, &qbits, 4);
 			break;
 		}
-		case 0x3: regs[R_UV] = field(lo, 0, 14) | (uint64_t(field(lo, 32, 14)) << 16); break;
+		case 0x3: dec.uv = field(lo, 0, 14) | (uint64_t(field(lo, 32, 14)) << 16); break;
 		case 0x4:
 		{
 			uint64_t v = field(lo, 0, 16) | (uint64_t(field(lo, 32, 16)) << 16) |
 			             (uint64_t(field(hi, 4, 24)) << 32) | (uint64_t(field(hi, 36, 8)) << 56);
 			bool adc = field(hi, 47, 1) != 0;
 			vertex_kick_xyzf(v);
-			drawing_kick(adc);
+			drawing_kick(s, adc);
 			break;
 		}
 		case 0x5:
@@ -2783,34 +2870,35 @@ struct pgs_gs : TrackerClient
 			uint64_t v = field(lo, 0, 16) | (uint64_t(field(lo, 32, 16)) << 16) | (uint64_t(uint32_t(hi)) << 32);
 			bool adc = field(hi, 47, 1) != 0;
 			vertex_kick_xyz(v);
-			drawing_kick(adc);
+			drawing_kick(s, adc);
 			break;
 		}
-		case 0xa: regs[R_FOG] = uint64_t(field(hi, 36, 8)) << 56; break;
+		case 0xa: dec.fog = uint64_t(field(hi, 36, 8)) << 56; break;
 		case 0xc:
 		{
 			uint64_t v = field(lo, 0, 16) | (uint64_t(field(lo, 32, 16)) << 16) |
 			             (uint64_t(field(hi, 4, 24)) << 32) | (uint64_t(field(hi, 36, 8)) << 56);
 			vertex_kick_xyzf(v);
-			drawing_kick(true);
+			drawing_kick(s, true);
 			break;
 		}
 		case 0xd:
 		{
 			uint64_t v = field(lo, 0, 16) | (uint64_t(field(lo, 32, 16)) << 16) | (uint64_t(uint32_t(hi)) << 32);
 			vertex_kick_xyz(v);
-			drawing_kick(true);
+			drawing_kick(s, true);
 			break;
 		}
-		case 0xe: write_register(uint32_t(hi & 0x7f), lo); break;
-		case 0x6: case 0x7: case 0x8: case 0x9: write_register(desc, lo); break;
+		case 0xe: assemble_register(s, uint32_t(hi & 0x7f), lo); break;
+		case 0x6: case 0x7: case 0x8: case 0x9: assemble_register(s, desc, lo); break;
 		default: break;
 		}
 	}
 
-	void gif_transfer(uint32_t pi, const uint64_t *words, size_t qwords)
+	template <class Sink>
+	void decode(Sink &s, uint32_t pi, const uint64_t *words, size_t qwords)
 	{
-		auto &path = paths[pi & 3];
+		auto &path = dec.paths[pi & 3];
 		size_t i = 0;
 		while (i < qwords)
 		{
@@ -2827,12 +2915,12 @@ struct pgs_gs : TrackerClient
 				if (path.flg == 0 && pre && path.nloop)
 				{
 					// GIFtag PRIM field: behaves like an A+D PRIM write.
-					write_register(R_PRIM, field(path.tag_lo, 47, 11));
+					assemble_register(s, R_PRIM, field(path.tag_lo, 47, 11));
 				}
 				path.loop = 0;
 				path.reg = 0;
 				if (path.nloop)
-					internal_q = 1.0f;
+					dec.internal_q = 1.0f;
 				i++;
 				continue;
 			}
@@ -2850,13 +2938,13 @@ struct pgs_gs : TrackerClient
 					const uint64_t *q = &words[2 * i];
 					for (size_t l = 0; l < loops; l++, q += 2 * nreg)
 						for (uint32_t r = 0; r < nreg; r++)
-							packed_write(desc[r], q + 2 * r);
+							packed_write(s, desc[r], q + 2 * r);
 					i += loops * nreg;
 					path.loop += uint32_t(loops);
 					continue;
 				}
 				uint32_t desc = uint32_t(path.tag_hi >> (4 * path.reg)) & 0xf;
-				packed_write(desc, &words[2 * i]);
+				packed_write(s, desc, &words[2 * i]);
 				i++;
 				if (++path.reg == path.nreg)
 				{
@@ -2870,7 +2958,7 @@ struct pgs_gs : TrackerClient
 				{
 					uint32_t desc = uint32_t(path.tag_hi >> (4 * path.reg)) & 0xf;
 					uint64_t v = words[2 * i + j];
-					reglist_write(desc, v);
+					reglist_write(s, desc, v);
 					if (++path.reg == path.nreg)
 					{
 						path.reg = 0;
@@ -2884,25 +2972,419 @@ struct pgs_gs : TrackerClient
 			else
 			{
 				size_t n = std::min<size_t>(qwords - i, path.nloop - path.loop);
-				hwreg(&words[2 * i], n * 2);
+				s.hwreg(&words[2 * i], n * 2);
 				i += n;
 				path.loop += uint32_t(n);
 			}
 		}
 	}
 
-	void reglist_write(uint32_t desc, uint64_t v)
+	template <class Sink>
+	void reglist_write(Sink &s, uint32_t desc, uint64_t v)
 	{
 		// REGLIST: descriptors address registers directly; A+D and NOP are ignored.
 		if (desc == 0xe || desc == 0xf || desc == 0xb)
 			return;
 		if (desc == 0x1)
 		{
-			regs[R_RGBAQ] = v;
+			dec.rgbaq = v;
 			return;
 		}
-		write_register(desc, v);
+		assemble_register(s, desc, v);
 	}
+
+	// A+D register write on the vertex side (the a_d_* handlers,
+	// gs/gs_interface.cpp:3506-3990): vertex registers and kicks stay here;
+	// PRIM, PRMODE, PRMODECONT and XYOFFSET update the decoder's copies and,
+	// like every other register, go on to the state side in stream order.
+	template <class Sink>
+	void assemble_register(Sink &s, uint32_t addr, uint64_t v)
+	{
+		addr &= 0x7f;
+		switch (addr)
+		{
+		case R_RGBAQ: case R_RGBAQ_UNDOC: dec.rgbaq = v; return;
+		case R_ST: dec.st = v; return;
+		case R_UV: dec.uv = v; return;
+		case R_FOG: dec.fog = v; return;
+		case R_XYZF2: vertex_kick_xyzf(v); drawing_kick(s, false); return;
+		case R_XYZ2: vertex_kick_xyz(v); drawing_kick(s, false); return;
+		case R_XYZF3: vertex_kick_xyzf(v); drawing_kick(s, true); return;
+		case R_XYZ3: vertex_kick_xyz(v); drawing_kick(s, true); return;
+		case R_PRIM:
+			// With PRMODECONT.AC = 0 only the primitive type comes from PRIM.
+			dec.prim = field(dec.prmodecont, 0, 1) ? v : (dec.prim & ~7ull) | (v & 7ull);
+			dec.vq.count = 0;
+			update_offsets();
+			break;
+		case R_PRMODE:
+			if (!field(dec.prmodecont, 0, 1))
+			{
+				dec.prim = (v & ~7ull) | (dec.prim & 7ull);
+				update_offsets();
+			}
+			break;
+		case R_PRMODECONT: dec.prmodecont = v; break;
+		case R_XYOFFSET_1: case R_XYOFFSET_2:
+			dec.xyoffset[addr - R_XYOFFSET_1] = v;
+			update_offsets();
+			break;
+		default: break;
+		}
+		s.reg(addr, v);
+		// A host callback sees the stream stopped at its register, as the
+		// callback may call back in.
+		if ((addr == R_SIGNAL && signal_iface.on_signal) || (addr == R_FINISH && signal_iface.on_finish) ||
+		    (addr == R_LABEL && signal_iface.on_label))
+			s.barrier();
+	}
+
+	// ---------------------------------------------------------------
+	// Where the decoder's output goes.  A primitive's vertices are written
+	// by the decoder into the slot begin_draw returns.
+	struct DrawSlot
+	{
+		pgs_vertex_position *pos;
+		pgs_vertex_attribute *attr;
+	};
+
+	// Straight into the state side, on the calling thread.
+	struct DirectSink
+	{
+		explicit DirectSink(pgs_gs *g) : gs(g) {}
+		pgs_gs *gs;
+		uint32_t nv = 0;
+		bool quad = false;
+		pgs_vertex_position pos[3];
+		pgs_vertex_attribute attr[3];
+		void reg(uint32_t addr, uint64_t v) { gs->write_state_register(addr, v); }
+		void kick() { gs->post_kick(); }
+		void hwreg(const uint64_t *data, size_t count) { gs->hwreg(data, count); }
+		DrawSlot begin_draw(uint32_t n, bool q)
+		{
+			nv = n;
+			quad = q;
+			return { pos, attr };
+		}
+		void end_draw() { gs->draw(nv, quad, pos, attr); }
+		void barrier() {}
+	};
+
+	// Threaded decode.  For large transfers a worker thread runs the decoder
+	// over the caller's buffer and hands its output to the calling thread as
+	// commands, in chunks through a ring; the calling thread runs the state
+	// side (hazards, render passes, the backend, host callbacks) exactly as
+	// the direct path does, in stream order, while the worker decodes ahead.
+	enum : uint32_t
+	{
+		CMD_REG = 1, CMD_KICK = 2, CMD_DRAW = 3, CMD_HWREG = 4, CMD_BARRIER = 5, CMD_END = 6,
+	};
+	static constexpr size_t RING_CHUNK_BYTES = 64 * 1024, RING_CHUNKS = 16;
+	static constexpr size_t THREADED_DECODE_MIN_QWORDS = 16 * 1024;
+
+	struct CmdRing
+	{
+		alignas(64) std::atomic<uint64_t> produced{ 0 };
+		alignas(64) std::atomic<uint64_t> consumed{ 0 };
+		alignas(64) uint32_t used[RING_CHUNKS] = {};
+		std::unique_ptr<uint64_t[]> storage{ new uint64_t[RING_CHUNKS * RING_CHUNK_BYTES / 8 + 8] };
+		uint8_t *chunk(uint64_t index)
+		{
+			uint8_t *base = reinterpret_cast<uint8_t *>(storage.get());
+			base += (64 - (reinterpret_cast<uintptr_t>(base) & 63)) & 63;
+			return base + (index % RING_CHUNKS) * RING_CHUNK_BYTES;
+		}
+	};
+
+	// Spin on a condition, then yield the core.
+	template <class Pred>
+	static void wait_until(Pred pred)
+	{
+		for (uint32_t spins = 0; !pred(); spins++)
+			if (spins > 4096)
+				std::this_thread::yield();
+	}
+
+	// The decoder's side of the ring.  Kicks that draw nothing are counted
+	// and handed over with the next command: the state side runs their
+	// post_kick calls first.
+	struct RingSink
+	{
+		CmdRing *r;
+		uint8_t *cur = nullptr;
+		size_t off = 0;
+		uint64_t index = 0;
+		uint32_t kicks = 0;
+
+		uint8_t *reserve(size_t bytes)
+		{
+			if (!cur || off + bytes > RING_CHUNK_BYTES)
+			{
+				publish();
+				index = r->produced.load(std::memory_order_relaxed);
+				const uint64_t idx = index;
+				CmdRing *ring = r;
+				wait_until([ring, idx] { return idx - ring->consumed.load(std::memory_order_acquire) < RING_CHUNKS; });
+				cur = r->chunk(index);
+				off = 0;
+			}
+			uint8_t *p = cur + off;
+			off += bytes;
+			return p;
+		}
+		void publish()
+		{
+			if (!cur)
+				return;
+			r->used[index % RING_CHUNKS] = uint32_t(off);
+			r->produced.store(index + 1, std::memory_order_release);
+			cur = nullptr;
+		}
+		void header(uint8_t *p, uint32_t h) { memcpy(p, &h, 4); }
+		void flush_kicks()
+		{
+			if (kicks)
+			{
+				header(reserve(8), CMD_KICK | (kicks << 24));
+				kicks = 0;
+			}
+		}
+		void reg(uint32_t addr, uint64_t v)
+		{
+			flush_kicks();
+			uint8_t *p = reserve(16);
+			header(p, CMD_REG | (addr << 8));
+			memcpy(p + 8, &v, 8);
+		}
+		void kick()
+		{
+			if (++kicks == 255)
+				flush_kicks();
+		}
+		void hwreg(const uint64_t *data, size_t count)
+		{
+			flush_kicks();
+			uint8_t *p = reserve(24);
+			header(p, CMD_HWREG);
+			memcpy(p + 8, &data, sizeof(data));
+			uint64_t n = count;
+			memcpy(p + 16, &n, 8);
+		}
+		DrawSlot begin_draw(uint32_t nv, bool quad)
+		{
+			uint8_t *p = reserve(8 + 40 * nv);
+			header(p, CMD_DRAW | (nv << 8) | (uint32_t(quad) << 16) | (kicks << 24));
+			kicks = 0;
+			return { reinterpret_cast<pgs_vertex_position *>(p + 8),
+			         reinterpret_cast<pgs_vertex_attribute *>(p + 8 + 16 * nv) };
+		}
+		void end_draw() {}
+		// Hands everything over and waits until the state side has run it.
+		void barrier()
+		{
+			flush_kicks();
+			header(reserve(8), CMD_BARRIER);
+			publish();
+			CmdRing *ring = r;
+			const uint64_t done = r->produced.load(std::memory_order_relaxed);
+			wait_until([ring, done] { return ring->consumed.load(std::memory_order_acquire) == done; });
+		}
+		void end()
+		{
+			flush_kicks();
+			header(reserve(8), CMD_END);
+			publish();
+		}
+	};
+
+	struct DecodeWorker
+	{
+		std::thread thread;
+		std::mutex mutex;
+		std::condition_variable cv;
+		uint64_t job_seq = 0;
+		std::atomic<uint64_t> done_seq{ 0 };
+		bool quit = false;
+		uint32_t path = 0;
+		const uint64_t *words = nullptr;
+		size_t qwords = 0;
+		CmdRing ring;
+		pid_t pid = 0;
+	};
+	DecodeWorker *worker = nullptr;
+	// pgs_gs_options.threaded_decode.
+	uint32_t threaded_decode = 0;
+
+	void worker_main(DecodeWorker *w)
+	{
+		uint64_t seen = 0;
+		for (;;)
+		{
+			uint32_t pi;
+			const uint64_t *words;
+			size_t qwords;
+			{
+				std::unique_lock<std::mutex> lock(w->mutex);
+				w->cv.wait(lock, [w, seen] { return w->quit || w->job_seq != seen; });
+				if (w->quit)
+					return;
+				seen = w->job_seq;
+				pi = w->path;
+				words = w->words;
+				qwords = w->qwords;
+			}
+			RingSink sink{ &w->ring };
+			decode(sink, pi, words, qwords);
+			sink.end();
+			w->done_seq.store(seen, std::memory_order_release);
+		}
+	}
+
+	void stop_worker()
+	{
+		if (!worker)
+			return;
+		if (worker->pid != getpid())
+		{
+			// A forked child: the thread is not there to join.
+			worker = nullptr;
+			return;
+		}
+		{
+			std::lock_guard<std::mutex> lock(worker->mutex);
+			worker->quit = true;
+		}
+		worker->cv.notify_one();
+		worker->thread.join();
+		delete worker;
+		worker = nullptr;
+	}
+
+	// Runs the state side over the worker's commands until the transfer's end.
+	void run_commands(CmdRing &r)
+	{
+		uint64_t idx = r.consumed.load(std::memory_order_relaxed);
+		for (;;)
+		{
+			const uint64_t want = idx;
+			wait_until([&r, want] { return r.produced.load(std::memory_order_acquire) != want; });
+			const uint8_t *c = r.chunk(idx);
+			const size_t used = r.used[idx % RING_CHUNKS];
+			bool end = false;
+			for (size_t off = 0; off < used;)
+			{
+				uint32_t h;
+				memcpy(&h, c + off, 4);
+				switch (h & 0xffu)
+				{
+				case CMD_REG:
+				{
+					uint64_t v;
+					memcpy(&v, c + off + 8, 8);
+					write_state_register(h >> 8, v);
+					off += 16;
+					break;
+				}
+				case CMD_KICK:
+					for (uint32_t k = h >> 24; k; k--)
+						post_kick();
+					off += 8;
+					break;
+				case CMD_DRAW:
+				{
+					for (uint32_t k = h >> 24; k; k--)
+						post_kick();
+					const uint32_t nv = (h >> 8) & 0xffu;
+					draw(nv, ((h >> 16) & 1u) != 0, reinterpret_cast<const pgs_vertex_position *>(c + off + 8),
+					     reinterpret_cast<const pgs_vertex_attribute *>(c + off + 8 + 16 * nv));
+					off += 8 + 40 * nv;
+					break;
+				}
+				case CMD_HWREG:
+				{
+					const uint64_t *data;
+					uint64_t n;
+					memcpy(&data, c + off + 8, sizeof(data));
+					memcpy(&n, c + off + 16, 8);
+					hwreg(data, size_t(n));
+					off += 24;
+					break;
+				}
+				case CMD_BARRIER:
+					off += 8;
+					break;
+				default:
+					end = true;
+					off = used;
+					break;
+				}
+			}
+			idx++;
+			r.consumed.store(idx, std::memory_order_release);
+			if (end)
+				return;
+		}
+	}
+
+	bool threaded_transfer(uint32_t pi, const uint64_t *words, size_t qwords)
+	{
+		if (worker && worker->pid != getpid())
+			stop_worker();
+		if (!worker)
+		{
+			auto *w = new (std::nothrow) DecodeWorker();
+			if (!w)
+				return false;
+			w->pid = getpid();
+			try
+			{
+				w->thread = std::thread(&pgs_gs::worker_main, this, w);
+			}
+			catch (...)
+			{
+				delete w;
+				return false;
+			}
+			worker = w;
+		}
+		uint64_t seq;
+		{
+			std::lock_guard<std::mutex> lock(worker->mutex);
+			worker->path = pi;
+			worker->words = words;
+			worker->qwords = qwords;
+			seq = ++worker->job_seq;
+		}
+		worker->cv.notify_one();
+		run_commands(worker->ring);
+		DecodeWorker *w = worker;
+		wait_until([w, seq] { return w->done_seq.load(std::memory_order_acquire) == seq; });
+		return true;
+	}
+
+	// GIFInterface::gif_transfer.
+	void gif_transfer(uint32_t pi, const uint64_t *words, size_t qwords)
+	{
+		const bool threaded =
+		    threaded_decode == PGS_THREADED_DECODE_ALWAYS ||
+		    (threaded_decode == PGS_THREADED_DECODE_AUTO && qwords >= THREADED_DECODE_MIN_QWORDS);
+		if (!threaded || !threaded_transfer(pi, words, qwords))
+		{
+			DirectSink sink(this);
+			decode(sink, pi, words, qwords);
+		}
+		decoder_store();
+	}
+
+	// GSInterface::write_register from the host.
+	void write_register(uint32_t addr, uint64_t v)
+	{
+		DirectSink sink(this);
+		assemble_register(sink, addr, v);
+		decoder_store();
+	}
+
+	~pgs_gs() { stop_worker(); }
 };
 
 // ---------------------------------------------------------------------------
@@ -2954,6 +3436,13 @@ pgs_gs *pgs_gs_create(const pgs_backend_ops *ops, void *backend, const pgs_gs_op
 	if (!options)
 		o.super_sampling = 1, o.ordered_super_sampling = 1;
 	gs->set_super_sampling(o.super_sampling, o.ordered_super_sampling != 0, o.super_sampled_textures != 0);
+	if (o.threaded_decode > PGS_THREADED_DECODE_ALWAYS)
+	{
+		delete gs;
+		*status = PGS_ERROR_INVALID_ARGUMENT;
+		return nullptr;
+	}
+	gs->threaded_decode = o.threaded_decode;
 	gs->reserve_buffers();
 	*status = gs->sticky_error;
 	if (gs->sticky_error)
@@ -3611,9 +4100,9 @@ int pgs_gs_reset_context_state(pgs_gs *gs)
 		return PGS_ERROR_INVALID_ARGUMENT;
 	gs->flush();
 	memset(gs->regs, 0, sizeof(gs->regs));
-	for (auto &p : gs->paths)
+	for (auto &p : gs->dec.paths)
 		p = pgs_gs::Path();
-	gs->internal_q = 1.0f;
+	gs->dec.internal_q = 1.0f;
 	gs->clobber_state();
 	return gs->sticky_error;
 }
@@ -3630,7 +4119,7 @@ int pgs_gs_read_register(const pgs_gs *gs, uint32_t addr, uint64_t *value)
 {
 	if (!gs || !value || addr >= 128)
 		return PGS_ERROR_INVALID_ARGUMENT;
-	*value = gs->regs[addr];
+	*value = gs->read_reg(addr);
 	return PGS_OK;
 }
 
@@ -3638,7 +4127,7 @@ int pgs_gs_set_register(pgs_gs *gs, uint32_t addr, uint64_t value)
 {
 	if (!gs || addr >= 128)
 		return PGS_ERROR_INVALID_ARGUMENT;
-	gs->regs[addr] = value;
+	gs->set_reg(addr, value);
 	return PGS_OK;
 }
 
@@ -3646,7 +4135,7 @@ int pgs_gs_get_gif_path(const pgs_gs *gs, uint32_t path, pgs_gif_path *out)
 {
 	if (!gs || !out || path >= 4)
 		return PGS_ERROR_INVALID_ARGUMENT;
-	const auto &p = gs->paths[path];
+	const auto &p = gs->dec.paths[path];
 	out->tag[0] = p.tag_lo;
 	out->tag[1] = p.tag_hi;
 	out->reg = p.reg;
@@ -3670,7 +4159,7 @@ int pgs_gs_set_gif_path(pgs_gs *gs, uint32_t path, const pgs_gif_path *in)
 		return PGS_ERROR_INVALID_ARGUMENT;
 	p.reg = in->reg;
 	p.loop = in->loop;
-	gs->paths[path] = p;
+	gs->dec.paths[path] = p;
 	return PGS_OK;
 }
 
@@ -3792,10 +4281,10 @@ int pgs_gs_dump_open(pgs_gs *gs, const char *path)
 		return r;
 	}
 	memcpy(gs->regs, regs, sizeof(regs));
-	gs->internal_q = q;
+	gs->dec.internal_q = q;
 	for (int i = 0; i < 4; i++)
 	{
-		auto &p = gs->paths[i];
+		auto &p = gs->dec.paths[i];
 		p.tag_lo = tags[i][0];
 		p.tag_hi = tags[i][1];
 		p.nloop = field(p.tag_lo, 0, 15);
@@ -3915,20 +4404,20 @@ int pgs_gs_dump_record_begin(pgs_gs *gs, const char *path)
 	for (uint32_t ctx = 0; ctx < 2; ctx++)
 		for (uint32_t reg : DUMP_CTX_REGS)
 			ok = ok && wrv(f, gs->regs[reg + ctx]);
-	ok = ok && wrv(f, gs->regs[R_RGBAQ]) && wrv(f, gs->regs[R_ST]) && wrv(f, uint32_t(gs->regs[R_UV])) &&
-	     wrv(f, uint32_t(gs->regs[R_FOG])) && wrv(f, uint64_t(0)) && wrv(f, 0xffffffffu) && wrv(f, 0xffffffffu) &&
+	ok = ok && wrv(f, gs->read_reg(R_RGBAQ)) && wrv(f, gs->read_reg(R_ST)) && wrv(f, uint32_t(gs->read_reg(R_UV))) &&
+	     wrv(f, uint32_t(gs->read_reg(R_FOG))) && wrv(f, uint64_t(0)) && wrv(f, 0xffffffffu) && wrv(f, 0xffffffffu) &&
 	     wrv(f, uint32_t(0)) && wrv(f, uint32_t(0));
 	ok = ok && wr(f, vram.data(), vram.size());
 	for (int i = 0; i < 4; i++)
 	{
-		const auto &p = gs->paths[i];
+		const auto &p = gs->dec.paths[i];
 		uint64_t lo = p.tag_lo;
 		// NLOOP minus the loops already done (the format has no loop counter).
 		uint32_t remaining = p.nloop >= p.loop ? p.nloop - p.loop : 0;
 		lo = (lo & ~0x7fffull) | (remaining & 0x7fffu);
 		ok = ok && wrv(f, lo) && wrv(f, p.tag_hi) && wrv(f, p.reg);
 	}
-	ok = ok && wrv(f, gs->internal_q);
+	ok = ok && wrv(f, gs->dec.internal_q);
 	std::vector<uint64_t> priv(PRIV_STATE_BYTES / 8, 0);
 	for (int i = 0; i < 15; i++)
 		priv[2 * i] = gs->priv[i];

@@ -54,7 +54,12 @@ class FlushStats(C.Structure):
 
 class GSOptions(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("super_sampling", C.c_uint32), ("ordered_super_sampling", C.c_uint32), ("vram_size", C.c_uint32),
-                ("dynamic_super_sampling", C.c_uint32), ("super_sampled_textures", C.c_uint32)]
+                ("dynamic_super_sampling", C.c_uint32), ("super_sampled_textures", C.c_uint32),
+                ("threaded_decode", C.c_uint32)]
+
+
+# pgs_gs_options.threaded_decode.
+THREADED_DECODE_AUTO, THREADED_DECODE_OFF, THREADED_DECODE_ALWAYS = 0, 1, 2
 
 
 class CudaBackendOptions(C.Structure):
@@ -323,11 +328,12 @@ class GSInterface:
     """GSInterface (gs/gs_interface.hpp:251-304) over any backend."""
 
     def __init__(self, backend: Backend, super_sampling: int = 1, ordered: bool = True, lib: C.CDLL | None = None,
-                 super_sampled_textures: bool = False, dynamic_super_sampling: bool = False):
+                 super_sampled_textures: bool = False, dynamic_super_sampling: bool = False,
+                 threaded_decode: int = THREADED_DECODE_AUTO):
         self.lib = lib or load_library()
         self.backend = backend
         opts = GSOptions(C.sizeof(GSOptions), super_sampling, int(ordered), VRAM_SIZE, int(dynamic_super_sampling),
-                         int(super_sampled_textures))
+                         int(super_sampled_textures), threaded_decode)
         status = C.c_int(0)
         self.handle = self.lib.pgs_gs_create(C.c_void_p(backend.ops), C.c_void_p(backend.handle), C.byref(opts),
                                              C.byref(status))

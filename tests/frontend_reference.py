@@ -39,19 +39,21 @@ def run_reference(data: bytes, super_sampling: int = 1, ordered: bool = True) ->
     return events
 
 
-def run_product(data: bytes, super_sampling: int = 1, ordered: bool = True) -> RecordingBackend:
+def run_product(data: bytes, super_sampling: int = 1, ordered: bool = True,
+                threaded_decode: int = pgs.THREADED_DECODE_AUTO) -> RecordingBackend:
     be = RecordingBackend()
-    gs = pgs.GSInterface(be, super_sampling=super_sampling, ordered=ordered)
+    gs = pgs.GSInterface(be, super_sampling=super_sampling, ordered=ordered, threaded_decode=threaded_decode)
     gs.gif_transfer(0, data)
     gs.flush()
     gs.close()
     return be
 
 
-def compare(data: bytes, super_sampling: int = 1, ordered: bool = True) -> list[str]:
+def compare(data: bytes, super_sampling: int = 1, ordered: bool = True,
+            threaded_decode: int = pgs.THREADED_DECODE_AUTO) -> list[str]:
     """Differences between the two frontends as readable lines (empty: none)."""
     events = run_reference(data, super_sampling, ordered)
-    be = run_product(data, super_sampling, ordered)
+    be = run_product(data, super_sampling, ordered, threaded_decode)
     ref_passes = [e for e in events if e["type"] == "pass"]
     tex_desc = {e["id"]: e for e in events if e["type"] == "texture"}
     out: list[str] = []

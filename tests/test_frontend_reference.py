@@ -11,6 +11,7 @@ reference's sources, so these tests skip where those are not mounted."""
 import pytest
 
 import gsgen as g
+import pgs
 import pgs_ref_frontend
 from frontend_reference import compare
 
@@ -34,10 +35,17 @@ STREAMS = [
   + [("hazards_%d" % i, (lambda i=i: g.frame_hazards(i))) for i in range(16)]
 
 
+DECODE_MODES = {"auto": pgs.THREADED_DECODE_AUTO, "direct": pgs.THREADED_DECODE_OFF,
+                "threaded": pgs.THREADED_DECODE_ALWAYS}
+
+
+@pytest.mark.parametrize("mode", sorted(DECODE_MODES))
 @pytest.mark.parametrize("name,make", STREAMS, ids=[n for n, _ in STREAMS])
-def test_frontend_matches_reference(name, make):
+def test_frontend_matches_reference(name, make, mode):
+    """Every stream with the GIF decoder on the calling thread, on the worker
+    thread, and chosen by transfer size."""
     frame = make()
-    diffs = compare(frame.data, frame.super_sampling, frame.ordered)
+    diffs = compare(frame.data, frame.super_sampling, frame.ordered, DECODE_MODES[mode])
     assert not diffs, "\n".join(diffs[:20])
 
 
