@@ -39,14 +39,18 @@ struct __align__(16) PrimSetup
 };
 static_assert(sizeof(PrimSetup) == 80, "PrimSetup layout");
 
+// Interpolation terms per primitive: value at the first vertex and the
+// differences to the other two, for S T Q FOG and for the unorm colour.
 struct __align__(16) TransformedAttr
 {
 	float stqf0[4];
 	float stqf1[4];
 	float stqf2[4];
-	uint32_t rgba0, rgba1, rgba2, padding;
+	float rgba0[4];
+	float rgba1[4];
+	float rgba2[4];
 };
-static_assert(sizeof(TransformedAttr) == 64, "TransformedAttr layout");
+static_assert(sizeof(TransformedAttr) == 96, "TransformedAttr layout");
 
 // Decoded framebuffer instance for the shading kernels.
 struct DevInstance
@@ -261,6 +265,24 @@ __device__ __forceinline__ void dswap(T &a, T &b) { T t = a; a = b; b = t; }
 
 // ---------------------------------------------------------------------------
 // K1: triangle setup.
+__device__ __forceinline__ float unorm8_lut(const float *lut, uint32_t c, int ch) { return __ldg(lut + ((c >> (8 * ch)) & 0xffu)); }
+
+// Colour terms of the shading interpolation c0 + (c1 - c0) i + (c2 - c0) j,
+// per channel in unorm floats.
+__device__ __forceinline__ void set_color_terms(const PassParams &P, TransformedAttr &ta, uint32_t r0, uint32_t r1,
+                                                uint32_t r2)
+{
+	#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		const float c0 = unorm8_lut(P.unorm_lut, r0, k), c1 = unorm8_lut(P.unorm_lut, r1, k);
+		const float c2 = unorm8_lut(P.unorm_lut, r2, k);
+		ta.rgba0[k] = c0;
+		ta.rgba1[k] = fsub(c1, c0);
+		ta.rgba2[k] = fsub(c2, c0);
+	}
+}
+
 __global__ void __launch_bounds__(128) setup_kernel(PassParams P)
 {
 	uint32_t index = blockIdx.x * blockDim.x + threadIdx.x;
@@ -482,14 +504,13 @@ __global__ void __launch_bounds__(128) setup_kernel(PassParams P)
 		uint32_t r0 = at0.rgba, r1 = at1.rgba, r2 = at2.rgba;
 		if (fix) r1 = r0;
 		if (fix || line) r2 = r0;
-		ta.rgba0 = r0; ta.rgba1 = r1; ta.rgba2 = r2;
+		set_color_terms(P, ta, r0, r1, r2);
 	}
 	else
 	{
 		uint32_t flat = P.attr[3 * index].rgba;
-		ta.rgba0 = flat; ta.rgba1 = flat; ta.rgba2 = flat;
+		set_color_terms(P, ta, flat, flat, flat);
 	}
-	ta.padding = 0;
 
 	int32_t pa0 = dadx, pa1 = dady, pa2 = int32_t(uint32_t(uint64_t(const_a) >> 1));
 	int32_t pb0 = dbdx, pb1 = dbdy, pb2 = int32_t(uint32_t(uint64_t(const_b) >> 1));
@@ -1000,7 +1021,6 @@ struct Request
 
 // unpackUnorm4x8 channel: float(c) / 255 correctly rounded.  The 256 values are
 // computed on the host with IEEE division and read from a table.
-__device__ __forceinline__ float unorm8_lut(const float *lut, uint32_t c, int ch) { return __ldg(lut + ((c >> (8 * ch)) & 0xffu)); }
 __device__ __forceinline__ float unorm8(uint32_t c, int ch) { return __fdiv_rn(float((c >> (8 * ch)) & 0xffu), 255.0f); }
 
 __device__ __forceinline__ uint32_t pack_unorm(float r, float g, float b, float a)
@@ -1475,8 +1495,7 @@ __device__ void combined_color(const ShadeCtx &C, uint32_t pi, const Request &r,
 	#pragma unroll
 	for (int k = 0; k < 4; k++)
 	{
-		float c0 = unorm8_lut(P.unorm_lut, a.rgba0, k), c1 = unorm8_lut(P.unorm_lut, a.rgba1, k), c2 = unorm8_lut(P.unorm_lut, a.rgba2, k);
-		float t = interp(c0, fsub(c1, c0), fsub(c2, c0), r.i, r.j);
+		float t = interp(a.rgba0[k], a.rgba1[k], a.rgba2[k], r.i, r.j);
 		col[k] = floorf(fadd(fmul(255.0f, t), 1.0f / 256.0f));
 	}
 	bool fog = (combiner & COMBINER_FOG_BIT) != 0, tcc = (combiner & COMBINER_TCC_BIT) != 0;
@@ -1876,11 +1895,9 @@ __device__ __forceinline__ void sample_offset(uint32_t s, uint32_t xl, uint32_t 
 // rectangle costs more than the coverage test it would skip, so coverage
 // alone decides.
 template <bool SS, bool AA, bool MIP>
-__device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi, SampleState &S, uint32_t &covered)
+__device__ __forceinline__ void process_primitive_with(const ShadeCtx &C, uint32_t pi, const PrimSetup &s, uint32_t st,
+                                                       SampleState &S, uint32_t &covered)
 {
-	const PassParams &P = *C.P;
-	const PrimSetup s = P.setup[pi];
-	uint32_t st = P.prims[pi].state;
 	bool opaque, any_cov;
 	Request q = shade_early<AA, MIP>(C, s, pi, st, S, opaque, any_cov);
 	if (!any_cov)
@@ -1940,6 +1957,190 @@ __device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi
 			S.pending_prim = pi;
 		}
 	}
+	// A primitive that is not opaque is shaded right away rather than left
+	// pending.  The result is the same as shading it at the next flush:
+	// leaving it pending only saves work when a later opaque primitive covers
+	// the sample, which blended primitives seldom meet, and shading now keeps
+	// every lane of the call on the same primitive.
+	if (!((st >> STATE_BIT_OPAQUE) & 1u) &&
+	    __any_sync(0xffffffffu, S.pending.coverage > 0 && S.pending_prim == pi))
+	{
+		if (S.pending.coverage > 0 && S.pending_prim == pi)
+		{
+			shade_resolve<MIP>(C, S);
+			S.pending.coverage = 0;
+			S.pending.z_write = false;
+		}
+	}
+}
+
+template <bool SS, bool AA, bool MIP>
+__device__ __forceinline__ void process_primitive(const ShadeCtx &C, uint32_t pi, SampleState &S, uint32_t &covered)
+{
+	const PassParams &P = *C.P;
+	const PrimSetup s = P.setup[pi];
+	process_primitive_with<SS, AA, MIP>(C, pi, s, P.prims[pi].state, S, covered);
+}
+
+// ---------------------------------------------------------------------------
+// Primitive culling per warp.  A warp's samples have raster positions (after
+// any snapping of coverage) inside a rectangle; a primitive whose box misses
+// it, or one of whose edges is negative at every point of it, covers none of
+// the warp's samples and would be a no-op for that warp.  The edge test
+// follows the coverage test's 32-bit wrapping arithmetic: the value at the
+// rectangle's best corner is exact modulo 2^32, every other sample's value
+// is that minus at most d, and a primitive is only dropped when no sample's
+// value can wrap back to non-negative.
+
+// Whether edge e can be non-negative somewhere in r (raster units, shift sh
+// to the coverage test's sub-pixel units).
+__device__ __forceinline__ bool edge_may_pass(const int32_t e[3], int4 r, int sh)
+{
+	const int32_t x = e[0] >= 0 ? r.z : r.x, y = e[1] >= 0 ? r.w : r.y;
+	const int32_t v = idot3(e, x << sh, y << sh);
+	if (v >= 0)
+		return true;
+	const int64_t d = llabs(int64_t(e[0])) * (int64_t(r.z - r.x) << sh) + llabs(int64_t(e[1])) * (int64_t(r.w - r.y) << sh);
+	return int64_t(v) - d < -2147483648LL;
+}
+
+// Conservative: false only when the primitive covers no sample whose raster
+// position lies in r = (x0, y0, x1, y1).  Parallelograms (sprites, lines,
+// fused rectangles) shift edges past the diagonal and AA1 multisampled
+// edges cover outside the triangle, so those keep to the box test.
+template <bool AA>
+__device__ __forceinline__ bool may_cover(const PrimSetup &s, uint32_t st, int4 r, int dim)
+{
+	if ((r.z >> dim) < s.bb[0] || (r.x >> dim) > s.bb[2] || (r.w >> dim) < s.bb[1] || (r.y >> dim) > s.bb[3])
+		return false;
+	if (((st >> STATE_BIT_PARALLELOGRAM) & 1u) || (AA && ((st >> STATE_BIT_MULTISAMPLE) & 1u)))
+		return true;
+	const int sh = 3 - dim;
+	const int32_t A[3] = { s.a[0] >> 6, s.a[1], s.a[2] };
+	return edge_may_pass(A, r, sh) && edge_may_pass(s.b, r, sh) && edge_may_pass(s.c, r, sh);
+}
+
+// The sub-tile's primitive list walked by the whole CTA, in chunks of up to
+// CH primitives in ascending order: warp 0 expands the bin's bitmask into
+// primitive indices, every thread then tests one primitive against the
+// rectangles of all warps and stages its setup record in shared memory, and
+// each warp shades the primitives that can touch it.  The primitives a warp
+// skips are the ones whose coverage test would fail on every lane, so each
+// warp sees the same sequence of covering primitives as walking the whole
+// list.
+template <int NS, bool SS, bool AA, bool MIP>
+__device__ __forceinline__ void walk_culled(const ShadeCtx &C, const DevInstance &I, const uint32_t *summary,
+                                            const uint32_t *mask, uint32_t t, SampleState &S, uint32_t &covered)
+{
+	constexpr uint32_t T = 64u * NS, WARPS = T / 32u, CH = T < 256u ? T : 256u;
+	__shared__ uint32_t s_ids[CH], s_wmask[CH], s_state[CH];
+	__shared__ PrimSetup s_setup[CH];
+	__shared__ int4 s_rect[WARPS];
+	// Bitmask cursor of warp 0 between chunks.
+	__shared__ uint32_t s_sv[32], s_mw[32];
+	__shared__ uint32_t s_next_group, s_group, s_nz, s_words, s_word_base, s_n, s_more;
+	const PassParams &P = *C.P;
+	const uint32_t lane = t & 31u, warp = t >> 5;
+	const unsigned full = 0xffffffffu;
+	{
+		const int32_t x0 = S.hx & C.snap_mask_x, y0 = S.hy & C.snap_mask_x & C.snap_mask_y;
+		const int4 r = make_int4(__reduce_min_sync(full, x0), __reduce_min_sync(full, y0),
+		                         __reduce_max_sync(full, S.hx), __reduce_max_sync(full, S.hy));
+		if (lane == 0)
+			s_rect[warp] = r;
+	}
+	if (t == 0)
+	{
+		s_next_group = 0;
+		s_nz = 0;
+		s_words = 0;
+	}
+	__syncthreads();
+	for (;;)
+	{
+		if (warp == 0)
+		{
+			uint32_t next_group = s_next_group, group = s_group, nz = s_nz, words = s_words, word_base = s_word_base;
+			uint32_t sv = s_sv[lane], mw = s_mw[lane];
+			uint32_t n = 0;
+			bool more = true;
+			while (n + 32u <= CH)
+			{
+				// The next non-zero mask word: summary group -> summary word -> mask word.
+				while (words == 0u && more)
+				{
+					while (nz == 0u && next_group < I.summary_words)
+					{
+						group = next_group;
+						next_group += 32u;
+						sv = (group + lane < I.summary_words) ? __ldg(summary + group + lane) : 0u;
+						nz = __ballot_sync(full, sv != 0u);
+					}
+					if (nz == 0u)
+					{
+						more = false;
+						break;
+					}
+					const int l = __ffs(nz) - 1;
+					nz &= nz - 1u;
+					words = __shfl_sync(full, sv, l);
+					word_base = (group + uint32_t(l)) * 32u;
+					mw = ((words >> lane) & 1u) ? __ldg(mask + word_base + lane) : 0u;
+				}
+				if (!more)
+					break;
+				const int j = __ffs(words) - 1;
+				words &= words - 1u;
+				const uint32_t m = __shfl_sync(full, mw, j);
+				if ((m >> lane) & 1u)
+					s_ids[n + __popc(m & ((1u << lane) - 1u))] = I.prim_lo + (word_base + uint32_t(j)) * 32u + lane;
+				n += __popc(m);
+			}
+			s_sv[lane] = sv;
+			s_mw[lane] = mw;
+			if (lane == 0)
+			{
+				s_next_group = next_group;
+				s_group = group;
+				s_nz = nz;
+				s_words = words;
+				s_word_base = word_base;
+				s_n = n;
+				s_more = more;
+			}
+		}
+		__syncthreads();
+		const uint32_t n = s_n;
+		const bool more = s_more != 0u;
+		if (t < n)
+		{
+			const uint32_t pi = s_ids[t];
+			const PrimSetup ps = P.setup[pi];
+			const uint32_t st = P.prims[pi].state;
+			uint32_t wm = 0;
+			#pragma unroll
+			for (uint32_t w = 0; w < WARPS; w++)
+				wm |= uint32_t(may_cover<AA>(ps, st, s_rect[w], C.dim)) << w;
+			s_setup[t] = ps;
+			s_state[t] = st;
+			s_wmask[t] = wm;
+		}
+		__syncthreads();
+		for (uint32_t kb = 0; kb < n; kb += 32u)
+		{
+			const uint32_t k = kb + lane;
+			uint32_t bits = __ballot_sync(full, k < n && ((s_wmask[k] >> warp) & 1u));
+			while (bits)
+			{
+				const uint32_t b = uint32_t(__ffs(bits) - 1);
+				bits &= bits - 1u;
+				process_primitive_with<SS, AA, MIP>(C, s_ids[kb + b], s_setup[kb + b], s_state[kb + b], S, covered);
+			}
+		}
+		if (!more)
+			break;
+		__syncthreads();
+	}
 }
 
 // One CTA per 8x8-pixel sub-tile, NS samples per pixel, one thread per sample.
@@ -1964,9 +2165,10 @@ __device__ __forceinline__ uint32_t subtile_mode(const PassParams &P, const DevI
 }
 
 // One sub-tile's pixel samples; `t` is the thread's index among the 64 * NS
-// threads that cover the sub-tile.  Warps are independent: each walks the
-// sub-tile's primitive bitmask on its own and needs no barrier.
-template <int NS, bool SS, bool AA, bool MIP = false>
+// threads that cover the sub-tile.  CULL: the whole CTA runs the sub-tile and
+// walks its primitive list together (walk_culled); otherwise each warp walks
+// the sub-tile's primitive bitmask on its own and needs no barrier.
+template <int NS, bool SS, bool AA, bool MIP = false, bool CULL = false>
 __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInstance &I, const uint32_t *sub_masks,
                                               const uint32_t *sub_summary, uint32_t sub, uint32_t t)
 {
@@ -2060,6 +2262,9 @@ __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInst
 
 	// Walk the primitive list in ascending order: summary word -> mask words -> bits.
 	uint32_t covered = 0;
+	if constexpr (CULL)
+		walk_culled<NS, SS, AA, MIP>(C, I, summary, mask, t, S, covered);
+	else
 	for (uint32_t sbase = 0; sbase < I.summary_words; sbase += 32u)
 	{
 		uint32_t sv = (sbase + lane < I.summary_words) ? __ldg(summary + sbase + lane) : 0u;
@@ -2211,7 +2416,7 @@ __global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kerne
 		return;
 	if (subtile_mode(P, I, tile_flags, sub) != (SS ? 2u : 1u))
 		return;
-	shade_subtile<NS, SS, AA, MIP>(P, I, sub_masks, sub_summary, sub, threadIdx.x);
+	shade_subtile<NS, SS, AA, MIP, true>(P, I, sub_masks, sub_summary, sub, threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
