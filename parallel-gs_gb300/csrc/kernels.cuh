@@ -1158,6 +1158,30 @@ __device__ __forceinline__ void effective_wrap(pgs_texture_desc &t, uint32_t tex
 		t.wmt = (tex_word & TEX_SAMPLER_CLAMP_T_BIT) ? WRAP_CLAMP : WRAP_REPEAT;
 }
 
+// A wrap mode as (v & and_mask | or_mask) clamped to [lo, hi]: REPEAT masks,
+// CLAMP and REGION_CLAMP clamp, REGION_REPEAT masks with MINU and ors MAXU.
+struct WrapAxis
+{
+	int32_t and_mask, or_mask, lo, hi;
+};
+
+__device__ __forceinline__ WrapAxis wrap_axis(uint32_t mode, uint32_t size_log2, uint32_t lo, uint32_t hi)
+{
+	const int32_t m = (1 << size_log2) - 1;
+	switch (mode)
+	{
+	case WRAP_REPEAT: return { m, 0, INT32_MIN, INT32_MAX };
+	case WRAP_CLAMP: return { -1, 0, 0, m };
+	case WRAP_REGION_CLAMP: return { -1, 0, int32_t(lo), int32_t(hi) };
+	default: return { m & int32_t(lo), int32_t(hi), INT32_MIN, INT32_MAX };
+	}
+}
+
+__device__ __forceinline__ int32_t wrap_apply(int32_t v, const WrapAxis &w)
+{
+	return min(max((v & w.and_mask) | w.or_mask, w.lo), w.hi);
+}
+
 __device__ __forceinline__ int32_t wrap_coord(int32_t v, uint32_t mode, uint32_t size_log2, uint32_t lo, uint32_t hi)
 {
 	int32_t size = 1 << size_log2;
@@ -1263,10 +1287,11 @@ __device__ void sample_level(const PassParams &P, uint32_t tex_index, const pgs_
 	int32_t kv = int32_t(floorf(fadd(fmul(vv, 16.0f), 1.0f / 64.0f)));
 	const TexImage im = P.tex_images[tex_index * TEX_SLOTS + slot];
 	const uint32_t *img = P.texels + im.offset;
+	const WrapAxis wu = wrap_axis(t.wms, twl, minu, maxu), wv = wrap_axis(t.wmt, thl, minv, maxv);
 	if (!linear)
 	{
-		int32_t x = wrap_coord(ku >> 4, t.wms, twl, minu, maxu);
-		int32_t y = wrap_coord(kv >> 4, t.wmt, thl, minv, maxv);
+		int32_t x = wrap_apply(ku >> 4, wu);
+		int32_t y = wrap_apply(kv >> 4, wv);
 		uint32_t c = __ldg(img + uint32_t(y) * im.ext_u + uint32_t(x));
 		#pragma unroll
 		for (int k = 0; k < 4; k++)
@@ -1276,27 +1301,27 @@ __device__ void sample_level(const PassParams &P, uint32_t tex_index, const pgs_
 	int32_t bu = ku - 8, bv = kv - 8;
 	int32_t x0 = bu >> 4, y0 = bv >> 4;
 	uint32_t fx = uint32_t(bu) & 15u, fy = uint32_t(bv) & 15u;
-	int32_t xs0 = wrap_coord(x0, t.wms, twl, minu, maxu);
-	int32_t xs1 = wrap_coord(x0 + 1, t.wms, twl, minu, maxu);
-	int32_t ys0 = wrap_coord(y0, t.wmt, thl, minv, maxv);
-	int32_t ys1 = wrap_coord(y0 + 1, t.wmt, thl, minv, maxv);
+	int32_t xs0 = wrap_apply(x0, wu);
+	int32_t xs1 = wrap_apply(x0 + 1, wu);
+	int32_t ys0 = wrap_apply(y0, wv);
+	int32_t ys1 = wrap_apply(y0 + 1, wv);
 	uint32_t w00 = (16u - fx) * (16u - fy), w10 = fx * (16u - fy), w01 = (16u - fx) * fy, w11 = fx * fy;
 	const uint32_t *row0 = img + uint32_t(ys0) * im.ext_u, *row1 = img + uint32_t(ys1) * im.ext_u;
 	uint32_t c00 = __ldg(row0 + xs0);
 	uint32_t c10 = __ldg(row0 + xs1);
 	uint32_t c01 = __ldg(row1 + xs0);
 	uint32_t c11 = __ldg(row1 + xs1);
-	#pragma unroll
-	for (int k = 0; k < 4; k++)
-	{
-		int sh = 8 * k;
-		uint32_t acc = w00 * ((c00 >> sh) & 0xffu) + w10 * ((c10 >> sh) & 0xffu) + w01 * ((c01 >> sh) & 0xffu) +
-		               w11 * ((c11 >> sh) & 0xffu);
-		uint32_t q = acc >> 8, r = acc & 0xffu;
-		if (r > 128u || (r == 128u && (q & 1u)))
-			q++;
-		rgba[k] = q;
-	}
+	// Two channels per 32-bit word (R and B, then G and A), 16 bits each:
+	// the weights sum to 256, so a channel's sum stays below 2^16.
+	const uint32_t m = 0x00ff00ffu;
+	const uint32_t rb = w00 * (c00 & m) + w10 * (c10 & m) + w01 * (c01 & m) + w11 * (c11 & m);
+	const uint32_t ga = w00 * ((c00 >> 8) & m) + w10 * ((c10 >> 8) & m) + w01 * ((c01 >> 8) & m) + w11 * ((c11 >> 8) & m);
+	// acc / 256 rounded half to even.
+	auto round256 = [](uint32_t acc) { return (acc + 127u + ((acc >> 8) & 1u)) >> 8; };
+	rgba[0] = round256(rb & 0xffffu);
+	rgba[1] = round256(ga & 0xffffu);
+	rgba[2] = round256(rb >> 16);
+	rgba[3] = round256(ga >> 16);
 }
 
 // Level of detail and filter choice (sample_texture, ubershader.comp:1064-1131):
@@ -1452,6 +1477,17 @@ __device__ void sample_texture(const PassParams &P, uint32_t tex_word, uint32_t 
 	}
 	const bool clamp_s = (tex_word & TEX_SAMPLER_CLAMP_S_BIT) != 0;
 	const bool clamp_t = (tex_word & TEX_SAMPLER_CLAMP_T_BIT) != 0;
+	if (!MIP)
+	{
+		// Level 0 through MMAG: the level blend below is the identity.
+		uint32_t c[4];
+		sample_level(P, tex_index, t, 0, 0, clamp_s, clamp_t, (tex_word & TEX_SAMPLER_MAG_LINEAR_BIT) != 0, u, v,
+		             perspective, c);
+		#pragma unroll
+		for (int k = 0; k < 4; k++)
+			out[k] = float(c[k]);
+		return;
+	}
 	uint32_t sel = (tex_word & TEX_SAMPLER_MAG_LINEAR_BIT) ? (1u << 16) : 0u;
 	if (MIP && ((tex_word >> TEX_MAX_MIP_LEVEL_OFFSET) & 7u))
 		sel = select_lod(t.levels, tex_word, tex2, q);
