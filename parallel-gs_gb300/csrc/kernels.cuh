@@ -2056,28 +2056,29 @@ __device__ __forceinline__ bool may_cover(const PrimSetup &s, uint32_t st, int4 
 	return edge_may_pass(A, r, sh) && edge_may_pass(s.b, r, sh) && edge_may_pass(s.c, r, sh);
 }
 
-// The sub-tile's primitive list walked by the whole CTA, in chunks of up to
-// CH primitives in ascending order: warp 0 expands the bin's bitmask into
-// primitive indices, every thread then tests one primitive against the
-// rectangles of all warps and stages its setup record in shared memory, and
-// each warp shades the primitives that can touch it.  The primitives a warp
-// skips are the ones whose coverage test would fail on every lane, so each
-// warp sees the same sequence of covering primitives as walking the whole
-// list.
+// The sub-tile's primitive list, expanded by the whole CTA into primitive
+// indices in ascending order in shared memory (CAP at a time), then walked by
+// each warp on its own, 32 primitives at a time: every lane tests one
+// primitive against the warp's rectangle and the warp shades, in order, the
+// primitives that can touch it.  The primitives a warp skips are the ones
+// whose coverage test would fail on every lane, so each warp sees the same
+// sequence of covering primitives as walking the whole list.  Expansion:
+// each warp counts the primitives under its summary words, warp 0 turns the
+// counts into offsets, and each warp writes its indices at those offsets.
 template <int NS, bool SS, bool AA, bool MIP>
 __device__ __forceinline__ void walk_culled(const ShadeCtx &C, const DevInstance &I, const uint32_t *summary,
                                             const uint32_t *mask, uint32_t t, SampleState &S, uint32_t &covered)
 {
-	constexpr uint32_t T = 64u * NS, WARPS = T / 32u, CH = T < 256u ? T : 256u;
-	__shared__ uint32_t s_ids[CH], s_wmask[CH], s_state[CH];
-	__shared__ PrimSetup s_setup[CH];
+	constexpr uint32_t T = 64u * NS, WARPS = T / 32u, CAP = 2048u;
+	// One summary word per 32 mask words of 32 primitives.
+	constexpr uint32_t MAX_SW = (PGS_MAX_PRIMITIVES_PER_FLUSH + 1023u) / 1024u;
+	__shared__ uint32_t s_ids[CAP];
+	__shared__ uint32_t s_off[MAX_SW + 1];
 	__shared__ int4 s_rect[WARPS];
-	// Bitmask cursor of warp 0 between chunks.
-	__shared__ uint32_t s_sv[32], s_mw[32];
-	__shared__ uint32_t s_next_group, s_group, s_nz, s_words, s_word_base, s_n, s_more;
 	const PassParams &P = *C.P;
 	const uint32_t lane = t & 31u, warp = t >> 5;
 	const unsigned full = 0xffffffffu;
+	const uint32_t SW = I.summary_words;
 	{
 		const int32_t x0 = S.hx & C.snap_mask_x, y0 = S.hy & C.snap_mask_x & C.snap_mask_y;
 		const int4 r = make_int4(__reduce_min_sync(full, x0), __reduce_min_sync(full, y0),
@@ -2085,97 +2086,85 @@ __device__ __forceinline__ void walk_culled(const ShadeCtx &C, const DevInstance
 		if (lane == 0)
 			s_rect[warp] = r;
 	}
-	if (t == 0)
+	for (uint32_t sw = warp; sw < SW; sw += WARPS)
 	{
-		s_next_group = 0;
-		s_nz = 0;
-		s_words = 0;
+		const uint32_t words = __ldg(summary + sw);
+		const uint32_t mw = ((words >> lane) & 1u) ? __ldg(mask + sw * 32u + lane) : 0u;
+		const uint32_t c = __reduce_add_sync(full, uint32_t(__popc(mw)));
+		if (lane == 0)
+			s_off[sw] = c;
 	}
 	__syncthreads();
-	for (;;)
+	if (warp == 0)
 	{
-		if (warp == 0)
+		uint32_t carry = 0;
+		for (uint32_t base = 0; base < SW; base += 32u)
 		{
-			uint32_t next_group = s_next_group, group = s_group, nz = s_nz, words = s_words, word_base = s_word_base;
-			uint32_t sv = s_sv[lane], mw = s_mw[lane];
-			uint32_t n = 0;
-			bool more = true;
-			while (n + 32u <= CH)
-			{
-				// The next non-zero mask word: summary group -> summary word -> mask word.
-				while (words == 0u && more)
-				{
-					while (nz == 0u && next_group < I.summary_words)
-					{
-						group = next_group;
-						next_group += 32u;
-						sv = (group + lane < I.summary_words) ? __ldg(summary + group + lane) : 0u;
-						nz = __ballot_sync(full, sv != 0u);
-					}
-					if (nz == 0u)
-					{
-						more = false;
-						break;
-					}
-					const int l = __ffs(nz) - 1;
-					nz &= nz - 1u;
-					words = __shfl_sync(full, sv, l);
-					word_base = (group + uint32_t(l)) * 32u;
-					mw = ((words >> lane) & 1u) ? __ldg(mask + word_base + lane) : 0u;
-				}
-				if (!more)
-					break;
-				const int j = __ffs(words) - 1;
-				words &= words - 1u;
-				const uint32_t m = __shfl_sync(full, mw, j);
-				if ((m >> lane) & 1u)
-					s_ids[n + __popc(m & ((1u << lane) - 1u))] = I.prim_lo + (word_base + uint32_t(j)) * 32u + lane;
-				n += __popc(m);
-			}
-			s_sv[lane] = sv;
-			s_mw[lane] = mw;
-			if (lane == 0)
-			{
-				s_next_group = next_group;
-				s_group = group;
-				s_nz = nz;
-				s_words = words;
-				s_word_base = word_base;
-				s_n = n;
-				s_more = more;
-			}
-		}
-		__syncthreads();
-		const uint32_t n = s_n;
-		const bool more = s_more != 0u;
-		if (t < n)
-		{
-			const uint32_t pi = s_ids[t];
-			const PrimSetup ps = P.setup[pi];
-			const uint32_t st = P.prims[pi].state;
-			uint32_t wm = 0;
+			const uint32_t i = base + lane;
+			const uint32_t v = i < SW ? s_off[i] : 0u;
+			uint32_t x = v;
 			#pragma unroll
-			for (uint32_t w = 0; w < WARPS; w++)
-				wm |= uint32_t(may_cover<AA>(ps, st, s_rect[w], C.dim)) << w;
-			s_setup[t] = ps;
-			s_state[t] = st;
-			s_wmask[t] = wm;
+			for (int o = 1; o < 32; o <<= 1)
+			{
+				const uint32_t y = __shfl_up_sync(full, x, o);
+				if (lane >= uint32_t(o))
+					x += y;
+			}
+			if (i < SW)
+				s_off[i] = carry + x - v;
+			carry += __shfl_sync(full, x, 31);
+		}
+		if (lane == 0)
+			s_off[SW] = carry;
+	}
+	__syncthreads();
+	const uint32_t total = s_off[SW];
+	for (uint32_t round = 0; round < total; round += CAP)
+	{
+		for (uint32_t sw = warp; sw < SW; sw += WARPS)
+		{
+			const uint32_t off = s_off[sw], end = s_off[sw + 1];
+			if (end <= round || off >= round + CAP)
+				continue;
+			const uint32_t words = __ldg(summary + sw);
+			const uint32_t mw = ((words >> lane) & 1u) ? __ldg(mask + sw * 32u + lane) : 0u;
+			const uint32_t pc = uint32_t(__popc(mw));
+			uint32_t x = pc;
+			#pragma unroll
+			for (int o = 1; o < 32; o <<= 1)
+			{
+				const uint32_t y = __shfl_up_sync(full, x, o);
+				if (lane >= uint32_t(o))
+					x += y;
+			}
+			uint32_t pos = off + x - pc;
+			const uint32_t prim_base = I.prim_lo + (sw * 32u + lane) * 32u;
+			for (uint32_t m = mw; m; m &= m - 1u, pos++)
+				if (pos >= round && pos < round + CAP)
+					s_ids[pos - round] = prim_base + uint32_t(__ffs(m) - 1);
 		}
 		__syncthreads();
+		const uint32_t n = min(total - round, CAP);
 		for (uint32_t kb = 0; kb < n; kb += 32u)
 		{
 			const uint32_t k = kb + lane;
-			uint32_t bits = __ballot_sync(full, k < n && ((s_wmask[k] >> warp) & 1u));
+			uint32_t pi = 0;
+			bool hit = false;
+			if (k < n)
+			{
+				pi = s_ids[k];
+				hit = may_cover<AA>(P.setup[pi], P.prims[pi].state, s_rect[warp], C.dim);
+			}
+			uint32_t bits = __ballot_sync(full, hit);
 			while (bits)
 			{
-				const uint32_t b = uint32_t(__ffs(bits) - 1);
+				const int b = __ffs(bits) - 1;
 				bits &= bits - 1u;
-				process_primitive_with<SS, AA, MIP>(C, s_ids[kb + b], s_setup[kb + b], s_state[kb + b], S, covered);
+				process_primitive<SS, AA, MIP>(C, __shfl_sync(full, pi, b), S, covered);
 			}
 		}
-		if (!more)
-			break;
-		__syncthreads();
+		if (round + CAP < total)
+			__syncthreads();
 	}
 }
 
