@@ -144,7 +144,7 @@ typedef uint64_t Word2 __attribute__((vector_size(16), aligned(4), may_alias));
 
 // Vertex copy in the widths the vertex queue writes: the 16-byte position,
 // then the attributes as 16 + 8 bytes.
-static inline void copy_vertex(pgs_vertex_position &dp, pgs_vertex_attribute &da, const pgs_vertex_position &sp,
+static __attribute__((always_inline)) inline void copy_vertex(pgs_vertex_position &dp, pgs_vertex_attribute &da, const pgs_vertex_position &sp,
                                const pgs_vertex_attribute &sa)
 {
 	static_assert(sizeof(pgs_vertex_position) == 16 && sizeof(pgs_vertex_attribute) == 24, "vertex layout");
@@ -1391,7 +1391,7 @@ struct pgs_gs : TrackerClient
 
 	// ---------------------------------------------------------------
 	// Vertex queue (gs/gs_interface.cpp:843-897).
-	void shift_queue()
+	__attribute__((always_inline)) inline void shift_queue()
 	{
 		auto &vq = dec.vq;
 		if (vq.count == 3)
@@ -1404,7 +1404,7 @@ struct pgs_gs : TrackerClient
 
 	// The queue entry: position (x, y, z, 0) and attributes (s, t, q, rgba |
 	// fog, u, v) packed into words in registers and stored whole.
-	void push_vertex(uint64_t v, uint32_t z, float fog)
+	__attribute__((always_inline)) inline void push_vertex(uint64_t v, uint32_t z, float fog)
 	{
 		shift_queue();
 		auto &vq = dec.vq;
@@ -1422,8 +1422,8 @@ struct pgs_gs : TrackerClient
 		vq.count++;
 	}
 
-	void vertex_kick_xyz(uint64_t v) { push_vertex(v, uint32_t(v >> 32), float(field(dec.fog, 56, 8))); }
-	void vertex_kick_xyzf(uint64_t v) { push_vertex(v, field(v, 32, 24), float(field(v, 56, 8))); }
+	__attribute__((always_inline)) inline void vertex_kick_xyz(uint64_t v) { push_vertex(v, uint32_t(v >> 32), float(field(dec.fog, 56, 8))); }
+	__attribute__((always_inline)) inline void vertex_kick_xyzf(uint64_t v) { push_vertex(v, field(v, 32, 24), float(field(v, 56, 8))); }
 
 	// ---------------------------------------------------------------
 	// draw_is_degenerate (gs/gs_interface.cpp:2036-2115).
@@ -2406,7 +2406,7 @@ struct pgs_gs : TrackerClient
 	// checks for degenerate state and appends; every kick ends in post_kick
 	// on the state side.
 	template <class Sink>
-	void drawing_kick(Sink &s, bool adc)
+	__attribute__((always_inline)) inline void drawing_kick(Sink &s, bool adc)
 	{
 		auto &vq = dec.vq;
 		uint32_t type = field(dec.prim, 0, 3);
@@ -2832,7 +2832,7 @@ struct pgs_gs : TrackerClient
 	// ---------------------------------------------------------------
 	// GIF packet decode (gs/gs_interface.cpp:4290-4397).
 	template <class Sink>
-	void packed_write(Sink &s, uint32_t desc, const uint64_t *q)
+	__attribute__((always_inline)) inline void packed_write(Sink &s, uint32_t desc, const uint64_t *q)
 	{
 		uint64_t lo = q[0], hi = q[1];
 		switch (desc)
@@ -3116,7 +3116,7 @@ struct pgs_gs : TrackerClient
 		uint64_t index = 0;
 		uint32_t kicks = 0;
 
-		uint8_t *reserve(size_t bytes)
+		__attribute__((always_inline)) inline uint8_t *reserve(size_t bytes)
 		{
 			if (!cur || off + bytes > RING_CHUNK_BYTES)
 			{
@@ -3170,7 +3170,7 @@ struct pgs_gs : TrackerClient
 			uint64_t n = count;
 			memcpy(p + 16, &n, 8);
 		}
-		DrawSlot begin_draw(uint32_t nv, bool quad)
+		__attribute__((always_inline)) inline DrawSlot begin_draw(uint32_t nv, bool quad)
 		{
 			uint8_t *p = reserve(8 + 40 * nv);
 			header(p, CMD_DRAW | (nv << 8) | (uint32_t(quad) << 16) | (kicks << 24));
