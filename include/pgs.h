@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define PGS_ABI_VERSION 5u
+#define PGS_ABI_VERSION 6u
 /* VRAM snapshots a render pass can hold (pgs_render_pass.snapshot_textures). */
 #define PGS_MAX_VRAM_SNAPSHOTS 4u
 
@@ -355,6 +355,15 @@ typedef struct pgs_backend_ops
 	 * decodes the pass's textures from the snapshots pgs_render_pass names and
 	 * releases the slots. */
 	int (*snapshot_vram)(void *self);
+	/* abi_version >= 6, optional (NULL: the frontend reads plane 0 whole and
+	 * de-swizzles it on the host).  LOCAL->HOST read-out of the source
+	 * rectangle desc names (BITBLTBUF SBP/SBW/SPSM, TRXPOS SSAX/SSAY, TRXREG),
+	 * as vram_readback packs it (gs/gs_util.hpp:50-110): pixels in row order,
+	 * 4, 3, 2 or 1 bytes each for the 32-, 24-, 16- and 8-bit formats, the
+	 * 4-bit formats unsupported (nothing written).  Reads plane 0 behind all
+	 * submitted work and returns when dst (dst_size bytes, at least the
+	 * rectangle's) holds the result. */
+	int (*readback_rect)(void *self, const pgs_copy_desc *desc, void *dst, uint64_t dst_size);
 } pgs_backend_ops;
 
 /* TimestampType (gs/gs_renderer.hpp:67-79). */

@@ -3256,7 +3256,7 @@ static int o_vsync(void *self, const pgs_merge_params *mp, void *dst)
 
 static const pgs_backend_ops ORACLE_OPS = {
 	PGS_ABI_VERSION, o_destroy, o_reserve, o_flush_rendering, o_copy, o_palette, o_set_ss, o_submit, o_read, o_write, o_error,
-	nullptr, nullptr, o_circuit, o_vsync, nullptr, o_snapshot,
+	nullptr, nullptr, o_circuit, o_vsync, nullptr, o_snapshot, nullptr,
 };
 
 extern "C" {

@@ -269,6 +269,8 @@ struct CudaBackend
 	uint32_t *d_texels = nullptr;
 	size_t texels_cap = 0;
 	uint32_t *d_circuit = nullptr;
+	uint8_t *d_readback = nullptr;
+	uint64_t readback_cap = 0;
 	uint8_t *d_zcache = nullptr; // depth snapshot for aliased frame / depth buffers
 	size_t zcache_cap = 0;
 	// vsync: circuit read-outs, merged image, output and the last four
@@ -286,6 +288,7 @@ struct CudaBackend
 	// Recording.
 	bool recording = false;
 	std::vector<Op> ops;
+	std::vector<uint64_t> batch_blocks;
 	uint8_t *d_reset_vram = nullptr;
 	uint16_t *d_reset_clut = nullptr;
 	uint32_t reset_planes = 0;
@@ -484,6 +487,7 @@ struct CudaBackend
 		cudaFree(d_flags);
 		cudaFree(d_texels);
 		cudaFree(d_circuit);
+		cudaFree(d_readback);
 		cudaFree(d_zcache);
 		cudaFree(d_phase_lut);
 		for (DevImage *im : { &vs_circuit[0], &vs_circuit[1], &vs_merged, &vs_out, &vs_fields[0], &vs_fields[1],
@@ -1114,6 +1118,112 @@ struct CudaBackend
 		return PGS_ERROR_INVALID_ARGUMENT;
 	}
 
+	// VRAM blocks (256 bytes) a host->local upload can write, one entry per
+	// block-sized cell of its rectangle (a cell is one block whatever the
+	// swizzle); false when the rectangle wraps the 2048 x 2048 address space.
+	static bool upload_blocks(const CopyParams &c, std::vector<uint32_t> &out)
+	{
+		out.clear();
+		if (c.dsax + c.width > 2048u || c.dsay + c.height > 2048u || c.width == 0 || c.height == 0)
+			return false;
+		const Layout L = psm_layout(c.dpsm);
+		const uint32_t x1 = c.dsax + c.width - 1u, y1 = c.dsay + c.height - 1u;
+		for (uint32_t cy = c.dsay >> L.bh; cy <= y1 >> L.bh; cy++)
+			for (uint32_t cx = c.dsax >> L.bw; cx <= x1 >> L.bw; cx++)
+			{
+				const uint32_t x = std::max(cx << L.bw, c.dsax), y = std::max(cy << L.bh, c.dsay);
+				const uint32_t a = swizzle_address(x, y, c.dbp, c.dbw, c.dpsm);
+				const uint32_t byte = c.dpsm == PSMT4 ? a >> 1 : c.dpsm == PSMT8 ? a : psm_is_16bit(c.dpsm) ? a * 2u : a * 4u;
+				out.push_back((byte >> 8) & (VRAM_SIZE / 256u - 1u));
+			}
+		return true;
+	}
+
+	// Blocks of each host->local upload of `ops`, by op index (filled on first use).
+	std::vector<std::vector<uint32_t>> op_blocks;
+	std::vector<uint8_t> op_blocks_state; // 0 unknown, 1 known, 2 not batchable
+
+	// Runs list[i] and advances i.  Consecutive host->local uploads whose
+	// destination pages do not overlap, and chains of CLUT loads, go in one
+	// launch each (replays; the recording run executes one op at a time).
+	int execute_from(const std::vector<Op> &list, size_t &i)
+	{
+		const Op &first = list[i];
+		if (first.type == OP_COPY && first.copy.xdir == HOST_TO_LOCAL)
+		{
+			UploadBatch B;
+			B.count = 0;
+			uint32_t blocks = 0;
+			size_t j = i;
+			if (op_blocks.size() != list.size())
+			{
+				op_blocks.assign(list.size(), {});
+				op_blocks_state.assign(list.size(), 0);
+			}
+			std::vector<uint64_t> &used = batch_blocks;
+			used.assign(VRAM_SIZE / 256u / 64u, 0);
+			while (j < list.size() && B.count < UPLOAD_BATCH_MAX && list[j].type == OP_COPY &&
+			       list[j].copy.xdir == HOST_TO_LOCAL)
+			{
+				if (!op_blocks_state[j])
+					op_blocks_state[j] = upload_blocks(list[j].copy, op_blocks[j]) ? 1 : 2;
+				if (op_blocks_state[j] != 1)
+					break;
+				bool overlap = false;
+				for (uint32_t b : op_blocks[j])
+					overlap = overlap || ((used[b >> 6] >> (b & 63u)) & 1u);
+				if (overlap)
+					break;
+				for (uint32_t b : op_blocks[j])
+					used[b >> 6] |= 1ull << (b & 63u);
+				CopyParams c = list[j].copy;
+				c.host = d_arena + list[j].copy_host_off;
+				B.c[B.count] = c;
+				B.block_start[B.count] = blocks;
+				blocks += ((c.width + 31u) / 32u) * ((c.height + 7u) / 8u);
+				B.count++;
+				j++;
+			}
+			if (B.count >= 2)
+			{
+				B.block_start[B.count] = blocks;
+				StageScope ts(this, PGS_TIMESTAMP_COPY_VRAM);
+				upload_batch_kernel<<<blocks, 256, 0, stream>>>(B, d_vram);
+				launch_counter++;
+				CUDA_TRY(cudaGetLastError());
+				i = j;
+				return PGS_OK;
+			}
+		}
+		else if (first.type == OP_CLUT && first.clut.instance != first.clut.base_instance)
+		{
+			ClutBatch B;
+			B.count = 0;
+			size_t j = i;
+			while (j < list.size() && B.count < CLUT_BATCH_MAX && list[j].type == OP_CLUT)
+			{
+				const ClutParams &c = list[j].clut;
+				bool ok = !B.count || (c.base_instance == B.c[B.count - 1].instance && c.instance != B.c[0].base_instance);
+				for (uint32_t k = 0; ok && k < B.count; k++)
+					ok = c.instance != B.c[k].instance;
+				if (!ok)
+					break;
+				B.c[B.count++] = c;
+				j++;
+			}
+			if (B.count >= 2)
+			{
+				StageScope ts(this, PGS_TIMESTAMP_PALETTE_UPDATE);
+				clut_batch_kernel<<<B.count, 256, 0, stream>>>(B, d_vram, d_clut);
+				launch_counter++;
+				CUDA_TRY(cudaGetLastError());
+				i = j;
+				return PGS_OK;
+			}
+		}
+		return execute(list[i++]);
+	}
+
 	// One bin + shade dispatch: primitives [lo, lo + count) of instance `inst`.
 	// `cached_depth`: depth is read from a snapshot of VRAM taken just before
 	// the dispatch (frame and depth buffer share memory; see alias_split).
@@ -1607,6 +1717,52 @@ struct CudaBackend
 		return PGS_OK;
 	}
 
+	// LOCAL->HOST read-out of a source rectangle, de-swizzled on the device:
+	// only the rectangle's bytes cross to the host.
+	int readback_rect(const pgs_copy_desc &d, void *dst, uint64_t dst_size)
+	{
+		ReadbackParams R = {};
+		R.sbp = field(d.bitbltbuf, 0, 14);
+		R.sbw = field(d.bitbltbuf, 16, 6);
+		R.spsm = field(d.bitbltbuf, 24, 6);
+		R.ssax = field(d.trxpos, 0, 11);
+		R.ssay = field(d.trxpos, 16, 11);
+		R.width = field(d.trxreg, 0, 12);
+		R.height = field(d.trxreg, 32, 12);
+		switch (R.spsm)
+		{
+		case PSMCT32: case PSMZ32: R.bytes_per_pixel = 4; break;
+		case PSMCT24: case PSMZ24: R.bytes_per_pixel = 3; break;
+		case PSMCT16: case PSMCT16S: case PSMZ16: case PSMZ16S: R.bytes_per_pixel = 2; break;
+		case PSMT8: case PSMT8H: R.bytes_per_pixel = 1; break;
+		default: return PGS_OK; // 4-bit formats: nothing to read out
+		}
+		R.size = uint64_t(R.width) * R.height * R.bytes_per_pixel;
+		if (R.size == 0)
+			return PGS_OK;
+		if (!dst || dst_size < R.size)
+			return PGS_ERROR_INVALID_ARGUMENT;
+		if (R.size > readback_cap)
+		{
+			cudaFree(d_readback);
+			d_readback = nullptr;
+			readback_cap = 0;
+			CUDA_TRY(cudaMalloc(&d_readback, R.size));
+			readback_cap = R.size;
+		}
+		{
+			StageScope ts(this, PGS_TIMESTAMP_READBACK);
+			const uint64_t threads = (R.size + 15u) / 16u;
+			readback_kernel<<<uint32_t((threads + 255u) / 256u), 256, 0, stream>>>(R, d_vram, d_readback);
+			launch_counter++;
+			CUDA_TRY(cudaGetLastError());
+			CUDA_TRY(cudaMemcpyAsync(dst, d_readback, R.size, cudaMemcpyDeviceToHost, stream));
+		}
+		CUDA_TRY(cudaStreamSynchronize(stream));
+		d2h_bytes += R.size;
+		return PGS_OK;
+	}
+
 	static int ensure_image(DevImage &im, size_t pixels)
 	{
 		if (pixels * 4 <= im.cap)
@@ -1778,6 +1934,8 @@ struct CudaBackend
 			graph_exec = nullptr;
 		}
 		ops.clear();
+		op_blocks.clear();
+		op_blocks_state.clear();
 		arena_used = 0;
 		size_t vbytes = size_t(num_planes) * VRAM_SIZE;
 		cudaFree(d_reset_vram);
@@ -1811,9 +1969,9 @@ struct CudaBackend
 			CUDA_TRY(cudaMemcpyAsync(d_clut, d_reset_clut, size_t(PGS_CLUT_INSTANCES) * PGS_CLUT_SIZE_BYTES,
 			                         cudaMemcpyDeviceToDevice, stream));
 		}
-		for (const Op &op : ops)
+		for (size_t i = 0; i < ops.size();)
 		{
-			int r = execute(op);
+			int r = execute_from(ops, i);
 			if (r)
 				return r;
 		}
@@ -2034,9 +2192,9 @@ struct BatchEngine
 		{
 			if (!solo[s])
 				continue;
-			for (const Op &op : streams[s]->ops)
+			for (size_t i = 0; i < streams[s]->ops.size();)
 			{
-				r = streams[s]->execute(op);
+				r = streams[s]->execute_from(streams[s]->ops, i);
 				if (r)
 					return r;
 			}
@@ -2057,7 +2215,7 @@ struct BatchEngine
 				c.seg = 0;
 				while (c.op < b->ops.size() && b->ops[c.op].type != OP_PASS)
 				{
-					r = b->execute(b->ops[c.op++]);
+					r = b->execute_from(b->ops, c.op);
 					if (r)
 						return r;
 				}
@@ -2143,7 +2301,7 @@ struct BatchEngine
 		for (size_t s = 0; s < streams.size(); s++)
 			while (cur[s].op < streams[s]->ops.size())
 			{
-				r = streams[s]->execute(streams[s]->ops[cur[s].op++]);
+				r = streams[s]->execute_from(streams[s]->ops, cur[s].op);
 				if (r)
 					return r;
 			}
@@ -2303,10 +2461,14 @@ static int c_vsync(void *self, const pgs_merge_params *m, void *dst)
 }
 static int c_timestamps(void *self, int enable, double *totals) { return B(self)->timestamps(enable, totals); }
 static int c_snapshot(void *self) { return B(self)->snapshot_vram(); }
+static int c_readback(void *self, const pgs_copy_desc *d, void *dst, uint64_t size)
+{
+	return d ? B(self)->readback_rect(*d, dst, size) : PGS_ERROR_INVALID_ARGUMENT;
+}
 
 const pgs_backend_ops CUDA_OPS = {
 	PGS_ABI_VERSION, c_destroy, c_reserve, c_flush_rendering, c_copy, c_palette, c_set_ss, c_submit, c_read, c_write, c_error,
-	c_read_async, c_wait, c_circuit, c_vsync, c_timestamps, c_snapshot,
+	c_read_async, c_wait, c_circuit, c_vsync, c_timestamps, c_snapshot, c_readback,
 };
 
 // ---------------------------------------------------------------------------

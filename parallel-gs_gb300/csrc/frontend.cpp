@@ -947,6 +947,19 @@ struct pgs_gs : TrackerClient
 
 	void readback_to_fifo(uint32_t sbp, uint32_t sbw, uint32_t spsm, uint32_t sx, uint32_t sy, uint32_t w, uint32_t h)
 	{
+		if (ops->abi_version >= 6 && ops->readback_rect)
+		{
+			// The backend de-swizzles the rectangle itself.
+			pgs_copy_desc d = {};
+			d.bitbltbuf = xfer.bitbltbuf;
+			d.trxpos = xfer.trxpos;
+			d.trxreg = xfer.trxreg;
+			d.trxdir = xfer.trxdir;
+			int r = ops->readback_rect(be, &d, xfer.fifo.data(), xfer.fifo.size());
+			if (r != 0)
+				sticky_error = r;
+			return;
+		}
 		std::vector<uint8_t> vram(VRAM_SIZE);
 		int r = ops->read_vram(be, 0, 0, VRAM_SIZE, vram.data());
 		if (r != 0)

@@ -2844,10 +2844,8 @@ __device__ __forceinline__ uint32_t read_pixel(const uint8_t *vram, uint32_t psm
 	return v32[a];
 }
 
-__global__ void __launch_bounds__(256) upload_kernel(CopyParams C, uint8_t *vram)
+__device__ __forceinline__ void upload_pixel(const CopyParams &C, uint8_t *vram, uint32_t x, uint32_t y)
 {
-	uint32_t x = blockIdx.x * 32u + (threadIdx.x & 31u);
-	uint32_t y = blockIdx.y * 8u + (threadIdx.x >> 5);
 	if (x >= C.width || y >= C.height)
 		return;
 	uint32_t eff_stride = C.dbw;
@@ -2885,6 +2883,97 @@ __global__ void __launch_bounds__(256) upload_kernel(CopyParams C, uint8_t *vram
 	write_pixel(vram, C.dpsm, swizzle_address(dx, dy, C.dbp, C.dbw, C.dpsm), data, C.invalidate_ss != 0);
 }
 
+__global__ void __launch_bounds__(256) upload_kernel(CopyParams C, uint8_t *vram)
+{
+	upload_pixel(C, vram, blockIdx.x * 32u + (threadIdx.x & 31u), blockIdx.y * 8u + (threadIdx.x >> 5));
+}
+
+// Consecutive host->local uploads whose destination pages do not overlap, in
+// one launch: the order among them cannot change VRAM.  Blocks of 32 x 8
+// pixels are dealt out to the uploads by block_start.
+constexpr uint32_t UPLOAD_BATCH_MAX = 16;
+struct UploadBatch
+{
+	CopyParams c[UPLOAD_BATCH_MAX];
+	uint32_t block_start[UPLOAD_BATCH_MAX + 1];
+	uint32_t count;
+};
+
+__global__ void __launch_bounds__(256) upload_batch_kernel(UploadBatch B, uint8_t *vram)
+{
+	uint32_t i = 0;
+	while (i + 1u < B.count && blockIdx.x >= B.block_start[i + 1])
+		i++;
+	const CopyParams &C = B.c[i];
+	const uint32_t local = blockIdx.x - B.block_start[i], bw = (C.width + 31u) / 32u;
+	upload_pixel(C, vram, (local % bw) * 32u + (threadIdx.x & 31u), (local / bw) * 8u + (threadIdx.x >> 5));
+}
+
+// LOCAL->HOST read-out of a rectangle of plane 0 into linear bytes
+// (vram_readback, gs/gs_util.hpp:50-110): pixels in row order at their host
+// size (4, 3, 2 or 1 bytes).  Each thread packs 16 consecutive output bytes
+// and writes them as one 16-byte store where the output allows.
+struct ReadbackParams
+{
+	uint32_t sbp, sbw, spsm, ssax, ssay, width, height, bytes_per_pixel;
+	uint64_t size; // output bytes
+};
+
+// Byte k of the pixel at word/halfword/byte address a.
+__device__ __forceinline__ uint32_t readback_fetch(uint32_t spsm, const uint8_t *vram, uint32_t a, uint32_t k)
+{
+	switch (spsm)
+	{
+	case PSMCT16: case PSMCT16S: case PSMZ16: case PSMZ16S: return vram[2u * a + k];
+	case PSMT8: return vram[a];
+	case PSMT8H: return vram[4u * a + 3u];
+	default: return vram[4u * a + k];
+	}
+}
+
+__global__ void __launch_bounds__(256) readback_kernel(ReadbackParams R, const uint8_t *vram, uint8_t *out)
+{
+	const uint64_t first = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) * 16u;
+	if (first >= R.size)
+		return;
+	const uint32_t B = R.bytes_per_pixel;
+	const uint64_t i = first / B;
+	uint32_t k = uint32_t(first - i * B);
+	uint32_t x = uint32_t(i % R.width), y = uint32_t(i / R.width);
+	uint32_t a = swizzle_address((x + R.ssax) & 2047u, (y + R.ssay) & 2047u, R.sbp, R.sbw, R.spsm);
+	auto next = [&]() {
+		const uint32_t v = readback_fetch(R.spsm, vram, a, k);
+		if (++k == B)
+		{
+			k = 0;
+			if (++x == R.width)
+			{
+				x = 0;
+				y++;
+			}
+			a = swizzle_address((x + R.ssax) & 2047u, (y + R.ssay) & 2047u, R.sbp, R.sbw, R.spsm);
+		}
+		return v;
+	};
+	if (first + 16u <= R.size)
+	{
+		uint32_t w[4];
+		#pragma unroll
+		for (int q = 0; q < 4; q++)
+		{
+			uint32_t v = 0;
+			#pragma unroll
+			for (int b = 0; b < 4; b++)
+				v |= next() << (8 * b);
+			w[q] = v;
+		}
+		*reinterpret_cast<uint4 *>(out + first) = make_uint4(w[0], w[1], w[2], w[3]);
+	}
+	else
+		for (uint64_t b = first; b < R.size; b++)
+			out[b] = uint8_t(next());
+}
+
 // ---------------------------------------------------------------------------
 // K6: CLUT load into a new ring instance.
 struct ClutParams
@@ -2895,13 +2984,9 @@ struct ClutParams
 	uint32_t base_instance, instance;
 };
 
-__global__ void __launch_bounds__(256) clut_kernel(ClutParams C, const uint8_t *vram, uint16_t *clut)
+// One CLUT load applied to the 512 entries in tmp (256 threads).
+__device__ __forceinline__ void clut_apply(const ClutParams &C, const uint8_t *vram, uint16_t *tmp, uint32_t lane)
 {
-	__shared__ uint16_t tmp[512];
-	uint32_t lane = threadIdx.x;
-	tmp[lane] = clut[size_t(C.base_instance) * 512u + lane];
-	tmp[lane + 256u] = clut[size_t(C.base_instance) * 512u + lane + 256u];
-	__syncthreads();
 	bool index4 = C.psm == PSMT4 || C.psm == PSMT4HH || C.psm == PSMT4HL;
 	bool active;
 	uint32_t wc = lane + C.csa * 16u, rc = lane;
@@ -2940,8 +3025,59 @@ __global__ void __launch_bounds__(256) clut_kernel(ClutParams C, const uint8_t *
 			if (wc < 512u) tmp[wc] = uint16_t(v);
 		}
 	}
+}
+
+__global__ void __launch_bounds__(256) clut_kernel(ClutParams C, const uint8_t *vram, uint16_t *clut)
+{
+	__shared__ uint16_t tmp[512];
+	uint32_t lane = threadIdx.x;
+	tmp[lane] = clut[size_t(C.base_instance) * 512u + lane];
+	tmp[lane + 256u] = clut[size_t(C.base_instance) * 512u + lane + 256u];
+	__syncthreads();
+	clut_apply(C, vram, tmp, lane);
 	__syncthreads();
 	clut[size_t(C.instance) * 512u + lane] = tmp[lane];
 	clut[size_t(C.instance) * 512u + lane + 256u] = tmp[lane + 256u];
+}
+
+// A chain of consecutive CLUT loads (each one's base is the previous one's
+// instance) in one launch: block k starts from the first load's base and
+// applies loads 0..k, so it writes the instance load k would have written.
+// VRAM does not change between the loads, and no load of the chain writes
+// the first load's base.
+constexpr uint32_t CLUT_BATCH_MAX = 16;
+struct ClutBatch
+{
+	ClutParams c[CLUT_BATCH_MAX];
+	uint32_t count;
+};
+
+__global__ void __launch_bounds__(256) clut_batch_kernel(ClutBatch B, const uint8_t *vram, uint16_t *clut)
+{
+	__shared__ uint16_t tmp[512];
+	const uint32_t lane = threadIdx.x, k = blockIdx.x;
+	// An 8-bit CT32 load at CSA 0 rewrites all 512 entries: start from the
+	// last one at or before k.
+	uint32_t j0 = 0;
+	for (uint32_t j = k + 1u; j-- > 0u;)
+	{
+		const ClutParams &c = B.c[j];
+		if ((c.psm == PSMT8 || c.psm == PSMT8H) && c.csm == 0 && c.cpsm == PSMCT32 && c.csa == 0)
+		{
+			j0 = j;
+			break;
+		}
+	}
+	const uint32_t base = B.c[0].base_instance;
+	tmp[lane] = clut[size_t(base) * 512u + lane];
+	tmp[lane + 256u] = clut[size_t(base) * 512u + lane + 256u];
+	__syncthreads();
+	for (uint32_t j = j0; j <= k; j++)
+	{
+		clut_apply(B.c[j], vram, tmp, lane);
+		__syncthreads();
+	}
+	clut[size_t(B.c[k].instance) * 512u + lane] = tmp[lane];
+	clut[size_t(B.c[k].instance) * 512u + lane + 256u] = tmp[lane + 256u];
 }
 } // namespace pgs

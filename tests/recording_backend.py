@@ -87,7 +87,7 @@ class Ops(C.Structure):
                 ("copy", COPY), ("palette", PALETTE), ("set_ss", SETSS), ("submit", SUBMIT), ("read", READ),
                 ("write", WRITE), ("error", ERROR), ("read_async", C.c_void_p), ("wait_ticket", C.c_void_p),
                 ("sample_circuit", C.c_void_p), ("vsync", VSYNC), ("timestamps", C.c_void_p),
-                ("snapshot_vram", SUBMIT)]
+                ("snapshot_vram", SUBMIT), ("readback_rect", C.c_void_p)]
 
 
 def _struct_array(ptr, n, fields):
@@ -109,7 +109,7 @@ class RecordingBackend(pgs.Backend):
         self._attr = (VertexAttribute * (3 * MAXP))()
         self._prim = (PrimitiveAttribute * MAXP)()
         self.vsyncs = 0
-        self._cbs = Ops(5, DESTROY(lambda s: None), RESERVE(self._reserve), FLUSH(self._flush), COPY(self._copy),
+        self._cbs = Ops(6, DESTROY(lambda s: None), RESERVE(self._reserve), FLUSH(self._flush), COPY(self._copy),
                         PALETTE(self._palette), SETSS(self._set_ss), SUBMIT(lambda s: 0), READ(self._read),
                         WRITE(self._write), ERROR(self._error), None, None, None, VSYNC(self._vsync), None,
                         SUBMIT(self._snapshot))

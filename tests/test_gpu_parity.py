@@ -87,6 +87,41 @@ def test_record_replay_reproduces_frame():
     assert np.array_equal(first, graph)
 
 
+REPLAY_STREAMS = {
+    "c2_8_textures": lambda: gsgen.frame_c2(seed=4, num_triangles=2000, num_sprites=100, num_textures=8),
+    "c3_psmt4": lambda: gsgen.stream_c3(3, num_primitives=3000),
+    "c3_ct16": lambda: gsgen.stream_c3(6, num_primitives=3000),
+    "hazards": lambda: gsgen.frame_hazards(2),
+    "fuzz": lambda: gsgen.frame_fuzz(5),
+}
+
+
+@pytest.mark.parametrize("name", sorted(REPLAY_STREAMS))
+def test_replay_batches_uploads_and_clut_loads(name):
+    """Replays launch consecutive host->local uploads with disjoint pages, and
+    chains of CLUT loads, as one kernel each; every plane must still equal the
+    recorded run, which executed them one at a time."""
+    f = REPLAY_STREAMS[name]()
+    be = pgs.CudaBackend(0, max_samples_log2=4)
+    try:
+        gs = pgs.GSInterface(be, super_sampling=f.super_sampling, ordered=f.ordered)
+        be.begin_record()
+        gs.gif_transfer(0, f.data)
+        gs.flush()
+        be.end_record()
+        planes = 2 + f.super_sampling if f.super_sampling > 1 else 1
+        first = np.stack([be.read_plane(p) for p in range(planes)])
+        be.replay(1, reset_vram=True, use_graph=False)
+        again = np.stack([be.read_plane(p) for p in range(planes)])
+        be.replay(2, reset_vram=True, use_graph=True)
+        graph = np.stack([be.read_plane(p) for p in range(planes)])
+        gs.close()
+    finally:
+        be.close()
+    assert np.array_equal(first, again)
+    assert np.array_equal(first, graph)
+
+
 @pytest.mark.parametrize("ss,ordered", [(2, True), (4, False), (8, False), (16, True), (16, False)])
 def test_c2_small_sampling_rates(ss, ordered):
     """Every sampling grid the frontend offers: 2x, 4x sparse, 8x (2x4), 16x ordered and sparse."""
