@@ -195,10 +195,10 @@ def algorithmic_bytes(frame, ss: int) -> dict:
     planes = 1 if ss == 1 else 2 + ss
     passes = frame.meta.get("passes", 1)
     fbz = passes * (2 * (4 + 4) * px * (planes - 1 if ss > 1 else 1) + (2 * 8 * px if ss > 1 else 0))
-    setup_rw = (80 + 64 + 32) * p * 2
+    setup_rw = (80 + 96 + 32) * p * 2
     records = 152 * p
     textures = frame.meta.get("texture_bytes", 0)
-    shade = fbz + (80 + 64 + 32) * p + textures
+    shade = fbz + (80 + 96 + 32) * p + textures
     return {"frame": records + setup_rw + fbz + textures + 4 * 1024 * 1024, "shade": shade}
 
 

@@ -525,8 +525,8 @@ int pgs_upscaler_synchronize(void *upscaler);
 /* Allocation-free local->local VRAM copy                               */
 /* ------------------------------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device
- * memory — code running under a memory-capture or pool-restricted allocator,
- * inside another framework's arena, or with a hard no-cudaMalloc rule on a
+ * memory — code running under a pool-restricted allocator, inside another
+ * framework's arena, or with a hard no-cudaMalloc rule on a
  * latency-critical path — this performs the LOCAL_TO_LOCAL transfer described
  * by desc (BITBLTBUF/TRXPOS/TRXREG, XDIR = 2) on a caller-owned VRAM image
  * without allocating anything.  vram points to num_planes consecutive 4 MiB
