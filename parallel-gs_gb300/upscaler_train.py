@@ -45,6 +45,7 @@ class PairRenderer:
     both framebuffers out as RGBA8 into device tensors."""
 
     def __init__(self, device: int = 0) -> None:
+        self.b1_device = device
         self.b1 = pgs.CudaBackend(device, max_samples_log2=0, arena_mib=32)
         self.b16 = pgs.CudaBackend(device, max_samples_log2=4, arena_mib=32)
         self.g1 = pgs.GSInterface(self.b1, super_sampling=1)
@@ -61,6 +62,20 @@ class PairRenderer:
             be.sample_circuit(out.data_ptr(), frame.meta["fbp"], WIDTH // 64, gsgen.PSMCT32, WIDTH, HEIGHT)
         self.b1_sync()
 
+    def render_rate(self, frame: gsgen.Frame, out, ss: int) -> None:
+        """The scene at `ss`x SSAA (ordered grid), read out like the target."""
+        if not hasattr(self, "rates"):
+            self.rates = {}
+        if ss not in self.rates:
+            be = pgs.CudaBackend(self.b1_device, max_samples_log2={2: 1, 4: 2, 8: 3, 16: 4}[ss], arena_mib=32)
+            self.rates[ss] = (be, pgs.GSInterface(be, super_sampling=ss, ordered=True))
+        be, gs = self.rates[ss]
+        gs.write_vram(self.zeros)
+        gs.gif_transfer(0, frame.data)
+        gs.flush()
+        be.sample_circuit(out.data_ptr(), frame.meta["fbp"], WIDTH // 64, gsgen.PSMCT32, WIDTH, HEIGHT)
+        self.b1_sync()
+
     def b1_sync(self) -> None:
         import torch
         torch.cuda.synchronize()
@@ -68,6 +83,9 @@ class PairRenderer:
     def close(self) -> None:
         self.g1.close()
         self.g16.close()
+        for be, gs in getattr(self, "rates", {}).values():
+            gs.close()
+            be.close()
         self.b1.close()
         self.b16.close()
 
@@ -86,21 +104,38 @@ def build_dataset(renderer: PairRenderer, seeds, log=None):
 
 
 def train(up: pgs.Upscaler, inp, tgt, steps: int, batch: int = 16, crop: int = 128, lr: float = 1e-3,
-          seed: int = 0, log=None) -> list[float]:
+          seed: int = 0, log=None, eval_every: int = 0, eval_set=None, curve=None) -> list[float]:
+    """Adam on random crops with a cosine learning rate.  With eval_every, the
+    held-out PSNR of eval_set (inputs, targets) is logged into `curve` every
+    eval_every steps, next to the mean training loss since the last point."""
     import torch
     g = torch.Generator(device="cpu").manual_seed(seed)
     stream = torch.cuda.ExternalStream(up.stream())
     losses = []
+    window = []
     n = inp.shape[0]
     with torch.cuda.stream(stream):
         for step in range(steps):
+            if eval_every and eval_set is not None and step and step % eval_every == 0:
+                up.synchronize()
+                m = evaluate(up, *eval_set)
+                tr = float(np.mean(window)) if window else float("nan")
+                window = []
+                point = {"step": step, "train_loss": tr, "train_psnr_db": psnr(tr * 255.0 ** 2) if tr == tr else None,
+                         "heldout_psnr_db": m["psnr_net_db"]}
+                if curve is not None:
+                    curve.append(point)
+                if log:
+                    log("curve %s" % json.dumps(point))
             idx = torch.randint(0, n, (batch,), generator=g).tolist()
             ys = torch.randint(0, HEIGHT - crop + 1, (batch,), generator=g).tolist()
             xs = torch.randint(0, WIDTH - crop + 1, (batch,), generator=g).tolist()
             bi = torch.stack([inp[i, y:y + crop, x:x + crop] for i, y, x in zip(idx, ys, xs)]).contiguous()
             bt = torch.stack([tgt[i, y:y + crop, x:x + crop] for i, y, x in zip(idx, ys, xs)]).contiguous()
-            want = (step % 200 == 0) or step == steps - 1
+            want = (step % 200 == 0) or step == steps - 1 or bool(eval_every and step % 50 == 0)
             loss = up.backward(bi, bt, want_loss=want)
+            if want:
+                window.append(loss)
             cur = lr * (0.02 + 0.98 * 0.5 * (1.0 + math.cos(math.pi * step / steps)))
             up.adam_step(cur)
             if want:
@@ -153,6 +188,10 @@ def main() -> None:
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default="upscaler_out")
+    ap.add_argument("--eval-every", type=int, default=0, help="log held-out PSNR every this many steps")
+    ap.add_argument("--curve-scenes", type=int, default=100, help="held-out scenes used for the curve")
+    ap.add_argument("--ceilings", action="store_true",
+                    help="also report 2x, 4x and 8x SSAA against the 16x targets on the held-out scenes")
     ap.add_argument("--tensor-path", type=int, default=2,
                     help="32->32 layers: 0 mma.sync, 1 or 2 tcgen05 with that many persistent CTAs per SM")
     args = ap.parse_args()
@@ -172,6 +211,20 @@ def main() -> None:
     tr_in, tr_tgt = build_dataset(r, range(TRAIN_SEED0, TRAIN_SEED0 + args.train), log)
     ev_in, ev_tgt = build_dataset(r, range(EVAL_SEED0, EVAL_SEED0 + args.eval), log)
     t_data = time.perf_counter() - t0
+    ceilings = {}
+    if args.ceilings:
+        # What more samples per pixel recover, on the same held-out scenes: the
+        # 1x input is one sample of what the 16x target averages.
+        for ss in (2, 4, 8):
+            se, count = 0.0, 0
+            img = torch.empty((HEIGHT, WIDTH, 4), dtype=torch.uint8, device="cuda")
+            for i, sd in enumerate(range(EVAL_SEED0, EVAL_SEED0 + args.eval)):
+                r.render_rate(scene(sd), img, ss)
+                d = img[..., :3].float() - ev_tgt[i, ..., :3].float()
+                se += float((d * d).sum())
+                count += HEIGHT * WIDTH * 3
+            ceilings["ssaa%dx_psnr_db" % ss] = psnr(se / count)
+            log("%dx SSAA against 16x on %d held-out scenes: %.2f dB" % (ss, args.eval, ceilings["ssaa%dx_psnr_db" % ss]))
     r.close()
     up = pgs.Upscaler(0)
     up.set_tensor_path(args.tensor_path)
@@ -179,11 +232,15 @@ def main() -> None:
     before = evaluate(up, ev_in[:64], ev_tgt[:64])
     log("before training: %s" % json.dumps(before))
     t1 = time.perf_counter()
-    losses = train(up, tr_in, tr_tgt, args.steps, args.batch, lr=args.lr, log=log)
+    curve = []
+    k = min(args.curve_scenes, args.eval)
+    losses = train(up, tr_in, tr_tgt, args.steps, args.batch, lr=args.lr, log=log, eval_every=args.eval_every,
+                   eval_set=(ev_in[:k], ev_tgt[:k]), curve=curve)
     t_train = time.perf_counter() - t1
     metrics = evaluate(up, ev_in, ev_tgt)
     metrics.update({"train_scenes": args.train, "eval_scenes": args.eval, "steps": args.steps, "batch": args.batch,
                     "crop": 128, "dataset_seconds": t_data, "train_seconds": t_train, "losses": losses,
+                    "curve": curve, "curve_scenes": k, "lr": args.lr, **ceilings,
                     "scene": "frame_c2 style, 12500 triangles + 500 sprites, 640x448, input 1x, target 16x SSAA 4x4"})
     log("held-out: %s" % json.dumps({k: v for k, v in metrics.items() if k != "losses"}))
     np.save(out / "weights.npy", up.params())
