@@ -941,64 +941,121 @@ __device__ __forceinline__ bool intersects_tile(const PrimSetup &s, int32_t lo0,
 __global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, uint32_t *sub_masks,
                                                   uint32_t *sub_summary, uint32_t *tile_flags)
 {
-	uint32_t local = blockIdx.x * blockDim.x + threadIdx.x;
-	if (local >= I.prim_count)
-		return;
-	uint32_t p = I.prim_lo + local;
-	pgs_primitive_attribute pa = P.prims[p];
-	if (((pa.state >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u) != I.instance)
-		return;
-	const PrimSetup s = P.setup[p];
-	if (s.bb[2] < s.bb[0] || s.bb[3] < s.bb[1])
-		return;
+	const unsigned full = 0xffffffffu;
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t local = blockIdx.x * blockDim.x + threadIdx.x;
+	const uint32_t p = I.prim_lo + local;
+	bool live = local < I.prim_count;
+	pgs_primitive_attribute pa = {};
+	PrimSetup s = {};
+	if (live)
+	{
+		pa = P.prims[p];
+		live = ((pa.state >> STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET) & 7u) == I.instance;
+	}
+	if (live)
+	{
+		s = P.setup[p];
+		live = !(s.bb[2] < s.bb[0] || s.bb[3] < s.bb[1]);
+	}
 
 	const int ts = int(P.tile_size_log2);
-	int32_t tx0 = max((s.bb[0] - I.base_x) >> ts, 0), ty0 = max((s.bb[1] - I.base_y) >> ts, 0);
-	int32_t tx1 = min((s.bb[2] - I.base_x) >> ts, int32_t(I.tiles_w) - 1);
-	int32_t ty1 = min((s.bb[3] - I.base_y) >> ts, int32_t(I.tiles_h) - 1);
-
-	bool ms_tri = ((pa.state >> STATE_BIT_MULTISAMPLE) & 1) && !((pa.state >> STATE_BIT_LINE) & 1);
-	uint32_t flags = TILE_NONEMPTY;
-	if (I.rate_y_log2 != 0)
+	const bool ms_tri = ((pa.state >> STATE_BIT_MULTISAMPLE) & 1) && !((pa.state >> STATE_BIT_LINE) & 1);
+	// Coarse tiles: membership and super-sampling flags, one primitive per thread.
+	if (live)
 	{
-		const uint32_t full_mask = (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_Z_TEST) | (1u << STATE_BIT_OPAQUE);
-		const uint32_t color_mask = (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_OPAQUE);
-		if ((pa.state & full_mask) != color_mask) flags |= TILE_REQ_SS_ZW;
-		if ((pa.state & color_mask) != color_mask) flags |= TILE_REQ_SS;
-		if (pa.state & (1u << STATE_BIT_Z_WRITE)) flags |= TILE_HAS_ZW;
-		if (pa.tex & TEX_PER_SAMPLE_BIT) flags |= TILE_REQ_SS;
-	}
-	const uint32_t word = local >> 5, bit = 1u << (local & 31u);
-	const uint32_t sword = word >> 5, sbit = 1u << (word & 31u);
-	for (int32_t ty = ty0; ty <= ty1; ty++)
-	{
-		for (int32_t tx = tx0; tx <= tx1; tx++)
+		int32_t tx0 = max((s.bb[0] - I.base_x) >> ts, 0), ty0 = max((s.bb[1] - I.base_y) >> ts, 0);
+		int32_t tx1 = min((s.bb[2] - I.base_x) >> ts, int32_t(I.tiles_w) - 1);
+		int32_t ty1 = min((s.bb[3] - I.base_y) >> ts, int32_t(I.tiles_h) - 1);
+		uint32_t flags = TILE_NONEMPTY;
+		if (I.rate_y_log2 != 0)
 		{
-			int32_t lo0 = I.base_x + (tx << ts), lo1 = I.base_y + (ty << ts);
-			int32_t hi0 = lo0 + (1 << ts) - 1, hi1 = lo1 + (1 << ts) - 1;
-			if (!intersects_tile(s, lo0, lo1, hi0, hi1, ms_tri))
-				continue;
-			uint32_t tile = uint32_t(ty) * I.tiles_w + uint32_t(tx);
-			atomicOr(&tile_flags[tile], flags);
-			if (I.blend_demote)
-				atomicAdd(&tile_flags[tile], 1u << TILE_COUNT_SHIFT);
-
-			int32_t gx0 = (max(s.bb[0], lo0) - I.base_x) >> 3, gx1 = (min(s.bb[2], hi0) - I.base_x) >> 3;
-			int32_t gy0 = (max(s.bb[1], lo1) - I.base_y) >> 3, gy1 = (min(s.bb[3], hi1) - I.base_y) >> 3;
-			for (int32_t gy = gy0; gy <= gy1; gy++)
-			{
-				for (int32_t gx = gx0; gx <= gx1; gx++)
-				{
-					int32_t sx = I.base_x + (gx << 3), sy = I.base_y + (gy << 3);
-					if (!intersects_tile(s, sx, sy, sx + 7, sy + 7, ms_tri))
-						continue;
-					// Results unused: both compile to fire-and-forget reductions.
-					size_t sub = size_t(gy) * I.sub_w + size_t(gx);
-					atomicOr(&sub_masks[sub * I.mask_words + word], bit);
-					atomicOr(&sub_summary[sub * I.summary_words + sword], sbit);
-				}
-			}
+			const uint32_t full_mask = (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_Z_TEST) | (1u << STATE_BIT_OPAQUE);
+			const uint32_t color_mask = (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_OPAQUE);
+			if ((pa.state & full_mask) != color_mask) flags |= TILE_REQ_SS_ZW;
+			if ((pa.state & color_mask) != color_mask) flags |= TILE_REQ_SS;
+			if (pa.state & (1u << STATE_BIT_Z_WRITE)) flags |= TILE_HAS_ZW;
+			if (pa.tex & TEX_PER_SAMPLE_BIT) flags |= TILE_REQ_SS;
 		}
+		for (int32_t ty = ty0; ty <= ty1; ty++)
+			for (int32_t tx = tx0; tx <= tx1; tx++)
+			{
+				int32_t lo0 = I.base_x + (tx << ts), lo1 = I.base_y + (ty << ts);
+				if (!intersects_tile(s, lo0, lo1, lo0 + (1 << ts) - 1, lo1 + (1 << ts) - 1, ms_tri))
+					continue;
+				uint32_t tile = uint32_t(ty) * I.tiles_w + uint32_t(tx);
+				atomicOr(&tile_flags[tile], flags);
+				if (I.blend_demote)
+					atomicAdd(&tile_flags[tile], 1u << TILE_COUNT_SHIFT);
+			}
+	}
+
+	// 8x8 sub-tiles: the warp's (primitive, sub-tile) candidates are dealt out
+	// to its lanes 32 at a time, so one large primitive does not hold the warp.
+	// A sub-tile that passes the test lies in a coarse tile that passes it
+	// (the test is monotonic in the rectangle), so testing the sub-tiles of the
+	// primitive's box inside the instance is the same as testing those of its
+	// member coarse tiles.
+	int32_t gx0 = 0, gy0 = 0, gw = 0, gh = 0;
+	if (live)
+	{
+		const int32_t xmax = I.base_x + int32_t(I.tiles_w << ts) - 1, ymax = I.base_y + int32_t(I.tiles_h << ts) - 1;
+		const int32_t x0 = max(s.bb[0], I.base_x), y0 = max(s.bb[1], I.base_y);
+		const int32_t x1 = min(s.bb[2], xmax), y1 = min(s.bb[3], ymax);
+		if (x1 >= x0 && y1 >= y0)
+		{
+			gx0 = (x0 - I.base_x) >> 3;
+			gy0 = (y0 - I.base_y) >> 3;
+			gw = ((x1 - I.base_x) >> 3) - gx0 + 1;
+			gh = ((y1 - I.base_y) >> 3) - gy0 + 1;
+		}
+	}
+	const uint32_t count = uint32_t(gw * gh);
+	uint32_t incl = count;
+	#pragma unroll
+	for (int o = 1; o < 32; o <<= 1)
+	{
+		const uint32_t y = __shfl_up_sync(full, incl, o);
+		if (lane >= uint32_t(o))
+			incl += y;
+	}
+	const uint32_t total = __shfl_sync(full, incl, 31);
+	const uint32_t warp_first = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+	for (uint32_t base = 0; base < total; base += 32u)
+	{
+		const uint32_t j = base + lane;
+		// Owner: the first lane whose inclusive count exceeds j.
+		uint32_t lo = 0, hi = 31;
+		#pragma unroll
+		for (int it = 0; it < 5; it++)
+		{
+			const uint32_t mid = (lo + hi) >> 1;
+			const uint32_t v = __shfl_sync(full, incl, int(mid));
+			if (v > j)
+				hi = mid;
+			else
+				lo = mid + 1u;
+		}
+		const uint32_t o = lo;
+		const uint32_t o_incl = __shfl_sync(full, incl, int(o)), o_count = __shfl_sync(full, count, int(o));
+		const int32_t o_gx0 = __shfl_sync(full, gx0, int(o)), o_gy0 = __shfl_sync(full, gy0, int(o));
+		const int32_t o_gw = __shfl_sync(full, gw, int(o));
+		const bool o_ms = __shfl_sync(full, ms_tri ? 1 : 0, int(o)) != 0;
+		if (j >= total)
+			continue;
+		const uint32_t k = j - (o_incl - o_count);
+		const int32_t gx = o_gx0 + int32_t(k % uint32_t(o_gw)), gy = o_gy0 + int32_t(k / uint32_t(o_gw));
+		const uint32_t o_local = warp_first + o;
+		const PrimSetup &os = P.setup[I.prim_lo + o_local];
+		const int32_t sx = I.base_x + (gx << 3), sy = I.base_y + (gy << 3);
+		if (!intersects_tile(os, sx, sy, sx + 7, sy + 7, o_ms))
+			continue;
+		// Results unused: both compile to fire-and-forget reductions.
+		const uint32_t word = o_local >> 5, bit = 1u << (o_local & 31u);
+		const uint32_t sword = word >> 5, sbit = 1u << (word & 31u);
+		const size_t sub = size_t(gy) * I.sub_w + size_t(gx);
+		atomicOr(&sub_masks[sub * I.mask_words + word], bit);
+		atomicOr(&sub_summary[sub * I.summary_words + sword], sbit);
 	}
 }
 
