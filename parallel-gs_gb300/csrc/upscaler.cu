@@ -636,9 +636,19 @@ constexpr uint32_t SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + W_BYTES + 1024;
 constexpr int THREADS = 160;
 }
 
+// Epilogue outputs of conv32_tc_kernel: EPI_RELU writes out = relu(acc +
+// bias); EPI_MASK (the data gradient of a 32 -> 32 layer through the ReLU
+// before it) writes out = acc where mask > 0, else 0.
+struct TcOut
+{
+	__nv_bfloat16 *out;
+	const __nv_bfloat16 *mask;
+};
+
+template <int EPI>
 __global__ void __launch_bounds__(tc::THREADS, 2) conv32_tc_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                     const __nv_bfloat16 *wt, const float *bias,
-                                                                    __nv_bfloat16 *out, int n, int h, int w, uint32_t *err)
+                                                                    TcOut o, int n, int h, int w, uint32_t *err)
 {
 	using namespace pgs_umma;
 	extern __shared__ uint8_t smem_dyn[];
@@ -661,7 +671,7 @@ __global__ void __launch_bounds__(tc::THREADS, 2) conv32_tc_kernel(const __grid_
 		    *reinterpret_cast<const uint4 *>(wt + (tap * 32u + co) * 32u + ci);
 	}
 	if (tid < 32)
-		s_bias[tid] = bias[tid];
+		s_bias[tid] = EPI == EPI_MASK ? 0.0f : bias[tid];
 	if (warp == 0)
 		tmem_alloc(&tmem_slot, 64);
 	if (tid == 0)
@@ -777,17 +787,43 @@ __global__ void __launch_bounds__(tc::THREADS, 2) conv32_tc_kernel(const __grid_
 			tile_coords(first + i * step, img, x0, y0);
 			const int pix = int(quarter * 32u + lane);
 			const int gy = y0 + pix / tc::COLS, gx = x0 + pix % tc::COLS;
+			const size_t pixel = (size_t(img) * h + gy) * w + gx;
 			if (gx < w && gy < h)
 			{
+				uint32_t m[16];
+				if (EPI == EPI_MASK)
+				{
+					const uint4 *src = reinterpret_cast<const uint4 *>(o.mask + pixel * 32);
+					#pragma unroll
+					for (int q = 0; q < 4; q++)
+					{
+						const uint4 t = src[q];
+						m[4 * q] = t.x;
+						m[4 * q + 1] = t.y;
+						m[4 * q + 2] = t.z;
+						m[4 * q + 3] = t.w;
+					}
+				}
 				uint32_t packed[16];
 				#pragma unroll
 				for (int c = 0; c < 16; c++)
 				{
-					float lo = fmaxf(__uint_as_float(v[2 * c]) + s_bias[2 * c], 0.0f);
-					float hi = fmaxf(__uint_as_float(v[2 * c + 1]) + s_bias[2 * c + 1], 0.0f);
+					float lo, hi;
+					if (EPI == EPI_MASK)
+					{
+						// Data gradient through the ReLU: keep where the layer's output was positive.
+						__nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162 *>(&m[c]);
+						lo = __bfloat162float(mk.x) > 0.0f ? __uint_as_float(v[2 * c]) : 0.0f;
+						hi = __bfloat162float(mk.y) > 0.0f ? __uint_as_float(v[2 * c + 1]) : 0.0f;
+					}
+					else
+					{
+						lo = fmaxf(__uint_as_float(v[2 * c]) + s_bias[2 * c], 0.0f);
+						hi = fmaxf(__uint_as_float(v[2 * c + 1]) + s_bias[2 * c + 1], 0.0f);
+					}
 					packed[c] = pack_bf16x2(lo, hi);
 				}
-				uint4 *dst = reinterpret_cast<uint4 *>(out + ((size_t(img) * h + gy) * w + gx) * 32);
+				uint4 *dst = reinterpret_cast<uint4 *>(o.out + pixel * 32);
 				#pragma unroll
 				for (int q = 0; q < 4; q++)
 					dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
@@ -859,7 +895,7 @@ struct Upscaler
 		int n, h, w;
 		CUtensorMap map;
 	};
-	TmapEntry tmaps[8] = {};
+	TmapEntry tmaps[12] = {};
 	int tmap_count = 0;
 
 	int act_tmap(const void *ptr, int n, int h, int w, CUtensorMap *&out)
@@ -870,7 +906,7 @@ struct Upscaler
 				out = &tmaps[i].map;
 				return PGS_OK;
 			}
-		TmapEntry &e = tmaps[tmap_count < 8 ? tmap_count++ : 7];
+		TmapEntry &e = tmaps[tmap_count < 12 ? tmap_count++ : 11];
 		int r = make_act_tmap(&e.map, ptr, n, h, w);
 		if (r)
 			return r;
@@ -916,7 +952,10 @@ struct Upscaler
 		UP_TRY(cudaMalloc(&d_loss, sizeof(double)));
 		UP_TRY(cudaMalloc(&d_err, sizeof(uint32_t)));
 		UP_TRY(cudaMemset(d_err, 0, sizeof(uint32_t)));
-		UP_TRY(cudaFuncSetAttribute(conv32_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::SMEM_BYTES)));
+		UP_TRY(cudaFuncSetAttribute(conv32_tc_kernel<EPI_RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                            int(tc::SMEM_BYTES)));
+		UP_TRY(cudaFuncSetAttribute(conv32_tc_kernel<EPI_MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                            int(tc::SMEM_BYTES)));
 		return PGS_OK;
 	}
 
@@ -1009,7 +1048,9 @@ struct Upscaler
 		return PGS_OK;
 	}
 
-	// 32 -> 32 + bias + ReLU on tcgen05 (conv32_tc_kernel).
+	// 3x3 convolution of a 32-channel tensor into 32 accumulator channels on
+	// tcgen05 (conv32_tc_kernel) with the given epilogue.
+	template <int EPI>
 	int conv_tc(const ConvArgs &a)
 	{
 		CUtensorMap *m = nullptr;
@@ -1018,7 +1059,8 @@ struct Upscaler
 			return r;
 		int tiles = ((a.w + tc::COLS - 1) / tc::COLS) * ((a.h + tc::ROWS - 1) / tc::ROWS) * a.n;
 		int grid = std::min(tiles, sm_count * use_tc);
-		conv32_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, stream>>>(*m, a.wt, a.bias, a.out, a.n, a.h, a.w, d_err);
+		TcOut o = { a.out, a.mask };
+		conv32_tc_kernel<EPI><<<grid, tc::THREADS, tc::SMEM_BYTES, stream>>>(*m, a.wt, a.bias, o, a.n, a.h, a.w, d_err);
 		UP_TRY(cudaGetLastError());
 		return PGS_OK;
 	}
@@ -1055,15 +1097,18 @@ struct Upscaler
 			if (l < LAYERS - 1)
 			{
 				k.out = d_act[l];
+				// The 4 -> 32 layer stays on mma.sync: on tcgen05 it would be a
+				// 32 -> 32 layer with 28 zero input channels, which measured slower.
 				if (l == 0)
 					r = conv<16, 32, EPI_RELU>(k);
 				else if (use_tc)
-					r = conv_tc(k);
+					r = conv_tc<EPI_RELU>(k);
 				else
 					r = conv<32, 32, EPI_RELU>(k);
 			}
 			else
 			{
+				// 32 -> 4 likewise (N = 32 with 28 zero output channels).
 				k.out = nullptr;
 				k.image = d_img;
 				k.out_f32 = d_out;
@@ -1126,7 +1171,7 @@ struct Upscaler
 			k.wt = bf.dgrad[l];
 			k.mask = d_act[l - 1];
 			k.out = g2;
-			if ((r = conv<32, 32, EPI_MASK>(k)))
+			if ((r = use_tc ? conv_tc<EPI_MASK>(k) : conv<32, 32, EPI_MASK>(k)))
 				return r;
 			std::swap(g, g2);
 		}
