@@ -1093,9 +1093,8 @@ struct CudaBackend
 				CUDA_TRY(cudaMemcpyAsync(d_snapshot, d_vram, VRAM_SIZE, cudaMemcpyDeviceToDevice, stream));
 				c.src_vram = d_snapshot;
 			}
-			dim3 grid((c.width + 31) / 32, (c.height + 7) / 8);
 			StageScope ts(this, PGS_TIMESTAMP_COPY_VRAM);
-			upload_kernel<<<grid, 256, 0, stream>>>(c, d_vram);
+			upload_kernel<<<dim3((c.width + 31) / 32, (c.height + 7) / 8), 256, 0, stream>>>(c, d_vram);
 			launch_counter++;
 			CUDA_TRY(cudaGetLastError());
 			return PGS_OK;

@@ -2925,12 +2925,14 @@ __device__ __forceinline__ void upload_pixel(const CopyParams &C, uint8_t *vram,
 		uint64_t avail = b == 32 ? C.host_size / 4 : (b == 24 ? C.host_size / 3 : (b == 16 ? C.host_size / 2 : (b == 8 ? C.host_size : 2 * C.host_size)));
 		if (sa * factor < C.host_offset_qwords || sa >= avail)
 			return;
+		// The payload starts 256-byte aligned: a warp's 32 consecutive pixels
+		// read one contiguous span, with one load of the pixel's width each.
 		const uint8_t *h = C.host;
 		if (b == 24) data = uint32_t(h[3 * sa]) | (uint32_t(h[3 * sa + 1]) << 8) | (uint32_t(h[3 * sa + 2]) << 16);
-		else if (b == 16) data = uint32_t(h[2 * sa]) | (uint32_t(h[2 * sa + 1]) << 8);
+		else if (b == 16) data = reinterpret_cast<const uint16_t *>(h)[sa];
 		else if (b == 8) data = h[sa];
 		else if (b == 4) data = (uint32_t(h[sa >> 1]) >> ((sa & 1) * 4)) & 15u;
-		else data = uint32_t(h[4 * sa]) | (uint32_t(h[4 * sa + 1]) << 8) | (uint32_t(h[4 * sa + 2]) << 16) | (uint32_t(h[4 * sa + 3]) << 24);
+		else data = reinterpret_cast<const uint32_t *>(h)[sa];
 	}
 	else
 	{
@@ -2945,7 +2947,7 @@ __global__ void __launch_bounds__(256) upload_kernel(CopyParams C, uint8_t *vram
 	upload_pixel(C, vram, blockIdx.x * 32u + (threadIdx.x & 31u), blockIdx.y * 8u + (threadIdx.x >> 5));
 }
 
-// Consecutive host->local uploads whose destination pages do not overlap, in
+// Consecutive host->local uploads whose destination blocks do not overlap, in
 // one launch: the order among them cannot change VRAM.  Blocks of 32 x 8
 // pixels are dealt out to the uploads by block_start.
 constexpr uint32_t UPLOAD_BATCH_MAX = 16;
