@@ -2537,14 +2537,30 @@ struct pgs_gs : TrackerClient
 		}
 
 		bool is_line = !quad && nv == 2;
-		int32_t lo[2] = { std::min(pos[0].x, pos[1].x), std::min(pos[0].y, pos[1].y) };
-		int32_t hi[2] = { std::max(pos[0].x, pos[1].x), std::max(pos[0].y, pos[1].y) };
-		if (!quad && !is_line)
+		// The box from the records as handed in, not from the copies just
+		// stored (reading a field of a 16-byte store right after it can wait
+		// for the store to retire).
+		int32_t lo[2], hi[2];
+		if (nv == 1)
 		{
-			lo[0] = std::min(lo[0], pos[2].x);
-			lo[1] = std::min(lo[1], pos[2].y);
-			hi[0] = std::max(hi[0], pos[2].x);
-			hi[1] = std::max(hi[1], pos[2].y);
+			lo[0] = vp[0].x - ((1 << (SUBPIXEL_BITS - 1)) - 1);
+			lo[1] = vp[0].y - ((1 << (SUBPIXEL_BITS - 1)) - 1);
+			hi[0] = lo[0] + (1 << SUBPIXEL_BITS);
+			hi[1] = lo[1] + (1 << SUBPIXEL_BITS);
+		}
+		else
+		{
+			lo[0] = std::min(vp[0].x, vp[1].x);
+			lo[1] = std::min(vp[0].y, vp[1].y);
+			hi[0] = std::max(vp[0].x, vp[1].x);
+			hi[1] = std::max(vp[0].y, vp[1].y);
+			if (!quad && !is_line)
+			{
+				lo[0] = std::min(lo[0], vp[2].x);
+				lo[1] = std::min(lo[1], vp[2].y);
+				hi[0] = std::max(hi[0], vp[2].x);
+				hi[1] = std::max(hi[1], vp[2].y);
+			}
 		}
 		const int32_t pre_lo[2] = { lo[0], lo[1] }, pre_hi[2] = { hi[0], hi[1] };
 		hi[0] -= 1;
@@ -2580,9 +2596,11 @@ struct pgs_gs : TrackerClient
 		{
 			PrimReg prim(regs[R_PRIM]);
 			uint32_t order[3];
-			para_candidate = parallelogram_candidate(pos, attr, pre_lo, pre_hi, prim, order);
+			// Triangles: pos / attr are still copies of vp / va; the tests read
+			// the records as handed in (see the box above).
+			para_candidate = parallelogram_candidate(vp, va, pre_lo, pre_hi, prim, order);
 			if (dirty == 0 && para_candidate && last_para_candidate && primitive_count &&
-			    forms_parallelogram(pos, attr, order, positions + 3 * (primitive_count - 1),
+			    forms_parallelogram(vp, va, order, positions + 3 * (primitive_count - 1),
 			                        attributes + 3 * (primitive_count - 1), last_para_order, prim))
 			{
 				prims[primitive_count - 1].state |= (1u << STATE_BIT_PARALLELOGRAM) |
@@ -3094,6 +3112,8 @@ struct pgs_gs : TrackerClient
 	};
 	static constexpr size_t RING_CHUNK_BYTES = 64 * 1024, RING_CHUNKS = 16;
 	static constexpr size_t THREADED_DECODE_MIN_QWORDS = 16 * 1024;
+	// How far ahead of the command being run the state side prefetches.
+	static constexpr size_t RING_PREFETCH_BYTES = 1024;
 
 	struct CmdRing
 	{
@@ -3286,6 +3306,9 @@ struct pgs_gs : TrackerClient
 			bool end = false;
 			for (size_t off = 0; off < used;)
 			{
+				// The worker wrote this chunk from another core: fetch ahead so
+				// the vertex records arrive before draw() reads them.
+				__builtin_prefetch(c + off + RING_PREFETCH_BYTES, 0, 3);
 				uint32_t h;
 				memcpy(&h, c + off, 4);
 				switch (h & 0xffu)
