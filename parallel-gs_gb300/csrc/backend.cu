@@ -289,6 +289,7 @@ struct CudaBackend
 	bool recording = false;
 	std::vector<Op> ops;
 	std::vector<uint64_t> batch_blocks;
+	std::vector<uint32_t> scratch_blocks;
 	uint8_t *d_reset_vram = nullptr;
 	uint16_t *d_reset_clut = nullptr;
 	uint32_t reset_planes = 0;
@@ -553,6 +554,9 @@ struct CudaBackend
 		{
 			if (!recording)
 			{
+				int r = flush_deferred();
+				if (r)
+					return r;
 				CUDA_TRY(cudaStreamSynchronize(stream));
 				arena_used = 0;
 			}
@@ -790,9 +794,16 @@ struct CudaBackend
 			if (r)
 				return r;
 			memcpy(h_arena + off, d->host_data, d->host_size);
-			r = upload_arena(off, d->host_size);
-			if (r)
-				return r;
+			// One host->device copy for a run of payloads placed back to back.
+			if (pending_h2d_hi != off)
+			{
+				r = flush_pending_h2d();
+				if (r)
+					return r;
+				pending_h2d_lo = off;
+			}
+			pending_h2d_hi = off + align_up(d->host_size, 256);
+			h2d_bytes += d->host_size;
 			op.copy_host_off = off;
 		}
 		return submit(op);
@@ -903,11 +914,54 @@ struct CudaBackend
 	}
 
 	// ------------------------------------------------------------------
+	// Host->local uploads and CLUT loads wait in `deferred` until the next
+	// operation that is not one of them, or anything else that touches the
+	// stream or reads results (every entry point but copy_vram,
+	// update_palette_cache and reserve_primitive_buffers flushes first), so
+	// that a run of them goes out as one batched launch each, with one
+	// host->device copy of their payloads.
+	static bool deferrable(const Op &op)
+	{
+		return (op.type == OP_COPY && op.copy.xdir == HOST_TO_LOCAL) || op.type == OP_CLUT;
+	}
+
+	std::vector<Op> deferred;
+	size_t pending_h2d_lo = 0, pending_h2d_hi = 0; // arena bytes not yet copied to the device
+	int deferred_status = PGS_OK;
+
+	int flush_pending_h2d()
+	{
+		if (pending_h2d_hi > pending_h2d_lo)
+		{
+			const size_t lo = pending_h2d_lo, size = pending_h2d_hi - pending_h2d_lo;
+			pending_h2d_lo = pending_h2d_hi = 0;
+			CUDA_TRY(cudaMemcpyAsync(d_arena + lo, h_arena + lo, size, cudaMemcpyHostToDevice, stream));
+		}
+		return PGS_OK;
+	}
+
+	int flush_deferred()
+	{
+		int r = flush_pending_h2d();
+		for (size_t i = 0; r == PGS_OK && i < deferred.size();)
+			r = execute_from(deferred, i, nullptr);
+		deferred.clear();
+		if (r && !deferred_status)
+			deferred_status = r;
+		return r;
+	}
+
 	int submit(Op &op)
 	{
 		if (recording)
 			ops.push_back(op);
-		return execute(op);
+		if (deferrable(op))
+		{
+			deferred.push_back(op);
+			return deferred.size() >= 64 ? flush_deferred() : PGS_OK;
+		}
+		int r = flush_deferred();
+		return r ? r : execute(op);
 	}
 
 	int ensure_masks(size_t words, size_t tiles)
@@ -1145,7 +1199,11 @@ struct CudaBackend
 	// Runs list[i] and advances i.  Consecutive host->local uploads whose
 	// destination pages do not overlap, and chains of CLUT loads, go in one
 	// launch each (replays; the recording run executes one op at a time).
-	int execute_from(const std::vector<Op> &list, size_t &i)
+	int execute_from(const std::vector<Op> &list, size_t &i) { return execute_from(list, i, &op_blocks); }
+
+	// blocks_cache: the block lists of `list` by index, kept across calls
+	// (the recorded frame), or NULL to compute them each time.
+	int execute_from(const std::vector<Op> &list, size_t &i, std::vector<std::vector<uint32_t>> *blocks_cache)
 	{
 		const Op &first = list[i];
 		if (first.type == OP_COPY && first.copy.xdir == HOST_TO_LOCAL)
@@ -1154,9 +1212,9 @@ struct CudaBackend
 			B.count = 0;
 			uint32_t blocks = 0;
 			size_t j = i;
-			if (op_blocks.size() != list.size())
+			if (blocks_cache && blocks_cache->size() != list.size())
 			{
-				op_blocks.assign(list.size(), {});
+				blocks_cache->assign(list.size(), {});
 				op_blocks_state.assign(list.size(), 0);
 			}
 			std::vector<uint64_t> &used = batch_blocks;
@@ -1164,16 +1222,23 @@ struct CudaBackend
 			while (j < list.size() && B.count < UPLOAD_BATCH_MAX && list[j].type == OP_COPY &&
 			       list[j].copy.xdir == HOST_TO_LOCAL)
 			{
-				if (!op_blocks_state[j])
-					op_blocks_state[j] = upload_blocks(list[j].copy, op_blocks[j]) ? 1 : 2;
-				if (op_blocks_state[j] != 1)
+				const std::vector<uint32_t> *cells = &scratch_blocks;
+				if (blocks_cache)
+				{
+					if (!op_blocks_state[j])
+						op_blocks_state[j] = upload_blocks(list[j].copy, (*blocks_cache)[j]) ? 1 : 2;
+					if (op_blocks_state[j] != 1)
+						break;
+					cells = &(*blocks_cache)[j];
+				}
+				else if (!upload_blocks(list[j].copy, scratch_blocks))
 					break;
 				bool overlap = false;
-				for (uint32_t b : op_blocks[j])
+				for (uint32_t b : *cells)
 					overlap = overlap || ((used[b >> 6] >> (b & 63u)) & 1u);
 				if (overlap)
 					break;
-				for (uint32_t b : op_blocks[j])
+				for (uint32_t b : *cells)
 					used[b >> 6] |= 1ull << (b & 63u);
 				CopyParams c = list[j].copy;
 				c.host = d_arena + list[j].copy_host_off;
@@ -2414,7 +2479,18 @@ struct BatchEngine
 // pgs_backend_ops table.
 // Every entry point makes the backend's device current for the calling
 // thread: frontends of different streams may run on different host threads.
+// The backend with its device current and its deferred uploads and CLUT
+// loads issued: every entry point that may touch the stream or read results.
 CudaBackend *B(void *s)
+{
+	CudaBackend *b = static_cast<CudaBackend *>(s);
+	cudaSetDevice(b->device);
+	b->flush_deferred();
+	return b;
+}
+
+// Entry points that may leave uploads and CLUT loads deferred.
+CudaBackend *B_defer(void *s)
 {
 	CudaBackend *b = static_cast<CudaBackend *>(s);
 	cudaSetDevice(b->device);
@@ -2429,13 +2505,20 @@ void c_destroy(void *self)
 }
 int c_reserve(void *self, uint32_t n, pgs_vertex_position **p, pgs_vertex_attribute **a, pgs_primitive_attribute **pr)
 {
-	return B(self)->reserve(n, p, a, pr);
+	// Handing out the staging buffers touches neither VRAM nor the stream.
+	return B_defer(self)->reserve(n, p, a, pr);
 }
 int c_flush_rendering(void *self, const pgs_render_pass *rp) { return B(self)->flush_rendering(rp); }
-int c_copy(void *self, const pgs_copy_desc *d) { return d ? B(self)->copy_vram(d) : PGS_ERROR_INVALID_ARGUMENT; }
-int c_palette(void *self, const pgs_palette_upload *u) { return u ? B(self)->update_palette(u) : PGS_ERROR_INVALID_ARGUMENT; }
+int c_copy(void *self, const pgs_copy_desc *d) { return d ? B_defer(self)->copy_vram(d) : PGS_ERROR_INVALID_ARGUMENT; }
+int c_palette(void *self, const pgs_palette_upload *u) { return u ? B_defer(self)->update_palette(u) : PGS_ERROR_INVALID_ARGUMENT; }
 int c_set_ss(void *self, uint32_t x, uint32_t y) { return B(self)->set_super_sampling(x, y); }
-int c_submit(void *self) { return B(self)->flush_submit(); }
+int c_submit(void *self)
+{
+	CudaBackend *b = B(self);
+	const int r = b->deferred_status;
+	b->deferred_status = PGS_OK;
+	return r ? r : b->flush_submit();
+}
 int c_read(void *self, uint32_t plane, uint64_t off, uint64_t size, void *dst)
 {
 	return dst ? B(self)->read_vram(plane, off, size, dst) : PGS_ERROR_INVALID_ARGUMENT;
