@@ -436,17 +436,18 @@ def run_c3(args, frames, rank, world, local):
             gs.gif_transfer(0, frames[i].data)
             gs.wait(gs.read_vram_async(outs[i]))
 
-        st0 = [be.stats() for be in backends]
         with ThreadPoolExecutor(max_workers=min(32, os.cpu_count() or 1)) as pool:
-            list(pool.map(one, range(len(frames))))
+            for _ in range(3):
+                list(pool.map(one, range(len(frames))))
+            st0 = [be.stats() for be in backends]
             t0 = time.perf_counter()
             for _ in range(e2e_steps):
                 list(pool.map(one, range(len(frames))))
             e2e_dt = time.perf_counter() - t0
         st1 = [be.stats() for be in backends]
         e2e_fps = world * len(frames) * e2e_steps / e2e_dt
-        h2d = sum(b["h2d_bytes"] - a["h2d_bytes"] for a, b in zip(st0, st1)) // (e2e_steps + 1)
-        d2h = sum(b["d2h_bytes"] - a["d2h_bytes"] for a, b in zip(st0, st1)) // (e2e_steps + 1)
+        h2d = sum(b["h2d_bytes"] - a["h2d_bytes"] for a, b in zip(st0, st1)) // e2e_steps
+        d2h = sum(b["d2h_bytes"] - a["d2h_bytes"] for a, b in zip(st0, st1)) // e2e_steps
         for gs in ifaces:
             gs.close()
     if batch:
@@ -704,8 +705,9 @@ def measure_frame(frame, local, steps, warmup, e2e_steps, verify=True, pg=None) 
 
         vram = [torch.empty(pgs.VRAM_SIZE, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(2)]
         gs2 = pgs.GSInterface(backend, super_sampling=frame.super_sampling, ordered=frame.ordered)
-        gs2.gif_transfer(0, frame.data)
-        gs2.read_vram(out=vram[0])
+        for _ in range(max(3, warmup)):
+            gs2.gif_transfer(0, frame.data)
+            gs2.read_vram(out=vram[0])
         torch.cuda.synchronize()
         st0 = backend.stats()
         t0 = time.perf_counter()
@@ -1018,7 +1020,7 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         pg = dist
 
-    e2e_steps = 0 if args.quick else max(5, min(args.steps, 20))
+    e2e_steps = 0 if args.quick else max(5, min(2 * args.steps, 40))
     m = measure_frame(frame, local, args.steps, args.warmup, e2e_steps, verify=not args.no_verify and rank == 0,
                       pg=pg)
     total_ms = m["total_ms"]

@@ -142,6 +142,16 @@ struct Tex1Reg
 // NEON on AArch64).
 typedef uint64_t Word2 __attribute__((vector_size(16), aligned(4), may_alias));
 
+// Records ahead of the one being written whose arena lines are prefetched.
+static constexpr uint32_t ARENA_PREFETCH_RECORDS = 12;
+
+// A write prefetch of the line `offset` bytes past `base` (which may lie past
+// the end of the buffer: a prefetch never faults).
+static inline void prefetch_for_write(const void *base, size_t offset)
+{
+	__builtin_prefetch(reinterpret_cast<const void *>(reinterpret_cast<uintptr_t>(base) + offset), 1, 3);
+}
+
 // Vertex copy in the widths the vertex queue writes: the 16-byte position,
 // then the attributes as 16 + 8 bytes.
 static __attribute__((always_inline)) inline void copy_vertex(pgs_vertex_position &dp, pgs_vertex_attribute &da, const pgs_vertex_position &sp,
@@ -2513,27 +2523,32 @@ struct pgs_gs : TrackerClient
 	void append(uint32_t nv, bool quad, const pgs_vertex_position *vp, const pgs_vertex_attribute *va)
 	{
 		const DrawConsts &D = draw_consts();
-		pgs_vertex_position pos[3] = {};
-		pgs_vertex_attribute attr[3] = {};
-
-		if (nv == 1)
+		// Triangles and sprites are read from the records as handed in and
+		// copied once, into the pass (sp / sa point at them).  Points and
+		// lines, whose unused vertices read as zero, and primitives that the
+		// frame-buffer wrap below moves go through the local copies.
+		pgs_vertex_position pos[3];
+		pgs_vertex_attribute attr[3];
+		const pgs_vertex_position *sp = vp;
+		const pgs_vertex_attribute *sa = va;
+		if (nv == 1 || (nv == 2 && !quad))
 		{
+			pos[2] = {};
+			attr[1] = {};
+			attr[2] = {};
 			copy_vertex(pos[0], attr[0], vp[0], va[0]);
-			pos[0].x -= (1 << (SUBPIXEL_BITS - 1)) - 1;
-			pos[0].y -= (1 << (SUBPIXEL_BITS - 1)) - 1;
-			pos[1] = pos[0];
-			pos[1].x += 1 << SUBPIXEL_BITS;
-			pos[1].y += 1 << SUBPIXEL_BITS;
-		}
-		else if (nv == 2)
-		{
-			for (uint32_t i = 0; i < 2; i++)
-				copy_vertex(pos[i], attr[i], vp[i], va[i]);
-		}
-		else
-		{
-			for (uint32_t i = 0; i < 3; i++)
-				copy_vertex(pos[i], attr[i], vp[i], va[i]);
+			if (nv == 1)
+			{
+				pos[0].x -= (1 << (SUBPIXEL_BITS - 1)) - 1;
+				pos[0].y -= (1 << (SUBPIXEL_BITS - 1)) - 1;
+				pos[1] = pos[0];
+				pos[1].x += 1 << SUBPIXEL_BITS;
+				pos[1].y += 1 << SUBPIXEL_BITS;
+			}
+			else
+				copy_vertex(pos[1], attr[1], vp[1], va[1]);
+			sp = pos;
+			sa = attr;
 		}
 
 		bool is_line = !quad && nv == 2;
@@ -2613,16 +2628,17 @@ struct pgs_gs : TrackerClient
 
 		// Texture feedback against the frame / depth buffer
 		// (drawing_kick_append, gs/gs_interface.cpp:2604-2630).
-		update_color_feedback_state();
+		if ((dirty & DIRTY_FEEDBACK) || is_color_feedback || is_depth_feedback)
+			update_color_feedback_state();
 		uint32_t feedback_mode = FEEDBACK_NONE;
 		int32_t uv_bb[4] = {};
 		if (is_color_feedback || is_depth_feedback)
 		{
 			last_para_candidate = para_candidate;
-			feedback_mode = deduce_feedback_mode(pos, attr, nv, quad, uv_bb, bb);
+			feedback_mode = deduce_feedback_mode(sp, sa, nv, quad, uv_bb, bb);
 		}
 		else if (is_potential_feedback || (is_potential_channel_shuffle && quad))
-			compute_uv_bb(attr, quad, false, uv_bb, nullptr, nullptr);
+			compute_uv_bb(sa, quad, false, uv_bb, nullptr, nullptr);
 		current_is_channel_shuffle = false;
 		if (quad && is_potential_channel_shuffle)
 		{
@@ -2657,44 +2673,40 @@ struct pgs_gs : TrackerClient
 			}
 		}
 
-		update_state(feedback_mode, uv_bb, bb);
+		if (dirty & DIRTY_PRIM_TEMPLATE)
+			update_state(feedback_mode, uv_bb, bb);
 
 		auto &inst = instances[current_instance];
-		pgs_primitive_attribute pa = {};
-		pa.tex = tpl_tex;
-		pa.tex2 = tpl_tex2;
-		pa.state = tpl_state;
-		pa.fbmsk = frame.fbmsk;
-		pa.fogcol = D.fogcol;
-		pa.alpha = D.alpha_word;
-
+		const uint32_t tex = tpl_tex, tex2 = tpl_tex2, alpha_word = D.alpha_word, fbmsk = frame.fbmsk,
+		               fogcol = D.fogcol;
+		uint32_t state = tpl_state;
 		if (quad)
 		{
-			pa.state |= (1u << STATE_BIT_PARALLELOGRAM) | (1u << STATE_BIT_SPRITE) |
-			            (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
-			pa.state &= ~(1u << STATE_BIT_MULTISAMPLE);
+			state |= (1u << STATE_BIT_PARALLELOGRAM) | (1u << STATE_BIT_SPRITE) |
+			         (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
+			state &= ~(1u << STATE_BIT_MULTISAMPLE);
 		}
 		else if (is_line)
 		{
-			pa.state |= (1u << STATE_BIT_PARALLELOGRAM) | (1u << STATE_BIT_LINE);
-			if (pa.state & (1u << STATE_BIT_MULTISAMPLE))
-				pa.state &= ~(1u << STATE_BIT_Z_WRITE);
+			state |= (1u << STATE_BIT_PARALLELOGRAM) | (1u << STATE_BIT_LINE);
+			if (state & (1u << STATE_BIT_MULTISAMPLE))
+				state &= ~(1u << STATE_BIT_Z_WRITE);
 		}
 		if (nv == 1)
-			pa.state |= (1u << STATE_BIT_FIX) | (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
-		pa.state |= current_instance << STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET;
+			state |= (1u << STATE_BIT_FIX) | (1u << STATE_BIT_SNAP_RASTER) | (1u << STATE_BIT_SNAP_ATTRIBUTE);
+		state |= current_instance << STATE_VERTEX_RENDER_PASS_INSTANCE_OFFSET;
 
 		// The pages the instance writes are marked when its damage grows
 		// (gs/gs_interface.cpp:2712-2816): from no depth to read-only depth, to
 		// depth writes, to more colour bits written, or a larger box.
 		bool expands = false;
-		const bool z_sens = state_is_z_sensitive();
+		const bool z_sens = D.z_sens;
 		if (!inst.z_sensitive && z_sens)
 		{
 			inst.z_sensitive = true;
 			expands = true;
 		}
-		if (z_sens && ZbufReg(ctx_reg(R_ZBUF_1)).zmsk == 0 && !inst.z_write)
+		if (z_sens && D.zb.zmsk == 0 && !inst.z_write)
 		{
 			inst.z_write = true;
 			// Depth writes may create a feedback that was not there.
@@ -2710,6 +2722,18 @@ struct pgs_gs : TrackerClient
 
 		if (can_wrap && bb[0] > sci_hi_x_fb)
 		{
+			if (sp != pos)
+			{
+				for (uint32_t i = 0; i < nv; i++)
+					copy_vertex(pos[i], attr[i], sp[i], sa[i]);
+				for (uint32_t i = nv; i < 3; i++)
+				{
+					pos[i] = {};
+					attr[i] = {};
+				}
+				sp = pos;
+				sa = attr;
+			}
 			Layout L = psm_layout(frame.psm);
 			int32_t x_off = -int32_t(frame.fbw << L.pw);
 			int32_t y_off = int32_t(1u << L.ph);
@@ -2752,15 +2776,42 @@ struct pgs_gs : TrackerClient
 			}
 		}
 
-		pa.bb[0] = int16_t(bb[0]);
-		pa.bb[1] = int16_t(bb[1]);
-		pa.bb[2] = int16_t(bb[2]);
-		pa.bb[3] = int16_t(bb[3]);
-
-		uint32_t n = primitive_count;
-		prims[n] = pa;
-		for (uint32_t i = 0; i < 3; i++)
-			copy_vertex(positions[3 * n + i], attributes[3 * n + i], pos[i], attr[i]);
+		// The record is assembled in registers and stored as two 16-byte
+		// words: bb, state | tex, tex2 | alpha, fbmsk | fogcol.
+		const uint32_t n = primitive_count;
+		// The pass's buffers are written once, front to back: ask for the
+		// lines a few records ahead (a prefetch past the end does not fault).
+		prefetch_for_write(prims, (n + ARENA_PREFETCH_RECORDS) * sizeof(pgs_primitive_attribute));
+		prefetch_for_write(positions, 3 * (n + ARENA_PREFETCH_RECORDS) * sizeof(pgs_vertex_position));
+		prefetch_for_write(attributes, 3 * (n + ARENA_PREFETCH_RECORDS) * sizeof(pgs_vertex_attribute));
+		prefetch_for_write(attributes, 3 * (n + ARENA_PREFETCH_RECORDS) * sizeof(pgs_vertex_attribute) + 64);
+		{
+			static_assert(sizeof(pgs_primitive_attribute) == 32 && offsetof(pgs_primitive_attribute, state) == 8 &&
+			              offsetof(pgs_primitive_attribute, fogcol) == 28, "primitive record layout");
+			Word2 w0, w1;
+			w0[0] = uint64_t(uint16_t(bb[0])) | (uint64_t(uint16_t(bb[1])) << 16) |
+			        (uint64_t(uint16_t(bb[2])) << 32) | (uint64_t(uint16_t(bb[3])) << 48);
+			w0[1] = uint64_t(state) | (uint64_t(tex) << 32);
+			w1[0] = uint64_t(tex2) | (uint64_t(alpha_word) << 32);
+			w1[1] = uint64_t(fbmsk) | (uint64_t(fogcol) << 32);
+			memcpy(&prims[n], &w0, 16);
+			memcpy(reinterpret_cast<char *>(&prims[n]) + 16, &w1, 16);
+		}
+		if (sp == pos)
+		{
+			for (uint32_t i = 0; i < 3; i++)
+				copy_vertex(positions[3 * n + i], attributes[3 * n + i], pos[i], attr[i]);
+		}
+		else
+		{
+			for (uint32_t i = 0; i < nv; i++)
+				copy_vertex(positions[3 * n + i], attributes[3 * n + i], sp[i], sa[i]);
+			if (nv == 2)
+			{
+				positions[3 * n + 2] = {};
+				attributes[3 * n + 2] = {};
+			}
+		}
 		primitive_count++;
 		// Set after any flush above, which clears it.
 		last_para_candidate = para_candidate;
@@ -2926,6 +2977,19 @@ struct pgs_gs : TrackerClient
 		}
 	}
 
+	// Whole loops of a register list known at compile time: each write is
+	// the one case of packed_write, with no dispatch on the descriptor.
+	template <class Sink, uint32_t... D>
+	__attribute__((always_inline)) inline void packed_loops(Sink &s, const uint64_t *q, size_t loops)
+	{
+		constexpr uint32_t nreg = sizeof...(D);
+		for (size_t l = 0; l < loops; l++, q += 2 * nreg)
+		{
+			const uint64_t *w = q;
+			((packed_write(s, D, w), w += 2), ...);
+		}
+	}
+
 	template <class Sink>
 	void decode(Sink &s, uint32_t pi, const uint64_t *words, size_t qwords)
 	{
@@ -2961,15 +3025,27 @@ struct pgs_gs : TrackerClient
 				if (path.reg == 0 && qwords - i >= path.nreg)
 				{
 					// Whole loops at a time: the descriptors come from the tag once.
-					uint32_t desc[16];
-					for (uint32_t r = 0; r < path.nreg; r++)
-						desc[r] = uint32_t(path.tag_hi >> (4 * r)) & 0xf;
+					// The usual vertex lists (ST / UV, RGBAQ, XYZ2 and RGBAQ,
+					// XYZ2) run a loop with the writes spelled out.
 					const size_t loops = std::min<size_t>((qwords - i) / path.nreg, path.nloop - path.loop);
 					const uint32_t nreg = path.nreg;
 					const uint64_t *q = &words[2 * i];
-					for (size_t l = 0; l < loops; l++, q += 2 * nreg)
+					const uint64_t list = nreg < 16 ? path.tag_hi & ((uint64_t(1) << (4 * nreg)) - 1) : path.tag_hi;
+					if (nreg == 3 && list == 0x512)
+						packed_loops<Sink, 0x2, 0x1, 0x5>(s, q, loops);
+					else if (nreg == 3 && list == 0x513)
+						packed_loops<Sink, 0x3, 0x1, 0x5>(s, q, loops);
+					else if (nreg == 2 && list == 0x51)
+						packed_loops<Sink, 0x1, 0x5>(s, q, loops);
+					else
+					{
+						uint32_t desc[16];
 						for (uint32_t r = 0; r < nreg; r++)
-							packed_write(s, desc[r], q + 2 * r);
+							desc[r] = uint32_t(path.tag_hi >> (4 * r)) & 0xf;
+						for (size_t l = 0; l < loops; l++, q += 2 * nreg)
+							for (uint32_t r = 0; r < nreg; r++)
+								packed_write(s, desc[r], q + 2 * r);
+					}
 					i += loops * nreg;
 					path.loop += uint32_t(loops);
 					continue;
