@@ -2481,8 +2481,17 @@ struct pgs_gs : TrackerClient
 		post_kick();
 	}
 
-	// post_draw_kick_handler (gs/gs_interface.cpp:2930-2943).
-	void post_kick()
+	// post_draw_kick_handler (gs/gs_interface.cpp:2930-2943).  Runs after
+	// every kick: the checks are inline, the flushes out of line.
+	__attribute__((always_inline)) inline void post_kick()
+	{
+		if (__builtin_expect(pending_palette_updates >= PGS_CLUT_INSTANCES - 1 ||
+		                     primitive_count >= PGS_MAX_PRIMITIVES_PER_FLUSH || textures.size() >= PGS_MAX_TEXTURES ||
+		                     state_vectors.size() >= PGS_MAX_STATE_VECTORS || tracker.memory_pressure(), 0))
+			post_kick_flush();
+	}
+
+	__attribute__((noinline)) void post_kick_flush()
 	{
 		if (pending_palette_updates >= PGS_CLUT_INSTANCES - 1 || primitive_count >= PGS_MAX_PRIMITIVES_PER_FLUSH ||
 		    textures.size() >= PGS_MAX_TEXTURES || state_vectors.size() >= PGS_MAX_STATE_VECTORS)
@@ -3383,8 +3392,10 @@ struct pgs_gs : TrackerClient
 			for (size_t off = 0; off < used;)
 			{
 				// The worker wrote this chunk from another core: fetch ahead so
-				// the vertex records arrive before draw() reads them.
+				// the vertex records arrive before draw() reads them.  A draw
+				// record spans two lines or more, so two lines per command.
 				__builtin_prefetch(c + off + RING_PREFETCH_BYTES, 0, 3);
+				__builtin_prefetch(c + off + RING_PREFETCH_BYTES + 64, 0, 3);
 				uint32_t h;
 				memcpy(&h, c + off, 4);
 				switch (h & 0xffu)

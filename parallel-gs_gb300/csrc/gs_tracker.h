@@ -523,6 +523,7 @@ public:
 	}
 
 	void mark_memory_pressure() { pressure = true; }
+	bool memory_pressure() const { return pressure; }
 
 	void flush_if_memory_pressure()
 	{
