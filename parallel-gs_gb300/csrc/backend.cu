@@ -1079,7 +1079,7 @@ struct CudaBackend
 			StageScope ts(this, PGS_TIMESTAMP_BINNING);
 			CUDA_TRY(cudaMemsetAsync(d_masks, 0, (mask_words + summary_words) * sizeof(uint32_t), stream));
 			CUDA_TRY(cudaMemsetAsync(d_flags, 0, tiles * sizeof(uint32_t), stream));
-			bin_kernel<<<(count + 127) / 128, 128, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags);
+			bin_kernel<<<(count + 31) / 32, 32 * BIN_GROUP_WARPS, 0, stream>>>(P, I, d_sub_masks, d_sub_summary, d_flags);
 			launch_counter++;
 		}
 		uint32_t grid = uint32_t(subs);

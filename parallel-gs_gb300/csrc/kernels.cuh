@@ -2,10 +2,10 @@
 //
 //   setup_kernel     one thread per primitive: edge planes, reciprocal area,
 //                    attribute deltas, bounding box (triangle_setup.comp)
-//   bin_kernel       one thread per primitive: sets the primitive's bit in the
-//                    bitmask of every coarse tile it may touch, plus per-tile
-//                    super-sampling flags (binning.comp); the bitmask keeps
-//                    primitive order without any sort
+//   bin_kernel       32 primitives per CTA: per-coarse-tile membership and
+//                    super-sampling flags (binning.comp), and the primitive's
+//                    bit in the bitmask of every 8x8 sub-tile it may touch;
+//                    the bitmask keeps primitive order without any sort
 //   shade_kernel     one CTA per 8x8-pixel sub-tile of a coarse tile, one
 //                    thread per pixel sample; walks the tile's primitives in
 //                    order with the deferred-shading logic of ubershader.comp
@@ -937,13 +937,18 @@ __device__ __forceinline__ bool intersects_tile(const PrimSetup &s, int32_t lo0,
 // membership test and super-sampling flags (binning.comp:74-125); shading
 // lists are kept per 8x8 sub-tile as bitmasks over the pass's primitive range
 // so that ascending primitive order needs no sort.  A summary bitmask marks
-// non-empty mask words.
-__global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, uint32_t *sub_masks,
-                                                  uint32_t *sub_summary, uint32_t *tile_flags)
+// non-empty mask words.  A CTA takes 32 primitives (one mask word): each of
+// its BIN_GROUP_WARPS warps loads all 32, warp 0 marks the coarse tiles, and
+// the warps share the (primitive, sub-tile) tests, so that the dependent
+// loads and shuffles of one batch overlap those of the others.
+constexpr uint32_t BIN_GROUP_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * BIN_GROUP_WARPS) bin_kernel(PassParams P, DevInstance I, uint32_t *sub_masks,
+                                                                   uint32_t *sub_summary, uint32_t *tile_flags)
 {
 	const unsigned full = 0xffffffffu;
-	const uint32_t lane = threadIdx.x & 31u;
-	const uint32_t local = blockIdx.x * blockDim.x + threadIdx.x;
+	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+	const uint32_t local = blockIdx.x * 32u + lane;
 	const uint32_t p = I.prim_lo + local;
 	bool live = local < I.prim_count;
 	pgs_primitive_attribute pa = {};
@@ -961,8 +966,9 @@ __global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, u
 
 	const int ts = int(P.tile_size_log2);
 	const bool ms_tri = ((pa.state >> STATE_BIT_MULTISAMPLE) & 1) && !((pa.state >> STATE_BIT_LINE) & 1);
-	// Coarse tiles: membership and super-sampling flags, one primitive per thread.
-	if (live)
+	// Coarse tiles: membership and super-sampling flags, one primitive per
+	// thread of warp 0.
+	if (warp == 0 && live)
 	{
 		int32_t tx0 = max((s.bb[0] - I.base_x) >> ts, 0), ty0 = max((s.bb[1] - I.base_y) >> ts, 0);
 		int32_t tx1 = min((s.bb[2] - I.base_x) >> ts, int32_t(I.tiles_w) - 1);
@@ -1020,8 +1026,8 @@ __global__ void __launch_bounds__(128) bin_kernel(PassParams P, DevInstance I, u
 			incl += y;
 	}
 	const uint32_t total = __shfl_sync(full, incl, 31);
-	const uint32_t warp_first = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
-	for (uint32_t base = 0; base < total; base += 32u)
+	const uint32_t warp_first = blockIdx.x * 32u;
+	for (uint32_t base = warp * 32u; base < total; base += 32u * BIN_GROUP_WARPS)
 	{
 		const uint32_t j = base + lane;
 		// Owner: the first lane whose inclusive count exceeds j.
