@@ -91,6 +91,14 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
 	return *reinterpret_cast<uint32_t *>(&v);
 }
 
+// One RGBA8 pixel as the network's first four input channels (x / 255 in
+// BF16), two channels per word.
+__device__ __forceinline__ void rgba8_to_bf16x4(uint32_t c, uint32_t &rg, uint32_t &ba)
+{
+	rg = pack_bf16x2(float(c & 0xffu) / 255.0f, float((c >> 8) & 0xffu) / 255.0f);
+	ba = pack_bf16x2(float((c >> 16) & 0xffu) / 255.0f, float(c >> 24) / 255.0f);
+}
+
 // Epilogue kinds of conv3x3_kernel.
 enum : int
 {
@@ -102,6 +110,7 @@ enum : int
 struct ConvArgs
 {
 	const __nv_bfloat16 *in;     // N x H x W x CIN
+	const uint8_t *in_rgba;      // CIN 16 only: N x H x W x 4 RGBA8 read in place of `in` (converted as by image_to_bf16_kernel)
 	const __nv_bfloat16 *wt;     // 9 x COUT x CIN (tap, out channel, in channel)
 	const float *bias;           // COUT (EPI_RELU / EPI_LAST)
 	__nv_bfloat16 *out;          // N x H x W x COUT (EPI_RELU / EPI_MASK)
@@ -126,6 +135,23 @@ __global__ void __launch_bounds__(256) conv3x3_kernel(ConvArgs A)
 
 	// Input halo, 16-byte chunks, zero outside the image.
 	constexpr int CH = CIN / 8;
+	if (CIN == 16 && A.in_rgba)
+	{
+		// The RGBA8 image itself: channels 0-3 scaled by 1/255, 4-15 zero.
+		for (int p = tid; p < HALO * HALO; p += 256)
+		{
+			int gx = x0 - 1 + p % HALO, gy = y0 - 1 + p / HALO;
+			uint4 v = make_uint4(0, 0, 0, 0);
+			if (gx >= 0 && gy >= 0 && gx < A.w && gy < A.h)
+			{
+				const uint32_t c = reinterpret_cast<const uint32_t *>(A.in_rgba)[(size_t(img) * A.h + gy) * A.w + gx];
+				rgba8_to_bf16x4(c, v.x, v.y);
+			}
+			*reinterpret_cast<uint4 *>(s_in + p * PS) = v;
+			*reinterpret_cast<uint4 *>(s_in + p * PS + 8) = make_uint4(0, 0, 0, 0);
+		}
+	}
+	else
 	for (int i = tid; i < HALO * HALO * CH; i += 256)
 	{
 		int p = i / CH, c = (i % CH) * 8;
@@ -397,8 +423,7 @@ __global__ void __launch_bounds__(256) image_to_bf16_kernel(const uint8_t *img, 
 		return;
 	uint32_t c = reinterpret_cast<const uint32_t *>(img)[p];
 	uint32_t w[8];
-	w[0] = pack_bf16x2(float(c & 0xffu) / 255.0f, float((c >> 8) & 0xffu) / 255.0f);
-	w[1] = pack_bf16x2(float((c >> 16) & 0xffu) / 255.0f, float(c >> 24) / 255.0f);
+	rgba8_to_bf16x4(c, w[0], w[1]);
 	for (int i = 2; i < 8; i++)
 		w[i] = 0;
 	uint4 *o = reinterpret_cast<uint4 *>(out + p * 16);
@@ -1077,14 +1102,20 @@ struct Upscaler
 	// Forward pass of `n` images of h x w RGBA8 (device memory).  The FP32
 	// result stays in d_out; out_rgba (device, optional) gets it clamped and
 	// rounded to RGBA8.
-	int forward(const uint8_t *d_img, int n, int h, int w, uint8_t *out_rgba)
+	// keep_input: the 16-channel BF16 input is kept in d_x0 (training needs
+	// it for the first layer's weight gradient); otherwise the first layer
+	// reads the RGBA8 image directly.
+	int forward(const uint8_t *d_img, int n, int h, int w, uint8_t *out_rgba, bool keep_input)
 	{
 		size_t pixels = size_t(n) * h * w;
 		int r = ensure(pixels);
 		if (r)
 			return r;
-		image_to_bf16_kernel<<<unsigned((pixels + 255) / 256), 256, 0, stream>>>(d_img, d_x0, pixels);
-		UP_TRY(cudaGetLastError());
+		if (keep_input)
+		{
+			image_to_bf16_kernel<<<unsigned((pixels + 255) / 256), 256, 0, stream>>>(d_img, d_x0, pixels);
+			UP_TRY(cudaGetLastError());
+		}
 		ConvArgs k = {};
 		k.n = n;
 		k.h = h;
@@ -1092,6 +1123,7 @@ struct Upscaler
 		for (int l = 0; l < LAYERS; l++)
 		{
 			k.in = l == 0 ? d_x0 : d_act[l - 1];
+			k.in_rgba = l == 0 && !keep_input ? d_img : nullptr;
 			k.wt = bf.fwd[l];
 			k.bias = d_params + off.b[l];
 			if (l < LAYERS - 1)
@@ -1138,7 +1170,7 @@ struct Upscaler
 	// squared error over all four channels.
 	int backward(const uint8_t *d_img, const uint8_t *d_target, int n, int h, int w, double *loss)
 	{
-		int r = forward(d_img, n, h, w, nullptr);
+		int r = forward(d_img, n, h, w, nullptr, true);
 		if (r)
 			return r;
 		size_t pixels = size_t(n) * h * w;
@@ -1278,7 +1310,8 @@ int pgs_upscaler_forward(void *up, const void *d_images, uint32_t n, uint32_t h,
 		return PGS_ERROR_INVALID_ARGUMENT;
 	Upscaler *u = static_cast<Upscaler *>(up);
 	cudaSetDevice(u->device);
-	return u->forward(static_cast<const uint8_t *>(d_images), int(n), int(h), int(w), static_cast<uint8_t *>(d_out_rgba));
+	return u->forward(static_cast<const uint8_t *>(d_images), int(n), int(h), int(w), static_cast<uint8_t *>(d_out_rgba),
+	                  false);
 }
 
 int pgs_upscaler_backward(void *up, const void *d_images, const void *d_targets, uint32_t n, uint32_t h, uint32_t w,
