@@ -510,8 +510,15 @@ int pgs_upscaler_adam_step(void *upscaler, float learning_rate);
 int pgs_upscaler_set_tensor_path(void *upscaler, int tcgen05);
 /* Sticky error flags of the tcgen05 kernels (a bounded wait that ran out). */
 int pgs_upscaler_get_error(void *upscaler, uint32_t *flags);
-/* The upscaler's cudaStream_t, as an opaque pointer. */
+/* The stream the upscaler queues its work on (a cudaStream_t, as an opaque
+ * pointer): its own stream unless pgs_upscaler_set_stream chose another. */
 void *pgs_upscaler_stream(void *upscaler);
+/* Queues the upscaler's later work on `stream` (a cudaStream_t of the same
+ * device, e.g. a backend's stream, so that a frame's rendering and its
+ * upscaling follow each other with no cross-stream wait); NULL selects the
+ * upscaler's own stream again.  Waits for the work queued so far first.  The
+ * caller keeps `stream` alive while it is selected. */
+int pgs_upscaler_set_stream(void *upscaler, void *stream);
 /* Self-test of the tcgen05 tensor-core path: a 128x32x32 BF16 product from
  * shared memory (mode 0: no-swizzle operand layout, 1: 64-byte swizzle) read
  * back from tensor memory into out (128 x 32 floats, row-major).  Mode 2

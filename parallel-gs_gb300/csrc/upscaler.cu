@@ -893,7 +893,8 @@ static int make_act_tmap(CUtensorMap *m, const void *ptr, int n, int h, int w)
 struct Upscaler
 {
 	int device = 0;
-	cudaStream_t stream = nullptr;
+	cudaStream_t stream = nullptr;      // where the upscaler's work is queued
+	cudaStream_t own_stream = nullptr;  // created with the upscaler
 	LayerOffsets off = {};
 	float *d_params = nullptr, *d_m = nullptr, *d_v = nullptr, *d_grad = nullptr;
 	float *d_wgrad = nullptr, *d_bgrad = nullptr;   // padded scratch, per layer
@@ -947,7 +948,8 @@ struct Upscaler
 	{
 		device = dev;
 		UP_TRY(cudaSetDevice(device));
-		UP_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+		UP_TRY(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+		stream = own_stream;
 		UP_TRY(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
 		int o = 0;
 		for (int l = 0; l < LAYERS; l++)
@@ -1003,8 +1005,18 @@ struct Upscaler
 		free_acts();
 		cudaFree(d_loss);
 		cudaFree(d_err);
-		if (stream)
-			cudaStreamDestroy(stream);
+		if (own_stream)
+			cudaStreamDestroy(own_stream);
+	}
+
+	// Later work goes to `s` (the upscaler's own stream when null), after
+	// what is queued on the current one.
+	int set_stream(cudaStream_t s)
+	{
+		UP_TRY(cudaSetDevice(device));
+		UP_TRY(cudaStreamSynchronize(stream));
+		stream = s ? s : own_stream;
+		return PGS_OK;
 	}
 
 	void free_acts()
@@ -1383,6 +1395,13 @@ int pgs_upscaler_get_error(void *up, uint32_t *flags)
 }
 
 void *pgs_upscaler_stream(void *up) { return up ? static_cast<void *>(static_cast<Upscaler *>(up)->stream) : nullptr; }
+
+int pgs_upscaler_set_stream(void *up, void *stream)
+{
+	if (!up)
+		return PGS_ERROR_INVALID_ARGUMENT;
+	return static_cast<Upscaler *>(up)->set_stream(static_cast<cudaStream_t>(stream));
+}
 
 int pgs_upscaler_synchronize(void *up)
 {

@@ -93,7 +93,8 @@ EXPORTED_SYMBOLS = [
     "pgs_batch_synchronize",
     "pgs_upscaler_create", "pgs_upscaler_destroy", "pgs_upscaler_param_count", "pgs_upscaler_set_params",
     "pgs_upscaler_get_params", "pgs_upscaler_get_gradient", "pgs_upscaler_forward", "pgs_upscaler_backward",
-    "pgs_upscaler_adam_step", "pgs_upscaler_stream", "pgs_upscaler_synchronize", "pgs_umma_selftest",
+    "pgs_upscaler_adam_step", "pgs_upscaler_stream", "pgs_upscaler_set_stream", "pgs_upscaler_synchronize",
+    "pgs_umma_selftest",
     "pgs_upscaler_set_tensor_path", "pgs_upscaler_get_error",
     "pgs_gs_create", "pgs_gs_destroy", "pgs_gs_gif_transfer", "pgs_gs_write_register", "pgs_gs_flush",
     "pgs_gs_read_vram", "pgs_gs_read_vram_async", "pgs_gs_wait",
@@ -610,6 +611,7 @@ class Upscaler:
         lib.pgs_upscaler_adam_step.argtypes = [vp, C.c_float]
         lib.pgs_upscaler_stream.argtypes = [vp]
         lib.pgs_upscaler_stream.restype = vp
+        lib.pgs_upscaler_set_stream.argtypes = [vp, vp]
         lib.pgs_upscaler_synchronize.argtypes = [vp]
         lib.pgs_upscaler_set_tensor_path.argtypes = [vp, C.c_int]
         lib.pgs_upscaler_get_error.argtypes = [vp, C.POINTER(u32)]
@@ -660,6 +662,11 @@ class Upscaler:
 
     def stream(self) -> int:
         return self.lib.pgs_upscaler_stream(self.handle)
+
+    def set_stream(self, stream: int | None) -> None:
+        """Queues later work on `stream` (a cudaStream_t pointer, e.g. a
+        backend's stream()); None returns to the upscaler's own stream."""
+        check(self.lib.pgs_upscaler_set_stream(self.handle, stream), "upscaler_set_stream")
 
     def synchronize(self) -> None:
         check(self.lib.pgs_upscaler_synchronize(self.handle), "upscaler_synchronize")

@@ -114,3 +114,34 @@ def test_tcgen05_and_mma_sync_paths_agree_on_full_frames():
         up.close()
     d = np.abs(outs[0] - outs[1])
     assert d.max() <= 2 and np.mean(d == 0) > 0.99
+
+
+def test_forward_on_a_caller_stream_is_identical():
+    """pgs_upscaler_set_stream: the same frames through the upscaler's own
+    stream and through a stream the caller owns give the same bytes, and
+    None returns to the upscaler's stream."""
+    import torch
+    rng = np.random.default_rng(11)
+    img = torch.from_numpy(rng.integers(0, 256, size=(2, 448, 640, 4), dtype=np.uint8)).cuda()
+    side = torch.cuda.Stream()
+    up = pgs.Upscaler(0)
+    try:
+        up.set_params(params(11))
+        own = up.stream()
+        a = torch.empty_like(img)
+        up.forward(img, a)
+        up.synchronize()
+        up.set_stream(side.cuda_stream)
+        assert up.stream() == side.cuda_stream
+        b = torch.empty_like(img)
+        up.forward(img, b)
+        side.synchronize()
+        up.set_stream(None)
+        assert up.stream() == own
+        c = torch.empty_like(img)
+        up.forward(img, c)
+        up.synchronize()
+        assert up.error_flags() == 0
+    finally:
+        up.close()
+    assert torch.equal(a, b) and torch.equal(a, c)
