@@ -249,12 +249,16 @@ struct CudaBackend
 	uint8_t *h_arena = nullptr, *d_arena = nullptr;
 	size_t arena_cap = 0, arena_used = 0;
 
-	// Reserved primitive buffers (pinned, double buffered so the frontend can
-	// fill one while the other is being copied).
-	uint8_t *h_stage[2] = {};
-	cudaEvent_t stage_done[2] = {};
-	int stage_index = 0;
-	bool stage_pending[2] = {};
+	// Reserved primitive buffers (pinned).  Two to start with, so that the
+	// frontend fills one while the other is copied; when every buffer still
+	// waits for its copy (the copies queue behind the passes before them), one
+	// more is added, up to MAX_STAGES, so that a frame of many passes is
+	// recorded ahead of the device instead of in step with it.
+	static constexpr int MAX_STAGES = 6;
+	uint8_t *h_stage[MAX_STAGES] = {};
+	cudaEvent_t stage_done[MAX_STAGES] = {};
+	int stage_index = 0, num_stages = 0;
+	bool stage_pending[MAX_STAGES] = {};
 
 	// Scratch.
 	PrimSetup *d_setup = nullptr;
@@ -445,13 +449,24 @@ struct CudaBackend
 		CUDA_TRY(cudaMemset(d_heuristic_action, 0, n));
 		for (int i = 0; i < 2; i++)
 		{
-			CUDA_TRY(cudaMallocHost(&h_stage[i], stage_bytes()));
-			CUDA_TRY(cudaEventCreateWithFlags(&stage_done[i], cudaEventDisableTiming));
+			int r = add_stage();
+			if (r)
+				return r;
 			CUDA_TRY(cudaEventCreate(&shade_ev[i]));
 		}
 		for (auto &rb : readbacks)
 			CUDA_TRY(cudaEventCreateWithFlags(&rb.done, cudaEventDisableTiming));
 		return grow_arena(size_t(opt && opt->arena_mib ? opt->arena_mib : 256u) << 20);
+	}
+
+	int add_stage()
+	{
+		const int i = num_stages;
+		CUDA_TRY(cudaMallocHost(&h_stage[i], stage_bytes()));
+		CUDA_TRY(cudaEventCreateWithFlags(&stage_done[i], cudaEventDisableTiming));
+		stage_pending[i] = false;
+		num_stages++;
+		return PGS_OK;
 	}
 
 	static size_t stage_bytes()
@@ -498,12 +513,13 @@ struct CudaBackend
 		cudaFree(d_reset_vram);
 		cudaFree(d_reset_clut);
 		cudaFreeHost(h_arena);
-		for (int i = 0; i < 2; i++)
+		for (int i = 0; i < MAX_STAGES; i++)
 		{
-			cudaFreeHost(h_stage[i]);
+			if (h_stage[i]) cudaFreeHost(h_stage[i]);
 			if (stage_done[i]) cudaEventDestroy(stage_done[i]);
-			if (shade_ev[i]) cudaEventDestroy(shade_ev[i]);
 		}
+		for (int i = 0; i < 2; i++)
+			if (shade_ev[i]) cudaEventDestroy(shade_ev[i]);
 		for (auto &rb : readbacks)
 		{
 			if (rb.done) cudaEventDestroy(rb.done);
@@ -576,7 +592,7 @@ struct CudaBackend
 	int staging_buffer_of(const pgs_render_pass *rp) const
 	{
 		const size_t N = PGS_MAX_PRIMITIVES_PER_FLUSH;
-		for (int i = 0; i < 2; i++)
+		for (int i = 0; i < num_stages; i++)
 		{
 			const uint8_t *base = h_stage[i];
 			if (reinterpret_cast<const uint8_t *>(rp->positions) == base &&
@@ -601,12 +617,41 @@ struct CudaBackend
 	{
 		if (n > PGS_MAX_PRIMITIVES_PER_FLUSH)
 			return PGS_ERROR_INVALID_ARGUMENT;
-		stage_index ^= 1;
-		if (stage_pending[stage_index])
+		// The next buffer whose copy has finished; else a new one; else wait
+		// for the next in turn.
+		int pick = -1;
+		for (int k = 1; k <= num_stages && pick < 0; k++)
 		{
-			CUDA_TRY(cudaEventSynchronize(stage_done[stage_index]));
-			stage_pending[stage_index] = false;
+			const int i = (stage_index + k) % num_stages;
+			if (stage_pending[i])
+			{
+				const cudaError_t q = cudaEventQuery(stage_done[i]);
+				if (q == cudaErrorNotReady)
+				{
+					// Not an error: keep it out of the launch checks' last error.
+					if (cudaPeekAtLastError() == cudaErrorNotReady)
+						(void)cudaGetLastError();
+					continue;
+				}
+				CUDA_TRY(q);
+				stage_pending[i] = false;
+			}
+			pick = i;
 		}
+		if (pick < 0 && num_stages < MAX_STAGES)
+		{
+			int r = add_stage();
+			if (r)
+				return r;
+			pick = num_stages - 1;
+		}
+		if (pick < 0)
+		{
+			pick = (stage_index + 1) % num_stages;
+			CUDA_TRY(cudaEventSynchronize(stage_done[pick]));
+			stage_pending[pick] = false;
+		}
+		stage_index = pick;
 		const size_t N = PGS_MAX_PRIMITIVES_PER_FLUSH;
 		uint8_t *base = h_stage[stage_index];
 		*pos = reinterpret_cast<pgs_vertex_position *>(base);
