@@ -27,6 +27,7 @@
 #include <cstdint>
 #include <cstring>
 #include <new>
+#include <utility>
 #include <vector>
 
 namespace pgs_up
@@ -99,6 +100,21 @@ __device__ __forceinline__ void rgba8_to_bf16x4(uint32_t c, uint32_t &rg, uint32
 	ba = pack_bf16x2(float((c >> 16) & 0xffu) / 255.0f, float(c >> 24) / 255.0f);
 }
 
+// Programmatic dependent launch.  launch_dependents lets the next kernel of
+// the stream start its CTAs (their set-up) once every CTA of this one has
+// started; wait blocks until every kernel this one depends on has finished
+// and its writes are visible.  Both do nothing when the launch did not ask
+// for it.
+__device__ __forceinline__ void griddep_launch_dependents()
+{
+	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+__device__ __forceinline__ void griddep_wait()
+{
+	asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // Epilogue kinds of conv3x3_kernel.
 enum : int
 {
@@ -132,9 +148,19 @@ __global__ void __launch_bounds__(256) conv3x3_kernel(ConvArgs A)
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int x0 = blockIdx.x * TILE, y0 = blockIdx.y * TILE, img = blockIdx.z;
+	griddep_launch_dependents();
+
+	// Weights (not written by the kernels before this one), then the wait
+	// for the previous layer, then its output.
+	constexpr int CH = CIN / 8;
+	for (int i = tid; i < 9 * COUT * CH; i += 256)
+	{
+		int r = i / CH, c = (i % CH) * 8;
+		*reinterpret_cast<uint4 *>(s_w + r * PS + c) = *reinterpret_cast<const uint4 *>(A.wt + r * CIN + c);
+	}
+	griddep_wait();
 
 	// Input halo, 16-byte chunks, zero outside the image.
-	constexpr int CH = CIN / 8;
 	if (CIN == 16 && A.in_rgba)
 	{
 		// The RGBA8 image itself: channels 0-3 scaled by 1/255, 4-15 zero.
@@ -160,11 +186,6 @@ __global__ void __launch_bounds__(256) conv3x3_kernel(ConvArgs A)
 		if (gx >= 0 && gy >= 0 && gx < A.w && gy < A.h)
 			v = *reinterpret_cast<const uint4 *>(A.in + ((size_t(img) * A.h + gy) * A.w + gx) * CIN + c);
 		*reinterpret_cast<uint4 *>(s_in + p * PS + c) = v;
-	}
-	for (int i = tid; i < 9 * COUT * CH; i += 256)
-	{
-		int r = i / CH, c = (i % CH) * 8;
-		*reinterpret_cast<uint4 *>(s_w + r * PS + c) = *reinterpret_cast<const uint4 *>(A.wt + r * CIN + c);
 	}
 	__syncthreads();
 
@@ -687,6 +708,7 @@ __global__ void __launch_bounds__(tc::THREADS, 2) conv32_tc_kernel(const __grid_
 	const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
 	const int tiles_x = (w + tc::COLS - 1) / tc::COLS, tiles_y = (h + tc::ROWS - 1) / tc::ROWS;
 	const int tiles = tiles_x * tiles_y * n;
+	griddep_launch_dependents();
 
 	// Weights: 16-byte chunks of 8 input channels into their swizzled slots.
 	for (uint32_t i = tid; i < 9 * 32 * 4; i += tc::THREADS)
@@ -719,6 +741,9 @@ __global__ void __launch_bounds__(tc::THREADS, 2) conv32_tc_kernel(const __grid_
 	__syncthreads();
 	tc_fence_after();
 	const uint32_t tmem = tmem_slot;
+	// Weights, barriers and tensor memory are set up; the input is the
+	// previous layer's output.
+	griddep_wait();
 
 	auto tile_coords = [&](int tile, int &img, int &x0, int &y0) {
 		img = tile / (tiles_x * tiles_y);
@@ -1088,7 +1113,7 @@ struct Upscaler
 	// 3x3 convolution of a 32-channel tensor into 32 accumulator channels on
 	// tcgen05 (conv32_tc_kernel) with the given epilogue.
 	template <int EPI>
-	int conv_tc(const ConvArgs &a)
+	int conv_tc(const ConvArgs &a, bool pdl = false)
 	{
 		CUtensorMap *m = nullptr;
 		int r = act_tmap(a.in, a.n, a.h, a.w, m);
@@ -1097,17 +1122,33 @@ struct Upscaler
 		int tiles = ((a.w + tc::COLS - 1) / tc::COLS) * ((a.h + tc::ROWS - 1) / tc::ROWS) * a.n;
 		int grid = std::min(tiles, sm_count * use_tc);
 		TcOut o = { a.out, a.mask };
-		conv32_tc_kernel<EPI><<<grid, tc::THREADS, tc::SMEM_BYTES, stream>>>(*m, a.wt, a.bias, o, a.n, a.h, a.w, d_err);
-		UP_TRY(cudaGetLastError());
-		return PGS_OK;
+		return launch(conv32_tc_kernel<EPI>, dim3(grid), dim3(tc::THREADS), tc::SMEM_BYTES, pdl, *m, a.wt, a.bias, o,
+		              a.n, a.h, a.w, d_err);
 	}
 
 	template <int CIN, int COUT, int EPI>
-	int conv(const ConvArgs &a)
+	int conv(const ConvArgs &a, bool pdl = false)
 	{
 		dim3 grid((a.w + TILE - 1) / TILE, (a.h + TILE - 1) / TILE, a.n);
-		conv3x3_kernel<CIN, COUT, EPI><<<grid, 256, 0, stream>>>(a);
-		UP_TRY(cudaGetLastError());
+		return launch(conv3x3_kernel<CIN, COUT, EPI>, grid, dim3(256), 0, pdl, a);
+	}
+
+	// Launch on the upscaler's stream; pdl: the kernel may start while the
+	// one before it in the stream runs (it waits for it in griddep_wait).
+	template <typename... KArgs, typename... Args>
+	int launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, bool pdl, Args &&...args)
+	{
+		cudaLaunchConfig_t cfg = {};
+		cfg.gridDim = grid;
+		cfg.blockDim = block;
+		cfg.dynamicSmemBytes = smem;
+		cfg.stream = stream;
+		cudaLaunchAttribute attr[1];
+		attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+		attr[0].val.programmaticStreamSerializationAllowed = 1;
+		cfg.attrs = attr;
+		cfg.numAttrs = pdl ? 1 : 0;
+		UP_TRY(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
 		return PGS_OK;
 	}
 
@@ -1143,12 +1184,16 @@ struct Upscaler
 				k.out = d_act[l];
 				// The 4 -> 32 layer stays on mma.sync: on tcgen05 it would be a
 				// 32 -> 32 layer with 28 zero input channels, which measured slower.
+				// Inference launches every layer after the first with
+				// programmatic dependent launch: its set-up overlaps the
+				// previous layer's last wave.
+				const bool pdl = !keep_input && l > 0;
 				if (l == 0)
 					r = conv<16, 32, EPI_RELU>(k);
 				else if (use_tc)
-					r = conv_tc<EPI_RELU>(k);
+					r = conv_tc<EPI_RELU>(k, pdl);
 				else
-					r = conv<32, 32, EPI_RELU>(k);
+					r = conv<32, 32, EPI_RELU>(k, pdl);
 			}
 			else
 			{
@@ -1157,7 +1202,7 @@ struct Upscaler
 				k.image = d_img;
 				k.out_f32 = d_out;
 				k.out_rgba = out_rgba;
-				r = conv<32, 8, EPI_LAST>(k);
+				r = conv<32, 8, EPI_LAST>(k, !keep_input);
 			}
 			if (r)
 				return r;
