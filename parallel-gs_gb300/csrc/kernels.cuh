@@ -2001,6 +2001,51 @@ __device__ __forceinline__ void process_primitive_with(const ShadeCtx &C, uint32
 	Request q = shade_early<AA, MIP>(C, s, pi, st, S, opaque, any_cov);
 	if (!any_cov)
 		return;
+	// A primitive that is not opaque (warp-uniform: a state bit) is shaded
+	// right away rather than left pending.  The result is the same as shading
+	// it at the next flush: leaving it pending only saves work when a later
+	// opaque primitive covers the sample, which blended primitives seldom
+	// meet, and shading now keeps every lane of the call on the same
+	// primitive.  What was pending is shaded first wherever this primitive
+	// covers a sample that has a pending one.  The super-sampled variants take
+	// this path on its own; the single-sampled one keeps the shared path below
+	// (measured: the separate path speeds the first up and slows the second).
+	if (SS && !opaque)
+	{
+		if (q.coverage > 0)
+		{
+			covered++;
+			if (q.z_test && !S.pending.z_write)
+			{
+				const bool zp = ((st >> STATE_BIT_Z_TEST_GREATER) & 1) ? q.z > S.depth : q.z >= S.depth;
+				if (!zp)
+				{
+					q.coverage = 0;
+					q.z_write = false;
+				}
+				q.z_test = false;
+			}
+		}
+		if (__any_sync(0xffffffffu, q.coverage > 0 && S.pending.coverage > 0))
+		{
+			if (S.pending.coverage > 0)
+				shade_resolve<MIP>(C, S);
+			S.pending.coverage = 0;
+			S.pending.z_write = false;
+		}
+		if (__any_sync(0xffffffffu, q.coverage > 0))
+		{
+			if (q.coverage > 0)
+			{
+				S.pending = q;
+				S.pending_prim = pi;
+				shade_resolve<MIP>(C, S);
+				S.pending.coverage = 0;
+				S.pending.z_write = false;
+			}
+		}
+		return;
+	}
 	if (q.coverage > 0)
 	{
 		covered++;
@@ -2056,11 +2101,7 @@ __device__ __forceinline__ void process_primitive_with(const ShadeCtx &C, uint32
 			S.pending_prim = pi;
 		}
 	}
-	// A primitive that is not opaque is shaded right away rather than left
-	// pending.  The result is the same as shading it at the next flush:
-	// leaving it pending only saves work when a later opaque primitive covers
-	// the sample, which blended primitives seldom meet, and shading now keeps
-	// every lane of the call on the same primitive.
+	// The shared path shades a primitive that is not opaque at once too.
 	if (!((st >> STATE_BIT_OPAQUE) & 1u) &&
 	    __any_sync(0xffffffffu, S.pending.coverage > 0 && S.pending_prim == pi))
 	{
