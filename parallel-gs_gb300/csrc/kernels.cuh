@@ -191,11 +191,15 @@ constexpr uint32_t ERROR_FLAG_TILE_OVERFLOW = 1u << 0;
 __constant__ uint8_t c_rcp_tab[256];
 
 // Occupancy target of the shading kernels in 256-thread units per SM: 4 means
-// at most 64 registers per thread for the 1x..4x variants.
+// at most 64 registers per thread for the 1x..4x variants.  The plain 4x
+// variant (no AA1, no mipmaps) asks for 5 CTAs (48 registers, a few spills):
+// measured on the C2 frame, 3 CTAs 1.24 ms, 4 CTAs 1.10 ms, 5 CTAs 1.09 ms.
+// The AA1 / mipmap variants, larger, stay at 4.
 #ifndef PGS_SHADE_OCC
 #define PGS_SHADE_OCC 4
 #endif
-#define PGS_SHADE_MIN_BLOCKS(NS) (PGS_SHADE_OCC * 4 / (NS) > 0 ? PGS_SHADE_OCC * 4 / (NS) : 1)
+#define PGS_SHADE_MIN_BLOCKS(NS, LARGE) \
+	((NS) == 4 && !(LARGE) ? PGS_SHADE_OCC + 1 : (PGS_SHADE_OCC * 4 / (NS) > 0 ? PGS_SHADE_OCC * 4 / (NS) : 1))
 
 // ---------------------------------------------------------------------------
 // Scalar helpers.
@@ -2537,7 +2541,7 @@ __device__ __forceinline__ void shade_subtile(const PassParams &P, const DevInst
 }
 
 template <int NS, bool SS, bool AA, bool MIP>
-__global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS)) shade_kernel(PassParams P, DevInstance I, const uint32_t *sub_masks,
+__global__ void __launch_bounds__(64 * NS, PGS_SHADE_MIN_BLOCKS(NS, AA || MIP)) shade_kernel(PassParams P, DevInstance I, const uint32_t *sub_masks,
                                                         const uint32_t *sub_summary, const uint32_t *tile_flags)
 {
 	const uint32_t sub = blockIdx.x;
