@@ -996,6 +996,10 @@ struct CudaBackend
 		return r;
 	}
 
+	// Set while an op submitted outside recording runs: nothing will run it
+	// again, so it may work on its arena records in place.
+	bool live_op = false;
+
 	int submit(Op &op)
 	{
 		if (recording)
@@ -1006,7 +1010,12 @@ struct CudaBackend
 			return deferred.size() >= 64 ? flush_deferred() : PGS_OK;
 		}
 		int r = flush_deferred();
-		return r ? r : execute(op);
+		if (r)
+			return r;
+		live_op = !recording;
+		r = execute(op);
+		live_op = false;
+		return r;
 	}
 
 	int ensure_masks(size_t words, size_t tiles)
@@ -1499,7 +1508,10 @@ struct CudaBackend
 			if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
 		}
 		P.texels = d_texels;
-		P.prims = d_prims_work;
+		// Setup and the single-sample heuristic rewrite primitive words in
+		// place: a recorded pass works on a copy so that its records stay as
+		// recorded for the next replay; a pass run once works on its records.
+		P.prims = live_op ? reinterpret_cast<pgs_primitive_attribute *>(d_arena + p.prim_off) : d_prims_work;
 		P.setup = d_setup;
 		P.tattr = d_tattr;
 		P.num_prims = p.num_prims;
@@ -1531,8 +1543,9 @@ struct CudaBackend
 			P.setup_rate_x_log2 = std::max(P.setup_rate_x_log2, p.instances[i].sampling_rate_x_log2);
 			P.setup_rate_y_log2 = std::max(P.setup_rate_y_log2, p.instances[i].sampling_rate_y_log2);
 		}
-		CUDA_TRY(cudaMemcpyAsync(d_prims_work, d_arena + p.prim_off, size_t(p.num_prims) * sizeof(pgs_primitive_attribute),
-		                         cudaMemcpyDeviceToDevice, stream));
+		if (!live_op)
+			CUDA_TRY(cudaMemcpyAsync(d_prims_work, d_arena + p.prim_off, size_t(p.num_prims) * sizeof(pgs_primitive_attribute),
+			                         cudaMemcpyDeviceToDevice, stream));
 		{
 			StageScope ts(this, PGS_TIMESTAMP_TRIANGLE_SETUP);
 			if (H.instance_mask)
