@@ -366,13 +366,16 @@ def test_framebuffer_write_over_sampled_page_keeps_the_pass(tex_page, rect):
             ref.close()
 
 
-@pytest.mark.parametrize("maker", ["c2", "fuzz", "strips"])
+@pytest.mark.parametrize("maker", ["c2", "c1", "fuzz", "strips"])
 def test_records_do_not_depend_on_transfer_chunking(maker):
-    """Whole PACKED loops are decoded a tag's worth at a time; sent one qword
+    """Whole PACKED loops are decoded a tag's worth at a time (with the writes
+    spelled out for ST / UV, RGBAQ, XYZ2 and RGBAQ, XYZ2 lists); sent one qword
     per call they take the per-qword path.  Both must give the same records,
     states and passes."""
     if maker == "c2":
         data = g.frame_c2(seed=9, num_triangles=6000, num_sprites=300, super_sampling=1, num_textures=2).data
+    elif maker == "c1":
+        data = g.frame_c1(seed=4, num_triangles=4000).data
     elif maker == "fuzz":
         data = g.frame_fuzz(5).data
     else:
