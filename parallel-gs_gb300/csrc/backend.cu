@@ -462,7 +462,14 @@ struct CudaBackend
 	int add_stage()
 	{
 		const int i = num_stages;
-		CUDA_TRY(cudaMallocHost(&h_stage[i], stage_bytes()));
+		if (cudaMallocHost(&h_stage[i], stage_bytes()) != cudaSuccess)
+		{
+			// Out of pinned memory is not fatal past the first two buffers:
+			// the caller waits for one instead.
+			(void)cudaGetLastError();
+			h_stage[i] = nullptr;
+			return PGS_ERROR_OUT_OF_MEMORY;
+		}
 		CUDA_TRY(cudaEventCreateWithFlags(&stage_done[i], cudaEventDisableTiming));
 		stage_pending[i] = false;
 		num_stages++;
@@ -638,13 +645,8 @@ struct CudaBackend
 			}
 			pick = i;
 		}
-		if (pick < 0 && num_stages < MAX_STAGES)
-		{
-			int r = add_stage();
-			if (r)
-				return r;
+		if (pick < 0 && num_stages < MAX_STAGES && add_stage() == PGS_OK)
 			pick = num_stages - 1;
-		}
 		if (pick < 0)
 		{
 			pick = (stage_index + 1) % num_stages;
